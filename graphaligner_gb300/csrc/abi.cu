@@ -1,0 +1,436 @@
+// C ABI of the GB300 seed-extension path (declared in include/graphaligner_gb300.h).
+//
+// Handles own their device memory.  ga_extend_batch copies a host batch in,
+// runs the fill and traceback kernels (with an on-GPU retry at larger
+// per-thread capacities for the few extensions whose band, frontier or trace
+// outgrew the first pass), and copies the results out.  No CPU fallback exists:
+// every extension is computed by the kernels or reported with its status.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+#include "extend.cuh"
+#include "../../include/graphaligner_gb300.h"
+
+namespace
+{
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    return fail(GA_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define GA_CUDA(call) do { cudaError_t _e = (call); if (_e != cudaSuccess) return cuda_fail(_e, #call); } while (0)
+
+template <typename T>
+struct DevBuf
+{
+    T* ptr = nullptr;
+    size_t count = 0;
+    cudaError_t reserve(size_t n)
+    {
+        if (n <= count) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+        size_t grow = std::max(n, count * 3 / 2);
+        cudaError_t e = cudaMalloc((void**)&ptr, std::max<size_t>(grow, 1) * sizeof(T));
+        if (e == cudaSuccess) count = grow;
+        return e;
+    }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+};
+
+__global__ void count_status_kernel(const int32_t* status, uint32_t n, int32_t value, uint32_t* out)
+{
+    uint32_t local = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (status[i] == value) local++;
+    if (local) atomicAdd(out, local);
+}
+}
+
+struct ga_graph
+{
+    int device = 0;
+    uint32_t N = 0;
+    gadev::DevGraph d {};
+    std::vector<void*> allocations;
+};
+
+struct ga_extender
+{
+    ga_graph* graph = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[3] {};
+    int sms = 0;
+    int block = 128;
+    gadev::Caps caps {};
+    uint8_t* workspace = nullptr;
+    uint64_t workspaceBytes = 0;
+    uint8_t* arena = nullptr;
+    uint64_t arenaBytes = 0;
+    uint32_t* counters = nullptr;          // [0] fill work, [1] trace work, [2] status count
+    unsigned long long* arenaCursor = nullptr;
+    float lastFillMs = 0;
+    float lastTraceMs = 0;
+    uint32_t lastLaunches = 0;
+    // host-batch staging
+    DevBuf<uint8_t> seq;
+    DevBuf<uint64_t> seqOff, traceOff, traceItems, cellSteps;
+    DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order;
+    DevBuf<int32_t> status, score, prevStatus;
+    DevBuf<gadev::ExtState> state;
+};
+
+extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
+extern "C" const char* ga_version(void) { return "graphaligner_gb300 0.1 (sm_103a)"; }
+
+extern "C" int ga_graph_upload(const ga_graph_desc* desc, int device, ga_graph_t* out)
+{
+    if (!desc || !out) return fail(GA_ERR_ARGUMENT, "null argument");
+    if (desc->num_nodes == 0 || desc->first_ambiguous > desc->num_nodes) return fail(GA_ERR_ARGUMENT, "bad node counts");
+    const uint32_t N = desc->num_nodes;
+    for (uint32_t i = 0; i < N; i++)
+        if (desc->node_length[i] == 0 || desc->node_length[i] > 64) return fail(GA_ERR_ARGUMENT, "node length outside 1..64");
+    GA_CUDA(cudaSetDevice(device));
+    ga_graph* g = new ga_graph();
+    g->device = device;
+    g->N = N;
+    auto up = [&](const void* src, size_t bytes, void** dst) -> cudaError_t
+    {
+        *dst = nullptr;
+        cudaError_t e = cudaMalloc(dst, std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) return e;
+        g->allocations.push_back(*dst);
+        if (bytes) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+        return e;
+    };
+    const uint32_t nIn = desc->in_offsets[N];
+    const uint32_t nOut = desc->out_offsets[N];
+    void *len, *seq2, *seqAmb, *inOff, *inNb, *outOff, *outNb, *lin, *comp;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = up(desc->node_length, (size_t)N * 4, &len);
+    if (e == cudaSuccess) e = up(desc->seq2bit, (size_t)desc->first_ambiguous * 16, &seq2);
+    if (e == cudaSuccess) e = up(desc->seq_ambiguous, (size_t)(N - desc->first_ambiguous) * 32, &seqAmb);
+    if (e == cudaSuccess) e = up(desc->in_offsets, (size_t)(N + 1) * 4, &inOff);
+    if (e == cudaSuccess) e = up(desc->in_neighbors, (size_t)nIn * 4, &inNb);
+    if (e == cudaSuccess) e = up(desc->out_offsets, (size_t)(N + 1) * 4, &outOff);
+    if (e == cudaSuccess) e = up(desc->out_neighbors, (size_t)nOut * 4, &outNb);
+    if (e == cudaSuccess) e = up(desc->linearizable, (size_t)N, &lin);
+    if (e == cudaSuccess) e = up(desc->component, (size_t)N * 4, &comp);
+    if (e != cudaSuccess)
+    {
+        for (void* p : g->allocations) cudaFree(p);
+        delete g;
+        return cuda_fail(e, "graph upload");
+    }
+    g->d.N = N;
+    g->d.firstAmbiguous = desc->first_ambiguous;
+    g->d.len = (const uint32_t*)len;
+    g->d.seq2 = (const uint64_t*)seq2;
+    g->d.seqAmb = (const uint64_t*)seqAmb;
+    g->d.inOff = (const uint32_t*)inOff;
+    g->d.inNb = (const uint32_t*)inNb;
+    g->d.outOff = (const uint32_t*)outOff;
+    g->d.outNb = (const uint32_t*)outNb;
+    g->d.lin = (const uint8_t*)lin;
+    g->d.comp = (const uint32_t*)comp;
+    *out = g;
+    return GA_OK;
+}
+
+extern "C" int ga_graph_free(ga_graph_t g)
+{
+    if (!g) return GA_OK;
+    cudaSetDevice(g->device);
+    for (void* p : g->allocations) cudaFree(p);
+    delete g;
+    return GA_OK;
+}
+
+static gadev::Caps base_caps()
+{
+    gadev::Caps c;
+    c.band = 64;
+    c.hash = 512;
+    c.heap = 128;
+    c.extras = 256;
+    return c;
+}
+
+static gadev::Caps scaled_caps(int round)
+{
+    gadev::Caps c = base_caps();
+    uint32_t f = round == 0 ? 1 : (round == 1 ? 8 : 64);
+    c.band = std::min<uint32_t>(c.band * f, 16384);
+    c.hash = std::min<uint32_t>(c.hash * f, 65536);
+    c.heap = std::min<uint32_t>(c.heap * f, 16384);
+    c.extras = std::min<uint32_t>(c.extras * f, 32768);
+    return c;
+}
+
+extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out)
+{
+    if (!graph || !out) return fail(GA_ERR_ARGUMENT, "null argument");
+    GA_CUDA(cudaSetDevice(graph->device));
+    ga_extender* x = new ga_extender();
+    x->graph = graph;
+    cudaDeviceProp prop;
+    GA_CUDA(cudaGetDeviceProperties(&prop, graph->device));
+    x->sms = prop.multiProcessorCount;
+    x->caps = base_caps();
+    int occ = std::max(1, ga_fill_occupancy(x->block));
+    uint64_t slots = (uint64_t)x->sms * occ * x->block;
+    uint64_t stride = ga_workspace_bytes(x->caps);
+    x->workspaceBytes = slots * stride;
+    GA_CUDA(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking));
+    for (auto& e : x->ev) GA_CUDA(cudaEventCreate(&e));
+    cudaError_t e = cudaMalloc((void**)&x->workspace, x->workspaceBytes);
+    if (e != cudaSuccess) { delete x; return cuda_fail(e, "workspace"); }
+    GA_CUDA(cudaMemset(x->workspace, 0, x->workspaceBytes));
+    if (arena_bytes == 0) arena_bytes = 4ULL << 30;
+    x->arenaBytes = arena_bytes;
+    e = cudaMalloc((void**)&x->arena, x->arenaBytes);
+    if (e != cudaSuccess) { cudaFree(x->workspace); delete x; return cuda_fail(e, "arena"); }
+    GA_CUDA(cudaMalloc((void**)&x->counters, 16 * sizeof(uint32_t)));
+    GA_CUDA(cudaMalloc((void**)&x->arenaCursor, sizeof(unsigned long long)));
+    *out = x;
+    return GA_OK;
+}
+
+extern "C" int ga_extender_free(ga_extender_t x)
+{
+    if (!x) return GA_OK;
+    cudaSetDevice(x->graph->device);
+    cudaStreamSynchronize(x->stream);
+    cudaFree(x->workspace);
+    cudaFree(x->arena);
+    cudaFree(x->counters);
+    cudaFree(x->arenaCursor);
+    x->seq.release(); x->seqOff.release(); x->traceOff.release(); x->traceItems.release(); x->cellSteps.release();
+    x->seqLen.release(); x->startNode.release(); x->startOffset.release(); x->traceCap.release(); x->traceLen.release();
+    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release(); x->state.release();
+    for (auto& e : x->ev) cudaEventDestroy(e);
+    cudaStreamDestroy(x->stream);
+    delete x;
+    return GA_OK;
+}
+
+// Runs one batch whose buffers are all on the device.  order: processing order.
+static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend_batch_desc* b, ga_extend_results* r,
+    const uint32_t* order, gadev::ExtState* state, int32_t* prevStatus, cudaStream_t stream, bool sync)
+{
+    gadev::FillArgs fa {};
+    fa.g = x->graph->d;
+    fa.bandwidth = p->bandwidth;
+    fa.xdrop = p->xdrop;
+    fa.maxCells = p->max_cells_per_slice;
+    fa.cost = p->xscore_error_cost;
+    fa.num = b->num;
+    fa.order = order;
+    fa.seq = b->seq;
+    fa.seqOff = b->seq_offset;
+    fa.seqLen = b->seq_len;
+    fa.startNode = b->start_node;
+    fa.startOffset = b->start_offset;
+    fa.state = state;
+    fa.arena = x->arena;
+    fa.arenaBytes = x->arenaBytes;
+    fa.arenaCursor = x->arenaCursor;
+    fa.workCounter = x->counters;
+    fa.workspace = x->workspace;
+
+    gadev::TraceArgs ta {};
+    ta.g = x->graph->d;
+    ta.cost = p->xscore_error_cost;
+    ta.num = b->num;
+    ta.order = order;
+    ta.seq = b->seq;
+    ta.seqOff = b->seq_offset;
+    ta.seqLen = b->seq_len;
+    ta.state = state;
+    ta.arena = x->arena;
+    ta.traceOffset = b->trace_offset;
+    ta.traceCap = b->trace_capacity;
+    ta.status = r->status;
+    ta.score = r->score;
+    ta.traceLen = r->trace_len;
+    ta.traceItems = r->trace_items;
+    ta.cellSteps = r->cell_steps;
+    ta.workCounter = x->counters + 1;
+
+    x->lastFillMs = 0;
+    x->lastTraceMs = 0;
+    x->lastLaunches = 0;
+    const int traceOcc = std::max(1, ga_trace_occupancy(x->block));
+    for (int round = 0; round < 3; round++)
+    {
+        gadev::Caps caps = scaled_caps(round);
+        uint64_t stride = ga_workspace_bytes(caps);
+        uint64_t slots = x->workspaceBytes / stride;
+        int fillGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>(slots / x->block, (b->num + x->block - 1) / x->block));
+        int traceGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)x->sms * traceOcc, (b->num + x->block - 1) / x->block));
+        if (round > 0)
+        {
+            // only extensions that ran out of a capacity in the previous round run again
+            GA_CUDA(cudaMemcpyAsync(prevStatus, r->status, (size_t)b->num * 4, cudaMemcpyDeviceToDevice, stream));
+            // workspace tables laid out for other capacities: clear their generation stamps
+            GA_CUDA(cudaMemsetAsync(x->workspace, 0, x->workspaceBytes, stream));
+        }
+        fa.caps = caps;
+        fa.workspaceStride = stride;
+        fa.prevStatus = round > 0 ? prevStatus : nullptr;
+        ta.prevStatus = round > 0 ? prevStatus : nullptr;
+        GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), stream));
+        GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, sizeof(unsigned long long), stream));
+        GA_CUDA(cudaEventRecord(x->ev[0], stream));
+        ga_launch_fill(fa, fillGrid, x->block, stream);
+        GA_CUDA(cudaGetLastError());
+        GA_CUDA(cudaEventRecord(x->ev[1], stream));
+        ga_launch_trace(ta, traceGrid, x->block, stream);
+        GA_CUDA(cudaGetLastError());
+        GA_CUDA(cudaEventRecord(x->ev[2], stream));
+        count_status_kernel<<<64, 256, 0, stream>>>(r->status, b->num, GA_CAPACITY, x->counters + 2);
+        GA_CUDA(cudaGetLastError());
+        x->lastLaunches += 3;
+        uint32_t capFails = 0;
+        GA_CUDA(cudaMemcpyAsync(&capFails, x->counters + 2, 4, cudaMemcpyDeviceToHost, stream));
+        GA_CUDA(cudaStreamSynchronize(stream));
+        float f = 0, t = 0;
+        GA_CUDA(cudaEventElapsedTime(&f, x->ev[0], x->ev[1]));
+        GA_CUDA(cudaEventElapsedTime(&t, x->ev[1], x->ev[2]));
+        x->lastFillMs += f;
+        x->lastTraceMs += t;
+        if (capFails == 0) break;
+    }
+    (void)sync;
+    return GA_OK;
+}
+
+static std::vector<uint32_t> longest_first(const uint32_t* len, uint32_t n)
+{
+    std::vector<uint32_t> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [len](uint32_t a, uint32_t b) { return len[a] > len[b]; });
+    return order;
+}
+
+extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const ga_extend_batch_desc* b, ga_extend_results* r)
+{
+    if (!x || !p || !b || !r) return fail(GA_ERR_ARGUMENT, "null argument");
+    GA_CUDA(cudaSetDevice(x->graph->device));
+    const uint32_t n = b->num;
+    if (n == 0) return GA_OK;
+    uint64_t seqBytes = 0, items = 0;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        seqBytes = std::max<uint64_t>(seqBytes, b->seq_offset[i] + b->seq_len[i]);
+        items = std::max<uint64_t>(items, b->trace_offset[i] + b->trace_capacity[i]);
+    }
+    std::vector<uint32_t> order = longest_first(b->seq_len, n);
+    GA_CUDA(x->seq.reserve(seqBytes));
+    GA_CUDA(x->seqOff.reserve(n));
+    GA_CUDA(x->seqLen.reserve(n));
+    GA_CUDA(x->startNode.reserve(n));
+    GA_CUDA(x->startOffset.reserve(n));
+    GA_CUDA(x->traceOff.reserve(n));
+    GA_CUDA(x->traceCap.reserve(n));
+    GA_CUDA(x->order.reserve(n));
+    GA_CUDA(x->status.reserve(n));
+    GA_CUDA(x->prevStatus.reserve(n));
+    GA_CUDA(x->score.reserve(n));
+    GA_CUDA(x->traceLen.reserve(n));
+    GA_CUDA(x->cellSteps.reserve(n));
+    GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(items, 1)));
+    GA_CUDA(x->state.reserve(n));
+    cudaStream_t s = x->stream;
+    GA_CUDA(cudaMemcpyAsync(x->seq.ptr, b->seq, seqBytes, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->seqOff.ptr, b->seq_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->seqLen.ptr, b->seq_len, n * 4ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->startNode.ptr, b->start_node, n * 4ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->startOffset.ptr, b->start_offset, n * 4ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->traceOff.ptr, b->trace_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->traceCap.ptr, b->trace_capacity, n * 4ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
+    ga_extend_batch_desc db = *b;
+    db.seq = x->seq.ptr;
+    db.seq_offset = x->seqOff.ptr;
+    db.seq_len = x->seqLen.ptr;
+    db.start_node = x->startNode.ptr;
+    db.start_offset = x->startOffset.ptr;
+    db.trace_offset = x->traceOff.ptr;
+    db.trace_capacity = x->traceCap.ptr;
+    ga_extend_results dr;
+    dr.status = x->status.ptr;
+    dr.score = x->score.ptr;
+    dr.trace_len = x->traceLen.ptr;
+    dr.trace_items = x->traceItems.ptr;
+    dr.cell_steps = x->cellSteps.ptr;
+    int rc = run_device(x, p, &db, &dr, x->order.ptr, x->state.ptr, x->prevStatus.ptr, s, true);
+    if (rc != GA_OK) return rc;
+    GA_CUDA(cudaMemcpyAsync(r->status, dr.status, n * 4ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaMemcpyAsync(r->score, dr.score, n * 4ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaMemcpyAsync(r->trace_len, dr.trace_len, n * 4ULL, cudaMemcpyDeviceToHost, s));
+    if (r->cell_steps) GA_CUDA(cudaMemcpyAsync(r->cell_steps, dr.cell_steps, n * 8ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaMemcpyAsync(r->trace_items, dr.trace_items, items * 8ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaStreamSynchronize(s));
+    return GA_OK;
+}
+
+extern "C" int ga_extend_batch_device(ga_extender_t x, const ga_extend_params* p, const ga_extend_batch_desc* b,
+    ga_extend_results* r, void* stream)
+{
+    if (!x || !p || !b || !r) return fail(GA_ERR_ARGUMENT, "null argument");
+    GA_CUDA(cudaSetDevice(x->graph->device));
+    const uint32_t n = b->num;
+    if (n == 0) return GA_OK;
+    // the processing order needs the lengths; read them back once (4 bytes per extension)
+    std::vector<uint32_t> len(n);
+    cudaStream_t s = stream ? (cudaStream_t)stream : x->stream;
+    GA_CUDA(cudaMemcpyAsync(len.data(), b->seq_len, n * 4ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint32_t> order = longest_first(len.data(), n);
+    GA_CUDA(x->order.reserve(n));
+    GA_CUDA(x->state.reserve(n));
+    GA_CUDA(x->prevStatus.reserve(n));
+    GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
+    return run_device(x, p, b, r, x->order.ptr, x->state.ptr, x->prevStatus.ptr, s, false);
+}
+
+extern "C" int ga_extender_last_kernel_ms(ga_extender_t x, float* ms)
+{
+    if (!x || !ms) return fail(GA_ERR_ARGUMENT, "null argument");
+    *ms = x->lastFillMs + x->lastTraceMs;
+    return GA_OK;
+}
+
+extern "C" int ga_extender_last_times(ga_extender_t x, float* fill_ms, float* trace_ms)
+{
+    if (!x || !fill_ms || !trace_ms) return fail(GA_ERR_ARGUMENT, "null argument");
+    *fill_ms = x->lastFillMs;
+    *trace_ms = x->lastTraceMs;
+    return GA_OK;
+}
+
+extern "C" int ga_extender_last_launches(ga_extender_t x, uint32_t* launches)
+{
+    if (!x || !launches) return fail(GA_ERR_ARGUMENT, "null argument");
+    *launches = x->lastLaunches;
+    return GA_OK;
+}

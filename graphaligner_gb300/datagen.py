@@ -1,0 +1,337 @@
+"""Seeded synthetic workloads for the seed-extension path.
+
+No public dataset is named for this path, so graphs, reads and seeds are
+generated here with the shapes the workloads call for:
+
+* variation graph: a uniform-random ACGT backbone with one variant site every
+  ``spacing`` bp on average; a site is a SNP (two 1-bp alleles) with
+  probability ``snp_frac`` and otherwise an insertion or deletion of
+  1..``indel_max`` bp (a bubble with an empty branch).  Nodes are split at
+  variant sites and written as GFA with ``0M`` links.
+* reads: a random allele per site gives a haplotype path; a read is a window of
+  that path on a random strand with per-base errors (60% substitution, 20%
+  insertion, 20% deletion of the error budget).
+* seeds: exact k-mers of the read that map to consecutive, unedited path bases;
+  the seed position is the k-mer's last base, as MinimizerSeeder reports it
+  (MinimizerSeeder.cpp:82,545-555).
+
+Everything is a pure function of the seed, so the same inputs are rebuilt on
+any machine.
+"""
+from __future__ import annotations
+
+import dataclasses
+import numpy as np
+
+_BASES = np.frombuffer(b"ACGT", dtype=np.uint8)
+_COMP = np.zeros(256, dtype=np.uint8)
+for _a, _b in zip(b"ACGTacgtN", b"TGCAtgcaN"):
+    _COMP[_a] = _b
+
+
+def revcomp(seq: bytes | np.ndarray) -> np.ndarray:
+    arr = np.frombuffer(seq, dtype=np.uint8) if isinstance(seq, (bytes, bytearray)) else seq
+    return _COMP[arr[::-1]]
+
+
+@dataclasses.dataclass
+class VariationGraph:
+    """A bidirected GFA graph in forward orientation (ids start at 1)."""
+    node_seqs: list            # list of np.uint8 arrays, index = id - 1
+    edges: list                # list of (from_id, to_id), both '+' strand
+    sites: list                # per site: (kind, [allele node id lists])
+    backbone_nodes: list       # ordered backbone segment ids between sites
+
+    def to_gfa(self) -> str:
+        lines = []
+        for i, s in enumerate(self.node_seqs):
+            lines.append(f"S\t{i + 1}\t{s.tobytes().decode()}")
+        for a, b in self.edges:
+            lines.append(f"L\t{a}\t+\t{b}\t+\t0M")
+        return "\n".join(lines) + "\n"
+
+    @property
+    def total_bp(self) -> int:
+        return int(sum(len(s) for s in self.node_seqs))
+
+
+def make_variation_graph(genome_len: int, spacing: int, snp_frac: float = 0.7,
+                         indel_max: int = 20, seed: int = 0) -> VariationGraph:
+    """Backbone of ``genome_len`` bp with a variant roughly every ``spacing`` bp."""
+    rng = np.random.default_rng(seed)
+    backbone = _BASES[rng.integers(0, 4, genome_len)]
+    node_seqs: list = []
+    edges: list = []
+    sites: list = []
+    backbone_nodes: list = []
+
+    def new_node(seq):
+        node_seqs.append(np.ascontiguousarray(seq, dtype=np.uint8))
+        return len(node_seqs)
+
+    # previous "ends": node ids whose right end connects to the next segment
+    prev_ends: list = []
+    seg_start = 0
+    pos = int(rng.integers(spacing // 2, spacing + 1))
+    while True:
+        if pos >= genome_len - indel_max - 2:
+            break
+        r = rng.random()
+        if r < snp_frac:
+            kind, length = "snp", 1
+        elif r < snp_frac + (1 - snp_frac) / 2:
+            kind, length = "ins", int(rng.integers(1, indel_max + 1))
+        else:
+            kind, length = "del", int(rng.integers(1, indel_max + 1))
+        if pos <= seg_start:
+            pos = seg_start + 1
+        seg = new_node(backbone[seg_start:pos])
+        backbone_nodes.append(seg)
+        for p in prev_ends:
+            edges.append((p, seg))
+        if kind == "snp":
+            ref = backbone[pos:pos + 1]
+            alt = _BASES[(int(np.searchsorted(_BASES, ref[0])) + int(rng.integers(1, 4))) % 4:][:1]
+            a = new_node(ref)
+            b = new_node(alt)
+            edges.append((seg, a))
+            edges.append((seg, b))
+            sites.append(("snp", [[a], [b]]))
+            prev_ends = [a, b]
+            seg_start = pos + 1
+        elif kind == "del":
+            d = new_node(backbone[pos:pos + length])
+            edges.append((seg, d))
+            sites.append(("del", [[d], []]))
+            prev_ends = [d, seg]
+            seg_start = pos + length
+        else:
+            ins = new_node(_BASES[rng.integers(0, 4, length)])
+            edges.append((seg, ins))
+            sites.append(("ins", [[], [ins]]))
+            prev_ends = [ins, seg]
+            seg_start = pos
+        step = int(rng.integers(max(1, spacing // 2), spacing + spacing // 2 + 1))
+        pos = seg_start + max(step, 2)
+    last = new_node(backbone[seg_start:])
+    backbone_nodes.append(last)
+    for p in prev_ends:
+        edges.append((p, last))
+    return VariationGraph(node_seqs, edges, sites, backbone_nodes)
+
+
+@dataclasses.dataclass
+class Haplotype:
+    seq: np.ndarray        # path sequence (uint8 ASCII)
+    node: np.ndarray       # GFA node id of each path base
+    offset: np.ndarray     # offset of each path base inside its node
+
+
+def sample_haplotype(g: VariationGraph, seed: int) -> Haplotype:
+    """One allele per site, chosen uniformly."""
+    rng = np.random.default_rng(seed)
+    choice = rng.integers(0, 2, len(g.sites))
+    order = []
+    for i, seg in enumerate(g.backbone_nodes):
+        order.append(seg)
+        if i < len(g.sites):
+            order.extend(g.sites[i][1][choice[i]])
+    seqs = [g.node_seqs[n - 1] for n in order]
+    lens = np.array([len(s) for s in seqs], dtype=np.int64)
+    seq = np.concatenate(seqs)
+    node = np.repeat(np.array(order, dtype=np.int64), lens)
+    starts = np.repeat(np.cumsum(lens) - lens, lens)
+    offset = np.arange(len(seq), dtype=np.int64) - starts
+    return Haplotype(seq, node, offset)
+
+
+@dataclasses.dataclass
+class Read:
+    name: str
+    seq: bytes
+    # per read base: bigraph node id (GFA id*2 + strand) and offset on that strand,
+    # or -1 for inserted / substituted bases
+    bignode: np.ndarray
+    bigoffset: np.ndarray
+    exact: np.ndarray      # True where the base is an unedited copy of the path
+
+
+def _apply_errors(rng, truth: np.ndarray, rate: float):
+    """Returns (read bases, source index into truth or -1, exact flag)."""
+    n = len(truth)
+    u = rng.random(n)
+    kind = np.full(n, 0, dtype=np.int8)            # 0 keep, 1 sub, 2 ins, 3 del
+    err = u < rate
+    t = rng.random(n)
+    kind[err & (t < 0.6)] = 1
+    kind[err & (t >= 0.6) & (t < 0.8)] = 2
+    kind[err & (t >= 0.8)] = 3
+    out_bases = []
+    out_src = []
+    out_exact = []
+    subs = (np.searchsorted(_BASES, truth) + rng.integers(1, 4, n)) % 4
+    ins_bases = _BASES[rng.integers(0, 4, n)]
+    keep = kind != 3
+    # build per source position a list of emitted bases: optional inserted base then the base
+    emit_ins = kind == 2
+    total = int(keep.sum() + emit_ins.sum())
+    bases = np.empty(total, dtype=np.uint8)
+    src = np.empty(total, dtype=np.int64)
+    exact = np.empty(total, dtype=bool)
+    counts = keep.astype(np.int64) + emit_ins.astype(np.int64)
+    pos = np.cumsum(counts) - counts
+    ins_pos = pos[emit_ins]
+    bases[ins_pos] = ins_bases[emit_ins]
+    src[ins_pos] = -1
+    exact[ins_pos] = False
+    base_pos = pos[keep] + emit_ins[keep].astype(np.int64)
+    kb = truth[keep].copy()
+    is_sub = (kind[keep] == 1)
+    kb[is_sub] = _BASES[subs[keep][is_sub]]
+    bases[base_pos] = kb
+    src[base_pos] = np.nonzero(keep)[0]
+    exact[base_pos] = ~is_sub
+    return bases, src, exact
+
+
+def sample_reads(g: VariationGraph, n_reads: int, seed: int, length_fn, error_fn,
+                 prefix: str = "read") -> list:
+    """Reads along one haplotype per read, on a random strand."""
+    rng = np.random.default_rng(seed)
+    node_len = np.array([len(s) for s in g.node_seqs], dtype=np.int64)
+    reads = []
+    hap_cache = {}
+    for r in range(n_reads):
+        hap_seed = int(rng.integers(0, 4))
+        if hap_seed not in hap_cache:
+            hap_cache[hap_seed] = sample_haplotype(g, seed * 1000003 + hap_seed)
+        hap = hap_cache[hap_seed]
+        length = int(min(length_fn(rng), len(hap.seq) - 1))
+        start = int(rng.integers(0, len(hap.seq) - length + 1))
+        truth = hap.seq[start:start + length]
+        node = hap.node[start:start + length]
+        off = hap.offset[start:start + length]
+        reverse = bool(rng.integers(0, 2))
+        if reverse:
+            truth = revcomp(truth)
+            node = node[::-1]
+            off = node_len[node - 1] - 1 - off[::-1]
+            bignode = node * 2 + 1
+        else:
+            bignode = node * 2
+        bases, src, exact = _apply_errors(rng, truth, float(error_fn(rng)))
+        bn = np.where(src >= 0, bignode[np.maximum(src, 0)], -1)
+        bo = np.where(src >= 0, off[np.maximum(src, 0)], -1)
+        bn[~exact] = -1
+        bo[~exact] = -1
+        reads.append(Read(f"{prefix}{r}", bases.tobytes(), bn, bo, exact))
+    return reads
+
+
+def exact_seed_positions(read: Read, k: int) -> np.ndarray:
+    """Read positions q such that read[q-k+1..q] copies k consecutive path bases."""
+    ex = read.exact.astype(np.int64)
+    n = len(ex)
+    if n < k:
+        return np.zeros(0, dtype=np.int64)
+    run = np.convolve(ex, np.ones(k, dtype=np.int64), mode="valid") == k
+    q = np.nonzero(run)[0] + k - 1
+    # consecutive path positions on the same strand: bigoffset/bignode continuity
+    ok = np.ones(len(q), dtype=bool)
+    for d in range(1, k):
+        a = q - d
+        same = read.bignode[a] == read.bignode[a + 1]
+        ok &= ~same | (read.bigoffset[a] + 1 == read.bigoffset[a + 1])
+    return q[ok]
+
+
+def lognormal_length(mean: float, sigma: float, lo: int, hi: int):
+    mu = np.log(mean) - sigma * sigma / 2
+
+    def fn(rng):
+        return int(np.clip(rng.lognormal(mu, sigma), lo, hi))
+    return fn
+
+
+def uniform_length(lo: int, hi: int):
+    def fn(rng):
+        return int(rng.integers(lo, hi + 1))
+    return fn
+
+
+def uniform_error(lo: float, hi: float):
+    def fn(rng):
+        return float(rng.uniform(lo, hi))
+    return fn
+
+
+@dataclasses.dataclass
+class ExtensionSet:
+    """Seed extensions in the form GraphAlignerBitvectorBanded::getReverseTraceFromSeed
+    takes them (GraphAlignerBitvectorBanded.h:59): a sequence, a bigraph node id and
+    an offset on that node."""
+    seqs: list             # list of bytes
+    bignode: np.ndarray    # int64
+    offset: np.ndarray     # int64
+
+    def __len__(self):
+        return len(self.seqs)
+
+    def to_tsv(self) -> str:
+        return "".join(f"{int(n)}\t{int(o)}\t{s.decode()}\n" for n, o, s in zip(self.bignode, self.offset, self.seqs))
+
+
+def seed_extensions(reads: list, node_len_by_id: np.ndarray, k: int, seed: int,
+                    per_read: int = 1) -> ExtensionSet:
+    """Two extensions per chosen seed, exactly as GraphAligner::getTwoDirectionalTrace
+    forms them (GraphAligner.h:475-506): the forward part read[q+1:] from the seed's
+    node and offset, and the reverse complement of read[:q] from the reverse-strand
+    position of the seed base."""
+    rng = np.random.default_rng(seed)
+    seqs, nodes, offs = [], [], []
+    for read in reads:
+        q_all = exact_seed_positions(read, k)
+        if len(q_all) == 0:
+            continue
+        for q in rng.choice(q_all, size=min(per_read, len(q_all)), replace=False):
+            q = int(q)
+            fw_node = int(read.bignode[q])
+            fw_off = int(read.bigoffset[q])
+            size = int(node_len_by_id[fw_node // 2])
+            if q > 0:
+                bw_node = fw_node ^ 1
+                bw_off = size - fw_off - 1
+                seqs.append(revcomp(read.seq[:q]).tobytes())
+                nodes.append(bw_node)
+                offs.append(bw_off)
+            if q < len(read.seq) - 1:
+                seqs.append(read.seq[q + 1:])
+                nodes.append(fw_node)
+                offs.append(fw_off)
+    return ExtensionSet(seqs, np.array(nodes, dtype=np.int64), np.array(offs, dtype=np.int64))
+
+
+def write_fasta(reads: list) -> str:
+    return "".join(f">{r.name}\n{r.seq.decode()}\n" for r in reads)
+
+
+# Named workloads ------------------------------------------------------------
+
+def small_vg(seed: int = 0):
+    """50 kbp backbone, a bubble every ~200 bp, 70% SNP / 30% indels of 1-20 bp."""
+    return make_variation_graph(50_000, 200, 0.7, 20, seed)
+
+
+def small_vg_reads(g: VariationGraph, n: int = 200, seed: int = 1):
+    """Reads of 5-15 kbp at 10% error."""
+    return sample_reads(g, n, seed, uniform_length(5_000, 15_000), lambda rng: 0.10)
+
+
+def batch_vg(seed: int = 0):
+    """5 Mbp backbone, a variant every ~100 bp."""
+    return make_variation_graph(5_000_000, 100, 0.7, 20, seed)
+
+
+def batch_vg_reads(g: VariationGraph, n: int, seed: int = 1):
+    """Log-normal lengths with mean 10 kbp clipped to 1-50 kbp, error U[5%, 15%]."""
+    return sample_reads(g, n, seed, lognormal_length(10_000, 0.6, 1_000, 50_000), uniform_error(0.05, 0.15))

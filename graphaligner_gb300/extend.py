@@ -1,0 +1,194 @@
+"""Host mirror of GraphAligner's seed-extension interface over the C ABI.
+
+``Extender.extend`` is the batched form of
+``GraphAlignerBitvectorBanded::getReverseTraceFromSeed(sequence, bigraphNodeId,
+nodeOffset, Xdrop, state)`` (GraphAlignerBitvectorBanded.h:59-76): the same
+arguments per extension, the same result (``OnewayTrace``: trace items in DP
+order plus the score; a failed extension has score INT32_MAX,
+GraphAlignerCommon.h:154-163), computed by the CUDA kernels in one batch.
+A request that would make the reference throw ThreadReadAssertion::AssertionFailure
+comes back with status GA_ASSERT, which the read-level code turns into the same
+per-read drop the reference applies (Aligner.cpp:493-500).
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import numpy as np
+
+from . import _abi
+from ._abi import ptr
+from ._lib import lib, check
+
+INT32_MAX = 2**31 - 1
+
+
+def xscore_error_cost(precise_clipping: float = 0.66) -> int:
+    """GraphAlignerCommon::Params::XscoreErrorCost (GraphAlignerCommon.h:94)."""
+    return int(100 * (precise_clipping / (1.0 - precise_clipping) + 1.0))
+
+
+def default_xdrop(precise_clipping: float = 0.66) -> int:
+    """AlignerMain.cpp:220-231: X-drop so that a block of 50 mismatches ends an alignment."""
+    x = 50.0
+    if precise_clipping >= 0.501:
+        x = max(x, 50 * (100 * (precise_clipping / (1.0 - precise_clipping) + 1.0)))
+    return int(x)
+
+
+@dataclasses.dataclass
+class ExtendParams:
+    bandwidth: int = 10
+    xdrop: int = default_xdrop()
+    max_cells_per_slice: int = 2**64 - 1
+    xscore_error_cost: int = xscore_error_cost()
+
+    def c(self):
+        return _abi.ExtendParams(self.bandwidth, self.xdrop, self.max_cells_per_slice, self.xscore_error_cost)
+
+
+@dataclasses.dataclass
+class PackedBatch:
+    """A batch in the C-ABI layout (host arrays)."""
+    seq: np.ndarray
+    seq_offset: np.ndarray
+    seq_len: np.ndarray
+    start_node: np.ndarray
+    start_offset: np.ndarray
+    trace_offset: np.ndarray
+    trace_capacity: np.ndarray
+
+    @property
+    def num(self) -> int:
+        return len(self.seq_len)
+
+    @property
+    def total_items(self) -> int:
+        return int(self.trace_offset[-1] + self.trace_capacity[-1]) if self.num else 0
+
+    def desc(self):
+        return _abi.BatchDesc(self.num, ptr(self.seq, ctypes.c_uint8), ptr(self.seq_offset, ctypes.c_uint64),
+                              ptr(self.seq_len, ctypes.c_uint32), ptr(self.start_node, ctypes.c_uint32),
+                              ptr(self.start_offset, ctypes.c_uint32), ptr(self.trace_offset, ctypes.c_uint64),
+                              ptr(self.trace_capacity, ctypes.c_uint32))
+
+
+def trace_capacity_for(seq_len: np.ndarray) -> np.ndarray:
+    """Room for a trace: every read row plus horizontal steps inside the band."""
+    return (np.asarray(seq_len, dtype=np.uint64) * 3 + 1024).astype(np.uint32)
+
+
+def pack_batch(graph, seqs, bignodes, offsets) -> PackedBatch:
+    """Resolves (bigraphNodeId, nodeOffset) to split node + offset (AlignmentGraph::GetUnitigNode)
+    and lays the sequences out contiguously."""
+    n = len(seqs)
+    lens = np.fromiter((len(s) for s in seqs), dtype=np.uint32, count=n)
+    offs = np.zeros(n, dtype=np.uint64)
+    if n > 1:
+        offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+    blob = np.frombuffer(b"".join(bytes(s) for s in seqs), dtype=np.uint8).copy() if n else np.zeros(1, np.uint8)
+    sn = np.zeros(n, dtype=np.uint32)
+    so = np.zeros(n, dtype=np.uint32)
+    for i in range(n):
+        sn[i], so[i] = graph.unitig_node(int(bignodes[i]), int(offsets[i]))
+    cap = trace_capacity_for(lens)
+    toff = np.zeros(n, dtype=np.uint64)
+    if n > 1:
+        toff[1:] = np.cumsum(cap[:-1].astype(np.uint64))
+    return PackedBatch(blob, offs, lens, sn, so, toff, cap)
+
+
+@dataclasses.dataclass
+class BatchResult:
+    status: np.ndarray
+    score: np.ndarray
+    trace_len: np.ndarray
+    trace_items: np.ndarray
+    trace_offset: np.ndarray
+    cell_steps: np.ndarray
+
+    def items(self, i: int) -> np.ndarray:
+        o = int(self.trace_offset[i])
+        return self.trace_items[o:o + int(self.trace_len[i])]
+
+    def positions(self, i: int):
+        """(node, nodeOffset, seqPos, nodeSwitch) per trace item, seqPos -1 above the read."""
+        it = self.items(i)
+        return ((it & 0xffffffff).astype(np.int64), ((it >> 32) & 63).astype(np.int64),
+                (it >> 39).astype(np.int64) - 1, ((it >> 38) & 1).astype(np.int64))
+
+
+def alloc_results(b: PackedBatch) -> BatchResult:
+    n = b.num
+    return BatchResult(np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.uint32),
+                       np.zeros(max(b.total_items, 1), np.uint64), b.trace_offset, np.zeros(n, np.uint64))
+
+
+def results_desc(r: BatchResult):
+    return _abi.Results(ptr(r.status, ctypes.c_int32), ptr(r.score, ctypes.c_int32), ptr(r.trace_len, ctypes.c_uint32),
+                        ptr(r.trace_items, ctypes.c_uint64), ptr(r.cell_steps, ctypes.c_uint64))
+
+
+class DeviceGraph:
+    """AlignmentGraph arrays resident in HBM (ga_graph_upload)."""
+
+    def __init__(self, graph, device: int = 0):
+        self.graph = graph
+        self._desc = graph.desc()
+        h = ctypes.c_void_p()
+        check(lib().ga_graph_upload(ctypes.byref(self._desc), device, ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().ga_graph_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Extender:
+    """Batched getReverseTraceFromSeed on the GPU."""
+
+    def __init__(self, dgraph: DeviceGraph, arena_bytes: int = 0):
+        self.dgraph = dgraph
+        h = ctypes.c_void_p()
+        check(lib().ga_extender_create(dgraph.handle, ctypes.c_uint64(arena_bytes), ctypes.byref(h)))
+        self.handle = h
+
+    def run(self, params: ExtendParams, batch: PackedBatch, out: BatchResult | None = None) -> BatchResult:
+        r = out if out is not None else alloc_results(batch)
+        p = params.c()
+        d = batch.desc()
+        rd = results_desc(r)
+        check(lib().ga_extend_batch(self.handle, ctypes.byref(p), ctypes.byref(d), ctypes.byref(rd)))
+        return r
+
+    def extend(self, params: ExtendParams, seqs, bignodes, offsets) -> BatchResult:
+        return self.run(params, pack_batch(self.dgraph.graph, seqs, bignodes, offsets))
+
+    def last_times(self):
+        f = ctypes.c_float()
+        t = ctypes.c_float()
+        check(lib().ga_extender_last_times(self.handle, ctypes.byref(f), ctypes.byref(t)))
+        return f.value, t.value
+
+    def last_launches(self) -> int:
+        n = ctypes.c_uint32()
+        check(lib().ga_extender_last_launches(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def close(self):
+        if self.handle:
+            lib().ga_extender_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,387 @@
+"""Host-side alignment graph: the AlignmentGraph fields the DP reads, as arrays.
+
+Two sources:
+
+* ``load_gag`` reads the GAG1 binary layout (arrays of an AlignmentGraph built by
+  GraphAligner's own ``DirectedGraph::BuildFromGFA`` + ``AlignmentGraph::Finalize``,
+  dumped field by field), so the GPU path runs on the reference's exact node
+  numbering, component order and neighbour order.
+* ``build_from_gfa`` builds the same kind of graph from a GFA with 0-bp overlaps
+  (the variation-graph workloads).  It follows AlignmentGraph's construction
+  rules (AlignmentGraph.cpp:48-296): both strands (GFA id*2 forward, id*2+1
+  reverse complement), nodes split into pieces of at most 64 bp, ambiguous
+  nodes renumbered to the end, the linearizable flags of findLinearizable and
+  the Tarjan component order of doComponentOrder.  Its node numbering is its
+  own (GFA order); results are exact against the oracle on the same arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import numpy as np
+
+SPLIT_NODE_SIZE = 64
+
+_CODE = np.full(256, 255, dtype=np.uint8)
+for _i, _c in enumerate(b"ACGT"):
+    _CODE[_c] = _i
+    _CODE[ord(chr(_c).lower())] = _i
+_CODE[ord("U")] = 3
+_CODE[ord("u")] = 3
+_IUPAC = {
+    "A": 1, "C": 2, "G": 4, "T": 8, "U": 8, "R": 5, "Y": 10, "K": 12, "M": 3,
+    "S": 6, "W": 9, "B": 14, "D": 13, "H": 11, "V": 7, "N": 15,
+}
+_COMPLEMENT = bytes.maketrans(b"ACGTUacgtuRYKMSWBDHVNrykmswbdhvn", b"TGCAAtgcaaYRMKSWVHDBNyrmkswvhdbn")
+
+
+@dataclasses.dataclass
+class Graph:
+    num_nodes: int
+    first_ambiguous: int
+    node_length: np.ndarray      # uint32 [N]
+    node_ids: np.ndarray         # int32  [N] bigraph node id (GFA id*2 + strand)
+    node_offset: np.ndarray      # uint32 [N] offset of the piece inside its bigraph node
+    reverse: np.ndarray          # uint8  [N]
+    linearizable: np.ndarray     # uint8  [N]
+    component: np.ndarray        # uint32 [N]
+    chain_number: np.ndarray     # uint64 [N]
+    chain_approx_pos: np.ndarray # uint64 [N]
+    seq2bit: np.ndarray          # uint64 [first_ambiguous * 2]
+    seq_ambiguous: np.ndarray    # uint64 [(N - first_ambiguous) * 4] A,C,G,T
+    in_offsets: np.ndarray       # uint32 [N + 1]
+    in_neighbors: np.ndarray     # uint32
+    out_offsets: np.ndarray      # uint32 [N + 1]
+    out_neighbors: np.ndarray    # uint32
+    lookup_ids: np.ndarray       # int32  [M] bigraph node ids in nodeLookup order
+    original_size: np.ndarray    # uint32 [M]
+    lookup_offsets: np.ndarray   # uint32 [M + 1]
+    lookup_nodes: np.ndarray     # uint32 split nodes of each bigraph node, in offset order
+    names: list                  # [M] original names ("" = numeric GFA id)
+    bp_size: int = 0
+
+    def __post_init__(self):
+        self._lookup_index = {int(b): i for i, b in enumerate(self.lookup_ids)}
+
+    # AlignmentGraph::GetUnitigNode (AlignmentGraph.cpp:812-828)
+    def unitig_node(self, bignode: int, offset: int) -> tuple[int, int]:
+        i = self._lookup_index[int(bignode)]
+        nodes = self.lookup_nodes[self.lookup_offsets[i]:self.lookup_offsets[i + 1]]
+        starts = self.node_offset[nodes]
+        k = int(np.searchsorted(starts, offset, side="right")) - 1
+        node = int(nodes[k])
+        return node, int(offset - self.node_offset[node])
+
+    def original_size_of(self, bignode: int) -> int:
+        return int(self.original_size[self._lookup_index[int(bignode)]])
+
+    # AlignmentGraph::GetReversePosition (AlignmentGraph.cpp:830-847)
+    def reverse_position(self, bignode: int, offset: int) -> tuple[int, int]:
+        size = self.original_size_of(bignode)
+        return (bignode ^ 1), size - offset - 1
+
+    def node_sequence(self, node: int) -> str:
+        n = int(self.node_length[node])
+        if node < self.first_ambiguous:
+            w = self.seq2bit[node * 2:node * 2 + 2]
+            return "".join("ACGT"[(int(w[p // 32]) >> ((p % 32) * 2)) & 3] for p in range(n))
+        a = self.seq_ambiguous[(node - self.first_ambiguous) * 4:(node - self.first_ambiguous) * 4 + 4]
+        table = "?ACMGRSVTWYHKDBN"
+        return "".join(table[sum(((int(a[c]) >> p) & 1) << c for c in range(4))] for p in range(n))
+
+    def char_table(self) -> np.ndarray:
+        """[N, 64] uint8 characters of every split node (AlignmentGraph::NodeSequences)."""
+        out = np.zeros((self.num_nodes, 64), dtype=np.uint8)
+        fa = self.first_ambiguous
+        if fa:
+            w = self.seq2bit.reshape(fa, 2)
+            pos = np.arange(64)
+            codes = (w[:, pos // 32] >> (2 * (pos % 32)).astype(np.uint64)) & np.uint64(3)
+            out[:fa] = np.frombuffer(b"ACGT", dtype=np.uint8)[codes.astype(np.int64)]
+        for n in range(fa, self.num_nodes):
+            s = self.node_sequence(n).encode()
+            out[n, :len(s)] = np.frombuffer(s, dtype=np.uint8)
+        return out
+
+    def desc(self):
+        """A ga_graph_desc ctypes struct pointing at this graph's arrays."""
+        from ._abi import GraphDesc
+        return GraphDesc.from_graph(self)
+
+
+def _arr(buf, off, dtype, count):
+    n = np.dtype(dtype).itemsize * count
+    return np.frombuffer(buf, dtype=dtype, count=count, offset=off).copy(), off + n
+
+
+def load_gag(path: str) -> Graph:
+    """Reads the GAG1 layout written by the reference-graph dumper."""
+    buf = open(path, "rb").read()
+    if buf[:4] != b"GAG1":
+        raise ValueError(f"{path}: not a GAG1 graph")
+    hdr = np.frombuffer(buf, dtype=np.uint64, count=8, offset=4)
+    N, fa, n_in, n_out, M, n_lookup, n_names, bp = (int(x) for x in hdr)
+    off = 4 + 64
+    node_length, off = _arr(buf, off, np.uint32, N)
+    node_ids, off = _arr(buf, off, np.int32, N)
+    node_offset, off = _arr(buf, off, np.uint32, N)
+    reverse, off = _arr(buf, off, np.uint8, N)
+    linearizable, off = _arr(buf, off, np.uint8, N)
+    component, off = _arr(buf, off, np.uint32, N)
+    chain_number, off = _arr(buf, off, np.uint64, N)
+    chain_pos, off = _arr(buf, off, np.uint64, N)
+    seq2, off = _arr(buf, off, np.uint64, fa * 2)
+    seqa, off = _arr(buf, off, np.uint64, (N - fa) * 4)
+    in_off, off = _arr(buf, off, np.uint32, N + 1)
+    in_nb, off = _arr(buf, off, np.uint32, n_in)
+    out_off, off = _arr(buf, off, np.uint32, N + 1)
+    out_nb, off = _arr(buf, off, np.uint32, n_out)
+    lookup_ids, off = _arr(buf, off, np.int32, M)
+    orig_size, off = _arr(buf, off, np.uint32, M)
+    lookup_off, off = _arr(buf, off, np.uint32, M + 1)
+    lookup_nodes, off = _arr(buf, off, np.uint32, n_lookup)
+    name_len, off = _arr(buf, off, np.uint32, M)
+    blob = buf[off:off + n_names].decode()
+    names, p = [], 0
+    for ln in name_len:
+        names.append(blob[p:p + int(ln)])
+        p += int(ln)
+    return Graph(N, fa, node_length, node_ids, node_offset, reverse, linearizable, component,
+                 chain_number, chain_pos, seq2, seqa, in_off, in_nb, out_off, out_nb,
+                 lookup_ids, orig_size, lookup_off, lookup_nodes, names, bp)
+
+
+def save_gag(g: Graph, path: str) -> None:
+    with open(path, "wb") as f:
+        f.write(b"GAG1")
+        blob = "".join(g.names).encode()
+        f.write(np.array([g.num_nodes, g.first_ambiguous, len(g.in_neighbors), len(g.out_neighbors),
+                          len(g.lookup_ids), len(g.lookup_nodes), len(blob), g.bp_size], dtype=np.uint64).tobytes())
+        for a, dt in ((g.node_length, np.uint32), (g.node_ids, np.int32), (g.node_offset, np.uint32),
+                      (g.reverse, np.uint8), (g.linearizable, np.uint8), (g.component, np.uint32),
+                      (g.chain_number, np.uint64), (g.chain_approx_pos, np.uint64), (g.seq2bit, np.uint64),
+                      (g.seq_ambiguous, np.uint64), (g.in_offsets, np.uint32), (g.in_neighbors, np.uint32),
+                      (g.out_offsets, np.uint32), (g.out_neighbors, np.uint32), (g.lookup_ids, np.int32),
+                      (g.original_size, np.uint32), (g.lookup_offsets, np.uint32), (g.lookup_nodes, np.uint32),
+                      (np.array([len(n.encode()) for n in g.names], dtype=np.uint32), np.uint32)):
+            f.write(np.ascontiguousarray(a, dtype=dt).tobytes())
+        f.write(blob)
+
+
+# --- builder ---------------------------------------------------------------
+
+def _csr(lists):
+    off = np.zeros(len(lists) + 1, dtype=np.uint32)
+    off[1:] = np.cumsum([len(x) for x in lists])
+    flat = np.fromiter((v for x in lists for v in x), dtype=np.uint32, count=int(off[-1]))
+    return off, flat
+
+
+def _find_linearizable(in_lists):
+    """AlignmentGraph::findLinearizable (AlignmentGraph.cpp:632-724), step for step.
+
+    The reference marks a node checked before pushing it, and its walk ends as
+    soon as the top of the stack is checked, so every walk ends on its first
+    step and no node is ever marked linearizable.  The restatement keeps that
+    behaviour (the flag feeds the queue-seeding skip at
+    GraphAlignerBitvectorBanded.h:317)."""
+    n = len(in_lists)
+    lin = np.zeros(n, dtype=np.uint8)
+    checked = np.zeros(n, dtype=bool)
+    on_stack = np.zeros(n, dtype=bool)
+    for node in range(n):
+        if checked[node]:
+            continue
+        if len(in_lists[node]) != 1:
+            checked[node] = True
+            continue
+        checked[node] = True
+        stack = [node]
+        on_stack[node] = True
+        while True:
+            top = stack[-1]
+            if len(in_lists[top]) != 1 or checked[top]:
+                for s_ in stack[:-1]:
+                    checked[s_] = True
+                    lin[s_] = 1
+                    on_stack[s_] = False
+                lin[top] = 0
+                checked[top] = True
+                on_stack[top] = False
+                break
+            nb = in_lists[top][0]
+            if nb == node:
+                for s_ in stack:
+                    checked[s_] = True
+                    lin[s_] = 0
+                    on_stack[s_] = False
+                break
+            if on_stack[nb]:
+                k = stack.index(nb)
+                for s_ in stack[k + 1:]:
+                    checked[s_] = True
+                    lin[s_] = 0
+                    on_stack[s_] = False
+                for s_ in stack[:k]:
+                    checked[s_] = True
+                    lin[s_] = 1
+                    on_stack[s_] = False
+                break
+            stack.append(nb)
+            on_stack[nb] = True
+    return lin
+
+
+def _component_order(out_lists):
+    """AlignmentGraph::doComponentOrder (AlignmentGraph.cpp:987-1094): iterative Tarjan
+    from node 0 upward, components numbered in reverse finishing order so that every
+    edge goes from a lower to an equal or higher component number."""
+    n = len(out_lists)
+    UNSET = -1
+    index = np.full(n, UNSET, dtype=np.int64)
+    low = np.full(n, UNSET, dtype=np.int64)
+    on_stack = np.zeros(n, dtype=bool)
+    comp = np.full(n, UNSET, dtype=np.int64)
+    stack = []
+    counter = 0
+    next_comp = 0
+    for root in range(n):
+        if index[root] != UNSET:
+            continue
+        call = [(root, 0)]
+        index[root] = low[root] = counter
+        counter += 1
+        stack.append(root)
+        on_stack[root] = True
+        while call:
+            v, i = call[-1]
+            outs = out_lists[v]
+            if i < len(outs):
+                w = outs[i]
+                call[-1] = (v, i + 1)
+                if index[w] == UNSET:
+                    index[w] = low[w] = counter
+                    counter += 1
+                    stack.append(w)
+                    on_stack[w] = True
+                    call.append((w, 0))
+                elif on_stack[w]:
+                    low[v] = min(low[v], index[w])
+                continue
+            call.pop()
+            if call:
+                u = call[-1][0]
+                low[u] = min(low[u], low[v])
+            if low[v] == index[v]:
+                while True:
+                    w = stack.pop()
+                    on_stack[w] = False
+                    comp[w] = next_comp
+                    if w == v:
+                        break
+                next_comp += 1
+    return (next_comp - 1 - comp).astype(np.uint32)
+
+
+def build_from_gfa(gfa_text: str) -> Graph:
+    """Alignment graph from a GFA whose links all have 0-bp overlap."""
+    seqs = {}
+    order = []
+    links = []
+    for line in gfa_text.splitlines():
+        if not line or line[0] not in "SL":
+            continue
+        f = line.split("\t")
+        if f[0] == "S":
+            seqs[f[1]] = f[2]
+            order.append(f[1])
+        else:
+            if f[5] not in ("0M", "*"):
+                raise ValueError("build_from_gfa handles 0-bp overlaps only")
+            links.append((f[1], f[2] == "+", f[3], f[4] == "+"))
+    numeric = all(s.lstrip("-").isdigit() for s in order)
+    ids = {name: (int(name) if numeric else k + 1) for k, name in enumerate(order)}
+    pieces = []     # (bignode, offset, sequence)
+    lookup = []     # (bignode, [piece indices])
+    names = []
+    size_of = {}
+    for name in order:
+        s = seqs[name]
+        nid = ids[name]
+        for strand, text in ((0, s), (1, s.encode().translate(_COMPLEMENT)[::-1].decode())):
+            big = nid * 2 + strand
+            idx = []
+            for o in range(0, len(text), SPLIT_NODE_SIZE):
+                idx.append(len(pieces))
+                pieces.append((big, o, text[o:o + SPLIT_NODE_SIZE]))
+            lookup.append((big, idx))
+            names.append("" if numeric else name)
+            size_of[big] = len(text)
+    n = len(pieces)
+    in_lists = [[] for _ in range(n)]
+    out_lists = [[] for _ in range(n)]
+    first_piece = {big: idx[0] for big, idx in lookup}
+    last_piece = {big: idx[-1] for big, idx in lookup}
+    for big, idx in lookup:
+        for a, b in zip(idx, idx[1:]):
+            out_lists[a].append(b)
+            in_lists[b].append(a)
+
+    def add_edge(frm, to):
+        a, b = last_piece[frm], first_piece[to]
+        if a not in in_lists[b]:
+            in_lists[b].append(a)
+        if b not in out_lists[a]:
+            out_lists[a].append(b)
+    for a, ap, b, bp in links:
+        fa_, fb = ids[a] * 2 + (0 if ap else 1), ids[b] * 2 + (0 if bp else 1)
+        add_edge(fa_, fb)
+        add_edge(fb ^ 1, fa_ ^ 1)
+    # ambiguous pieces go to the end in reverse order (RenumberAmbiguousToEnd, AlignmentGraph.cpp:898-985)
+    amb = [any(c not in "ACGTUacgtu" for c in p[2]) for p in pieces]
+    renum = np.zeros(n, dtype=np.int64)
+    na = 0
+    nn = 0
+    for i in range(n):
+        if amb[i]:
+            renum[i] = n - 1 - na
+            na += 1
+        else:
+            renum[i] = nn
+            nn += 1
+    perm = np.empty(n, dtype=np.int64)
+    perm[renum] = np.arange(n)
+    pieces = [pieces[perm[i]] for i in range(n)]
+    in_lists = [[int(renum[x]) for x in in_lists[perm[i]]] for i in range(n)]
+    out_lists = [[int(renum[x]) for x in out_lists[perm[i]]] for i in range(n)]
+    lookup = [(big, [int(renum[x]) for x in idx]) for big, idx in lookup]
+    node_length = np.array([len(p[2]) for p in pieces], dtype=np.uint32)
+    node_ids = np.array([p[0] for p in pieces], dtype=np.int32)
+    node_offset = np.array([p[1] for p in pieces], dtype=np.uint32)
+    reverse = (node_ids % 2 == 1).astype(np.uint8)
+    seq2 = np.zeros((nn, 2), dtype=np.uint64)
+    for i in range(nn):
+        codes = _CODE[np.frombuffer(pieces[i][2].encode(), dtype=np.uint8)].astype(np.uint64)
+        for c in range(2):
+            part = codes[c * 32:(c + 1) * 32]
+            if len(part):
+                seq2[i, c] = np.bitwise_or.reduce(part << (2 * np.arange(len(part), dtype=np.uint64)))
+    seqa = np.zeros((na, 4), dtype=np.uint64)
+    for k in range(na):
+        text = pieces[nn + k][2].upper()
+        for p_, ch in enumerate(text):
+            m = _IUPAC[ch]
+            for c in range(4):
+                if m >> c & 1:
+                    seqa[k, c] |= np.uint64(1 << p_)
+    in_off, in_nb = _csr(in_lists)
+    out_off, out_nb = _csr(out_lists)
+    lin = _find_linearizable(in_lists)
+    comp = _component_order(out_lists)
+    l_off, l_nodes = _csr([idx for _, idx in lookup])
+    return Graph(n, nn, node_length, node_ids, node_offset, reverse, lin, comp,
+                 np.arange(n, dtype=np.uint64), np.zeros(n, dtype=np.uint64),
+                 seq2.reshape(-1), seqa.reshape(-1), in_off, in_nb, out_off, out_nb,
+                 np.array([b for b, _ in lookup], dtype=np.int32),
+                 np.array([size_of[b] for b, _ in lookup], dtype=np.uint32), l_off, l_nodes,
+                 names, int(node_length.sum()))

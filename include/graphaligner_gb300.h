@@ -1,0 +1,139 @@
+/*
+ * graphaligner_gb300 — C ABI of the GB300 seed-extension path.
+ *
+ * These entry points replace GraphAligner's seed-extension hot path behind its
+ * own C++ API.  Every call returns an int status (GA_OK on success) and never
+ * throws; device buffers belong to the handles.  All inputs and outputs are
+ * host pointers with explicit sizes unless a name says "device".
+ *
+ * Reference interfaces replaced (paths inside the GraphAligner project):
+ *   ga_graph_upload      AlignmentGraph device-visible fields, built by
+ *                        AlignmentGraph::Finalize (src/AlignmentGraph.h:121-139,
+ *                        src/AlignmentGraph.cpp:252-296)
+ *   ga_extend_batch      GraphAlignerBitvectorBanded::getReverseTraceFromSeed
+ *                        (src/GraphAlignerBitvectorBanded.h:59-76), called twice
+ *                        per seed by GraphAligner::getTwoDirectionalTrace
+ *                        (src/GraphAligner.h:475-520)
+ *   ga_index_upload /    MinimizerSeeder index arrays and getSeeds lookup
+ *   ga_seed_batch        (src/MinimizerSeeder.h:16-33, src/MinimizerSeeder.cpp:521-543)
+ */
+#ifndef GRAPHALIGNER_GB300_H
+#define GRAPHALIGNER_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GA_OK              0
+#define GA_TRACE_FAILED    1   /* OnewayTrace::TraceFailed(): score INT32_MAX (GraphAlignerCommon.h:154-163) */
+#define GA_ASSERT          2   /* a reference assert would have thrown ThreadReadAssertion::AssertionFailure */
+#define GA_CAPACITY        3   /* a per-extension device capacity (band, queue, trace, arena) was exceeded */
+#define GA_BAD_REQUEST     4
+#define GA_ERR_ARGUMENT   -1
+#define GA_ERR_CUDA       -2
+#define GA_ERR_NOMEM      -3
+#define GA_ERR_STATE      -4
+
+/* The AlignmentGraph fields the DP reads, as plain arrays.  Node indices are the
+ * AlignmentGraph's split-node indices (<= 64 bp per node).  Nodes below
+ * first_ambiguous carry 2-bit sequence (two 64-bit chunks of 32 bp, A=0 C=1 G=2
+ * T=3, AlignmentGraph.cpp:111-139); nodes from first_ambiguous on carry four
+ * 64-bit masks A,C,G,T (AlignmentGraph.h:36-68).  Neighbour lists keep the
+ * AlignmentGraph's order, which decides traceback ties. */
+typedef struct ga_graph_desc {
+    uint32_t num_nodes;
+    uint32_t first_ambiguous;
+    const uint32_t* node_length;      /* [num_nodes] 1..64 */
+    const uint64_t* seq2bit;          /* [first_ambiguous * 2] */
+    const uint64_t* seq_ambiguous;    /* [(num_nodes - first_ambiguous) * 4] A,C,G,T */
+    const uint32_t* in_offsets;       /* [num_nodes + 1] */
+    const uint32_t* in_neighbors;
+    const uint32_t* out_offsets;      /* [num_nodes + 1] */
+    const uint32_t* out_neighbors;
+    const uint8_t*  linearizable;     /* [num_nodes] */
+    const uint32_t* component;        /* [num_nodes] componentNumber (AlignmentGraph.cpp:987-1094) */
+} ga_graph_desc;
+
+/* Extension parameters, GraphAlignerCommon::Params (GraphAlignerCommon.h:83-109). */
+typedef struct ga_extend_params {
+    uint32_t bandwidth;               /* alignmentBandwidth */
+    int32_t  xdrop;                   /* Xdropcutoff */
+    uint64_t max_cells_per_slice;     /* maxCellsPerSlice (tangle effort); UINT64_MAX = unlimited */
+    int32_t  xscore_error_cost;       /* XscoreErrorCost = int(100*(c/(1-c)+1)) */
+} ga_extend_params;
+
+/* A batch of extensions.  Extension i aligns seq[seq_offset[i] .. +seq_len[i]) starting
+ * at split node start_node[i], offset start_offset[i] inside it — the node and offset
+ * getInitialSliceExactPosition resolves from (bigraphNodeId, nodeOffset)
+ * (GraphAlignerBitvectorCommon.h:1551-1587). */
+typedef struct ga_extend_batch_desc {
+    uint32_t num;
+    const uint8_t*  seq;
+    const uint64_t* seq_offset;
+    const uint32_t* seq_len;
+    const uint32_t* start_node;
+    const uint32_t* start_offset;
+    const uint64_t* trace_offset;     /* where extension i's trace items start in trace_items */
+    const uint32_t* trace_capacity;   /* room for extension i's trace items */
+} ga_extend_batch_desc;
+
+/* Results.  A trace item packs one OnewayTrace TraceItem in DP order (end of the
+ * alignment first, GraphAlignerBitvectorCommon.h:571-758):
+ *   bits  0..31  split node index
+ *   bits 32..37  nodeOffset inside the split node
+ *   bit  38      nodeSwitch
+ *   bits 39..63  seqPos + 1 (0 encodes seqPos == (size_t)-1, the row above the read) */
+typedef struct ga_extend_results {
+    int32_t*  status;                 /* [num] GA_OK / GA_TRACE_FAILED / GA_ASSERT / GA_CAPACITY */
+    int32_t*  score;                  /* [num] OnewayTrace::score */
+    uint32_t* trace_len;              /* [num] items written */
+    uint64_t* trace_items;            /* packed items, laid out by trace_offset */
+    uint64_t* cell_steps;             /* [num] or NULL: Myers column steps in the fill (GCUPS numerator / 64) */
+} ga_extend_results;
+
+#define GA_TRACE_NODE(x)      ((uint32_t)((x) & 0xffffffffu))
+#define GA_TRACE_OFFSET(x)    ((uint32_t)(((x) >> 32) & 63u))
+#define GA_TRACE_SWITCH(x)    ((uint32_t)(((x) >> 38) & 1u))
+#define GA_TRACE_SEQPOS1(x)   ((uint64_t)((x) >> 39))
+
+/* ---- device graph ---- */
+typedef struct ga_graph* ga_graph_t;
+int ga_graph_upload(const ga_graph_desc* desc, int device, ga_graph_t* out);
+int ga_graph_free(ga_graph_t graph);
+
+/* ---- batched extension ---- */
+typedef struct ga_extender* ga_extender_t;
+/* arena_bytes: device bytes for per-extension DP tables; 0 picks a default. */
+int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out);
+int ga_extender_free(ga_extender_t ext);
+/* Host buffers in, host buffers out: copies, launches and waits. */
+int ga_extend_batch(ga_extender_t ext, const ga_extend_params* params,
+                    const ga_extend_batch_desc* batch, ga_extend_results* results);
+/* Device-resident variant: every pointer in batch/results is a device pointer.
+ * Work is enqueued on `stream` (a cudaStream_t; NULL = the extender's stream);
+ * the call reads the lengths back once to order the work and waits for the
+ * kernels, because extensions that outgrow the first pass's per-thread
+ * capacities are re-run with larger capacities before it returns. */
+int ga_extend_batch_device(ga_extender_t ext, const ga_extend_params* params,
+                           const ga_extend_batch_desc* batch, ga_extend_results* results,
+                           void* stream);
+/* Kernel time of the last ga_extend_batch* call in milliseconds (CUDA events on
+ * the launching stream); valid after the stream has been synchronised. */
+int ga_extender_last_kernel_ms(ga_extender_t ext, float* ms);
+/* Split of the same: fill kernel and traceback kernel milliseconds. */
+int ga_extender_last_times(ga_extender_t ext, float* fill_ms, float* trace_ms);
+/* Number of kernel launches made by the last ga_extend_batch* call. */
+int ga_extender_last_launches(ga_extender_t ext, uint32_t* launches);
+
+const char* ga_last_error(void);
+const char* ga_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,67 @@
+"""Loads the golden vectors in tests/golden/ (made by tests/golden/make_golden.py
+from the reference's own source) and digests results in the same form."""
+from __future__ import annotations
+
+import gzip
+import hashlib
+import os
+import tempfile
+
+import numpy as np
+
+from graphaligner_gb300 import graph as gg
+from graphaligner_gb300.extend import pack_batch
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_graph(name: str):
+    with tempfile.NamedTemporaryFile(suffix=".gag") as f:
+        f.write(gzip.open(os.path.join(GOLDEN, f"{name}_graph.gag.gz")).read())
+        f.flush()
+        return gg.load_gag(f.name)
+
+
+def load_requests(name: str):
+    seqs, nodes, offs = [], [], []
+    for line in gzip.open(os.path.join(GOLDEN, f"{name}_ext.tsv.gz"), "rt"):
+        a, b, c = line.rstrip("\n").split("\t")
+        nodes.append(int(a))
+        offs.append(int(b))
+        seqs.append(c.encode())
+    return seqs, np.array(nodes), np.array(offs)
+
+
+def load_digests(name: str, bandwidth: int):
+    out = []
+    for line in open(os.path.join(GOLDEN, f"{name}_ext_b{bandwidth}.digest")):
+        s, sc, n, h = line.split()
+        out.append((int(s), int(sc), int(n), h))
+    return out
+
+
+def digest(result, i: int):
+    status = int(result.status[i])
+    if status != 0:
+        return (status, 0, 0, hashlib.sha1(b"").hexdigest())
+    items = np.ascontiguousarray(result.items(i))
+    return (status, int(result.score[i]), len(items), hashlib.sha1(items.tobytes()).hexdigest())
+
+
+def golden_case(name: str):
+    g = load_graph(name)
+    seqs, nodes, offs = load_requests(name)
+    return g, pack_batch(g, seqs, nodes, offs)
+
+
+def compare(result, expected):
+    """Indices whose (status, score, n, digest) differ."""
+    bad = []
+    for i, e in enumerate(expected):
+        d = digest(result, i)
+        if e[0] != 0:
+            if d[0] != e[0]:
+                bad.append(i)
+        elif d != e:
+            bad.append(i)
+    return bad

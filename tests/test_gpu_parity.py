@@ -1,0 +1,67 @@
+"""GPU kernels against the reference's golden vectors and against the oracle."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from golden_sets import compare, golden_case, load_digests  # noqa: E402
+
+from graphaligner_gb300 import datagen as dg  # noqa: E402
+from graphaligner_gb300 import graph as gg  # noqa: E402
+from graphaligner_gb300.extend import DeviceGraph, Extender, ExtendParams, pack_batch  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def golden_vg():
+    g, batch = golden_case("vg50k")
+    dgraph = DeviceGraph(g)
+    ext = Extender(dgraph)
+    yield g, batch, ext
+    ext.close()
+    dgraph.close()
+
+
+@pytest.mark.parametrize("bandwidth", [10, 5])
+def test_gpu_matches_reference_golden(cuda_lib, golden_vg, bandwidth):
+    g, batch, ext = golden_vg
+    res = ext.run(ExtendParams(bandwidth=bandwidth), batch)
+    bad = compare(res, load_digests("vg50k", bandwidth))
+    assert not bad, f"{len(bad)} extensions differ from the reference, first {bad[:5]}"
+
+
+def test_gpu_matches_reference_golden_high_error(cuda_lib):
+    g, batch = golden_case("vg50k_hi")
+    with_graph = DeviceGraph(g)
+    ext = Extender(with_graph)
+    res = ext.run(ExtendParams(bandwidth=10), batch)
+    bad = compare(res, load_digests("vg50k_hi", 10))
+    assert not bad, f"{len(bad)} extensions differ, first {bad[:5]}"
+
+
+def _assert_same(a, b, n):
+    assert np.array_equal(a.status[:n], b.status[:n])
+    assert np.array_equal(a.score[:n], b.score[:n])
+    assert np.array_equal(a.trace_len[:n], b.trace_len[:n])
+    for i in range(n):
+        assert np.array_equal(a.items(i), b.items(i)), f"trace {i} differs"
+
+
+def test_gpu_matches_oracle_generated(cuda_lib, oracle_lib):
+    vg = dg.small_vg(11)
+    g = gg.build_from_gfa(vg.to_gfa())
+    nl = np.zeros(len(vg.node_seqs) + 1, dtype=np.int64)
+    nl[1:] = [len(s) for s in vg.node_seqs]
+    reads = dg.sample_reads(vg, 80, 12, dg.uniform_length(200, 12_000), dg.uniform_error(0.03, 0.2))
+    ext = dg.seed_extensions(reads, nl, 15, 13, per_read=2)
+    batch = pack_batch(g, ext.seqs, ext.bignode, ext.offset)
+    dgraph = DeviceGraph(g)
+    x = Extender(dgraph)
+    for bw, cells in ((10, 2**64 - 1), (5, 2**64 - 1), (10, 300)):
+        p = ExtendParams(bandwidth=bw, max_cells_per_slice=cells)
+        gpu = x.run(p, batch)
+        ref = oracle_lib.extend(g, p, batch, threads=8)
+        _assert_same(gpu, ref, batch.num)
