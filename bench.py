@@ -1,0 +1,384 @@
+"""Benchmark of the batched seed-extension path on one GB300.
+
+Workload (the batched-extension configuration): a 5 Mbp variation graph with a
+variant every ~100 bp (70% SNPs, 30% indels of 1-20 bp), 50k reads log-normal
+with mean 10 kbp clipped to 1-50 kbp at U[5%,15%] error, one exact 15-mer seed
+per read taken from the true path, and both extensions of each seed
+(GraphAligner::getTwoDirectionalTrace) -> ~100k extensions, bandwidth 10,
+default X-drop, unlimited tangle effort.  Seeded synthetic data stands in for
+real reads (no public dataset is named for this path).
+
+A step is one pass of getReverseTraceFromSeed (fill + traceback) over the whole
+batch.  `value` is aligned read bp per second with the batch resident in HBM
+(device time of the fill and traceback kernels, CUDA events on their stream);
+`e2e` is the same through the host-buffer C-ABI call ga_extend_batch with the
+requests in pinned memory and the results copied back, timed around the call.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "read bp aligned/s"
+UNIT = "read bp/s"
+WORKLOAD = "batched seed extension: 5 Mbp VG (variant/100 bp), 50k reads lognormal mean 10 kbp [1,50] kbp, err U[5,15]%, exact 15-mer seed, both directions, bandwidth 10"
+INT32_OPS_PER_STEP = 40          # 20 u64 ops (two 32-bit halves each) per Myers column step
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--reads", type=int, default=50_000)
+    ap.add_argument("--cpu-sample-bp", type=float, default=200e6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(n_reads: int, rank: int):
+    from graphaligner_gb300 import datagen as dg
+    from graphaligner_gb300 import graph as gg
+    from graphaligner_gb300.extend import pack_batch
+    vg = dg.batch_vg(0)
+    g = gg.build_from_gfa(vg.to_gfa())
+    ext = dg.batch_extension_workload(n_reads, graph_seed=0, read_seed=1 + rank)
+    batch = pack_batch(g, ext.seqs, ext.bignode, ext.offset)
+    return g, batch
+
+
+def aligned_bp(res) -> int:
+    """Read bp covered by the successful extensions: seqPos of the alignment end + 1
+    (the first trace item in DP order)."""
+    total = 0
+    ok = np.nonzero(res.status == 0)[0]
+    first = res.trace_items[res.trace_offset[ok].astype(np.int64)]
+    total = int(((first >> np.uint64(39)).astype(np.int64)).sum())
+    return total
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(g, batch, params, sample_bp: float, threads: int):
+    """The oracle port of getReverseTraceFromSeed on the host cores over a bounded
+    sample (every k-th extension until sample_bp read bp), all threads."""
+    import oracle
+    from graphaligner_gb300.extend import pack_batch
+    oracle.build(reference=False)
+    lens = batch.seq_len.astype(np.int64)
+    step = max(1, int(lens.sum() / sample_bp))
+    idx = np.arange(0, batch.num, step)
+    seqs = [bytes(batch.seq[int(batch.seq_offset[i]):int(batch.seq_offset[i]) + int(lens[i])]) for i in idx]
+    sub = _subset(batch, idx)
+    t = time.perf_counter()
+    res = oracle.extend(g, params, sub, threads=threads)
+    dt = time.perf_counter() - t
+    bp = aligned_bp(res)
+    return {"value": bp / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(idx)} of {batch.num} extensions (every {step}th, {int(lens[idx].sum())} read bp), oracle restatement in C++, {threads} threads, {dt:.1f} s"}, res, idx
+
+
+def _subset(batch, idx):
+    from graphaligner_gb300.extend import PackedBatch, trace_capacity_for
+    lens = batch.seq_len[idx]
+    offs = np.zeros(len(idx), dtype=np.uint64)
+    if len(idx) > 1:
+        offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+    seq = np.concatenate([batch.seq[int(batch.seq_offset[i]):int(batch.seq_offset[i]) + int(batch.seq_len[i])] for i in idx])
+    cap = trace_capacity_for(lens)
+    toff = np.zeros(len(idx), dtype=np.uint64)
+    if len(idx) > 1:
+        toff[1:] = np.cumsum(cap[:-1].astype(np.uint64))
+    return PackedBatch(seq, offs, lens.copy(), batch.start_node[idx].copy(), batch.start_offset[idx].copy(), toff, cap)
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the CPU implementation of the path on this machine's host cores."""
+    if rank != 0:
+        return
+    from graphaligner_gb300.extend import ExtendParams
+    g, batch = make_workload(args.reads, 0)
+    params = ExtendParams(bandwidth=10)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb, _, _ = cpu_baseline(g, batch, params, args.cpu_sample_bp, threads)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's C++ source needs /root/reference to compile; on this box the oracle restatement (bit-exact with it on the golden vectors) is timed"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from graphaligner_gb300 import build
+    from graphaligner_gb300._lib import lib, check
+    from graphaligner_gb300 import _abi
+    from graphaligner_gb300._abi import ptr
+    from graphaligner_gb300.extend import DeviceGraph, Extender, ExtendParams, alloc_results, results_desc
+    build()
+    L = lib()
+
+    # ---- workload (host) ----
+    t0 = time.perf_counter()
+    g, batch = make_workload(args.reads, rank)
+    gen_s = time.perf_counter() - t0
+    params = ExtendParams(bandwidth=10)
+
+    # ---- CPU baseline first (before any GPU state exists in worker processes) ----
+    cpu = None
+    cpu_res = None
+    cpu_idx = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, cpu_res, cpu_idx = cpu_baseline(g, batch, params, args.cpu_sample_bp, os.cpu_count() or 1)
+
+    dgraph = DeviceGraph(g, device=local)
+    arena = int(min(64 << 30, max(4 << 30, int(batch.seq_len.astype(np.int64).sum()) * 24)))
+    ext = Extender(dgraph, arena_bytes=arena)
+
+    # ---- device-resident batch ----
+    dev = torch.device("cuda", local)
+    def to_dev(a, dt):
+        return torch.from_numpy(np.ascontiguousarray(a).view(dt)).to(dev)
+    d_seq = to_dev(batch.seq, np.uint8)
+    d_soff = to_dev(batch.seq_offset, np.int64)
+    d_slen = to_dev(batch.seq_len, np.int32)
+    d_sn = to_dev(batch.start_node, np.int32)
+    d_so = to_dev(batch.start_offset, np.int32)
+    d_toff = to_dev(batch.trace_offset, np.int64)
+    d_tcap = to_dev(batch.trace_capacity, np.int32)
+    n = batch.num
+    d_status = torch.empty(n, dtype=torch.int32, device=dev)
+    d_score = torch.empty(n, dtype=torch.int32, device=dev)
+    d_tlen = torch.empty(n, dtype=torch.int32, device=dev)
+    d_items = torch.empty(max(batch.total_items, 1), dtype=torch.int64, device=dev)
+    d_steps = torch.empty(n, dtype=torch.int64, device=dev)
+    u8, u32, u64, i32 = ctypes.c_uint8, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
+    def P(t, c):
+        return ctypes.cast(ctypes.c_void_p(t.data_ptr()), ctypes.POINTER(c))
+    dbatch = _abi.BatchDesc(n, P(d_seq, u8), P(d_soff, u64), P(d_slen, u32), P(d_sn, u32), P(d_so, u32), P(d_toff, u64), P(d_tcap, u32))
+    dres = _abi.Results(P(d_status, i32), P(d_score, i32), P(d_tlen, u32), P(d_items, u64), P(d_steps, u64))
+    cparams = params.c()
+    stream = torch.cuda.current_stream(dev)
+
+    def device_step():
+        check(L.ga_extend_batch_device(ext.handle, ctypes.byref(cparams), ctypes.byref(dbatch), ctypes.byref(dres),
+                                       ctypes.c_void_p(stream.cuda_stream)))
+        ms = ctypes.c_float()
+        check(L.ga_extender_last_kernel_ms(ext.handle, ctypes.byref(ms)))
+        launches = ctypes.c_uint32()
+        check(L.ga_extender_last_launches(ext.handle, ctypes.byref(launches)))
+        return ms.value, launches.value
+
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    kernel_ms, launches = [], 0
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            k, nl = device_step()
+            kernel_ms.append(k)
+            launches += nl
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    kernel_s = sum(kernel_ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([kernel_s], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        kernel_s = float(tt.item())
+
+    # results of the last step
+    res = alloc_results(batch)
+    res.status[:] = d_status.cpu().numpy()
+    res.score[:] = d_score.cpu().numpy()
+    res.trace_len[:] = d_tlen.cpu().numpy().view(np.uint32)
+    res.cell_steps[:] = d_steps.cpu().numpy().view(np.uint64)
+    res.trace_items[:] = d_items.cpu().numpy().view(np.uint64)
+    bp = aligned_bp(res)
+    steps_total = int(res.cell_steps.sum())
+    statuses = {int(s): int(c) for s, c in zip(*np.unique(res.status, return_counts=True))}
+    # the CPU sample must agree with the GPU on the same extensions
+    cpu_agree = None
+    if cpu_res is not None:
+        cpu_agree = bool(np.array_equal(cpu_res.status, res.status[cpu_idx]) and np.array_equal(cpu_res.score, res.score[cpu_idx]))
+
+    value = bp * args.steps * world / kernel_s
+    ms_per_step = kernel_s * 1e3 / args.steps
+    gcups = steps_total * 64 * args.steps / kernel_s / 1e9
+
+    # ---- end to end through the host-buffer C ABI, pinned host memory ----
+    def pinned(nbytes):
+        p = ctypes.c_void_p()
+        check(L.ga_host_alloc(ctypes.c_uint64(nbytes), ctypes.byref(p)))
+        return p
+    host_bufs = []
+    def pinned_like(a):
+        p = pinned(a.nbytes)
+        host_bufs.append(p)
+        arr = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)), shape=(a.nbytes,)).view(a.dtype)
+        arr[:] = a
+        return arr
+    from graphaligner_gb300.extend import PackedBatch, BatchResult
+    hb = PackedBatch(pinned_like(batch.seq), pinned_like(batch.seq_offset), pinned_like(batch.seq_len),
+                     pinned_like(batch.start_node), pinned_like(batch.start_offset), pinned_like(batch.trace_offset),
+                     pinned_like(batch.trace_capacity))
+    hr = BatchResult(pinned_like(np.zeros(n, np.int32)), pinned_like(np.zeros(n, np.int32)), pinned_like(np.zeros(n, np.uint32)),
+                     pinned_like(np.zeros(max(batch.total_items, 1), np.uint64)), hb.trace_offset, pinned_like(np.zeros(n, np.uint64)))
+    h2d = int(hb.seq.nbytes + n * (8 + 4 + 4 + 4 + 8 + 4 + 4))
+    d2h = int(n * (4 + 4 + 4 + 8) + batch.total_items * 8)
+    ext.run(params, hb, hr)   # warm the staging buffers
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ext.run(params, hb, hr)
+        e2e_times.append(time.perf_counter() - t)
+    e2e_same = bool(np.array_equal(hr.status, res.status) and np.array_equal(hr.score, res.score))
+    e2e_value = bp * world / statistics.median(e2e_times)
+
+    # ---- roofline ----
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    arena_bytes = ctypes.c_uint64()
+    check(L.ga_extender_last_arena_bytes(ext.handle, ctypes.byref(arena_bytes)))
+    fill_s = statistics.median(kernel_ms) / 1e3
+    alg_bytes = int(batch.seq.nbytes + arena_bytes.value)
+    achieved_gbs = alg_bytes / fill_s / 1e9
+    int_peak = ctypes.c_double()
+    check(L.ga_measure_int32_peak(local, ctypes.byref(int_peak)))
+    alu_achieved = steps_total * INT32_OPS_PER_STEP / fill_s
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "extend_kernel_traffic.json")
+    if os.path.exists(tpath):
+        t = json.load(open(tpath))
+        traffic = t.get("bytes_per_read_bp", 0) * int(batch.seq_len.astype(np.int64).sum())
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded generator; graph, reads and seeds as the workload describes)",
+        "config": {"workload": WORKLOAD, "extensions": n, "read_bp": int(batch.seq_len.astype(np.int64).sum()),
+                   "graph_nodes": g.num_nodes, "bandwidth": 10, "xdrop": params.xdrop,
+                   "l2": "inputs larger than L2 (sequences + DP-table arena written every step)",
+                   "parallelism": f"replicas{world}"},
+        "gcups": gcups,
+        "gpu_launches": launches,
+        "statuses": statuses,
+        "kernel_ms": statistics.median(kernel_ms), "wall_s_timed_region": wall,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "seconds_per_step": statistics.median(e2e_times), "same_results": e2e_same},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak, "traffic": traffic, "kernel": "extend_kernel (fill + traceback, fused)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+                     "note": "the fill is integer-ALU / dependency-latency bound, see alu"},
+        "alu": {"achieved": alu_achieved, "peak": int_peak.value, "unit": "int32 op/s", "frac": alu_achieved / int_peak.value,
+                "ops_per_column_step": INT32_OPS_PER_STEP, "peak_source": "ga_measure_int32_peak (xor+add chains, this GPU)"},
+        "cpu_baseline": cpu, "cpu_sample_agrees": cpu_agree,
+        "clocks": clocks.summary(),
+        "workload_gen_s": gen_s,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ext.close()
+    dgraph.close()
+    for p in host_bufs:
+        L.ga_host_free(p)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -77,7 +77,8 @@ struct ga_extender
 {
     ga_graph* graph = nullptr;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[3] {};
+    cudaEvent_t ev[4] {};
+    cudaStream_t side = nullptr;          // the one-extension-per-warp launch runs beside the bulk one
     int sms = 0;
     int block = 128;
     gadev::Caps caps {};
@@ -89,13 +90,14 @@ struct ga_extender
     unsigned long long* arenaCursor = nullptr;
     float lastFillMs = 0;
     float lastTraceMs = 0;
+    uint64_t lastArenaBytes = 0;
+    uint32_t lastDedicated = 0;
     uint32_t lastLaunches = 0;
     // host-batch staging
     DevBuf<uint8_t> seq;
     DevBuf<uint64_t> seqOff, traceOff, traceItems, cellSteps;
     DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order;
     DevBuf<int32_t> status, score, prevStatus;
-    DevBuf<gadev::ExtState> state;
 };
 
 extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
@@ -109,6 +111,7 @@ extern "C" int ga_graph_upload(const ga_graph_desc* desc, int device, ga_graph_t
     for (uint32_t i = 0; i < N; i++)
         if (desc->node_length[i] == 0 || desc->node_length[i] > 64) return fail(GA_ERR_ARGUMENT, "node length outside 1..64");
     GA_CUDA(cudaSetDevice(device));
+    if (ga_upload_tables() != 0) return fail(GA_ERR_CUDA, "constant tables");
     ga_graph* g = new ga_graph();
     g->device = device;
     g->N = N;
@@ -164,6 +167,12 @@ extern "C" int ga_graph_free(ga_graph_t g)
     return GA_OK;
 }
 
+// Extensions at least this many times the median length run one per warp (lane 0
+// alone), the rest 32 per warp in longest-first groups; at most kMaxDedicated
+// warps per SM are given to the long ones.
+static constexpr double kDedicatedFactor = 4.0;
+static constexpr uint32_t kMaxDedicated = 8;
+
 static gadev::Caps base_caps()
 {
     gadev::Caps c;
@@ -195,11 +204,12 @@ extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_ext
     GA_CUDA(cudaGetDeviceProperties(&prop, graph->device));
     x->sms = prop.multiProcessorCount;
     x->caps = base_caps();
-    int occ = std::max(1, ga_fill_occupancy(x->block));
-    uint64_t slots = (uint64_t)x->sms * occ * x->block;
+    int occ = std::max(1, ga_extend_occupancy(x->block));
+    uint64_t slots = (uint64_t)x->sms * occ * x->block + (uint64_t)x->sms * kMaxDedicated * 32;
     uint64_t stride = ga_workspace_bytes(x->caps);
     x->workspaceBytes = slots * stride;
     GA_CUDA(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking));
+    GA_CUDA(cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking));
     for (auto& e : x->ev) GA_CUDA(cudaEventCreate(&e));
     cudaError_t e = cudaMalloc((void**)&x->workspace, x->workspaceBytes);
     if (e != cudaSuccess) { delete x; return cuda_fail(e, "workspace"); }
@@ -225,16 +235,18 @@ extern "C" int ga_extender_free(ga_extender_t x)
     cudaFree(x->arenaCursor);
     x->seq.release(); x->seqOff.release(); x->traceOff.release(); x->traceItems.release(); x->cellSteps.release();
     x->seqLen.release(); x->startNode.release(); x->startOffset.release(); x->traceCap.release(); x->traceLen.release();
-    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release(); x->state.release();
+    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
+    cudaStreamDestroy(x->side);
     delete x;
     return GA_OK;
 }
 
-// Runs one batch whose buffers are all on the device.  order: processing order.
+// Runs one batch whose buffers are all on the device.  order: processing order
+// (longest first); lengths: host copy of the sequence lengths.
 static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend_batch_desc* b, ga_extend_results* r,
-    const uint32_t* order, gadev::ExtState* state, int32_t* prevStatus, cudaStream_t stream, bool sync)
+    const uint32_t* order, const std::vector<uint32_t>& sortedLen, int32_t* prevStatus, cudaStream_t stream)
 {
     gadev::FillArgs fa {};
     fa.g = x->graph->d;
@@ -249,11 +261,9 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     fa.seqLen = b->seq_len;
     fa.startNode = b->start_node;
     fa.startOffset = b->start_offset;
-    fa.state = state;
     fa.arena = x->arena;
     fa.arenaBytes = x->arenaBytes;
     fa.arenaCursor = x->arenaCursor;
-    fa.workCounter = x->counters;
     fa.workspace = x->workspace;
 
     gadev::TraceArgs ta {};
@@ -264,7 +274,6 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     ta.seq = b->seq;
     ta.seqOff = b->seq_offset;
     ta.seqLen = b->seq_len;
-    ta.state = state;
     ta.arena = x->arena;
     ta.traceOffset = b->trace_offset;
     ta.traceCap = b->trace_capacity;
@@ -273,53 +282,74 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     ta.traceLen = r->trace_len;
     ta.traceItems = r->trace_items;
     ta.cellSteps = r->cell_steps;
-    ta.workCounter = x->counters + 1;
 
+    const uint32_t n = b->num;
+    uint32_t dedicated = 0;
+    if (n > 0)
+    {
+        const double median = sortedLen[n / 2];
+        while (dedicated < n && dedicated < (uint32_t)x->sms * kMaxDedicated && sortedLen[dedicated] >= kDedicatedFactor * median && sortedLen[dedicated] > 2048)
+            dedicated++;
+    }
     x->lastFillMs = 0;
     x->lastTraceMs = 0;
     x->lastLaunches = 0;
-    const int traceOcc = std::max(1, ga_trace_occupancy(x->block));
     for (int round = 0; round < 3; round++)
     {
         gadev::Caps caps = scaled_caps(round);
         uint64_t stride = ga_workspace_bytes(caps);
         uint64_t slots = x->workspaceBytes / stride;
-        int fillGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>(slots / x->block, (b->num + x->block - 1) / x->block));
-        int traceGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)x->sms * traceOcc, (b->num + x->block - 1) / x->block));
         if (round > 0)
         {
             // only extensions that ran out of a capacity in the previous round run again
-            GA_CUDA(cudaMemcpyAsync(prevStatus, r->status, (size_t)b->num * 4, cudaMemcpyDeviceToDevice, stream));
-            // workspace tables laid out for other capacities: clear their generation stamps
+            GA_CUDA(cudaMemcpyAsync(prevStatus, r->status, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream));
+            // the workspace tables are laid out for other capacities: clear their stamps
             GA_CUDA(cudaMemsetAsync(x->workspace, 0, x->workspaceBytes, stream));
         }
         fa.caps = caps;
         fa.workspaceStride = stride;
         fa.prevStatus = round > 0 ? prevStatus : nullptr;
-        ta.prevStatus = round > 0 ? prevStatus : nullptr;
+        ta.prevStatus = fa.prevStatus;
+        const uint32_t ded = round == 0 ? dedicated : 0;
+        const uint64_t dedSlots = (uint64_t)ded * 32;
+        const uint64_t bulkSlots = slots > dedSlots ? slots - dedSlots : 0;
+        const uint32_t bulkCount = n - ded;
+        int bulkGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>(bulkSlots / x->block, ((uint64_t)bulkCount + x->block - 1) / x->block));
+        int dedGrid = (int)((dedSlots + x->block - 1) / x->block);
         GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), stream));
         GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, sizeof(unsigned long long), stream));
         GA_CUDA(cudaEventRecord(x->ev[0], stream));
-        ga_launch_fill(fa, fillGrid, x->block, stream);
-        GA_CUDA(cudaGetLastError());
+        if (ded > 0)
+        {
+            GA_CUDA(cudaStreamWaitEvent(x->side, x->ev[0], 0));
+            ga_launch_extend(fa, ta, 1, 0, ded, x->counters + 3, (uint32_t)bulkSlots, dedGrid, x->block, x->side);
+            GA_CUDA(cudaGetLastError());
+            GA_CUDA(cudaEventRecord(x->ev[3], x->side));
+            x->lastLaunches += 1;
+        }
+        if (bulkCount > 0)
+        {
+            ga_launch_extend(fa, ta, 32, ded, bulkCount, x->counters, 0, bulkGrid, x->block, stream);
+            GA_CUDA(cudaGetLastError());
+            x->lastLaunches += 1;
+        }
+        if (ded > 0) GA_CUDA(cudaStreamWaitEvent(stream, x->ev[3], 0));
         GA_CUDA(cudaEventRecord(x->ev[1], stream));
-        ga_launch_trace(ta, traceGrid, x->block, stream);
+        count_status_kernel<<<64, 256, 0, stream>>>(r->status, n, GA_CAPACITY, x->counters + 2);
         GA_CUDA(cudaGetLastError());
-        GA_CUDA(cudaEventRecord(x->ev[2], stream));
-        count_status_kernel<<<64, 256, 0, stream>>>(r->status, b->num, GA_CAPACITY, x->counters + 2);
-        GA_CUDA(cudaGetLastError());
-        x->lastLaunches += 3;
+        x->lastLaunches += 1;
         uint32_t capFails = 0;
+        unsigned long long arenaUsed = 0;
         GA_CUDA(cudaMemcpyAsync(&capFails, x->counters + 2, 4, cudaMemcpyDeviceToHost, stream));
+        GA_CUDA(cudaMemcpyAsync(&arenaUsed, x->arenaCursor, 8, cudaMemcpyDeviceToHost, stream));
         GA_CUDA(cudaStreamSynchronize(stream));
-        float f = 0, t = 0;
-        GA_CUDA(cudaEventElapsedTime(&f, x->ev[0], x->ev[1]));
-        GA_CUDA(cudaEventElapsedTime(&t, x->ev[1], x->ev[2]));
-        x->lastFillMs += f;
-        x->lastTraceMs += t;
+        if (round == 0) x->lastArenaBytes = std::min<uint64_t>(arenaUsed, x->arenaBytes);
+        float ms = 0;
+        GA_CUDA(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
+        x->lastFillMs += ms;
+        x->lastDedicated = ded;
         if (capFails == 0) break;
     }
-    (void)sync;
     return GA_OK;
 }
 
@@ -344,6 +374,8 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
         items = std::max<uint64_t>(items, b->trace_offset[i] + b->trace_capacity[i]);
     }
     std::vector<uint32_t> order = longest_first(b->seq_len, n);
+    std::vector<uint32_t> sortedLen(n);
+    for (uint32_t i = 0; i < n; i++) sortedLen[i] = b->seq_len[order[i]];
     GA_CUDA(x->seq.reserve(seqBytes));
     GA_CUDA(x->seqOff.reserve(n));
     GA_CUDA(x->seqLen.reserve(n));
@@ -358,7 +390,6 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
     GA_CUDA(x->traceLen.reserve(n));
     GA_CUDA(x->cellSteps.reserve(n));
     GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(items, 1)));
-    GA_CUDA(x->state.reserve(n));
     cudaStream_t s = x->stream;
     GA_CUDA(cudaMemcpyAsync(x->seq.ptr, b->seq, seqBytes, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->seqOff.ptr, b->seq_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
@@ -382,7 +413,7 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
     dr.trace_len = x->traceLen.ptr;
     dr.trace_items = x->traceItems.ptr;
     dr.cell_steps = x->cellSteps.ptr;
-    int rc = run_device(x, p, &db, &dr, x->order.ptr, x->state.ptr, x->prevStatus.ptr, s, true);
+    int rc = run_device(x, p, &db, &dr, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
     if (rc != GA_OK) return rc;
     GA_CUDA(cudaMemcpyAsync(r->status, dr.status, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->score, dr.score, n * 4ULL, cudaMemcpyDeviceToHost, s));
@@ -406,11 +437,12 @@ extern "C" int ga_extend_batch_device(ga_extender_t x, const ga_extend_params* p
     GA_CUDA(cudaMemcpyAsync(len.data(), b->seq_len, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaStreamSynchronize(s));
     std::vector<uint32_t> order = longest_first(len.data(), n);
+    std::vector<uint32_t> sortedLen(n);
+    for (uint32_t i = 0; i < n; i++) sortedLen[i] = len[order[i]];
     GA_CUDA(x->order.reserve(n));
-    GA_CUDA(x->state.reserve(n));
     GA_CUDA(x->prevStatus.reserve(n));
     GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
-    return run_device(x, p, b, r, x->order.ptr, x->state.ptr, x->prevStatus.ptr, s, false);
+    return run_device(x, p, b, r, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
 }
 
 extern "C" int ga_extender_last_kernel_ms(ga_extender_t x, float* ms)
@@ -424,7 +456,7 @@ extern "C" int ga_extender_last_times(ga_extender_t x, float* fill_ms, float* tr
 {
     if (!x || !fill_ms || !trace_ms) return fail(GA_ERR_ARGUMENT, "null argument");
     *fill_ms = x->lastFillMs;
-    *trace_ms = x->lastTraceMs;
+    *trace_ms = x->lastTraceMs;   // the traceback runs inside the same kernel as the fill
     return GA_OK;
 }
 
@@ -432,5 +464,83 @@ extern "C" int ga_extender_last_launches(ga_extender_t x, uint32_t* launches)
 {
     if (!x || !launches) return fail(GA_ERR_ARGUMENT, "null argument");
     *launches = x->lastLaunches;
+    return GA_OK;
+}
+
+extern "C" int ga_extender_last_arena_bytes(ga_extender_t x, uint64_t* bytes)
+{
+    if (!x || !bytes) return fail(GA_ERR_ARGUMENT, "null argument");
+    *bytes = x->lastArenaBytes;
+    return GA_OK;
+}
+
+namespace
+{
+// Independent chains of 32-bit xor + add (LOP3 + IADD3 in SASS), the operation mix of
+// the Myers column step, to measure the integer-ALU issue rate of this GPU.
+__global__ void int_peak_kernel(uint32_t* out, int iters, uint32_t seed)
+{
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t a0 = t ^ seed, a1 = t + 1, a2 = t + 2, a3 = t + 3, a4 = t + 4, a5 = t + 5, a6 = t + 6, a7 = t + 7;
+    const uint32_t k1 = seed | 1, k2 = seed * 3 + 7;
+    for (int i = 0; i < iters; i++)
+    {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+        {
+            a0 = (a0 ^ k1) + k2; a1 = (a1 ^ k2) + k1; a2 = (a2 ^ k1) + k2; a3 = (a3 ^ k2) + k1;
+            a4 = (a4 ^ k1) + k2; a5 = (a5 ^ k2) + k1; a6 = (a6 ^ k1) + k2; a7 = (a7 ^ k2) + k1;
+        }
+    }
+    uint32_t r = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
+    if (r == 0x12345678u) out[t] = r;
+}
+}
+
+extern "C" int ga_measure_int32_peak(int device, double* ops_per_second)
+{
+    if (!ops_per_second) return fail(GA_ERR_ARGUMENT, "null argument");
+    GA_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    GA_CUDA(cudaGetDeviceProperties(&prop, device));
+    const int block = 256;
+    const int grid = prop.multiProcessorCount * 8;
+    const int iters = 4096;
+    uint32_t* out = nullptr;
+    GA_CUDA(cudaMalloc((void**)&out, (size_t)grid * block * 4));
+    cudaEvent_t e0, e1;
+    GA_CUDA(cudaEventCreate(&e0));
+    GA_CUDA(cudaEventCreate(&e1));
+    int_peak_kernel<<<grid, block>>>(out, 64, 1u);
+    GA_CUDA(cudaDeviceSynchronize());
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; rep++)
+    {
+        GA_CUDA(cudaEventRecord(e0));
+        int_peak_kernel<<<grid, block>>>(out, iters, (uint32_t)rep + 3);
+        GA_CUDA(cudaEventRecord(e1));
+        GA_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        GA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double ops = (double)grid * block * iters * 8.0 * 8.0 * 2.0;
+    *ops_per_second = ops / (best * 1e-3);
+    return GA_OK;
+}
+
+extern "C" int ga_host_alloc(uint64_t bytes, void** out)
+{
+    if (!out) return fail(GA_ERR_ARGUMENT, "null argument");
+    GA_CUDA(cudaHostAlloc(out, std::max<uint64_t>(bytes, 16), cudaHostAllocDefault));
+    return GA_OK;
+}
+
+extern "C" int ga_host_free(void* p)
+{
+    if (p) GA_CUDA(cudaFreeHost(p));
     return GA_OK;
 }

@@ -114,23 +114,27 @@ __device__ __forceinline__ HSlot* hash_get_or_add(HSlot* t, u32 cap, u32 gen, u3
     return nullptr;
 }
 
+// IUPAC membership of every byte value (bit0 A, bit1 C, bit2 G, bit3 T; 0 = '-',
+// -1 = not a sequence character), filled from iupac_mask on the host at load time
+__constant__ int8_t c_iupac[256];
+
 // match masks of the 64 rows starting at read position j (getEqVector, Common.h:279-318)
-__device__ __forceinline__ bool eq_vector(const uint8_t* seq, u32 len, int64_t j, u64 eq[4])
+__device__ __forceinline__ bool eq_vector(const uint8_t* seq, u32 len, int64_t j, EqV4& eq)
 {
-    eq[0] = eq[1] = eq[2] = eq[3] = 0;
+    eq.a = eq.c = eq.g = eq.t = 0;
     bool ok = true;
     for (int r = 0; r < 64; r++)
     {
         int64_t p = j + r;
         if (p >= (int64_t)len) break;
-        int m = iupac_mask(seq[p]);
+        int m = c_iupac[seq[p]];
         // a non-sequence byte always fails; a gap fails only inside a full 64-row window
         if (m < 0 || (m == 0 && j + 64 <= (int64_t)len)) ok = false;
         u64 bit = 1ULL << r;
-        if (m & 1) eq[0] |= bit;
-        if (m & 2) eq[1] |= bit;
-        if (m & 4) eq[2] |= bit;
-        if (m & 8) eq[3] |= bit;
+        if (m & 1) eq.a |= bit;
+        if (m & 2) eq.c |= bit;
+        if (m & 4) eq.g |= bit;
+        if (m & 8) eq.t |= bit;
     }
     return ok;
 }
@@ -178,7 +182,7 @@ struct PrevInfo
 // Fill = true: the slice fill (early leave allowed, calculateNodeClipPrecise).
 // Fill = false: recalcNodeWordslice (no early leave, every column written to cols).
 template <bool Fill>
-__device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const u64 eqv[4], const PrevInfo& prev,
+__device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const EqV4& eqv, const PrevInfo& prev,
     const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, WS* cols, u64& steps, int& err)
 {
     NodeCalc result;
@@ -202,8 +206,8 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
         a0 = a[0]; a1 = a[1]; a2 = a[2]; a3 = a[3];
     }
     u64 eq0;
-    if (!amb) eq0 = eqv[c0 & 3];
-    else eq0 = ((a0 & 1) ? eqv[0] : 0) | ((a1 & 1) ? eqv[1] : 0) | ((a2 & 1) ? eqv[2] : 0) | ((a3 & 1) ? eqv[3] : 0);
+    if (!amb) eq0 = eq_pick(eqv, (u32)(c0 & 3));
+    else eq0 = eq_amb(eqv, (u32)((a0 & 1) | ((a1 & 1) << 1) | ((a2 & 1) << 2) | ((a3 & 1) << 3)));
 
     WS ws = ws_make(0, 0, 0);
     bool hasWs = false;
@@ -249,7 +253,7 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
     result.minScore = ws.end;
     result.minScoreNode = i;
     result.minScoreOffset = 0;
-    result.maxX = ws_max_xscore(ws, seqOffset, cost, 64, kAllOnes);
+    if (Fill) result.maxX = ws_max_xscore(ws, seqOffset, cost, 64, kAllOnes);
     result.maxXNode = i;
     const bool exists = (slice.node & kExists) != 0;
     if (exists)
@@ -353,11 +357,11 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
         if (!amb)
         {
             u64 chunk = pos < 32 ? c0 : c1;
-            eq = eqv[(chunk >> ((pos & 31) * 2)) & 3];
+            eq = eq_pick(eqv, (u32)((chunk >> ((pos & 31) * 2)) & 3));
         }
         else
         {
-            eq = (((a0 >> pos) & 1) ? eqv[0] : 0) | (((a1 >> pos) & 1) ? eqv[1] : 0) | (((a2 >> pos) & 1) ? eqv[2] : 0) | (((a3 >> pos) & 1) ? eqv[3] : 0);
+            eq = eq_amb(eqv, (u32)(((a0 >> pos) & 1) | (((a1 >> pos) & 1) << 1) | (((a2 >> pos) & 1) << 2) | (((a3 >> pos) & 1) << 3)));
         }
         eq &= forceEq;
         u64 Ph, Mh;
@@ -374,7 +378,7 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
             result.minScore = ws.end;
             result.minScoreOffset = pos;
         }
-        result.maxX = imax(result.maxX, ws_max_xscore(ws, seqOffset, cost, 64, Mh));
+        if (Fill) result.maxX = imax(result.maxX, ws_max_xscore(ws, seqOffset, cost, 64, Mh));
         if (!Fill) cols[pos] = ws;
         outHP |= (Ph >> 63) << pos;
         outHN |= (Mh >> 63) << pos;
@@ -486,7 +490,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
     res.maxX = kIntMin;
     res.maxXNode = 0;
     res.cells = 0;
-    u64 eqv[4];
+    EqV4 eqv;
     if (!eq_vector(seq, seqLen, j, eqv)) { err = GA_ASSERT; return res; }
     u32 heapN = 0;
     u32 poolN = 0;
@@ -625,7 +629,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
     return res;
 }
 
-__device__ void fill_extension(const FillArgs& a, const Workspace& w, u32& gen, ArenaCursor& arena, u32 ext)
+__device__ ExtState fill_extension(const FillArgs& a, const Workspace& w, u32& gen, ArenaCursor& arena, u32 ext)
 {
     const DevGraph& g = a.g;
     ExtState st;
@@ -642,15 +646,13 @@ __device__ void fill_extension(const FillArgs& a, const Workspace& w, u32& gen, 
     if (startNode >= g.N || startOff >= g.len[startNode])
     {
         st.status = GA_BAD_REQUEST;
-        a.state[ext] = st;
-        return;
+        return st;
     }
     u64 dirOff;
     if (!arena_alloc(a, arena, (u64)(numSlices + 1) * 8, dirOff))
     {
         st.status = GA_CAPACITY;
-        a.state[ext] = st;
-        return;
+        return st;
     }
     u64* dir = (u64*)(a.arena + dirOff);
     st.dir = dirOff;
@@ -676,8 +678,7 @@ __device__ void fill_extension(const FillArgs& a, const Workspace& w, u32& gen, 
         if (!commit_slice(a, arena, dir, 0, &it, 1, 0, 1, 0, startNode, false))
         {
             st.status = GA_CAPACITY;
-            a.state[ext] = st;
-            return;
+            return st;
         }
     }
     u32 prevCount = 1;
@@ -714,33 +715,7 @@ __device__ void fill_extension(const FillArgs& a, const Workspace& w, u32& gen, 
     st.committed = committed;
     if (err) st.status = err;
     else if (committed <= 1) st.status = GA_TRACE_FAILED;
-    a.state[ext] = st;
-}
-
-__global__ void __launch_bounds__(128) fill_kernel(FillArgs a)
-{
-    const u32 slot = blockIdx.x * blockDim.x + threadIdx.x;
-    Workspace w = workspace_at(a.workspace + (u64)slot * a.workspaceStride, a.caps);
-    u32 gen = w.header[0];
-    ArenaCursor arena;
-    arena.pos = 0;
-    arena.end = 0;
-    while (true)
-    {
-        u32 k = atomicAdd(a.workCounter, 1u);
-        if (k >= a.num) break;
-        u32 ext = a.order[k];
-        if (a.prevStatus && a.prevStatus[ext] != GA_CAPACITY) continue;
-        fill_extension(a, w, gen, arena, ext);
-        if (gen > 0xF0000000u)
-        {
-            // generation stamps are about to wrap: clear this thread's tables
-            for (u32 t = 0; t < 2; t++)
-                for (u32 k2 = 0; k2 < a.caps.hash; k2++) w.hash[t][k2].gen = 0;
-            gen = 0;
-        }
-    }
-    w.header[0] = gen;
+    return st;
 }
 
 // ---------------------------------------------------------------- traceback
@@ -939,7 +914,7 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
 }
 
 // recalcNodeWordslice (Common.h:1078-1102): all columns of one node-slice
-__device__ bool recalc(TraceCtx& c, u32 s, u32 node, const u64 eqv[4], WS* cols)
+__device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, WS* cols)
 {
     const Item* it = c.t.find(s, node);
     if (!it) { c.err = GA_ASSERT; return false; }
@@ -959,10 +934,9 @@ __device__ bool recalc(TraceCtx& c, u32 s, u32 node, const u64 eqv[4], WS* cols)
     return true;
 }
 
-__device__ void trace_extension(const TraceArgs& a, u32 ext, WS* cols)
+__device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st, WS* cols)
 {
     const DevGraph& g = a.g;
-    ExtState st = a.state[ext];
     u64* out = a.traceItems + a.traceOffset[ext];
     const u32 cap = a.traceCap[ext];
     if (a.cellSteps) a.cellSteps[ext] = st.steps;
@@ -995,7 +969,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, WS* cols)
     u32 node = br->maxXNode;
     i32 score = br->maxX;
     int64_t j = ((int64_t)best - 1) * 64;
-    u64 eqv[4];
+    EqV4 eqv;
     if (!eq_vector(c.seq, c.seqLen, j, eqv)) c.err = GA_ASSERT;
     u32 nodeOffset = 0xffffffffu, bvOffset = 0xffffffffu;
     if (!c.err && recalc(c, best, node, eqv, cols))
@@ -1206,24 +1180,76 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, WS* cols)
                 if (!to.overflow && trace_circular(to)) { c.err = GA_ASSERT; break; }
                 continue;
             }
-            // pickBacktraceInside (Common.h:770-815)
+            // pickBacktraceInside (Common.h:770-815).  The four neighbouring scores are
+            // carried incrementally: a vertical step moves up one row in both columns
+            // (score(r-1) = score(r) - VP_r + VN_r); a diagonal or horizontal step makes
+            // the left column current and loads the next one.  The read/graph match of
+            // a cell is bit `row` of the column's match mask (the fill's Eq), which is
+            // GraphAlignerCommon::characterMatch for every read and graph character.
             {
                 u32 hori = b.off;
                 u32 vert = row;
-                while (hori > 0 && vert > 0)
+                const bool amb = b.node >= g.firstAmbiguous;
+                const u64 nc0 = amb ? 0 : g.seq2[(u64)b.node * 2];
+                const u64 nc1 = amb ? 0 : g.seq2[(u64)b.node * 2 + 1];
+                auto colEq = [&](u32 h) -> u64
                 {
-                    i32 here = ws_value(cols[hori], (int)vert);
-                    i32 vs = ws_value(cols[hori], (int)vert - 1);
-                    i32 hs = ws_value(cols[hori - 1], (int)vert);
-                    i32 ds = ws_value(cols[hori - 1], (int)vert - 1);
-                    bool bad = false;
-                    bool eq = char_match(g, c.seq[sj + vert], b.node, hori, bad);
-                    if (bad) { c.err = GA_ASSERT; break; }
-                    if (vs == here - 1) { vert--; to.push(TPos { b.node, hori, sj + vert }, false); continue; }
-                    if (ds == here - (eq ? 0 : 1)) { hori--; vert--; to.push(TPos { b.node, hori, sj + vert }, false); continue; }
-                    if (hs == here - 1) { hori--; to.push(TPos { b.node, hori, sj + vert }, false); continue; }
-                    if (here != fake_value()) { c.err = GA_ASSERT; }
-                    break;
+                    if (!amb) return eq_pick(eqv, (u32)(((h < 32 ? nc0 : nc1) >> ((h & 31) * 2)) & 3));
+                    return eq_amb(eqv, (u32)node_char_mask(g, b.node, h));
+                };
+                if (hori > 0 && vert > 0)
+                {
+                    WS colH = cols[hori];
+                    WS colL = cols[hori - 1];
+                    i32 here = ws_value(colH, (int)vert);
+                    i32 left = ws_value(colL, (int)vert);
+                    u64 eqH = colEq(hori);
+                    while (true)
+                    {
+                        const i32 vs = here - (i32)((colH.VP >> vert) & 1) + (i32)((colH.VN >> vert) & 1);
+                        const i32 ds = left - (i32)((colL.VP >> vert) & 1) + (i32)((colL.VN >> vert) & 1);
+                        const bool eq = (eqH >> vert) & 1;
+                        if (vs == here - 1)
+                        {
+                            vert--;
+                            to.push(TPos { b.node, hori, sj + vert }, false);
+                            here = vs;
+                            left = ds;
+                        }
+                        else if (ds == here - (eq ? 0 : 1))
+                        {
+                            hori--;
+                            vert--;
+                            to.push(TPos { b.node, hori, sj + vert }, false);
+                            here = ds;
+                            colH = colL;
+                            if (hori > 0)
+                            {
+                                colL = cols[hori - 1];
+                                left = ws_value(colL, (int)vert);
+                                eqH = colEq(hori);
+                            }
+                        }
+                        else if (left == here - 1)
+                        {
+                            hori--;
+                            to.push(TPos { b.node, hori, sj + vert }, false);
+                            here = left;
+                            colH = colL;
+                            if (hori > 0)
+                            {
+                                colL = cols[hori - 1];
+                                left = ws_value(colL, (int)vert);
+                                eqH = colEq(hori);
+                            }
+                        }
+                        else
+                        {
+                            if (here != fake_value()) c.err = GA_ASSERT;
+                            break;
+                        }
+                        if (to.overflow || hori == 0 || vert == 0) break;
+                    }
                 }
                 if (c.err || to.overflow) break;
                 if (ws_value(cols[to.back.off], (int)mod64(to.back.seq)) == fake_value()) break;
@@ -1281,42 +1307,67 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, WS* cols)
     a.traceLen[ext] = status == GA_OK ? to.n : 0;
 }
 
-__global__ void __launch_bounds__(128) trace_kernel(TraceArgs a)
+// One persistent kernel per batch: a thread fills the DP table of an extension
+// and walks it back right away.  Warps take `lanesPerWarp` consecutive entries of
+// the longest-first order at a time, so the lanes of a warp hold extensions of
+// similar length; with lanesPerWarp = 1 a warp runs one extension on lane 0 alone,
+// which keeps the longest extensions free of divergence with their neighbours.
+__global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, u32 lanesPerWarp, u32 first, u32 count,
+    u32* counter, u32 slotBase)
 {
+    const u32 slot = slotBase + blockIdx.x * blockDim.x + threadIdx.x;
+    Workspace w = workspace_at(fa.workspace + (u64)slot * fa.workspaceStride, fa.caps);
+    u32 gen = w.header[0];
+    ArenaCursor arena;
+    arena.pos = 0;
+    arena.end = 0;
     WS cols[64];
+    const u32 lane = threadIdx.x & 31;
     while (true)
     {
-        u32 k = atomicAdd(a.workCounter, 1u);
-        if (k >= a.num) break;
-        u32 ext = a.order[k];
-        if (a.prevStatus && a.prevStatus[ext] != GA_CAPACITY) continue;
-        trace_extension(a, ext, cols);
+        u32 base = 0;
+        if (lane == 0) base = atomicAdd(counter, lanesPerWarp);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count) break;
+        if (lane < lanesPerWarp && base + lane < count)
+        {
+            const u32 ext = fa.order[first + base + lane];
+            if (!fa.prevStatus || fa.prevStatus[ext] == GA_CAPACITY)
+            {
+                ExtState st = fill_extension(fa, w, gen, arena, ext);
+                trace_extension(ta, ext, st, cols);
+                if (gen > 0xF0000000u)
+                {
+                    // generation stamps are about to wrap: clear this thread's tables
+                    for (u32 t = 0; t < 2; t++)
+                        for (u32 k2 = 0; k2 < fa.caps.hash; k2++) w.hash[t][k2].gen = 0;
+                    gen = 0;
+                }
+            }
+        }
     }
+    w.header[0] = gen;
 }
 
 }
 
-void ga_launch_fill(const gadev::FillArgs& a, int grid, int block, void* stream)
+void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t lanesPerWarp, uint32_t first, uint32_t count,
+    uint32_t* counter, uint32_t slotBase, int grid, int block, void* stream)
 {
-    gadev::fill_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(a);
+    gadev::extend_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(fa, ta, lanesPerWarp, first, count, counter, slotBase);
 }
 
-void ga_launch_trace(const gadev::TraceArgs& a, int grid, int block, void* stream)
+int ga_upload_tables()
 {
-    gadev::trace_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(a);
+    int8_t t[256];
+    for (int i = 0; i < 256; i++) t[i] = (int8_t)gadev::iupac_mask((unsigned char)i);
+    return cudaMemcpyToSymbol(gadev::c_iupac, t, sizeof(t)) == cudaSuccess ? 0 : -1;
 }
 
-int ga_fill_occupancy(int block)
-{
-    int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::fill_kernel, block, 0);
-    return n;
-}
-
-int ga_trace_occupancy(int block)
+int ga_extend_occupancy(int block)
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::trace_kernel, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::extend_kernel, block, 0);
     return n;
 }
 

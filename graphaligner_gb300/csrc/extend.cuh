@@ -81,16 +81,13 @@ struct FillArgs
     const u32* seqLen;
     const u32* startNode;
     const u32* startOffset;
-    ExtState* state;
     uint8_t* arena;
     u64 arenaBytes;
     unsigned long long* arenaCursor;
-    u32* workCounter;
     uint8_t* workspace;
     u64 workspaceStride;
     Caps caps;
-    const u32* onlyStatus; // when non-null, only extensions whose previous status is GA_CAPACITY run
-    const i32* prevStatus;
+    const i32* prevStatus; // when non-null, only extensions whose previous status is GA_CAPACITY run
 };
 
 struct TraceArgs
@@ -102,7 +99,6 @@ struct TraceArgs
     const uint8_t* seq;
     const u64* seqOff;
     const u32* seqLen;
-    const ExtState* state;
     const uint8_t* arena;
     const u64* traceOffset;
     const u32* traceCap;
@@ -111,14 +107,13 @@ struct TraceArgs
     u32* traceLen;
     u64* traceItems;
     u64* cellSteps;
-    u32* workCounter;
     const i32* prevStatus;
 };
 
 }
 
-void ga_launch_fill(const gadev::FillArgs& a, int grid, int block, void* stream);
-void ga_launch_trace(const gadev::TraceArgs& a, int grid, int block, void* stream);
-int ga_fill_occupancy(int block);
-int ga_trace_occupancy(int block);
+void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t lanesPerWarp, uint32_t first, uint32_t count,
+    uint32_t* counter, uint32_t slotBase, int grid, int block, void* stream);
+int ga_extend_occupancy(int block);
+int ga_upload_tables();
 uint64_t ga_workspace_bytes(const gadev::Caps& caps);

@@ -229,19 +229,19 @@ def sample_reads(g: VariationGraph, n_reads: int, seed: int, length_fn, error_fn
 
 
 def exact_seed_positions(read: Read, k: int) -> np.ndarray:
-    """Read positions q such that read[q-k+1..q] copies k consecutive path bases."""
-    ex = read.exact.astype(np.int64)
-    n = len(ex)
+    """Read positions q such that read[q-k+1..q] copies path bases with no edit
+    inside a node (prefix-sum test over the exact flags and offset continuity)."""
+    n = len(read.exact)
     if n < k:
         return np.zeros(0, dtype=np.int64)
-    run = np.convolve(ex, np.ones(k, dtype=np.int64), mode="valid") == k
-    q = np.nonzero(run)[0] + k - 1
-    # consecutive path positions on the same strand: bigoffset/bignode continuity
-    ok = np.ones(len(q), dtype=bool)
-    for d in range(1, k):
-        a = q - d
-        same = read.bignode[a] == read.bignode[a + 1]
-        ok &= ~same | (read.bigoffset[a] + 1 == read.bigoffset[a + 1])
+    bad = ~read.exact
+    step = np.zeros(n, dtype=bool)
+    same = read.bignode[1:] == read.bignode[:-1]
+    step[1:] = same & (read.bigoffset[1:] != read.bigoffset[:-1] + 1)
+    cb = np.concatenate([[0], np.cumsum(bad)])
+    cs = np.concatenate([[0], np.cumsum(step)])
+    q = np.arange(k - 1, n)
+    ok = (cb[q + 1] - cb[q + 1 - k] == 0) & (cs[q + 1] - cs[q + 2 - k] == 0)
     return q[ok]
 
 
@@ -335,3 +335,35 @@ def batch_vg(seed: int = 0):
 def batch_vg_reads(g: VariationGraph, n: int, seed: int = 1):
     """Log-normal lengths with mean 10 kbp clipped to 1-50 kbp, error U[5%, 15%]."""
     return sample_reads(g, n, seed, lognormal_length(10_000, 0.6, 1_000, 50_000), uniform_error(0.05, 0.15))
+
+
+def _extension_chunk(args):
+    graph_seed, genome_len, spacing, chunk_index, n, read_seed, k = args
+    g = make_variation_graph(genome_len, spacing, 0.7, 20, graph_seed)
+    nl = np.zeros(len(g.node_seqs) + 1, dtype=np.int64)
+    nl[1:] = [len(x) for x in g.node_seqs]
+    reads = sample_reads(g, n, read_seed * 1_000_003 + chunk_index,
+                         lognormal_length(10_000, 0.6, 1_000, 50_000), uniform_error(0.05, 0.15),
+                         prefix=f"c{chunk_index}_")
+    return seed_extensions(reads, nl, k, read_seed * 7919 + chunk_index)
+
+
+def batch_extension_workload(n_reads: int, graph_seed: int = 0, read_seed: int = 1, k: int = 15,
+                             genome_len: int = 5_000_000, spacing: int = 100, chunk: int = 1000,
+                             workers: int | None = None) -> ExtensionSet:
+    """Seed extensions of the batched-extension workload: one exact k-mer seed per read,
+    both directions, reads log-normal (mean 10 kbp, 1-50 kbp) at U[5%,15%] error.
+    Reads are made in fixed chunks with per-chunk seeds, so the result does not depend
+    on the number of worker processes."""
+    import multiprocessing as mp
+    import os
+    chunks = [(graph_seed, genome_len, spacing, c, min(chunk, n_reads - c * chunk), read_seed, k)
+              for c in range((n_reads + chunk - 1) // chunk)]
+    workers = workers or min(len(chunks), os.cpu_count() or 1)
+    if workers > 1 and len(chunks) > 1:
+        with mp.get_context("spawn").Pool(workers) as pool:
+            parts = pool.map(_extension_chunk, chunks)
+    else:
+        parts = [_extension_chunk(c) for c in chunks]
+    seqs = [x for p in parts for x in p.seqs]
+    return ExtensionSet(seqs, np.concatenate([p.bignode for p in parts]), np.concatenate([p.offset for p in parts]))

@@ -128,6 +128,16 @@ int ga_extender_last_kernel_ms(ga_extender_t ext, float* ms);
 int ga_extender_last_times(ga_extender_t ext, float* fill_ms, float* trace_ms);
 /* Number of kernel launches made by the last ga_extend_batch* call. */
 int ga_extender_last_launches(ga_extender_t ext, uint32_t* launches);
+/* DP-table bytes the first fill pass of the last call wrote to the arena. */
+int ga_extender_last_arena_bytes(ga_extender_t ext, uint64_t* bytes);
+
+/* ---- utilities ---- */
+/* Page-locked host memory for the host-buffer entry points. */
+int ga_host_alloc(uint64_t bytes, void** out);
+int ga_host_free(void* ptr);
+/* Measured issue rate of independent 32-bit xor+add chains on `device`
+ * (integer ops per second), the denominator of the DP kernels' ALU roofline. */
+int ga_measure_int32_peak(int device, double* ops_per_second);
 
 const char* ga_last_error(void);
 const char* ga_version(void);
