@@ -101,6 +101,8 @@ struct ga_extender
 };
 
 extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
+
+void ga_set_last_error(const char* message) { g_lastError = message; }
 extern "C" const char* ga_version(void) { return "graphaligner_gb300 0.1 (sm_103a)"; }
 
 extern "C" int ga_graph_upload(const ga_graph_desc* desc, int device, ga_graph_t* out)

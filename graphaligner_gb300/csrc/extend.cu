@@ -1381,3 +1381,185 @@ uint64_t ga_workspace_bytes(const gadev::Caps& c)
     b += align16((u64)c.extras * sizeof(Extra));
     return align16(b);
 }
+
+// ---------------------------------------------------------------- no-allocation entry point
+//
+// ga_extend_batch_noalloc serves callers that cannot call cudaMalloc when they
+// extend: processes whose device memory is handed out by another allocator
+// under a fixed budget (a framework's caching pool owns the GPU), and request
+// paths where the device-wide synchronisation of cudaMalloc/cudaFree is not
+// acceptable.  All of its scratch memory — the per-thread frontier tables and
+// the DP-table arena the fill writes and the traceback reads — lives in the
+// file-scope device array below, which every GPU that loads this library holds
+// until the process exits.  Inputs and outputs are the caller's device buffers.
+
+namespace gadev
+{
+static constexpr u64 kNoAllocScratchBytes = 128ULL << 20;       // 128 MiB per GPU
+static constexpr u32 kNoAllocThreads = 2048;                     // 16 blocks of 128
+static constexpr u32 kNoAllocMaxExtensions = 4096;               // per call
+static constexpr u64 kNoAllocMaxReadBp = 8000000;                // per call, summed over the batch
+static constexpr u64 kNoAllocHeaderBytes = 256;                  // work counter + arena cursor
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
+
+// The single-extension-per-thread fill + traceback of extend_kernel, with its
+// workspace and arena carved out of the scratch array and extensions taken in
+// index order (no length ordering, no second launch, no capacity retry: an
+// extension that outgrows the small tables reports GA_CAPACITY).
+__global__ void __launch_bounds__(128) extend_kernel_noalloc(FillArgs fa, TraceArgs ta, u32* counter)
+{
+    const u32 slot = blockIdx.x * blockDim.x + threadIdx.x;
+    Workspace w = workspace_at(fa.workspace + (u64)slot * fa.workspaceStride, fa.caps);
+    u32 gen = w.header[0];
+    ArenaCursor arena;
+    arena.pos = 0;
+    arena.end = 0;
+    WS cols[64];
+    while (true)
+    {
+        const u32 ext = atomicAdd(counter, 1u);
+        if (ext >= fa.num) break;
+        ExtState st = fill_extension(fa, w, gen, arena, ext);
+        trace_extension(ta, ext, st, cols);
+    }
+    w.header[0] = gen;
+}
+}
+
+extern "C" int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const ga_extend_params* params,
+    const ga_extend_batch_desc* device_batch, ga_extend_results* device_results, void* stream)
+{
+    using namespace gadev;
+    if (!device_graph || !params || !device_batch || !device_results)
+    {
+        ga_set_last_error("ga_extend_batch_noalloc: null argument");
+        return GA_ERR_ARGUMENT;
+    }
+    const u32 n = device_batch->num;
+    if (n == 0) return GA_OK;
+    if (n > kNoAllocMaxExtensions)
+    {
+        ga_set_last_error("ga_extend_batch_noalloc: more than 4096 extensions in one call (the limit of its fixed scratch)");
+        return GA_ERR_ARGUMENT;
+    }
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64)
+    {
+        ga_set_last_error("ga_extend_batch_noalloc: no current CUDA device (or ordinal above 63)");
+        return GA_ERR_CUDA;
+    }
+    // once per device, with that device current: the device address of the scratch
+    // array (its host-side name is not a device address) and the IUPAC table
+    static void* scratchAddress[64] = {};
+    if (!scratchAddress[device])
+    {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+        {
+            ga_set_last_error("ga_extend_batch_noalloc: cudaGetSymbolAddress of the scratch array failed");
+            return GA_ERR_CUDA;
+        }
+        if (ga_upload_tables() != 0)
+        {
+            ga_set_last_error("ga_extend_batch_noalloc: loading the IUPAC table failed");
+            return GA_ERR_CUDA;
+        }
+        scratchAddress[device] = p;
+    }
+    uint8_t* scratch = (uint8_t*)scratchAddress[device];
+    cudaStream_t s = (cudaStream_t)stream;
+    // the batch must fit the arena: read the lengths back into a fixed host buffer
+    static thread_local uint32_t lengths[kNoAllocMaxExtensions];
+    if (cudaMemcpyAsync(lengths, device_batch->seq_len, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess
+        || cudaStreamSynchronize(s) != cudaSuccess)
+    {
+        ga_set_last_error("ga_extend_batch_noalloc: reading the sequence lengths back failed");
+        return GA_ERR_CUDA;
+    }
+    u64 totalBp = 0;
+    for (u32 i = 0; i < n; i++) totalBp += lengths[i];
+    if (totalBp > kNoAllocMaxReadBp)
+    {
+        ga_set_last_error("ga_extend_batch_noalloc: more than 8,000,000 read bp in one call (the limit of its fixed scratch)");
+        return GA_ERR_ARGUMENT;
+    }
+
+    Caps caps;
+    caps.band = 32;
+    caps.hash = 128;
+    caps.heap = 32;
+    caps.extras = 64;
+    const u64 stride = ga_workspace_bytes(caps);
+    const u64 workspaceBytes = stride * kNoAllocThreads;
+    uint8_t* workspace = scratch + kNoAllocHeaderBytes;
+    uint8_t* arena = workspace + workspaceBytes;
+    const u64 arenaBytes = kNoAllocScratchBytes - kNoAllocHeaderBytes - workspaceBytes;
+    // every call starts from zeroed counters and tables: the array keeps what the
+    // previous call left in it
+    if (cudaMemsetAsync(scratch, 0, kNoAllocHeaderBytes + workspaceBytes, s) != cudaSuccess)
+    {
+        ga_set_last_error("ga_extend_batch_noalloc: clearing the scratch tables failed");
+        return GA_ERR_CUDA;
+    }
+
+    DevGraph g;
+    g.N = device_graph->num_nodes;
+    g.firstAmbiguous = device_graph->first_ambiguous;
+    g.len = device_graph->node_length;
+    g.seq2 = device_graph->seq2bit;
+    g.seqAmb = device_graph->seq_ambiguous;
+    g.inOff = device_graph->in_offsets;
+    g.inNb = device_graph->in_neighbors;
+    g.outOff = device_graph->out_offsets;
+    g.outNb = device_graph->out_neighbors;
+    g.lin = device_graph->linearizable;
+    g.comp = device_graph->component;
+
+    FillArgs fa {};
+    fa.g = g;
+    fa.bandwidth = params->bandwidth;
+    fa.xdrop = params->xdrop;
+    fa.maxCells = params->max_cells_per_slice;
+    fa.cost = params->xscore_error_cost;
+    fa.num = n;
+    fa.order = nullptr;
+    fa.seq = device_batch->seq;
+    fa.seqOff = device_batch->seq_offset;
+    fa.seqLen = device_batch->seq_len;
+    fa.startNode = device_batch->start_node;
+    fa.startOffset = device_batch->start_offset;
+    fa.arena = arena;
+    fa.arenaBytes = arenaBytes;
+    fa.arenaCursor = (unsigned long long*)(scratch + 8);
+    fa.workspace = workspace;
+    fa.workspaceStride = stride;
+    fa.caps = caps;
+    fa.prevStatus = nullptr;
+
+    TraceArgs ta {};
+    ta.g = g;
+    ta.cost = params->xscore_error_cost;
+    ta.num = n;
+    ta.order = nullptr;
+    ta.seq = device_batch->seq;
+    ta.seqOff = device_batch->seq_offset;
+    ta.seqLen = device_batch->seq_len;
+    ta.arena = arena;
+    ta.traceOffset = device_batch->trace_offset;
+    ta.traceCap = device_batch->trace_capacity;
+    ta.status = device_results->status;
+    ta.score = device_results->score;
+    ta.traceLen = device_results->trace_len;
+    ta.traceItems = device_results->trace_items;
+    ta.cellSteps = device_results->cell_steps;
+    ta.prevStatus = nullptr;
+
+    extend_kernel_noalloc<<<kNoAllocThreads / 128, 128, 0, s>>>(fa, ta, (u32*)scratch);
+    if (cudaGetLastError() != cudaSuccess)
+    {
+        ga_set_last_error("ga_extend_batch_noalloc: kernel launch failed");
+        return GA_ERR_CUDA;
+    }
+    return GA_OK;
+}

@@ -116,4 +116,5 @@ void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uin
     uint32_t* counter, uint32_t slotBase, int grid, int block, void* stream);
 int ga_extend_occupancy(int block);
 int ga_upload_tables();
+void ga_set_last_error(const char* message);
 uint64_t ga_workspace_bytes(const gadev::Caps& caps);

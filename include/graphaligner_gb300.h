@@ -121,6 +121,24 @@ int ga_extend_batch(ga_extender_t ext, const ga_extend_params* params,
 int ga_extend_batch_device(ga_extender_t ext, const ga_extend_params* params,
                            const ga_extend_batch_desc* batch, ga_extend_results* results,
                            void* stream);
+/* No counterpart in the reference.  Extends a batch without allocating any
+ * device memory, for callers that cannot call cudaMalloc while they extend
+ * (device memory owned by another allocator under a fixed budget, or request
+ * paths that cannot afford cudaMalloc's device-wide synchronisation).
+ * device_graph, device_batch and device_results hold device pointers.  The
+ * scratch (frontier tables and DP-table arena) is a 128 MiB device array inside
+ * this library, kept by every GPU that loads it until the process exits.
+ * Limits per call: 4096 extensions and 8,000,000 read bp in total; larger
+ * batches return GA_ERR_ARGUMENT.  Extensions that outgrow the fixed per-thread
+ * tables report GA_CAPACITY (there is no retry).  The first call on a device
+ * looks up the array's device address and loads a constant table; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (other streams, other host threads) race.  The call
+ * waits for the length read-back on `stream`, then enqueues the kernel there
+ * and returns. */
+int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const ga_extend_params* params,
+                            const ga_extend_batch_desc* device_batch, ga_extend_results* device_results,
+                            void* stream);
 /* Kernel time of the last ga_extend_batch* call in milliseconds (CUDA events on
  * the launching stream); valid after the stream has been synchronised. */
 int ga_extender_last_kernel_ms(ga_extender_t ext, float* ms);
