@@ -1,0 +1,134 @@
+"""Read-level alignment over the C ABI: GraphAligner's per-read flow with minimizer
+seeding and both extensions of every seed on the GPU, GAF out.
+
+``Aligner.align(names, seqs)`` returns the GAF text runComponentMappings would
+write for those reads with the -x vg (or -x dbg) parameters (Aligner.cpp:440-592),
+reads in input order.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import numpy as np
+
+from . import _abi
+from ._abi import ptr
+from ._lib import check, lib
+
+
+class HostGraphDesc(ctypes.Structure):
+    _fields_ = [
+        ("base", _abi.GraphDesc),
+        ("node_ids", ctypes.POINTER(ctypes.c_int32)),
+        ("node_offset", ctypes.POINTER(ctypes.c_uint32)),
+        ("reverse", ctypes.POINTER(ctypes.c_uint8)),
+        ("chain_number", ctypes.POINTER(ctypes.c_uint64)),
+        ("chain_approx_pos", ctypes.POINTER(ctypes.c_uint64)),
+        ("num_lookup", ctypes.c_uint32),
+        ("lookup_ids", ctypes.POINTER(ctypes.c_int32)),
+        ("original_size", ctypes.POINTER(ctypes.c_uint32)),
+        ("lookup_offsets", ctypes.POINTER(ctypes.c_uint32)),
+        ("lookup_nodes", ctypes.POINTER(ctypes.c_uint32)),
+        ("names", ctypes.POINTER(ctypes.c_char_p)),
+    ]
+
+    @classmethod
+    def from_graph(cls, g):
+        keep = [np.ascontiguousarray(x, dtype=dt) for x, dt in (
+            (g.node_ids, np.int32), (g.node_offset, np.uint32), (g.reverse, np.uint8), (g.chain_number, np.uint64),
+            (g.chain_approx_pos, np.uint64), (g.lookup_ids, np.int32), (g.original_size, np.uint32),
+            (g.lookup_offsets, np.uint32), (g.lookup_nodes, np.uint32))]
+        names = (ctypes.c_char_p * max(1, len(g.names)))(*[n.encode() for n in g.names])
+        d = cls(_abi.GraphDesc.from_graph(g), ptr(keep[0], ctypes.c_int32), ptr(keep[1], ctypes.c_uint32),
+                ptr(keep[2], ctypes.c_uint8), ptr(keep[3], ctypes.c_uint64), ptr(keep[4], ctypes.c_uint64),
+                len(g.lookup_ids), ptr(keep[5], ctypes.c_int32), ptr(keep[6], ctypes.c_uint32),
+                ptr(keep[7], ctypes.c_uint32), ptr(keep[8], ctypes.c_uint32), names)
+        d._keep = (keep, names, d.base)
+        return d
+
+
+class AlignParams(ctypes.Structure):
+    _fields_ = [
+        ("extend", _abi.ExtendParams),
+        ("minimizer_length", ctypes.c_uint32),
+        ("minimizer_window", ctypes.c_uint32),
+        ("minimizer_density", ctypes.c_double),
+        ("minimizer_discard_fraction", ctypes.c_double),
+        ("seed_extend_density", ctypes.c_double),
+        ("min_cluster_size", ctypes.c_uint64),
+        ("sloppy", ctypes.c_uint8),
+        ("cigar_match_mismatch", ctypes.c_uint8),
+        ("min_alignment_score", ctypes.c_int32),
+        ("multimap_score_fraction", ctypes.c_double),
+    ]
+
+
+class AlignStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("reads", "reads_with_seeds", "reads_aligned", "failed_reads", "bp_aligned",
+                                                "rounds", "extensions", "cell_steps")] + \
+               [(n, ctypes.c_double) for n in ("seed_ms", "extend_ms", "host_ms")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+def preset(name: str = "vg", bandwidth: int | None = None, tangle_effort: int | None = None) -> AlignParams:
+    """AlignerMain.cpp:119-231 for the two presets (X-drop from the 0.66 clipping cutoff)."""
+    from .extend import default_xdrop, xscore_error_cost
+    if name == "vg":
+        bw, cells, k, w, dens, ext_dens, discard = 10, 2**64 - 1, 15, 20, 10.0, -1.0, 0.001
+    elif name == "dbg":
+        bw, cells, k, w, dens, ext_dens, discard = 5, 10000, 19, 30, 5.0, 0.002, 0.0002
+    else:
+        raise ValueError(name)
+    if bandwidth is not None:
+        bw = bandwidth
+    if tangle_effort is not None:
+        cells = tangle_effort
+    return AlignParams(_abi.ExtendParams(bw, default_xdrop(), cells, xscore_error_cost()), k, w, dens, discard,
+                       ext_dens, 1, 1, 0, 0, 0.9)
+
+
+class Aligner:
+    def __init__(self, extender, graph, params: AlignParams):
+        self.extender = extender
+        self._desc = HostGraphDesc.from_graph(graph)
+        self.params = params
+        h = ctypes.c_void_p()
+        check(lib().ga_aligner_create(extender.handle, ctypes.byref(self._desc), ctypes.byref(params), ctypes.byref(h)))
+        self.handle = h
+
+    def align(self, names, seqs) -> str:
+        n = len(seqs)
+        lens = np.fromiter((len(s) for s in seqs), dtype=np.uint32, count=n)
+        offs = np.zeros(n, dtype=np.uint64)
+        if n > 1:
+            offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+        blob = np.frombuffer(b"".join(bytes(s) for s in seqs) or b"\0", dtype=np.uint8).copy()
+        cnames = (ctypes.c_char_p * max(1, n))(*[x.encode() for x in names])
+        check(lib().ga_align_reads(self.handle, n, cnames, ptr(blob, ctypes.c_uint8), ptr(offs, ctypes.c_uint64), ptr(lens, ctypes.c_uint32)))
+        text = ctypes.c_char_p()
+        size = ctypes.c_uint64()
+        check(lib().ga_aligner_gaf(self.handle, ctypes.byref(text), ctypes.byref(size)))
+        return ctypes.string_at(text, size.value).decode()
+
+    def stats(self) -> dict:
+        s = AlignStats()
+        check(lib().ga_aligner_stats(self.handle, ctypes.byref(s)))
+        return s.as_dict()
+
+    def read_bp(self, n: int) -> np.ndarray:
+        out = np.zeros(n, dtype=np.uint64)
+        check(lib().ga_aligner_read_bp(self.handle, ptr(out, ctypes.c_uint64)))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().ga_aligner_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

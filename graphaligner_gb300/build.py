@@ -10,8 +10,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgraphaligner_gb300.so")
-SOURCES = ["extend.cu", "abi.cu"]
-HEADERS = ["extend.cuh", "wordslice.cuh"]
+SOURCES = ["extend.cu", "abi.cu", "seed_kernel.cu", "align_abi.cu", "readalign.cpp", "seeding.cpp"]
+HEADERS = ["extend.cuh", "wordslice.cuh", "seed_kernel.cuh", "readalign.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,7 +38,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     procs = []
     for src in SOURCES:
-        obj = os.path.join(LIBDIR, src.replace(".cu", ".o"))
+        obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:

@@ -1,0 +1,270 @@
+// C ABI of the read-level alignment flow (ga_aligner_*): host orchestration in
+// readalign.cpp / seeding.cpp, k-mer lookups in seed_kernel.cu, extensions in
+// extend.cu through ga_extend_batch.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "readalign.h"
+#include "seed_kernel.cuh"
+#include "extend.cuh"
+#include "../../include/graphaligner_gb300.h"
+
+namespace
+{
+double ms_since(std::chrono::steady_clock::time_point t)
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+}
+}
+
+struct ga_aligner
+{
+    ga_extender_t ext = nullptr;
+    int device = 0;
+    ga_align_params params {};
+    gahost::HostGraph* graph = nullptr;
+    gahost::MinimizerIndex index;
+    gadev::SeedSlot* slots = nullptr;
+    uint64_t capacity = 0;
+    std::string gaf;
+    std::vector<uint64_t> readBp;
+    ga_align_stats stats {};
+    cudaStream_t stream = nullptr;
+    // staging
+    std::vector<uint8_t> blob;
+    std::vector<uint64_t> off, toff;
+    std::vector<uint32_t> len, node, nodeOff, cap, tlen;
+    std::vector<int32_t> status, score;
+    std::vector<uint64_t> items, steps;
+};
+
+static void extend_callback(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs)
+{
+    ga_aligner* a = (ga_aligner*)ctx;
+    const size_t n = rq.size();
+    a->off.resize(n);
+    a->len.resize(n);
+    a->node.resize(n);
+    a->nodeOff.resize(n);
+    a->cap.resize(n);
+    a->toff.resize(n);
+    uint64_t total = 0, totalItems = 0;
+    for (size_t i = 0; i < n; i++)
+    {
+        a->off[i] = total;
+        a->len[i] = rq[i].len;
+        a->node[i] = rq[i].node;
+        a->nodeOff[i] = rq[i].nodeOffset;
+        a->cap[i] = rq[i].len + rq[i].len / 4 + 512;
+        a->toff[i] = totalItems;
+        total += rq[i].len;
+        totalItems += a->cap[i];
+    }
+    a->blob.resize(std::max<uint64_t>(total, 1));
+    for (size_t i = 0; i < n; i++) memcpy(a->blob.data() + a->off[i], rq[i].seq, rq[i].len);
+    a->status.resize(n);
+    a->score.resize(n);
+    a->tlen.resize(n);
+    a->steps.resize(n);
+    a->items.resize(std::max<uint64_t>(totalItems, 1));
+    ga_extend_batch_desc b { (uint32_t)n, a->blob.data(), a->off.data(), a->len.data(), a->node.data(), a->nodeOff.data(), a->toff.data(), a->cap.data() };
+    ga_extend_results r { a->status.data(), a->score.data(), a->tlen.data(), a->items.data(), a->steps.data() };
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = ga_extend_batch(a->ext, &a->params.extend, &b, &r);
+    a->stats.extend_ms += ms_since(t0);
+    for (size_t i = 0; i < n; i++)
+    {
+        if (rc != GA_OK)
+        {
+            rs[i].status = GA_CAPACITY;
+            continue;
+        }
+        rs[i].status = a->status[i];
+        rs[i].score = a->score[i];
+        rs[i].steps = a->steps[i];
+        rs[i].items.assign(a->items.begin() + a->toff[i], a->items.begin() + a->toff[i] + a->tlen[i]);
+    }
+}
+
+extern "C" int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* graph, const ga_align_params* params, ga_aligner_t* out)
+{
+    if (!ext || !graph || !params || !out) return GA_ERR_ARGUMENT;
+    if (params->minimizer_length == 0 || params->minimizer_length > 31 || params->minimizer_window < params->minimizer_length)
+    {
+        ga_set_last_error("ga_aligner_create: minimizer length must be 1..31 and at most the window size");
+        return GA_ERR_ARGUMENT;
+    }
+    ga_aligner* a = new ga_aligner();
+    a->ext = ext;
+    a->params = *params;
+    cudaGetDevice(&a->device);
+    try
+    {
+        a->graph = new gahost::HostGraph(*graph);
+        gahost::buildMinimizerIndex(*a->graph, params->minimizer_length, params->minimizer_window, 1.0 - params->minimizer_discard_fraction, a->index);
+    }
+    catch (...)
+    {
+        delete a->graph;
+        delete a;
+        ga_set_last_error("ga_aligner_create: the graph or its minimizer index is inconsistent");
+        return GA_ERR_ARGUMENT;
+    }
+    // open-addressing table of the distinct k-mers, uploaded once
+    uint64_t capacity = 16;
+    while (capacity < 2 * a->index.keys.size()) capacity <<= 1;
+    std::vector<gadev::SeedSlot> slots(capacity, gadev::SeedSlot { gadev::kEmptyKmer, 0, 0 });
+    for (size_t r = 0; r < a->index.keys.size(); r++)
+    {
+        uint64_t key = a->index.keys[r];
+        uint64_t h = gadev::seed_slot_hash(key) & (capacity - 1);
+        while (slots[h].key != gadev::kEmptyKmer) h = (h + 1) & (capacity - 1);
+        slots[h] = gadev::SeedSlot { key, (uint32_t)a->index.startPos[r], (uint32_t)(a->index.startPos[r + 1] - a->index.startPos[r]) };
+    }
+    if (cudaMalloc((void**)&a->slots, capacity * sizeof(gadev::SeedSlot)) != cudaSuccess
+        || cudaMemcpy(a->slots, slots.data(), capacity * sizeof(gadev::SeedSlot), cudaMemcpyHostToDevice) != cudaSuccess
+        || cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        if (a->slots) cudaFree(a->slots);
+        delete a->graph;
+        delete a;
+        ga_set_last_error("ga_aligner_create: uploading the seed table failed");
+        return GA_ERR_CUDA;
+    }
+    a->capacity = capacity;
+    *out = a;
+    return GA_OK;
+}
+
+extern "C" int ga_aligner_free(ga_aligner_t a)
+{
+    if (!a) return GA_OK;
+    if (a->slots) cudaFree(a->slots);
+    if (a->stream) cudaStreamDestroy(a->stream);
+    delete a->graph;
+    delete a;
+    return GA_OK;
+}
+
+extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* names, const uint8_t* seq, const uint64_t* seqOffset, const uint32_t* seqLen)
+{
+    if (!a || (n > 0 && (!names || !seq || !seqOffset || !seqLen))) return GA_ERR_ARGUMENT;
+    auto start = std::chrono::steady_clock::now();
+    a->stats = ga_align_stats {};
+    a->stats.reads = n;
+    a->gaf.clear();
+    a->readBp.assign(n, 0);
+    if (n == 0) return GA_OK;
+    // ---- k-mer lookups on the GPU ----
+    auto ts = std::chrono::steady_clock::now();
+    uint64_t seqBytes = 0, matchSlots = 0;
+    std::vector<uint64_t> matchOff(n);
+    for (uint32_t i = 0; i < n; i++)
+    {
+        seqBytes = std::max<uint64_t>(seqBytes, seqOffset[i] + seqLen[i]);
+        matchOff[i] = matchSlots;
+        matchSlots += seqLen[i];
+    }
+    uint8_t* dSeq = nullptr;
+    uint64_t *dOff = nullptr, *dMatchOff = nullptr;
+    uint32_t *dLen = nullptr, *dCount = nullptr;
+    gadev::SeedMatch* dMatch = nullptr;
+    auto release = [&]()
+    {
+        cudaFree(dSeq); cudaFree(dOff); cudaFree(dMatchOff); cudaFree(dLen); cudaFree(dCount); cudaFree(dMatch);
+    };
+    if (cudaMalloc((void**)&dSeq, std::max<uint64_t>(seqBytes, 1)) != cudaSuccess
+        || cudaMalloc((void**)&dOff, n * 8ULL) != cudaSuccess
+        || cudaMalloc((void**)&dMatchOff, n * 8ULL) != cudaSuccess
+        || cudaMalloc((void**)&dLen, n * 4ULL) != cudaSuccess
+        || cudaMalloc((void**)&dCount, n * 4ULL) != cudaSuccess
+        || cudaMalloc((void**)&dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch)) != cudaSuccess)
+    {
+        release();
+        ga_set_last_error("ga_align_reads: device buffers for seeding");
+        return GA_ERR_CUDA;
+    }
+    cudaMemcpyAsync(dSeq, seq, seqBytes, cudaMemcpyHostToDevice, a->stream);
+    cudaMemcpyAsync(dOff, seqOffset, n * 8ULL, cudaMemcpyHostToDevice, a->stream);
+    cudaMemcpyAsync(dMatchOff, matchOff.data(), n * 8ULL, cudaMemcpyHostToDevice, a->stream);
+    cudaMemcpyAsync(dLen, seqLen, n * 4ULL, cudaMemcpyHostToDevice, a->stream);
+    gadev::SeedTable table { a->slots, a->capacity, (uint32_t)std::min<uint64_t>(a->index.maxCount, 0xffffffffu) };
+    ga_launch_seed_lookup(table, a->params.minimizer_length, a->params.minimizer_window, n, dSeq, dOff, dLen, dMatchOff, dMatch, dCount, a->stream);
+    std::vector<uint32_t> counts(n);
+    std::vector<gadev::SeedMatch> matches(std::max<uint64_t>(matchSlots, 1));
+    cudaMemcpyAsync(counts.data(), dCount, n * 4ULL, cudaMemcpyDeviceToHost, a->stream);
+    cudaMemcpyAsync(matches.data(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
+    cudaError_t e = cudaStreamSynchronize(a->stream);
+    release();
+    if (e != cudaSuccess)
+    {
+        ga_set_last_error("ga_align_reads: seed lookup kernel failed");
+        return GA_ERR_CUDA;
+    }
+    std::vector<gahost::ReadInput> reads(n);
+    std::vector<gahost::KmerMatch> km;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        reads[i].name = names[i] ? names[i] : "";
+        reads[i].seq.assign((const char*)seq + seqOffset[i], seqLen[i]);
+        km.clear();
+        for (uint32_t k = 0; k < counts[i]; k++)
+        {
+            const auto& m = matches[matchOff[i] + k];
+            km.push_back(gahost::KmerMatch { m.pos, m.start, m.count });
+        }
+        gahost::selectSeeds(*a->graph, a->index, reads[i].seq, a->params.minimizer_density, km, reads[i].seeds);
+        if (!reads[i].seeds.empty()) a->stats.reads_with_seeds++;
+    }
+    a->stats.seed_ms = ms_since(ts);
+    // ---- seed loops, extensions on the GPU ----
+    gahost::ReadAlignParams rp;
+    rp.sloppy = a->params.sloppy != 0;
+    rp.minClusterSize = a->params.min_cluster_size;
+    rp.seedExtendDensity = a->params.seed_extend_density;
+    rp.xscoreErrorCost = a->params.extend.xscore_error_cost;
+    rp.minAlignmentScore = a->params.min_alignment_score;
+    rp.multimapScoreFraction = a->params.multimap_score_fraction;
+    rp.cigarMatchMismatchMerge = a->params.cigar_match_mismatch != 0;
+    std::vector<gahost::ReadOutput> outs;
+    gahost::BatchStats bs;
+    gahost::alignBatch(*a->graph, rp, reads, extend_callback, a, outs, bs);
+    for (uint32_t i = 0; i < n; i++)
+    {
+        a->gaf += outs[i].gaf;
+        a->readBp[i] = outs[i].bpAligned;
+        if (outs[i].alignments > 0) a->stats.reads_aligned++;
+    }
+    a->stats.failed_reads = bs.failedReads;
+    a->stats.bp_aligned = bs.bpAligned;
+    a->stats.rounds = bs.rounds;
+    a->stats.extensions = bs.extensions;
+    a->stats.cell_steps = bs.cellSteps;
+    a->stats.host_ms = ms_since(start) - a->stats.extend_ms;
+    return GA_OK;
+}
+
+extern "C" int ga_aligner_gaf(ga_aligner_t a, const char** text, uint64_t* bytes)
+{
+    if (!a || !text || !bytes) return GA_ERR_ARGUMENT;
+    *text = a->gaf.c_str();
+    *bytes = a->gaf.size();
+    return GA_OK;
+}
+
+extern "C" int ga_aligner_read_bp(ga_aligner_t a, uint64_t* bp)
+{
+    if (!a || !bp) return GA_ERR_ARGUMENT;
+    std::copy(a->readBp.begin(), a->readBp.end(), bp);
+    return GA_OK;
+}
+
+extern "C" int ga_aligner_stats(ga_aligner_t a, ga_align_stats* out)
+{
+    if (!a || !out) return GA_ERR_ARGUMENT;
+    *out = a->stats;
+    return GA_OK;
+}

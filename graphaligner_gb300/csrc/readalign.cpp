@@ -1,0 +1,893 @@
+// Read-level host layer of the GB300 extension path: the reference's per-read
+// alignment flow restated over batched GPU extensions.
+//
+// For every read of a batch this follows runComponentMappings' GAF path
+// (Aligner.cpp:440-592): minimizer seeds (MinimizerSeeder::getSeeds, with the
+// k-mer lookup done by the seed_lookup kernel) -> OrderSeeds
+// (GraphAligner::orderSeedsByChaining, GraphAligner.h:250-312) -> the seed loop of
+// GraphAligner::AlignOneWay (GraphAligner.h:94-181) -> SelectAlignments
+// (AlignmentSelection.cpp:31-53) -> GAF lines (GraphAlignerGAFAlignment.h:37-200).
+// The seed loop is sequential per read because its skip rules read the traces
+// of earlier seeds; reads advance in lock step instead: every round collects the
+// two extensions (GraphAligner::getTwoDirectionalTrace, GraphAligner.h:475-520)
+// of each read's next seed and runs them as one ga_extend_batch call.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+#include "../../include/graphaligner_gb300.h"
+#include "readalign.h"
+
+namespace gahost
+{
+
+struct ReadFailure {};
+#define GAH_ASSERT(x) do { if (!(x)) throw ::gahost::ReadFailure{}; } while (0)
+
+// ------------------------------------------------------------------ graph
+
+int iupac(char c)
+{
+    switch (c)
+    {
+        case 'A': case 'a': return 1;
+        case 'C': case 'c': return 2;
+        case 'G': case 'g': return 4;
+        case 'T': case 't': case 'U': case 'u': return 8;
+        case 'R': case 'r': return 5;
+        case 'Y': case 'y': return 10;
+        case 'K': case 'k': return 12;
+        case 'M': case 'm': return 3;
+        case 'S': case 's': return 6;
+        case 'W': case 'w': return 9;
+        case 'B': case 'b': return 14;
+        case 'D': case 'd': return 13;
+        case 'H': case 'h': return 11;
+        case 'V': case 'v': return 7;
+        case 'N': case 'n': return 15;
+        case '-': return 0;
+    }
+    return -1;
+}
+
+// GraphAlignerCommon::characterMatch (GraphAlignerCommon.h:176-200)
+bool characterMatch(char s, char g)
+{
+    if (s == g) return true;
+    int a = iupac(s), b = iupac(g);
+    GAH_ASSERT(a >= 0 && b >= 0);
+    return (a & b) != 0;
+}
+
+// CommonUtils::Complement (CommonUtils.cpp:78-134)
+char complement(char c)
+{
+    switch (c)
+    {
+        case 'A': case 'a': return 'T';
+        case 'C': case 'c': return 'G';
+        case 'T': case 't': return 'A';
+        case 'G': case 'g': return 'C';
+        case 'N': case 'n': return 'N';
+        case 'U': case 'u': return 'A';
+        case 'R': case 'r': return 'Y';
+        case 'Y': case 'y': return 'R';
+        case 'K': case 'k': return 'M';
+        case 'M': case 'm': return 'K';
+        case 'S': case 's': return 'S';
+        case 'W': case 'w': return 'W';
+        case 'B': case 'b': return 'V';
+        case 'V': case 'v': return 'B';
+        case 'D': case 'd': return 'H';
+        case 'H': case 'h': return 'D';
+    }
+    GAH_ASSERT(false);
+    return 'N';
+}
+
+std::string reverseComplement(const std::string& s)
+{
+    std::string r;
+    r.reserve(s.size());
+    for (size_t i = s.size(); i > 0; i--) r += complement(s[i - 1]);
+    return r;
+}
+
+HostGraph::HostGraph(const ga_host_graph_desc& d) :
+    N(d.base.num_nodes), firstAmbiguous(d.base.first_ambiguous)
+{
+    len.assign(d.base.node_length, d.base.node_length + N);
+    seq2.assign(d.base.seq2bit, d.base.seq2bit + (size_t)firstAmbiguous * 2);
+    seqAmb.assign(d.base.seq_ambiguous, d.base.seq_ambiguous + (size_t)(N - firstAmbiguous) * 4);
+    inOff.assign(d.base.in_offsets, d.base.in_offsets + N + 1);
+    inNb.assign(d.base.in_neighbors, d.base.in_neighbors + inOff[N]);
+    outOff.assign(d.base.out_offsets, d.base.out_offsets + N + 1);
+    outNb.assign(d.base.out_neighbors, d.base.out_neighbors + outOff[N]);
+    nodeIds.assign(d.node_ids, d.node_ids + N);
+    nodeOffset.assign(d.node_offset, d.node_offset + N);
+    reverse.assign(d.reverse, d.reverse + N);
+    chainNumber.assign(d.chain_number, d.chain_number + N);
+    chainApproxPos.assign(d.chain_approx_pos, d.chain_approx_pos + N);
+    lookupIds.assign(d.lookup_ids, d.lookup_ids + d.num_lookup);
+    originalSize.assign(d.original_size, d.original_size + d.num_lookup);
+    lookupOff.assign(d.lookup_offsets, d.lookup_offsets + d.num_lookup + 1);
+    lookupNodes.assign(d.lookup_nodes, d.lookup_nodes + lookupOff[d.num_lookup]);
+    names.resize(d.num_lookup);
+    for (size_t i = 0; i < d.num_lookup; i++)
+    {
+        if (d.names && d.names[i]) names[i] = d.names[i];
+        lookupIndex[lookupIds[i]] = i;
+    }
+    bpSize = 0;
+    for (uint32_t i = 0; i < N; i++) bpSize += len[i];
+}
+
+size_t HostGraph::lookup(int bignode) const
+{
+    auto f = lookupIndex.find(bignode);
+    GAH_ASSERT(f != lookupIndex.end());
+    return f->second;
+}
+
+char HostGraph::charAt(size_t node, size_t pos) const
+{
+    GAH_ASSERT(node < N && pos < len[node]);
+    if (node < firstAmbiguous)
+    {
+        uint64_t c = seq2[node * 2 + pos / 32];
+        return "ACGT"[(c >> ((pos % 32) * 2)) & 3];
+    }
+    const uint64_t* a = &seqAmb[(node - firstAmbiguous) * 4];
+    int m = 0;
+    for (int k = 0; k < 4; k++) if ((a[k] >> pos) & 1) m |= 1 << k;
+    static const char table[16] = { '?', 'A', 'C', 'M', 'G', 'R', 'S', 'V', 'T', 'W', 'Y', 'H', 'K', 'D', 'B', 'N' };
+    return table[m];
+}
+
+// AlignmentGraph::GetUnitigNode (AlignmentGraph.cpp:812-828): the piece of the
+// bigraph node that contains offset
+size_t HostGraph::unitigNode(int bignode, size_t offset) const
+{
+    size_t i = lookup(bignode);
+    GAH_ASSERT(offset < originalSize[i]);
+    size_t lo = lookupOff[i], hi = lookupOff[i + 1];
+    for (size_t k = lo; k < hi; k++)
+    {
+        size_t n = lookupNodes[k];
+        if (nodeOffset[n] <= offset && nodeOffset[n] + len[n] > offset) return n;
+    }
+    GAH_ASSERT(false);
+    return 0;
+}
+
+// AlignmentGraph::GetReversePosition (AlignmentGraph.cpp:830-847)
+std::pair<int, size_t> HostGraph::reversePosition(int bignode, size_t offset) const
+{
+    size_t size = originalSize[lookup(bignode)];
+    GAH_ASSERT(offset < size);
+    int rev = (bignode % 2 == 0) ? (bignode / 2) * 2 + 1 : (bignode / 2) * 2;
+    return { rev, size - offset - 1 };
+}
+
+size_t HostGraph::sizeOf(int bignode) const { return originalSize[lookup(bignode)]; }
+const std::string& HostGraph::nameOf(int bignode) const { return names[lookup(bignode)]; }
+
+// ------------------------------------------------------------------ seeds
+
+// GraphAligner::orderSeedsByChaining (GraphAligner.h:250-312)
+void orderSeeds(const HostGraph& g, std::vector<SeedHit>& seedHits)
+{
+    std::vector<size_t> chainOrder;
+    std::unordered_map<size_t, std::vector<std::pair<size_t, size_t>>> seedPoses;
+    for (size_t i = 0; i < seedHits.size(); i++)
+    {
+        int forwardNodeId = seedHits[i].reverse ? seedHits[i].nodeID * 2 + 1 : seedHits[i].nodeID * 2;
+        size_t nodeIndex, realOffset;
+        if (seedHits[i].alignmentGraphNodeId == std::numeric_limits<size_t>::max())
+        {
+            nodeIndex = g.unitigNode(forwardNodeId, seedHits[i].nodeOffset);
+            GAH_ASSERT(seedHits[i].nodeOffset >= g.nodeOffset[nodeIndex]);
+            realOffset = seedHits[i].nodeOffset - g.nodeOffset[nodeIndex];
+        }
+        else
+        {
+            nodeIndex = seedHits[i].alignmentGraphNodeId;
+            realOffset = seedHits[i].alignmentGraphNodeOffset;
+        }
+        GAH_ASSERT(g.chainApproxPos[nodeIndex] + realOffset >= seedHits[i].seqPos);
+        size_t chain = g.chainNumber[nodeIndex];
+        auto found = seedPoses.find(chain);
+        if (found == seedPoses.end())
+        {
+            chainOrder.push_back(chain);
+            found = seedPoses.emplace(chain, std::vector<std::pair<size_t, size_t>>{}).first;
+        }
+        found->second.emplace_back(i, g.chainApproxPos[nodeIndex] + realOffset - seedHits[i].seqPos);
+    }
+    for (size_t chain : chainOrder)
+    {
+        auto& list = seedPoses[chain];
+        std::sort(list.begin(), list.end(), [](std::pair<size_t, size_t> a, std::pair<size_t, size_t> b) { return a.second < b.second; });
+        size_t clusterStart = 0;
+        for (size_t i = 1; i <= list.size(); i++)
+        {
+            if (i < list.size() && list[i].second <= list[i - 1].second + 100) continue;
+            std::sort(list.begin() + clusterStart, list.begin() + i, [&seedHits](std::pair<size_t, size_t> a, std::pair<size_t, size_t> b) { return seedHits[a.first].seqPos < seedHits[b.first].seqPos; });
+            size_t matchingBps = 0;
+            int lastEnd = std::numeric_limits<int>::min();
+            for (size_t j = clusterStart; j < i; j++)
+            {
+                int thisStart = (int)seedHits[list[j].first].seqPos - (int)seedHits[list[j].first].matchLen + 1;
+                int thisEnd = (int)seedHits[list[j].first].seqPos;
+                GAH_ASSERT(thisEnd >= lastEnd);
+                GAH_ASSERT(thisEnd > thisStart);
+                matchingBps += (thisEnd - std::max(thisStart, lastEnd));
+                lastEnd = thisEnd;
+            }
+            for (size_t j = clusterStart; j < i; j++)
+            {
+                seedHits[list[j].first].seedGoodness = matchingBps + seedHits[list[j].first].rawSeedGoodness;
+                seedHits[list[j].first].seedClusterSize = i - clusterStart;
+            }
+            clusterStart = i;
+        }
+    }
+    std::sort(seedHits.begin(), seedHits.end(), [](const SeedHit& a, const SeedHit& b) { return a.seedGoodness < b.seedGoodness; });
+    std::reverse(seedHits.begin(), seedHits.end());
+}
+
+// ------------------------------------------------------------------ traces
+
+// GraphAligner::fixForwardTraceSeqPos (GraphAligner.h:522-559)
+void fixForwardTraceSeqPos(const HostGraph& g, OnewayTrace& trace, size_t start, const std::string& sequence)
+{
+    if (trace.trace.size() == 0) return;
+    trace.score = 0;
+    for (size_t i = 0; i < trace.trace.size(); i++)
+    {
+        auto& t = trace.trace[i];
+        t.seqPos += start;
+        size_t nodeIndex = t.node;
+        t.node = g.nodeIds[nodeIndex];
+        t.nodeOffset += g.nodeOffset[nodeIndex];
+        GAH_ASSERT(t.seqPos < sequence.size());
+        if (t.seqPos == start - 1)
+        {
+            GAH_ASSERT(t.seqChar == '-');
+            t.seqChar = sequence[t.seqPos];
+        }
+        GAH_ASSERT(t.seqChar == sequence[t.seqPos]);
+        if (i == 0 && !characterMatch(t.seqChar, t.graphChar)) trace.score += 1;
+        if (i > 0)
+        {
+            const auto& p = trace.trace[i - 1];
+            if (t.seqPos == p.seqPos) trace.score += 1;
+            else if (!p.nodeSwitch && t.node == p.node && t.nodeOffset == p.nodeOffset) trace.score += 1;
+            else if (!characterMatch(t.seqChar, t.graphChar)) trace.score += 1;
+        }
+    }
+}
+
+// GraphAligner::fixReverseTraceSeqPosAndOrder (GraphAligner.h:562-601)
+void fixReverseTraceSeqPosAndOrder(const HostGraph& g, OnewayTrace& trace, size_t end, const std::string& sequence)
+{
+    if (trace.trace.size() == 0) return;
+    std::reverse(trace.trace.begin(), trace.trace.end());
+    trace.score = 0;
+    for (size_t i = 0; i + 1 < trace.trace.size(); i++) trace.trace[i].nodeSwitch = trace.trace[i + 1].nodeSwitch;
+    trace.trace.back().nodeSwitch = false;
+    for (size_t i = 0; i < trace.trace.size(); i++)
+    {
+        auto& t = trace.trace[i];
+        GAH_ASSERT(t.seqPos <= end || t.seqPos == (size_t)-1);
+        t.seqPos = end - t.seqPos;
+        size_t offset = g.nodeOffset[t.node] + t.nodeOffset;
+        auto rp = g.reversePosition(g.nodeIds[t.node], offset);
+        t.node = rp.first;
+        t.nodeOffset = rp.second;
+        GAH_ASSERT(t.seqPos < sequence.size());
+        t.seqChar = sequence[t.seqPos];
+        t.graphChar = complement(t.graphChar);
+        if (i == 0 && !characterMatch(t.seqChar, t.graphChar)) trace.score += 1;
+        if (i > 0)
+        {
+            const auto& p = trace.trace[i - 1];
+            if (t.seqPos == p.seqPos) trace.score += 1;
+            else if (!p.nodeSwitch && t.node == p.node && t.nodeOffset == p.nodeOffset) trace.score += 1;
+            else if (!characterMatch(t.seqChar, t.graphChar)) trace.score += 1;
+        }
+    }
+}
+
+// GraphAligner::exactAlignmentPart (GraphAligner.h:403-457)
+bool exactAlignmentPart(const AlignmentItem& aln, const SeedHit& seedHit)
+{
+    const auto& trace = aln.trace->trace;
+    GAH_ASSERT(trace.size() > 0);
+    GAH_ASSERT(trace.back().seqPos > trace[0].seqPos);
+    if (trace.back().seqPos < seedHit.seqPos) return false;
+    if (trace[0].seqPos > seedHit.seqPos) return false;
+    size_t high = trace.size();
+    size_t low = 0;
+    size_t mid = (seedHit.seqPos - trace[0].seqPos) / (trace.back().seqPos - trace[0].seqPos);
+    while (trace[mid].seqPos != seedHit.seqPos)
+    {
+        if (trace[mid].seqPos < seedHit.seqPos)
+        {
+            low = mid;
+            mid = (high + low) / 2;
+            if (mid == low) mid += 1;
+            GAH_ASSERT(mid < trace.size());
+        }
+        if (trace[mid].seqPos > seedHit.seqPos)
+        {
+            high = mid;
+            mid = (high + low) / 2;
+            GAH_ASSERT(mid < trace.size());
+        }
+        GAH_ASSERT(low < mid);
+        GAH_ASSERT(mid < high);
+    }
+    size_t down = mid;
+    size_t compareNode = seedHit.nodeID * 2;
+    if (seedHit.reverse) compareNode += 1;
+    while (trace[down].seqPos == seedHit.seqPos)
+    {
+        if (compareNode == trace[down].node && seedHit.nodeOffset == trace[down].nodeOffset) return true;
+        if (down == 0) break;
+        down -= 1;
+    }
+    size_t up = mid;
+    while (trace[up].seqPos == seedHit.seqPos)
+    {
+        if (compareNode == trace[up].node && seedHit.nodeOffset == trace[up].nodeOffset) return true;
+        up += 1;
+        if (up == trace.size()) break;
+    }
+    return false;
+}
+
+// ------------------------------------------------------------------ selection, GAF
+
+// AlignmentSelection::alignmentIncompatible (AlignmentSelection.cpp:13-29)
+static bool alignmentIncompatible(const AlignmentItem& l, const AlignmentItem& r)
+{
+    const float OverlapIncompatibleFractionCutoff = 0.05;
+    auto minOverlapLen = std::min((l.alignmentEnd - l.alignmentStart), (r.alignmentEnd - r.alignmentStart)) * OverlapIncompatibleFractionCutoff;
+    size_t leftStart = l.alignmentStart, leftEnd = l.alignmentEnd, rightStart = r.alignmentStart, rightEnd = r.alignmentEnd;
+    if (leftStart > rightStart)
+    {
+        std::swap(leftStart, rightStart);
+        std::swap(leftEnd, rightEnd);
+    }
+    int overlap = 0;
+    if (leftEnd > rightStart) overlap = leftEnd - rightStart;
+    return overlap > minOverlapLen;
+}
+
+// AlignmentSelection::SelectAlignments (AlignmentSelection.cpp:31-95) without the E-value filter
+std::vector<AlignmentItem> selectAlignments(const std::vector<AlignmentItem>& all, int minAlignmentScore, double fractionCutoff)
+{
+    std::vector<AlignmentItem> filtered;
+    bool wasFiltered = false;
+    if (minAlignmentScore > std::numeric_limits<int>::min())
+    {
+        std::vector<AlignmentItem> r;
+        for (const auto& a : all) if (a.alignmentXScore >= (double)minAlignmentScore) r.push_back(a);
+        filtered = r;
+        wasFiltered = true;
+    }
+    if (fractionCutoff != 0)
+    {
+        const std::vector<AlignmentItem>& in = wasFiltered ? filtered : all;
+        std::vector<AlignmentItem> r;
+        for (size_t i = 0; i < in.size(); i++)
+        {
+            bool skipped = false;
+            for (size_t j = 0; j < in.size(); j++)
+            {
+                if (i == j) continue;
+                if (!alignmentIncompatible(in[i], in[j])) continue;
+                if (in[i].alignmentXScore < in[j].alignmentXScore * fractionCutoff)
+                {
+                    skipped = true;
+                    break;
+                }
+            }
+            if (!skipped) r.push_back(in[i]);
+        }
+        filtered = r;
+        wasFiltered = true;
+    }
+    return wasFiltered ? filtered : all;
+}
+
+static void addPos(std::stringstream& s, int nodeId, bool reverse, const HostGraph& g)
+{
+    s << (reverse ? "<" : ">");
+    const std::string& name = g.nameOf(nodeId);
+    if (name == "") s << nodeId / 2;
+    else s << name;
+}
+
+// GraphAlignerGAFAlignment::addCigarItem (GraphAlignerGAFAlignment.h:225-250)
+static void addCigarItem(std::stringstream& s, size_t editLength, int type)
+{
+    if (editLength == 0) return;
+    static const char codes[] = { '=', 'X', 'M', 'I', 'D' };
+    s << editLength;
+    if (type >= 0 && type <= 4) s << codes[type];
+}
+
+// GraphAlignerGAFAlignment::traceToAlignment (GraphAlignerGAFAlignment.h:37-200)
+std::string gafLine(const HostGraph& g, const std::string& readName, const std::string& sequence, const OnewayTrace& t,
+    double alignmentXScore, int mappingQuality, bool cigarMatchMismatchMerge)
+{
+    enum { Match = 0, Mismatch = 1, MatchOrMismatch = 2, Insertion = 3, Deletion = 4, Empty = 5 };
+    const auto& trace = t.trace;
+    GAH_ASSERT(trace.size() > 0);
+    std::stringstream cigar;
+    size_t readLen = sequence.size();
+    size_t readStart = trace[0].seqPos;
+    size_t readEnd = trace.back().seqPos + 1;
+    std::stringstream nodePath;
+    size_t nodePathLen = 0;
+    size_t nodePathStart = trace[0].nodeOffset;
+    size_t nodePathEnd = 0;
+    size_t matches = 0, mismatches = 0, deletions = 0, insertions = 0, editLength = 0;
+    size_t blockLength = trace.size();
+    int curNode = (int)trace[0].node;
+    bool curRev = (trace[0].node % 2) == 1;
+    size_t curOffset = trace[0].nodeOffset;
+    size_t curSeq = trace[0].seqPos;
+    int currentEdit = Empty;
+    if (cigarMatchMismatchMerge)
+    {
+        currentEdit = MatchOrMismatch;
+        editLength = 1;
+        if (characterMatch(trace[0].seqChar, trace[0].graphChar)) matches++; else mismatches++;
+    }
+    else if (characterMatch(trace[0].seqChar, trace[0].graphChar))
+    {
+        currentEdit = Match;
+        editLength = 1;
+        matches++;
+    }
+    else
+    {
+        currentEdit = Mismatch;
+        editLength = 1;
+        mismatches++;
+    }
+    addPos(nodePath, curNode, curRev, g);
+    nodePathLen += g.sizeOf(curNode);
+    for (size_t pos = 1; pos < trace.size(); pos++)
+    {
+        GAH_ASSERT(trace[pos].seqPos < sequence.size());
+        int newNode = (int)trace[pos].node;
+        bool newRev = (trace[pos].node % 2) == 1;
+        size_t newOffset = trace[pos].nodeOffset;
+        size_t newSeq = trace[pos].seqPos;
+        bool insideNode = !trace[pos - 1].nodeSwitch || (newNode == curNode && newRev == curRev && newOffset > curOffset);
+        GAH_ASSERT(newSeq >= curSeq);
+        if (!insideNode)
+        {
+            size_t skippedBefore = g.sizeOf(curNode) - 1 - trace[pos - 1].nodeOffset;
+            curNode = newNode;
+            curRev = newRev;
+            curOffset = newOffset;
+            curSeq = newSeq;
+            addPos(nodePath, curNode, curRev, g);
+            GAH_ASSERT(trace[pos].nodeOffset < g.sizeOf(curNode));
+            size_t skippedAfter = trace[pos].nodeOffset;
+            nodePathLen += g.sizeOf(curNode) - (skippedBefore + skippedAfter);
+        }
+        auto step = [&](int type)
+        {
+            if (currentEdit == Empty) currentEdit = type;
+            if (currentEdit != type)
+            {
+                addCigarItem(cigar, editLength, currentEdit);
+                currentEdit = type;
+                editLength = 0;
+            }
+            editLength += 1;
+        };
+        if (trace[pos - 1].seqPos == trace[pos].seqPos)
+        {
+            step(Deletion);
+            deletions++;
+        }
+        else if (insideNode && trace[pos - 1].nodeOffset == trace[pos].nodeOffset)
+        {
+            step(Insertion);
+            insertions++;
+        }
+        else if (cigarMatchMismatchMerge)
+        {
+            step(MatchOrMismatch);
+            if (characterMatch(trace[pos].seqChar, trace[pos].graphChar)) matches++; else mismatches++;
+        }
+        else if (characterMatch(trace[pos].seqChar, trace[pos].graphChar))
+        {
+            step(Match);
+            matches++;
+        }
+        else
+        {
+            step(Mismatch);
+            mismatches++;
+        }
+    }
+    GAH_ASSERT(matches + mismatches + deletions + insertions == trace.size());
+    addCigarItem(cigar, editLength, currentEdit);
+    nodePathEnd = nodePathLen - (g.sizeOf((int)trace.back().node) - 1 - trace.back().nodeOffset);
+    std::stringstream s;
+    s << readName << "\t" << readLen << "\t" << readStart << "\t" << readEnd << "\t" << "+" << "\t" << nodePath.str() << "\t" << nodePathLen << "\t" << nodePathStart << "\t" << nodePathEnd << "\t" << matches << "\t" << blockLength << "\t" << mappingQuality;
+    s << "\t" << "NM:i:" << (mismatches + deletions + insertions);
+    if (alignmentXScore != -1) s << "\t" << "AS:f:" << alignmentXScore;
+    s << "\t" << "dv:f:" << 1.0 - ((double)matches / (double)(matches + mismatches + deletions + insertions));
+    s << "\t" << "id:f:" << ((double)matches / (double)(matches + mismatches + deletions + insertions));
+    s << "\t" << "cg:Z:" << cigar.str();
+    return s.str();
+}
+
+// ------------------------------------------------------------------ the batched seed loop
+
+struct PendingExtension
+{
+    size_t read;
+    size_t seed;
+    int64_t backward = -1;  // batch index or -1
+    int64_t forward = -1;
+};
+
+struct ReadState
+{
+    std::string name;
+    std::string seq;
+    std::string rev;
+    std::vector<SeedHit> seeds;
+    size_t next = 0;
+    size_t extendSeeds = 0;
+    size_t seedScoreForEndToEndAln = 0;
+    size_t worstExtendedSeedScore = 0;
+    size_t seedsExtended = 0;
+    std::vector<AlignmentItem> alignments;
+    bool done = false;
+    bool failed = false;
+};
+
+// advances a read's seed loop (GraphAligner.h:105-154) to the next seed that needs an
+// extension; returns false when the loop ends
+static bool nextSeed(const ReadAlignParams& p, ReadState& r, size_t& seedIndex)
+{
+    while (r.next < r.seeds.size())
+    {
+        const size_t i = r.next;
+        const SeedHit& s = r.seeds[i];
+        if (p.sloppy && (s.seedGoodness == r.seedScoreForEndToEndAln || s.seedGoodness < r.seedScoreForEndToEndAln)) return false;
+        if (r.seedsExtended >= r.extendSeeds && s.seedGoodness < r.worstExtendedSeedScore) return false;
+        r.next++;
+        if (s.seedClusterSize < p.minClusterSize) continue;
+        if (p.sloppy)
+        {
+            bool found = false;
+            for (const auto& aln : r.alignments)
+            {
+                if (aln.alignmentStart <= s.seqPos && aln.alignmentEnd >= s.seqPos && aln.seedGoodness > s.seedGoodness)
+                {
+                    found = true;
+                    break;
+                }
+            }
+            if (found) continue;
+        }
+        bool found = false;
+        for (const auto& aln : r.alignments)
+        {
+            if (exactAlignmentPart(aln, s))
+            {
+                found = true;
+                break;
+            }
+        }
+        if (found) continue;
+        r.worstExtendedSeedScore = s.seedGoodness;
+        r.seedsExtended += 1;
+        seedIndex = i;
+        return true;
+    }
+    return false;
+}
+
+static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, const std::string& seqView)
+{
+    OnewayTrace t;
+    if (e.status == GA_TRACE_FAILED)
+    {
+        t.score = INT32_MAX;
+        return t;
+    }
+    GAH_ASSERT(e.status == GA_OK);
+    t.score = e.score;
+    t.trace.reserve(e.items.size());
+    for (uint64_t x : e.items)
+    {
+        TraceItem it;
+        it.node = GA_TRACE_NODE(x);
+        it.nodeOffset = GA_TRACE_OFFSET(x);
+        uint64_t sp1 = GA_TRACE_SEQPOS1(x);
+        it.seqPos = sp1 == 0 ? (size_t)-1 : (size_t)(sp1 - 1);
+        it.nodeSwitch = GA_TRACE_SWITCH(x) != 0;
+        it.seqChar = it.seqPos < seqView.size() ? seqView[it.seqPos] : '-';
+        it.graphChar = g.charAt(it.node, it.nodeOffset);
+        t.trace.push_back(it);
+    }
+    return t;
+}
+
+// GraphAligner::getAlignmentFromSeed (GraphAligner.h:631-692) after the two extensions ran
+static void finishSeed(const HostGraph& g, const ReadAlignParams& p, ReadState& r, const SeedHit& seedHit,
+    OnewayTrace backward, OnewayTrace forward, int backwardNodeId, int forwardNodeId)
+{
+    // getTwoDirectionalTrace (GraphAligner.h:508-518): both traces to read order
+    if (!backward.failed())
+    {
+        auto rp = g.reversePosition(forwardNodeId, seedHit.nodeOffset);
+        const auto& b = backward.trace.back();
+        GAH_ASSERT(b.seqPos == (size_t)-1 && g.nodeIds[b.node] == backwardNodeId && g.nodeOffset[b.node] + b.nodeOffset == rp.second);
+        std::reverse(backward.trace.begin(), backward.trace.end());
+    }
+    if (!forward.failed())
+    {
+        const auto& b = forward.trace.back();
+        GAH_ASSERT(b.seqPos == (size_t)-1 && g.nodeIds[b.node] == forwardNodeId && g.nodeOffset[b.node] + b.nodeOffset == seedHit.nodeOffset);
+        std::reverse(forward.trace.begin(), forward.trace.end());
+    }
+    fixReverseTraceSeqPosAndOrder(g, backward, seedHit.seqPos - 1, r.seq);
+    fixForwardTraceSeqPos(g, forward, seedHit.seqPos + 1, r.seq);
+    if (forward.failed() && backward.failed()) return;
+    GAH_ASSERT(backward.trace.size() > 0 || backward.failed());
+    OnewayTrace merged = std::move(backward);
+    if (merged.failed())
+    {
+        merged = std::move(forward);
+    }
+    else if (!forward.failed())
+    {
+        GAH_ASSERT(merged.trace.size() > 0);
+        const auto& a = merged.trace.back();
+        const auto& b = forward.trace[0];
+        GAH_ASSERT(a.node == b.node && a.nodeOffset == b.nodeOffset && a.seqPos == b.seqPos);
+        merged.trace.pop_back();
+        merged.trace.insert(merged.trace.end(), forward.trace.begin(), forward.trace.end());
+        merged.score += forward.score;
+    }
+    AlignmentItem item;
+    item.trace = std::make_shared<OnewayTrace>(std::move(merged));
+    GAH_ASSERT(item.trace->trace.size() > 0);
+    item.alignmentScore = item.trace->score;
+    item.alignmentStart = item.trace->trace[0].seqPos;
+    item.alignmentEnd = item.trace->trace.back().seqPos + 1;
+    GAH_ASSERT(item.alignmentEnd - 1 < r.seq.size());
+    item.alignmentXScore = (int32_t)(item.alignmentEnd - item.alignmentStart) * 100 - p.xscoreErrorCost * (int32_t)item.alignmentScore;
+    item.alignmentXScore /= 100.0;
+    if (item.alignmentEnd == item.alignmentStart) return;
+    item.seedGoodness = seedHit.seedGoodness;
+    r.alignments.push_back(item);
+    if (p.sloppy)
+    {
+        std::sort(r.alignments.begin(), r.alignments.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentStart < b.alignmentStart; });
+        if (r.alignments[0].alignmentStart == 0)
+        {
+            size_t minSeedGoodness = r.alignments[0].seedGoodness;
+            size_t contiguousEnd = r.alignments[0].alignmentEnd;
+            for (size_t i = 1; i < r.alignments.size(); i++)
+            {
+                if (r.alignments[i].alignmentStart <= contiguousEnd)
+                {
+                    minSeedGoodness = std::min(minSeedGoodness, r.alignments[i].seedGoodness);
+                    contiguousEnd = std::max(contiguousEnd, r.alignments[i].alignmentEnd);
+                }
+            }
+            if (contiguousEnd == r.seq.size()) r.seedScoreForEndToEndAln = minSeedGoodness;
+        }
+    }
+}
+
+void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,
+    std::vector<ReadOutput>& out, BatchStats& stats)
+{
+    std::vector<ReadState> st(reads.size());
+    out.assign(reads.size(), ReadOutput {});
+    for (size_t i = 0; i < reads.size(); i++)
+    {
+        st[i].name = reads[i].name;
+        st[i].seq = reads[i].seq;
+        st[i].seeds = std::move(reads[i].seeds);
+        if (st[i].seeds.size() == 0)
+        {
+            st[i].done = true;
+            out[i].noSeeds = true;
+            continue;
+        }
+        try
+        {
+            orderSeeds(g, st[i].seeds);
+            st[i].rev = reverseComplement(st[i].seq);
+        }
+        catch (const ReadFailure&)
+        {
+            st[i].done = true;
+            st[i].failed = true;
+        }
+        st[i].extendSeeds = (size_t)(p.seedExtendDensity * st[i].seq.size() + 1);
+        if (p.seedExtendDensity == -1) st[i].extendSeeds = st[i].seeds.size();
+    }
+    std::vector<PendingExtension> pending;
+    std::vector<ExtensionRequest> requests;
+    std::vector<ExtensionResult> results;
+    while (true)
+    {
+        pending.clear();
+        requests.clear();
+        for (size_t i = 0; i < st.size(); i++)
+        {
+            ReadState& r = st[i];
+            if (r.done) continue;
+            size_t seedIndex = 0;
+            bool more;
+            try
+            {
+                more = nextSeed(p, r, seedIndex);
+            }
+            catch (const ReadFailure&)
+            {
+                r.failed = true;
+                r.done = true;
+                continue;
+            }
+            if (!more)
+            {
+                r.done = true;
+                continue;
+            }
+            const SeedHit& s = r.seeds[seedIndex];
+            PendingExtension pe;
+            pe.read = i;
+            pe.seed = seedIndex;
+            int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
+            try
+            {
+                GAH_ASSERT(s.seqPos < r.seq.size());
+                if (s.seqPos > 0)
+                {
+                    auto rp = g.reversePosition(forwardNodeId, s.nodeOffset);
+                    ExtensionRequest q;
+                    q.seq = r.rev.data() + r.rev.size() - s.seqPos;
+                    q.len = s.seqPos;
+                    q.bignode = rp.first;
+                    q.offset = rp.second;
+                    size_t node = g.unitigNode(q.bignode, q.offset);
+                    q.node = (uint32_t)node;
+                    q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
+                    pe.backward = (int64_t)requests.size();
+                    requests.push_back(q);
+                }
+                if (s.seqPos < r.seq.size() - 1)
+                {
+                    ExtensionRequest q;
+                    q.seq = r.seq.data() + s.seqPos + 1;
+                    q.len = r.seq.size() - s.seqPos - 1;
+                    q.bignode = forwardNodeId;
+                    q.offset = s.nodeOffset;
+                    size_t node = g.unitigNode(q.bignode, q.offset);
+                    q.node = (uint32_t)node;
+                    q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
+                    pe.forward = (int64_t)requests.size();
+                    requests.push_back(q);
+                }
+            }
+            catch (const ReadFailure&)
+            {
+                r.failed = true;
+                r.done = true;
+                continue;
+            }
+            pending.push_back(pe);
+        }
+        if (pending.empty()) break;
+        stats.rounds++;
+        stats.extensions += requests.size();
+        results.assign(requests.size(), ExtensionResult {});
+        if (!requests.empty()) extend(ctx, requests, results);
+        for (const auto& pe : pending)
+        {
+            ReadState& r = st[pe.read];
+            const SeedHit& s = r.seeds[pe.seed];
+            int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
+            int backwardNodeId = s.reverse ? s.nodeID * 2 : s.nodeID * 2 + 1;
+            try
+            {
+                for (int64_t k : { pe.backward, pe.forward })
+                {
+                    if (k >= 0)
+                    {
+                        stats.cellSteps += results[k].steps;
+                        if (results[k].status == GA_ASSERT || results[k].status == GA_CAPACITY || results[k].status == GA_BAD_REQUEST) throw ReadFailure {};
+                    }
+                }
+                OnewayTrace bw, fw;
+                bw.score = INT32_MAX;
+                fw.score = INT32_MAX;
+                if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], std::string(requests[pe.backward].seq, requests[pe.backward].len));
+                if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], std::string(requests[pe.forward].seq, requests[pe.forward].len));
+                finishSeed(g, p, r, s, std::move(bw), std::move(fw), backwardNodeId, forwardNodeId);
+            }
+            catch (const ReadFailure&)
+            {
+                r.failed = true;
+                r.done = true;
+            }
+        }
+    }
+    // Aligner.cpp:505-566: selection, bp aligned, order, GAF
+    for (size_t i = 0; i < st.size(); i++)
+    {
+        ReadState& r = st[i];
+        ReadOutput& o = out[i];
+        if (r.failed)
+        {
+            o.failed = true;
+            stats.failedReads++;
+            continue;
+        }
+        if (r.alignments.empty()) continue;
+        try
+        {
+            std::vector<AlignmentItem> alns = selectAlignments(r.alignments, p.minAlignmentScore, p.multimapScoreFraction);
+            if (alns.empty()) continue;
+            std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentStart < b.alignmentStart; });
+            size_t bpAligned = 0, lastEnd = 0;
+            for (const auto& a : alns)
+            {
+                size_t countStart = std::max(lastEnd, a.alignmentStart);
+                if (a.alignmentEnd > countStart)
+                {
+                    bpAligned += a.alignmentEnd - countStart;
+                    lastEnd = a.alignmentEnd;
+                }
+            }
+            std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentXScore > b.alignmentXScore; });
+            std::string text;
+            for (auto& a : alns)
+            {
+                text += gafLine(g, r.name, r.seq, *a.trace, a.alignmentXScore, a.mappingQuality, p.cigarMatchMismatchMerge);
+                text += '\n';
+            }
+            o.gaf = std::move(text);
+            o.bpAligned = bpAligned;
+            o.alignments = alns.size();
+            stats.bpAligned += bpAligned;
+        }
+        catch (const ReadFailure&)
+        {
+            o.failed = true;
+            o.gaf.clear();
+            stats.failedReads++;
+        }
+    }
+}
+
+}

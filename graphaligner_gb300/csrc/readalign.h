@@ -1,0 +1,159 @@
+// Host-side types of the read-level layer (readalign.cpp, seeding.cpp).
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#include "../../include/graphaligner_gb300.h"
+
+namespace gahost
+{
+
+// AlignmentGraph fields the host logic reads (AlignmentGraph.h:121-139)
+struct HostGraph
+{
+    explicit HostGraph(const ga_host_graph_desc& d);
+    uint32_t N;
+    uint32_t firstAmbiguous;
+    std::vector<uint32_t> len, inOff, inNb, outOff, outNb, nodeOffset;
+    std::vector<uint64_t> seq2, seqAmb, chainNumber, chainApproxPos;
+    std::vector<int32_t> nodeIds;
+    std::vector<uint8_t> reverse;
+    std::vector<int32_t> lookupIds;
+    std::vector<uint32_t> originalSize, lookupOff, lookupNodes;
+    std::vector<std::string> names;
+    std::unordered_map<int, size_t> lookupIndex;
+    size_t bpSize;
+    size_t lookup(int bignode) const;
+    char charAt(size_t node, size_t pos) const;
+    size_t unitigNode(int bignode, size_t offset) const;
+    std::pair<int, size_t> reversePosition(int bignode, size_t offset) const;
+    size_t sizeOf(int bignode) const;
+    const std::string& nameOf(int bignode) const;
+};
+
+// SeedHit (GraphAlignerWrapper.h:11-50)
+struct SeedHit
+{
+    int nodeID = INT32_MIN;
+    size_t nodeOffset = SIZE_MAX;
+    size_t seqPos = SIZE_MAX;
+    size_t matchLen = SIZE_MAX;
+    bool reverse = false;
+    size_t alignmentGraphNodeId = SIZE_MAX;
+    size_t alignmentGraphNodeOffset = SIZE_MAX;
+    size_t rawSeedGoodness = 0;
+    size_t seedGoodness = 0;
+    size_t seedClusterSize = 0;
+};
+
+// TraceItem / OnewayTrace (GraphAlignerCommon.h:110-166)
+struct TraceItem
+{
+    size_t node;
+    size_t nodeOffset;
+    size_t seqPos;
+    bool nodeSwitch;
+    char seqChar;
+    char graphChar;
+};
+
+struct OnewayTrace
+{
+    std::vector<TraceItem> trace;
+    int32_t score = 0;
+    bool failed() const { return score == INT32_MAX; }
+};
+
+// AlignmentResult::AlignmentItem (GraphAlignerCommon.h:289-340)
+struct AlignmentItem
+{
+    std::shared_ptr<OnewayTrace> trace;
+    size_t seedGoodness = 0;
+    size_t alignmentStart = 0;
+    size_t alignmentEnd = 0;
+    size_t alignmentScore = SIZE_MAX;
+    double alignmentXScore = -1;
+    int mappingQuality = 255;
+};
+
+struct ReadAlignParams
+{
+    bool sloppy = true;
+    size_t minClusterSize = 1;
+    double seedExtendDensity = -1;
+    int32_t xscoreErrorCost = 294;
+    int minAlignmentScore = 0;
+    double multimapScoreFraction = 0.9;
+    bool cigarMatchMismatchMerge = false;
+};
+
+struct ReadInput
+{
+    std::string name;
+    std::string seq;
+    std::vector<SeedHit> seeds;
+};
+
+struct ReadOutput
+{
+    std::string gaf;
+    size_t bpAligned = 0;
+    size_t alignments = 0;
+    bool failed = false;     // an assert would have dropped the read
+    bool noSeeds = false;
+};
+
+struct BatchStats
+{
+    uint64_t rounds = 0;
+    uint64_t extensions = 0;
+    uint64_t cellSteps = 0;
+    uint64_t bpAligned = 0;
+    uint64_t failedReads = 0;
+};
+
+struct ExtensionRequest
+{
+    const char* seq;
+    uint32_t len;
+    int bignode;
+    size_t offset;
+    uint32_t node;
+    uint32_t nodeOffset;
+};
+
+struct ExtensionResult
+{
+    int32_t status = 0;
+    int32_t score = 0;
+    uint64_t steps = 0;
+    std::vector<uint64_t> items;
+};
+
+typedef void (*ExtendFn)(void* ctx, const std::vector<ExtensionRequest>& requests, std::vector<ExtensionResult>& results);
+
+void orderSeeds(const HostGraph& g, std::vector<SeedHit>& seedHits);
+void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,
+    std::vector<ReadOutput>& out, BatchStats& stats);
+
+// MinimizerSeeder with one bucket (MinimizerSeeder.h:14-47)
+struct MinimizerIndex
+{
+    size_t k = 15;
+    size_t w = 20;
+    size_t maxCount = 0;
+    std::vector<uint64_t> keys;        // distinct k-mers, sorted (the dense id of a k-mer is its rank)
+    std::vector<uint64_t> startPos;    // [keys + 1]
+    std::vector<uint64_t> positions;   // (split node << 6) | offset, grouped by id
+};
+
+void buildMinimizerIndex(const HostGraph& g, size_t k, size_t w, double keepLeastFrequentFraction, MinimizerIndex& idx);
+// k-mer hits of one read in iterateKmers order: (read position, start, count), count < maxCount
+struct KmerMatch { uint64_t pos; uint64_t start; uint64_t count; };
+void kmerMatchesHost(const MinimizerIndex& idx, const std::string& seq, std::vector<KmerMatch>& out);
+void selectSeeds(const HostGraph& g, const MinimizerIndex& idx, const std::string& seq, double density,
+    std::vector<KmerMatch>& matches, std::vector<SeedHit>& out);
+
+}

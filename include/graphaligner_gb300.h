@@ -157,6 +157,71 @@ int ga_host_free(void* ptr);
  * (integer ops per second), the denominator of the DP kernels' ALU roofline. */
 int ga_measure_int32_peak(int device, double* ops_per_second);
 
+/* ---- read-level alignment ----
+ * The per-read flow of GraphAligner's aligner (Aligner.cpp:440-592): minimizer
+ * seeds (MinimizerSeeder::getSeeds, k-mer lookups on the GPU), OrderSeeds
+ * (GraphAligner.h:250-312), the seed loop of GraphAligner::AlignOneWay
+ * (GraphAligner.h:94-181; src/GraphAlignerWrapper.h:54) with both extensions of
+ * each seed on the GPU, SelectAlignments (AlignmentSelection.cpp:31-53) and GAF
+ * lines (GraphAlignerGAFAlignment.h:37-200).  Reads of a call advance through
+ * their seed loops together; each round's extensions run as one GPU batch. */
+typedef struct ga_host_graph_desc {
+    ga_graph_desc base;               /* the DP fields, host pointers */
+    const int32_t*  node_ids;         /* [num_nodes] bigraph node id of each piece (GFA id*2 + strand) */
+    const uint32_t* node_offset;      /* [num_nodes] offset of the piece inside its bigraph node */
+    const uint8_t*  reverse;          /* [num_nodes] */
+    const uint64_t* chain_number;     /* [num_nodes] AlignmentGraph::chainNumber */
+    const uint64_t* chain_approx_pos; /* [num_nodes] AlignmentGraph::chainApproxPos */
+    uint32_t num_lookup;              /* bigraph nodes, in AlignmentGraph::nodeLookup order */
+    const int32_t*  lookup_ids;
+    const uint32_t* original_size;
+    const uint32_t* lookup_offsets;   /* [num_lookup + 1] */
+    const uint32_t* lookup_nodes;     /* pieces of each bigraph node, in offset order */
+    const char* const* names;         /* [num_lookup] original names ("" = numeric GFA id), or NULL */
+} ga_host_graph_desc;
+
+/* AlignerParams fields of this flow (Aligner.h:10-47); -x vg: 15, 20, 10, 0.001, -1, 1, 1, 0, 0, 0.9 */
+typedef struct ga_align_params {
+    ga_extend_params extend;
+    uint32_t minimizer_length;
+    uint32_t minimizer_window;
+    double   minimizer_density;
+    double   minimizer_discard_fraction;
+    double   seed_extend_density;
+    uint64_t min_cluster_size;
+    uint8_t  sloppy;                   /* not --try-all-seeds */
+    uint8_t  cigar_match_mismatch;
+    int32_t  min_alignment_score;
+    double   multimap_score_fraction;
+} ga_align_params;
+
+typedef struct ga_align_stats {
+    uint64_t reads;
+    uint64_t reads_with_seeds;
+    uint64_t reads_aligned;
+    uint64_t failed_reads;            /* reads a reference assert would have dropped */
+    uint64_t bp_aligned;              /* union of alignment intervals per read (Aligner.cpp:536-547) */
+    uint64_t rounds;
+    uint64_t extensions;
+    uint64_t cell_steps;
+    double   seed_ms;
+    double   extend_ms;
+    double   host_ms;
+} ga_align_stats;
+
+typedef struct ga_aligner* ga_aligner_t;
+/* Builds the minimizer index of the graph on the host and uploads its lookup table. */
+int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* graph, const ga_align_params* params, ga_aligner_t* out);
+int ga_aligner_free(ga_aligner_t aligner);
+/* Aligns a batch of reads (host buffers); the GAF text stays with the aligner. */
+int ga_align_reads(ga_aligner_t aligner, uint32_t num_reads, const char* const* names, const uint8_t* seq,
+                   const uint64_t* seq_offset, const uint32_t* seq_len);
+/* GAF lines of the last ga_align_reads call, reads in input order; valid until the next call. */
+int ga_aligner_gaf(ga_aligner_t aligner, const char** text, uint64_t* bytes);
+/* Per-read bp aligned of the last call. */
+int ga_aligner_read_bp(ga_aligner_t aligner, uint64_t* bp_per_read);
+int ga_aligner_stats(ga_aligner_t aligner, ga_align_stats* out);
+
 const char* ga_last_error(void);
 const char* ga_version(void);
 

@@ -8,7 +8,10 @@ synthetic inputs and stores what it produced:
   *_ext.tsv.gz     extension requests "bigraphNodeId offset sequence"
   *_ext_bN.digest  per request: status score n_items sha1(packed items)
                    from getReverseTraceFromSeed at bandwidth N
-  test_graph.gaf   GAF of the reference's own quickstart (test/graph.gfa, test/read.fa)
+  test_graph.gaf   GAF of the reference's own quickstart (test/graph.gfa, test/read.fa),
+                   with the read as test_read.fa and the graph as test_graph.gag.gz
+  vg50k_reads.fa.gz, vg50k_b{10,5}.gaf.gz   reads and the reference's GAF (-x vg, -b 10 / 5)
+  vg50k_seeds.digest  sha1 of every line of MinimizerSeeder::getSeeds + OrderSeeds output
 
 The packed item layout is the one include/graphaligner_gb300.h documents, so
 the oracle restatement and the GPU kernels are compared byte for byte.
@@ -61,18 +64,24 @@ def run_ext(gfa, tsv, bandwidth, max_cells=UNLIMITED):
         return digest_ref_output(out)
 
 
+def digest_lines(text: str) -> str:
+    """sha1 of every line (seed lists are long; their digests pin them)."""
+    return "".join(hashlib.sha1(line.encode()).hexdigest() + "\n" for line in text.splitlines())
+
+
 def gz_write(path, data: bytes):
     with open(path, "wb") as raw, gzip.GzipFile(fileobj=raw, mode="wb", mtime=0) as g:
         g.write(data)
 
 
-def make_set(name, graph, ext, bandwidths, max_cells=UNLIMITED):
+def make_set(name, graph, ext, bandwidths, max_cells=UNLIMITED, write_graph=True):
     with tempfile.TemporaryDirectory() as td:
         gfa = os.path.join(td, "g.gfa")
         open(gfa, "w").write(graph.to_gfa())
         gag = os.path.join(td, "g.gag")
         subprocess.run([REF, "graphdump", gfa, gag], check=True)
-        gz_write(os.path.join(HERE, f"{name}_graph.gag.gz"), open(gag, "rb").read())
+        if write_graph:
+            gz_write(os.path.join(HERE, f"{name}_graph.gag.gz"), open(gag, "rb").read())
         tsv = os.path.join(td, "ext.tsv")
         open(tsv, "w").write(ext.to_tsv())
         gz_write(os.path.join(HERE, f"{name}_ext.tsv.gz"), ext.to_tsv().encode())
@@ -97,13 +106,28 @@ def main():
     # same graph, reads 0.5-20 kbp at 5-25% error
     reads2 = dg.sample_reads(g, 60, 7, dg.uniform_length(500, 20_000), dg.uniform_error(0.05, 0.25))
     ext2 = dg.seed_extensions(reads2, node_lengths(g), 15, 4, per_read=1)
-    make_set("vg50k_hi", g, ext2, [10])
+    make_set("vg50k_hi", g, ext2, [10], write_graph=False)   # graph: vg50k_graph.gag.gz
+    # read-level GAF (seeding + seed loop + selection + GAF) on the same graph, -x vg at bandwidth 10 and 5
+    with tempfile.TemporaryDirectory() as td:
+        gfa = os.path.join(td, "g.gfa")
+        open(gfa, "w").write(g.to_gfa())
+        fa = os.path.join(td, "reads.fa")
+        open(fa, "w").write(dg.write_fasta(reads))
+        gz_write(os.path.join(HERE, "vg50k_reads.fa.gz"), dg.write_fasta(reads).encode())
+        for bw in (10, 5):
+            out = os.path.join(td, f"b{bw}.gaf")
+            subprocess.run([REF, "align", gfa, fa, out, "vg", str(bw)], check=True)
+            gz_write(os.path.join(HERE, f"vg50k_b{bw}.gaf.gz"), open(out, "rb").read())
+        out = os.path.join(td, "seeds.txt")
+        subprocess.run([REF, "seeds", gfa, fa, out, "15", "20", "10", "0.001"], check=True)
+        open(os.path.join(HERE, "vg50k_seeds.digest"), "w").write(digest_lines(open(out).read()))
     # the reference's quickstart
     ref_test = "/root/reference/test"
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "aln.gaf")
         subprocess.run([REF, "align", os.path.join(ref_test, "graph.gfa"), os.path.join(ref_test, "read.fa"), out, "vg"], check=True)
         open(os.path.join(HERE, "test_graph.gaf"), "w").write(open(out).read())
+        open(os.path.join(HERE, "test_read.fa"), "w").write(open(os.path.join(ref_test, "read.fa")).read())
         subprocess.run([REF, "graphdump", os.path.join(ref_test, "graph.gfa"), os.path.join(td, "t.gag")], check=True)
         gz_write(os.path.join(HERE, "test_graph.gag.gz"), open(os.path.join(td, "t.gag"), "rb").read())
 

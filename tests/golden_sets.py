@@ -15,7 +15,11 @@ from graphaligner_gb300.extend import pack_batch
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+GRAPH_OF = {"vg50k_hi": "vg50k"}
+
+
 def load_graph(name: str):
+    name = GRAPH_OF.get(name, name)
     with tempfile.NamedTemporaryFile(suffix=".gag") as f:
         f.write(gzip.open(os.path.join(GOLDEN, f"{name}_graph.gag.gz")).read())
         f.flush()
@@ -65,3 +69,27 @@ def compare(result, expected):
         elif d != e:
             bad.append(i)
     return bad
+
+
+def load_reads(name: str = "vg50k"):
+    names, seqs = [], []
+    for line in gzip.open(os.path.join(GOLDEN, f"{name}_reads.fa.gz"), "rt"):
+        line = line.rstrip("\n")
+        if line.startswith(">"):
+            names.append(line[1:].split()[0])
+            seqs.append("")
+        elif line:
+            seqs[-1] += line
+    return names, [s.encode() for s in seqs]
+
+
+def load_gaf(name: str, bandwidth: int) -> str:
+    return gzip.open(os.path.join(GOLDEN, f"{name}_b{bandwidth}.gaf.gz"), "rt").read()
+
+
+def graph_file(name: str, directory: str) -> str:
+    """Writes the golden graph as a plain GAG1 file into directory and returns its path."""
+    name = GRAPH_OF.get(name, name)
+    path = os.path.join(directory, f"{name}.gag")
+    open(path, "wb").write(gzip.open(os.path.join(GOLDEN, f"{name}_graph.gag.gz")).read())
+    return path

@@ -1,0 +1,173 @@
+// Test harness (CPU): the read-level host logic of the package (seeding.cpp,
+// readalign.cpp) driven by the oracle's extensions, printing seeds or GAF in the
+// formats oracle/_ref/ga_ref prints, so the two can be diffed.
+//   pipeline <graph.gag> <reads.fa> seeds <k> <w> <density> <discard>
+//   pipeline <graph.gag> <reads.fa> gaf <bandwidth> <maxcells|->
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+#include "../../include/graphaligner_gb300.h"
+#include "../../graphaligner_gb300/csrc/readalign.h"
+
+extern "C" int ora_extend_batch(const ga_graph_desc*, const ga_extend_params*, const ga_extend_batch_desc*, ga_extend_results*, int);
+
+struct Gag
+{
+    uint64_t h[8];
+    std::vector<uint32_t> len, off, comp, inOff, inNb, outOff, outNb, origSize, lookupOff, lookupNodes, nameLen;
+    std::vector<int32_t> ids, lookupIds;
+    std::vector<uint8_t> rev, lin;
+    std::vector<uint64_t> chain, chainPos, seq2, seqAmb;
+    std::vector<std::string> names;
+    std::vector<const char*> namePtr;
+};
+
+template <typename T>
+static void rd(std::ifstream& f, std::vector<T>& v, size_t n)
+{
+    v.resize(n);
+    if (n) f.read((char*)v.data(), n * sizeof(T));
+}
+
+static bool loadGag(const char* path, Gag& g)
+{
+    std::ifstream f(path, std::ios::binary);
+    char magic[4];
+    f.read(magic, 4);
+    if (memcmp(magic, "GAG1", 4) != 0) return false;
+    f.read((char*)g.h, sizeof(g.h));
+    size_t N = g.h[0], fa = g.h[1], nIn = g.h[2], nOut = g.h[3], M = g.h[4], nL = g.h[5], nNames = g.h[6];
+    rd(f, g.len, N); rd(f, g.ids, N); rd(f, g.off, N); rd(f, g.rev, N); rd(f, g.lin, N); rd(f, g.comp, N);
+    rd(f, g.chain, N); rd(f, g.chainPos, N); rd(f, g.seq2, fa * 2); rd(f, g.seqAmb, (N - fa) * 4);
+    rd(f, g.inOff, N + 1); rd(f, g.inNb, nIn); rd(f, g.outOff, N + 1); rd(f, g.outNb, nOut);
+    rd(f, g.lookupIds, M); rd(f, g.origSize, M); rd(f, g.lookupOff, M + 1); rd(f, g.lookupNodes, nL); rd(f, g.nameLen, M);
+    std::string blob(nNames, ' ');
+    if (nNames) f.read(&blob[0], nNames);
+    size_t p = 0;
+    for (size_t i = 0; i < M; i++) { g.names.push_back(blob.substr(p, g.nameLen[i])); p += g.nameLen[i]; }
+    for (auto& s : g.names) g.namePtr.push_back(s.c_str());
+    return true;
+}
+
+static std::vector<std::pair<std::string, std::string>> readFasta(const char* path)
+{
+    std::vector<std::pair<std::string, std::string>> r;
+    std::ifstream in(path);
+    std::string line;
+    while (std::getline(in, line))
+    {
+        if (line.empty()) continue;
+        if (line[0] == '>')
+        {
+            std::string name = line.substr(1);
+            auto sp = name.find_first_of(" \t");
+            if (sp != std::string::npos) name = name.substr(0, sp);
+            r.emplace_back(name, "");
+        }
+        else r.back().second += line;
+    }
+    return r;
+}
+
+struct Ctx
+{
+    ga_graph_desc* d;
+    ga_extend_params p;
+};
+
+static void oracleExtend(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs)
+{
+    Ctx* c = (Ctx*)ctx;
+    size_t n = rq.size();
+    std::vector<uint8_t> blob;
+    std::vector<uint64_t> off(n), toff(n), items, steps(n);
+    std::vector<uint32_t> len(n), node(n), noff(n), cap(n), tlen(n);
+    std::vector<int32_t> status(n), score(n);
+    uint64_t ti = 0;
+    for (size_t i = 0; i < n; i++)
+    {
+        off[i] = blob.size();
+        blob.insert(blob.end(), rq[i].seq, rq[i].seq + rq[i].len);
+        len[i] = rq[i].len; node[i] = rq[i].node; noff[i] = rq[i].nodeOffset;
+        cap[i] = rq[i].len + rq[i].len / 4 + 512;
+        toff[i] = ti; ti += cap[i];
+    }
+    if (blob.empty()) blob.push_back(0);
+    items.resize(ti + 1);
+    ga_extend_batch_desc b { (uint32_t)n, blob.data(), off.data(), len.data(), node.data(), noff.data(), toff.data(), cap.data() };
+    ga_extend_results r { status.data(), score.data(), tlen.data(), items.data(), steps.data() };
+    ora_extend_batch(c->d, &c->p, &b, &r, 8);
+    for (size_t i = 0; i < n; i++)
+    {
+        rs[i].status = status[i];
+        rs[i].score = score[i];
+        rs[i].steps = steps[i];
+        rs[i].items.assign(items.begin() + toff[i], items.begin() + toff[i] + tlen[i]);
+    }
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 4) return 1;
+    Gag g;
+    if (!loadGag(argv[1], g)) return 2;
+    ga_host_graph_desc hd {};
+    hd.base = ga_graph_desc { (uint32_t)g.h[0], (uint32_t)g.h[1], g.len.data(), g.seq2.data(), g.seqAmb.data(), g.inOff.data(), g.inNb.data(),
+        g.outOff.data(), g.outNb.data(), g.lin.data(), g.comp.data() };
+    hd.node_ids = g.ids.data(); hd.node_offset = g.off.data(); hd.reverse = g.rev.data();
+    hd.chain_number = g.chain.data(); hd.chain_approx_pos = g.chainPos.data();
+    hd.num_lookup = (uint32_t)g.lookupIds.size(); hd.lookup_ids = g.lookupIds.data(); hd.original_size = g.origSize.data();
+    hd.lookup_offsets = g.lookupOff.data(); hd.lookup_nodes = g.lookupNodes.data(); hd.names = g.namePtr.data();
+    gahost::HostGraph graph(hd);
+    auto reads = readFasta(argv[2]);
+    std::string mode = argv[3];
+    if (mode == "seeds")
+    {
+        size_t k = std::stoul(argv[4]), w = std::stoul(argv[5]);
+        double density = std::stod(argv[6]), discard = std::stod(argv[7]);
+        gahost::MinimizerIndex idx;
+        gahost::buildMinimizerIndex(graph, k, w, 1.0 - discard, idx);
+        std::cout << "maxCount " << idx.maxCount << "\n";
+        std::vector<gahost::KmerMatch> km;
+        std::vector<gahost::SeedHit> seeds;
+        for (auto& r : reads)
+        {
+            gahost::kmerMatchesHost(idx, r.second, km);
+            gahost::selectSeeds(graph, idx, r.second, density, km, seeds);
+            std::cout << "R " << r.first << " " << seeds.size();
+            for (auto& s : seeds) std::cout << " " << s.nodeID << "," << s.nodeOffset << "," << s.seqPos << "," << s.matchLen << "," << s.reverse << "," << s.alignmentGraphNodeId << "," << s.alignmentGraphNodeOffset << "," << s.rawSeedGoodness;
+            std::cout << "\n";
+            gahost::orderSeeds(graph, seeds);
+            std::cout << "O " << r.first << " " << seeds.size();
+            for (auto& s : seeds) std::cout << " " << s.nodeID << "," << s.nodeOffset << "," << s.seqPos << "," << s.seedGoodness << "," << s.seedClusterSize;
+            std::cout << "\n";
+        }
+        return 0;
+    }
+    // gaf: -x vg parameters (AlignerMain.cpp:161-178) with the given bandwidth
+    size_t bw = std::stoul(argv[4]);
+    uint64_t maxCells = (argc > 5 && std::string(argv[5]) != "-") ? std::stoull(argv[5]) : UINT64_MAX;
+    gahost::MinimizerIndex idx;
+    gahost::buildMinimizerIndex(graph, 15, 20, 1.0 - 0.001, idx);
+    std::vector<gahost::ReadInput> in(reads.size());
+    std::vector<gahost::KmerMatch> km;
+    for (size_t i = 0; i < reads.size(); i++)
+    {
+        in[i].name = reads[i].first;
+        in[i].seq = reads[i].second;
+        gahost::kmerMatchesHost(idx, in[i].seq, km);
+        gahost::selectSeeds(graph, idx, in[i].seq, 10, km, in[i].seeds);
+    }
+    Ctx ctx { &hd.base, ga_extend_params { (uint32_t)bw, 14705, maxCells, 294 } };
+    gahost::ReadAlignParams p;
+    std::vector<gahost::ReadOutput> out;
+    gahost::BatchStats st;
+    gahost::alignBatch(graph, p, in, oracleExtend, &ctx, out, st);
+    for (auto& o : out) std::cout << o.gaf;
+    std::cerr << "rounds " << st.rounds << " extensions " << st.extensions << " bp " << st.bpAligned << " failed " << st.failedReads << std::endl;
+    return 0;
+}

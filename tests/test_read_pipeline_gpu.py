@@ -1,0 +1,39 @@
+"""The read-level path on the GPU (k-mer lookups and extensions as kernels)
+against the reference's GAF."""
+import gzip
+import os
+import sys
+
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from golden_sets import GOLDEN, load_gaf, load_graph, load_reads  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("bandwidth", [10, 5])
+def test_gpu_gaf_matches_reference(cuda_lib, bandwidth):
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    g = load_graph("vg50k")
+    names, seqs = load_reads("vg50k")
+    x = Extender(DeviceGraph(g))
+    a = Aligner(x, g, preset("vg", bandwidth=bandwidth))
+    gaf = a.align(names, seqs)
+    st = a.stats()
+    assert st["failed_reads"] == 0
+    assert gaf == load_gaf("vg50k", bandwidth)
+
+
+def test_gpu_quickstart(cuda_lib, tmp_path):
+    from graphaligner_gb300 import graph as gg
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    path = os.path.join(tmp_path, "t.gag")
+    open(path, "wb").write(gzip.open(os.path.join(GOLDEN, "test_graph.gag.gz")).read())
+    g = gg.load_gag(path)
+    lines = open(os.path.join(GOLDEN, "test_read.fa")).read().split()
+    x = Extender(DeviceGraph(g))
+    a = Aligner(x, g, preset("vg"))
+    assert a.align([lines[0][1:]], [lines[1].encode()]) == open(os.path.join(GOLDEN, "test_graph.gaf")).read()

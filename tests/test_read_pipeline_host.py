@@ -1,0 +1,59 @@
+"""The package's read-level host logic (minimizer index, seed selection and
+ordering, the seed loop, trace fix-up and merge, selection, GAF) driven by the
+oracle's extensions, against the reference's own seeds and GAF."""
+import hashlib
+import os
+import subprocess
+import sys
+
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from golden_sets import GOLDEN, graph_file, load_gaf  # noqa: E402
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+BUILD = os.path.join(ROOT, "tests", "_build")
+HARNESS = os.path.join(BUILD, "pipeline")
+SOURCES = [os.path.join(ROOT, "tests", "harness", "pipeline.cpp"),
+           os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.cpp"),
+           os.path.join(ROOT, "graphaligner_gb300", "csrc", "seeding.cpp"),
+           os.path.join(ROOT, "oracle", "ga_oracle.cpp")]
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    os.makedirs(BUILD, exist_ok=True)
+    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
+    if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < max(os.path.getmtime(d) for d in deps):
+        subprocess.run(["g++", "-std=c++17", "-O2", "-o", HARNESS, *SOURCES, "-lpthread"], check=True)
+    d = tmp_path_factory.mktemp("pipeline")
+    import gzip
+    reads = os.path.join(d, "reads.fa")
+    open(reads, "wb").write(gzip.open(os.path.join(GOLDEN, "vg50k_reads.fa.gz")).read())
+    return HARNESS, graph_file("vg50k", str(d)), reads, d
+
+
+def test_seeds_match_reference(harness):
+    exe, gag, reads, _ = harness
+    out = subprocess.run([exe, gag, reads, "seeds", "15", "20", "10", "0.001"], check=True, capture_output=True, text=True).stdout
+    mine = [hashlib.sha1(line.encode()).hexdigest() for line in out.splitlines()]
+    ref = open(os.path.join(GOLDEN, "vg50k_seeds.digest")).read().split()
+    assert mine == ref
+
+
+@pytest.mark.parametrize("bandwidth", [10, 5])
+def test_gaf_matches_reference(harness, oracle_lib, bandwidth):
+    exe, gag, reads, _ = harness
+    out = subprocess.run([exe, gag, reads, "gaf", str(bandwidth)], check=True, capture_output=True, text=True).stdout
+    assert out == load_gaf("vg50k", bandwidth)
+
+
+def test_quickstart_gaf(harness, tmp_path):
+    exe, _, _, _ = harness
+    import gzip
+    gag = os.path.join(tmp_path, "t.gag")
+    open(gag, "wb").write(gzip.open(os.path.join(GOLDEN, "test_graph.gag.gz")).read())
+    out = subprocess.run([exe, gag, os.path.join(GOLDEN, "test_read.fa"), "gaf", "10"], check=True, capture_output=True, text=True).stdout
+    assert out == open(os.path.join(GOLDEN, "test_graph.gaf")).read()
+    fields = out.split("\t")
+    assert fields[5] == ">1>2>4" and fields[2:4] == ["0", "71"] and fields[6] == "87"
