@@ -367,3 +367,227 @@ def batch_extension_workload(n_reads: int, graph_seed: int = 0, read_seed: int =
         parts = [_extension_chunk(c) for c in chunks]
     seqs = [x for p in parts for x in p.seqs]
     return ExtensionSet(seqs, np.concatenate([p.bignode for p in parts]), np.concatenate([p.offset for p in parts]))
+
+
+# De Bruijn graph workload ----------------------------------------------------
+
+def _is_rc_rotation(unit: np.ndarray) -> bool:
+    """True when the reverse complement of a tandem unit is one of its rotations,
+    i.e. the tandem array reads the same on both strands."""
+    rc = revcomp(unit).tobytes()
+    doubled = (unit.tobytes() * 2)
+    return rc in doubled
+
+
+def _mutate(rng, seq: np.ndarray, divergence: float) -> np.ndarray:
+    """A diverged copy: substitutions (80 %) and 1-bp indels (20 %) at the given rate."""
+    n = len(seq)
+    u = rng.random(n)
+    t = rng.random(n)
+    out = seq.copy()
+    sub = (u < divergence) & (t < 0.8)
+    out[sub] = _BASES[(np.searchsorted(_BASES, seq[sub]) + rng.integers(1, 4, int(sub.sum()))) % 4]
+    dele = (u < divergence) & (t >= 0.8) & (t < 0.9)
+    ins = (u < divergence) & (t >= 0.9)
+    keep = ~dele
+    counts = keep.astype(np.int64) + ins.astype(np.int64)
+    res = np.empty(int(counts.sum()), dtype=np.uint8)
+    pos = np.cumsum(counts) - counts
+    res[pos[ins]] = _BASES[rng.integers(0, 4, int(ins.sum()))]
+    res[pos[keep] + ins[keep].astype(np.int64)] = out[keep]
+    return res
+
+
+def make_repeat_genome(genome_len: int, n_copies: int, repeat_len: int, div_lo: float, div_hi: float,
+                       n_tandem: int, tandem_period: tuple = (2, 50), tandem_len: tuple = (500, 3000),
+                       seed: int = 0) -> np.ndarray:
+    """A uniform-random genome of ``genome_len`` bp with ``n_copies`` inserted copies of
+    one ``repeat_len`` bp repeat family (each copy diverged by U[div_lo, div_hi], random
+    strand) and ``n_tandem`` tandem arrays of a random unit of period U[tandem_period].
+    Units that read the same on both strands are redrawn."""
+    rng = np.random.default_rng(seed)
+    parts = [_BASES[rng.integers(0, 4, genome_len)]]
+    family = _BASES[rng.integers(0, 4, repeat_len)]
+    inserts = []
+    for _ in range(n_copies):
+        c = _mutate(rng, family, float(rng.uniform(div_lo, div_hi)))
+        if rng.integers(0, 2):
+            c = revcomp(c)
+        inserts.append(c)
+    for _ in range(n_tandem):
+        p = int(rng.integers(tandem_period[0], tandem_period[1] + 1))
+        while True:
+            unit = _BASES[rng.integers(0, 4, p)]
+            if not _is_rc_rotation(unit):
+                break
+        length = int(rng.integers(tandem_len[0], tandem_len[1] + 1))
+        inserts.append(np.resize(unit, length))
+    order = rng.permutation(len(inserts))
+    cuts = np.sort(rng.integers(1, genome_len, len(inserts)))
+    out = []
+    prev = 0
+    base = parts[0]
+    for cut, idx in zip(cuts, order):
+        out.append(base[prev:cut])
+        out.append(inserts[idx])
+        prev = cut
+    out.append(base[prev:])
+    return np.concatenate(out)
+
+
+def _windows(codes: np.ndarray, m: int) -> np.ndarray:
+    """w[i] = 2-bit packing of codes[i:i+m], first base most significant."""
+    n = len(codes) - m + 1
+    w = np.zeros(n, dtype=np.uint64)
+    for j in range(m):
+        w = (w << np.uint64(2)) | codes[j:j + n]
+    return w
+
+
+@dataclasses.dataclass
+class DbgGraph:
+    """A compacted de Bruijn graph with the place of every genome base in it."""
+    gfa: str
+    node_len: np.ndarray     # int64 [U + 1], length of unitig id (index 0 unused)
+    pos_bignode: np.ndarray  # int64 [genome length], bigraph node holding the base in genome orientation
+    pos_offset: np.ndarray   # int64 [genome length], offset of the base on that node
+
+
+def compact_dbg(genome: np.ndarray, k: int = 63, with_positions: bool = False):
+    """The compacted de Bruijn graph of one linear genome as GFA (k-1 bp overlaps).
+
+    Edge-centric: the edges are the genome's (k+1)-mers on both strands.  A unitig is a
+    maximal path whose inner edges go from an oriented k-mer with one successor to one
+    with one predecessor (and not to its own reverse complement).  Every genome walk
+    between two non-compactable edges is then exactly one unitig, so unitigs are cut
+    from the genome directly: a unitig is named by the smaller canonical id of its two
+    end k-mers, numbered by first occurrence, and written in the orientation whose
+    first k-mer has the smaller id (a single k-mer: its canonical orientation)."""
+    assert k % 2 == 1 and 33 <= k <= 63
+    lut = np.full(256, 255, dtype=np.uint8)
+    lut[np.frombuffer(b"ACGT", dtype=np.uint8)] = np.arange(4, dtype=np.uint8)
+    codes = lut[genome].astype(np.uint64)
+    if (codes > 3).any():
+        raise ValueError("compact_dbg expects an ACGT genome")
+    L = len(codes)
+    nk = L - k + 1
+    lo_len = k - 32
+    w32 = _windows(codes, 32)
+    wlo = _windows(codes, lo_len)
+    rcodes = (np.uint64(3) - codes)[::-1].copy()
+    r32 = _windows(rcodes, 32)
+    rlo = _windows(rcodes, lo_len)
+    hi_f = w32[:nk]
+    lo_f = wlo[32:32 + nk]
+    ridx = L - k - np.arange(nk)
+    hi_r = r32[ridx]
+    lo_r = rlo[ridx + 32]
+    fwd = (hi_f < hi_r) | ((hi_f == hi_r) & (lo_f < lo_r))
+    ch = np.where(fwd, hi_f, hi_r)
+    cl = np.where(fwd, lo_f, lo_r)
+    orient = (~fwd).astype(np.int64)
+    perm = np.lexsort((cl, ch))
+    newk = np.ones(nk, dtype=bool)
+    newk[1:] = (ch[perm][1:] != ch[perm][:-1]) | (cl[perm][1:] != cl[perm][:-1])
+    kid = np.empty(nk, dtype=np.int64)
+    kid[perm] = np.cumsum(newk) - 1
+    nkid = int(kid.max()) + 1
+    node = 2 * kid + orient                      # oriented k-mer along the genome
+    a, b = node[:-1], node[1:]
+    fr = np.concatenate([a, b ^ 1])
+    to = np.concatenate([b, a ^ 1])
+    key = np.unique(fr * (2 * nkid) + to)
+    outdeg = np.bincount(key // (2 * nkid), minlength=2 * nkid)
+    indeg = np.bincount(key % (2 * nkid), minlength=2 * nkid)
+    compactable = (outdeg[a] == 1) & (indeg[b] == 1) & (kid[:-1] != kid[1:])
+    starts = np.concatenate([[0], np.nonzero(~compactable)[0] + 1])
+    ends = np.concatenate([starts[1:] - 1, [nk - 1]])
+    ks, ke = kid[starts], kid[ends]
+    canon = np.where(starts == ends, orient[starts] == 0, ks <= ke)
+    ukey = np.minimum(ks, ke)
+    _, first_occ, inverse = np.unique(ukey, return_index=True, return_inverse=True)
+    # number unitigs by first occurrence along the genome
+    rank = np.empty(len(first_occ), dtype=np.int64)
+    rank[np.argsort(first_occ, kind="stable")] = np.arange(len(first_occ))
+    uid = rank[inverse] + 1
+    order = np.argsort(rank)
+    lines = []
+    for u in order:
+        occ = first_occ[u]
+        s, e = int(starts[occ]), int(ends[occ])
+        seq = genome[s:e + k]
+        if not canon[occ]:
+            seq = revcomp(seq)
+        lines.append(f"S\t{rank[u] + 1}\t{seq.tobytes().decode()}")
+    # links between consecutive occurrences, one representative per reverse-complement pair
+    fa, fb = uid[:-1], uid[1:]
+    sa, sb = canon[:-1].astype(np.int64), canon[1:].astype(np.int64)
+    e1 = np.stack([fa, sa, fb, sb], axis=1)
+    e2 = np.stack([fb, 1 - sb, fa, 1 - sa], axis=1)
+    use2 = (e2[:, 0] < e1[:, 0]) | ((e2[:, 0] == e1[:, 0]) & ((e2[:, 1] > e1[:, 1]) | ((e2[:, 1] == e1[:, 1]) & ((e2[:, 2] < e1[:, 2]) | ((e2[:, 2] == e1[:, 2]) & (e2[:, 3] > e1[:, 3]))))))
+    edges = np.where(use2[:, None], e2, e1)
+    _, idx = np.unique(edges[:, 0] * (8 * len(first_occ) + 8) + edges[:, 1] * (4 * len(first_occ) + 4) + edges[:, 2] * 2 + edges[:, 3], return_index=True)
+    ov = k - 1
+    for i in np.sort(idx):
+        x, xs, y, ys = (int(v) for v in edges[i])
+        lines.append(f"L\t{x}\t{'+' if xs else '-'}\t{y}\t{'+' if ys else '-'}\t{ov}M")
+    gfa = "\n".join(lines) + "\n"
+    if not with_positions:
+        return gfa
+    # a base at genome position p lies in the occurrence that holds the k-mer starting at p
+    # (the last k-1 bases: in the last occurrence)
+    seg = np.searchsorted(starts, np.minimum(np.arange(L), nk - 1), side="right") - 1
+    pos_offset = np.arange(L) - starts[seg]
+    pos_bignode = uid[seg] * 2 + np.where(canon[seg], 0, 1)
+    node_len = np.zeros(len(first_occ) + 1, dtype=np.int64)
+    node_len[uid] = ends - starts + k
+    return DbgGraph(gfa, node_len, pos_bignode.astype(np.int64), pos_offset.astype(np.int64))
+
+
+def sample_genome_reads(genome: np.ndarray, n_reads: int, seed: int, length_fn, error_fn,
+                        prefix: str = "read", dbg: DbgGraph | None = None) -> list:
+    """Reads as windows of a linear genome on a random strand with errors
+    (60 % substitution, 20 % insertion, 20 % deletion of the error budget).  With the
+    genome's graph given, every unedited base carries its bigraph node and offset."""
+    rng = np.random.default_rng(seed)
+    reads = []
+    for r in range(n_reads):
+        length = int(min(length_fn(rng), len(genome) - 1))
+        start = int(rng.integers(0, len(genome) - length + 1))
+        gpos = np.arange(start, start + length)
+        truth = genome[start:start + length]
+        reverse = bool(rng.integers(0, 2))
+        if reverse:
+            truth = revcomp(truth)
+            gpos = gpos[::-1]
+        bases, src, exact = _apply_errors(rng, truth, float(error_fn(rng)))
+        if dbg is None:
+            bn = np.full(len(bases), -1, dtype=np.int64)
+            bo = bn.copy()
+        else:
+            p = gpos[np.maximum(src, 0)]
+            bn = dbg.pos_bignode[p]
+            bo = dbg.pos_offset[p]
+            if reverse:
+                bo = dbg.node_len[bn // 2] - 1 - bo
+                bn = bn ^ 1
+            bn = np.where(exact & (src >= 0), bn, -1)
+            bo = np.where(exact & (src >= 0), bo, -1)
+        reads.append(Read(f"{prefix}{r}", bases.tobytes(), bn, bo, exact & (src >= 0)))
+    return reads
+
+
+def small_dbg_genome(seed: int = 0) -> np.ndarray:
+    """100 kbp genome, 10 copies of a 2 kbp repeat at 1-3 % divergence, 20 tandem arrays."""
+    return make_repeat_genome(100_000, 10, 2_000, 0.01, 0.03, 20, tandem_len=(200, 1000), seed=seed)
+
+
+def stress_dbg_genome(seed: int = 0) -> np.ndarray:
+    """10 Mbp genome, 200 copies of a 5 kbp repeat at 1-3 % divergence, tandem repeats of period 2-50."""
+    return make_repeat_genome(10_000_000, 200, 5_000, 0.01, 0.03, 400, seed=seed)
+
+
+def dbg_reads(genome: np.ndarray, n: int, length: int = 20_000, error: float = 0.12, seed: int = 1,
+              dbg: DbgGraph | None = None) -> list:
+    """Reads of ``length`` bp at ``error`` from the genome on random strands."""
+    return sample_genome_reads(genome, n, seed, lambda rng: length, lambda rng: error, dbg=dbg)

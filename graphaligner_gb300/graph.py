@@ -7,7 +7,7 @@ Two sources:
   dumped field by field), so the GPU path runs on the reference's exact node
   numbering, component order and neighbour order.
 * ``build_from_gfa`` builds the same kind of graph from a GFA with 0-bp overlaps
-  (the variation-graph workloads).  It follows AlignmentGraph's construction
+  (the variation-graph workloads) or constant k-1 overlaps (de Bruijn graphs).  It follows AlignmentGraph's construction
   rules (AlignmentGraph.cpp:48-296): both strands (GFA id*2 forward, id*2+1
   reverse complement), nodes split into pieces of at most 64 bp, ambiguous
   nodes renumbered to the end, the linearizable flags of findLinearizable and
@@ -284,7 +284,13 @@ def _component_order(out_lists):
 
 
 def build_from_gfa(gfa_text: str) -> Graph:
-    """Alignment graph from a GFA whose links all have 0-bp overlap."""
+    """Alignment graph from a GFA (0-bp overlaps or de Bruijn k-1 overlaps).
+
+    An overlap of ``o`` bp on a link enters the target strand at offset ``o``: both
+    strands get a breakpoint there, pieces are cut between breakpoints in 64-bp steps
+    from each breakpoint, and the link joins the source's last piece to the target's
+    piece that starts at ``o`` (DirectedGraph::BuildFromGFA, BigraphToDigraph.cpp:214-266;
+    AlignmentGraph::AddNode / AddEdgeNodeId, AlignmentGraph.cpp:47-80, 230-248)."""
     seqs = {}
     order = []
     links = []
@@ -296,11 +302,18 @@ def build_from_gfa(gfa_text: str) -> Graph:
             seqs[f[1]] = f[2]
             order.append(f[1])
         else:
-            if f[5] not in ("0M", "*"):
-                raise ValueError("build_from_gfa handles 0-bp overlaps only")
-            links.append((f[1], f[2] == "+", f[3], f[4] == "+"))
+            ov = 0 if f[5] == "*" else int(f[5].rstrip("MS"))
+            links.append((f[1], f[2] == "+", f[3], f[4] == "+", ov))
     numeric = all(s.lstrip("-").isdigit() for s in order)
     ids = {name: (int(name) if numeric else k + 1) for k, name in enumerate(order)}
+    breaks = {}
+    for a, ap, b, bp, ov in links:
+        if ov >= len(seqs[a]) or ov >= len(seqs[b]):
+            raise ValueError(f"overlap between {a} and {b} is not smaller than both nodes")
+        if ov:
+            fa_, fb = ids[a] * 2 + (0 if ap else 1), ids[b] * 2 + (0 if bp else 1)
+            breaks.setdefault(fb, set()).add(ov)
+            breaks.setdefault(fa_ ^ 1, set()).add(ov)
     pieces = []     # (bignode, offset, sequence)
     lookup = []     # (bignode, [piece indices])
     names = []
@@ -311,32 +324,34 @@ def build_from_gfa(gfa_text: str) -> Graph:
         for strand, text in ((0, s), (1, s.encode().translate(_COMPLEMENT)[::-1].decode())):
             big = nid * 2 + strand
             idx = []
-            for o in range(0, len(text), SPLIT_NODE_SIZE):
-                idx.append(len(pieces))
-                pieces.append((big, o, text[o:o + SPLIT_NODE_SIZE]))
+            bp_ = sorted(breaks.get(big, set()) | {0, len(text)})
+            for lo, hi in zip(bp_, bp_[1:]):
+                for o in range(lo, hi, SPLIT_NODE_SIZE):
+                    idx.append(len(pieces))
+                    pieces.append((big, o, text[o:min(o + SPLIT_NODE_SIZE, hi)]))
             lookup.append((big, idx))
             names.append("" if numeric else name)
             size_of[big] = len(text)
     n = len(pieces)
     in_lists = [[] for _ in range(n)]
     out_lists = [[] for _ in range(n)]
-    first_piece = {big: idx[0] for big, idx in lookup}
+    piece_at = {(big, pieces[i][1]): i for big, idx in lookup for i in idx}
     last_piece = {big: idx[-1] for big, idx in lookup}
     for big, idx in lookup:
         for a, b in zip(idx, idx[1:]):
             out_lists[a].append(b)
             in_lists[b].append(a)
 
-    def add_edge(frm, to):
-        a, b = last_piece[frm], first_piece[to]
+    def add_edge(frm, to, ov):
+        a, b = last_piece[frm], piece_at[(to, ov)]
         if a not in in_lists[b]:
             in_lists[b].append(a)
         if b not in out_lists[a]:
             out_lists[a].append(b)
-    for a, ap, b, bp in links:
+    for a, ap, b, bp, ov in links:
         fa_, fb = ids[a] * 2 + (0 if ap else 1), ids[b] * 2 + (0 if bp else 1)
-        add_edge(fa_, fb)
-        add_edge(fb ^ 1, fa_ ^ 1)
+        add_edge(fa_, fb, ov)
+        add_edge(fb ^ 1, fa_ ^ 1, ov)
     # ambiguous pieces go to the end in reverse order (RenumberAmbiguousToEnd, AlignmentGraph.cpp:898-985)
     amb = [any(c not in "ACGTUacgtu" for c in p[2]) for p in pieces]
     renum = np.zeros(n, dtype=np.int64)

@@ -12,6 +12,8 @@ synthetic inputs and stores what it produced:
                    with the read as test_read.fa and the graph as test_graph.gag.gz
   vg50k_reads.fa.gz, vg50k_b{10,5}.gaf.gz   reads and the reference's GAF (-x vg, -b 10 / 5)
   vg50k_seeds.digest  sha1 of every line of MinimizerSeeder::getSeeds + OrderSeeds output
+  dbg100k_*        the same for a k=63 de Bruijn graph with repeats and tandem arrays
+                   (cyclic components), extensions at tangle effort 10000, GAF at -x dbg
 
 The packed item layout is the one include/graphaligner_gb300.h documents, so
 the oracle restatement and the GPU kernels are compared byte for byte.
@@ -77,7 +79,7 @@ def gz_write(path, data: bytes):
 def make_set(name, graph, ext, bandwidths, max_cells=UNLIMITED, write_graph=True):
     with tempfile.TemporaryDirectory() as td:
         gfa = os.path.join(td, "g.gfa")
-        open(gfa, "w").write(graph.to_gfa())
+        open(gfa, "w").write(graph if isinstance(graph, str) else graph.to_gfa())
         gag = os.path.join(td, "g.gag")
         subprocess.run([REF, "graphdump", gfa, gag], check=True)
         if write_graph:
@@ -121,6 +123,22 @@ def main():
         out = os.path.join(td, "seeds.txt")
         subprocess.run([REF, "seeds", gfa, fa, out, "15", "20", "10", "0.001"], check=True)
         open(os.path.join(HERE, "vg50k_seeds.digest"), "w").write(digest_lines(open(out).read()))
+    # de Bruijn graph (k=63, cyclic): 100 kbp genome + 10 copies of a 2 kbp repeat at 1-3 %
+    # divergence + 20 tandem arrays; -x dbg (bandwidth 5, tangle effort 10000)
+    genome = dg.small_dbg_genome(0)
+    d = dg.compact_dbg(genome, 63, with_positions=True)
+    ext_reads = dg.sample_genome_reads(genome, 60, 5, dg.uniform_length(500, 20_000), lambda rng: 0.12, dbg=d)
+    make_set("dbg100k", d.gfa, dg.seed_extensions(ext_reads, d.node_len, 15, 4), [5, 10], max_cells=10000)
+    reads = dg.dbg_reads(genome, 30, 20_000, 0.12, 1)
+    with tempfile.TemporaryDirectory() as td:
+        gfa = os.path.join(td, "g.gfa")
+        open(gfa, "w").write(d.gfa)
+        fa = os.path.join(td, "reads.fa")
+        open(fa, "w").write(dg.write_fasta(reads))
+        gz_write(os.path.join(HERE, "dbg100k_reads.fa.gz"), dg.write_fasta(reads).encode())
+        out = os.path.join(td, "b5.gaf")
+        subprocess.run([REF, "align", gfa, fa, out, "dbg"], check=True)
+        gz_write(os.path.join(HERE, "dbg100k_b5.gaf.gz"), open(out, "rb").read())
     # the reference's quickstart
     ref_test = "/root/reference/test"
     with tempfile.TemporaryDirectory() as td:

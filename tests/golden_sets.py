@@ -16,6 +16,8 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 GRAPH_OF = {"vg50k_hi": "vg50k"}
+# tangle effort (maxCellsPerSlice) the extension digests were made with; unlimited otherwise
+MAX_CELLS = {"dbg100k": 10000}
 
 
 def load_graph(name: str):

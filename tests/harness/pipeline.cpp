@@ -148,11 +148,12 @@ int main(int argc, char** argv)
         }
         return 0;
     }
-    // gaf: -x vg parameters (AlignerMain.cpp:161-178) with the given bandwidth
+    // gaf (-x vg, AlignerMain.cpp:170-177) or gafdbg (-x dbg, AlignerMain.cpp:160-168), with the given bandwidth
+    const bool dbg = mode == "gafdbg";
     size_t bw = std::stoul(argv[4]);
-    uint64_t maxCells = (argc > 5 && std::string(argv[5]) != "-") ? std::stoull(argv[5]) : UINT64_MAX;
+    uint64_t maxCells = (argc > 5 && std::string(argv[5]) != "-") ? std::stoull(argv[5]) : (dbg ? 10000 : UINT64_MAX);
     gahost::MinimizerIndex idx;
-    gahost::buildMinimizerIndex(graph, 15, 20, 1.0 - 0.001, idx);
+    gahost::buildMinimizerIndex(graph, dbg ? 19 : 15, dbg ? 30 : 20, 1.0 - (dbg ? 0.0002 : 0.001), idx);
     std::vector<gahost::ReadInput> in(reads.size());
     std::vector<gahost::KmerMatch> km;
     for (size_t i = 0; i < reads.size(); i++)
@@ -160,10 +161,11 @@ int main(int argc, char** argv)
         in[i].name = reads[i].first;
         in[i].seq = reads[i].second;
         gahost::kmerMatchesHost(idx, in[i].seq, km);
-        gahost::selectSeeds(graph, idx, in[i].seq, 10, km, in[i].seeds);
+        gahost::selectSeeds(graph, idx, in[i].seq, dbg ? 5 : 10, km, in[i].seeds);
     }
     Ctx ctx { &hd.base, ga_extend_params { (uint32_t)bw, 14705, maxCells, 294 } };
     gahost::ReadAlignParams p;
+    if (dbg) p.seedExtendDensity = 0.002;
     std::vector<gahost::ReadOutput> out;
     gahost::BatchStats st;
     gahost::alignBatch(graph, p, in, oracleExtend, &ctx, out, st);

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from golden_sets import compare, golden_case, load_digests  # noqa: E402
+from golden_sets import MAX_CELLS, compare, golden_case, load_digests  # noqa: E402
 
 from graphaligner_gb300 import datagen as dg  # noqa: E402
 from graphaligner_gb300 import graph as gg  # noqa: E402
@@ -40,6 +40,33 @@ def test_gpu_matches_reference_golden_high_error(cuda_lib):
     res = ext.run(ExtendParams(bandwidth=10), batch)
     bad = compare(res, load_digests("vg50k_hi", 10))
     assert not bad, f"{len(bad)} extensions differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("bandwidth", [5, 10])
+def test_gpu_matches_reference_golden_dbg(cuda_lib, bandwidth):
+    """Cyclic components (k=63 de Bruijn graph with repeats and tandem arrays) at tangle effort 10000."""
+    g, batch = golden_case("dbg100k")
+    ext = Extender(DeviceGraph(g))
+    res = ext.run(ExtendParams(bandwidth=bandwidth, max_cells_per_slice=MAX_CELLS["dbg100k"]), batch)
+    bad = compare(res, load_digests("dbg100k", bandwidth))
+    assert not bad, f"{len(bad)} extensions differ, first {bad[:5]}"
+
+
+def test_gpu_matches_oracle_dbg_generated(cuda_lib, oracle_lib):
+    """A second de Bruijn graph built here (own numbering), GPU against the oracle on the same arrays,
+    with tangle efforts that do and do not cut the band."""
+    genome = dg.make_repeat_genome(60_000, 12, 1_500, 0.01, 0.03, 15, tandem_len=(200, 800), seed=21)
+    d = dg.compact_dbg(genome, 63, with_positions=True)
+    g = gg.build_from_gfa(d.gfa)
+    reads = dg.sample_genome_reads(genome, 60, 22, dg.uniform_length(300, 10_000), dg.uniform_error(0.05, 0.15), dbg=d)
+    ext = dg.seed_extensions(reads, d.node_len, 15, 23, per_read=2)
+    batch = pack_batch(g, ext.seqs, ext.bignode, ext.offset)
+    x = Extender(DeviceGraph(g))
+    for bw, cells in ((5, 10000), (10, 10000), (5, 500)):
+        p = ExtendParams(bandwidth=bw, max_cells_per_slice=cells)
+        gpu = x.run(p, batch)
+        ref = oracle_lib.extend(g, p, batch, threads=8)
+        _assert_same(gpu, ref, batch.num)
 
 
 def _assert_same(a, b, n):

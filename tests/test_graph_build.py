@@ -1,0 +1,98 @@
+"""The workload generators' graph side: the de Bruijn compactor and the GFA builder,
+against brute force and against the reference-built graph of the same GFA."""
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from golden_sets import load_graph  # noqa: E402
+
+from graphaligner_gb300 import datagen as dg  # noqa: E402
+from graphaligner_gb300 import graph as gg  # noqa: E402
+
+
+def _rc(s: str) -> str:
+    return dg.revcomp(np.frombuffer(s.encode(), dtype=np.uint8)).tobytes().decode()
+
+
+def _canon(x: str) -> str:
+    return min(x, _rc(x))
+
+
+def test_compact_dbg_brute_force():
+    k = 33
+    genome = dg.make_repeat_genome(20_000, 8, 800, 0.01, 0.03, 10, tandem_len=(100, 400), seed=3)
+    gfa = dg.compact_dbg(genome, k)
+    seqs, links = {}, []
+    for line in gfa.splitlines():
+        f = line.split("\t")
+        if f[0] == "S":
+            seqs[int(f[1])] = f[2]
+        else:
+            links.append((int(f[1]), f[2], int(f[3]), f[4], f[5]))
+    gs = genome.tobytes().decode()
+    owner = {}
+    for u, s in seqs.items():
+        for i in range(len(s) - k + 1):
+            c = _canon(s[i:i + k])
+            assert c not in owner, "a k-mer in two unitigs"
+            owner[c] = u
+    assert set(owner) == {_canon(gs[i:i + k]) for i in range(len(gs) - k + 1)}
+    oriented = lambda u, o: seqs[u] if o == "+" else _rc(seqs[u])  # noqa: E731
+    edges = set()
+    for a, ao, b, bo, ov in links:
+        assert ov == f"{k - 1}M"
+        x, y = oriented(a, ao), oriented(b, bo)
+        assert x[-(k - 1):] == y[:k - 1]
+        edges.add((x[-k:], y[:k]))
+        edges.add((_rc(y[:k]), _rc(x[-k:])))
+    inside = set()
+    for s in seqs.values():
+        for i in range(len(s) - k):
+            inside.add((s[i:i + k], s[i + 1:i + 1 + k]))
+            inside.add((_rc(s[i + 1:i + 1 + k]), _rc(s[i:i + k])))
+    for i in range(len(gs) - k):
+        e = (gs[i:i + k], gs[i + 1:i + 1 + k])
+        assert e in inside or e in edges
+
+
+def test_dbg_positions_and_read_truth():
+    genome = dg.small_dbg_genome(0)
+    d = dg.compact_dbg(genome, 63, with_positions=True)
+    seqs = {}
+    for line in d.gfa.splitlines():
+        f = line.split("\t")
+        if f[0] == "S":
+            seqs[int(f[1])] = f[2]
+    strand = lambda bn: seqs[bn // 2] if bn % 2 == 0 else _rc(seqs[bn // 2])  # noqa: E731
+    for p in range(0, len(genome), 97):
+        assert strand(int(d.pos_bignode[p]))[int(d.pos_offset[p])] == chr(genome[p])
+    for r in dg.dbg_reads(genome, 4, 3000, 0.12, 9, dbg=d):
+        for j in np.nonzero(r.exact)[0][::11]:
+            assert strand(int(r.bignode[j]))[int(r.bigoffset[j])] == chr(r.seq[j])
+
+
+def _structure(g):
+    key = [(int(g.node_ids[i]), int(g.node_offset[i]), int(g.node_length[i])) for i in range(g.num_nodes)]
+    edges = set()
+    for v in range(g.num_nodes):
+        for e in range(int(g.out_offsets[v]), int(g.out_offsets[v + 1])):
+            w = int(g.out_neighbors[e])
+            edges.add((key[v], key[w], bool(g.component[v] == g.component[w]), bool(g.component[v] <= g.component[w])))
+    return set(key), edges, len(set(g.component.tolist()))
+
+
+def test_build_from_gfa_overlaps_matches_reference_graph():
+    """Pieces, edges, strongly connected components and the topological direction of
+    every edge equal those of the reference's build of the same k-1-overlap GFA."""
+    d = dg.compact_dbg(dg.small_dbg_genome(0), 63)
+    mine = _structure(gg.build_from_gfa(d))
+    ref = _structure(load_graph("dbg100k"))
+    assert mine == ref
+
+
+def test_build_from_gfa_variation_graph_matches_reference_graph():
+    mine = _structure(gg.build_from_gfa(dg.small_vg(0).to_gfa()))
+    ref = _structure(load_graph("vg50k"))
+    assert mine == ref

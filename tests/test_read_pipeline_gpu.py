@@ -26,6 +26,18 @@ def test_gpu_gaf_matches_reference(cuda_lib, bandwidth):
     assert gaf == load_gaf("vg50k", bandwidth)
 
 
+def test_gpu_gaf_matches_reference_dbg(cuda_lib):
+    """-x dbg (bandwidth 5, tangle effort 10000) on a k=63 de Bruijn graph with cyclic components."""
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    g = load_graph("dbg100k")
+    names, seqs = load_reads("dbg100k")
+    a = Aligner(Extender(DeviceGraph(g)), g, preset("dbg"))
+    gaf = a.align(names, seqs)
+    assert a.stats()["failed_reads"] == 0
+    assert gaf == load_gaf("dbg100k", 5)
+
+
 def test_gpu_quickstart(cuda_lib, tmp_path):
     from graphaligner_gb300 import graph as gg
     from graphaligner_gb300.align import Aligner, preset

@@ -48,6 +48,16 @@ def test_gaf_matches_reference(harness, oracle_lib, bandwidth):
     assert out == load_gaf("vg50k", bandwidth)
 
 
+def test_gaf_matches_reference_dbg(harness, oracle_lib, tmp_path):
+    """-x dbg on a k=63 de Bruijn graph with cyclic components."""
+    exe = harness[0]
+    import gzip
+    reads = os.path.join(tmp_path, "reads.fa")
+    open(reads, "wb").write(gzip.open(os.path.join(GOLDEN, "dbg100k_reads.fa.gz")).read())
+    out = subprocess.run([exe, graph_file("dbg100k", str(tmp_path)), reads, "gafdbg", "5"], check=True, capture_output=True, text=True).stdout
+    assert out == load_gaf("dbg100k", 5)
+
+
 def test_quickstart_gaf(harness, tmp_path):
     exe, _, _, _ = harness
     import gzip
