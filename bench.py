@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--reads", type=int, default=50_000)
     ap.add_argument("--cpu-sample-bp", type=float, default=200e6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-sample", type=int, default=300, help="extensions timed one launch each (0: skip)")
     return ap.parse_args()
 
 
@@ -329,6 +330,36 @@ def main():
     e2e_same = bool(np.array_equal(hr.status, res.status) and np.array_equal(hr.score, res.score))
     e2e_value = bp * world / statistics.median(e2e_times)
 
+    # ---- the plain form: one launch per extension, waited for, on a sample ----
+    plain = None
+    if rank == 0 and args.plain_sample > 0:
+        pidx = np.unique(np.linspace(0, n - 1, min(n, args.plain_sample)).astype(np.int64))
+        def Pi(t, c, i):
+            return ctypes.cast(ctypes.c_void_p(t.data_ptr() + i * t.element_size()), ctypes.POINTER(c))
+        plain_ms = 0.0
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for i in pidx:
+            i = int(i)
+            b1 = _abi.BatchDesc(1, P(d_seq, u8), Pi(d_soff, u64, i), Pi(d_slen, u32, i), Pi(d_sn, u32, i), Pi(d_so, u32, i),
+                                Pi(d_toff, u64, i), Pi(d_tcap, u32, i))
+            r1 = _abi.Results(Pi(d_status, i32, i), Pi(d_score, i32, i), Pi(d_tlen, u32, i), P(d_items, u64), Pi(d_steps, u64, i))
+            check(L.ga_extend_batch_device(ext.handle, ctypes.byref(cparams), ctypes.byref(b1), ctypes.byref(r1),
+                                           ctypes.c_void_p(stream.cuda_stream)))
+            ms = ctypes.c_float()
+            check(L.ga_extender_last_kernel_ms(ext.handle, ctypes.byref(ms)))
+            plain_ms += ms.value
+        torch.cuda.synchronize()
+        plain_wall = time.perf_counter() - t
+        st = d_status.cpu().numpy()
+        same = bool(np.array_equal(st[pidx], res.status[pidx]) and np.array_equal(d_score.cpu().numpy()[pidx], res.score[pidx]))
+        first = res.trace_items[res.trace_offset[pidx].astype(np.int64)]
+        pbp = int(np.where(res.status[pidx] == 0, (first >> np.uint64(39)).astype(np.int64), 0).sum())
+        plain = {"value": pbp / plain_wall, "unit": UNIT, "kernel_only_value": pbp / (plain_ms / 1e3),
+                 "sample": f"{len(pidx)} of {n} extensions, evenly spaced, {pbp} aligned bp",
+                 "batched_over_plain": value / (pbp / plain_wall), "same_results": same,
+                 "form": "ga_extend_batch_device with one extension per call (one fill+traceback launch, waited for), batch resident in HBM"}
+
     # ---- roofline ----
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
@@ -367,6 +398,7 @@ def main():
         "alu": {"achieved": alu_achieved, "peak": int_peak.value, "unit": "int32 op/s", "frac": alu_achieved / int_peak.value,
                 "ops_per_column_step": INT32_OPS_PER_STEP, "peak_source": "ga_measure_int32_peak (xor+add chains, this GPU)"},
         "cpu_baseline": cpu, "cpu_sample_agrees": cpu_agree,
+        "plain_per_extension": plain,
         "clocks": clocks.summary(),
         "workload_gen_s": gen_s,
     }

@@ -10,38 +10,15 @@
 #include "readalign.h"
 #include "seed_kernel.cuh"
 #include "extend.cuh"
+#include "aligner.h"
 #include "../../include/graphaligner_gb300.h"
 
-namespace
-{
-double ms_since(std::chrono::steady_clock::time_point t)
+static double ms_since(std::chrono::steady_clock::time_point t)
 {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
 }
-}
 
-struct ga_aligner
-{
-    ga_extender_t ext = nullptr;
-    int device = 0;
-    ga_align_params params {};
-    gahost::HostGraph* graph = nullptr;
-    gahost::MinimizerIndex index;
-    gadev::SeedSlot* slots = nullptr;
-    uint64_t capacity = 0;
-    std::string gaf;
-    std::vector<uint64_t> readBp;
-    ga_align_stats stats {};
-    cudaStream_t stream = nullptr;
-    // staging
-    std::vector<uint8_t> blob;
-    std::vector<uint64_t> off, toff;
-    std::vector<uint32_t> len, node, nodeOff, cap, tlen;
-    std::vector<int32_t> status, score;
-    std::vector<uint64_t> items, steps;
-};
-
-static void extend_callback(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs)
+void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs)
 {
     ga_aligner* a = (ga_aligner*)ctx;
     const size_t n = rq.size();
@@ -75,6 +52,7 @@ static void extend_callback(void* ctx, const std::vector<gahost::ExtensionReques
     auto t0 = std::chrono::steady_clock::now();
     int rc = ga_extend_batch(a->ext, &a->params.extend, &b, &r);
     a->stats.extend_ms += ms_since(t0);
+    a->launches++;
     for (size_t i = 0; i < n; i++)
     {
         if (rc != GA_OK)
@@ -87,6 +65,84 @@ static void extend_callback(void* ctx, const std::vector<gahost::ExtensionReques
         rs[i].steps = a->steps[i];
         rs[i].items.assign(a->items.begin() + a->toff[i], a->items.begin() + a->toff[i] + a->tlen[i]);
     }
+}
+
+gahost::ReadAlignParams ga_aligner_read_params(const ga_aligner* a)
+{
+    gahost::ReadAlignParams rp;
+    rp.sloppy = a->params.sloppy != 0;
+    rp.minClusterSize = a->params.min_cluster_size;
+    rp.seedExtendDensity = a->params.seed_extend_density;
+    rp.xscoreErrorCost = a->params.extend.xscore_error_cost;
+    rp.minAlignmentScore = a->params.min_alignment_score;
+    rp.multimapScoreFraction = a->params.multimap_score_fraction;
+    rp.cigarMatchMismatchMerge = a->params.cigar_match_mismatch != 0;
+    return rp;
+}
+
+int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const uint8_t* seq, const uint64_t* seqOffset,
+    const uint32_t* seqLen, std::vector<gahost::ReadInput>& reads)
+{
+    reads.assign(n, gahost::ReadInput {});
+    if (n == 0) return GA_OK;
+    uint64_t seqBytes = 0, matchSlots = 0;
+    std::vector<uint64_t> matchOff(n);
+    for (uint32_t i = 0; i < n; i++)
+    {
+        seqBytes = std::max<uint64_t>(seqBytes, seqOffset[i] + seqLen[i]);
+        matchOff[i] = matchSlots;
+        matchSlots += seqLen[i];
+    }
+    uint8_t* dSeq = nullptr;
+    uint64_t *dOff = nullptr, *dMatchOff = nullptr;
+    uint32_t *dLen = nullptr, *dCount = nullptr;
+    gadev::SeedMatch* dMatch = nullptr;
+    auto release = [&]()
+    {
+        cudaFree(dSeq); cudaFree(dOff); cudaFree(dMatchOff); cudaFree(dLen); cudaFree(dCount); cudaFree(dMatch);
+    };
+    if (cudaMalloc((void**)&dSeq, std::max<uint64_t>(seqBytes, 1)) != cudaSuccess
+        || cudaMalloc((void**)&dOff, n * 8ULL) != cudaSuccess
+        || cudaMalloc((void**)&dMatchOff, n * 8ULL) != cudaSuccess
+        || cudaMalloc((void**)&dLen, n * 4ULL) != cudaSuccess
+        || cudaMalloc((void**)&dCount, n * 4ULL) != cudaSuccess
+        || cudaMalloc((void**)&dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch)) != cudaSuccess)
+    {
+        release();
+        ga_set_last_error("seeding: device buffers for seeding");
+        return GA_ERR_CUDA;
+    }
+    cudaMemcpyAsync(dSeq, seq, seqBytes, cudaMemcpyHostToDevice, a->stream);
+    cudaMemcpyAsync(dOff, seqOffset, n * 8ULL, cudaMemcpyHostToDevice, a->stream);
+    cudaMemcpyAsync(dMatchOff, matchOff.data(), n * 8ULL, cudaMemcpyHostToDevice, a->stream);
+    cudaMemcpyAsync(dLen, seqLen, n * 4ULL, cudaMemcpyHostToDevice, a->stream);
+    gadev::SeedTable table { a->slots, a->capacity, (uint32_t)std::min<uint64_t>(a->index.maxCount, 0xffffffffu) };
+    ga_launch_seed_lookup(table, a->params.minimizer_length, a->params.minimizer_window, n, dSeq, dOff, dLen, dMatchOff, dMatch, dCount, a->stream);
+    std::vector<uint32_t> counts(n);
+    std::vector<gadev::SeedMatch> matches(std::max<uint64_t>(matchSlots, 1));
+    cudaMemcpyAsync(counts.data(), dCount, n * 4ULL, cudaMemcpyDeviceToHost, a->stream);
+    cudaMemcpyAsync(matches.data(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
+    cudaError_t e = cudaStreamSynchronize(a->stream);
+    release();
+    if (e != cudaSuccess)
+    {
+        ga_set_last_error("seeding: seed lookup kernel failed");
+        return GA_ERR_CUDA;
+    }
+    std::vector<gahost::KmerMatch> km;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        reads[i].name = names[i] ? names[i] : "";
+        reads[i].seq.assign((const char*)seq + seqOffset[i], seqLen[i]);
+        km.clear();
+        for (uint32_t k = 0; k < counts[i]; k++)
+        {
+            const auto& m = matches[matchOff[i] + k];
+            km.push_back(gahost::KmerMatch { m.pos, m.start, m.count });
+        }
+        gahost::selectSeeds(*a->graph, a->index, reads[i].seq, a->params.minimizer_density, km, reads[i].seeds);
+    }
+    return GA_OK;
 }
 
 extern "C" int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* graph, const ga_align_params* params, ga_aligner_t* out)
@@ -158,80 +214,18 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     a->gaf.clear();
     a->readBp.assign(n, 0);
     if (n == 0) return GA_OK;
-    // ---- k-mer lookups on the GPU ----
+    // ---- k-mer lookups on the GPU, seed selection on the host ----
     auto ts = std::chrono::steady_clock::now();
-    uint64_t seqBytes = 0, matchSlots = 0;
-    std::vector<uint64_t> matchOff(n);
-    for (uint32_t i = 0; i < n; i++)
-    {
-        seqBytes = std::max<uint64_t>(seqBytes, seqOffset[i] + seqLen[i]);
-        matchOff[i] = matchSlots;
-        matchSlots += seqLen[i];
-    }
-    uint8_t* dSeq = nullptr;
-    uint64_t *dOff = nullptr, *dMatchOff = nullptr;
-    uint32_t *dLen = nullptr, *dCount = nullptr;
-    gadev::SeedMatch* dMatch = nullptr;
-    auto release = [&]()
-    {
-        cudaFree(dSeq); cudaFree(dOff); cudaFree(dMatchOff); cudaFree(dLen); cudaFree(dCount); cudaFree(dMatch);
-    };
-    if (cudaMalloc((void**)&dSeq, std::max<uint64_t>(seqBytes, 1)) != cudaSuccess
-        || cudaMalloc((void**)&dOff, n * 8ULL) != cudaSuccess
-        || cudaMalloc((void**)&dMatchOff, n * 8ULL) != cudaSuccess
-        || cudaMalloc((void**)&dLen, n * 4ULL) != cudaSuccess
-        || cudaMalloc((void**)&dCount, n * 4ULL) != cudaSuccess
-        || cudaMalloc((void**)&dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch)) != cudaSuccess)
-    {
-        release();
-        ga_set_last_error("ga_align_reads: device buffers for seeding");
-        return GA_ERR_CUDA;
-    }
-    cudaMemcpyAsync(dSeq, seq, seqBytes, cudaMemcpyHostToDevice, a->stream);
-    cudaMemcpyAsync(dOff, seqOffset, n * 8ULL, cudaMemcpyHostToDevice, a->stream);
-    cudaMemcpyAsync(dMatchOff, matchOff.data(), n * 8ULL, cudaMemcpyHostToDevice, a->stream);
-    cudaMemcpyAsync(dLen, seqLen, n * 4ULL, cudaMemcpyHostToDevice, a->stream);
-    gadev::SeedTable table { a->slots, a->capacity, (uint32_t)std::min<uint64_t>(a->index.maxCount, 0xffffffffu) };
-    ga_launch_seed_lookup(table, a->params.minimizer_length, a->params.minimizer_window, n, dSeq, dOff, dLen, dMatchOff, dMatch, dCount, a->stream);
-    std::vector<uint32_t> counts(n);
-    std::vector<gadev::SeedMatch> matches(std::max<uint64_t>(matchSlots, 1));
-    cudaMemcpyAsync(counts.data(), dCount, n * 4ULL, cudaMemcpyDeviceToHost, a->stream);
-    cudaMemcpyAsync(matches.data(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
-    cudaError_t e = cudaStreamSynchronize(a->stream);
-    release();
-    if (e != cudaSuccess)
-    {
-        ga_set_last_error("ga_align_reads: seed lookup kernel failed");
-        return GA_ERR_CUDA;
-    }
-    std::vector<gahost::ReadInput> reads(n);
-    std::vector<gahost::KmerMatch> km;
-    for (uint32_t i = 0; i < n; i++)
-    {
-        reads[i].name = names[i] ? names[i] : "";
-        reads[i].seq.assign((const char*)seq + seqOffset[i], seqLen[i]);
-        km.clear();
-        for (uint32_t k = 0; k < counts[i]; k++)
-        {
-            const auto& m = matches[matchOff[i] + k];
-            km.push_back(gahost::KmerMatch { m.pos, m.start, m.count });
-        }
-        gahost::selectSeeds(*a->graph, a->index, reads[i].seq, a->params.minimizer_density, km, reads[i].seeds);
-        if (!reads[i].seeds.empty()) a->stats.reads_with_seeds++;
-    }
+    std::vector<gahost::ReadInput> reads;
+    int rc = ga_aligner_seed(a, n, names, seq, seqOffset, seqLen, reads);
+    if (rc != GA_OK) return rc;
+    for (const auto& r : reads) if (!r.seeds.empty()) a->stats.reads_with_seeds++;
     a->stats.seed_ms = ms_since(ts);
     // ---- seed loops, extensions on the GPU ----
-    gahost::ReadAlignParams rp;
-    rp.sloppy = a->params.sloppy != 0;
-    rp.minClusterSize = a->params.min_cluster_size;
-    rp.seedExtendDensity = a->params.seed_extend_density;
-    rp.xscoreErrorCost = a->params.extend.xscore_error_cost;
-    rp.minAlignmentScore = a->params.min_alignment_score;
-    rp.multimapScoreFraction = a->params.multimap_score_fraction;
-    rp.cigarMatchMismatchMerge = a->params.cigar_match_mismatch != 0;
+    gahost::ReadAlignParams rp = ga_aligner_read_params(a);
     std::vector<gahost::ReadOutput> outs;
     gahost::BatchStats bs;
-    gahost::alignBatch(*a->graph, rp, reads, extend_callback, a, outs, bs);
+    gahost::alignBatch(*a->graph, rp, reads, ga_aligner_extend, a, outs, bs);
     for (uint32_t i = 0; i < n; i++)
     {
         a->gaf += outs[i].gaf;

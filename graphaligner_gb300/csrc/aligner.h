@@ -1,0 +1,41 @@
+// State of one read-level aligner (ga_aligner_t) shared by align_abi.cu and serve.cpp.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "readalign.h"
+#include "seed_kernel.cuh"
+#include "../../include/graphaligner_gb300.h"
+
+struct ga_aligner
+{
+    ga_extender_t ext = nullptr;
+    int device = 0;
+    ga_align_params params {};
+    gahost::HostGraph* graph = nullptr;
+    gahost::MinimizerIndex index;
+    gadev::SeedSlot* slots = nullptr;
+    uint64_t capacity = 0;
+    std::string gaf;
+    std::vector<uint64_t> readBp;
+    ga_align_stats stats {};
+    uint64_t launches = 0;
+    cudaStream_t stream = nullptr;
+    // staging of one extension batch
+    std::vector<uint8_t> blob;
+    std::vector<uint64_t> off, toff;
+    std::vector<uint32_t> len, node, nodeOff, cap, tlen;
+    std::vector<int32_t> status, score;
+    std::vector<uint64_t> items, steps;
+};
+
+// MinimizerSeeder::getSeeds for a batch of reads: k-mer lookups on the GPU, the
+// least-frequent selection on the host.  Fills reads[i].name/seq/seeds.
+int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const uint8_t* seq, const uint64_t* seqOffset,
+    const uint32_t* seqLen, std::vector<gahost::ReadInput>& reads);
+
+// gahost::ExtendFn over ga_extend_batch (ctx = ga_aligner*)
+void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs);
+
+// the seed loop parameters of ga_align_params
+gahost::ReadAlignParams ga_aligner_read_params(const ga_aligner* a);

@@ -544,14 +544,6 @@ std::string gafLine(const HostGraph& g, const std::string& readName, const std::
 
 // ------------------------------------------------------------------ the batched seed loop
 
-struct PendingExtension
-{
-    size_t read;
-    size_t seed;
-    int64_t backward = -1;  // batch index or -1
-    int64_t forward = -1;
-};
-
 struct ReadState
 {
     std::string name;
@@ -706,188 +698,275 @@ static void finishSeed(const HostGraph& g, const ReadAlignParams& p, ReadState& 
     }
 }
 
+// Aligner.cpp:505-566: selection, bp aligned, order by X-score, GAF
+static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState& r, ReadOutput& o, BatchStats& stats)
+{
+    if (r.failed)
+    {
+        o.failed = true;
+        stats.failedReads++;
+        return;
+    }
+    if (r.alignments.empty()) return;
+    try
+    {
+        std::vector<AlignmentItem> alns = selectAlignments(r.alignments, p.minAlignmentScore, p.multimapScoreFraction);
+        if (alns.empty()) return;
+        std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentStart < b.alignmentStart; });
+        size_t bpAligned = 0, lastEnd = 0;
+        for (const auto& a : alns)
+        {
+            size_t countStart = std::max(lastEnd, a.alignmentStart);
+            if (a.alignmentEnd > countStart)
+            {
+                bpAligned += a.alignmentEnd - countStart;
+                lastEnd = a.alignmentEnd;
+            }
+        }
+        std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentXScore > b.alignmentXScore; });
+        std::string text;
+        for (auto& a : alns)
+        {
+            text += gafLine(g, r.name, r.seq, *a.trace, a.alignmentXScore, a.mappingQuality, p.cigarMatchMismatchMerge);
+            text += '\n';
+        }
+        o.gaf = std::move(text);
+        o.bpAligned = bpAligned;
+        o.alignments = alns.size();
+        stats.bpAligned += bpAligned;
+    }
+    catch (const ReadFailure&)
+    {
+        o.failed = true;
+        o.gaf.clear();
+        stats.failedReads++;
+    }
+}
+
+struct SeedLoopPool::Impl
+{
+    const HostGraph& g;
+    const ReadAlignParams p;
+    struct Live
+    {
+        std::unique_ptr<ReadState> r;
+        uint64_t tag;
+        bool noSeeds = false;
+    };
+    std::vector<Live> live;          // reads in their seed loops
+    std::vector<Live> finished;      // loop ended or failed; finalized by takeFinished
+    struct Pending
+    {
+        ReadState* r;
+        size_t seed;
+        int64_t backward = -1;       // request index or -1
+        int64_t forward = -1;
+    };
+    std::vector<Pending> pending;
+    std::vector<ExtensionRequest> requests;
+    Impl(const HostGraph& g_, const ReadAlignParams& p_) : g(g_), p(p_) {}
+};
+
+SeedLoopPool::SeedLoopPool(const HostGraph& g, const ReadAlignParams& p) : impl(new Impl(g, p)) {}
+SeedLoopPool::~SeedLoopPool() = default;
+
+size_t SeedLoopPool::active() const { return impl->live.size() + impl->finished.size(); }
+
+void SeedLoopPool::add(ReadInput&& read, uint64_t tag)
+{
+    Impl::Live l;
+    l.r.reset(new ReadState());
+    l.tag = tag;
+    ReadState& r = *l.r;
+    r.name = std::move(read.name);
+    r.seq = std::move(read.seq);
+    r.seeds = std::move(read.seeds);
+    if (r.seeds.size() == 0)
+    {
+        r.done = true;
+        l.noSeeds = true;
+        impl->finished.push_back(std::move(l));
+        return;
+    }
+    try
+    {
+        orderSeeds(impl->g, r.seeds);
+        r.rev = reverseComplement(r.seq);
+    }
+    catch (const ReadFailure&)
+    {
+        r.done = true;
+        r.failed = true;
+        impl->finished.push_back(std::move(l));
+        return;
+    }
+    r.extendSeeds = (size_t)(impl->p.seedExtendDensity * r.seq.size() + 1);
+    if (impl->p.seedExtendDensity == -1) r.extendSeeds = r.seeds.size();
+    impl->live.push_back(std::move(l));
+}
+
+bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
+{
+    const HostGraph& g = impl->g;
+    auto& pending = impl->pending;
+    pending.clear();
+    requests.clear();
+    size_t keep = 0;
+    for (size_t i = 0; i < impl->live.size(); i++)
+    {
+        Impl::Live& l = impl->live[i];
+        ReadState& r = *l.r;
+        size_t seedIndex = 0;
+        bool more = false;
+        try
+        {
+            more = nextSeed(impl->p, r, seedIndex);
+        }
+        catch (const ReadFailure&)
+        {
+            r.failed = true;
+        }
+        if (!more)
+        {
+            r.done = true;
+            impl->finished.push_back(std::move(l));
+            continue;
+        }
+        const SeedHit& s = r.seeds[seedIndex];
+        Impl::Pending pe;
+        pe.r = &r;
+        pe.seed = seedIndex;
+        int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
+        const size_t firstRequest = requests.size();
+        try
+        {
+            GAH_ASSERT(s.seqPos < r.seq.size());
+            if (s.seqPos > 0)
+            {
+                auto rp = g.reversePosition(forwardNodeId, s.nodeOffset);
+                ExtensionRequest q;
+                q.seq = r.rev.data() + r.rev.size() - s.seqPos;
+                q.len = s.seqPos;
+                q.bignode = rp.first;
+                q.offset = rp.second;
+                size_t node = g.unitigNode(q.bignode, q.offset);
+                q.node = (uint32_t)node;
+                q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
+                pe.backward = (int64_t)requests.size();
+                requests.push_back(q);
+            }
+            if (s.seqPos < r.seq.size() - 1)
+            {
+                ExtensionRequest q;
+                q.seq = r.seq.data() + s.seqPos + 1;
+                q.len = r.seq.size() - s.seqPos - 1;
+                q.bignode = forwardNodeId;
+                q.offset = s.nodeOffset;
+                size_t node = g.unitigNode(q.bignode, q.offset);
+                q.node = (uint32_t)node;
+                q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
+                pe.forward = (int64_t)requests.size();
+                requests.push_back(q);
+            }
+        }
+        catch (const ReadFailure&)
+        {
+            requests.resize(firstRequest);
+            r.failed = true;
+            r.done = true;
+            impl->finished.push_back(std::move(l));
+            continue;
+        }
+        pending.push_back(pe);
+        if (keep != i) impl->live[keep] = std::move(l);
+        keep++;
+    }
+    impl->live.resize(keep);
+    impl->requests = requests;
+    return !pending.empty();
+}
+
+void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchStats& stats)
+{
+    const HostGraph& g = impl->g;
+    const auto& requests = impl->requests;
+    stats.rounds++;
+    stats.extensions += requests.size();
+    for (const auto& pe : impl->pending)
+    {
+        ReadState& r = *pe.r;
+        const SeedHit& s = r.seeds[pe.seed];
+        int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
+        int backwardNodeId = s.reverse ? s.nodeID * 2 : s.nodeID * 2 + 1;
+        try
+        {
+            for (int64_t k : { pe.backward, pe.forward })
+            {
+                if (k >= 0)
+                {
+                    stats.cellSteps += results[k].steps;
+                    if (results[k].status == GA_ASSERT || results[k].status == GA_CAPACITY || results[k].status == GA_BAD_REQUEST) throw ReadFailure {};
+                }
+            }
+            OnewayTrace bw, fw;
+            bw.score = INT32_MAX;
+            fw.score = INT32_MAX;
+            if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], std::string(requests[pe.backward].seq, requests[pe.backward].len));
+            if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], std::string(requests[pe.forward].seq, requests[pe.forward].len));
+            finishSeed(g, impl->p, r, s, std::move(bw), std::move(fw), backwardNodeId, forwardNodeId);
+        }
+        catch (const ReadFailure&)
+        {
+            r.failed = true;
+        }
+    }
+    impl->pending.clear();
+    // a read that failed in this round leaves its loop now
+    size_t keep = 0;
+    for (size_t i = 0; i < impl->live.size(); i++)
+    {
+        Impl::Live& l = impl->live[i];
+        if (l.r->failed)
+        {
+            l.r->done = true;
+            impl->finished.push_back(std::move(l));
+            continue;
+        }
+        if (keep != i) impl->live[keep] = std::move(l);
+        keep++;
+    }
+    impl->live.resize(keep);
+}
+
+void SeedLoopPool::takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats)
+{
+    for (auto& l : impl->finished)
+    {
+        ReadOutput o;
+        o.noSeeds = l.noSeeds;
+        finalizeRead(impl->g, impl->p, *l.r, o, stats);
+        out.emplace_back(l.tag, std::move(o));
+    }
+    impl->finished.clear();
+}
+
 void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,
     std::vector<ReadOutput>& out, BatchStats& stats)
 {
-    std::vector<ReadState> st(reads.size());
     out.assign(reads.size(), ReadOutput {});
-    for (size_t i = 0; i < reads.size(); i++)
-    {
-        st[i].name = reads[i].name;
-        st[i].seq = reads[i].seq;
-        st[i].seeds = std::move(reads[i].seeds);
-        if (st[i].seeds.size() == 0)
-        {
-            st[i].done = true;
-            out[i].noSeeds = true;
-            continue;
-        }
-        try
-        {
-            orderSeeds(g, st[i].seeds);
-            st[i].rev = reverseComplement(st[i].seq);
-        }
-        catch (const ReadFailure&)
-        {
-            st[i].done = true;
-            st[i].failed = true;
-        }
-        st[i].extendSeeds = (size_t)(p.seedExtendDensity * st[i].seq.size() + 1);
-        if (p.seedExtendDensity == -1) st[i].extendSeeds = st[i].seeds.size();
-    }
-    std::vector<PendingExtension> pending;
+    SeedLoopPool pool(g, p);
+    for (size_t i = 0; i < reads.size(); i++) pool.add(std::move(reads[i]), i);
     std::vector<ExtensionRequest> requests;
     std::vector<ExtensionResult> results;
-    while (true)
+    while (pool.collect(requests))
     {
-        pending.clear();
-        requests.clear();
-        for (size_t i = 0; i < st.size(); i++)
-        {
-            ReadState& r = st[i];
-            if (r.done) continue;
-            size_t seedIndex = 0;
-            bool more;
-            try
-            {
-                more = nextSeed(p, r, seedIndex);
-            }
-            catch (const ReadFailure&)
-            {
-                r.failed = true;
-                r.done = true;
-                continue;
-            }
-            if (!more)
-            {
-                r.done = true;
-                continue;
-            }
-            const SeedHit& s = r.seeds[seedIndex];
-            PendingExtension pe;
-            pe.read = i;
-            pe.seed = seedIndex;
-            int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
-            try
-            {
-                GAH_ASSERT(s.seqPos < r.seq.size());
-                if (s.seqPos > 0)
-                {
-                    auto rp = g.reversePosition(forwardNodeId, s.nodeOffset);
-                    ExtensionRequest q;
-                    q.seq = r.rev.data() + r.rev.size() - s.seqPos;
-                    q.len = s.seqPos;
-                    q.bignode = rp.first;
-                    q.offset = rp.second;
-                    size_t node = g.unitigNode(q.bignode, q.offset);
-                    q.node = (uint32_t)node;
-                    q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
-                    pe.backward = (int64_t)requests.size();
-                    requests.push_back(q);
-                }
-                if (s.seqPos < r.seq.size() - 1)
-                {
-                    ExtensionRequest q;
-                    q.seq = r.seq.data() + s.seqPos + 1;
-                    q.len = r.seq.size() - s.seqPos - 1;
-                    q.bignode = forwardNodeId;
-                    q.offset = s.nodeOffset;
-                    size_t node = g.unitigNode(q.bignode, q.offset);
-                    q.node = (uint32_t)node;
-                    q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
-                    pe.forward = (int64_t)requests.size();
-                    requests.push_back(q);
-                }
-            }
-            catch (const ReadFailure&)
-            {
-                r.failed = true;
-                r.done = true;
-                continue;
-            }
-            pending.push_back(pe);
-        }
-        if (pending.empty()) break;
-        stats.rounds++;
-        stats.extensions += requests.size();
         results.assign(requests.size(), ExtensionResult {});
         if (!requests.empty()) extend(ctx, requests, results);
-        for (const auto& pe : pending)
-        {
-            ReadState& r = st[pe.read];
-            const SeedHit& s = r.seeds[pe.seed];
-            int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
-            int backwardNodeId = s.reverse ? s.nodeID * 2 : s.nodeID * 2 + 1;
-            try
-            {
-                for (int64_t k : { pe.backward, pe.forward })
-                {
-                    if (k >= 0)
-                    {
-                        stats.cellSteps += results[k].steps;
-                        if (results[k].status == GA_ASSERT || results[k].status == GA_CAPACITY || results[k].status == GA_BAD_REQUEST) throw ReadFailure {};
-                    }
-                }
-                OnewayTrace bw, fw;
-                bw.score = INT32_MAX;
-                fw.score = INT32_MAX;
-                if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], std::string(requests[pe.backward].seq, requests[pe.backward].len));
-                if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], std::string(requests[pe.forward].seq, requests[pe.forward].len));
-                finishSeed(g, p, r, s, std::move(bw), std::move(fw), backwardNodeId, forwardNodeId);
-            }
-            catch (const ReadFailure&)
-            {
-                r.failed = true;
-                r.done = true;
-            }
-        }
+        pool.consume(results, stats);
     }
-    // Aligner.cpp:505-566: selection, bp aligned, order, GAF
-    for (size_t i = 0; i < st.size(); i++)
-    {
-        ReadState& r = st[i];
-        ReadOutput& o = out[i];
-        if (r.failed)
-        {
-            o.failed = true;
-            stats.failedReads++;
-            continue;
-        }
-        if (r.alignments.empty()) continue;
-        try
-        {
-            std::vector<AlignmentItem> alns = selectAlignments(r.alignments, p.minAlignmentScore, p.multimapScoreFraction);
-            if (alns.empty()) continue;
-            std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentStart < b.alignmentStart; });
-            size_t bpAligned = 0, lastEnd = 0;
-            for (const auto& a : alns)
-            {
-                size_t countStart = std::max(lastEnd, a.alignmentStart);
-                if (a.alignmentEnd > countStart)
-                {
-                    bpAligned += a.alignmentEnd - countStart;
-                    lastEnd = a.alignmentEnd;
-                }
-            }
-            std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentXScore > b.alignmentXScore; });
-            std::string text;
-            for (auto& a : alns)
-            {
-                text += gafLine(g, r.name, r.seq, *a.trace, a.alignmentXScore, a.mappingQuality, p.cigarMatchMismatchMerge);
-                text += '\n';
-            }
-            o.gaf = std::move(text);
-            o.bpAligned = bpAligned;
-            o.alignments = alns.size();
-            stats.bpAligned += bpAligned;
-        }
-        catch (const ReadFailure&)
-        {
-            o.failed = true;
-            o.gaf.clear();
-            stats.failedReads++;
-        }
-    }
+    std::vector<std::pair<uint64_t, ReadOutput>> done;
+    pool.takeFinished(done, stats);
+    for (auto& d : done) out[d.first] = std::move(d.second);
 }
 
 }

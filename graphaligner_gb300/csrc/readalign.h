@@ -135,6 +135,30 @@ struct ExtensionResult
 typedef void (*ExtendFn)(void* ctx, const std::vector<ExtensionRequest>& requests, std::vector<ExtensionResult>& results);
 
 void orderSeeds(const HostGraph& g, std::vector<SeedHit>& seedHits);
+
+// Reads in their seed loops (GraphAligner::AlignOneWay, GraphAligner.h:94-181), advanced
+// in lock step: each round asks for the next seed's two extensions of every read.  Reads
+// can join between rounds, so a round's extensions mix reads at different stages.
+class SeedLoopPool
+{
+public:
+    SeedLoopPool(const HostGraph& g, const ReadAlignParams& p);
+    ~SeedLoopPool();
+    void add(ReadInput&& read, uint64_t tag);
+    // reads joined and not yet taken out by takeFinished
+    size_t active() const;
+    // the next extension requests (they point into the pool's reads); false when no read
+    // needs one.  Reads whose seed loop ended move to the finished list.
+    bool collect(std::vector<ExtensionRequest>& requests);
+    // results of the requests of the last collect, in the same order
+    void consume(const std::vector<ExtensionResult>& results, BatchStats& stats);
+    // selection, aligned bp and GAF of the finished reads (Aligner.cpp:505-566), with their tags
+    void takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats);
+private:
+    struct Impl;
+    std::unique_ptr<Impl> impl;
+};
+
 void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,
     std::vector<ReadOutput>& out, BatchStats& stats);
 

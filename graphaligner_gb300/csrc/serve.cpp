@@ -1,0 +1,272 @@
+// Serving loop over one resident graph and minimizer table: continuous batching of
+// reads through seeding, the batched seed loop and GAF output (the request side of
+// Aligner.cpp:440-592).
+//
+// One worker thread owns the GPU work.  Each turn of its loop
+//   1. admits queued reads while the reads in flight stay under max_reads_in_flight
+//      and their estimated band memory (read bp x band_bytes_per_bp) under
+//      max_band_bytes -- a read that alone exceeds the budget is admitted when
+//      nothing else is in flight;
+//   2. seeds the admitted group (one k-mer lookup launch, host selection);
+//   3. runs one round: the next seed's two extensions of every read in flight,
+//      old and new together, as one ga_extend_batch;
+//   4. publishes reads whose seed loop ended (selection + GAF) to the poll queue.
+// A read's seed loop only ever sees its own extensions' results and the
+// extensions are independent DP runs, so its GAF bytes are the same whichever
+// reads share its rounds.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+#include "aligner.h"
+
+void ga_set_last_error(const char* msg);
+
+namespace
+{
+using Clock = std::chrono::steady_clock;
+
+double ms_between(Clock::time_point a, Clock::time_point b)
+{
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct Submitted
+{
+    uint64_t ticket;
+    std::string name;
+    std::string seq;
+    Clock::time_point submit;
+};
+
+struct Flight
+{
+    Clock::time_point submit;
+    Clock::time_point admit;
+    uint64_t bytes;
+    uint64_t group;
+};
+}
+
+struct ga_server
+{
+    ga_aligner* a = nullptr;
+    uint32_t maxReads = 4096;
+    uint64_t budget = 2ULL << 30;
+    uint32_t bytesPerBp = 32;
+    std::mutex mu;
+    std::condition_variable cvWork, cvDone;
+    std::deque<Submitted> queue;
+    std::deque<ga_server_result> done;
+    std::unordered_map<uint64_t, std::string> texts;
+    uint64_t nextTicket = 1;
+    bool stop = false;
+    ga_server_stats stats {};
+    std::thread worker;
+};
+
+static void serve_loop(ga_server* s)
+{
+    ga_aligner* a = s->a;
+    cudaSetDevice(a->device);
+    gahost::SeedLoopPool pool(*a->graph, ga_aligner_read_params(a));
+    gahost::BatchStats bs;
+    std::vector<gahost::ExtensionRequest> rq;
+    std::vector<gahost::ExtensionResult> rs;
+    std::vector<std::pair<uint64_t, gahost::ReadOutput>> fin;
+    std::vector<std::pair<uint64_t, int32_t>> failedSeeding;
+    std::unordered_map<uint64_t, Flight> flight;
+    std::map<uint64_t, size_t> groupsInFlight;     // admission group -> reads of it in flight
+    uint64_t inflightBytes = 0;
+    uint64_t group = 0;
+    while (true)
+    {
+        std::vector<Submitted> adm;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (flight.empty()) s->cvWork.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+            if (flight.empty() && s->queue.empty() && s->stop) break;
+            while (!s->queue.empty() && flight.size() + adm.size() < s->maxReads)
+            {
+                const uint64_t b = (uint64_t)s->queue.front().seq.size() * s->bytesPerBp;
+                if ((flight.size() + adm.size()) > 0 && inflightBytes + b > s->budget) break;
+                inflightBytes += b;
+                adm.push_back(std::move(s->queue.front()));
+                s->queue.pop_front();
+            }
+        }
+        const auto t0 = Clock::now();
+        if (!adm.empty())
+        {
+            group++;
+            const uint32_t n = (uint32_t)adm.size();
+            std::vector<const char*> names(n);
+            std::vector<uint64_t> offs(n);
+            std::vector<uint32_t> lens(n);
+            std::string blob;
+            for (uint32_t i = 0; i < n; i++)
+            {
+                names[i] = adm[i].name.c_str();
+                offs[i] = blob.size();
+                lens[i] = (uint32_t)adm[i].seq.size();
+                blob += adm[i].seq;
+            }
+            std::vector<gahost::ReadInput> reads;
+            const int rc = ga_aligner_seed(a, n, names.data(), (const uint8_t*)blob.data(), offs.data(), lens.data(), reads);
+            const auto now = Clock::now();
+            for (uint32_t i = 0; i < n; i++)
+            {
+                flight[adm[i].ticket] = Flight { adm[i].submit, now, (uint64_t)adm[i].seq.size() * s->bytesPerBp, group };
+                groupsInFlight[group]++;
+                if (rc != GA_OK) failedSeeding.emplace_back(adm[i].ticket, rc);
+                else pool.add(std::move(reads[i]), adm[i].ticket);
+            }
+            s->stats.admissions++;
+        }
+        if (pool.collect(rq))
+        {
+            rs.assign(rq.size(), gahost::ExtensionResult {});
+            if (!rq.empty()) ga_aligner_extend(a, rq, rs);
+            pool.consume(rs, bs);
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stats.rounds++;
+            s->stats.extensions += rq.size();
+            if (groupsInFlight.size() > 1) s->stats.mixed_rounds++;
+        }
+        pool.takeFinished(fin, bs);
+        const auto tDone = Clock::now();
+        if (!fin.empty() || !failedSeeding.empty())
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            auto publish = [&](uint64_t ticket, int32_t status, const gahost::ReadOutput* o)
+            {
+                auto f = flight.find(ticket);
+                ga_server_result r {};
+                r.ticket = ticket;
+                r.status = status;
+                std::string& text = s->texts[ticket];
+                if (o)
+                {
+                    text = o->gaf;
+                    r.alignments = (uint32_t)o->alignments;
+                    r.bp_aligned = o->bpAligned;
+                }
+                r.gaf = text.c_str();
+                r.gaf_bytes = text.size();
+                r.queue_ms = ms_between(f->second.submit, f->second.admit);
+                r.latency_ms = ms_between(f->second.submit, tDone);
+                inflightBytes -= f->second.bytes;
+                auto g = groupsInFlight.find(f->second.group);
+                if (--g->second == 0) groupsInFlight.erase(g);
+                flight.erase(f);
+                s->done.push_back(r);
+                s->stats.completed++;
+            };
+            for (auto& fr : fin) publish(fr.first, fr.second.failed ? GA_ASSERT : GA_OK, &fr.second);
+            for (auto& fr : failedSeeding) publish(fr.first, fr.second, nullptr);
+            fin.clear();
+            failedSeeding.clear();
+            s->cvDone.notify_all();
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stats.max_in_flight = std::max<uint64_t>(s->stats.max_in_flight, flight.size());
+        s->stats.busy_ms += ms_between(t0, Clock::now());
+    }
+}
+
+extern "C" int ga_server_create(ga_aligner_t aligner, const ga_server_params* params, ga_server_t* out)
+{
+    if (!aligner || !out) return GA_ERR_ARGUMENT;
+    ga_server* s = new ga_server();
+    s->a = aligner;
+    if (params)
+    {
+        if (params->max_reads_in_flight) s->maxReads = params->max_reads_in_flight;
+        if (params->max_band_bytes) s->budget = params->max_band_bytes;
+        if (params->band_bytes_per_bp) s->bytesPerBp = params->band_bytes_per_bp;
+    }
+    try
+    {
+        s->worker = std::thread(serve_loop, s);
+    }
+    catch (...)
+    {
+        delete s;
+        ga_set_last_error("ga_server_create: cannot start the worker thread");
+        return GA_ERR_ARGUMENT;
+    }
+    *out = s;
+    return GA_OK;
+}
+
+extern "C" int ga_server_submit(ga_server_t s, const char* name, const uint8_t* seq, uint32_t len, uint64_t* ticket)
+{
+    if (!s || (len > 0 && !seq)) return GA_ERR_ARGUMENT;
+    Submitted q;
+    q.name = name ? name : "";
+    q.seq.assign((const char*)seq, len);
+    q.submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->stop) return GA_ERR_ARGUMENT;
+        q.ticket = s->nextTicket++;
+        if (ticket) *ticket = q.ticket;
+        s->queue.push_back(std::move(q));
+        s->stats.submitted++;
+    }
+    s->cvWork.notify_one();
+    return GA_OK;
+}
+
+extern "C" int ga_server_poll(ga_server_t s, ga_server_result* out, uint32_t max, uint32_t* count, int32_t wait_ms)
+{
+    if (!s || !count || (max > 0 && !out)) return GA_ERR_ARGUMENT;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto ready = [&] { return !s->done.empty(); };
+    if (wait_ms < 0) s->cvDone.wait(lk, ready);
+    else if (wait_ms > 0) s->cvDone.wait_for(lk, std::chrono::milliseconds(wait_ms), ready);
+    uint32_t n = 0;
+    while (n < max && !s->done.empty())
+    {
+        out[n++] = s->done.front();
+        s->done.pop_front();
+    }
+    *count = n;
+    return GA_OK;
+}
+
+extern "C" int ga_server_release(ga_server_t s, uint64_t ticket)
+{
+    if (!s) return GA_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->texts.erase(ticket);
+    return GA_OK;
+}
+
+extern "C" int ga_server_stats_get(ga_server_t s, ga_server_stats* out)
+{
+    if (!s || !out) return GA_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    return GA_OK;
+}
+
+extern "C" int ga_server_free(ga_server_t s)
+{
+    if (!s) return GA_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cvWork.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    delete s;
+    return GA_OK;
+}

@@ -222,6 +222,57 @@ int ga_aligner_gaf(ga_aligner_t aligner, const char** text, uint64_t* bytes);
 int ga_aligner_read_bp(ga_aligner_t aligner, uint64_t* bp_per_read);
 int ga_aligner_stats(ga_aligner_t aligner, ga_align_stats* out);
 
+/* ---- serving loop ----
+ * The request side of Aligner.cpp's worker loop (Aligner.cpp:440-592, one read per
+ * loop iteration there) as continuous batching: reads are submitted one at a time
+ * from any thread; a worker thread admits them while the reads in flight and their
+ * estimated band memory stay under the limits, seeds each admitted group on the GPU,
+ * and runs one extension batch per round over every read in flight, so reads that
+ * arrive while others are on the GPU join the next round and share its launch.  A
+ * read's GAF bytes do not depend on which other reads share its rounds.
+ * The graph, the DP arrays and the minimizer table stay resident on the device. */
+typedef struct ga_server_params {
+    uint32_t max_reads_in_flight;     /* reads in their seed loops at once; 0 = 4096 */
+    uint64_t max_band_bytes;          /* admission budget of estimated band + trace memory; 0 = 2 GiB */
+    uint32_t band_bytes_per_bp;       /* the estimate per read bp; 0 = 32 */
+} ga_server_params;
+
+typedef struct ga_server_result {
+    uint64_t ticket;
+    int32_t  status;                  /* GA_OK, GA_ASSERT (dropped as Aligner.cpp:493-500 does), or an error */
+    uint32_t alignments;              /* GAF lines */
+    uint64_t bp_aligned;
+    const char* gaf;                  /* valid until ga_server_release(ticket) */
+    uint64_t gaf_bytes;
+    double   queue_ms;                /* submit -> admitted */
+    double   latency_ms;              /* submit -> GAF ready */
+} ga_server_result;
+
+typedef struct ga_server_stats {
+    uint64_t submitted;
+    uint64_t completed;
+    uint64_t rounds;                  /* extension batches launched */
+    uint64_t extensions;
+    uint64_t admissions;              /* admitted groups (one seeding launch each) */
+    uint64_t max_in_flight;
+    uint64_t mixed_rounds;            /* rounds whose reads were admitted in different groups */
+    double   busy_ms;                 /* worker time spent seeding, extending and finishing */
+} ga_server_stats;
+
+typedef struct ga_server* ga_server_t;
+/* Starts the worker thread.  The aligner must outlive the server and must not be
+ * used by other calls meanwhile. */
+int ga_server_create(ga_aligner_t aligner, const ga_server_params* params, ga_server_t* out);
+/* Copies the read and queues it; returns at once with a ticket (from 1 up). */
+int ga_server_submit(ga_server_t server, const char* name, const uint8_t* seq, uint32_t len, uint64_t* ticket);
+/* Up to max finished reads, waiting up to wait_ms (0: no wait, -1: until one is ready). */
+int ga_server_poll(ga_server_t server, ga_server_result* out, uint32_t max, uint32_t* count, int32_t wait_ms);
+/* Frees the GAF text of a polled result. */
+int ga_server_release(ga_server_t server, uint64_t ticket);
+int ga_server_stats_get(ga_server_t server, ga_server_stats* out);
+/* Finishes every submitted read, stops the worker and frees the server. */
+int ga_server_free(ga_server_t server);
+
 const char* ga_last_error(void);
 const char* ga_version(void);
 

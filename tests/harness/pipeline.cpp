@@ -148,8 +148,11 @@ int main(int argc, char** argv)
         }
         return 0;
     }
-    // gaf (-x vg, AlignerMain.cpp:170-177) or gafdbg (-x dbg, AlignerMain.cpp:160-168), with the given bandwidth
+    // gaf (-x vg, AlignerMain.cpp:170-177), gafdbg (-x dbg, AlignerMain.cpp:160-168) or gafmix
+    // (-x vg with reads joining the seed-loop pool a few per round), with the given bandwidth
     const bool dbg = mode == "gafdbg";
+    const bool mixed = mode == "gafmix";
+    const size_t joinPerRound = 7;
     size_t bw = std::stoul(argv[4]);
     uint64_t maxCells = (argc > 5 && std::string(argv[5]) != "-") ? std::stoull(argv[5]) : (dbg ? 10000 : UINT64_MAX);
     gahost::MinimizerIndex idx;
@@ -168,7 +171,33 @@ int main(int argc, char** argv)
     if (dbg) p.seedExtendDensity = 0.002;
     std::vector<gahost::ReadOutput> out;
     gahost::BatchStats st;
-    gahost::alignBatch(graph, p, in, oracleExtend, &ctx, out, st);
+    if (mixed)
+    {
+        // continuous admission: a few reads join the pool before every round, so
+        // rounds hold reads at different stages of their seed loops
+        gahost::SeedLoopPool pool(graph, p);
+        std::vector<gahost::ExtensionRequest> rq;
+        std::vector<gahost::ExtensionResult> rs;
+        std::vector<std::pair<uint64_t, gahost::ReadOutput>> fin;
+        out.assign(in.size(), gahost::ReadOutput {});
+        size_t next = 0;
+        while (true)
+        {
+            for (size_t k = 0; k < joinPerRound && next < in.size(); k++, next++) pool.add(std::move(in[next]), next);
+            const bool any = pool.collect(rq);
+            if (any)
+            {
+                rs.assign(rq.size(), gahost::ExtensionResult {});
+                if (!rq.empty()) oracleExtend(&ctx, rq, rs);
+                pool.consume(rs, st);
+            }
+            pool.takeFinished(fin, st);
+            for (auto& f : fin) out[f.first] = std::move(f.second);
+            fin.clear();
+            if (!any && next == in.size() && pool.active() == 0) break;
+        }
+    }
+    else gahost::alignBatch(graph, p, in, oracleExtend, &ctx, out, st);
     for (auto& o : out) std::cout << o.gaf;
     std::cerr << "rounds " << st.rounds << " extensions " << st.extensions << " bp " << st.bpAligned << " failed " << st.failedReads << std::endl;
     return 0;

@@ -48,6 +48,14 @@ def test_gaf_matches_reference(harness, oracle_lib, bandwidth):
     assert out == load_gaf("vg50k", bandwidth)
 
 
+def test_gaf_same_when_reads_join_between_rounds(harness, oracle_lib):
+    """Reads admitted 7 per round (the serving loop's continuous batching): every
+    read's GAF is the reference's, byte for byte."""
+    exe, gag, reads, _ = harness
+    out = subprocess.run([exe, gag, reads, "gafmix", "10"], check=True, capture_output=True, text=True).stdout
+    assert out == load_gaf("vg50k", 10)
+
+
 def test_gaf_matches_reference_dbg(harness, oracle_lib, tmp_path):
     """-x dbg on a k=63 de Bruijn graph with cyclic components."""
     exe = harness[0]
