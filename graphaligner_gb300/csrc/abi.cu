@@ -313,25 +313,28 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
         fa.prevStatus = round > 0 ? prevStatus : nullptr;
         ta.prevStatus = fa.prevStatus;
         const uint32_t ded = round == 0 ? dedicated : 0;
-        const uint64_t dedSlots = (uint64_t)ded * 32;
+        // every thread of a launch owns one workspace slot: the dedicated launch gets whole
+        // blocks at the top of the slot range, the bulk launch whole blocks below them
+        const int dedGrid = (int)(((uint64_t)ded * 32 + x->block - 1) / x->block);
+        const uint64_t dedSlots = (uint64_t)dedGrid * x->block;
         const uint64_t bulkSlots = slots > dedSlots ? slots - dedSlots : 0;
         const uint32_t bulkCount = n - ded;
-        int bulkGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>(bulkSlots / x->block, ((uint64_t)bulkCount + x->block - 1) / x->block));
-        int dedGrid = (int)((dedSlots + x->block - 1) / x->block);
+        if (bulkCount > 0 && bulkSlots < (uint64_t)x->block) return fail(GA_ERR_CUDA, "workspace too small for the batch's capacities");
+        const int bulkGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>(bulkSlots / x->block, ((uint64_t)bulkCount + x->block - 1) / x->block));
         GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), stream));
         GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, sizeof(unsigned long long), stream));
         GA_CUDA(cudaEventRecord(x->ev[0], stream));
         if (ded > 0)
         {
             GA_CUDA(cudaStreamWaitEvent(x->side, x->ev[0], 0));
-            ga_launch_extend(fa, ta, 1, 0, ded, x->counters + 3, (uint32_t)bulkSlots, dedGrid, x->block, x->side);
+            ga_launch_extend(fa, ta, 1, 0, ded, x->counters + 3, (uint32_t)bulkSlots, (uint32_t)(bulkSlots + dedSlots), dedGrid, x->block, x->side);
             GA_CUDA(cudaGetLastError());
             GA_CUDA(cudaEventRecord(x->ev[3], x->side));
             x->lastLaunches += 1;
         }
         if (bulkCount > 0)
         {
-            ga_launch_extend(fa, ta, 32, ded, bulkCount, x->counters, 0, bulkGrid, x->block, stream);
+            ga_launch_extend(fa, ta, 32, ded, bulkCount, x->counters, 0, (uint32_t)bulkSlots, bulkGrid, x->block, stream);
             GA_CUDA(cudaGetLastError());
             x->lastLaunches += 1;
         }

@@ -1313,9 +1313,11 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
 // similar length; with lanesPerWarp = 1 a warp runs one extension on lane 0 alone,
 // which keeps the longest extensions free of divergence with their neighbours.
 __global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, u32 lanesPerWarp, u32 first, u32 count,
-    u32* counter, u32 slotBase)
+    u32* counter, u32 slotBase, u32 slotLimit)
 {
     const u32 slot = slotBase + blockIdx.x * blockDim.x + threadIdx.x;
+    // a warp whose slots are not all inside [slotBase, slotLimit) touches no workspace (warp-uniform)
+    if (slotBase + blockIdx.x * blockDim.x + (threadIdx.x & ~31u) + 32 > slotLimit) return;
     Workspace w = workspace_at(fa.workspace + (u64)slot * fa.workspaceStride, fa.caps);
     u32 gen = w.header[0];
     ArenaCursor arena;
@@ -1352,9 +1354,9 @@ __global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, 
 }
 
 void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t lanesPerWarp, uint32_t first, uint32_t count,
-    uint32_t* counter, uint32_t slotBase, int grid, int block, void* stream)
+    uint32_t* counter, uint32_t slotBase, uint32_t slotLimit, int grid, int block, void* stream)
 {
-    gadev::extend_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(fa, ta, lanesPerWarp, first, count, counter, slotBase);
+    gadev::extend_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(fa, ta, lanesPerWarp, first, count, counter, slotBase, slotLimit);
 }
 
 int ga_upload_tables()
