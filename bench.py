@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--cpu-sample-bp", type=float, default=200e6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=300, help="extensions timed one launch each (0: skip)")
+    ap.add_argument("--workload", default="extend", choices=["extend", "reads-vg", "reads-dbg", "pipeline", "serve"],
+                    help="extend: the batched-extension line; the others print read-level lines")
+    ap.add_argument("--reads-n", type=int, default=0, help="reads of a read-level workload (0: its default)")
+    ap.add_argument("--rates", default="50,100,200,400", help="serve: Poisson arrival rates, reads/s")
+    ap.add_argument("--plain-reads", type=int, default=40, help="serve: reads timed one ga_align_reads call each")
     return ap.parse_args()
 
 
@@ -190,11 +195,150 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+READ_WORKLOADS = {
+    "reads-vg": "read-level -x vg: 50 kbp VG (bubble/200 bp, 70% SNP, 30% indel 1-20 bp), 200 reads U[5,15] kbp at 10% error",
+    "reads-dbg": "read-level -x dbg: k=63 dBG of a 10 Mbp genome + 200 copies of a 5 kbp repeat (1-3% div.) + 400 tandem arrays (period 2-50), 20 kbp reads at 12% error",
+    "pipeline": "read-level -x vg: 50 Mbp VG (variant/100 bp, 70% SNP, 30% indel 1-50 bp), reads log-normal N50 ~20 kbp [0.5,100] kbp at U[5,15]% error",
+    "serve": "serving -x dbg: the reads-dbg graph resident, reads log-normal N50 ~20 kbp [0.5,100] kbp at U[5,15]% error, Poisson arrivals",
+}
+
+
+def make_read_workload(name: str, n_reads: int):
+    """(graph, names, seqs, preset name, arena bytes) of a read-level workload."""
+    from graphaligner_gb300 import datagen as dg
+    from graphaligner_gb300 import graph as gg
+    if name == "reads-vg":
+        vg = dg.small_vg(0)
+        reads = dg.small_vg_reads(vg, n_reads or 200, 1)
+        return gg.build_from_gfa(vg.to_gfa()), reads, "vg"
+    if name in ("reads-dbg", "serve"):
+        genome = dg.stress_dbg_genome(0)
+        g = gg.build_from_gfa(dg.compact_dbg(genome, 63))
+        if name == "reads-dbg":
+            reads = dg.dbg_reads(genome, n_reads or 2000, 20_000, 0.12, 1)
+        else:
+            reads = dg.sample_genome_reads(genome, n_reads or 4000, 2, dg.lognormal_length(15_600, 0.7, 500, 100_000),
+                                           dg.uniform_error(0.05, 0.15))
+        return g, reads, "dbg"
+    if name == "pipeline":
+        vg = dg.make_variation_graph(50_000_000, 100, 0.7, 50, 0)
+        reads = dg.sample_reads(vg, n_reads or 50_000, 1, dg.lognormal_length(15_600, 0.7, 500, 100_000), dg.uniform_error(0.05, 0.15))
+        return gg.build_from_gfa(vg.to_gfa()), reads, "vg"
+    raise ValueError(name)
+
+
+def run_reads(args):
+    """Read-level lines: seeding + seed loops + extensions + selection + GAF through ga_align_reads
+    (or the ga_server_* loop for 'serve'), host buffers in, GAF text out."""
+    import torch
+    torch.cuda.set_device(0)
+    from graphaligner_gb300 import build
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    build()
+    t0 = time.perf_counter()
+    g, reads, preset_name = make_read_workload(args.workload, args.reads_n)
+    gen_s = time.perf_counter() - t0
+    names = [r.name for r in reads]
+    seqs = [r.seq for r in reads]
+    read_bp = int(sum(len(s) for s in seqs))
+    arena = int(min(96 << 30, max(4 << 30, read_bp * 24)))
+    t0 = time.perf_counter()
+    dgraph = DeviceGraph(g)
+    ext = Extender(dgraph, arena_bytes=arena)
+    aligner = Aligner(ext, g, preset(preset_name))
+    index_s = time.perf_counter() - t0
+    line = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "u64",
+            "data": "synthetic (seeded generator)", "config": {"workload": READ_WORKLOADS[args.workload], "reads": len(seqs),
+            "read_bp": read_bp, "graph_nodes": g.num_nodes, "preset": preset_name},
+            "workload_gen_s": gen_s, "graph_upload_and_index_s": index_s}
+    if args.workload == "serve":
+        line.update(run_serving(args, aligner, names, seqs))
+    else:
+        # warm-up on a slice, then timed passes over all reads
+        aligner.align(names[:64], seqs[:64])
+        with ClockSampler(0) as clocks:
+            times = []
+            for _ in range(max(1, args.steps)):
+                t = time.perf_counter()
+                gaf = aligner.align(names, seqs)
+                times.append(time.perf_counter() - t)
+        st = aligner.stats()
+        wall = statistics.median(times)
+        line.update({"value": st["bp_aligned"] / wall, "steps": len(times), "warmup": 1, "ms_per_step": wall * 1e3,
+                     "gcups": st["cell_steps"] * 64 / (st["extend_ms"] / 1e3) / 1e9 if st["extend_ms"] else None,
+                     "stats": st, "gaf_bytes": len(gaf), "clocks": clocks.summary(),
+                     "e2e": {"value": st["bp_aligned"] / wall, "unit": UNIT, "h2d_bytes_per_step": read_bp, "d2h_bytes_per_step": len(gaf)}})
+        if args.workload == "reads-vg":
+            import gzip
+            golden = os.path.join(ROOT, "tests", "golden", "vg50k_b10.gaf.gz")
+            if os.path.exists(golden):
+                line["gaf_identical_to_reference"] = gzip.open(golden, "rt").read() == gaf
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args, aligner, names, seqs):
+    """Poisson arrivals at each rate of --rates (reads/s); p50/p99 submit->GAF latency and
+    throughput, and the plain per-read form (one ga_align_reads call per read) on a sample."""
+    from graphaligner_gb300.serve import Server
+    rng = np.random.default_rng(2)
+    out = {"sweep": []}
+    rates = [float(x) for x in args.rates.split(",")]
+    per_rate = max(1, len(seqs) // len(rates))
+    pos = 0
+    for rate in rates:
+        idx = list(range(pos, min(len(seqs), pos + per_rate)))
+        pos += per_rate
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(idx)))
+        got = {}
+        with Server(aligner) as srv:
+            t0 = time.perf_counter()
+            for k, i in enumerate(idx):
+                delay = arrivals[k] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                srv.submit(names[i], seqs[i])
+                for r in srv.poll():
+                    got[r.ticket] = r
+            while len(got) < len(idx):
+                for r in srv.poll(wait_ms=200):
+                    got[r.ticket] = r
+            span = time.perf_counter() - t0
+            st = srv.stats()
+        lat = np.array([r.latency_ms for r in got.values()])
+        bp = sum(r.bp_aligned for r in got.values())
+        out["sweep"].append({"offered_reads_per_s": rate, "reads": len(idx), "achieved_reads_per_s": len(idx) / span,
+                             "read_bp_aligned_per_s": bp / span, "p50_ms": float(np.percentile(lat, 50)),
+                             "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+                             "queue_p99_ms": float(np.percentile([r.queue_ms for r in got.values()], 99)),
+                             "rounds": st["rounds"], "mixed_rounds": st["mixed_rounds"], "max_in_flight": st["max_in_flight"],
+                             "failed": int(sum(1 for r in got.values() if r.status != 0))})
+    # plain form: each read alone through ga_align_reads, back to back
+    sample = list(range(0, len(seqs), max(1, len(seqs) // args.plain_reads)))[:args.plain_reads]
+    lat = []
+    bp = 0
+    t0 = time.perf_counter()
+    for i in sample:
+        t = time.perf_counter()
+        aligner.align([names[i]], [seqs[i]])
+        lat.append((time.perf_counter() - t) * 1e3)
+        bp += aligner.stats()["bp_aligned"]
+    span = time.perf_counter() - t0
+    out["plain_per_read"] = {"reads": len(sample), "reads_per_s": len(sample) / span, "read_bp_aligned_per_s": bp / span,
+                             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+    best = max(out["sweep"], key=lambda x: x["read_bp_aligned_per_s"])
+    out["value"] = best["read_bp_aligned_per_s"]
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload != "extend":
+        run_reads(args)
         return
     import torch
     torch.cuda.set_device(local)

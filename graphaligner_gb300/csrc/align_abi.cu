@@ -63,7 +63,8 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
         rs[i].status = a->status[i];
         rs[i].score = a->score[i];
         rs[i].steps = a->steps[i];
-        rs[i].items.assign(a->items.begin() + a->toff[i], a->items.begin() + a->toff[i] + a->tlen[i]);
+        rs[i].itemPtr = a->items.data() + a->toff[i];
+        rs[i].itemCount = a->tlen[i];
     }
 }
 
@@ -129,19 +130,18 @@ int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const u
         ga_set_last_error("seeding: seed lookup kernel failed");
         return GA_ERR_CUDA;
     }
-    std::vector<gahost::KmerMatch> km;
-    for (uint32_t i = 0; i < n; i++)
+    gahost::parallelFor(n, [&](size_t i)
     {
         reads[i].name = names[i] ? names[i] : "";
         reads[i].seq.assign((const char*)seq + seqOffset[i], seqLen[i]);
-        km.clear();
+        std::vector<gahost::KmerMatch> km(counts[i]);
         for (uint32_t k = 0; k < counts[i]; k++)
         {
             const auto& m = matches[matchOff[i] + k];
-            km.push_back(gahost::KmerMatch { m.pos, m.start, m.count });
+            km[k] = gahost::KmerMatch { m.pos, m.start, m.count };
         }
         gahost::selectSeeds(*a->graph, a->index, reads[i].seq, a->params.minimizer_density, km, reads[i].seeds);
-    }
+    });
     return GA_OK;
 }
 

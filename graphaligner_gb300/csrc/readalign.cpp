@@ -12,6 +12,8 @@
 // two extensions (GraphAligner::getTwoDirectionalTrace, GraphAligner.h:475-520)
 // of each read's next seed and runs them as one ga_extend_batch call.
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <climits>
 #include <cmath>
 #include <cstdint>
@@ -603,7 +605,7 @@ static bool nextSeed(const ReadAlignParams& p, ReadState& r, size_t& seedIndex)
     return false;
 }
 
-static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, const std::string& seqView)
+static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, const char* seq, size_t seqLen)
 {
     OnewayTrace t;
     if (e.status == GA_TRACE_FAILED)
@@ -613,20 +615,47 @@ static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, con
     }
     GAH_ASSERT(e.status == GA_OK);
     t.score = e.score;
-    t.trace.reserve(e.items.size());
-    for (uint64_t x : e.items)
+    const uint64_t* items = e.begin();
+    const uint64_t n = e.size();
+    t.trace.resize(n);
+    for (uint64_t i = 0; i < n; i++)
     {
-        TraceItem it;
+        const uint64_t x = items[i];
+        TraceItem& it = t.trace[i];
         it.node = GA_TRACE_NODE(x);
         it.nodeOffset = GA_TRACE_OFFSET(x);
         uint64_t sp1 = GA_TRACE_SEQPOS1(x);
         it.seqPos = sp1 == 0 ? (size_t)-1 : (size_t)(sp1 - 1);
         it.nodeSwitch = GA_TRACE_SWITCH(x) != 0;
-        it.seqChar = it.seqPos < seqView.size() ? seqView[it.seqPos] : '-';
+        it.seqChar = it.seqPos < seqLen ? seq[it.seqPos] : '-';
         it.graphChar = g.charAt(it.node, it.nodeOffset);
-        t.trace.push_back(it);
     }
     return t;
+}
+
+void parallelFor(size_t n, const std::function<void(size_t)>& fn)
+{
+    static const size_t hw = std::max<size_t>(1, std::min<size_t>(64, std::thread::hardware_concurrency()));
+    const size_t threads = std::min(hw, n / 8);
+    if (threads <= 1)
+    {
+        for (size_t i = 0; i < n; i++) fn(i);
+        return;
+    }
+    std::atomic<size_t> next(0);
+    auto work = [&]()
+    {
+        while (true)
+        {
+            const size_t i = next.fetch_add(1);
+            if (i >= n) break;
+            fn(i);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < threads; t++) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
 }
 
 // GraphAligner::getAlignmentFromSeed (GraphAligner.h:631-692) after the two extensions ran
@@ -699,12 +728,11 @@ static void finishSeed(const HostGraph& g, const ReadAlignParams& p, ReadState& 
 }
 
 // Aligner.cpp:505-566: selection, bp aligned, order by X-score, GAF
-static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState& r, ReadOutput& o, BatchStats& stats)
+static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState& r, ReadOutput& o)
 {
     if (r.failed)
     {
         o.failed = true;
-        stats.failedReads++;
         return;
     }
     if (r.alignments.empty()) return;
@@ -733,13 +761,13 @@ static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState
         o.gaf = std::move(text);
         o.bpAligned = bpAligned;
         o.alignments = alns.size();
-        stats.bpAligned += bpAligned;
     }
     catch (const ReadFailure&)
     {
         o.failed = true;
         o.gaf.clear();
-        stats.failedReads++;
+        o.bpAligned = 0;
+        o.alignments = 0;
     }
 }
 
@@ -892,8 +920,13 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
     const auto& requests = impl->requests;
     stats.rounds++;
     stats.extensions += requests.size();
-    for (const auto& pe : impl->pending)
+    for (const auto& rs : results) stats.cellSteps += rs.steps;
+    // every pending read touches only its own state: finish the seeds on all cores
+    const auto& pending = impl->pending;
+    const ReadAlignParams& p = impl->p;
+    parallelFor(pending.size(), [&](size_t i)
     {
+        const auto& pe = pending[i];
         ReadState& r = *pe.r;
         const SeedHit& s = r.seeds[pe.seed];
         int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
@@ -902,24 +935,20 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
         {
             for (int64_t k : { pe.backward, pe.forward })
             {
-                if (k >= 0)
-                {
-                    stats.cellSteps += results[k].steps;
-                    if (results[k].status == GA_ASSERT || results[k].status == GA_CAPACITY || results[k].status == GA_BAD_REQUEST) throw ReadFailure {};
-                }
+                if (k >= 0 && (results[k].status == GA_ASSERT || results[k].status == GA_CAPACITY || results[k].status == GA_BAD_REQUEST)) throw ReadFailure {};
             }
             OnewayTrace bw, fw;
             bw.score = INT32_MAX;
             fw.score = INT32_MAX;
-            if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], std::string(requests[pe.backward].seq, requests[pe.backward].len));
-            if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], std::string(requests[pe.forward].seq, requests[pe.forward].len));
-            finishSeed(g, impl->p, r, s, std::move(bw), std::move(fw), backwardNodeId, forwardNodeId);
+            if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], requests[pe.backward].seq, requests[pe.backward].len);
+            if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], requests[pe.forward].seq, requests[pe.forward].len);
+            finishSeed(g, p, r, s, std::move(bw), std::move(fw), backwardNodeId, forwardNodeId);
         }
         catch (const ReadFailure&)
         {
             r.failed = true;
         }
-    }
+    });
     impl->pending.clear();
     // a read that failed in this round leaves its loop now
     size_t keep = 0;
@@ -940,14 +969,22 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
 
 void SeedLoopPool::takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats)
 {
-    for (auto& l : impl->finished)
+    auto& fin = impl->finished;
+    const size_t base = out.size();
+    out.resize(base + fin.size());
+    parallelFor(fin.size(), [&](size_t i)
     {
         ReadOutput o;
-        o.noSeeds = l.noSeeds;
-        finalizeRead(impl->g, impl->p, *l.r, o, stats);
-        out.emplace_back(l.tag, std::move(o));
+        o.noSeeds = fin[i].noSeeds;
+        finalizeRead(impl->g, impl->p, *fin[i].r, o);
+        out[base + i] = std::make_pair(fin[i].tag, std::move(o));
+    });
+    for (size_t i = base; i < out.size(); i++)
+    {
+        if (out[i].second.failed) stats.failedReads++;
+        stats.bpAligned += out[i].second.bpAligned;
     }
-    impl->finished.clear();
+    fin.clear();
 }
 
 void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,

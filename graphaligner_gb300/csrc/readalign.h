@@ -1,6 +1,7 @@
 // Host-side types of the read-level layer (readalign.cpp, seeding.cpp).
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <string>
 #include <unordered_map>
@@ -129,8 +130,15 @@ struct ExtensionResult
     int32_t status = 0;
     int32_t score = 0;
     uint64_t steps = 0;
-    std::vector<uint64_t> items;
+    std::vector<uint64_t> items;          // packed trace items, owned here ...
+    const uint64_t* itemPtr = nullptr;    // ... or held by the extension callback until its next call
+    uint64_t itemCount = 0;
+    const uint64_t* begin() const { return itemPtr ? itemPtr : items.data(); }
+    uint64_t size() const { return itemPtr ? itemCount : items.size(); }
 };
+
+// fn(i) for i in [0, n) on the host's cores (serially for small n); fn handles its own errors
+void parallelFor(size_t n, const std::function<void(size_t)>& fn);
 
 typedef void (*ExtendFn)(void* ctx, const std::vector<ExtensionRequest>& requests, std::vector<ExtensionResult>& results);
 
