@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--reads-n", type=int, default=0, help="reads of a read-level workload (0: its default)")
     ap.add_argument("--rates", default="50,100,200,400", help="serve: Poisson arrival rates, reads/s")
     ap.add_argument("--plain-reads", type=int, default=40, help="serve: reads timed one ga_align_reads call each")
+    ap.add_argument("--serve-seconds", type=float, default=8.0, help="serve: seconds of Poisson arrivals per rate")
+    ap.add_argument("--cpu-reads", type=int, default=40, help="read-level: reads of the CPU baseline sample")
     return ap.parse_args()
 
 
@@ -210,6 +212,15 @@ def make_read_workload(name: str, n_reads: int):
     if name == "reads-vg":
         vg = dg.small_vg(0)
         reads = dg.small_vg_reads(vg, n_reads or 200, 1)
+        # the same graph as the reference built it (its numbering, component and chain order)
+        golden = os.path.join(ROOT, "tests", "golden", "vg50k_graph.gag.gz")
+        if os.path.exists(golden):
+            import gzip
+            import tempfile
+            with tempfile.NamedTemporaryFile(suffix=".gag") as f:
+                f.write(gzip.open(golden).read())
+                f.flush()
+                return gg.load_gag(f.name), reads, "vg"
         return gg.build_from_gfa(vg.to_gfa()), reads, "vg"
     if name in ("reads-dbg", "serve"):
         genome = dg.stress_dbg_genome(0)
@@ -274,7 +285,48 @@ def run_reads(args):
             golden = os.path.join(ROOT, "tests", "golden", "vg50k_b10.gaf.gz")
             if os.path.exists(golden):
                 line["gaf_identical_to_reference"] = gzip.open(golden, "rt").read() == gaf
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"], line["cpu_sample_gaf_identical"] = read_cpu_baseline(g, names, seqs, preset_name, gaf, args.cpu_reads)
     print(json.dumps(line), flush=True)
+
+
+def read_cpu_baseline(g, names, seqs, preset_name, gaf, n_sample):
+    """The same read-level flow on the host cores: the package's host code with the oracle's
+    extensions (tests/harness/pipeline.cpp), on an evenly spaced sample of reads.  Its GAF lines
+    must equal the GPU's lines for those reads."""
+    import subprocess
+    import tempfile
+    from graphaligner_gb300 import graph as gg
+    exe = os.path.join(ROOT, "tests", "_build", "pipeline")
+    srcs = [os.path.join(ROOT, "tests", "harness", "pipeline.cpp"),
+            os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.cpp"),
+            os.path.join(ROOT, "graphaligner_gb300", "csrc", "seeding.cpp"),
+            os.path.join(ROOT, "oracle", "ga_oracle.cpp")]
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-o", exe, *srcs, "-lpthread"], check=True)
+    idx = list(range(0, len(seqs), max(1, len(seqs) // n_sample)))[:n_sample]
+    with tempfile.TemporaryDirectory() as td:
+        gag = os.path.join(td, "g.gag")
+        gg.save_gag(g, gag)
+        fa = os.path.join(td, "r.fa")
+        with open(fa, "w") as f:
+            for i in idx:
+                f.write(f">{names[i]}\n{seqs[i].decode()}\n")
+        mode = "gafdbg" if preset_name == "dbg" else "gaf"
+        bw = "5" if preset_name == "dbg" else "10"
+        t = time.perf_counter()
+        out = subprocess.run([exe, gag, fa, mode, bw], check=True, capture_output=True, text=True)
+        dt = time.perf_counter() - t
+    want = {names[i] for i in idx}
+    gpu_lines = [ln for ln in gaf.splitlines(keepends=True) if ln.split("\t", 1)[0] in want]
+    cpu_lines = out.stdout.splitlines(keepends=True)
+    bp = 0
+    for ln in out.stderr.splitlines():
+        if ln.startswith("rounds "):
+            bp = int(ln.split()[5])
+    return ({"value": bp / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+             "sample": f"{len(idx)} of {len(seqs)} reads (evenly spaced); the package's host read-level code with the oracle restatement's extensions (8 threads per round), {dt:.1f} s"},
+            sorted(gpu_lines) == sorted(cpu_lines))
 
 
 def run_serving(args, aligner, names, seqs):
@@ -284,11 +336,12 @@ def run_serving(args, aligner, names, seqs):
     rng = np.random.default_rng(2)
     out = {"sweep": []}
     rates = [float(x) for x in args.rates.split(",")]
-    per_rate = max(1, len(seqs) // len(rates))
     pos = 0
     for rate in rates:
-        idx = list(range(pos, min(len(seqs), pos + per_rate)))
-        pos += per_rate
+        # about --serve-seconds of arrivals per rate, reads taken in order from the workload
+        n = int(max(20, rate * args.serve_seconds))
+        idx = [(pos + k) % len(seqs) for k in range(n)]
+        pos += n
         arrivals = np.cumsum(rng.exponential(1.0 / rate, len(idx)))
         got = {}
         with Server(aligner) as srv:

@@ -115,27 +115,58 @@ __device__ __forceinline__ HSlot* hash_get_or_add(HSlot* t, u32 cap, u32 gen, u3
 }
 
 // IUPAC membership of every byte value (bit0 A, bit1 C, bit2 G, bit3 T; 0 = '-',
-// -1 = not a sequence character), filled from iupac_mask on the host at load time
+// -1 = not a sequence character), filled from iupac_mask on the host at load time and
+// copied into shared memory by every block (lanes index it by data: the constant
+// cache would serialise distinct addresses of a warp, shared memory serves them at once)
 __constant__ int8_t c_iupac[256];
+__shared__ int8_t s_iupac[256];
 
-// match masks of the 64 rows starting at read position j (getEqVector, Common.h:279-318)
+// all threads of the block must call this before any other work
+__device__ __forceinline__ void load_iupac_table()
+{
+    for (u32 k = threadIdx.x; k < 256; k += blockDim.x) s_iupac[k] = c_iupac[k];
+    __syncthreads();
+}
+
+__device__ __forceinline__ void eq_add(EqV4& eq, int m, u32 r, bool full, bool& ok)
+{
+    // a non-sequence byte always fails; a gap fails only inside a full 64-row window
+    ok &= !(m < 0 || (m == 0 && full));
+    const u64 bit = 1ULL << r;
+    eq.a |= (m & 1) ? bit : 0;
+    eq.c |= (m & 2) ? bit : 0;
+    eq.g |= (m & 4) ? bit : 0;
+    eq.t |= (m & 8) ? bit : 0;
+}
+
+// match masks of the 64 rows starting at read position j (getEqVector, Common.h:279-318).
+// When the window and 3 bytes either side lie inside the read, it is read as aligned
+// 32-bit words (every word then lies inside the read); otherwise byte by byte.
 __device__ __forceinline__ bool eq_vector(const uint8_t* seq, u32 len, int64_t j, EqV4& eq)
 {
     eq.a = eq.c = eq.g = eq.t = 0;
     bool ok = true;
-    for (int r = 0; r < 64; r++)
+    const bool full = j + 64 <= (int64_t)len;
+    if (j >= 3 && j + 64 + 3 <= (int64_t)len)
     {
-        int64_t p = j + r;
-        if (p >= (int64_t)len) break;
-        int m = c_iupac[seq[p]];
-        // a non-sequence byte always fails; a gap fails only inside a full 64-row window
-        if (m < 0 || (m == 0 && j + 64 <= (int64_t)len)) ok = false;
-        u64 bit = 1ULL << r;
-        if (m & 1) eq.a |= bit;
-        if (m & 2) eq.c |= bit;
-        if (m & 4) eq.g |= bit;
-        if (m & 8) eq.t |= bit;
+        const uint8_t* p = seq + j;
+        const u32 shift = (u32)((uintptr_t)p & 3) * 8;
+        const u32* w = (const u32*)((uintptr_t)p & ~(uintptr_t)3);
+        u32 lo = w[0];
+#pragma unroll
+        for (u32 k = 0; k < 16; k++)
+        {
+            const u32 hi = w[k + 1];
+            const u32 word = __funnelshift_r(lo, hi, shift);
+            lo = hi;
+#pragma unroll
+            for (u32 b = 0; b < 4; b++) eq_add(eq, s_iupac[(word >> (8 * b)) & 0xff], k * 4 + b, full, ok);
+        }
+        return ok;
     }
+    const int64_t rem = (int64_t)len - j;
+    const u32 n = rem >= 64 ? 64u : (rem > 0 ? (u32)rem : 0u);
+    for (u32 r = 0; r < n; r++) eq_add(eq, s_iupac[seq[j + r]], r, full, ok);
     return ok;
 }
 
@@ -154,7 +185,7 @@ __device__ __forceinline__ int node_char_mask(const DevGraph& g, u32 n, u32 pos)
 // GraphAlignerCommon::characterMatch on a read byte and a graph position
 __device__ __forceinline__ bool char_match(const DevGraph& g, uint8_t c, u32 n, u32 pos, bool& bad)
 {
-    int a = iupac_mask(c);
+    int a = s_iupac[c];
     if (a < 0) { bad = true; return false; }
     int b = node_char_mask(g, n, pos);
     // identical characters always match; for distinct ones the IUPAC sets must overlap
@@ -419,6 +450,7 @@ __device__ __forceinline__ bool arena_alloc(const FillArgs& a, ArenaCursor& c, u
 
 __device__ __forceinline__ u32 rec_hash_cap(u32 count)
 {
+    if (count <= kInlineIds) return 0;
     u32 cap = 4;
     while (cap < 2 * count) cap <<= 1;
     return cap;
@@ -446,16 +478,20 @@ __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 in
     r->hashCap = cap;
     r->notValid = notValid ? 1u : 0u;
     r->pad = 0;
+    for (u32 k = 0; k < kInlineIds; k++) r->ids[k] = k < count ? (band[k].node & kNodeMask) : 0xffffffffu;
     Item* items = (Item*)(base + sizeof(SliceRec));
     uint16_t* h = (uint16_t*)(base + sizeof(SliceRec) + (u64)count * sizeof(Item));
-    for (u32 k = 0; k < cap; k++) h[k] = 0;
-    for (u32 k = 0; k < count; k++)
+    for (u32 k = 0; k < count; k++) items[k] = band[k];
+    if (cap > 0)
     {
-        items[k] = band[k];
-        u32 node = band[k].node & kNodeMask;
-        u32 p = hash_node(node) & (cap - 1);
-        while (h[p] != 0) p = (p + 1) & (cap - 1);
-        h[p] = (uint16_t)(k + 1);
+        for (u32 k = 0; k < cap; k++) h[k] = 0;
+        for (u32 k = 0; k < count; k++)
+        {
+            u32 node = band[k].node & kNodeMask;
+            u32 p = hash_node(node) & (cap - 1);
+            while (h[p] != 0) p = (p + 1) & (cap - 1);
+            h[p] = (uint16_t)(k + 1);
+        }
     }
     dir[index] = off;
     return true;
@@ -725,13 +761,33 @@ struct Table
     const uint8_t* arena;
     const u64* dir;
     u32 count;
-    __device__ __forceinline__ const SliceRec* rec(u32 s) const { return (const SliceRec*)(arena + dir[s]); }
-    __device__ __forceinline__ const Item* items(u32 s) const { return (const Item*)(arena + dir[s] + sizeof(SliceRec)); }
-    __device__ __forceinline__ const Item* find(u32 s, u32 node) const
+    // the traceback works on one slice and the one before it: their records are remembered
+    u32 cs[2];
+    const SliceRec* cr[2];
+    __device__ __forceinline__ void init() { cs[0] = cs[1] = 0xffffffffu; cr[0] = cr[1] = nullptr; }
+    __device__ __forceinline__ const SliceRec* rec(u32 s)
+    {
+        if (cs[0] == s) return cr[0];
+        if (cs[1] == s) return cr[1];
+        const SliceRec* r = (const SliceRec*)(arena + dir[s]);
+        cs[1] = cs[0]; cr[1] = cr[0];
+        cs[0] = s; cr[0] = r;
+        return r;
+    }
+    __device__ __forceinline__ const Item* items(u32 s) { return (const Item*)((const uint8_t*)rec(s) + sizeof(SliceRec)); }
+    __device__ __forceinline__ const Item* find(u32 s, u32 node)
     {
         const SliceRec* r = rec(s);
-        const Item* it = items(s);
-        const uint16_t* h = (const uint16_t*)((const uint8_t*)it + (u64)r->count * sizeof(Item));
+        const Item* it = (const Item*)((const uint8_t*)r + sizeof(SliceRec));
+        const u32 count = r->count;
+        if (count <= kInlineIds)
+        {
+            // the record's own line holds the band's node ids
+            for (u32 k = 0; k < count; k++)
+                if (r->ids[k] == node) return &it[k];
+            return nullptr;
+        }
+        const uint16_t* h = (const uint16_t*)((const uint8_t*)it + (u64)count * sizeof(Item));
         u32 cap = r->hashCap;
         u32 p = hash_node(node) & (cap - 1);
         for (u32 probe = 0; probe < cap; probe++)
@@ -954,6 +1010,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
     c.t.arena = a.arena;
     c.t.dir = (const u64*)(a.arena + st.dir);
     c.t.count = st.committed;
+    c.t.init();
     c.cost = a.cost;
     c.err = 0;
     TraceOut to;
@@ -1315,6 +1372,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
 __global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, u32 lanesPerWarp, u32 first, u32 count,
     u32* counter, u32 slotBase, u32 slotLimit)
 {
+    load_iupac_table();
     const u32 slot = slotBase + blockIdx.x * blockDim.x + threadIdx.x;
     // a warp whose slots are not all inside [slotBase, slotLimit) touches no workspace (warp-uniform)
     if (slotBase + blockIdx.x * blockDim.x + (threadIdx.x & ~31u) + 32 > slotLimit) return;
@@ -1411,6 +1469,7 @@ static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes]
 // extension that outgrows the small tables reports GA_CAPACITY).
 __global__ void __launch_bounds__(128) extend_kernel_noalloc(FillArgs fa, TraceArgs ta, u32* counter)
 {
+    load_iupac_table();
     const u32 slot = blockIdx.x * blockDim.x + threadIdx.x;
     Workspace w = workspace_at(fa.workspace + (u64)slot * fa.workspaceStride, fa.caps);
     u32 gen = w.header[0];

@@ -36,8 +36,11 @@ struct Item
 static constexpr u32 kExists = 0x80000000u;
 static constexpr u32 kNodeMask = 0x7fffffffu;
 
-// A committed DP slice in the per-batch arena: SliceRec, then count Items, then
-// hashCap uint16 slots (band index + 1, 0 = empty) keyed by node.
+// A committed DP slice in the per-batch arena: SliceRec (one 64-byte line), then count
+// Items, then hashCap uint16 slots (band index + 1, 0 = empty) keyed by node when the
+// band is larger than kInlineIds nodes.
+static constexpr u32 kInlineIds = 8;
+
 struct SliceRec
 {
     i32 minScore;
@@ -45,9 +48,10 @@ struct SliceRec
     i32 maxX;              // maxExactEndposScore
     u32 maxXNode;          // maxExactEndposNode
     u32 count;
-    u32 hashCap;
+    u32 hashCap;           // 0 when count <= kInlineIds (the ids below are the index)
     u32 notValid;          // scoresNotValid: the tangle-effort cap was hit
     u32 pad;
+    u32 ids[kInlineIds];   // node of band entry k, for bands of up to kInlineIds nodes
 };
 
 // Per-extension state passed from the fill kernel to the traceback kernel.

@@ -283,6 +283,169 @@ def _component_order(out_lists):
     return (next_comp - 1 - comp).astype(np.uint32)
 
 
+def _find_chains(n, in_lists, out_lists, comp, lookup_pieces, node_length):
+    """AlignmentGraph::findChains (AlignmentGraph.cpp:571-630) with chainTips (428-519),
+    chainCycles (521-569), chainBubble / findBubble (300-393) and fixChainApproxPos
+    (395-426): union-find with union by rank (merge, AlignmentGraph.cpp:344-354,
+    including its rank bump when both sides already share a root), bigraph nodes
+    visited in nodeLookup order."""
+    parent = list(range(n))
+    rank = [0] * n
+    max_ = (1 << 64) - 1
+
+    def find(x):
+        root = x
+        while parent[root] != root:
+            root = parent[root]
+        while parent[x] != root:
+            parent[x], x = root, parent[x]
+        return root
+
+    def merge(a, b):
+        a, b = find(a), find(b)
+        if rank[a] < rank[b]:
+            a, b = b, a
+        parent[b] = a
+        if rank[a] == rank[b]:
+            rank[a] += 1
+
+    for pieces in lookup_pieces:
+        for k in range(1, len(pieces)):
+            merge(pieces[0], pieces[k])
+    # chainTips
+    ignorable = [False] * n
+    order = sorted(range(n), key=lambda i: comp[i])
+    ncomp = int(comp[order[-1]]) + 1 if n else 0
+    fw = [True] * ncomp
+    for i in reversed(order):
+        ci = comp[i]
+        if not fw[ci]:
+            continue
+        for nb in out_lists[i]:
+            if comp[nb] == ci or not fw[comp[nb]]:
+                fw[ci] = False
+                break
+    for i in reversed(order):
+        if fw[comp[i]]:
+            for nb in out_lists[i]:
+                merge(i, nb)
+    bw = [True] * ncomp
+    for i in order:
+        ci = comp[i]
+        if not bw[ci]:
+            continue
+        for nb in in_lists[i]:
+            if comp[nb] == ci or not bw[comp[nb]]:
+                bw[ci] = False
+                break
+    for i in order:
+        if bw[comp[i]]:
+            for nb in in_lists[i]:
+                merge(i, nb)
+    tip_chainers = {}
+    for i in range(n):
+        b_, f_ = bw[comp[i]], fw[comp[i]]
+        if b_ or f_:
+            ignorable[i] = True
+        # the reference compares raw parent entries here, not roots
+        if b_:
+            for nb in out_lists[i]:
+                if parent[nb] != parent[i]:
+                    tip_chainers.setdefault(parent[i], []).append(nb)
+        if f_:
+            for nb in in_lists[i]:
+                if parent[nb] != parent[i]:
+                    tip_chainers.setdefault(parent[i], []).append(nb)
+    # chainCycles
+    for i in range(n):
+        ufw = max_
+        for u in out_lists[i]:
+            if ignorable[u] or u == i:
+                continue
+            ufw = u if ufw == max_ else max_ - 1
+        ubw = max_
+        for u in in_lists[i]:
+            if ignorable[u] or u == i:
+                continue
+            if ubw == max_:
+                ubw = u
+            elif u != ubw:
+                ubw = max_ - 1
+        if ufw != ubw or ufw >= max_ - 1:
+            continue
+        ignorable[i] = True
+        merge(i, ufw)
+
+    # chainBubble from the last piece of every bigraph node
+    def find_bubble(start):
+        stack = [start]
+        visited = set()
+        seen = {start}
+        while stack:
+            v = stack.pop()
+            seen.discard(v)
+            visited.add(v)
+            if not out_lists[v]:
+                return None
+            for u in out_lists[v]:
+                if ignorable[u] or u == v:
+                    continue
+                if u == start:
+                    return None
+                seen.add(u)
+                if not any((w != u and not ignorable[w] and w not in visited) for w in in_lists[u]):
+                    stack.append(u)
+            if len(stack) == 1 and len(seen) == 1 and stack[0] in seen:
+                t = stack[-1]
+                if start in out_lists[t]:
+                    return None
+                return t
+        return None
+
+    for pieces in lookup_pieces:
+        start = pieces[-1]
+        end = find_bubble(start)
+        if end is None:
+            continue
+        merge(start, end)
+        visited = set()
+        stack = [start]
+        while stack:
+            top = stack.pop()
+            if top in visited or ignorable[top]:
+                continue
+            visited.add(top)
+            merge(start, top)
+            for nb in out_lists[top]:
+                if nb not in visited and nb != end:
+                    stack.append(nb)
+    for key, nbs in tip_chainers.items():
+        if len({parent[x] for x in nbs}) != 1:
+            continue
+        merge(key, nbs[0])
+    chain = np.array([find(i) for i in range(n)], dtype=np.uint64)
+    # fixChainApproxPos
+    pos = np.full(n, max_, dtype=np.uint64)
+    big = (n + 5) * SPLIT_NODE_SIZE
+    for s0 in range(n):
+        if pos[s0] != max_:
+            continue
+        c = chain[s0]
+        stack = [(s0, big)]
+        while stack:
+            v, d = stack.pop()
+            if pos[v] != max_:
+                continue
+            pos[v] = d
+            for u in out_lists[v]:
+                if chain[u] == c and pos[u] == max_:
+                    stack.append((u, d + int(node_length[u])))
+            for u in in_lists[v]:
+                if chain[u] == c and pos[u] == max_:
+                    stack.append((u, d - int(node_length[v])))
+    return chain, pos
+
+
 def build_from_gfa(gfa_text: str) -> Graph:
     """Alignment graph from a GFA (0-bp overlaps or de Bruijn k-1 overlaps).
 
@@ -394,8 +557,9 @@ def build_from_gfa(gfa_text: str) -> Graph:
     lin = _find_linearizable(in_lists)
     comp = _component_order(out_lists)
     l_off, l_nodes = _csr([idx for _, idx in lookup])
+    chain, chain_pos = _find_chains(n, in_lists, out_lists, comp.tolist(), [idx for _, idx in lookup], node_length)
     return Graph(n, nn, node_length, node_ids, node_offset, reverse, lin, comp,
-                 np.arange(n, dtype=np.uint64), np.zeros(n, dtype=np.uint64),
+                 chain, chain_pos,
                  seq2.reshape(-1), seqa.reshape(-1), in_off, in_nb, out_off, out_nb,
                  np.array([b for b, _ in lookup], dtype=np.int32),
                  np.array([size_of[b] for b, _ in lookup], dtype=np.uint32), l_off, l_nodes,
