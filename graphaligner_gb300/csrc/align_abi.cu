@@ -22,14 +22,11 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
 {
     ga_aligner* a = (ga_aligner*)ctx;
     const size_t n = rq.size();
-    a->off.resize(n);
-    a->len.resize(n);
-    a->node.resize(n);
-    a->nodeOff.resize(n);
-    a->cap.resize(n);
-    a->toff.resize(n);
+    const auto tStage = std::chrono::steady_clock::now();
+    bool ok = a->off.reserve(n) && a->len.reserve(n) && a->node.reserve(n) && a->nodeOff.reserve(n) && a->cap.reserve(n)
+        && a->toff.reserve(n) && a->status.reserve(n) && a->score.reserve(n) && a->tlen.reserve(n) && a->steps.reserve(n);
     uint64_t total = 0, totalItems = 0;
-    for (size_t i = 0; i < n; i++)
+    for (size_t i = 0; ok && i < n; i++)
     {
         a->off[i] = total;
         a->len[i] = rq[i].len;
@@ -40,19 +37,23 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
         total += rq[i].len;
         totalItems += a->cap[i];
     }
-    a->blob.resize(std::max<uint64_t>(total, 1));
-    for (size_t i = 0; i < n; i++) memcpy(a->blob.data() + a->off[i], rq[i].seq, rq[i].len);
-    a->status.resize(n);
-    a->score.resize(n);
-    a->tlen.resize(n);
-    a->steps.resize(n);
-    a->items.resize(std::max<uint64_t>(totalItems, 1));
-    ga_extend_batch_desc b { (uint32_t)n, a->blob.data(), a->off.data(), a->len.data(), a->node.data(), a->nodeOff.data(), a->toff.data(), a->cap.data() };
-    ga_extend_results r { a->status.data(), a->score.data(), a->tlen.data(), a->items.data(), a->steps.data() };
-    auto t0 = std::chrono::steady_clock::now();
-    int rc = ga_extend_batch(a->ext, &a->params.extend, &b, &r);
-    a->stats.extend_ms += ms_since(t0);
-    a->launches++;
+    ok = ok && a->blob.reserve(std::max<uint64_t>(total, 1)) && a->items.reserve(std::max<uint64_t>(totalItems, 1));
+    int rc = GA_ERR_CUDA;
+    if (ok)
+    {
+        gahost::parallelFor(n, [&](size_t i) { memcpy(a->blob.data() + a->off[i], rq[i].seq, rq[i].len); });
+        ga_extend_batch_desc b { (uint32_t)n, a->blob.data(), a->off.data(), a->len.data(), a->node.data(), a->nodeOff.data(), a->toff.data(), a->cap.data() };
+        ga_extend_results r { a->status.data(), a->score.data(), a->tlen.data(), a->items.data(), a->steps.data() };
+        a->stagingMs += ms_since(tStage);
+        auto t0 = std::chrono::steady_clock::now();
+        rc = ga_extend_batch(a->ext, &a->params.extend, &b, &r);
+        a->stats.extend_ms += ms_since(t0);
+        a->launches++;
+    }
+    else
+    {
+        ga_set_last_error("extension staging: pinned host memory");
+    }
     for (size_t i = 0; i < n; i++)
     {
         if (rc != GA_OK)

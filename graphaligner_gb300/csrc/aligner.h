@@ -1,6 +1,7 @@
 // State of one read-level aligner (ga_aligner_t) shared by align_abi.cu and serve.cpp.
 #pragma once
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <string>
 #include <vector>
 #include "readalign.h"
@@ -21,12 +22,38 @@ struct ga_aligner
     ga_align_stats stats {};
     uint64_t launches = 0;
     cudaStream_t stream = nullptr;
-    // staging of one extension batch
-    std::vector<uint8_t> blob;
-    std::vector<uint64_t> off, toff;
-    std::vector<uint32_t> len, node, nodeOff, cap, tlen;
-    std::vector<int32_t> status, score;
-    std::vector<uint64_t> items, steps;
+    // staging of one extension batch: pinned, grown as needed, never cleared
+    template <typename T>
+    struct Pinned
+    {
+        T* p = nullptr;
+        size_t cap = 0;
+        bool reserve(size_t n)
+        {
+            if (n <= cap) return true;
+            size_t want = std::max(n, cap + cap / 2);
+            void* q = nullptr;
+            if (cudaHostAlloc(&q, want * sizeof(T), cudaHostAllocDefault) != cudaSuccess) return false;
+            if (p) cudaFreeHost(p);
+            p = (T*)q;
+            cap = want;
+            return true;
+        }
+        void release() { if (p) cudaFreeHost(p); p = nullptr; cap = 0; }
+        T* data() { return p; }
+        T& operator[](size_t i) { return p[i]; }
+    };
+    Pinned<uint8_t> blob;
+    Pinned<uint64_t> off, toff, items, steps;
+    Pinned<uint32_t> len, node, nodeOff, cap, tlen;
+    Pinned<int32_t> status, score;
+    double stagingMs = 0;      // host time packing requests and handing results over
+    ~ga_aligner()
+    {
+        blob.release(); off.release(); toff.release(); items.release(); steps.release();
+        len.release(); node.release(); nodeOff.release(); cap.release(); tlen.release();
+        status.release(); score.release();
+    }
 };
 
 // MinimizerSeeder::getSeeds for a batch of reads: k-mer lookups on the GPU, the

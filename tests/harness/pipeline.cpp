@@ -3,6 +3,7 @@
 // formats oracle/_ref/ga_ref prints, so the two can be diffed.
 //   pipeline <graph.gag> <reads.fa> seeds <k> <w> <density> <discard>
 //   pipeline <graph.gag> <reads.fa> gaf <bandwidth> <maxcells|->
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -157,6 +158,7 @@ int main(int argc, char** argv)
     uint64_t maxCells = (argc > 5 && std::string(argv[5]) != "-") ? std::stoull(argv[5]) : (dbg ? 10000 : UINT64_MAX);
     gahost::MinimizerIndex idx;
     gahost::buildMinimizerIndex(graph, dbg ? 19 : 15, dbg ? 30 : 20, 1.0 - (dbg ? 0.0002 : 0.001), idx);
+    const auto alignStart = std::chrono::steady_clock::now();
     std::vector<gahost::ReadInput> in(reads.size());
     std::vector<gahost::KmerMatch> km;
     for (size_t i = 0; i < reads.size(); i++)
@@ -199,6 +201,8 @@ int main(int argc, char** argv)
     }
     else gahost::alignBatch(graph, p, in, oracleExtend, &ctx, out, st);
     for (auto& o : out) std::cout << o.gaf;
-    std::cerr << "rounds " << st.rounds << " extensions " << st.extensions << " bp " << st.bpAligned << " failed " << st.failedReads << std::endl;
+    const double alignSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - alignStart).count();
+    std::cerr << "rounds " << st.rounds << " extensions " << st.extensions << " bp " << st.bpAligned << " failed " << st.failedReads
+              << " seconds " << alignSeconds << std::endl;
     return 0;
 }
