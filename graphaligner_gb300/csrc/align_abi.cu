@@ -211,6 +211,7 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     if (!a || (n > 0 && (!names || !seq || !seqOffset || !seqLen))) return GA_ERR_ARGUMENT;
     auto start = std::chrono::steady_clock::now();
     a->stats = ga_align_stats {};
+    a->stagingMs = 0;
     a->stats.reads = n;
     a->gaf.clear();
     a->readBp.assign(n, 0);
@@ -227,12 +228,19 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     std::vector<gahost::ReadOutput> outs;
     gahost::BatchStats bs;
     gahost::alignBatch(*a->graph, rp, reads, ga_aligner_extend, a, outs, bs);
+    size_t gafBytes = 0;
+    for (uint32_t i = 0; i < n; i++) gafBytes += outs[i].gaf.size();
+    a->gaf.reserve(gafBytes);
     for (uint32_t i = 0; i < n; i++)
     {
         a->gaf += outs[i].gaf;
         a->readBp[i] = outs[i].bpAligned;
         if (outs[i].alignments > 0) a->stats.reads_aligned++;
     }
+    a->stats.collect_ms = bs.collectMs;
+    a->stats.staging_ms = a->stagingMs;
+    a->stats.consume_ms = bs.consumeMs;
+    a->stats.finish_ms = bs.finishMs;
     a->stats.failed_reads = bs.failedReads;
     a->stats.bp_aligned = bs.bpAligned;
     a->stats.rounds = bs.rounds;

@@ -12,6 +12,7 @@
 // two extensions (GraphAligner::getTwoDirectionalTrace, GraphAligner.h:475-520)
 // of each read's next seed and runs them as one ga_extend_batch call.
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <thread>
 #include <climits>
@@ -792,6 +793,7 @@ struct SeedLoopPool::Impl
     };
     std::vector<Pending> pending;
     std::vector<ExtensionRequest> requests;
+    double collectMs = 0;
     Impl(const HostGraph& g_, const ReadAlignParams& p_) : g(g_), p(p_) {}
 };
 
@@ -833,8 +835,14 @@ void SeedLoopPool::add(ReadInput&& read, uint64_t tag)
     impl->live.push_back(std::move(l));
 }
 
+static double msSince(std::chrono::steady_clock::time_point t)
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+}
+
 bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
 {
+    const auto t0 = std::chrono::steady_clock::now();
     const HostGraph& g = impl->g;
     auto& pending = impl->pending;
     pending.clear();
@@ -911,6 +919,7 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
     }
     impl->live.resize(keep);
     impl->requests = requests;
+    impl->collectMs += msSince(t0);
     return !pending.empty();
 }
 
@@ -918,6 +927,9 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
 {
     const HostGraph& g = impl->g;
     const auto& requests = impl->requests;
+    const auto t0 = std::chrono::steady_clock::now();
+    stats.collectMs += impl->collectMs;
+    impl->collectMs = 0;
     stats.rounds++;
     stats.extensions += requests.size();
     for (const auto& rs : results) stats.cellSteps += rs.steps;
@@ -965,10 +977,12 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
         keep++;
     }
     impl->live.resize(keep);
+    stats.consumeMs += msSince(t0);
 }
 
 void SeedLoopPool::takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats)
 {
+    const auto t0 = std::chrono::steady_clock::now();
     auto& fin = impl->finished;
     const size_t base = out.size();
     out.resize(base + fin.size());
@@ -985,6 +999,7 @@ void SeedLoopPool::takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& ou
         stats.bpAligned += out[i].second.bpAligned;
     }
     fin.clear();
+    stats.finishMs += msSince(t0);
 }
 
 void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,

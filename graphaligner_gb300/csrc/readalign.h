@@ -113,6 +113,9 @@ struct BatchStats
     uint64_t cellSteps = 0;
     uint64_t bpAligned = 0;
     uint64_t failedReads = 0;
+    double collectMs = 0;      // next seeds and extension requests
+    double consumeMs = 0;      // trace decoding, fix-up and merge of every finished seed
+    double finishMs = 0;       // selection and GAF of finished reads
 };
 
 struct ExtensionRequest

@@ -205,8 +205,12 @@ typedef struct ga_align_stats {
     uint64_t extensions;
     uint64_t cell_steps;
     double   seed_ms;
-    double   extend_ms;
-    double   host_ms;
+    double   extend_ms;                /* ga_extend_batch calls: copies and kernels */
+    double   host_ms;                  /* everything else */
+    double   collect_ms;               /* of which: next seeds and extension requests */
+    double   staging_ms;               /*           packing requests for the GPU */
+    double   consume_ms;               /*           trace decoding, fix-up and merge per seed */
+    double   finish_ms;                /*           selection and GAF per read */
 } ga_align_stats;
 
 typedef struct ga_aligner* ga_aligner_t;
