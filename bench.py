@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--plain-reads", type=int, default=40, help="serve: reads timed one ga_align_reads call each")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serve: seconds of Poisson arrivals per rate")
     ap.add_argument("--cpu-reads", type=int, default=40, help="read-level: reads of the CPU baseline sample")
+    ap.add_argument("--truncate", type=int, default=0, help="extend: cut every extension to this many bases (small profiling cases)")
+    ap.add_argument("--arena-gb", type=float, default=0, help="extend: DP-table arena size (default: from the batch)")
     return ap.parse_args()
 
 
@@ -67,14 +69,15 @@ def dist_env():
     return rank, world, local
 
 
-def make_workload(n_reads: int, rank: int):
+def make_workload(n_reads: int, rank: int, truncate: int = 0):
     from graphaligner_gb300 import datagen as dg
     from graphaligner_gb300 import graph as gg
     from graphaligner_gb300.extend import pack_batch
     vg = dg.batch_vg(0)
     g = gg.build_from_gfa(vg.to_gfa())
     ext = dg.batch_extension_workload(n_reads, graph_seed=0, read_seed=1 + rank)
-    batch = pack_batch(g, ext.seqs, ext.bignode, ext.offset)
+    seqs = [x[:truncate] for x in ext.seqs] if truncate else ext.seqs
+    batch = pack_batch(g, seqs, ext.bignode, ext.offset)
     return g, batch
 
 
@@ -410,7 +413,7 @@ def main():
 
     # ---- workload (host) ----
     t0 = time.perf_counter()
-    g, batch = make_workload(args.reads, rank)
+    g, batch = make_workload(args.reads, rank, args.truncate)
     gen_s = time.perf_counter() - t0
     params = ExtendParams(bandwidth=10)
 
@@ -423,6 +426,8 @@ def main():
 
     dgraph = DeviceGraph(g, device=local)
     arena = int(min(64 << 30, max(4 << 30, int(batch.seq_len.astype(np.int64).sum()) * 24)))
+    if args.arena_gb:
+        arena = int(args.arena_gb * (1 << 30))
     ext = Extender(dgraph, arena_bytes=arena)
 
     # ---- device-resident batch ----

@@ -212,10 +212,28 @@ struct PrevInfo
 // calculateNodeInner (Common.h:1113-1478) with the single-seed fake extra slice.
 // Fill = true: the slice fill (early leave allowed, calculateNodeClipPrecise).
 // Fill = false: recalcNodeWordslice (no early leave, every column written to cols).
+// An upper bound of ws_max_xscore(w, seqOffset, cost, 64, mask): every candidate row m scores
+// 100 (m + 1) - cost s(m) with s(m) >= -popc(VN), plus 100 seqOffset - cost before.
+__device__ __forceinline__ int64_t xscore_bound(const WS& w, i32 seqOffset, i32 cost)
+{
+    const i32 vn = popc64(w.VN);
+    const i32 before = w.end - (popc64(w.VP) - vn);
+    return 6400 + (int64_t)cost * vn + (int64_t)seqOffset * 100 - (int64_t)cost * before;
+}
+
+// Below this read offset no term of the X-score can wrap around in 32 bits, so the bound
+// above also bounds the reference's (wrapping) arithmetic.
+static constexpr i32 kXBoundOffsetLimit = 10000000;
+
 template <bool Fill>
 __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const EqV4& eqv, const PrevInfo& prev,
-    const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, WS* cols, u64& steps, int& err)
+    const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, WS* cols, u64& steps, int& err,
+    i32 sliceMaxX = kIntMin)
 {
+    // The slice keeps the first node of strictly greatest X-score and the node keeps its
+    // greatest column, so a column whose bound is at most max(slice so far, node so far)
+    // changes neither: its exact X-score is skipped.
+    const bool boundOk = seqOffset < kXBoundOffsetLimit;
     NodeCalc result;
     result.minScore = kIntMax;
     result.minScoreNode = 0xffffffffu;
@@ -284,7 +302,8 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
     result.minScore = ws.end;
     result.minScoreNode = i;
     result.minScoreOffset = 0;
-    if (Fill) result.maxX = ws_max_xscore(ws, seqOffset, cost, 64, kAllOnes);
+    if (Fill && (!boundOk || xscore_bound(ws, seqOffset, cost) > (int64_t)sliceMaxX))
+        result.maxX = ws_max_xscore(ws, seqOffset, cost, 64, kAllOnes);
     result.maxXNode = i;
     const bool exists = (slice.node & kExists) != 0;
     if (exists)
@@ -409,7 +428,8 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
             result.minScore = ws.end;
             result.minScoreOffset = pos;
         }
-        if (Fill) result.maxX = imax(result.maxX, ws_max_xscore(ws, seqOffset, cost, 64, Mh));
+        if (Fill && (!boundOk || xscore_bound(ws, seqOffset, cost) > (int64_t)imax(sliceMaxX, result.maxX)))
+            result.maxX = imax(result.maxX, ws_max_xscore(ws, seqOffset, cost, 64, Mh));
         if (!Fill) cols[pos] = ws;
         outHP |= (Ph >> 63) << pos;
         outHN |= (Mh >> 63) << pos;
@@ -625,7 +645,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
             HSlot* q = hash_find(prevHash, hcap, prevGen, g.inNb[g.inOff[i]]);
             singleInPrev = q && q->band >= 0;
         }
-        NodeCalc nc = node_calc<true>(g, a.cost, i, thisNode, eqv, prev, w.extras, s->head, nullptr, singleInPrev, seqOffset, nullptr, steps, err);
+        NodeCalc nc = node_calc<true>(g, a.cost, i, thisNode, eqv, prev, w.extras, s->head, nullptr, singleInPrev, seqOffset, nullptr, steps, err, res.maxX);
         if (err) return res;
         heap_pop(w.heap, heapN);
         s->active = 0;

@@ -802,6 +802,46 @@ SeedLoopPool::~SeedLoopPool() = default;
 
 size_t SeedLoopPool::active() const { return impl->live.size() + impl->finished.size(); }
 
+void SeedLoopPool::addMany(std::vector<ReadInput>& reads, const std::vector<uint64_t>& tags)
+{
+    // orderSeeds and the reverse complement of every read on all cores, then the pool update
+    std::vector<Impl::Live> ls(reads.size());
+    parallelFor(reads.size(), [&](size_t i)
+    {
+        Impl::Live& l = ls[i];
+        l.r.reset(new ReadState());
+        l.tag = tags[i];
+        ReadState& r = *l.r;
+        r.name = std::move(reads[i].name);
+        r.seq = std::move(reads[i].seq);
+        r.seeds = std::move(reads[i].seeds);
+        if (r.seeds.size() == 0)
+        {
+            r.done = true;
+            l.noSeeds = true;
+            return;
+        }
+        try
+        {
+            orderSeeds(impl->g, r.seeds);
+            r.rev = reverseComplement(r.seq);
+        }
+        catch (const ReadFailure&)
+        {
+            r.done = true;
+            r.failed = true;
+            return;
+        }
+        r.extendSeeds = (size_t)(impl->p.seedExtendDensity * r.seq.size() + 1);
+        if (impl->p.seedExtendDensity == -1) r.extendSeeds = r.seeds.size();
+    });
+    for (auto& l : ls)
+    {
+        if (l.r->done) impl->finished.push_back(std::move(l));
+        else impl->live.push_back(std::move(l));
+    }
+}
+
 void SeedLoopPool::add(ReadInput&& read, uint64_t tag)
 {
     Impl::Live l;
@@ -847,11 +887,22 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
     auto& pending = impl->pending;
     pending.clear();
     requests.clear();
-    size_t keep = 0;
-    for (size_t i = 0; i < impl->live.size(); i++)
+    // every read advances its own seed loop (all cores); the requests are then gathered in
+    // read order, backward extension before forward, as a serial loop would emit them
+    struct Next
     {
-        Impl::Live& l = impl->live[i];
-        ReadState& r = *l.r;
+        int state = 0;           // 0 pending, 1 loop ended, 2 failed
+        size_t seed = 0;
+        int count = 0;
+        int backward = -1;       // index into q, or -1
+        int forward = -1;
+        ExtensionRequest q[2];
+    };
+    std::vector<Next> next(impl->live.size());
+    parallelFor(impl->live.size(), [&](size_t i)
+    {
+        ReadState& r = *impl->live[i].r;
+        Next& nx = next[i];
         size_t seedIndex = 0;
         bool more = false;
         try
@@ -864,23 +915,19 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
         }
         if (!more)
         {
-            r.done = true;
-            impl->finished.push_back(std::move(l));
-            continue;
+            nx.state = 1;
+            return;
         }
         const SeedHit& s = r.seeds[seedIndex];
-        Impl::Pending pe;
-        pe.r = &r;
-        pe.seed = seedIndex;
+        nx.seed = seedIndex;
         int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
-        const size_t firstRequest = requests.size();
         try
         {
             GAH_ASSERT(s.seqPos < r.seq.size());
             if (s.seqPos > 0)
             {
                 auto rp = g.reversePosition(forwardNodeId, s.nodeOffset);
-                ExtensionRequest q;
+                ExtensionRequest& q = nx.q[nx.count];
                 q.seq = r.rev.data() + r.rev.size() - s.seqPos;
                 q.len = s.seqPos;
                 q.bignode = rp.first;
@@ -888,12 +935,11 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
                 size_t node = g.unitigNode(q.bignode, q.offset);
                 q.node = (uint32_t)node;
                 q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
-                pe.backward = (int64_t)requests.size();
-                requests.push_back(q);
+                nx.backward = nx.count++;
             }
             if (s.seqPos < r.seq.size() - 1)
             {
-                ExtensionRequest q;
+                ExtensionRequest& q = nx.q[nx.count];
                 q.seq = r.seq.data() + s.seqPos + 1;
                 q.len = r.seq.size() - s.seqPos - 1;
                 q.bignode = forwardNodeId;
@@ -901,17 +947,38 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
                 size_t node = g.unitigNode(q.bignode, q.offset);
                 q.node = (uint32_t)node;
                 q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
-                pe.forward = (int64_t)requests.size();
-                requests.push_back(q);
+                nx.forward = nx.count++;
             }
         }
         catch (const ReadFailure&)
         {
-            requests.resize(firstRequest);
             r.failed = true;
-            r.done = true;
+            nx.state = 2;
+        }
+    });
+    size_t keep = 0;
+    for (size_t i = 0; i < impl->live.size(); i++)
+    {
+        Impl::Live& l = impl->live[i];
+        Next& nx = next[i];
+        if (nx.state != 0)
+        {
+            l.r->done = true;
             impl->finished.push_back(std::move(l));
             continue;
+        }
+        Impl::Pending pe;
+        pe.r = l.r.get();
+        pe.seed = nx.seed;
+        if (nx.backward >= 0)
+        {
+            pe.backward = (int64_t)requests.size();
+            requests.push_back(nx.q[nx.backward]);
+        }
+        if (nx.forward >= 0)
+        {
+            pe.forward = (int64_t)requests.size();
+            requests.push_back(nx.q[nx.forward]);
         }
         pending.push_back(pe);
         if (keep != i) impl->live[keep] = std::move(l);
@@ -1007,7 +1074,9 @@ void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadIn
 {
     out.assign(reads.size(), ReadOutput {});
     SeedLoopPool pool(g, p);
-    for (size_t i = 0; i < reads.size(); i++) pool.add(std::move(reads[i]), i);
+    std::vector<uint64_t> tags(reads.size());
+    for (size_t i = 0; i < reads.size(); i++) tags[i] = i;
+    pool.addMany(reads, tags);
     std::vector<ExtensionRequest> requests;
     std::vector<ExtensionResult> results;
     while (pool.collect(requests))

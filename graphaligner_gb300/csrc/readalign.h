@@ -156,6 +156,8 @@ public:
     SeedLoopPool(const HostGraph& g, const ReadAlignParams& p);
     ~SeedLoopPool();
     void add(ReadInput&& read, uint64_t tag);
+    // the same for a group of reads, prepared on all cores (reads are moved from)
+    void addMany(std::vector<ReadInput>& reads, const std::vector<uint64_t>& tags);
     // reads joined and not yet taken out by takeFinished
     size_t active() const;
     // the next extension requests (they point into the pool's reads); false when no read

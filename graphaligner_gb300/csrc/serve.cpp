@@ -121,13 +121,15 @@ static void serve_loop(ga_server* s)
             std::vector<gahost::ReadInput> reads;
             const int rc = ga_aligner_seed(a, n, names.data(), (const uint8_t*)blob.data(), offs.data(), lens.data(), reads);
             const auto now = Clock::now();
+            std::vector<uint64_t> tags(n);
             for (uint32_t i = 0; i < n; i++)
             {
                 flight[adm[i].ticket] = Flight { adm[i].submit, now, (uint64_t)adm[i].seq.size() * s->bytesPerBp, group };
                 groupsInFlight[group]++;
+                tags[i] = adm[i].ticket;
                 if (rc != GA_OK) failedSeeding.emplace_back(adm[i].ticket, rc);
-                else pool.add(std::move(reads[i]), adm[i].ticket);
             }
+            if (rc == GA_OK) pool.addMany(reads, tags);
             s->stats.admissions++;
         }
         if (pool.collect(rq))
