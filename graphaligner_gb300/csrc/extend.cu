@@ -228,7 +228,7 @@ static constexpr i32 kXBoundOffsetLimit = 10000000;
 template <bool Fill>
 __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const EqV4& eqv, const PrevInfo& prev,
     const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, WS* cols, u64& steps, int& err,
-    i32 sliceMaxX = kIntMin)
+    i32 sliceMaxX = kIntMin, u32 lastColumn = 63)
 {
     // The slice keeps the first node of strictly greatest X-score and the node keeps its
     // greatest column, so a column whose bound is at most max(slice so far, node so far)
@@ -401,7 +401,9 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
     const u64 forceEq = prev.exists ? kAllOnes : (kAllOnes ^ 1);
     u64 outHP = 0, outHN = 0;
     u32 pos = 1;
-    for (; pos < nodeLength; pos++)
+    // the traceback's recomputation stops at the column it needs last
+    const u32 columns = Fill ? nodeLength : (lastColumn + 1 < nodeLength ? lastColumn + 1 : nodeLength);
+    for (; pos < columns; pos++)
     {
         u64 eq;
         if (!amb)
@@ -989,8 +991,11 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
     return out;
 }
 
-// recalcNodeWordslice (Common.h:1078-1102): all columns of one node-slice
-__device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, WS* cols)
+// recalcNodeWordslice (Common.h:1078-1102): the columns 0..lastColumn of one node-slice
+// (the traceback only moves left inside a node, so it never needs the columns after the
+// one it enters at).  When every column is recomputed the last one must equal the
+// stored end column, as the reference asserts.
+__device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, WS* cols, u32 lastColumn = 63)
 {
     const Item* it = c.t.find(s, node);
     if (!it) { c.err = GA_ASSERT; return false; }
@@ -1003,10 +1008,11 @@ __device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, WS* cols)
     u64 steps = 0;
     int err = 0;
     int64_t j = ((int64_t)s - 1) * 64;
-    node_calc<false>(*c.g, c.cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, cols, steps, err);
+    node_calc<false>(*c.g, c.cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, cols, steps, err, kIntMin, lastColumn);
     if (err) { c.err = err; return false; }
     u32 L = c.g->len[node];
-    if (!ws_eq(cols[0], start) || !ws_eq(cols[L - 1], ws_make(it->eVP, it->eVN, it->eEnd))) { c.err = GA_ASSERT; return false; }
+    if (!ws_eq(cols[0], start)) { c.err = GA_ASSERT; return false; }
+    if (lastColumn + 1 >= L && !ws_eq(cols[L - 1], ws_make(it->eVP, it->eVN, it->eEnd))) { c.err = GA_ASSERT; return false; }
     return true;
 }
 
@@ -1084,6 +1090,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
         to.push(start, false);
         u32 curSlice = (u32)(start.seq / 64) + 1;
         u32 curNode = 0xffffffffu;
+        u32 colsUpTo = 0;             // columns 0..colsUpTo of (curSlice, curNode) are in cols
         if (!eq_vector(c.seq, c.seqLen, ((int64_t)curSlice - 1) * 64, eqv)) c.err = GA_ASSERT;
         i32 lastScore = kIntMax - 1;
         u64 guard = 0;
@@ -1094,13 +1101,15 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
             TPos b = to.back;
             u32 newSlice = (u32)(b.seq / 64) + 1;
             if (newSlice >= st.committed) { c.err = GA_ASSERT; break; }
-            if (newSlice != curSlice || b.node != curNode)
+            // a self-loop can re-enter the same node-slice further right than it was computed
+            if (newSlice != curSlice || b.node != curNode || b.off > colsUpTo)
             {
                 if (newSlice != curSlice && !eq_vector(c.seq, c.seqLen, ((int64_t)newSlice - 1) * 64, eqv)) { c.err = GA_ASSERT; break; }
                 curSlice = newSlice;
                 curNode = b.node;
                 if (curSlice == 0) { c.err = GA_ASSERT; break; }
-                if (!recalc(c, curSlice, curNode, eqv, cols)) break;
+                if (!recalc(c, curSlice, curNode, eqv, cols, b.off)) break;
+                colsUpTo = b.off;
             }
             const int64_t sj = ((int64_t)curSlice - 1) * 64;
             if (b.off >= g.len[curNode]) { c.err = GA_ASSERT; break; }
