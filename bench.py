@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--plain-reads", type=int, default=40, help="serve: reads timed one ga_align_reads call each")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serve: seconds of Poisson arrivals per rate")
     ap.add_argument("--cpu-reads", type=int, default=40, help="read-level: reads of the CPU baseline sample")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="extend: keep the default launch shape")
     ap.add_argument("--truncate", type=int, default=0, help="extend: cut every extension to this many bases (small profiling cases)")
     ap.add_argument("--arena-gb", type=float, default=0, help="extend: DP-table arena size (default: from the batch)")
     return ap.parse_args()
@@ -153,27 +154,13 @@ def cpu_baseline(g, batch, params, sample_bp: float, threads: int):
     step = max(1, int(lens.sum() / sample_bp))
     idx = np.arange(0, batch.num, step)
     seqs = [bytes(batch.seq[int(batch.seq_offset[i]):int(batch.seq_offset[i]) + int(lens[i])]) for i in idx]
-    sub = _subset(batch, idx)
+    sub = batch.subset(idx)
     t = time.perf_counter()
     res = oracle.extend(g, params, sub, threads=threads)
     dt = time.perf_counter() - t
     bp = aligned_bp(res)
     return {"value": bp / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(idx)} of {batch.num} extensions (every {step}th, {int(lens[idx].sum())} read bp), oracle restatement in C++, {threads} threads, {dt:.1f} s"}, res, idx
-
-
-def _subset(batch, idx):
-    from graphaligner_gb300.extend import PackedBatch, trace_capacity_for
-    lens = batch.seq_len[idx]
-    offs = np.zeros(len(idx), dtype=np.uint64)
-    if len(idx) > 1:
-        offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
-    seq = np.concatenate([batch.seq[int(batch.seq_offset[i]):int(batch.seq_offset[i]) + int(batch.seq_len[i])] for i in idx])
-    cap = trace_capacity_for(lens)
-    toff = np.zeros(len(idx), dtype=np.uint64)
-    if len(idx) > 1:
-        toff[1:] = np.cumsum(cap[:-1].astype(np.uint64))
-    return PackedBatch(seq, offs, lens.copy(), batch.start_node[idx].copy(), batch.start_offset[idx].copy(), toff, cap)
 
 
 def run_reference(args, rank, world):
@@ -429,6 +416,8 @@ def main():
     if args.arena_gb:
         arena = int(args.arena_gb * (1 << 30))
     ext = Extender(dgraph, arena_bytes=arena)
+    # launch shape for this workload class, tuned on every 4th extension before the timed region
+    tuning = ext.autotune(params, batch, sample_every=4) if args.autotune else {"chosen": ext.launch_shape().as_dict()}
 
     # ---- device-resident batch ----
     dev = torch.device("cuda", local)
@@ -590,6 +579,7 @@ def main():
                    "l2": "inputs larger than L2 (sequences + DP-table arena written every step)",
                    "parallelism": f"replicas{world}"},
         "gcups": gcups,
+        "launch_shape": tuning,
         "gpu_launches": launches,
         "statuses": statuses,
         "kernel_ms": statistics.median(kernel_ms), "wall_s_timed_region": wall,

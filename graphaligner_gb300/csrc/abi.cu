@@ -78,8 +78,8 @@ struct ga_extender
     ga_graph* graph = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] {};
-    cudaStream_t side = nullptr;          // the one-extension-per-warp launch runs beside the bulk one
     int sms = 0;
+    ga_launch_shape shape {};             // how the longest-first order is cut into warp chunks
     int block = 128;
     gadev::Caps caps {};
     uint8_t* workspace = nullptr;
@@ -91,12 +91,14 @@ struct ga_extender
     float lastFillMs = 0;
     float lastTraceMs = 0;
     uint64_t lastArenaBytes = 0;
-    uint32_t lastDedicated = 0;
+    uint32_t lastDedicated = 0;             // single-lane chunks of the last batch
+    uint32_t lastChunks = 0;
     uint32_t lastLaunches = 0;
+    std::vector<uint32_t> chunkHost;
     // host-batch staging
     DevBuf<uint8_t> seq;
     DevBuf<uint64_t> seqOff, traceOff, traceItems, cellSteps;
-    DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order;
+    DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order, chunks;
     DevBuf<int32_t> status, score, prevStatus;
 };
 
@@ -169,11 +171,26 @@ extern "C" int ga_graph_free(ga_graph_t g)
     return GA_OK;
 }
 
-// Extensions at least this many times the median length run one per warp (lane 0
-// alone), the rest 32 per warp in longest-first groups; at most kMaxDedicated
-// warps per SM are given to the long ones.
-static constexpr double kDedicatedFactor = 4.0;
-static constexpr uint32_t kMaxDedicated = 8;
+// Default chunking of the longest-first order (chosen by timing launch shapes on the
+// 5 Mbp variation-graph batch; results do not depend on it): extensions of at least
+// twice the median length (and over 2 kbp) run one per warp, at most 12 per SM; the
+// rest run 16 per warp.
+static ga_launch_shape default_shape()
+{
+    ga_launch_shape sh;
+    sh.single_factor = 2.0;
+    sh.single_min_bp = 2048;
+    sh.single_per_sm = 12;
+    sh.mid_factor = 1.0;
+    sh.mid_lanes = 16;
+    sh.bulk_lanes = 16;
+    return sh;
+}
+
+static bool shape_ok(const ga_launch_shape& sh)
+{
+    return sh.single_factor > 0 && sh.mid_factor > 0 && sh.mid_lanes >= 1 && sh.mid_lanes <= 32 && sh.bulk_lanes >= 1 && sh.bulk_lanes <= 32;
+}
 
 static gadev::Caps base_caps()
 {
@@ -206,12 +223,12 @@ extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_ext
     GA_CUDA(cudaGetDeviceProperties(&prop, graph->device));
     x->sms = prop.multiProcessorCount;
     x->caps = base_caps();
+    x->shape = default_shape();
     int occ = std::max(1, ga_extend_occupancy(x->block));
-    uint64_t slots = (uint64_t)x->sms * occ * x->block + (uint64_t)x->sms * kMaxDedicated * 32;
+    uint64_t slots = (uint64_t)x->sms * occ * x->block;
     uint64_t stride = ga_workspace_bytes(x->caps);
     x->workspaceBytes = slots * stride;
     GA_CUDA(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking));
-    GA_CUDA(cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking));
     for (auto& e : x->ev) GA_CUDA(cudaEventCreate(&e));
     cudaError_t e = cudaMalloc((void**)&x->workspace, x->workspaceBytes);
     if (e != cudaSuccess) { delete x; return cuda_fail(e, "workspace"); }
@@ -237,10 +254,9 @@ extern "C" int ga_extender_free(ga_extender_t x)
     cudaFree(x->arenaCursor);
     x->seq.release(); x->seqOff.release(); x->traceOff.release(); x->traceItems.release(); x->cellSteps.release();
     x->seqLen.release(); x->startNode.release(); x->startOffset.release(); x->traceCap.release(); x->traceLen.release();
-    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release();
+    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release(); x->chunks.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
-    cudaStreamDestroy(x->side);
     delete x;
     return GA_OK;
 }
@@ -286,13 +302,7 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     ta.cellSteps = r->cell_steps;
 
     const uint32_t n = b->num;
-    uint32_t dedicated = 0;
-    if (n > 0)
-    {
-        const double median = sortedLen[n / 2];
-        while (dedicated < n && dedicated < (uint32_t)x->sms * kMaxDedicated && sortedLen[dedicated] >= kDedicatedFactor * median && sortedLen[dedicated] > 2048)
-            dedicated++;
-    }
+    if (n >= (1u << 26)) return fail(GA_ERR_ARGUMENT, "at most 2^26 - 1 extensions per batch");
     x->lastFillMs = 0;
     x->lastTraceMs = 0;
     x->lastLaunches = 0;
@@ -312,33 +322,40 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
         fa.workspaceStride = stride;
         fa.prevStatus = round > 0 ? prevStatus : nullptr;
         ta.prevStatus = fa.prevStatus;
-        const uint32_t ded = round == 0 ? dedicated : 0;
-        // every thread of a launch owns one workspace slot: the dedicated launch gets whole
-        // blocks at the top of the slot range, the bulk launch whole blocks below them
-        const int dedGrid = (int)(((uint64_t)ded * 32 + x->block - 1) / x->block);
-        const uint64_t dedSlots = (uint64_t)dedGrid * x->block;
-        const uint64_t bulkSlots = slots > dedSlots ? slots - dedSlots : 0;
-        const uint32_t bulkCount = n - ded;
-        if (bulkCount > 0 && bulkSlots < (uint64_t)x->block) return fail(GA_ERR_CUDA, "workspace too small for the batch's capacities");
-        const int bulkGrid = (int)std::max<uint64_t>(1, std::min<uint64_t>(bulkSlots / x->block, ((uint64_t)bulkCount + x->block - 1) / x->block));
+        // chunk table over the longest-first order: (first position << 6) | (size - 1)
+        auto& ch = x->chunkHost;
+        ch.clear();
+        uint32_t pos = 0, singles = 0;
+        auto emit = [&](uint32_t size) { ch.push_back((pos << 6) | (size - 1)); pos += size; };
+        if (round == 0 && n > 0)
+        {
+            const ga_launch_shape& sh = x->shape;
+            const double median = sortedLen[n / 2];
+            const uint64_t maxSingles = (uint64_t)x->sms * sh.single_per_sm;
+            while (pos < n && singles < maxSingles && sortedLen[pos] >= sh.single_factor * median && sortedLen[pos] > sh.single_min_bp)
+            {
+                emit(1);
+                singles++;
+            }
+            while (pos < n && sortedLen[pos] >= sh.mid_factor * median) emit(std::min(sh.mid_lanes, n - pos));
+            while (pos < n) emit(std::min(sh.bulk_lanes, n - pos));
+        }
+        else
+        {
+            while (pos < n) emit(std::min(32u, n - pos));
+        }
+        const uint32_t numChunks = (uint32_t)ch.size();
+        GA_CUDA(x->chunks.reserve(std::max<uint32_t>(numChunks, 1)));
+        GA_CUDA(cudaMemcpyAsync(x->chunks.ptr, ch.data(), (size_t)numChunks * 4, cudaMemcpyHostToDevice, stream));
+        // every thread owns one workspace slot; a warp works one chunk at a time
+        if (slots < (uint64_t)x->block) return fail(GA_ERR_CUDA, "workspace too small for the batch's capacities");
+        const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(slots / x->block, ((uint64_t)numChunks * 32 + x->block - 1) / x->block));
         GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), stream));
         GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, sizeof(unsigned long long), stream));
         GA_CUDA(cudaEventRecord(x->ev[0], stream));
-        if (ded > 0)
-        {
-            GA_CUDA(cudaStreamWaitEvent(x->side, x->ev[0], 0));
-            ga_launch_extend(fa, ta, 1, 0, ded, x->counters + 3, (uint32_t)bulkSlots, (uint32_t)(bulkSlots + dedSlots), dedGrid, x->block, x->side);
-            GA_CUDA(cudaGetLastError());
-            GA_CUDA(cudaEventRecord(x->ev[3], x->side));
-            x->lastLaunches += 1;
-        }
-        if (bulkCount > 0)
-        {
-            ga_launch_extend(fa, ta, 32, ded, bulkCount, x->counters, 0, (uint32_t)bulkSlots, bulkGrid, x->block, stream);
-            GA_CUDA(cudaGetLastError());
-            x->lastLaunches += 1;
-        }
-        if (ded > 0) GA_CUDA(cudaStreamWaitEvent(stream, x->ev[3], 0));
+        ga_launch_extend(fa, ta, x->chunks.ptr, numChunks, x->counters, 0, (uint32_t)((uint64_t)grid * x->block), grid, x->block, stream);
+        GA_CUDA(cudaGetLastError());
+        x->lastLaunches += 1;
         GA_CUDA(cudaEventRecord(x->ev[1], stream));
         count_status_kernel<<<64, 256, 0, stream>>>(r->status, n, GA_CAPACITY, x->counters + 2);
         GA_CUDA(cudaGetLastError());
@@ -348,11 +365,15 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
         GA_CUDA(cudaMemcpyAsync(&capFails, x->counters + 2, 4, cudaMemcpyDeviceToHost, stream));
         GA_CUDA(cudaMemcpyAsync(&arenaUsed, x->arenaCursor, 8, cudaMemcpyDeviceToHost, stream));
         GA_CUDA(cudaStreamSynchronize(stream));
-        if (round == 0) x->lastArenaBytes = std::min<uint64_t>(arenaUsed, x->arenaBytes);
+        if (round == 0)
+        {
+            x->lastArenaBytes = std::min<uint64_t>(arenaUsed, x->arenaBytes);
+            x->lastDedicated = singles;
+            x->lastChunks = numChunks;
+        }
         float ms = 0;
         GA_CUDA(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
         x->lastFillMs += ms;
-        x->lastDedicated = ded;
         if (capFails == 0) break;
     }
     return GA_OK;
@@ -469,6 +490,21 @@ extern "C" int ga_extender_last_launches(ga_extender_t x, uint32_t* launches)
 {
     if (!x || !launches) return fail(GA_ERR_ARGUMENT, "null argument");
     *launches = x->lastLaunches;
+    return GA_OK;
+}
+
+extern "C" int ga_extender_set_launch_shape(ga_extender_t x, const ga_launch_shape* shape)
+{
+    if (!x || !shape) return fail(GA_ERR_ARGUMENT, "null argument");
+    if (!shape_ok(*shape)) return fail(GA_ERR_ARGUMENT, "launch shape: factors must be positive and lane counts within 1..32");
+    x->shape = *shape;
+    return GA_OK;
+}
+
+extern "C" int ga_extender_get_launch_shape(ga_extender_t x, ga_launch_shape* shape)
+{
+    if (!x || !shape) return fail(GA_ERR_ARGUMENT, "null argument");
+    *shape = x->shape;
     return GA_OK;
 }
 

@@ -1394,11 +1394,13 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
 }
 
 // One persistent kernel per batch: a thread fills the DP table of an extension
-// and walks it back right away.  Warps take `lanesPerWarp` consecutive entries of
-// the longest-first order at a time, so the lanes of a warp hold extensions of
-// similar length; with lanesPerWarp = 1 a warp runs one extension on lane 0 alone,
-// which keeps the longest extensions free of divergence with their neighbours.
-__global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, u32 lanesPerWarp, u32 first, u32 count,
+// and walks it back right away.  Warps take chunks of the longest-first order from
+// a chunk table the host builds (ga_launch_shape): a chunk is up to 32 consecutive
+// extensions, one per lane, so the lanes of a warp hold extensions of similar
+// length.  The longest extensions come in chunks of one (lane 0 alone), which keeps
+// them free of divergence with other lanes; the chunk sizes trade divergence within
+// a warp against the number of extensions in flight.
+__global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, const u32* chunks, u32 numChunks,
     u32* counter, u32 slotBase, u32 slotLimit)
 {
     load_iupac_table();
@@ -1414,13 +1416,15 @@ __global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, 
     const u32 lane = threadIdx.x & 31;
     while (true)
     {
-        u32 base = 0;
-        if (lane == 0) base = atomicAdd(counter, lanesPerWarp);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) break;
-        if (lane < lanesPerWarp && base + lane < count)
+        u32 ci = 0;
+        if (lane == 0) ci = atomicAdd(counter, 1u);
+        ci = __shfl_sync(0xffffffffu, ci, 0);
+        if (ci >= numChunks) break;
+        // chunk = first position in the order (high 26 bits) and size - 1 (low 6 bits)
+        const u32 chunk = chunks[ci];
+        if (lane <= (chunk & 63u))
         {
-            const u32 ext = fa.order[first + base + lane];
+            const u32 ext = fa.order[(chunk >> 6) + lane];
             if (!fa.prevStatus || fa.prevStatus[ext] == GA_CAPACITY)
             {
                 ExtState st = fill_extension(fa, w, gen, arena, ext);
@@ -1440,10 +1444,10 @@ __global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, 
 
 }
 
-void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t lanesPerWarp, uint32_t first, uint32_t count,
+void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, const uint32_t* chunks, uint32_t numChunks,
     uint32_t* counter, uint32_t slotBase, uint32_t slotLimit, int grid, int block, void* stream)
 {
-    gadev::extend_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(fa, ta, lanesPerWarp, first, count, counter, slotBase, slotLimit);
+    gadev::extend_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(fa, ta, chunks, numChunks, counter, slotBase, slotLimit);
 }
 
 int ga_upload_tables()

@@ -116,7 +116,7 @@ struct TraceArgs
 
 }
 
-void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t lanesPerWarp, uint32_t first, uint32_t count,
+void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, const uint32_t* chunks, uint32_t numChunks,
     uint32_t* counter, uint32_t slotBase, uint32_t slotLimit, int grid, int block, void* stream);
 int ga_extend_occupancy(int block);
 int ga_upload_tables();

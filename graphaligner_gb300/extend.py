@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import ptr
-from ._lib import lib, check
+from ._lib import GAError, check, lib
 
 INT32_MAX = 2**31 - 1
 
@@ -65,6 +65,21 @@ class PackedBatch:
     @property
     def total_items(self) -> int:
         return int(self.trace_offset[-1] + self.trace_capacity[-1]) if self.num else 0
+
+    def subset(self, idx) -> "PackedBatch":
+        """The extensions at positions idx, repacked."""
+        idx = np.asarray(idx, dtype=np.int64)
+        lens = self.seq_len[idx]
+        offs = np.zeros(len(idx), dtype=np.uint64)
+        if len(idx) > 1:
+            offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+        parts = [self.seq[int(self.seq_offset[i]):int(self.seq_offset[i]) + int(self.seq_len[i])] for i in idx]
+        seq = np.concatenate(parts) if parts else np.zeros(1, dtype=np.uint8)
+        cap = trace_capacity_for(lens)
+        toff = np.zeros(len(idx), dtype=np.uint64)
+        if len(idx) > 1:
+            toff[1:] = np.cumsum(cap[:-1].astype(np.uint64))
+        return PackedBatch(seq, offs, lens.copy(), self.start_node[idx].copy(), self.start_offset[idx].copy(), toff, cap)
 
     def desc(self):
         return _abi.BatchDesc(self.num, ptr(self.seq, ctypes.c_uint8), ptr(self.seq_offset, ctypes.c_uint64),
@@ -154,6 +169,30 @@ class DeviceGraph:
             pass
 
 
+class LaunchShape(ctypes.Structure):
+    """ga_launch_shape: how the longest-first order is cut into warp chunks (which extensions
+    share a warp; results never depend on it)."""
+    _fields_ = [
+        ("single_factor", ctypes.c_double),
+        ("single_min_bp", ctypes.c_uint32),
+        ("single_per_sm", ctypes.c_uint32),
+        ("mid_factor", ctypes.c_double),
+        ("mid_lanes", ctypes.c_uint32),
+        ("bulk_lanes", ctypes.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+# launch shapes the autotuner tries: (single_factor, single_per_sm, mid_factor, mid_lanes, bulk_lanes)
+DEFAULT_CANDIDATES = [
+    (2.0, 12, 1.0, 16, 16), (2.0, 8, 1.0, 16, 16), (1.5, 16, 1.0, 16, 16), (3.0, 12, 1.0, 16, 16),
+    (2.0, 12, 1.0, 32, 32), (2.0, 12, 1.0, 8, 8), (2.0, 12, 1.3, 8, 16), (2.0, 16, 1.3, 8, 32),
+    (4.0, 8, 1.0, 32, 32),
+]
+
+
 class Extender:
     """Batched getReverseTraceFromSeed on the GPU."""
 
@@ -173,6 +212,42 @@ class Extender:
 
     def extend(self, params: ExtendParams, seqs, bignodes, offsets) -> BatchResult:
         return self.run(params, pack_batch(self.dgraph.graph, seqs, bignodes, offsets))
+
+    def launch_shape(self) -> LaunchShape:
+        sh = LaunchShape()
+        check(lib().ga_extender_get_launch_shape(self.handle, ctypes.byref(sh)))
+        return sh
+
+    def set_launch_shape(self, single_factor=2.0, single_per_sm=12, mid_factor=1.0, mid_lanes=16, bulk_lanes=16, single_min_bp=2048):
+        sh = LaunchShape(single_factor, single_min_bp, single_per_sm, mid_factor, mid_lanes, bulk_lanes)
+        check(lib().ga_extender_set_launch_shape(self.handle, ctypes.byref(sh)))
+
+    def autotune(self, params: ExtendParams, batch: PackedBatch, candidates=None, sample_every: int = 4, repeats: int = 2) -> dict:
+        """Times each launch shape on an evenly spaced sample of the batch (device time of the
+        kernels) and keeps the fastest.  Every candidate must give the same statuses and scores."""
+        idx = np.arange(0, batch.num, max(1, sample_every))
+        sub = batch.subset(idx)
+        out = alloc_results(sub)
+        times = []
+        ref = None
+        for c in candidates or DEFAULT_CANDIDATES:
+            self.set_launch_shape(*c)
+            ms = []
+            for _ in range(repeats):
+                self.run(params, sub, out)
+                f = ctypes.c_float()
+                check(lib().ga_extender_last_kernel_ms(self.handle, ctypes.byref(f)))
+                ms.append(f.value)
+            key = (out.status.copy(), out.score.copy())
+            if ref is None:
+                ref = key
+            elif not (np.array_equal(ref[0], key[0]) and np.array_equal(ref[1], key[1])):
+                raise GAError(f"launch shape {c} changed results")
+            times.append((float(np.median(ms)), c))
+        best = min(times)[1]
+        self.set_launch_shape(*best)
+        return {"chosen": self.launch_shape().as_dict(), "sample_extensions": int(len(idx)),
+                "candidates_ms": [(round(t, 2), list(c)) for t, c in times]}
 
     def last_times(self):
         f = ctypes.c_float()

@@ -146,6 +146,22 @@ int ga_extender_last_kernel_ms(ga_extender_t ext, float* ms);
 int ga_extender_last_times(ga_extender_t ext, float* fill_ms, float* trace_ms);
 /* Number of kernel launches made by the last ga_extend_batch* call. */
 int ga_extender_last_launches(ga_extender_t ext, uint32_t* launches);
+
+/* How a batch's longest-first order is cut into warp chunks (no reference
+ * counterpart: it only decides which extensions share a warp, never a result).
+ * The longest extensions -- at least single_factor x the median length and over
+ * single_min_bp, at most single_per_sm per SM -- run one per warp; then those of at
+ * least mid_factor x the median run mid_lanes per warp; the rest bulk_lanes per warp. */
+typedef struct ga_launch_shape {
+    double   single_factor;
+    uint32_t single_min_bp;
+    uint32_t single_per_sm;
+    double   mid_factor;
+    uint32_t mid_lanes;               /* 1..32 */
+    uint32_t bulk_lanes;              /* 1..32 */
+} ga_launch_shape;
+int ga_extender_set_launch_shape(ga_extender_t ext, const ga_launch_shape* shape);
+int ga_extender_get_launch_shape(ga_extender_t ext, ga_launch_shape* shape);
 /* DP-table bytes the first fill pass of the last call wrote to the arena. */
 int ga_extender_last_arena_bytes(ga_extender_t ext, uint64_t* bytes);
 

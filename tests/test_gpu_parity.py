@@ -92,3 +92,23 @@ def test_gpu_matches_oracle_generated(cuda_lib, oracle_lib):
         gpu = x.run(p, batch)
         ref = oracle_lib.extend(g, p, batch, threads=8)
         _assert_same(gpu, ref, batch.num)
+
+
+def test_launch_shapes_do_not_change_results(cuda_lib):
+    """Which extensions share a warp never changes a result: every chunking of the
+    longest-first order gives the reference's digests."""
+    from graphaligner_gb300._lib import GAError
+    g, batch = golden_case("vg50k")
+    x = Extender(DeviceGraph(g))
+    expected = load_digests("vg50k", 10)
+    for shape in [(2.0, 12, 1.0, 16, 16), (0.5, 64, 1.0, 1, 1), (1.0, 1, 0.5, 3, 32), (100.0, 1, 1.5, 32, 7)]:
+        x.set_launch_shape(*shape)
+        res = x.run(ExtendParams(bandwidth=10), batch)
+        bad = compare(res, expected)
+        assert not bad, f"shape {shape}: {len(bad)} extensions differ"
+    with pytest.raises(GAError):
+        x.set_launch_shape(2.0, 12, 1.0, 0, 16)
+    with pytest.raises(GAError):
+        x.set_launch_shape(2.0, 12, 1.0, 16, 33)
+    tuned = x.autotune(ExtendParams(bandwidth=10), batch, sample_every=2, repeats=1)
+    assert tuned["chosen"]["bulk_lanes"] in (7, 8, 16, 32, 1)
