@@ -187,9 +187,9 @@ class LaunchShape(ctypes.Structure):
 
 # launch shapes the autotuner tries: (single_factor, single_per_sm, mid_factor, mid_lanes, bulk_lanes)
 DEFAULT_CANDIDATES = [
-    (2.0, 12, 1.0, 16, 16), (2.0, 8, 1.0, 16, 16), (1.5, 16, 1.0, 16, 16), (3.0, 12, 1.0, 16, 16),
-    (2.0, 12, 1.0, 32, 32), (2.0, 12, 1.0, 8, 8), (2.0, 12, 1.3, 8, 16), (2.0, 16, 1.3, 8, 32),
-    (4.0, 8, 1.0, 32, 32),
+    (2.0, 12, 1.0, 16, 16), (3.0, 12, 1.0, 16, 16), (2.0, 12, 1.0, 8, 8), (2.0, 12, 1.3, 8, 16),
+    (2.0, 16, 1.3, 8, 32), (2.0, 12, 1.3, 4, 16), (2.0, 12, 1.5, 4, 8), (1.5, 16, 1.2, 8, 16),
+    (2.5, 12, 1.3, 8, 16), (2.0, 12, 1.0, 32, 32),
 ]
 
 
