@@ -416,8 +416,15 @@ def main():
     if args.arena_gb:
         arena = int(args.arena_gb * (1 << 30))
     ext = Extender(dgraph, arena_bytes=arena)
-    # launch shape for this workload class, tuned on every 4th extension before the timed region
-    tuning = ext.autotune(params, batch, sample_every=4) if args.autotune else {"chosen": ext.launch_shape().as_dict()}
+    # launch shape for this workload class, tuned before the timed region on an independent batch
+    # of the same class and size (other read seed)
+    if args.autotune:
+        _, tune_batch = make_workload(args.reads, rank + 100, args.truncate)
+        tuning = ext.autotune(params, tune_batch, sample_every=1)
+        tuning["tuned_on"] = f"an independent batch of {tune_batch.num} extensions (read seed {rank + 101})"
+        del tune_batch
+    else:
+        tuning = {"chosen": ext.launch_shape().as_dict()}
 
     # ---- device-resident batch ----
     dev = torch.device("cuda", local)
