@@ -12,6 +12,8 @@ synthetic inputs and stores what it produced:
                    with the read as test_read.fa and the graph as test_graph.gag.gz
   vg50k_reads.fa.gz, vg50k_b{10,5}.gaf.gz   reads and the reference's GAF (-x vg, -b 10 / 5)
   vg50k_seeds.digest  sha1 of every line of MinimizerSeeder::getSeeds + OrderSeeds output
+  iupac20k_*       IUPAC codes in 6 % of the graph's nodes and 1 % of the read bases, lower
+                   case, and edge requests (lengths 1-2, 63-65, 127-129; node first/last base)
   dbg100k_*        the same for a k=63 de Bruijn graph with repeats and tandem arrays
                    (cyclic components), extensions at tangle effort 10000, GAF at -x dbg
 
@@ -97,6 +99,53 @@ def node_lengths(g):
     return nl
 
 
+IUPAC = np.frombuffer(b"NRYKMSWBDHV", dtype=np.uint8)
+
+
+def iupac_edge_set(seed: int = 5):
+    """A 20 kbp variation graph with IUPAC codes in ~6 % of its nodes (a few nodes all N),
+    reads with N / IUPAC codes and lower case, and extension requests at the edges: lengths
+    1, 2, 63-65, 127-129 and starts on a node's first and last base."""
+    rng = np.random.default_rng(seed)
+    g = dg.make_variation_graph(20_000, 100, 0.7, 20, seed)
+    clean = [s.copy() for s in g.node_seqs]
+    for i in range(len(g.node_seqs)):
+        s = g.node_seqs[i] = g.node_seqs[i].copy()
+        if rng.random() < 0.06:
+            if len(s) <= 3 and rng.random() < 0.5:
+                s[:] = ord("N")
+            else:
+                pos = rng.choice(len(s), size=min(len(s), int(rng.integers(1, 4))), replace=False)
+                s[pos] = IUPAC[rng.integers(0, len(IUPAC), len(pos))]
+    # reads from the ACGT graph, then N / IUPAC codes and lower case
+    g_clean = dg.VariationGraph(clean, g.edges, g.sites, g.backbone_nodes)
+    reads = dg.sample_reads(g_clean, 40, seed + 1, dg.uniform_length(200, 6_000), dg.uniform_error(0.03, 0.12))
+    out_reads = []
+    for r in reads:
+        b = np.frombuffer(r.seq, dtype=np.uint8).copy()
+        amb = rng.random(len(b)) < 0.01
+        b[amb] = IUPAC[rng.integers(0, len(IUPAC), int(amb.sum()))]
+        low = rng.random(len(b)) < 0.1
+        b[low] = b[low] + 32          # every base is an upper-case letter here
+        out_reads.append(dg.Read(r.name, b.tobytes(), r.bignode, r.bigoffset, r.exact))
+    ext = dg.seed_extensions(out_reads, node_lengths(g), 15, seed + 2, per_read=2)
+    seqs, nodes, offs = list(ext.seqs), list(ext.bignode), list(ext.offset)
+    nl = node_lengths(g)
+    for k in range(120):
+        nid = int(rng.integers(1, len(g.node_seqs) + 1))
+        strand = int(rng.integers(0, 2))
+        L = int(nl[nid])
+        off = 0 if k % 2 == 0 else L - 1
+        length = [1, 2, 63, 64, 65, 127, 128, 129][k % 8]
+        s_ = dg._BASES[rng.integers(0, 4, length)]
+        if k % 3 == 0:
+            s_[rng.integers(0, length)] = ord("N")
+        seqs.append(s_.tobytes())
+        nodes.append(nid * 2 + strand)
+        offs.append(off)
+    return g, dg.ExtensionSet(seqs, np.array(nodes, dtype=np.int64), np.array(offs, dtype=np.int64))
+
+
 def main():
     if not os.path.exists(REF):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"], check=True)
@@ -139,6 +188,9 @@ def main():
         out = os.path.join(td, "b5.gaf")
         subprocess.run([REF, "align", gfa, fa, out, "dbg"], check=True)
         gz_write(os.path.join(HERE, "dbg100k_b5.gaf.gz"), open(out, "rb").read())
+    # IUPAC codes in graph and reads, lower case, edge lengths and start offsets
+    g_iu, ext_iu = iupac_edge_set(5)
+    make_set("iupac20k", g_iu, ext_iu, [10, 5])
     # the reference's quickstart
     ref_test = "/root/reference/test"
     with tempfile.TemporaryDirectory() as td:

@@ -112,3 +112,18 @@ def test_launch_shapes_do_not_change_results(cuda_lib):
         x.set_launch_shape(2.0, 12, 1.0, 16, 33)
     tuned = x.autotune(ExtendParams(bandwidth=10), batch, sample_every=2, repeats=1)
     assert tuned["chosen"]["bulk_lanes"] in (7, 8, 16, 32, 1)
+
+
+@pytest.mark.parametrize("bandwidth", [10, 5])
+def test_gpu_matches_reference_golden_iupac_edges(cuda_lib, bandwidth):
+    """IUPAC codes in graph nodes (ambiguous-node storage) and in reads, lower case (on which
+    the reference's traceback asserts), and edge requests: lengths 1-2, 63-65, 127-129,
+    starts on a node's first and last base.  Statuses, including the asserts, must match."""
+    g, batch = golden_case("iupac20k")
+    assert g.first_ambiguous < g.num_nodes
+    ext = Extender(DeviceGraph(g))
+    res = ext.run(ExtendParams(bandwidth=bandwidth), batch)
+    expected = load_digests("iupac20k", bandwidth)
+    bad = compare(res, expected)
+    assert not bad, f"{len(bad)} extensions differ, first {bad[:5]}"
+    assert sum(1 for e in expected if e[0] == 2) > 0 and sum(1 for e in expected if e[0] == 0) > 0
