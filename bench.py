@@ -476,6 +476,9 @@ def main():
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     kernel_s = sum(kernel_ms) / 1e3
+    # DP-table bytes of the timed batch (later calls below overwrite the extender's figure)
+    arena_bytes = ctypes.c_uint64()
+    check(L.ga_extender_last_arena_bytes(ext.handle, ctypes.byref(arena_bytes)))
     if world > 1:
         tt = torch.tensor([kernel_s], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -563,10 +566,10 @@ def main():
     # ---- roofline ----
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    arena_bytes = ctypes.c_uint64()
-    check(L.ga_extender_last_arena_bytes(ext.handle, ctypes.byref(arena_bytes)))
     fill_s = statistics.median(kernel_ms) / 1e3
-    alg_bytes = int(batch.seq.nbytes + arena_bytes.value)
+    # algorithmic bytes per launch: the reads, the committed DP slices (written by the fill,
+    # read by the traceback) and the trace items written
+    alg_bytes = int(batch.seq.nbytes + 2 * arena_bytes.value + int(res.trace_len.astype(np.int64).sum()) * 8)
     achieved_gbs = alg_bytes / fill_s / 1e9
     int_peak = ctypes.c_double()
     check(L.ga_measure_int32_peak(local, ctypes.byref(int_peak)))
@@ -594,6 +597,7 @@ def main():
                 "seconds_per_step": statistics.median(e2e_times), "same_results": e2e_same},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak, "traffic": traffic, "kernel": "extend_kernel (fill + traceback, fused)",
+                     "algorithmic_bytes": alg_bytes,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
                      "note": "the fill is integer-ALU / dependency-latency bound, see alu"},
         "alu": {"achieved": alu_achieved, "peak": int_peak.value, "unit": "int32 op/s", "frac": alu_achieved / int_peak.value,
