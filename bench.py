@@ -63,6 +63,21 @@ def parse():
     return ap.parse_args()
 
 
+def combine_ranks(units: float, seconds: float, world: int, device=None):
+    """Whole-job figures of a replicated run: the units all ranks processed and the slowest
+    rank's time (all_reduce SUM / MAX over the default process group); the inputs
+    themselves when world == 1."""
+    if world <= 1:
+        return float(units), float(seconds)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    s = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    dist.all_reduce(s, op=dist.ReduceOp.MAX)
+    return float(t.item()), float(s.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -479,10 +494,6 @@ def main():
     # DP-table bytes of the timed batch (later calls below overwrite the extender's figure)
     arena_bytes = ctypes.c_uint64()
     check(L.ga_extender_last_arena_bytes(ext.handle, ctypes.byref(arena_bytes)))
-    if world > 1:
-        tt = torch.tensor([kernel_s], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        kernel_s = float(tt.item())
 
     # results of the last step
     res = alloc_results(batch)
@@ -499,9 +510,11 @@ def main():
     if cpu_res is not None:
         cpu_agree = bool(np.array_equal(cpu_res.status, res.status[cpu_idx]) and np.array_equal(cpu_res.score, res.score[cpu_idx]))
 
-    value = bp * args.steps * world / kernel_s
+    job_bp, kernel_s = combine_ranks(bp * args.steps, kernel_s, world, dev)
+    value = job_bp / kernel_s
     ms_per_step = kernel_s * 1e3 / args.steps
-    gcups = steps_total * 64 * args.steps / kernel_s / 1e9
+    job_steps, _ = combine_ranks(steps_total * args.steps, kernel_s, world, dev)
+    gcups = job_steps * 64 / kernel_s / 1e9
 
     # ---- end to end through the host-buffer C ABI, pinned host memory ----
     def pinned(nbytes):
@@ -531,7 +544,8 @@ def main():
         ext.run(params, hb, hr)
         e2e_times.append(time.perf_counter() - t)
     e2e_same = bool(np.array_equal(hr.status, res.status) and np.array_equal(hr.score, res.score))
-    e2e_value = bp * world / statistics.median(e2e_times)
+    job_bp_e2e, e2e_s = combine_ranks(bp, statistics.median(e2e_times), world, dev)
+    e2e_value = job_bp_e2e / e2e_s
 
     # ---- the plain form: one launch per extension, waited for, on a sample ----
     plain = None
