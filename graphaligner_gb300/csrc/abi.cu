@@ -243,6 +243,14 @@ extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_ext
     return GA_OK;
 }
 
+extern "C" int ga_extender_create_like(ga_extender_t x, ga_extender_t* out)
+{
+    if (!x || !out) return fail(GA_ERR_ARGUMENT, "null argument");
+    int rc = ga_extender_create(x->graph, x->arenaBytes, out);
+    if (rc == GA_OK) (*out)->shape = x->shape;
+    return rc;
+}
+
 extern "C" int ga_extender_free(ga_extender_t x)
 {
     if (!x) return GA_OK;

@@ -13,6 +13,9 @@
 #include "aligner.h"
 #include "../../include/graphaligner_gb300.h"
 
+// below this many reads a batch runs on one extender (a round would be too small to split)
+static constexpr uint32_t kTwoLaneMinReads = 256;
+
 static double ms_since(std::chrono::steady_clock::time_point t)
 {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
@@ -20,7 +23,7 @@ static double ms_since(std::chrono::steady_clock::time_point t)
 
 void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs)
 {
-    ga_aligner* a = (ga_aligner*)ctx;
+    ExtendLane* a = (ExtendLane*)ctx;
     const size_t n = rq.size();
     const auto tStage = std::chrono::steady_clock::now();
     bool ok = a->off.reserve(n) && a->len.reserve(n) && a->node.reserve(n) && a->nodeOff.reserve(n) && a->cap.reserve(n)
@@ -46,8 +49,8 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
         ga_extend_results r { a->status.data(), a->score.data(), a->tlen.data(), a->items.data(), a->steps.data() };
         a->stagingMs += ms_since(tStage);
         auto t0 = std::chrono::steady_clock::now();
-        rc = ga_extend_batch(a->ext, &a->params.extend, &b, &r);
-        a->stats.extend_ms += ms_since(t0);
+        rc = ga_extend_batch(a->ext, a->params, &b, &r);
+        a->extendMs += ms_since(t0);
         a->launches++;
     }
     else
@@ -67,6 +70,17 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
         rs[i].itemPtr = a->items.data() + a->toff[i];
         rs[i].itemCount = a->tlen[i];
     }
+}
+
+int ga_aligner_second_lane(ga_aligner* a)
+{
+    ExtendLane& l = a->lanes[1];
+    if (l.ext) return GA_OK;
+    int rc = ga_extender_create_like(a->ext, &l.ext);
+    if (rc != GA_OK) return rc;
+    l.owned = true;
+    l.params = &a->params.extend;
+    return GA_OK;
 }
 
 gahost::ReadAlignParams ga_aligner_read_params(const ga_aligner* a)
@@ -156,6 +170,8 @@ extern "C" int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* gr
     }
     ga_aligner* a = new ga_aligner();
     a->ext = ext;
+    a->lanes[0].ext = ext;
+    a->lanes[0].params = &a->params.extend;
     a->params = *params;
     cudaGetDevice(&a->device);
     try
@@ -211,7 +227,6 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     if (!a || (n > 0 && (!names || !seq || !seqOffset || !seqLen))) return GA_ERR_ARGUMENT;
     auto start = std::chrono::steady_clock::now();
     a->stats = ga_align_stats {};
-    a->stagingMs = 0;
     a->stats.reads = n;
     a->gaf.clear();
     a->readBp.assign(n, 0);
@@ -227,7 +242,14 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     gahost::ReadAlignParams rp = ga_aligner_read_params(a);
     std::vector<gahost::ReadOutput> outs;
     gahost::BatchStats bs;
-    gahost::alignBatch(*a->graph, rp, reads, ga_aligner_extend, a, outs, bs);
+    for (auto& l : a->lanes) { l.extendMs = 0; l.stagingMs = 0; }
+    // two groups of reads on two extenders, the host finishing one group's round while
+    // the other's runs on the GPU; small batches use one
+    if (n >= kTwoLaneMinReads && ga_aligner_second_lane(a) == GA_OK)
+        gahost::alignBatchTwoLanes(*a->graph, rp, reads, ga_aligner_extend, &a->lanes[0], &a->lanes[1], outs, bs);
+    else
+        gahost::alignBatch(*a->graph, rp, reads, ga_aligner_extend, &a->lanes[0], outs, bs);
+    a->stats.extend_ms = a->lanes[0].extendMs + a->lanes[1].extendMs;
     size_t gafBytes = 0;
     for (uint32_t i = 0; i < n; i++) gafBytes += outs[i].gaf.size();
     a->gaf.reserve(gafBytes);
@@ -238,7 +260,7 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
         if (outs[i].alignments > 0) a->stats.reads_aligned++;
     }
     a->stats.collect_ms = bs.collectMs;
-    a->stats.staging_ms = a->stagingMs;
+    a->stats.staging_ms = a->lanes[0].stagingMs + a->lanes[1].stagingMs;
     a->stats.consume_ms = bs.consumeMs;
     a->stats.finish_ms = bs.finishMs;
     a->stats.failed_reads = bs.failedReads;
@@ -246,7 +268,8 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     a->stats.rounds = bs.rounds;
     a->stats.extensions = bs.extensions;
     a->stats.cell_steps = bs.cellSteps;
-    a->stats.host_ms = ms_since(start) - a->stats.extend_ms;
+    // with two lanes the GPU calls overlap host work: host_ms is what they do not cover
+    a->stats.host_ms = std::max(0.0, ms_since(start) - a->stats.extend_ms);
     return GA_OK;
 }
 

@@ -8,6 +8,51 @@
 #include "seed_kernel.cuh"
 #include "../../include/graphaligner_gb300.h"
 
+// pinned host staging, grown as needed, never cleared
+template <typename T>
+struct Pinned
+{
+    T* p = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t n)
+    {
+        if (n <= cap) return true;
+        size_t want = std::max(n, cap + cap / 2);
+        void* q = nullptr;
+        if (cudaHostAlloc(&q, want * sizeof(T), cudaHostAllocDefault) != cudaSuccess) return false;
+        if (p) cudaFreeHost(p);
+        p = (T*)q;
+        cap = want;
+        return true;
+    }
+    void release() { if (p) cudaFreeHost(p); p = nullptr; cap = 0; }
+    T* data() { return p; }
+    T& operator[](size_t i) { return p[i]; }
+};
+
+// One extender and the staging of its batches: ga_aligner_extend's context.  Two lanes
+// let one group of reads extend on the GPU while the host finishes the other group.
+struct ExtendLane
+{
+    ga_extender_t ext = nullptr;
+    bool owned = false;        // created by the aligner (the second lane), freed with it
+    const ga_extend_params* params = nullptr;
+    Pinned<uint8_t> blob;
+    Pinned<uint64_t> off, toff, items, steps;
+    Pinned<uint32_t> len, node, nodeOff, cap, tlen;
+    Pinned<int32_t> status, score;
+    double extendMs = 0;       // ga_extend_batch calls
+    double stagingMs = 0;      // packing requests and handing results over
+    uint64_t launches = 0;
+    ~ExtendLane()
+    {
+        blob.release(); off.release(); toff.release(); items.release(); steps.release();
+        len.release(); node.release(); nodeOff.release(); cap.release(); tlen.release();
+        status.release(); score.release();
+        if (owned && ext) ga_extender_free(ext);
+    }
+};
+
 struct ga_aligner
 {
     ga_extender_t ext = nullptr;
@@ -20,40 +65,8 @@ struct ga_aligner
     std::string gaf;
     std::vector<uint64_t> readBp;
     ga_align_stats stats {};
-    uint64_t launches = 0;
     cudaStream_t stream = nullptr;
-    // staging of one extension batch: pinned, grown as needed, never cleared
-    template <typename T>
-    struct Pinned
-    {
-        T* p = nullptr;
-        size_t cap = 0;
-        bool reserve(size_t n)
-        {
-            if (n <= cap) return true;
-            size_t want = std::max(n, cap + cap / 2);
-            void* q = nullptr;
-            if (cudaHostAlloc(&q, want * sizeof(T), cudaHostAllocDefault) != cudaSuccess) return false;
-            if (p) cudaFreeHost(p);
-            p = (T*)q;
-            cap = want;
-            return true;
-        }
-        void release() { if (p) cudaFreeHost(p); p = nullptr; cap = 0; }
-        T* data() { return p; }
-        T& operator[](size_t i) { return p[i]; }
-    };
-    Pinned<uint8_t> blob;
-    Pinned<uint64_t> off, toff, items, steps;
-    Pinned<uint32_t> len, node, nodeOff, cap, tlen;
-    Pinned<int32_t> status, score;
-    double stagingMs = 0;      // host time packing requests and handing results over
-    ~ga_aligner()
-    {
-        blob.release(); off.release(); toff.release(); items.release(); steps.release();
-        len.release(); node.release(); nodeOff.release(); cap.release(); tlen.release();
-        status.release(); score.release();
-    }
+    ExtendLane lanes[2];       // lanes[0] uses ext; lanes[1] an extender made like it on first use
 };
 
 // MinimizerSeeder::getSeeds for a batch of reads: k-mer lookups on the GPU, the
@@ -61,8 +74,11 @@ struct ga_aligner
 int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const uint8_t* seq, const uint64_t* seqOffset,
     const uint32_t* seqLen, std::vector<gahost::ReadInput>& reads);
 
-// gahost::ExtendFn over ga_extend_batch (ctx = ga_aligner*)
+// gahost::ExtendFn over ga_extend_batch (ctx = ExtendLane*)
 void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs);
+
+// the second lane's extender (same device graph, arena size and launch shape as the first)
+int ga_aligner_second_lane(ga_aligner* a);
 
 // the seed loop parameters of ga_align_params
 gahost::ReadAlignParams ga_aligner_read_params(const ga_aligner* a);

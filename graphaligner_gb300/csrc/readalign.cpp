@@ -1090,4 +1090,62 @@ void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadIn
     for (auto& d : done) out[d.first] = std::move(d.second);
 }
 
+void alignBatchTwoLanes(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend,
+    void* ctxA, void* ctxB, std::vector<ReadOutput>& out, BatchStats& stats)
+{
+    out.assign(reads.size(), ReadOutput {});
+    // alternate reads between the groups after sorting by length, so both carry similar work
+    std::vector<size_t> byLen(reads.size());
+    for (size_t i = 0; i < reads.size(); i++) byLen[i] = i;
+    std::stable_sort(byLen.begin(), byLen.end(), [&](size_t a, size_t b) { return reads[a].seq.size() > reads[b].seq.size(); });
+    std::vector<ReadInput> part[2];
+    std::vector<uint64_t> tags[2];
+    for (size_t k = 0; k < byLen.size(); k++)
+    {
+        part[k & 1].push_back(std::move(reads[byLen[k]]));
+        tags[k & 1].push_back(byLen[k]);
+    }
+    SeedLoopPool pool0(g, p), pool1(g, p);
+    SeedLoopPool* pool[2] = { &pool0, &pool1 };
+    void* ctx[2] = { ctxA, ctxB };
+    pool0.addMany(part[0], tags[0]);
+    pool1.addMany(part[1], tags[1]);
+    std::vector<ExtensionRequest> rq[2];
+    std::vector<ExtensionResult> rs[2];
+    std::vector<std::pair<uint64_t, ReadOutput>> done;
+    bool active[2];
+    std::thread worker[2];
+    auto launch = [&](int k)
+    {
+        rs[k].assign(rq[k].size(), ExtensionResult {});
+        if (!rq[k].empty()) worker[k] = std::thread([&, k]() { extend(ctx[k], rq[k], rs[k]); });
+    };
+    auto finish = [&](int k)
+    {
+        if (worker[k].joinable()) worker[k].join();
+        pool[k]->consume(rs[k], stats);
+        pool[k]->takeFinished(done, stats);
+        active[k] = pool[k]->collect(rq[k]);
+        pool[k]->takeFinished(done, stats);
+    };
+    active[0] = pool0.collect(rq[0]);
+    pool0.takeFinished(done, stats);
+    if (active[0]) launch(0);
+    active[1] = pool1.collect(rq[1]);
+    pool1.takeFinished(done, stats);
+    while (active[0] || active[1])
+    {
+        // group 1 goes to the GPU while the host finishes group 0, and the other way round
+        if (active[1]) launch(1);
+        if (active[0])
+        {
+            finish(0);
+            if (active[0]) launch(0);
+        }
+        if (active[1]) finish(1);
+    }
+    for (auto& t : worker) if (t.joinable()) t.join();
+    for (auto& d : done) out[d.first] = std::move(d.second);
+}
+
 }

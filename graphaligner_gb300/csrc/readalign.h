@@ -174,6 +174,11 @@ private:
 
 void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,
     std::vector<ReadOutput>& out, BatchStats& stats);
+// The same with the reads in two groups, each with its own extension context: while one
+// group's round runs (on a worker thread), the caller's thread finishes the other group's
+// last round and collects its next requests.  Results are those of alignBatch.
+void alignBatchTwoLanes(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend,
+    void* ctxA, void* ctxB, std::vector<ReadOutput>& out, BatchStats& stats);
 
 // MinimizerSeeder with one bucket (MinimizerSeeder.h:14-47)
 struct MinimizerIndex

@@ -135,7 +135,7 @@ static void serve_loop(ga_server* s)
         if (pool.collect(rq))
         {
             rs.assign(rq.size(), gahost::ExtensionResult {});
-            if (!rq.empty()) ga_aligner_extend(a, rq, rs);
+            if (!rq.empty()) ga_aligner_extend(&a->lanes[0], rq, rs);
             pool.consume(rs, bs);
             std::lock_guard<std::mutex> lk(s->mu);
             s->stats.rounds++;

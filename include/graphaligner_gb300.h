@@ -109,6 +109,9 @@ int ga_graph_free(ga_graph_t graph);
 typedef struct ga_extender* ga_extender_t;
 /* arena_bytes: device bytes for per-extension DP tables; 0 picks a default. */
 int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out);
+/* A second extender on the same device graph with the same arena size and launch shape
+ * (no reference counterpart): two extenders let two batches run while the host works. */
+int ga_extender_create_like(ga_extender_t ext, ga_extender_t* out);
 int ga_extender_free(ga_extender_t ext);
 /* Host buffers in, host buffers out: copies, launches and waits. */
 int ga_extend_batch(ga_extender_t ext, const ga_extend_params* params,

@@ -149,10 +149,12 @@ int main(int argc, char** argv)
         }
         return 0;
     }
-    // gaf (-x vg, AlignerMain.cpp:170-177), gafdbg (-x dbg, AlignerMain.cpp:160-168) or gafmix
-    // (-x vg with reads joining the seed-loop pool a few per round), with the given bandwidth
+    // gaf (-x vg, AlignerMain.cpp:170-177), gafdbg (-x dbg, AlignerMain.cpp:160-168), gafmix
+    // (-x vg with reads joining the seed-loop pool a few per round) or gaf2 (-x vg, reads in two
+    // groups whose rounds alternate), with the given bandwidth
     const bool dbg = mode == "gafdbg";
     const bool mixed = mode == "gafmix";
+    const bool twoLanes = mode == "gaf2";
     const size_t joinPerRound = 7;
     size_t bw = std::stoul(argv[4]);
     uint64_t maxCells = (argc > 5 && std::string(argv[5]) != "-") ? std::stoull(argv[5]) : (dbg ? 10000 : UINT64_MAX);
@@ -198,6 +200,11 @@ int main(int argc, char** argv)
             fin.clear();
             if (!any && next == in.size() && pool.active() == 0) break;
         }
+    }
+    else if (twoLanes)
+    {
+        Ctx ctx2 = ctx;
+        gahost::alignBatchTwoLanes(graph, p, in, oracleExtend, &ctx, &ctx2, out, st);
     }
     else gahost::alignBatch(graph, p, in, oracleExtend, &ctx, out, st);
     for (auto& o : out) std::cout << o.gaf;

@@ -49,3 +49,22 @@ def test_gpu_quickstart(cuda_lib, tmp_path):
     x = Extender(DeviceGraph(g))
     a = Aligner(x, g, preset("vg"))
     assert a.align([lines[0][1:]], [lines[1].encode()]) == open(os.path.join(GOLDEN, "test_graph.gaf")).read()
+
+
+def test_gpu_two_lanes_gaf_matches_reference(cuda_lib):
+    """400 reads take the two-extender path (two groups whose rounds alternate between the GPU
+    and the host): the golden reads and renamed copies of them, each read's GAF the reference's."""
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    g = load_graph("vg50k")
+    names, seqs = load_reads("vg50k")
+    want = {}
+    for line in load_gaf("vg50k", 10).splitlines(keepends=True):
+        want.setdefault(line.split("\t", 1)[0], []).append(line)
+    copies = [n + "_copy" for n in names]
+    a = Aligner(Extender(DeviceGraph(g)), g, preset("vg"))
+    gaf = a.align(names + copies, seqs + seqs)
+    expected = "".join("".join(want.get(n, [])) for n in names)
+    expected += "".join("".join(l.replace(n + "\t", n + "_copy\t", 1) for l in want.get(n, [])) for n in names)
+    assert gaf == expected
+    assert a.stats()["failed_reads"] == 0

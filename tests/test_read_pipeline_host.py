@@ -56,6 +56,14 @@ def test_gaf_same_when_reads_join_between_rounds(harness, oracle_lib):
     assert out == load_gaf("vg50k", 10)
 
 
+def test_gaf_same_with_two_alternating_groups(harness, oracle_lib):
+    """The two-lane driver (reads in two groups, one group's round on the worker while the
+    other is finished) gives the reference's GAF."""
+    exe, gag, reads, _ = harness
+    out = subprocess.run([exe, gag, reads, "gaf2", "10"], check=True, capture_output=True, text=True).stdout
+    assert out == load_gaf("vg50k", 10)
+
+
 def test_gaf_matches_reference_dbg(harness, oracle_lib, tmp_path):
     """-x dbg on a k=63 de Bruijn graph with cyclic components."""
     exe = harness[0]
