@@ -198,7 +198,7 @@ def run_reference(args, rank, world):
             "config": {"workload": WORKLOAD},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference's C++ source needs /root/reference to compile; on this box the oracle restatement (bit-exact with it on the golden vectors) is timed"}
+            "note": "the reference's own C++ source is not present where this runs; the oracle restatement (bit-exact with it on the golden vectors) is timed"}
     print(json.dumps(line), flush=True)
 
 
