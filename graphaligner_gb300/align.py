@@ -66,7 +66,8 @@ class AlignParams(ctypes.Structure):
 class AlignStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("reads", "reads_with_seeds", "reads_aligned", "failed_reads", "bp_aligned",
                                                 "rounds", "extensions", "cell_steps")] + \
-               [(n, ctypes.c_double) for n in ("seed_ms", "extend_ms", "host_ms", "collect_ms", "staging_ms", "consume_ms", "finish_ms")]
+               [(n, ctypes.c_double) for n in ("seed_ms", "extend_ms", "host_ms", "collect_ms", "staging_ms", "consume_ms", "finish_ms")] + \
+              [(n, ctypes.c_uint64) for n in ("speculative_used", "speculative_discarded")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -263,6 +263,8 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     a->stats.staging_ms = a->lanes[0].stagingMs + a->lanes[1].stagingMs;
     a->stats.consume_ms = bs.consumeMs;
     a->stats.finish_ms = bs.finishMs;
+    a->stats.speculative_used = bs.speculativeUsed;
+    a->stats.speculative_discarded = bs.speculativeDiscarded;
     a->stats.failed_reads = bs.failedReads;
     a->stats.bp_aligned = bs.bpAligned;
     a->stats.rounds = bs.rounds;

@@ -565,15 +565,23 @@ struct ReadState
 
 // advances a read's seed loop (GraphAligner.h:105-154) to the next seed that needs an
 // extension; returns false when the loop ends
-static bool nextSeed(const ReadAlignParams& p, ReadState& r, size_t& seedIndex)
+// the loop's cursor: the next seed to look at and the two counters that extending changes
+struct SeedCursor
 {
-    while (r.next < r.seeds.size())
+    size_t next;
+    size_t worstExtendedSeedScore;
+    size_t seedsExtended;
+};
+
+static bool nextSeedOn(const ReadAlignParams& p, const ReadState& r, SeedCursor& c, size_t& seedIndex)
+{
+    while (c.next < r.seeds.size())
     {
-        const size_t i = r.next;
+        const size_t i = c.next;
         const SeedHit& s = r.seeds[i];
         if (p.sloppy && (s.seedGoodness == r.seedScoreForEndToEndAln || s.seedGoodness < r.seedScoreForEndToEndAln)) return false;
-        if (r.seedsExtended >= r.extendSeeds && s.seedGoodness < r.worstExtendedSeedScore) return false;
-        r.next++;
+        if (c.seedsExtended >= r.extendSeeds && s.seedGoodness < c.worstExtendedSeedScore) return false;
+        c.next++;
         if (s.seedClusterSize < p.minClusterSize) continue;
         if (p.sloppy)
         {
@@ -598,12 +606,22 @@ static bool nextSeed(const ReadAlignParams& p, ReadState& r, size_t& seedIndex)
             }
         }
         if (found) continue;
-        r.worstExtendedSeedScore = s.seedGoodness;
-        r.seedsExtended += 1;
+        c.worstExtendedSeedScore = s.seedGoodness;
+        c.seedsExtended += 1;
         seedIndex = i;
         return true;
     }
     return false;
+}
+
+static bool nextSeed(const ReadAlignParams& p, ReadState& r, size_t& seedIndex)
+{
+    SeedCursor c { r.next, r.worstExtendedSeedScore, r.seedsExtended };
+    const bool more = nextSeedOn(p, r, c, seedIndex);
+    r.next = c.next;
+    r.worstExtendedSeedScore = c.worstExtendedSeedScore;
+    r.seedsExtended = c.seedsExtended;
+    return more;
 }
 
 static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, const char* seq, size_t seqLen)
@@ -790,6 +808,7 @@ struct SeedLoopPool::Impl
         size_t seed;
         int64_t backward = -1;       // request index or -1
         int64_t forward = -1;
+        bool speculative = false;    // follows the read's previous pending entry
     };
     std::vector<Pending> pending;
     std::vector<ExtensionRequest> requests;
@@ -880,26 +899,75 @@ static double msSince(std::chrono::steady_clock::time_point t)
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
 }
 
+static constexpr int kMaxSpeculation = 8;
+
+// the two extensions of a seed (GraphAligner::getTwoDirectionalTrace, GraphAligner.h:475-506)
+static int seedRequests(const HostGraph& g, const ReadState& r, const SeedHit& s, ExtensionRequest* q, int& backward, int& forward)
+{
+    int n = 0;
+    backward = forward = -1;
+    int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
+    GAH_ASSERT(s.seqPos < r.seq.size());
+    if (s.seqPos > 0)
+    {
+        auto rp = g.reversePosition(forwardNodeId, s.nodeOffset);
+        ExtensionRequest& e = q[n];
+        e.seq = r.rev.data() + r.rev.size() - s.seqPos;
+        e.len = s.seqPos;
+        e.bignode = rp.first;
+        e.offset = rp.second;
+        size_t node = g.unitigNode(e.bignode, e.offset);
+        e.node = (uint32_t)node;
+        e.nodeOffset = (uint32_t)(e.offset - g.nodeOffset[node]);
+        backward = n++;
+    }
+    if (s.seqPos < r.seq.size() - 1)
+    {
+        ExtensionRequest& e = q[n];
+        e.seq = r.seq.data() + s.seqPos + 1;
+        e.len = r.seq.size() - s.seqPos - 1;
+        e.bignode = forwardNodeId;
+        e.offset = s.nodeOffset;
+        size_t node = g.unitigNode(e.bignode, e.offset);
+        e.node = (uint32_t)node;
+        e.nodeOffset = (uint32_t)(e.offset - g.nodeOffset[node]);
+        forward = n++;
+    }
+    return n;
+}
+
 bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
 {
     const auto t0 = std::chrono::steady_clock::now();
     const HostGraph& g = impl->g;
+    const ReadAlignParams& p = impl->p;
     auto& pending = impl->pending;
     pending.clear();
     requests.clear();
-    // every read advances its own seed loop (all cores); the requests are then gathered in
-    // read order, backward extension before forward, as a serial loop would emit them
+    const size_t nLive = impl->live.size();
+    const int spec = (int)std::max<size_t>(1, std::min<size_t>({ p.maxSpeculation, (size_t)kMaxSpeculation,
+        nLive ? p.speculationTarget / nLive : 1 }));
+    // every read advances its own seed loop (all cores): its next seed for real, then up to
+    // spec - 1 further candidates on a copy of its cursor (as if the seeds before them were
+    // extended without changing the alignments); the requests are then gathered in read
+    // order, backward extension before forward, as a serial loop would emit them
+    struct Cand
+    {
+        size_t seed;
+        int backward;
+        int forward;
+        int q0;
+    };
     struct Next
     {
         int state = 0;           // 0 pending, 1 loop ended, 2 failed
-        size_t seed = 0;
-        int count = 0;
-        int backward = -1;       // index into q, or -1
-        int forward = -1;
-        ExtensionRequest q[2];
+        int count = 0;           // candidate seeds
+        int nq = 0;
+        Cand cand[kMaxSpeculation];
+        ExtensionRequest q[2 * kMaxSpeculation];
     };
-    std::vector<Next> next(impl->live.size());
-    parallelFor(impl->live.size(), [&](size_t i)
+    std::vector<Next> next(nLive);
+    parallelFor(nLive, [&](size_t i)
     {
         ReadState& r = *impl->live[i].r;
         Next& nx = next[i];
@@ -907,7 +975,7 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
         bool more = false;
         try
         {
-            more = nextSeed(impl->p, r, seedIndex);
+            more = nextSeed(p, r, seedIndex);
         }
         catch (const ReadFailure&)
         {
@@ -918,46 +986,41 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
             nx.state = 1;
             return;
         }
-        const SeedHit& s = r.seeds[seedIndex];
-        nx.seed = seedIndex;
-        int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
         try
         {
-            GAH_ASSERT(s.seqPos < r.seq.size());
-            if (s.seqPos > 0)
-            {
-                auto rp = g.reversePosition(forwardNodeId, s.nodeOffset);
-                ExtensionRequest& q = nx.q[nx.count];
-                q.seq = r.rev.data() + r.rev.size() - s.seqPos;
-                q.len = s.seqPos;
-                q.bignode = rp.first;
-                q.offset = rp.second;
-                size_t node = g.unitigNode(q.bignode, q.offset);
-                q.node = (uint32_t)node;
-                q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
-                nx.backward = nx.count++;
-            }
-            if (s.seqPos < r.seq.size() - 1)
-            {
-                ExtensionRequest& q = nx.q[nx.count];
-                q.seq = r.seq.data() + s.seqPos + 1;
-                q.len = r.seq.size() - s.seqPos - 1;
-                q.bignode = forwardNodeId;
-                q.offset = s.nodeOffset;
-                size_t node = g.unitigNode(q.bignode, q.offset);
-                q.node = (uint32_t)node;
-                q.nodeOffset = (uint32_t)(q.offset - g.nodeOffset[node]);
-                nx.forward = nx.count++;
-            }
+            Cand& c = nx.cand[0];
+            c.seed = seedIndex;
+            c.q0 = 0;
+            nx.nq += seedRequests(g, r, r.seeds[seedIndex], nx.q, c.backward, c.forward);
+            nx.count = 1;
         }
         catch (const ReadFailure&)
         {
             r.failed = true;
             nx.state = 2;
+            return;
+        }
+        SeedCursor cur { r.next, r.worstExtendedSeedScore, r.seedsExtended };
+        while (nx.count < spec)
+        {
+            size_t si = 0;
+            try
+            {
+                if (!nextSeedOn(p, r, cur, si)) break;
+                Cand& c = nx.cand[nx.count];
+                c.seed = si;
+                c.q0 = nx.nq;
+                nx.nq += seedRequests(g, r, r.seeds[si], nx.q + nx.nq, c.backward, c.forward);
+                nx.count++;
+            }
+            catch (const ReadFailure&)
+            {
+                break;               // the loop may never reach this seed; if it does, it fails then
+            }
         }
     });
     size_t keep = 0;
-    for (size_t i = 0; i < impl->live.size(); i++)
+    for (size_t i = 0; i < nLive; i++)
     {
         Impl::Live& l = impl->live[i];
         Next& nx = next[i];
@@ -967,20 +1030,25 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
             impl->finished.push_back(std::move(l));
             continue;
         }
-        Impl::Pending pe;
-        pe.r = l.r.get();
-        pe.seed = nx.seed;
-        if (nx.backward >= 0)
+        for (int k = 0; k < nx.count; k++)
         {
-            pe.backward = (int64_t)requests.size();
-            requests.push_back(nx.q[nx.backward]);
+            const Cand& c = nx.cand[k];
+            Impl::Pending pe;
+            pe.r = l.r.get();
+            pe.seed = c.seed;
+            pe.speculative = k > 0;
+            if (c.backward >= 0)
+            {
+                pe.backward = (int64_t)requests.size();
+                requests.push_back(nx.q[c.q0 + c.backward]);
+            }
+            if (c.forward >= 0)
+            {
+                pe.forward = (int64_t)requests.size();
+                requests.push_back(nx.q[c.q0 + c.forward]);
+            }
+            pending.push_back(pe);
         }
-        if (nx.forward >= 0)
-        {
-            pe.forward = (int64_t)requests.size();
-            requests.push_back(nx.q[nx.forward]);
-        }
-        pending.push_back(pe);
         if (keep != i) impl->live[keep] = std::move(l);
         keep++;
     }
@@ -1000,13 +1068,17 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
     stats.rounds++;
     stats.extensions += requests.size();
     for (const auto& rs : results) stats.cellSteps += rs.steps;
-    // every pending read touches only its own state: finish the seeds on all cores
+    // every read touches only its own state: finish its seeds on all cores, a read's own
+    // entries in order
     const auto& pending = impl->pending;
     const ReadAlignParams& p = impl->p;
-    parallelFor(pending.size(), [&](size_t i)
+    std::vector<size_t> groupStart;
+    for (size_t i = 0; i < pending.size(); i++)
+        if (!pending[i].speculative) groupStart.push_back(i);
+    groupStart.push_back(pending.size());
+    std::atomic<uint64_t> used(0), discarded(0);
+    auto finish = [&](const Impl::Pending& pe, ReadState& r) -> bool
     {
-        const auto& pe = pending[i];
-        ReadState& r = *pe.r;
         const SeedHit& s = r.seeds[pe.seed];
         int forwardNodeId = s.reverse ? s.nodeID * 2 + 1 : s.nodeID * 2;
         int backwardNodeId = s.reverse ? s.nodeID * 2 : s.nodeID * 2 + 1;
@@ -1022,12 +1094,59 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
             if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], requests[pe.backward].seq, requests[pe.backward].len);
             if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], requests[pe.forward].seq, requests[pe.forward].len);
             finishSeed(g, p, r, s, std::move(bw), std::move(fw), backwardNodeId, forwardNodeId);
+            return true;
         }
         catch (const ReadFailure&)
         {
             r.failed = true;
+            return false;
         }
+    };
+    parallelFor(groupStart.size() - 1, [&](size_t gi)
+    {
+        const size_t first = groupStart[gi], last = groupStart[gi + 1];
+        ReadState& r = *pending[first].r;
+        size_t k = first;
+        if (finish(pending[k++], r))
+        {
+            // speculative entries: replay the seed loop on the read's true state; a result is
+            // used only if the loop extends exactly that seed next
+            for (; k < last; k++)
+            {
+                const Impl::Pending& pe = pending[k];
+                const SeedCursor saved { r.next, r.worstExtendedSeedScore, r.seedsExtended };
+                size_t idx = 0;
+                bool more = false;
+                try
+                {
+                    more = nextSeed(p, r, idx);
+                }
+                catch (const ReadFailure&)
+                {
+                    r.failed = true;
+                    break;
+                }
+                if (!more) break;
+                if (idx != pe.seed)
+                {
+                    // the loop goes elsewhere: leave its cursor where the next round starts
+                    r.next = saved.next;
+                    r.worstExtendedSeedScore = saved.worstExtendedSeedScore;
+                    r.seedsExtended = saved.seedsExtended;
+                    break;
+                }
+                used++;
+                if (!finish(pe, r))
+                {
+                    k++;
+                    break;
+                }
+            }
+        }
+        discarded += last - k;
     });
+    stats.speculativeUsed += used;
+    stats.speculativeDiscarded += discarded;
     impl->pending.clear();
     // a read that failed in this round leaves its loop now
     size_t keep = 0;

@@ -88,6 +88,12 @@ struct ReadAlignParams
     int minAlignmentScore = 0;
     double multimapScoreFraction = 0.9;
     bool cigarMatchMismatchMerge = false;
+    // speculative seeds: while a round would hold fewer than this many reads' worth of
+    // seeds, each read also sends its next candidate seeds (up to maxSpeculation in all);
+    // a speculative result is used only if the seed loop, replayed in order on the read's
+    // true state, extends exactly that seed next
+    size_t speculationTarget = 8192;
+    size_t maxSpeculation = 8;
 };
 
 struct ReadInput
@@ -113,6 +119,8 @@ struct BatchStats
     uint64_t cellSteps = 0;
     uint64_t bpAligned = 0;
     uint64_t failedReads = 0;
+    uint64_t speculativeUsed = 0;       // speculative extensions whose seed the loop then extended
+    uint64_t speculativeDiscarded = 0;  // speculative extensions it did not
     double collectMs = 0;      // next seeds and extension requests
     double consumeMs = 0;      // trace decoding, fix-up and merge of every finished seed
     double finishMs = 0;       // selection and GAF of finished reads

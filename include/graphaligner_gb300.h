@@ -230,6 +230,8 @@ typedef struct ga_align_stats {
     double   staging_ms;               /*           packing requests for the GPU */
     double   consume_ms;               /*           trace decoding, fix-up and merge per seed */
     double   finish_ms;                /*           selection and GAF per read */
+    uint64_t speculative_used;         /* extensions of later seeds sent ahead and then used ... */
+    uint64_t speculative_discarded;    /* ... and sent ahead but not used (the loop went elsewhere) */
 } ga_align_stats;
 
 typedef struct ga_aligner* ga_aligner_t;

@@ -210,6 +210,6 @@ int main(int argc, char** argv)
     for (auto& o : out) std::cout << o.gaf;
     const double alignSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - alignStart).count();
     std::cerr << "rounds " << st.rounds << " extensions " << st.extensions << " bp " << st.bpAligned << " failed " << st.failedReads
-              << " seconds " << alignSeconds << std::endl;
+              << " seconds " << alignSeconds << " speculative_used " << st.speculativeUsed << " discarded " << st.speculativeDiscarded << std::endl;
     return 0;
 }
