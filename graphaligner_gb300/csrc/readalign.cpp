@@ -813,6 +813,7 @@ struct SeedLoopPool::Impl
     std::vector<Pending> pending;
     std::vector<ExtensionRequest> requests;
     double collectMs = 0;
+    double stepsPerBp = 3.0;         // column steps per extended bp, from the last round
     Impl(const HostGraph& g_, const ReadAlignParams& p_) : g(g_), p(p_) {}
 };
 
@@ -945,8 +946,14 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
     pending.clear();
     requests.clear();
     const size_t nLive = impl->live.size();
-    const int spec = (int)std::max<size_t>(1, std::min<size_t>({ p.maxSpeculation, (size_t)kMaxSpeculation,
-        nLive ? p.speculationTarget / nLive : 1 }));
+    // speculation depth from the estimated work of a round: one seed of every read covers
+    // about its length, at the previous round's column steps per extended bp
+    double roundBp = 0;
+    for (const auto& l : impl->live) roundBp += (double)l.r->seq.size();
+    const double work = roundBp * impl->stepsPerBp;
+    int spec = 1;
+    if (work > 0 && work < p.speculationSteps)
+        spec = (int)std::min<double>({ (double)p.maxSpeculation, (double)kMaxSpeculation, 1.0 + (p.speculationSteps - work) / work });
     // every read advances its own seed loop (all cores): its next seed for real, then up to
     // spec - 1 further candidates on a copy of its cursor (as if the seeds before them were
     // extended without changing the alignments); the requests are then gathered in read
@@ -1067,7 +1074,16 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
     impl->collectMs = 0;
     stats.rounds++;
     stats.extensions += requests.size();
-    for (const auto& rs : results) stats.cellSteps += rs.steps;
+    {
+        double steps = 0, bp = 0;
+        for (size_t k = 0; k < results.size(); k++)
+        {
+            stats.cellSteps += results[k].steps;
+            steps += (double)results[k].steps;
+            bp += (double)requests[k].len;
+        }
+        if (bp > 0) impl->stepsPerBp = std::max(1.0, steps / bp);
+    }
     // every read touches only its own state: finish its seeds on all cores, a read's own
     // entries in order
     const auto& pending = impl->pending;

@@ -88,11 +88,12 @@ struct ReadAlignParams
     int minAlignmentScore = 0;
     double multimapScoreFraction = 0.9;
     bool cigarMatchMismatchMerge = false;
-    // speculative seeds: while a round would hold fewer than this many reads' worth of
-    // seeds, each read also sends its next candidate seeds (up to maxSpeculation in all);
-    // a speculative result is used only if the seed loop, replayed in order on the read's
-    // true state, extends exactly that seed next
-    size_t speculationTarget = 8192;
+    // speculative seeds: while a round's estimated work (read bp x the previous round's
+    // column steps per extended bp) stays under speculationSteps, each read also sends its
+    // next candidate seeds (up to maxSpeculation seeds per read, the extra ones together
+    // within the same budget); a speculative result is used only if the seed loop, replayed
+    // in order on the read's true state, extends exactly that seed next
+    double speculationSteps = 6e7;
     size_t maxSpeculation = 8;
 };
 
