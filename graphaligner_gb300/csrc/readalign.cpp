@@ -901,6 +901,7 @@ static double msSince(std::chrono::steady_clock::time_point t)
 }
 
 static constexpr int kMaxSpeculation = 8;
+static constexpr size_t kMinReadsToSpeculate = 16;
 
 // the two extensions of a seed (GraphAligner::getTwoDirectionalTrace, GraphAligner.h:475-506)
 static int seedRequests(const HostGraph& g, const ReadState& r, const SeedHit& s, ExtensionRequest* q, int& backward, int& forward)
@@ -952,7 +953,9 @@ bool SeedLoopPool::collect(std::vector<ExtensionRequest>& requests)
     for (const auto& l : impl->live) roundBp += (double)l.r->seq.size();
     const double work = roundBp * impl->stepsPerBp;
     int spec = 1;
-    if (work > 0 && work < p.speculationSteps)
+    // a round of a few reads waits for its slowest extension either way: more seeds per
+    // read only add extensions that can be slower still
+    if (nLive >= kMinReadsToSpeculate && work > 0 && work < p.speculationSteps)
         spec = (int)std::min<double>({ (double)p.maxSpeculation, (double)kMaxSpeculation, 1.0 + (p.speculationSteps - work) / work });
     // every read advances its own seed loop (all cores): its next seed for real, then up to
     // spec - 1 further candidates on a copy of its cursor (as if the seeds before them were

@@ -76,7 +76,10 @@ static void serve_loop(ga_server* s)
 {
     ga_aligner* a = s->a;
     cudaSetDevice(a->device);
-    gahost::SeedLoopPool pool(*a->graph, ga_aligner_read_params(a));
+    // latency is the point here: one seed per read and round, no speculative seeds
+    gahost::ReadAlignParams rp = ga_aligner_read_params(a);
+    rp.maxSpeculation = 1;
+    gahost::SeedLoopPool pool(*a->graph, rp);
     gahost::BatchStats bs;
     std::vector<gahost::ExtensionRequest> rq;
     std::vector<gahost::ExtensionResult> rs;
