@@ -96,3 +96,25 @@ def test_build_from_gfa_variation_graph_matches_reference_graph():
     mine = _structure(gg.build_from_gfa(dg.small_vg(0).to_gfa()))
     ref = _structure(load_graph("vg50k"))
     assert mine == ref
+
+
+def test_build_from_gfa_iupac_matches_reference_graph():
+    """Ambiguous (IUPAC) nodes: renumbered to the end, stored as 4-mask sequences; pieces,
+    edges and components equal the reference's build of the same GFA."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g_src, _ = mg.iupac_edge_set(5)
+    mine = gg.build_from_gfa(g_src.to_gfa())
+    ref = load_graph("iupac20k")
+    assert _structure(mine) == _structure(ref)
+    assert mine.num_nodes - mine.first_ambiguous == ref.num_nodes - ref.first_ambiguous > 0
+    # the same sequence masks for every ambiguous piece
+    def amb(g):
+        out = {}
+        for k in range(g.num_nodes - g.first_ambiguous):
+            i = g.first_ambiguous + k
+            out[(int(g.node_ids[i]), int(g.node_offset[i]))] = tuple(int(x) for x in g.seq_ambiguous[4 * k:4 * k + 4])
+        return out
+    assert amb(mine) == amb(ref)
