@@ -40,10 +40,11 @@ struct DevBuf
     cudaError_t reserve(size_t n)
     {
         if (n <= count) return cudaSuccess;
+        // 1.5x headroom: growing frees the old buffer, and cudaFree synchronises the device
+        const size_t grow = std::max(n, count * 3 / 2);
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
         count = 0;
-        size_t grow = std::max(n, count * 3 / 2);
         cudaError_t e = cudaMalloc((void**)&ptr, std::max<size_t>(grow, 1) * sizeof(T));
         if (e == cudaSuccess) count = grow;
         return e;

@@ -109,25 +109,16 @@ int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const u
         matchOff[i] = matchSlots;
         matchSlots += seqLen[i];
     }
-    uint8_t* dSeq = nullptr;
-    uint64_t *dOff = nullptr, *dMatchOff = nullptr;
-    uint32_t *dLen = nullptr, *dCount = nullptr;
-    gadev::SeedMatch* dMatch = nullptr;
-    auto release = [&]()
+    if (!a->dSeq.reserve(std::max<uint64_t>(seqBytes, 1)) || !a->dOff.reserve(n) || !a->dMatchOff.reserve(n)
+        || !a->dLen.reserve(n) || !a->dCount.reserve(n) || !a->dMatch.reserve(std::max<uint64_t>(matchSlots, 1)))
     {
-        cudaFree(dSeq); cudaFree(dOff); cudaFree(dMatchOff); cudaFree(dLen); cudaFree(dCount); cudaFree(dMatch);
-    };
-    if (cudaMalloc((void**)&dSeq, std::max<uint64_t>(seqBytes, 1)) != cudaSuccess
-        || cudaMalloc((void**)&dOff, n * 8ULL) != cudaSuccess
-        || cudaMalloc((void**)&dMatchOff, n * 8ULL) != cudaSuccess
-        || cudaMalloc((void**)&dLen, n * 4ULL) != cudaSuccess
-        || cudaMalloc((void**)&dCount, n * 4ULL) != cudaSuccess
-        || cudaMalloc((void**)&dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch)) != cudaSuccess)
-    {
-        release();
         ga_set_last_error("seeding: device buffers for seeding");
         return GA_ERR_CUDA;
     }
+    uint8_t* dSeq = a->dSeq.p;
+    uint64_t *dOff = a->dOff.p, *dMatchOff = a->dMatchOff.p;
+    uint32_t *dLen = a->dLen.p, *dCount = a->dCount.p;
+    gadev::SeedMatch* dMatch = a->dMatch.p;
     cudaMemcpyAsync(dSeq, seq, seqBytes, cudaMemcpyHostToDevice, a->stream);
     cudaMemcpyAsync(dOff, seqOffset, n * 8ULL, cudaMemcpyHostToDevice, a->stream);
     cudaMemcpyAsync(dMatchOff, matchOff.data(), n * 8ULL, cudaMemcpyHostToDevice, a->stream);
@@ -139,7 +130,6 @@ int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const u
     cudaMemcpyAsync(counts.data(), dCount, n * 4ULL, cudaMemcpyDeviceToHost, a->stream);
     cudaMemcpyAsync(matches.data(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
     cudaError_t e = cudaStreamSynchronize(a->stream);
-    release();
     if (e != cudaSuccess)
     {
         ga_set_last_error("seeding: seed lookup kernel failed");

@@ -30,6 +30,27 @@ struct Pinned
     T& operator[](size_t i) { return p[i]; }
 };
 
+// device buffers that only grow (cudaFree synchronises the device, so a steady state
+// must not allocate: a serving loop seeds new reads while other lanes' rounds run)
+template <typename T>
+struct DevGrow
+{
+    T* p = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t n)
+    {
+        if (n <= cap) return true;
+        size_t want = std::max(n, cap + cap / 2);
+        void* q = nullptr;
+        if (cudaMalloc(&q, want * sizeof(T)) != cudaSuccess) return false;
+        if (p) cudaFree(p);
+        p = (T*)q;
+        cap = want;
+        return true;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+};
+
 // One extender and the staging of its batches: ga_aligner_extend's context.  Two lanes
 // let one group of reads extend on the GPU while the host finishes the other group.
 struct ExtendLane
@@ -67,6 +88,15 @@ struct ga_aligner
     ga_align_stats stats {};
     cudaStream_t stream = nullptr;
     ExtendLane lanes[2];       // lanes[0] uses ext; lanes[1] an extender made like it on first use
+    // k-mer lookup buffers
+    DevGrow<uint8_t> dSeq;
+    DevGrow<uint64_t> dOff, dMatchOff;
+    DevGrow<uint32_t> dLen, dCount;
+    DevGrow<gadev::SeedMatch> dMatch;
+    ~ga_aligner()
+    {
+        dSeq.release(); dOff.release(); dMatchOff.release(); dLen.release(); dCount.release(); dMatch.release();
+    }
 };
 
 // MinimizerSeeder::getSeeds for a batch of reads: k-mer lookups on the GPU, the

@@ -21,6 +21,8 @@ class ServerParams(ctypes.Structure):
         ("max_reads_in_flight", ctypes.c_uint32),
         ("max_band_bytes", ctypes.c_uint64),
         ("band_bytes_per_bp", ctypes.c_uint32),
+        ("lanes", ctypes.c_uint32),
+        ("long_read_bp", ctypes.c_uint32),
     ]
 
 
@@ -64,9 +66,10 @@ class ServedRead:
 class Server:
     """``Server(aligner).submit(name, seq) -> ticket``; ``poll()`` returns finished reads."""
 
-    def __init__(self, aligner, max_reads_in_flight: int = 0, max_band_bytes: int = 0, band_bytes_per_bp: int = 0):
+    def __init__(self, aligner, max_reads_in_flight: int = 0, max_band_bytes: int = 0, band_bytes_per_bp: int = 0,
+                 lanes: int = 0, long_read_bp: int = 0):
         self.aligner = aligner
-        self.params = ServerParams(max_reads_in_flight, max_band_bytes, band_bytes_per_bp)
+        self.params = ServerParams(max_reads_in_flight, max_band_bytes, band_bytes_per_bp, lanes, long_read_bp)
         h = ctypes.c_void_p()
         check(lib().ga_server_create(aligner.handle, ctypes.byref(self.params), ctypes.byref(h)))
         self.handle = h

@@ -252,14 +252,16 @@ int ga_aligner_stats(ga_aligner_t aligner, ga_align_stats* out);
  * loop iteration there) as continuous batching: reads are submitted one at a time
  * from any thread; a worker thread admits them while the reads in flight and their
  * estimated band memory stay under the limits, seeds each admitted group on the GPU,
- * and runs one extension batch per round over every read in flight, so reads that
- * arrive while others are on the GPU join the next round and share its launch.  A
- * read's GAF bytes do not depend on which other reads share its rounds.
+ * and runs rounds of extensions on concurrent lanes (long reads on their own lane), so
+ * reads that arrive while others are on the GPU join their lane's next round and share
+ * its launch.  A read's GAF bytes do not depend on which other reads share its rounds.
  * The graph, the DP arrays and the minimizer table stay resident on the device. */
 typedef struct ga_server_params {
     uint32_t max_reads_in_flight;     /* reads in their seed loops at once; 0 = 4096 */
     uint64_t max_band_bytes;          /* admission budget of estimated band + trace memory; 0 = 2 GiB */
     uint32_t band_bytes_per_bp;       /* the estimate per read bp; 0 = 32 */
+    uint32_t lanes;                   /* concurrent rounds, each with its own extender; 0 = 2 */
+    uint32_t long_read_bp;            /* with 2+ lanes, reads this long are served on lane 0 only; 0 = 15000 */
 } ga_server_params;
 
 typedef struct ga_server_result {
