@@ -159,8 +159,11 @@ void buildMinimizerIndex(const HostGraph& g, size_t k, size_t w, double keepLeas
         }
         if (skipStart) m = std::max(m, (size_t)g.nodeOffset[i]);
     }
-    std::vector<uint64_t> kmers, positions;
-    for (size_t li = 0; li < g.lookupIds.size(); li++)
+    // minimizers of every bigraph node in nodeLookup order: nodes are scanned on all cores
+    // into per-node lists, which are then concatenated in that order (the serial order)
+    const size_t numLookup = g.lookupIds.size();
+    std::vector<std::vector<std::pair<uint64_t, uint64_t>>> perNode(numLookup);
+    parallelFor(numLookup, [&](size_t li)
     {
         int nodeId = g.lookupIds[li];
         std::string sequence(g.originalSize[li], 'N');
@@ -170,26 +173,48 @@ void buildMinimizerIndex(const HostGraph& g, size_t k, size_t w, double keepLeas
             sequence[pos] = g.charAt(here, pos - g.nodeOffset[here]);
         }
         const size_t minStart = nodeMinimizerStart.at((size_t)(int64_t)nodeId);
+        auto& out = perNode[li];
         iterateMinimizers(sequence, k, w, [&](size_t pos, uint64_t kmer)
         {
             if (pos < minStart) return;
             size_t splitNode = g.unitigNode(nodeId, pos);
             size_t remaining = pos - g.nodeOffset[splitNode];
-            kmers.push_back(kmer);
-            positions.push_back(((uint64_t)splitNode << 6) + remaining);
+            out.emplace_back(kmer, ((uint64_t)splitNode << 6) + remaining);
         });
+    });
+    size_t total = 0;
+    for (const auto& v : perNode) total += v.size();
+    std::vector<uint64_t> kmers, positions;
+    kmers.reserve(total);
+    positions.reserve(total);
+    for (auto& v : perNode)
+    {
+        for (const auto& kp : v)
+        {
+            kmers.push_back(kp.first);
+            positions.push_back(kp.second);
+        }
+        std::vector<std::pair<uint64_t, uint64_t>>().swap(v);
     }
     idx.keys = kmers;
     std::sort(idx.keys.begin(), idx.keys.end());
     idx.keys.erase(std::unique(idx.keys.begin(), idx.keys.end()), idx.keys.end());
     auto rank = [&](uint64_t kmer) -> size_t { return std::lower_bound(idx.keys.begin(), idx.keys.end(), kmer) - idx.keys.begin(); };
+    // the rank of every k-mer occurrence (binary searches on all cores), then the serial
+    // counting sort that fixes the positions' order within a k-mer
+    std::vector<uint32_t> ranks(kmers.size());
+    parallelFor((kmers.size() + 4095) / 4096, [&](size_t c)
+    {
+        const size_t end = std::min(kmers.size(), (c + 1) * 4096);
+        for (size_t i = c * 4096; i < end; i++) ranks[i] = (uint32_t)rank(kmers[i]);
+    });
     idx.startPos.assign(idx.keys.size() + 1, 0);
-    for (uint64_t kmer : kmers) idx.startPos[rank(kmer)] += 1;
+    for (uint32_t r : ranks) idx.startPos[r] += 1;
     for (size_t i = 1; i < idx.startPos.size(); i++) idx.startPos[i] += idx.startPos[i - 1];
     idx.positions.assign(kmers.size(), 0);
     for (size_t i = 0; i < kmers.size(); i++)
     {
-        size_t r = rank(kmers[i]);
+        const size_t r = ranks[i];
         idx.startPos[r] -= 1;
         idx.positions[idx.startPos[r]] = positions[i];
     }
