@@ -79,6 +79,11 @@ struct ga_extender
     ga_graph* graph = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] {};
+    // the trace items of a host-buffer batch go back in chunks on these streams, so that
+    // several copy engines share the (largest) device-to-host copy
+    static constexpr int kCopyStreams = 4;
+    cudaStream_t copy[kCopyStreams] {};
+    cudaEvent_t copyDone[kCopyStreams] {};
     int sms = 0;
     ga_launch_shape shape {};             // how the longest-first order is cut into warp chunks
     int block = 128;
@@ -230,6 +235,11 @@ extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_ext
     uint64_t stride = ga_workspace_bytes(x->caps);
     x->workspaceBytes = slots * stride;
     GA_CUDA(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking));
+    for (int k = 0; k < ga_extender::kCopyStreams; k++)
+    {
+        GA_CUDA(cudaStreamCreateWithFlags(&x->copy[k], cudaStreamNonBlocking));
+        GA_CUDA(cudaEventCreateWithFlags(&x->copyDone[k], cudaEventDisableTiming));
+    }
     for (auto& e : x->ev) GA_CUDA(cudaEventCreate(&e));
     cudaError_t e = cudaMalloc((void**)&x->workspace, x->workspaceBytes);
     if (e != cudaSuccess) { delete x; return cuda_fail(e, "workspace"); }
@@ -266,6 +276,11 @@ extern "C" int ga_extender_free(ga_extender_t x)
     x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release(); x->chunks.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
+    for (int k = 0; k < ga_extender::kCopyStreams; k++)
+    {
+        if (x->copy[k]) cudaStreamDestroy(x->copy[k]);
+        if (x->copyDone[k]) cudaEventDestroy(x->copyDone[k]);
+    }
     delete x;
     return GA_OK;
 }
@@ -454,7 +469,18 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
     GA_CUDA(cudaMemcpyAsync(r->score, dr.score, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->trace_len, dr.trace_len, n * 4ULL, cudaMemcpyDeviceToHost, s));
     if (r->cell_steps) GA_CUDA(cudaMemcpyAsync(r->cell_steps, dr.cell_steps, n * 8ULL, cudaMemcpyDeviceToHost, s));
-    GA_CUDA(cudaMemcpyAsync(r->trace_items, dr.trace_items, items * 8ULL, cudaMemcpyDeviceToHost, s));
+    // trace items: chunks on the copy streams, each after the kernels
+    GA_CUDA(cudaEventRecord(x->ev[2], s));
+    const uint64_t chunk = (items + ga_extender::kCopyStreams - 1) / ga_extender::kCopyStreams;
+    for (int k = 0; k < ga_extender::kCopyStreams; k++)
+    {
+        const uint64_t from = std::min<uint64_t>(items, (uint64_t)k * chunk);
+        const uint64_t to = std::min<uint64_t>(items, from + chunk);
+        GA_CUDA(cudaStreamWaitEvent(x->copy[k], x->ev[2], 0));
+        if (to > from) GA_CUDA(cudaMemcpyAsync(r->trace_items + from, dr.trace_items + from, (to - from) * 8ULL, cudaMemcpyDeviceToHost, x->copy[k]));
+        GA_CUDA(cudaEventRecord(x->copyDone[k], x->copy[k]));
+        GA_CUDA(cudaStreamWaitEvent(s, x->copyDone[k], 0));
+    }
     GA_CUDA(cudaStreamSynchronize(s));
     return GA_OK;
 }
