@@ -419,13 +419,6 @@ def main():
     gen_s = time.perf_counter() - t0
     params = ExtendParams(bandwidth=10)
 
-    # ---- CPU baseline first (before any GPU state exists in worker processes) ----
-    cpu = None
-    cpu_res = None
-    cpu_idx = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu, cpu_res, cpu_idx = cpu_baseline(g, batch, params, args.cpu_sample_bp, os.cpu_count() or 1)
-
     dgraph = DeviceGraph(g, device=local)
     arena = int(min(64 << 30, max(4 << 30, int(batch.seq_len.astype(np.int64).sum()) * 24)))
     if args.arena_gb:
@@ -505,10 +498,6 @@ def main():
     bp = aligned_bp(res)
     steps_total = int(res.cell_steps.sum())
     statuses = {int(s): int(c) for s, c in zip(*np.unique(res.status, return_counts=True))}
-    # the CPU sample must agree with the GPU on the same extensions
-    cpu_agree = None
-    if cpu_res is not None:
-        cpu_agree = bool(np.array_equal(cpu_res.status, res.status[cpu_idx]) and np.array_equal(cpu_res.score, res.score[cpu_idx]))
 
     job_bp, kernel_s = combine_ranks(bp * args.steps, kernel_s, world, dev)
     value = job_bp / kernel_s
@@ -576,6 +565,14 @@ def main():
                  "sample": f"{len(pidx)} of {n} extensions, evenly spaced, {pbp} aligned bp",
                  "batched_over_plain": value / (pbp / plain_wall), "same_results": same,
                  "form": "ga_extend_batch_device with one extension per call (one fill+traceback launch, waited for), batch resident in HBM"}
+
+    # ---- CPU baseline last (host threads, no process pool: the GPU timings above are not
+    # disturbed by its large host allocations); its sample must agree with the GPU ----
+    cpu = None
+    cpu_agree = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, cpu_res, cpu_idx = cpu_baseline(g, batch, params, args.cpu_sample_bp, os.cpu_count() or 1)
+        cpu_agree = bool(np.array_equal(cpu_res.status, res.status[cpu_idx]) and np.array_equal(cpu_res.score, res.score[cpu_idx]))
 
     # ---- roofline ----
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
