@@ -419,6 +419,34 @@ def main():
     gen_s = time.perf_counter() - t0
     params = ExtendParams(bandwidth=10)
 
+    # pinned host buffers of the end-to-end measurement, allocated before anything else
+    # makes large host allocations (the copies' speed depends on how these pages lie)
+    def pinned(nbytes):
+        p = ctypes.c_void_p()
+        check(L.ga_host_alloc(ctypes.c_uint64(nbytes), ctypes.byref(p)))
+        return p
+    host_bufs = []
+    def pinned_like(a):
+        p = pinned(a.nbytes)
+        host_bufs.append(p)
+        arr = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)), shape=(a.nbytes,)).view(a.dtype)
+        arr[:] = a
+        return arr
+    def pinned_zeros(count, dtype):
+        nbytes = int(count) * np.dtype(dtype).itemsize
+        p = pinned(nbytes)
+        host_bufs.append(p)
+        ctypes.memset(p, 0, nbytes)
+        return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)), shape=(nbytes,)).view(dtype)
+    from graphaligner_gb300.extend import PackedBatch, BatchResult
+    hb = PackedBatch(pinned_like(batch.seq), pinned_like(batch.seq_offset), pinned_like(batch.seq_len),
+                     pinned_like(batch.start_node), pinned_like(batch.start_offset), pinned_like(batch.trace_offset),
+                     pinned_like(batch.trace_capacity))
+    hr = BatchResult(pinned_zeros(batch.num, np.int32), pinned_zeros(batch.num, np.int32), pinned_zeros(batch.num, np.uint32),
+                     pinned_zeros(max(batch.total_items, 1), np.uint64), hb.trace_offset, pinned_zeros(batch.num, np.uint64))
+    h2d = int(hb.seq.nbytes + batch.num * (8 + 4 + 4 + 4 + 8 + 4 + 4))
+    d2h = int(batch.num * (4 + 4 + 4 + 8) + batch.total_items * 8)
+
     dgraph = DeviceGraph(g, device=local)
     arena = int(min(64 << 30, max(4 << 30, int(batch.seq_len.astype(np.int64).sum()) * 24)))
     if args.arena_gb:
@@ -506,25 +534,6 @@ def main():
     gcups = job_steps * 64 / kernel_s / 1e9
 
     # ---- end to end through the host-buffer C ABI, pinned host memory ----
-    def pinned(nbytes):
-        p = ctypes.c_void_p()
-        check(L.ga_host_alloc(ctypes.c_uint64(nbytes), ctypes.byref(p)))
-        return p
-    host_bufs = []
-    def pinned_like(a):
-        p = pinned(a.nbytes)
-        host_bufs.append(p)
-        arr = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)), shape=(a.nbytes,)).view(a.dtype)
-        arr[:] = a
-        return arr
-    from graphaligner_gb300.extend import PackedBatch, BatchResult
-    hb = PackedBatch(pinned_like(batch.seq), pinned_like(batch.seq_offset), pinned_like(batch.seq_len),
-                     pinned_like(batch.start_node), pinned_like(batch.start_offset), pinned_like(batch.trace_offset),
-                     pinned_like(batch.trace_capacity))
-    hr = BatchResult(pinned_like(np.zeros(n, np.int32)), pinned_like(np.zeros(n, np.int32)), pinned_like(np.zeros(n, np.uint32)),
-                     pinned_like(np.zeros(max(batch.total_items, 1), np.uint64)), hb.trace_offset, pinned_like(np.zeros(n, np.uint64)))
-    h2d = int(hb.seq.nbytes + n * (8 + 4 + 4 + 4 + 8 + 4 + 4))
-    d2h = int(n * (4 + 4 + 4 + 8) + batch.total_items * 8)
     ext.run(params, hb, hr)   # warm the staging buffers
     e2e_times = []
     for _ in range(max(1, min(args.steps, 3))):
