@@ -64,6 +64,21 @@ def test_gaf_same_with_two_alternating_groups(harness, oracle_lib):
     assert out == load_gaf("vg50k", 10)
 
 
+def test_reads_without_seeds(harness, oracle_lib, tmp_path):
+    """Reads that give no seed (shorter than k, all N, empty between others) write no GAF line
+    and leave every other read's lines unchanged."""
+    import gzip
+    exe, gag, reads, _ = harness
+    text = gzip.open(os.path.join(GOLDEN, "vg50k_reads.fa.gz"), "rt").read().splitlines()
+    extra = [">tiny", "ACGTACGTAC", ">alln", "N" * 3000, ">one", "A"]
+    mixed = text[:40] + extra + text[40:]
+    path = os.path.join(tmp_path, "mixed.fa")
+    open(path, "w").write("\n".join(mixed) + "\n")
+    out = subprocess.run([exe, gag, path, "gaf", "10"], check=True, capture_output=True, text=True)
+    assert out.stdout == load_gaf("vg50k", 10)
+    assert " failed 0 " in out.stderr
+
+
 def test_gaf_matches_reference_dbg(harness, oracle_lib, tmp_path):
     """-x dbg on a k=63 de Bruijn graph with cyclic components."""
     exe = harness[0]
