@@ -27,3 +27,43 @@ def test_library_exports_every_declared_symbol(cuda_lib):
 def test_version_string(cuda_lib):
     cuda_lib.ga_version.restype = ctypes.c_char_p
     assert b"sm_103a" in cuda_lib.ga_version()
+
+
+GA_OK = 0
+GA_ERR_ARGUMENT = -1
+
+
+def test_null_arguments_are_rejected_before_any_device_call(cuda_lib):
+    """Every entry point answers a missing argument with GA_ERR_ARGUMENT (and frees of NULL
+    with GA_OK) without touching CUDA, so a host-only process can rely on it."""
+    L = cuda_lib
+    n = None
+    calls = {
+        "ga_graph_upload": (n, 0, n),
+        "ga_extender_create": (n, ctypes.c_uint64(0), n),
+        "ga_extender_create_like": (n, n),
+        "ga_extend_batch": (n, n, n, n),
+        "ga_extend_batch_device": (n, n, n, n, n),
+        "ga_extend_batch_noalloc": (n, n, n, n, n),
+        "ga_extender_last_kernel_ms": (n, n),
+        "ga_extender_last_times": (n, n, n),
+        "ga_extender_last_launches": (n, n),
+        "ga_extender_set_launch_shape": (n, n),
+        "ga_extender_get_launch_shape": (n, n),
+        "ga_extender_last_arena_bytes": (n, n),
+        "ga_aligner_create": (n, n, n, n),
+        "ga_align_reads": (n, 0, n, n, n, n),
+        "ga_aligner_gaf": (n, n, n),
+        "ga_aligner_read_bp": (n, n),
+        "ga_aligner_stats": (n, n),
+        "ga_server_create": (n, n, n),
+        "ga_server_submit": (n, n, n, 0, n),
+        "ga_server_poll": (n, n, 0, n, 0),
+        "ga_server_release": (n, ctypes.c_uint64(1)),
+        "ga_server_stats_get": (n, n),
+    }
+    wrong = {name: getattr(L, name)(*args) for name, args in calls.items()}
+    wrong = {k: v for k, v in wrong.items() if v != GA_ERR_ARGUMENT}
+    assert not wrong, f"not GA_ERR_ARGUMENT: {wrong}"
+    for name in ("ga_graph_free", "ga_extender_free", "ga_aligner_free", "ga_server_free"):
+        assert getattr(L, name)(n) == GA_OK, name
