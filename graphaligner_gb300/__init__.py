@@ -2,8 +2,11 @@
 
 The package holds the CUDA kernels of GraphAligner's seed-extension hot path
 (banded Myers bit-vector DP over a genome graph with its component-ordered
-frontier, X-drop and traceback) behind a C ABI (include/graphaligner_gb300.h),
-and the host-side mirror of the reference interface that drives it.
+frontier, X-drop and traceback; minimizer k-mer lookups) and the host code of the
+read-level flow (seed loop, selection, GAF, serving loop) behind a C ABI
+(include/graphaligner_gb300.h), with the Python mirror of the reference interface:
+``extend.Extender`` (getReverseTraceFromSeed, batched), ``align.Aligner`` (the
+per-read flow of the aligner) and ``serve.Server`` (continuous batching).
 """
 from .build import build  # noqa: F401
 
