@@ -102,18 +102,26 @@ typedef struct ga_extend_results {
 
 /* ---- device graph ---- */
 typedef struct ga_graph* ga_graph_t;
+/* Replaces the AlignmentGraph the DP reads (src/AlignmentGraph.h:121-139), as
+ * AlignmentGraph::Finalize leaves it (src/AlignmentGraph.cpp:252-296): copied to
+ * `device` once, read-only afterwards, shared by every extender made on it. */
 int ga_graph_upload(const ga_graph_desc* desc, int device, ga_graph_t* out);
 int ga_graph_free(ga_graph_t graph);
 
 /* ---- batched extension ---- */
 typedef struct ga_extender* ga_extender_t;
-/* arena_bytes: device bytes for per-extension DP tables; 0 picks a default. */
+/* The device side of the per-thread AlignerGraphsizedState
+ * (src/GraphAlignerCommon.h:56-80), for a whole batch: per-thread frontier tables and
+ * the DP-table arena.  arena_bytes: device bytes for per-extension DP tables; 0 = 4 GiB. */
 int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out);
 /* A second extender on the same device graph with the same arena size and launch shape
  * (no reference counterpart): two extenders let two batches run while the host works. */
 int ga_extender_create_like(ga_extender_t ext, ga_extender_t* out);
 int ga_extender_free(ga_extender_t ext);
-/* Host buffers in, host buffers out: copies, launches and waits. */
+/* A batch of GraphAlignerBitvectorBanded::getReverseTraceFromSeed calls
+ * (src/GraphAlignerBitvectorBanded.h:59-76).  Host buffers in, host buffers out:
+ * copies, launches and waits.  Status GA_TRACE_FAILED is OnewayTrace::TraceFailed(),
+ * GA_ASSERT a reference assert (ThreadReadAssertion). */
 int ga_extend_batch(ga_extender_t ext, const ga_extend_params* params,
                     const ga_extend_batch_desc* batch, ga_extend_results* results);
 /* Device-resident variant: every pointer in batch/results is a device pointer.
@@ -145,7 +153,8 @@ int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const ga_extend_p
 /* Kernel time of the last ga_extend_batch* call in milliseconds (CUDA events on
  * the launching stream); valid after the stream has been synchronised. */
 int ga_extender_last_kernel_ms(ga_extender_t ext, float* ms);
-/* Split of the same: fill kernel and traceback kernel milliseconds. */
+/* The same as a pair: fill and traceback run fused in one kernel, so fill_ms is the
+ * kernel time and trace_ms is 0. */
 int ga_extender_last_times(ga_extender_t ext, float* fill_ms, float* trace_ms);
 /* Number of kernel launches made by the last ga_extend_batch* call. */
 int ga_extender_last_launches(ga_extender_t ext, uint32_t* launches);
@@ -168,7 +177,7 @@ int ga_extender_get_launch_shape(ga_extender_t ext, ga_launch_shape* shape);
 /* DP-table bytes the first fill pass of the last call wrote to the arena. */
 int ga_extender_last_arena_bytes(ga_extender_t ext, uint64_t* bytes);
 
-/* ---- utilities ---- */
+/* ---- utilities (no reference counterpart) ---- */
 /* Page-locked host memory for the host-buffer entry points. */
 int ga_host_alloc(uint64_t bytes, void** out);
 int ga_host_free(void* ptr);
