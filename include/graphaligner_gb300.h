@@ -111,7 +111,7 @@ int ga_graph_free(ga_graph_t graph);
 /* ---- batched extension ---- */
 typedef struct ga_extender* ga_extender_t;
 /* The device side of the per-thread AlignerGraphsizedState
- * (src/GraphAlignerCommon.h:56-80), for a whole batch: per-thread frontier tables and
+ * (src/GraphAlignerCommon.h:52-81), for a whole batch: per-thread frontier tables and
  * the DP-table arena.  arena_bytes: device bytes for per-extension DP tables; 0 = 4 GiB. */
 int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out);
 /* A second extender on the same device graph with the same arena size and launch shape
