@@ -535,12 +535,17 @@ def main():
 
     # ---- end to end through the host-buffer C ABI, pinned host memory ----
     ext.run(params, hb, hr)   # warm the staging buffers
-    e2e_times = []
+    e2e_times, e2e_parts = [], []
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t = time.perf_counter()
         ext.run(params, hb, hr)
         e2e_times.append(time.perf_counter() - t)
+        # where the step's time went: copies in, kernels, copies out (CUDA events of the call)
+        h2d_ms, d2h_ms, k_ms = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+        check(L.ga_extender_last_copy_ms(ext.handle, ctypes.byref(h2d_ms), ctypes.byref(d2h_ms)))
+        check(L.ga_extender_last_kernel_ms(ext.handle, ctypes.byref(k_ms)))
+        e2e_parts.append((h2d_ms.value, k_ms.value, d2h_ms.value))
     e2e_same = bool(np.array_equal(hr.status, res.status) and np.array_equal(hr.score, res.score))
     job_bp_e2e, e2e_s = combine_ranks(bp, statistics.median(e2e_times), world, dev)
     e2e_value = job_bp_e2e / e2e_s
@@ -614,7 +619,8 @@ def main():
         "statuses": statuses,
         "kernel_ms": statistics.median(kernel_ms), "wall_s_timed_region": wall,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "seconds_per_step": statistics.median(e2e_times), "same_results": e2e_same},
+                "seconds_per_step": statistics.median(e2e_times), "same_results": e2e_same,
+                "ms_h2d_kernel_d2h": [[round(v, 1) for v in part] for part in e2e_parts]},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak, "traffic": traffic, "kernel": "extend_kernel (fill + traceback, fused)",
                      "algorithmic_bytes": alg_bytes,

@@ -78,7 +78,7 @@ struct ga_extender
 {
     ga_graph* graph = nullptr;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[4] {};
+    cudaEvent_t ev[6] {};                 // kernel start/end, D2H start, H2D start/end, D2H end
     // the trace items of a host-buffer batch go back in chunks on these streams, so that
     // several copy engines share the (largest) device-to-host copy
     static constexpr int kCopyStreams = 4;
@@ -96,11 +96,14 @@ struct ga_extender
     unsigned long long* arenaCursor = nullptr;
     float lastFillMs = 0;
     float lastTraceMs = 0;
+    float lastH2DMs = 0;                    // host-buffer copies of the last ga_extend_batch
+    float lastD2HMs = 0;
     uint64_t lastArenaBytes = 0;
     uint32_t lastDedicated = 0;             // single-lane chunks of the last batch
     uint32_t lastChunks = 0;
     uint32_t lastLaunches = 0;
     std::vector<uint32_t> chunkHost;
+    std::vector<uint32_t> orderHost;      // processing order of the last host batch
     // host-batch staging
     DevBuf<uint8_t> seq;
     DevBuf<uint64_t> seqOff, traceOff, traceItems, cellSteps;
@@ -411,20 +414,21 @@ static std::vector<uint32_t> longest_first(const uint32_t* len, uint32_t n)
     return order;
 }
 
-extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const ga_extend_batch_desc* b, ga_extend_results* r)
+// Copies a host batch into the extender's device buffers and points db/dr at them.
+// sortedLen: the lengths in processing order; items: trace items the batch spans.
+static int stage_host_batch(ga_extender* x, const ga_extend_batch_desc* b, ga_extend_batch_desc* db,
+    ga_extend_results* dr, std::vector<uint32_t>& sortedLen, uint64_t* itemsOut)
 {
-    if (!x || !p || !b || !r) return fail(GA_ERR_ARGUMENT, "null argument");
-    GA_CUDA(cudaSetDevice(x->graph->device));
     const uint32_t n = b->num;
-    if (n == 0) return GA_OK;
     uint64_t seqBytes = 0, items = 0;
     for (uint32_t i = 0; i < n; i++)
     {
         seqBytes = std::max<uint64_t>(seqBytes, b->seq_offset[i] + b->seq_len[i]);
         items = std::max<uint64_t>(items, b->trace_offset[i] + b->trace_capacity[i]);
     }
-    std::vector<uint32_t> order = longest_first(b->seq_len, n);
-    std::vector<uint32_t> sortedLen(n);
+    std::vector<uint32_t>& order = x->orderHost;   // kept until the next batch: the copy below is asynchronous
+    order = longest_first(b->seq_len, n);
+    sortedLen.resize(n);
     for (uint32_t i = 0; i < n; i++) sortedLen[i] = b->seq_len[order[i]];
     GA_CUDA(x->seq.reserve(seqBytes));
     GA_CUDA(x->seqOff.reserve(n));
@@ -441,6 +445,7 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
     GA_CUDA(x->cellSteps.reserve(n));
     GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(items, 1)));
     cudaStream_t s = x->stream;
+    GA_CUDA(cudaEventRecord(x->ev[3], s));
     GA_CUDA(cudaMemcpyAsync(x->seq.ptr, b->seq, seqBytes, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->seqOff.ptr, b->seq_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->seqLen.ptr, b->seq_len, n * 4ULL, cudaMemcpyHostToDevice, s));
@@ -449,21 +454,39 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
     GA_CUDA(cudaMemcpyAsync(x->traceOff.ptr, b->trace_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->traceCap.ptr, b->trace_capacity, n * 4ULL, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
-    ga_extend_batch_desc db = *b;
-    db.seq = x->seq.ptr;
-    db.seq_offset = x->seqOff.ptr;
-    db.seq_len = x->seqLen.ptr;
-    db.start_node = x->startNode.ptr;
-    db.start_offset = x->startOffset.ptr;
-    db.trace_offset = x->traceOff.ptr;
-    db.trace_capacity = x->traceCap.ptr;
+    GA_CUDA(cudaEventRecord(x->ev[4], s));
+    *db = *b;
+    db->seq = x->seq.ptr;
+    db->seq_offset = x->seqOff.ptr;
+    db->seq_len = x->seqLen.ptr;
+    db->start_node = x->startNode.ptr;
+    db->start_offset = x->startOffset.ptr;
+    db->trace_offset = x->traceOff.ptr;
+    db->trace_capacity = x->traceCap.ptr;
+    dr->status = x->status.ptr;
+    dr->score = x->score.ptr;
+    dr->trace_len = x->traceLen.ptr;
+    dr->trace_items = x->traceItems.ptr;
+    dr->cell_steps = x->cellSteps.ptr;
+    *itemsOut = items;
+    return GA_OK;
+}
+
+extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const ga_extend_batch_desc* b, ga_extend_results* r)
+{
+    if (!x || !p || !b || !r) return fail(GA_ERR_ARGUMENT, "null argument");
+    GA_CUDA(cudaSetDevice(x->graph->device));
+    x->lastH2DMs = x->lastD2HMs = 0;
+    const uint32_t n = b->num;
+    if (n == 0) return GA_OK;
+    ga_extend_batch_desc db;
     ga_extend_results dr;
-    dr.status = x->status.ptr;
-    dr.score = x->score.ptr;
-    dr.trace_len = x->traceLen.ptr;
-    dr.trace_items = x->traceItems.ptr;
-    dr.cell_steps = x->cellSteps.ptr;
-    int rc = run_device(x, p, &db, &dr, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
+    std::vector<uint32_t> sortedLen;
+    uint64_t items = 0;
+    int rc = stage_host_batch(x, b, &db, &dr, sortedLen, &items);
+    if (rc != GA_OK) return rc;
+    cudaStream_t s = x->stream;
+    rc = run_device(x, p, &db, &dr, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
     if (rc != GA_OK) return rc;
     GA_CUDA(cudaMemcpyAsync(r->status, dr.status, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->score, dr.score, n * 4ULL, cudaMemcpyDeviceToHost, s));
@@ -481,7 +504,61 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
         GA_CUDA(cudaEventRecord(x->copyDone[k], x->copy[k]));
         GA_CUDA(cudaStreamWaitEvent(s, x->copyDone[k], 0));
     }
+    GA_CUDA(cudaEventRecord(x->ev[5], s));
     GA_CUDA(cudaStreamSynchronize(s));
+    GA_CUDA(cudaEventElapsedTime(&x->lastH2DMs, x->ev[3], x->ev[4]));
+    GA_CUDA(cudaEventElapsedTime(&x->lastD2HMs, x->ev[2], x->ev[5]));
+    return GA_OK;
+}
+
+extern "C" int ga_extender_autotune(ga_extender_t x, const ga_extend_params* p, const ga_extend_batch_desc* b,
+    const ga_launch_shape* shapes, uint32_t count, uint32_t repeats, float* ms_out)
+{
+    if (!x || !p || !b || !shapes) return fail(GA_ERR_ARGUMENT, "null argument");
+    if (count == 0) return fail(GA_ERR_ARGUMENT, "no launch shapes");
+    for (uint32_t i = 0; i < count; i++)
+        if (!shape_ok(shapes[i])) return fail(GA_ERR_ARGUMENT, "launch shape: factors must be positive and lane counts within 1..32");
+    GA_CUDA(cudaSetDevice(x->graph->device));
+    x->lastH2DMs = x->lastD2HMs = 0;
+    const uint32_t n = b->num;
+    if (n == 0) return GA_OK;
+    repeats = std::max<uint32_t>(repeats, 1);
+    ga_extend_batch_desc db;
+    ga_extend_results dr;
+    std::vector<uint32_t> sortedLen;
+    uint64_t items = 0;
+    int rc = stage_host_batch(x, b, &db, &dr, sortedLen, &items);
+    if (rc != GA_OK) return rc;
+    cudaStream_t s = x->stream;
+    std::vector<int32_t> refStatus(n), refScore(n), status(n), score(n);
+    uint32_t best = 0;
+    float bestMs = 0;
+    for (uint32_t i = 0; i < count; i++)
+    {
+        x->shape = shapes[i];
+        std::vector<float> ms;
+        for (uint32_t rep = 0; rep < repeats; rep++)
+        {
+            rc = run_device(x, p, &db, &dr, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
+            if (rc != GA_OK) return rc;
+            ms.push_back(x->lastFillMs);
+        }
+        std::sort(ms.begin(), ms.end());
+        const float median = ms[ms.size() / 2];
+        if (ms_out) ms_out[i] = median;
+        if (i == 0 || median < bestMs) { best = i; bestMs = median; }
+        int32_t* st = i == 0 ? refStatus.data() : status.data();
+        int32_t* sc = i == 0 ? refScore.data() : score.data();
+        GA_CUDA(cudaMemcpyAsync(st, dr.status, n * 4ULL, cudaMemcpyDeviceToHost, s));
+        GA_CUDA(cudaMemcpyAsync(sc, dr.score, n * 4ULL, cudaMemcpyDeviceToHost, s));
+        GA_CUDA(cudaStreamSynchronize(s));
+        if (i > 0 && (status != refStatus || score != refScore))
+        {
+            x->shape = shapes[0];
+            return fail(GA_ERR_STATE, "launch shape " + std::to_string(i) + " changed results");
+        }
+    }
+    x->shape = shapes[best];
     return GA_OK;
 }
 
@@ -490,6 +567,7 @@ extern "C" int ga_extend_batch_device(ga_extender_t x, const ga_extend_params* p
 {
     if (!x || !p || !b || !r) return fail(GA_ERR_ARGUMENT, "null argument");
     GA_CUDA(cudaSetDevice(x->graph->device));
+    x->lastH2DMs = x->lastD2HMs = 0;
     const uint32_t n = b->num;
     if (n == 0) return GA_OK;
     // the processing order needs the lengths; read them back once (4 bytes per extension)
@@ -518,6 +596,14 @@ extern "C" int ga_extender_last_times(ga_extender_t x, float* fill_ms, float* tr
     if (!x || !fill_ms || !trace_ms) return fail(GA_ERR_ARGUMENT, "null argument");
     *fill_ms = x->lastFillMs;
     *trace_ms = x->lastTraceMs;   // the traceback runs inside the same kernel as the fill
+    return GA_OK;
+}
+
+extern "C" int ga_extender_last_copy_ms(ga_extender_t x, float* h2d_ms, float* d2h_ms)
+{
+    if (!x || !h2d_ms || !d2h_ms) return fail(GA_ERR_ARGUMENT, "null argument");
+    *h2d_ms = x->lastH2DMs;
+    *d2h_ms = x->lastD2HMs;
     return GA_OK;
 }
 

@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import ptr
-from ._lib import GAError, check, lib
+from ._lib import check, lib
 
 INT32_MAX = 2**31 - 1
 
@@ -224,30 +224,21 @@ class Extender:
 
     def autotune(self, params: ExtendParams, batch: PackedBatch, candidates=None, sample_every: int = 4, repeats: int = 2) -> dict:
         """Times each launch shape on an evenly spaced sample of the batch (device time of the
-        kernels) and keeps the fastest.  Every candidate must give the same statuses and scores."""
+        kernels, ``ga_extender_autotune``) and keeps the fastest.  The sample stays on the
+        device; every candidate must give the same statuses and scores (GAError otherwise)."""
         idx = np.arange(0, batch.num, max(1, sample_every))
         sub = batch.subset(idx)
-        out = alloc_results(sub)
-        times = []
-        ref = None
-        for c in candidates or DEFAULT_CANDIDATES:
-            self.set_launch_shape(*c)
-            ms = []
-            for _ in range(repeats):
-                self.run(params, sub, out)
-                f = ctypes.c_float()
-                check(lib().ga_extender_last_kernel_ms(self.handle, ctypes.byref(f)))
-                ms.append(f.value)
-            key = (out.status.copy(), out.score.copy())
-            if ref is None:
-                ref = key
-            elif not (np.array_equal(ref[0], key[0]) and np.array_equal(ref[1], key[1])):
-                raise GAError(f"launch shape {c} changed results")
-            times.append((float(np.median(ms)), c))
-        best = min(times)[1]
-        self.set_launch_shape(*best)
+        cands = list(candidates or DEFAULT_CANDIDATES)
+        shapes = (LaunchShape * len(cands))()
+        for i, (sf, sps, mf, ml, bl) in enumerate(cands):
+            shapes[i] = LaunchShape(sf, 2048, sps, mf, ml, bl)
+        ms = (ctypes.c_float * len(cands))()
+        p = params.c()
+        d = sub.desc()
+        check(lib().ga_extender_autotune(self.handle, ctypes.byref(p), ctypes.byref(d), shapes,
+                                         ctypes.c_uint32(len(cands)), ctypes.c_uint32(max(1, repeats)), ms))
         return {"chosen": self.launch_shape().as_dict(), "sample_extensions": int(len(idx)),
-                "candidates_ms": [(round(t, 2), list(c)) for t, c in times]}
+                "candidates_ms": [(round(float(ms[i]), 2), list(c)) for i, c in enumerate(cands)]}
 
     def last_times(self):
         f = ctypes.c_float()

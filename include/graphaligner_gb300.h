@@ -156,6 +156,10 @@ int ga_extender_last_kernel_ms(ga_extender_t ext, float* ms);
 /* The same as a pair: fill and traceback run fused in one kernel, so fill_ms is the
  * kernel time and trace_ms is 0. */
 int ga_extender_last_times(ga_extender_t ext, float* fill_ms, float* trace_ms);
+/* Host-to-device and device-to-host copy times of the last ga_extend_batch call in
+ * milliseconds (CUDA events; the trace items' copy spans the copy streams); 0 after
+ * the device-resident entry points. */
+int ga_extender_last_copy_ms(ga_extender_t ext, float* h2d_ms, float* d2h_ms);
 /* Number of kernel launches made by the last ga_extend_batch* call. */
 int ga_extender_last_launches(ga_extender_t ext, uint32_t* launches);
 
@@ -174,6 +178,15 @@ typedef struct ga_launch_shape {
 } ga_launch_shape;
 int ga_extender_set_launch_shape(ga_extender_t ext, const ga_launch_shape* shape);
 int ga_extender_get_launch_shape(ga_extender_t ext, ga_launch_shape* shape);
+/* Times `count` launch shapes on a host batch and makes the fastest the extender's
+ * shape (no reference counterpart).  The batch is copied to the device once; each
+ * shape runs `repeats` times there (kernel time by CUDA events, the median kept) and
+ * only statuses and scores come back: no trace is copied to the host.  Every shape
+ * must reproduce the first one's statuses and scores, else GA_ERR_STATE and the first
+ * shape is kept.  ms_out (NULL or [count]) receives each shape's median milliseconds. */
+int ga_extender_autotune(ga_extender_t ext, const ga_extend_params* params,
+                         const ga_extend_batch_desc* batch, const ga_launch_shape* shapes,
+                         uint32_t count, uint32_t repeats, float* ms_out);
 /* DP-table bytes the first fill pass of the last call wrote to the arena. */
 int ga_extender_last_arena_bytes(ga_extender_t ext, uint64_t* bytes);
 

@@ -48,8 +48,10 @@ def test_null_arguments_are_rejected_before_any_device_call(cuda_lib):
         "ga_extender_last_kernel_ms": (n, n),
         "ga_extender_last_times": (n, n, n),
         "ga_extender_last_launches": (n, n),
+        "ga_extender_last_copy_ms": (n, n, n),
         "ga_extender_set_launch_shape": (n, n),
         "ga_extender_get_launch_shape": (n, n),
+        "ga_extender_autotune": (n, n, n, n, 0, 0, n),
         "ga_extender_last_arena_bytes": (n, n),
         "ga_aligner_create": (n, n, n, n),
         "ga_align_reads": (n, 0, n, n, n, n),

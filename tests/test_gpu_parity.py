@@ -110,8 +110,16 @@ def test_launch_shapes_do_not_change_results(cuda_lib):
         x.set_launch_shape(2.0, 12, 1.0, 0, 16)
     with pytest.raises(GAError):
         x.set_launch_shape(2.0, 12, 1.0, 16, 33)
-    tuned = x.autotune(ExtendParams(bandwidth=10), batch, sample_every=2, repeats=1)
-    assert tuned["chosen"]["bulk_lanes"] in (7, 8, 16, 32, 1)
+    cands = [(2.0, 12, 1.0, 16, 16), (0.5, 64, 1.0, 1, 1), (100.0, 1, 1.5, 32, 7)]
+    tuned = x.autotune(ExtendParams(bandwidth=10), batch, candidates=cands, sample_every=2, repeats=1)
+    assert len(tuned["candidates_ms"]) == len(cands) and all(ms > 0 for ms, _ in tuned["candidates_ms"])
+    best_ms = min(ms for ms, _ in tuned["candidates_ms"])
+    ch = tuned["chosen"]
+    chosen = (ch["single_factor"], ch["single_per_sm"], ch["mid_factor"], ch["mid_lanes"], ch["bulk_lanes"])
+    assert chosen in [tuple(c) for ms, c in tuned["candidates_ms"] if ms == best_ms]
+    assert not compare(x.run(ExtendParams(bandwidth=10), batch), expected)
+    with pytest.raises(GAError):
+        x.autotune(ExtendParams(bandwidth=10), batch, candidates=[(2.0, 12, 1.0, 16, 40)])
 
 
 @pytest.mark.parametrize("bandwidth", [10, 5])
