@@ -8,11 +8,11 @@
 // (the reference uses a minimal perfect hash there; the id only matters through
 // initMaxCount, MinimizerSeeder.cpp:557-575, which skips the last id).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <deque>
 #include <limits>
 #include <tuple>
-#include <unordered_map>
 #include "readalign.h"
 
 namespace gahost
@@ -138,97 +138,200 @@ start:
     }
 }
 
+// A vector whose resize leaves elements uninitialised, so that large arrays are first
+// touched by the threads that fill them.
+template <typename T>
+struct UninitAllocator : std::allocator<T>
+{
+    template <typename U> struct rebind { using other = UninitAllocator<U>; };
+    UninitAllocator() = default;
+    template <typename U> UninitAllocator(const UninitAllocator<U>&) {}
+    template <typename U> void construct(U* p) noexcept { ::new ((void*)p) U; }
+    template <typename U, typename... A> void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
+};
+template <typename T> using RawVec = std::vector<T, UninitAllocator<T>>;
+
+// Stable LSD radix sort of (key, index) pairs by the low `bits` bits of key, on all
+// cores: each of `parts` contiguous slices histograms a digit, the slices' buckets are
+// laid out digit-major then slice-major, and each slice scatters its elements in order,
+// so equal keys keep their input order.
+static void radixSortPairs(RawVec<uint64_t>& key, RawVec<uint32_t>& val, unsigned bits)
+{
+    const size_t n = key.size();
+    constexpr unsigned kDigit = 11;
+    constexpr size_t kRadix = (size_t)1 << kDigit;
+    const size_t parts = std::max<size_t>(1, std::min<size_t>(256, n / 65536));
+    const size_t per = (n + parts - 1) / parts;
+    RawVec<uint64_t> key2(n);
+    RawVec<uint32_t> val2(n);
+    std::vector<size_t> hist(parts * kRadix);
+    for (unsigned shift = 0; shift < bits; shift += kDigit)
+    {
+        std::fill(hist.begin(), hist.end(), 0);
+        parallelFor(parts, [&](size_t c)
+        {
+            size_t* h = &hist[c * kRadix];
+            const size_t end = std::min(n, (c + 1) * per);
+            for (size_t i = c * per; i < end; i++) h[(key[i] >> shift) & (kRadix - 1)]++;
+        });
+        size_t running = 0;
+        for (size_t d = 0; d < kRadix; d++)
+        {
+            for (size_t c = 0; c < parts; c++)
+            {
+                const size_t count = hist[c * kRadix + d];
+                hist[c * kRadix + d] = running;
+                running += count;
+            }
+        }
+        parallelFor(parts, [&](size_t c)
+        {
+            size_t* h = &hist[c * kRadix];
+            const size_t end = std::min(n, (c + 1) * per);
+            for (size_t i = c * per; i < end; i++)
+            {
+                const size_t to = h[(key[i] >> shift) & (kRadix - 1)]++;
+                key2[to] = key[i];
+                val2[to] = val[i];
+            }
+        });
+        key.swap(key2);
+        val.swap(val2);
+    }
+}
+
 // MinimizerSeeder::initMinimizers + initMaxCount with one bucket (MinimizerSeeder.cpp:299-491, 557-575)
 void buildMinimizerIndex(const HostGraph& g, size_t k, size_t w, double keepLeastFrequentFraction, MinimizerIndex& idx)
 {
     idx.k = k;
     idx.w = w;
-    std::unordered_map<size_t, size_t> nodeMinimizerStart;
-    for (size_t i = 0; i < g.N; i++)
-    {
-        size_t id = (size_t)(int64_t)g.nodeIds[i];
-        size_t& m = nodeMinimizerStart[id];
-        bool skipStart = false;
-        for (uint32_t e = g.inOff[i]; e < g.inOff[i + 1]; e++)
-        {
-            if (g.nodeIds[g.inNb[e]] != g.nodeIds[i])
-            {
-                skipStart = true;
-                break;
-            }
-        }
-        if (skipStart) m = std::max(m, (size_t)g.nodeOffset[i]);
-    }
+    const size_t numLookup = g.lookupIds.size();
     // minimizers of every bigraph node in nodeLookup order: nodes are scanned on all cores
     // into per-node lists, which are then concatenated in that order (the serial order)
-    const size_t numLookup = g.lookupIds.size();
     std::vector<std::vector<std::pair<uint64_t, uint64_t>>> perNode(numLookup);
+    std::atomic<bool> inconsistent(false);   // a piece out of range, or a position no piece covers
     parallelFor(numLookup, [&](size_t li)
     {
-        int nodeId = g.lookupIds[li];
-        std::string sequence(g.originalSize[li], 'N');
-        for (size_t pos = 0; pos < sequence.size(); pos++)
+        const size_t size = g.originalSize[li];
+        // the node's sequence and, per position, its piece: GetUnitigNode's first piece
+        // in nodeLookup order that covers the position (AlignmentGraph.cpp:812-828)
+        std::string sequence(size, 'N');
+        std::vector<uint32_t> pieceOf(size, UINT32_MAX);
+        // minimizers start after the last piece entered from another bigraph node
+        // (MinimizerSeeder.cpp:323-340)
+        size_t minStart = 0;
+        for (uint32_t e = g.lookupOff[li]; e < g.lookupOff[li + 1]; e++)
         {
-            size_t here = g.unitigNode(nodeId, pos);
-            sequence[pos] = g.charAt(here, pos - g.nodeOffset[here]);
+            const uint32_t piece = g.lookupNodes[e];
+            if (piece >= g.N)
+            {
+                inconsistent = true;
+                return;
+            }
+            for (uint32_t p = g.inOff[piece]; p < g.inOff[piece + 1]; p++)
+            {
+                if (g.nodeIds[g.inNb[p]] != g.nodeIds[piece])
+                {
+                    minStart = std::max<size_t>(minStart, g.nodeOffset[piece]);
+                    break;
+                }
+            }
+            const size_t from = g.nodeOffset[piece], to = std::min<size_t>(size, from + g.len[piece]);
+            for (size_t pos = from; pos < to; pos++)
+            {
+                if (pieceOf[pos] != UINT32_MAX) continue;
+                pieceOf[pos] = piece;
+                sequence[pos] = g.charAt(piece, pos - from);
+            }
         }
-        const size_t minStart = nodeMinimizerStart.at((size_t)(int64_t)nodeId);
+        for (size_t pos = 0; pos < size; pos++)
+        {
+            if (pieceOf[pos] == UINT32_MAX)
+            {
+                inconsistent = true;
+                return;
+            }
+        }
         auto& out = perNode[li];
         iterateMinimizers(sequence, k, w, [&](size_t pos, uint64_t kmer)
         {
             if (pos < minStart) return;
-            size_t splitNode = g.unitigNode(nodeId, pos);
-            size_t remaining = pos - g.nodeOffset[splitNode];
+            const size_t splitNode = pieceOf[pos];
+            const size_t remaining = pos - g.nodeOffset[splitNode];
             out.emplace_back(kmer, ((uint64_t)splitNode << 6) + remaining);
         });
     });
-    size_t total = 0;
-    for (const auto& v : perNode) total += v.size();
-    std::vector<uint64_t> kmers, positions;
-    kmers.reserve(total);
-    positions.reserve(total);
-    for (auto& v : perNode)
+    if (inconsistent) throw IndexFailure {};
+    std::vector<size_t> firstOf(numLookup + 1, 0);
+    for (size_t li = 0; li < numLookup; li++) firstOf[li + 1] = firstOf[li] + perNode[li].size();
+    const size_t total = firstOf[numLookup];
+    if (total >= ((size_t)1 << 32)) throw IndexFailure {};
+    RawVec<uint64_t> kmers(total), positions(total);
+    RawVec<uint32_t> order(total);
+    parallelFor(numLookup, [&](size_t li)
     {
-        for (const auto& kp : v)
+        size_t at = firstOf[li];
+        for (const auto& kp : perNode[li])
         {
-            kmers.push_back(kp.first);
-            positions.push_back(kp.second);
+            kmers[at] = kp.first;
+            positions[at] = kp.second;
+            order[at] = (uint32_t)at;
+            at++;
         }
-        std::vector<std::pair<uint64_t, uint64_t>>().swap(v);
-    }
-    idx.keys = kmers;
-    std::sort(idx.keys.begin(), idx.keys.end());
-    idx.keys.erase(std::unique(idx.keys.begin(), idx.keys.end()), idx.keys.end());
-    auto rank = [&](uint64_t kmer) -> size_t { return std::lower_bound(idx.keys.begin(), idx.keys.end(), kmer) - idx.keys.begin(); };
-    // the rank of every k-mer occurrence (binary searches on all cores), then the serial
-    // counting sort that fixes the positions' order within a k-mer
-    std::vector<uint32_t> ranks(kmers.size());
-    parallelFor((kmers.size() + 4095) / 4096, [&](size_t c)
-    {
-        const size_t end = std::min(kmers.size(), (c + 1) * 4096);
-        for (size_t i = c * 4096; i < end; i++) ranks[i] = (uint32_t)rank(kmers[i]);
+        std::vector<std::pair<uint64_t, uint64_t>>().swap(perNode[li]);
     });
-    idx.startPos.assign(idx.keys.size() + 1, 0);
-    for (uint32_t r : ranks) idx.startPos[r] += 1;
-    for (size_t i = 1; i < idx.startPos.size(); i++) idx.startPos[i] += idx.startPos[i - 1];
-    idx.positions.assign(kmers.size(), 0);
-    for (size_t i = 0; i < kmers.size(); i++)
+    // k-mers in increasing order, occurrences of one k-mer in insertion order; a k-mer's id
+    // is its rank among the distinct k-mers
+    radixSortPairs(kmers, order, (unsigned)(2 * k));
+    size_t distinct = 0;
+    for (size_t i = 0; i < total; i++) distinct += i == 0 || kmers[i] != kmers[i - 1];
+    idx.keys.resize(distinct);
+    idx.startPos.resize(distinct + 1);
+    for (size_t i = 0, r = 0; i < total; i++)
     {
-        const size_t r = ranks[i];
-        idx.startPos[r] -= 1;
-        idx.positions[idx.startPos[r]] = positions[i];
+        if (i == 0 || kmers[i] != kmers[i - 1])
+        {
+            idx.keys[r] = kmers[i];
+            idx.startPos[r] = i;
+            r++;
+        }
     }
+    idx.startPos[distinct] = total;
+    RawVec<uint64_t>().swap(kmers);
+    // within a k-mer, the reference's counting sort leaves the occurrences in reverse
+    // insertion order
+    idx.positions.assign(total, 0);
+    const size_t numKeys = idx.keys.size();
+    parallelFor((numKeys + 4095) / 4096, [&](size_t c)
+    {
+        const size_t end = std::min(numKeys, (c + 1) * 4096);
+        for (size_t r = c * 4096; r < end; r++)
+        {
+            const size_t from = idx.startPos[r], to = idx.startPos[r + 1];
+            for (size_t j = from; j < to; j++) idx.positions[from + (to - 1 - j)] = positions[order[j]];
+        }
+    });
+    // initMaxCount: the occurrence count at the keep fraction of the sorted counts of every
+    // id but the last, plus one (read off a histogram of the counts)
     idx.maxCount = 0;
-    std::vector<size_t> counts;
-    if (idx.keys.size() > 0)
+    if (numKeys < 2) return;
+    const size_t numCounts = numKeys - 1;
+    size_t largest = 0;
+    for (size_t r = 0; r < numCounts; r++) largest = std::max<size_t>(largest, idx.startPos[r + 1] - idx.startPos[r]);
+    std::vector<size_t> histogram(largest + 1, 0);
+    for (size_t r = 0; r < numCounts; r++) histogram[idx.startPos[r + 1] - idx.startPos[r]]++;
+    size_t index = numCounts * keepLeastFrequentFraction;
+    if (index == numCounts) index = numCounts - 1;
+    size_t seen = 0;
+    for (size_t c = 0; c <= largest; c++)
     {
-        for (size_t i = 0; i + 1 < idx.keys.size(); i++) counts.push_back(idx.startPos[i + 1] - idx.startPos[i]);
+        seen += histogram[c];
+        if (seen > index)
+        {
+            idx.maxCount = c + 1;
+            break;
+        }
     }
-    std::sort(counts.begin(), counts.end());
-    if (counts.size() == 0) return;
-    size_t index = counts.size() * keepLeastFrequentFraction;
-    if (index == counts.size()) index = counts.size() - 1;
-    idx.maxCount = counts[index] + 1;
 }
 
 // iterateKmers + the lookup of MinimizerSeeder::getSeeds (MinimizerSeeder.cpp:59-102, 524-537)
