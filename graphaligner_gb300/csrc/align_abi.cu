@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 #include "readalign.h"
@@ -176,19 +177,12 @@ extern "C" int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* gr
         ga_set_last_error("ga_aligner_create: the graph or its minimizer index is inconsistent");
         return GA_ERR_ARGUMENT;
     }
-    // open-addressing table of the distinct k-mers, uploaded once
-    uint64_t capacity = 16;
-    while (capacity < 2 * a->index.keys.size()) capacity <<= 1;
-    std::vector<gadev::SeedSlot> slots(capacity, gadev::SeedSlot { gadev::kEmptyKmer, 0, 0 });
-    for (size_t r = 0; r < a->index.keys.size(); r++)
-    {
-        uint64_t key = a->index.keys[r];
-        uint64_t h = gadev::seed_slot_hash(key) & (capacity - 1);
-        while (slots[h].key != gadev::kEmptyKmer) h = (h + 1) & (capacity - 1);
-        slots[h] = gadev::SeedSlot { key, (uint32_t)a->index.startPos[r], (uint32_t)(a->index.startPos[r + 1] - a->index.startPos[r]) };
-    }
+    // open-addressing table of the distinct k-mers, built on all cores and uploaded once
+    const uint64_t capacity = gahost::seedTableCapacity(a->index);
+    std::unique_ptr<gadev::SeedSlot[]> slots(new gadev::SeedSlot[capacity]);
+    gahost::buildSeedTable(a->index, slots.get(), capacity);
     if (cudaMalloc((void**)&a->slots, capacity * sizeof(gadev::SeedSlot)) != cudaSuccess
-        || cudaMemcpy(a->slots, slots.data(), capacity * sizeof(gadev::SeedSlot), cudaMemcpyHostToDevice) != cudaSuccess
+        || cudaMemcpy(a->slots, slots.get(), capacity * sizeof(gadev::SeedSlot), cudaMemcpyHostToDevice) != cudaSuccess
         || cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess)
     {
         if (a->slots) cudaFree(a->slots);

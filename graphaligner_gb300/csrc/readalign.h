@@ -7,6 +7,7 @@
 #include <unordered_map>
 #include <vector>
 #include "../../include/graphaligner_gb300.h"
+#include "seed_table.h"
 
 namespace gahost
 {
@@ -201,6 +202,11 @@ struct MinimizerIndex
 };
 
 void buildMinimizerIndex(const HostGraph& g, size_t k, size_t w, double keepLeastFrequentFraction, MinimizerIndex& idx);
+// Slots of the open-addressing table of idx's distinct k-mers: a power of two, at least
+// twice the number of keys.
+uint64_t seedTableCapacity(const MinimizerIndex& idx);
+// Fills the table (seed_table.h layout: key, first position, count) on all cores.
+void buildSeedTable(const MinimizerIndex& idx, gadev::SeedSlot* slots, uint64_t capacity);
 // k-mer hits of one read in iterateKmers order: (read position, start, count), count < maxCount
 struct KmerMatch { uint64_t pos; uint64_t start; uint64_t count; };
 void kmerMatchesHost(const MinimizerIndex& idx, const std::string& seq, std::vector<KmerMatch>& out);

@@ -334,6 +334,45 @@ void buildMinimizerIndex(const HostGraph& g, size_t k, size_t w, double keepLeas
     }
 }
 
+uint64_t seedTableCapacity(const MinimizerIndex& idx)
+{
+    uint64_t capacity = 16;
+    while (capacity < 2 * idx.keys.size()) capacity <<= 1;
+    return capacity;
+}
+
+// Linear probing from seed_slot_hash.  Threads claim slots by compare-and-swap on the
+// key; the keys are distinct, so each is placed once, and every slot a key's probe
+// passes on its way was already taken, so a lookup finds it whatever order the claims
+// came in (the slot a key lands in may differ between builds, its lookup result not).
+void buildSeedTable(const MinimizerIndex& idx, gadev::SeedSlot* slots, uint64_t capacity)
+{
+    const size_t parts = 256;
+    parallelFor(parts, [&](size_t c)
+    {
+        const uint64_t from = capacity * c / parts, to = capacity * (c + 1) / parts;
+        for (uint64_t i = from; i < to; i++) slots[i] = gadev::SeedSlot { gadev::kEmptyKmer, 0, 0 };
+    });
+    const size_t numKeys = idx.keys.size();
+    parallelFor((numKeys + 4095) / 4096, [&](size_t c)
+    {
+        const size_t end = std::min(numKeys, (c + 1) * 4096);
+        for (size_t r = c * 4096; r < end; r++)
+        {
+            const uint64_t key = idx.keys[r];
+            uint64_t h = gadev::seed_slot_hash(key) & (capacity - 1);
+            while (true)
+            {
+                uint64_t expected = gadev::kEmptyKmer;
+                if (__atomic_compare_exchange_n(&slots[h].key, &expected, key, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) break;
+                h = (h + 1) & (capacity - 1);
+            }
+            slots[h].start = (uint32_t)idx.startPos[r];
+            slots[h].count = (uint32_t)(idx.startPos[r + 1] - idx.startPos[r]);
+        }
+    });
+}
+
 // iterateKmers + the lookup of MinimizerSeeder::getSeeds (MinimizerSeeder.cpp:59-102, 524-537)
 void kmerMatchesHost(const MinimizerIndex& idx, const std::string& str, std::vector<KmerMatch>& out)
 {

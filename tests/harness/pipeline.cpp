@@ -2,7 +2,9 @@
 // readalign.cpp) driven by the oracle's extensions, printing seeds or GAF in the
 // formats oracle/_ref/ga_ref prints, so the two can be diffed.
 //   pipeline <graph.gag> <reads.fa> seeds <k> <w> <density> <discard>
+//   pipeline <graph.gag> <reads.fa> table <k> <w> <discard>
 //   pipeline <graph.gag> <reads.fa> gaf <bandwidth> <maxcells|->
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -126,6 +128,49 @@ int main(int argc, char** argv)
     gahost::HostGraph graph(hd);
     auto reads = readFasta(argv[2]);
     std::string mode = argv[3];
+    if (mode == "table")
+    {
+        // the k-mer table the lookup kernel probes: every key found with its group, and
+        // k-mers that are not in the index not found
+        size_t k = std::stoul(argv[4]), w = std::stoul(argv[5]);
+        double discard = std::stod(argv[6]);
+        gahost::MinimizerIndex idx;
+        gahost::buildMinimizerIndex(graph, k, w, 1.0 - discard, idx);
+        const uint64_t capacity = gahost::seedTableCapacity(idx);
+        std::vector<gadev::SeedSlot> slots(capacity);
+        gahost::buildSeedTable(idx, slots.data(), capacity);
+        auto find = [&](uint64_t key, gadev::SeedSlot& out)
+        {
+            uint64_t h = gadev::seed_slot_hash(key) & (capacity - 1);
+            for (uint64_t n = 0; n < capacity; n++)
+            {
+                if (slots[h].key == key) { out = slots[h]; return true; }
+                if (slots[h].key == gadev::kEmptyKmer) return false;
+                h = (h + 1) & (capacity - 1);
+            }
+            return false;
+        };
+        size_t bad = 0, used = 0;
+        for (const auto& sl : slots) used += sl.key != gadev::kEmptyKmer;
+        for (size_t r = 0; r < idx.keys.size(); r++)
+        {
+            gadev::SeedSlot sl;
+            if (!find(idx.keys[r], sl) || sl.start != idx.startPos[r] || sl.count != idx.startPos[r + 1] - idx.startPos[r]) bad++;
+        }
+        size_t absentFound = 0, absentTried = 0;
+        const uint64_t mask = (k * 2 >= 64) ? ~0ULL : ((1ULL << (k * 2)) - 1);
+        for (uint64_t x = 1; absentTried < 100000; x++)
+        {
+            const uint64_t key = (x * 0x9e3779b97f4a7c15ULL) & mask;
+            if (std::binary_search(idx.keys.begin(), idx.keys.end(), key)) continue;
+            absentTried++;
+            gadev::SeedSlot sl;
+            absentFound += find(key, sl);
+        }
+        std::cout << "keys " << idx.keys.size() << " capacity " << capacity << " used " << used << " bad " << bad
+                  << " absent_found " << absentFound << "\n";
+        return 0;
+    }
     if (mode == "seeds")
     {
         size_t k = std::stoul(argv[4]), w = std::stoul(argv[5]);

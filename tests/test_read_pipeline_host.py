@@ -23,7 +23,7 @@ SOURCES = [os.path.join(ROOT, "tests", "harness", "pipeline.cpp"),
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
     os.makedirs(BUILD, exist_ok=True)
-    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
+    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "seed_table.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
     if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < max(os.path.getmtime(d) for d in deps):
         subprocess.run(["g++", "-std=c++17", "-O2", "-o", HARNESS, *SOURCES, "-lpthread"], check=True)
     d = tmp_path_factory.mktemp("pipeline")
@@ -39,6 +39,18 @@ def test_seeds_match_reference(harness):
     mine = [hashlib.sha1(line.encode()).hexdigest() for line in out.splitlines()]
     ref = open(os.path.join(GOLDEN, "vg50k_seeds.digest")).read().split()
     assert mine == ref
+
+
+@pytest.mark.parametrize("name,k,w,discard", [("vg50k", 15, 20, 0.001), ("dbg100k", 19, 30, 0.0002)])
+def test_seed_table_finds_every_key(harness, tmp_path, name, k, w, discard):
+    """The k-mer table the lookup kernel probes, built on all cores: every k-mer of the index
+    is found with its group, and k-mers outside the index are not."""
+    exe, _, reads, _ = harness
+    out = subprocess.run([exe, graph_file(name, str(tmp_path)), reads, "table", str(k), str(w), str(discard)],
+                         check=True, capture_output=True, text=True).stdout.split()
+    f = dict(zip(out[0::2], (int(v) for v in out[1::2])))
+    assert f["keys"] > 10000 and f["used"] == f["keys"] and f["capacity"] >= 2 * f["keys"]
+    assert f["bad"] == 0 and f["absent_found"] == 0
 
 
 @pytest.mark.parametrize("bandwidth", [10, 5])
