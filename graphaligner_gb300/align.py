@@ -38,12 +38,18 @@ class HostGraphDesc(ctypes.Structure):
             (g.node_ids, np.int32), (g.node_offset, np.uint32), (g.reverse, np.uint8), (g.chain_number, np.uint64),
             (g.chain_approx_pos, np.uint64), (g.lookup_ids, np.int32), (g.original_size, np.uint32),
             (g.lookup_offsets, np.uint32), (g.lookup_nodes, np.uint32))]
-        names = (ctypes.c_char_p * max(1, len(g.names)))(*[n.encode() for n in g.names])
+        # node names as one NUL-separated buffer and a pointer per name into it
+        blob = ("\0".join(g.names) + "\0").encode()
+        raw = np.frombuffer(blob, dtype=np.uint8)
+        ends = np.flatnonzero(raw == 0)
+        starts = np.concatenate(([0], ends[:-1] + 1)).astype(np.uint64)
+        name_ptrs = starts + np.uint64(raw.ctypes.data)
+        names = ctypes.cast(ctypes.c_void_p(name_ptrs.ctypes.data), ctypes.POINTER(ctypes.c_char_p))
         d = cls(_abi.GraphDesc.from_graph(g), ptr(keep[0], ctypes.c_int32), ptr(keep[1], ctypes.c_uint32),
                 ptr(keep[2], ctypes.c_uint8), ptr(keep[3], ctypes.c_uint64), ptr(keep[4], ctypes.c_uint64),
                 len(g.lookup_ids), ptr(keep[5], ctypes.c_int32), ptr(keep[6], ctypes.c_uint32),
                 ptr(keep[7], ctypes.c_uint32), ptr(keep[8], ctypes.c_uint32), names)
-        d._keep = (keep, names, d.base)
+        d._keep = (keep, blob, name_ptrs, d.base)
         return d
 
 

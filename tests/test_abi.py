@@ -69,3 +69,22 @@ def test_null_arguments_are_rejected_before_any_device_call(cuda_lib):
     assert not wrong, f"not GA_ERR_ARGUMENT: {wrong}"
     for name in ("ga_graph_free", "ga_extender_free", "ga_aligner_free", "ga_server_free"):
         assert getattr(L, name)(n) == GA_OK, name
+
+
+def test_host_graph_desc_points_at_every_node_name():
+    """ga_host_graph_desc.names, as align.HostGraphDesc lays it out (one NUL-separated buffer
+    and a pointer per name), reads back as the graph's names, in nodeLookup order."""
+    import gzip
+    import tempfile
+    from graphaligner_gb300 import graph as gg
+    from graphaligner_gb300.align import HostGraphDesc
+    with tempfile.NamedTemporaryFile(suffix=".gag") as f:
+        f.write(gzip.open(os.path.join(ROOT, "tests", "golden", "vg50k_graph.gag.gz")).read())
+        f.flush()
+        g = gg.load_gag(f.name)
+    d = HostGraphDesc.from_graph(g)
+    assert d.num_lookup == len(g.names) > 1000
+    assert [d.names[i].decode() for i in range(d.num_lookup)] == list(g.names)
+    g.names = ["a", "", "node 3"] + list(g.names[3:])
+    d = HostGraphDesc.from_graph(g)
+    assert [d.names[i].decode() for i in range(3)] == ["a", "", "node 3"]
