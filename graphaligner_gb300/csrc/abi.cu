@@ -406,6 +406,17 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     return GA_OK;
 }
 
+// The packed trace item holds seqPos + 1 in 25 bits.
+static_assert(GA_MAX_SEQ_LEN == (1u << 25) - 1, "read position field of the trace item");
+
+static int check_lengths(const uint32_t* len, uint32_t n)
+{
+    for (uint32_t i = 0; i < n; i++)
+        if (len[i] > GA_MAX_SEQ_LEN)
+            return fail(GA_ERR_ARGUMENT, "extension " + std::to_string(i) + ": sequence longer than GA_MAX_SEQ_LEN (33,554,431 bp)");
+    return GA_OK;
+}
+
 static std::vector<uint32_t> longest_first(const uint32_t* len, uint32_t n)
 {
     std::vector<uint32_t> order(n);
@@ -420,6 +431,8 @@ static int stage_host_batch(ga_extender* x, const ga_extend_batch_desc* b, ga_ex
     ga_extend_results* dr, std::vector<uint32_t>& sortedLen, uint64_t* itemsOut)
 {
     const uint32_t n = b->num;
+    int rc = check_lengths(b->seq_len, n);
+    if (rc != GA_OK) return rc;
     uint64_t seqBytes = 0, items = 0;
     for (uint32_t i = 0; i < n; i++)
     {
@@ -575,6 +588,8 @@ extern "C" int ga_extend_batch_device(ga_extender_t x, const ga_extend_params* p
     cudaStream_t s = stream ? (cudaStream_t)stream : x->stream;
     GA_CUDA(cudaMemcpyAsync(len.data(), b->seq_len, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaStreamSynchronize(s));
+    int rc = check_lengths(len.data(), n);
+    if (rc != GA_OK) return rc;
     std::vector<uint32_t> order = longest_first(len.data(), n);
     std::vector<uint32_t> sortedLen(n);
     for (uint32_t i = 0; i < n; i++) sortedLen[i] = len[order[i]];

@@ -209,6 +209,14 @@ extern "C" int ga_aligner_free(ga_aligner_t a)
 extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* names, const uint8_t* seq, const uint64_t* seqOffset, const uint32_t* seqLen)
 {
     if (!a || (n > 0 && (!names || !seq || !seqOffset || !seqLen))) return GA_ERR_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        if (seqLen[i] > GA_MAX_SEQ_LEN)
+        {
+            ga_set_last_error(("ga_align_reads: read " + std::to_string(i) + " is longer than GA_MAX_SEQ_LEN (33,554,431 bp)").c_str());
+            return GA_ERR_ARGUMENT;
+        }
+    }
     auto start = std::chrono::steady_clock::now();
     a->stats = ga_align_stats {};
     a->stats.reads = n;

@@ -321,6 +321,11 @@ extern "C" int ga_server_create(ga_aligner_t aligner, const ga_server_params* pa
 extern "C" int ga_server_submit(ga_server_t s, const char* name, const uint8_t* seq, uint32_t len, uint64_t* ticket)
 {
     if (!s || (len > 0 && !seq)) return GA_ERR_ARGUMENT;
+    if (len > GA_MAX_SEQ_LEN)
+    {
+        ga_set_last_error("ga_server_submit: read longer than GA_MAX_SEQ_LEN (33,554,431 bp)");
+        return GA_ERR_ARGUMENT;
+    }
     Submitted q;
     q.name = name ? name : "";
     q.seq.assign((const char*)seq, len);

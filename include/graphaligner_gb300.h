@@ -14,8 +14,10 @@
  *                        (src/GraphAlignerBitvectorBanded.h:59-76), called twice
  *                        per seed by GraphAligner::getTwoDirectionalTrace
  *                        (src/GraphAligner.h:475-520)
- *   ga_index_upload /    MinimizerSeeder index arrays and getSeeds lookup
- *   ga_seed_batch        (src/MinimizerSeeder.h:16-33, src/MinimizerSeeder.cpp:521-543)
+ *   ga_aligner_create    the MinimizerSeeder index (src/MinimizerSeeder.cpp:299-491)
+ *   ga_align_reads       the per-read body of runComponentMappings: getSeeds, AlignOneWay,
+ *                        SelectAlignments and the GAF line (src/Aligner.cpp:443-592)
+ *   ga_server_*          the worker loop around it, as a submit/poll request interface
  */
 #ifndef GRAPHALIGNER_GB300_H
 #define GRAPHALIGNER_GB300_H
@@ -88,12 +90,17 @@ typedef struct ga_extend_batch_desc {
  *   bit  38      nodeSwitch
  *   bits 39..63  seqPos + 1 (0 encodes seqPos == (size_t)-1, the row above the read) */
 typedef struct ga_extend_results {
-    int32_t*  status;                 /* [num] GA_OK / GA_TRACE_FAILED / GA_ASSERT / GA_CAPACITY */
+    int32_t*  status;                 /* [num] GA_OK / GA_TRACE_FAILED / GA_ASSERT / GA_CAPACITY /
+                                         GA_BAD_REQUEST (start node or offset outside the graph) */
     int32_t*  score;                  /* [num] OnewayTrace::score */
     uint32_t* trace_len;              /* [num] items written */
     uint64_t* trace_items;            /* packed items, laid out by trace_offset */
     uint64_t* cell_steps;             /* [num] or NULL: Myers column steps in the fill (GCUPS numerator / 64) */
 } ga_extend_results;
+
+/* Longest extension sequence or read: seqPos + 1 must fit the item's 25 bits.  Longer
+ * ones make ga_extend_batch*, ga_align_reads and ga_server_submit return GA_ERR_ARGUMENT. */
+#define GA_MAX_SEQ_LEN        33554431u
 
 #define GA_TRACE_NODE(x)      ((uint32_t)((x) & 0xffffffffu))
 #define GA_TRACE_OFFSET(x)    ((uint32_t)(((x) >> 32) & 63u))

@@ -68,3 +68,32 @@ def test_gpu_two_lanes_gaf_matches_reference(cuda_lib):
     expected += "".join("".join(l.replace(n + "\t", n + "_copy\t", 1) for l in want.get(n, [])) for n in names)
     assert gaf == expected
     assert a.stats()["failed_reads"] == 0
+
+
+def test_gpu_sequences_over_the_trace_limit_are_rejected(cuda_lib, tmp_path):
+    """A sequence longer than GA_MAX_SEQ_LEN (its read positions would not fit the trace item)
+    is refused with GA_ERR_ARGUMENT before anything is copied or launched, by the extension,
+    read-level and serving entry points; the handles stay usable."""
+    from graphaligner_gb300 import graph as gg
+    from graphaligner_gb300._lib import GAError
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender, ExtendParams
+    from graphaligner_gb300.serve import Server
+    max_len = 33554431
+    path = os.path.join(tmp_path, "t.gag")
+    open(path, "wb").write(gzip.open(os.path.join(GOLDEN, "test_graph.gag.gz")).read())
+    g = gg.load_gag(path)
+    lines = open(os.path.join(GOLDEN, "test_read.fa")).read().split()
+    x = Extender(DeviceGraph(g))
+    a = Aligner(x, g, preset("vg"))
+    long_read = b"A" * (max_len + 1)
+    with pytest.raises(GAError):
+        x.extend(ExtendParams(bandwidth=10), [long_read], [int(g.node_ids[0])], [0])
+    with pytest.raises(GAError):
+        a.align(["too_long"], [long_read])
+    with Server(a) as srv:
+        with pytest.raises(GAError):
+            srv.submit("too_long", long_read)
+    assert a.align([lines[0][1:]], [lines[1].encode()]) == open(os.path.join(GOLDEN, "test_graph.gaf")).read()
+    res = x.extend(ExtendParams(bandwidth=10), [lines[1].encode()[:40]], [int(g.node_ids[0])], [0])
+    assert res.status[0] in (0, 1)
