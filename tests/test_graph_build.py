@@ -118,3 +118,77 @@ def test_build_from_gfa_iupac_matches_reference_graph():
             out[(int(g.node_ids[i]), int(g.node_offset[i]))] = tuple(int(x) for x in g.seq_ambiguous[4 * k:4 * k + 4])
         return out
     assert amb(mine) == amb(ref)
+
+
+GRAPH_FIELDS = ["num_nodes", "first_ambiguous", "node_length", "node_ids", "node_offset", "reverse", "linearizable",
+                "component", "chain_number", "chain_approx_pos", "seq2bit", "seq_ambiguous", "in_offsets", "in_neighbors",
+                "out_offsets", "out_neighbors", "lookup_ids", "original_size", "lookup_offsets", "lookup_nodes", "names",
+                "bp_size"]
+
+
+def _differing_fields(a, b):
+    bad = []
+    for f in GRAPH_FIELDS:
+        x, y = getattr(a, f), getattr(b, f)
+        if isinstance(x, np.ndarray):
+            if x.dtype != y.dtype or x.shape != y.shape or not np.array_equal(x, y):
+                bad.append(f)
+        elif x != y:
+            bad.append(f)
+    return bad
+
+
+# numeric and named segments, links on both strands, overlaps, lower case, U, IUPAC codes,
+# a segment longer than one piece, a self-loop and a bubble
+HAND_GFA_NUMERIC = "\n".join([
+    "H\tVN:Z:1.0",
+    "S\t1\tACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTACGTAC",
+    "S\t2\tacgtnACGUu",
+    "S\t3\tGGGCCCTTTAAA",
+    "S\t4\tTTTT",
+    "S\t5\tRYKMSWBDHVNacgt",
+    "L\t1\t+\t2\t+\t0M",
+    "L\t1\t+\t3\t+\t0M",
+    "L\t2\t+\t4\t+\t0M",
+    "L\t3\t+\t4\t+\t0M",
+    "L\t4\t+\t4\t+\t0M",
+    "L\t4\t-\t5\t+\t*",
+    "L\t3\t+\t1\t-\t2M",
+]) + "\n"
+HAND_GFA_NAMED = HAND_GFA_NUMERIC.replace("\t1\t", "\tseg_one\t").replace("\t4\t", "\tfour\t")
+
+
+def test_native_builder_equals_the_restatement():
+    """graph.build_from_gfa (native, csrc/gfa_build.cpp) gives exactly the arrays of the
+    Python restatement (tests/gfa_restatement.py): numbering, edges in order, components,
+    chains and chain positions, sequences and names."""
+    import gfa_restatement as gr
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    cases = {
+        "vg": dg.small_vg(0).to_gfa(),
+        "vg_1m": dg.make_variation_graph(1_000_000, 100, 0.7, 20, 5).to_gfa(),
+        "dbg": dg.compact_dbg(dg.small_dbg_genome(0), 63),
+        "iupac": mg.iupac_edge_set(5)[0].to_gfa(),
+        "hand_numeric": HAND_GFA_NUMERIC,
+        "hand_named": HAND_GFA_NAMED,
+        "crlf": HAND_GFA_NUMERIC.replace("\n", "\r\n"),
+    }
+    for name, text in cases.items():
+        a, b = gg.build_from_gfa(text), gr.build_from_gfa(text)
+        assert a.num_nodes > 0
+        assert not _differing_fields(a, b), (name, _differing_fields(a, b))
+
+
+def test_native_builder_refuses_what_it_cannot_build():
+    import pytest
+    from graphaligner_gb300._lib import GAError
+    for bad in ["S\t1\tACGT\nL\t1\t+\t9\t+\t0M\n",          # link to an unknown segment
+                "S\t1\tACGT\nS\t2\tACGT\nL\t1\t+\t2\t+\t4M\n",  # overlap not smaller than both
+                "S\t1\t\n",                                    # empty segment
+                "S\t1\tAC-GT\n",                               # not an IUPAC code
+                "S\t1\tACGT\nS\t2\tACGT\nL\t1\t+\t2\t+\tx\n"]:  # overlap not a number
+        with pytest.raises(GAError):
+            gg.build_from_gfa(bad)
