@@ -174,7 +174,7 @@ def cpu_baseline(g, batch, params, sample_bp: float, threads: int):
     res = oracle.extend(g, params, sub, threads=threads)
     dt = time.perf_counter() - t
     bp = aligned_bp(res)
-    return {"value": bp / dt, "unit": UNIT, "cores": threads, "kind": "port",
+    return {"value": bp / dt, "unit": UNIT, "cores": threads, "kind": "port", "seconds": dt,
             "sample": f"{len(idx)} of {batch.num} extensions (every {step}th, {int(lens[idx].sum())} read bp), oracle restatement in C++, {threads} threads, {dt:.1f} s"}, res, idx
 
 
@@ -186,19 +186,20 @@ def run_reference(args, rank, world):
     g, batch = make_workload(args.reads, 0)
     params = ExtendParams(bandwidth=10)
     threads = os.cpu_count() or 1
-    vals = []
+    vals, secs = [], []
     for i in range(args.warmup + args.steps):
         cb, _, _ = cpu_baseline(g, batch, params, args.cpu_sample_bp, threads)
         if i >= args.warmup:
             vals.append(cb["value"])
+            secs.append(cb["seconds"])
     v = statistics.median(vals)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic", "impl": "reference",
+            "ms_per_step": statistics.median(secs) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference's own C++ source is not present where this runs; the oracle restatement (bit-exact with it on the golden vectors) is timed"}
+            "note": "the reference's own C++ source is not present where this runs; the oracle restatement (bit-exact with it on the golden vectors) is timed; a step is the bounded sample of the batch named in cpu_baseline.sample"}
     print(json.dumps(line), flush=True)
 
 
