@@ -255,6 +255,7 @@ int main(int argc, char** argv)
     for (auto& o : out) std::cout << o.gaf;
     const double alignSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - alignStart).count();
     std::cerr << "rounds " << st.rounds << " extensions " << st.extensions << " bp " << st.bpAligned << " failed " << st.failedReads
-              << " seconds " << alignSeconds << " speculative_used " << st.speculativeUsed << " discarded " << st.speculativeDiscarded << std::endl;
+              << " seconds " << alignSeconds << " speculative_used " << st.speculativeUsed << " discarded " << st.speculativeDiscarded
+              << " collect_ms " << st.collectMs << " consume_ms " << st.consumeMs << " finish_ms " << st.finishMs << std::endl;
     return 0;
 }
