@@ -192,3 +192,34 @@ def test_native_builder_refuses_what_it_cannot_build():
                 "S\t1\tACGT\nS\t2\tACGT\nL\t1\t+\t2\t+\tx\n"]:  # overlap not a number
         with pytest.raises(GAError):
             gg.build_from_gfa(bad)
+
+
+def _random_gfa(rng, numeric: bool) -> str:
+    """Random segments (ACGT with some lower case, U and IUPAC codes), random links in
+    both orientations with 0-bp or small overlaps, self-links and repeated links."""
+    n = int(rng.integers(5, 40))
+    names = [str(int(x)) for x in rng.choice(10_000, n, replace=False) + 1] if numeric else [f"s{k}x" for k in range(n)]
+    alphabet = np.frombuffer(b"ACGTACGTACGTACGTacgtUNRYKMSWBDHV", dtype=np.uint8)
+    weights = np.array([8.0] * 16 + [1.0] * 4 + [0.2] * 12)
+    weights /= weights.sum()
+    lens = rng.integers(1, 300, n)
+    lines = []
+    for name, length in zip(names, lens):
+        seq = rng.choice(alphabet, int(length), p=weights).tobytes().decode()
+        lines.append(f"S\t{name}\t{seq}")
+    for _ in range(int(rng.integers(0, 3 * n))):
+        a, b = int(rng.integers(0, n)), int(rng.integers(0, n))
+        limit = int(min(lens[a], lens[b]))
+        ov = 0 if rng.random() < 0.6 or limit <= 1 else int(rng.integers(1, limit))
+        ov_text = "*" if ov == 0 and rng.random() < 0.2 else f"{ov}M"
+        lines.append(f"L\t{names[a]}\t{'+-'[int(rng.integers(0, 2))]}\t{names[b]}\t{'+-'[int(rng.integers(0, 2))]}\t{ov_text}")
+    return "\n".join(lines) + "\n"
+
+
+def test_native_builder_equals_the_restatement_on_random_gfas():
+    import gfa_restatement as gr
+    rng = np.random.default_rng(2024)
+    for k in range(60):
+        text = _random_gfa(rng, numeric=k % 2 == 0)
+        a, b = gg.build_from_gfa(text), gr.build_from_gfa(text)
+        assert not _differing_fields(a, b), (k, _differing_fields(a, b), text)
