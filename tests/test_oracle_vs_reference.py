@@ -82,3 +82,43 @@ def test_oracle_matches_reference_on_generated_inputs(oracle_lib, kind, seed, ba
     assert len(expected) == batch.num > 20
     bad = compare(res, expected)
     assert not bad, f"{len(bad)} of {batch.num} extensions differ from the reference, first {bad[:5]}"
+
+
+from test_read_pipeline_host import harness  # noqa: E402,F401  (the host read-level harness fixture)
+
+
+# (kind, seed, bandwidth): reads from freshly generated graphs, -x vg at the bandwidth or -x dbg
+READ_CASES = [("vg", 31, 10), ("vg", 32, 5), ("vg", 33, 15), ("dbg", 34, 5)]
+
+
+@pytest.mark.parametrize("kind,seed,bandwidth", READ_CASES)
+def test_read_level_matches_reference_on_generated_inputs(harness, oracle_lib, tmp_path, kind, seed, bandwidth):  # noqa: F811
+    """Seeds (getSeeds + OrderSeeds) and GAF of the package's host read-level code, driven by
+    the oracle's extensions, against the reference's own on graphs and reads made here."""
+    exe = harness[0]
+    if kind == "vg":
+        g = dg.make_variation_graph(40_000, 150, 0.7, 20, seed)
+        gfa_text = g.to_gfa()
+        reads = dg.sample_reads(g, 30, seed + 1, dg.uniform_length(300, 9_000), dg.uniform_error(0.04, 0.16))
+        k, w, density, discard, mode = "15", "20", "10", "0.001", "gaf"
+    else:
+        genome = dg.make_repeat_genome(40_000, 6, 1_500, 0.01, 0.04, 10, tandem_len=(200, 800), seed=seed)
+        gfa_text = dg.compact_dbg(genome, 63)
+        reads = dg.dbg_reads(genome, 12, 8_000, 0.1, seed + 1)
+        k, w, density, discard, mode = "19", "30", "5", "0.0002", "gafdbg"
+    gfa = os.path.join(tmp_path, "g.gfa")
+    open(gfa, "w").write(gfa_text)
+    gag = os.path.join(tmp_path, "g.gag")
+    subprocess.run([REF, "graphdump", gfa, gag], check=True)
+    fa = os.path.join(tmp_path, "reads.fa")
+    open(fa, "w").write(dg.write_fasta(reads))
+    ref_seeds = os.path.join(tmp_path, "seeds.txt")
+    subprocess.run([REF, "seeds", gfa, fa, ref_seeds, k, w, density, discard], check=True)
+    mine = subprocess.run([exe, gag, fa, "seeds", k, w, density, discard], check=True, capture_output=True, text=True).stdout
+    assert mine == open(ref_seeds).read()
+    ref_gaf = os.path.join(tmp_path, "ref.gaf")
+    subprocess.run([REF, "align", gfa, fa, ref_gaf] + (["vg", str(bandwidth)] if kind == "vg" else ["dbg"]), check=True)
+    mine = subprocess.run([exe, gag, fa, mode, str(bandwidth)], check=True, capture_output=True, text=True).stdout
+    expected = open(ref_gaf).read()
+    assert expected.count("\n") >= len(reads) // 2
+    assert mine == expected
