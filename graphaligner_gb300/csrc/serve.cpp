@@ -78,7 +78,6 @@ struct ga_server
     bool stop = false;
     ga_server_stats stats {};
     std::thread worker;
-    int startError = GA_OK;
     // the read class a lane serves
     int laneClass(uint32_t lane) const { return lanes > 1 && lane == 0 ? 0 : 1; }
     int readClass(size_t len) const { return lanes > 1 && len >= longBp ? 0 : 1; }
@@ -121,10 +120,13 @@ static void serve_loop(ga_server* s)
         lanes[k].ext->params = &a->params.extend;
         if (ga_extender_create_like(a->ext, &lanes[k].ext->ext) != GA_OK)
         {
+            // no device memory for another extender: serve every read on lane 0, including
+            // long reads already queued for it
             std::lock_guard<std::mutex> lk(s->mu);
-            s->startError = GA_ERR_CUDA;
             s->lanes = 1;
             lanes.resize(1);
+            for (auto& q : s->queue[0]) s->queue[1].push_back(std::move(q));
+            s->queue[0].clear();
             break;
         }
         lanes[k].ext->owned = true;

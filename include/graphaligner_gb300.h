@@ -289,7 +289,8 @@ typedef struct ga_server_params {
     uint32_t max_reads_in_flight;     /* reads in their seed loops at once; 0 = 4096 */
     uint64_t max_band_bytes;          /* admission budget of estimated band + trace memory; 0 = 2 GiB */
     uint32_t band_bytes_per_bp;       /* the estimate per read bp; 0 = 32 */
-    uint32_t lanes;                   /* concurrent rounds, each with its own extender; 0 = 2 */
+    uint32_t lanes;                   /* concurrent rounds, each with its own extender; 0 = 2, at most 8;
+                                         one lane if the device has no room for another extender */
     uint32_t long_read_bp;            /* with 2+ lanes, reads this long are served on lane 0 only; 0 = 15000 */
 } ga_server_params;
 
