@@ -7,6 +7,8 @@ read-level flow (seed loop, selection, GAF, serving loop) behind a C ABI
 (include/graphaligner_gb300.h), with the Python mirror of the reference interface:
 ``extend.Extender`` (getReverseTraceFromSeed, batched), ``align.Aligner`` (the
 per-read flow of the aligner) and ``serve.Server`` (continuous batching).
+``graph.build_from_gfa`` builds an alignment graph from GFA text in native code;
+``graph.load_gag`` reads one the reference built.
 """
 from .build import build  # noqa: F401
 
