@@ -79,9 +79,9 @@ struct Built
 
 struct Link
 {
-    std::string from;
+    uint32_t from;      // segment slots
+    uint32_t to;
     bool fromForward;
-    std::string to;
     bool toForward;
     int64_t overlap;
 };
@@ -513,9 +513,12 @@ struct Chains
 void build(const char* text, size_t bytes, Built& g)
 {
     // ---- GFA: segments in file order, links ----
-    std::unordered_map<std::string, std::string> seqs;
-    std::vector<std::string> order;
-    std::vector<Link> links;
+    // one slot per segment name, holding the last sequence given for it
+    std::unordered_map<std::string, uint32_t> slotOf;
+    std::vector<std::string> slotName, slotSeq;
+    std::vector<uint32_t> order;      // the slot of every S line, in file order
+    std::vector<std::vector<std::string>> linkFields;
+    slotOf.reserve(bytes / 64 + 16);
     size_t pos = 0;
     while (pos < bytes)
     {
@@ -530,33 +533,53 @@ void build(const char* text, size_t bytes, Built& g)
             if (f[0] == "S")
             {
                 if (f.size() < 3) throw GfaError { "segment line with fewer than 3 fields" };
-                seqs[f[1]] = f[2];
-                order.push_back(f[1]);
+                auto it = slotOf.find(f[1]);
+                uint32_t slot;
+                if (it == slotOf.end())
+                {
+                    slot = (uint32_t)slotName.size();
+                    slotOf.emplace(f[1], slot);
+                    slotName.push_back(f[1]);
+                    slotSeq.push_back(std::move(f[2]));
+                }
+                else
+                {
+                    slot = it->second;
+                    slotSeq[slot] = std::move(f[2]);
+                }
+                order.push_back(slot);
             }
             else if (f[0] == "L")
             {
                 if (f.size() < 6) throw GfaError { "link line with fewer than 6 fields" };
-                links.push_back(Link { f[1], f[2] == "+", f[3], f[4] == "+", parseOverlap(f[5]) });
+                f.resize(6);
+                linkFields.push_back(std::move(f));
             }
         }
         pos = end + 1;
     }
     bool numeric = true;
-    for (const auto& name : order) numeric = numeric && numericName(name);
-    std::unordered_map<std::string, int64_t> ids;
-    for (size_t k = 0; k < order.size(); k++) ids[order[k]] = numeric ? parseId(order[k]) : (int64_t)k + 1;
-    auto segment = [&](const std::string& name) -> const std::string&
+    for (uint32_t slot : order) numeric = numeric && numericName(slotName[slot]);
+    // a repeated name takes the id of its last S line
+    std::vector<int64_t> ids(slotName.size());
+    for (size_t k = 0; k < order.size(); k++) ids[order[k]] = numeric ? parseId(slotName[order[k]]) : (int64_t)k + 1;
+    auto slotNamed = [&](const std::string& name) -> uint32_t
     {
-        auto it = seqs.find(name);
-        if (it == seqs.end()) throw GfaError { "link to an unknown segment '" + name + "'" };
+        auto it = slotOf.find(name);
+        if (it == slotOf.end()) throw GfaError { "link to an unknown segment '" + name + "'" };
         return it->second;
     };
+    std::vector<Link> links;
+    links.reserve(linkFields.size());
+    for (const auto& f : linkFields)
+        links.push_back(Link { slotNamed(f[1]), slotNamed(f[3]), f[2] == "+", f[4] == "+", parseOverlap(f[5]) });
+    std::vector<std::vector<std::string>>().swap(linkFields);
     std::unordered_map<int64_t, std::vector<int64_t>> breaks;
     for (const auto& l : links)
     {
-        const int64_t la = (int64_t)segment(l.from).size(), lb = (int64_t)segment(l.to).size();
+        const int64_t la = (int64_t)slotSeq[l.from].size(), lb = (int64_t)slotSeq[l.to].size();
         if (l.overlap >= la || l.overlap >= lb)
-            throw GfaError { "overlap between " + l.from + " and " + l.to + " is not smaller than both nodes" };
+            throw GfaError { "overlap between " + slotName[l.from] + " and " + slotName[l.to] + " is not smaller than both nodes" };
         if (l.overlap)
         {
             const int64_t fa = ids[l.from] * 2 + (l.fromForward ? 0 : 1), fb = ids[l.to] * 2 + (l.toForward ? 0 : 1);
@@ -570,10 +593,11 @@ void build(const char* text, size_t bytes, Built& g)
     std::vector<std::pair<int64_t, std::vector<uint32_t>>> lookup;
     std::vector<std::string> names;
     std::unordered_map<int64_t, uint32_t> sizeOf;
-    for (const auto& name : order)
+    for (uint32_t slot : order)
     {
-        const std::string& s = seqs[name];
-        const int64_t nid = ids[name];
+        const std::string& name = slotName[slot];
+        const std::string& s = slotSeq[slot];
+        const int64_t nid = ids[slot];
         std::string rc(s.rbegin(), s.rend());
         for (auto& c : rc) c = (char)kTables.complement[(unsigned char)c];
         for (int strand = 0; strand < 2; strand++)
@@ -611,8 +635,10 @@ void build(const char* text, size_t bytes, Built& g)
     const size_t n = pieces.size();
     Lists in(n), out(n);
     std::unordered_map<uint64_t, uint32_t> pieceAt;   // (bigraph node, offset) -> piece
+    pieceAt.reserve(n);
     auto key = [](int64_t big, int64_t offset) { return ((uint64_t)(uint32_t)(int32_t)big << 32) | (uint64_t)(uint32_t)offset; };
     std::unordered_map<int64_t, uint32_t> lastPiece;
+    lastPiece.reserve(lookup.size());
     for (const auto& l : lookup)
     {
         for (uint32_t i : l.second) pieceAt[key(l.first, pieces[i].offset)] = i;
