@@ -209,7 +209,6 @@ uint64_t seedTableCapacity(const MinimizerIndex& idx);
 void buildSeedTable(const MinimizerIndex& idx, gadev::SeedSlot* slots, uint64_t capacity);
 // k-mer hits of one read in iterateKmers order: (read position, start, count), count < maxCount
 struct KmerMatch { uint64_t pos; uint64_t start; uint64_t count; };
-void kmerMatchesHost(const MinimizerIndex& idx, const std::string& seq, std::vector<KmerMatch>& out);
 void selectSeeds(const HostGraph& g, const MinimizerIndex& idx, const std::string& seq, double density,
     std::vector<KmerMatch>& matches, std::vector<SeedHit>& out);
 

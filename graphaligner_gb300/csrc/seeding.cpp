@@ -373,63 +373,6 @@ void buildSeedTable(const MinimizerIndex& idx, gadev::SeedSlot* slots, uint64_t 
     });
 }
 
-// iterateKmers + the lookup of MinimizerSeeder::getSeeds (MinimizerSeeder.cpp:59-102, 524-537)
-void kmerMatchesHost(const MinimizerIndex& idx, const std::string& str, std::vector<KmerMatch>& out)
-{
-    out.clear();
-    const size_t k = idx.k;
-    const size_t realWindow = idx.w - k + 1;
-    if (str.size() < k) return;
-    const uint64_t mask = ~(0xFFFFFFFFFFFFFFFFULL << (k * 2));
-    auto emit = [&](size_t pos, uint64_t kmer)
-    {
-        auto f = std::lower_bound(idx.keys.begin(), idx.keys.end(), kmer);
-        if (f == idx.keys.end() || *f != kmer) return;
-        size_t r = f - idx.keys.begin();
-        uint64_t start = idx.startPos[r];
-        uint64_t count = idx.startPos[r + 1] - start;
-        if (count >= idx.maxCount) return;
-        out.push_back(KmerMatch { pos, start, count });
-    };
-    size_t offset = 0;
-start:
-    while (offset < str.size() && !validChar(str[offset])) offset++;
-    if (offset + k > str.size()) return;
-    {
-        uint64_t kmer = 0;
-        for (size_t i = 0; i < k; i++)
-        {
-            if (!validChar(str[offset + i]))
-            {
-                offset += i;
-                goto start;
-            }
-            kmer <<= 2;
-            kmer |= charToInt(str[offset + i]);
-        }
-        emit(offset + k - 1, kmer);
-        uint64_t lastKmer = kmer;
-        size_t lastPos = offset + k - 1;
-        for (size_t i = k; offset + i < str.size(); i++)
-        {
-            if (!validChar(str[offset + i]))
-            {
-                offset += i;
-                goto start;
-            }
-            kmer <<= 2;
-            kmer &= mask;
-            kmer |= charToInt(str[offset + i]);
-            if (lastKmer != kmer || lastPos <= offset + i - realWindow)
-            {
-                emit(offset + i, kmer);
-                lastKmer = kmer;
-                lastPos = offset + i;
-            }
-        }
-    }
-}
-
 // MinimizerSeeder::addMinimizers + matchToSeedHit (MinimizerSeeder.cpp:493-519, 538-555)
 void selectSeeds(const HostGraph& g, const MinimizerIndex& idx, const std::string& seq, double density,
     std::vector<KmerMatch>& matches, std::vector<SeedHit>& out)

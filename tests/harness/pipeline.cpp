@@ -76,6 +76,81 @@ static std::vector<std::pair<std::string, std::string>> readFasta(const char* pa
     return r;
 }
 
+static inline bool validChar(char c)
+{
+    return c == 'a' || c == 'A' || c == 'c' || c == 'C' || c == 'g' || c == 'G' || c == 't' || c == 'T';
+}
+
+static inline uint64_t charToInt(char c)
+{
+    switch (c)
+    {
+        case 'a': case 'A': return 0;
+        case 'c': case 'C': return 1;
+        case 'g': case 'G': return 2;
+        case 't': case 'T': return 3;
+    }
+    return 0;
+}
+
+// iterateKmers + the lookup of MinimizerSeeder::getSeeds (MinimizerSeeder.cpp:59-102, 524-537): the
+// host restatement of the GPU k-mer lookup (seed_kernel.cu), for driving the host pipeline on the CPU
+static void kmerMatchesHost(const gahost::MinimizerIndex& idx, const std::string& str, std::vector<gahost::KmerMatch>& out)
+{
+    out.clear();
+    const size_t k = idx.k;
+    const size_t realWindow = idx.w - k + 1;
+    if (str.size() < k) return;
+    const uint64_t mask = ~(0xFFFFFFFFFFFFFFFFULL << (k * 2));
+    auto emit = [&](size_t pos, uint64_t kmer)
+    {
+        auto f = std::lower_bound(idx.keys.begin(), idx.keys.end(), kmer);
+        if (f == idx.keys.end() || *f != kmer) return;
+        size_t r = f - idx.keys.begin();
+        uint64_t start = idx.startPos[r];
+        uint64_t count = idx.startPos[r + 1] - start;
+        if (count >= idx.maxCount) return;
+        out.push_back(gahost::KmerMatch { pos, start, count });
+    };
+    size_t offset = 0;
+start:
+    while (offset < str.size() && !validChar(str[offset])) offset++;
+    if (offset + k > str.size()) return;
+    {
+        uint64_t kmer = 0;
+        for (size_t i = 0; i < k; i++)
+        {
+            if (!validChar(str[offset + i]))
+            {
+                offset += i;
+                goto start;
+            }
+            kmer <<= 2;
+            kmer |= charToInt(str[offset + i]);
+        }
+        emit(offset + k - 1, kmer);
+        uint64_t lastKmer = kmer;
+        size_t lastPos = offset + k - 1;
+        for (size_t i = k; offset + i < str.size(); i++)
+        {
+            if (!validChar(str[offset + i]))
+            {
+                offset += i;
+                goto start;
+            }
+            kmer <<= 2;
+            kmer &= mask;
+            kmer |= charToInt(str[offset + i]);
+            if (lastKmer != kmer || lastPos <= offset + i - realWindow)
+            {
+                emit(offset + i, kmer);
+                lastKmer = kmer;
+                lastPos = offset + i;
+            }
+        }
+    }
+}
+
 struct Ctx
 {
     ga_graph_desc* d;
@@ -182,7 +257,7 @@ int main(int argc, char** argv)
         std::vector<gahost::SeedHit> seeds;
         for (auto& r : reads)
         {
-            gahost::kmerMatchesHost(idx, r.second, km);
+            kmerMatchesHost(idx, r.second, km);
             gahost::selectSeeds(graph, idx, r.second, density, km, seeds);
             std::cout << "R " << r.first << " " << seeds.size();
             for (auto& s : seeds) std::cout << " " << s.nodeID << "," << s.nodeOffset << "," << s.seqPos << "," << s.matchLen << "," << s.reverse << "," << s.alignmentGraphNodeId << "," << s.alignmentGraphNodeOffset << "," << s.rawSeedGoodness;
@@ -212,7 +287,7 @@ int main(int argc, char** argv)
     {
         in[i].name = reads[i].first;
         in[i].seq = reads[i].second;
-        gahost::kmerMatchesHost(idx, in[i].seq, km);
+        kmerMatchesHost(idx, in[i].seq, km);
         gahost::selectSeeds(graph, idx, in[i].seq, dbg ? 5 : 10, km, in[i].seeds);
     }
     Ctx ctx { &hd.base, ga_extend_params { (uint32_t)bw, 14705, maxCells, 294 } };
