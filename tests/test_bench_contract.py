@@ -1,5 +1,5 @@
 """bench.py's reference arm runs on the host cores alone, so its JSON line (the
-contract the driver reads) is checked here without a GPU, on a small batch."""
+fields every bench.py line carries) is checked here without a GPU, on a small batch."""
 import json
 import os
 import subprocess
