@@ -41,6 +41,11 @@ def _vg_case(seed):
     return g.to_gfa(), dg.seed_extensions(reads, nl, 15, seed + 2, per_read=1)
 
 
+def _iupac_case(seed):
+    g, ext = _make_golden().iupac_edge_set(seed)
+    return g.to_gfa(), ext
+
+
 def _dbg_case(seed):
     genome = dg.make_repeat_genome(40_000, 6, 1_500, 0.01, 0.04, 10, tandem_len=(200, 800), seed=seed)
     d = dg.compact_dbg(genome, 63, with_positions=True)
@@ -58,13 +63,15 @@ CASES = [
     ("vg", 26, 1, 14705, UNLIMITED),
     ("vg", 27, 40, 14705, UNLIMITED),
     ("dbg", 28, 3, 14705, 500),
+    ("iupac", 29, 7, 3000, UNLIMITED),
+    ("iupac", 30, 12, 14705, UNLIMITED),
 ]
 
 
 @pytest.mark.parametrize("kind,seed,bandwidth,xdrop,max_cells", CASES)
 def test_oracle_matches_reference_on_generated_inputs(oracle_lib, kind, seed, bandwidth, xdrop, max_cells):
     mg = _make_golden()
-    gfa_text, ext = _vg_case(seed) if kind == "vg" else _dbg_case(seed)
+    gfa_text, ext = {"vg": _vg_case, "dbg": _dbg_case, "iupac": _iupac_case}[kind](seed)
     with tempfile.TemporaryDirectory() as td:
         gfa = os.path.join(td, "g.gfa")
         open(gfa, "w").write(gfa_text)
