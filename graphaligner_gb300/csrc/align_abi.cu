@@ -127,9 +127,11 @@ int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const u
     gadev::SeedTable table { a->slots, a->capacity, (uint32_t)std::min<uint64_t>(a->index.maxCount, 0xffffffffu) };
     ga_launch_seed_lookup(table, a->params.minimizer_length, a->params.minimizer_window, n, dSeq, dOff, dLen, dMatchOff, dMatch, dCount, a->stream);
     std::vector<uint32_t> counts(n);
-    std::vector<gadev::SeedMatch> matches(std::max<uint64_t>(matchSlots, 1));
+    // one slot per read base, of which only the first counts[i] of each read are read below:
+    // left uninitialised rather than zeroed (it is as large as 16 B per read base)
+    std::unique_ptr<gadev::SeedMatch[]> matches(new gadev::SeedMatch[std::max<uint64_t>(matchSlots, 1)]);
     cudaMemcpyAsync(counts.data(), dCount, n * 4ULL, cudaMemcpyDeviceToHost, a->stream);
-    cudaMemcpyAsync(matches.data(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
+    cudaMemcpyAsync(matches.get(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
     cudaError_t e = cudaStreamSynchronize(a->stream);
     if (e != cudaSuccess)
     {
