@@ -95,7 +95,7 @@ from test_read_pipeline_host import harness  # noqa: E402,F401  (the host read-l
 
 
 # (kind, seed, bandwidth): reads from freshly generated graphs, -x vg at the bandwidth or -x dbg
-READ_CASES = [("vg", 31, 10), ("vg", 32, 5), ("vg", 33, 15), ("dbg", 34, 5)]
+READ_CASES = [("vg", 31, 10), ("vg", 32, 5), ("vg", 33, 15), ("vg", 35, 3), ("vg", 36, 25), ("dbg", 34, 5), ("dbg", 37, 5)]
 
 
 @pytest.mark.parametrize("kind,seed,bandwidth", READ_CASES)
