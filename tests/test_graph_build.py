@@ -223,3 +223,15 @@ def test_native_builder_equals_the_restatement_on_random_gfas():
         text = _random_gfa(rng, numeric=k % 2 == 0)
         a, b = gg.build_from_gfa(text), gr.build_from_gfa(text)
         assert not _differing_fields(a, b), (k, _differing_fields(a, b), text)
+
+
+def test_gag_round_trip(tmp_path):
+    """save_gag then load_gag gives back every array of a built graph (the layout the
+    reference-graph dumper writes and the harness reads)."""
+    g = gg.build_from_gfa(HAND_GFA_NAMED)
+    path = os.path.join(tmp_path, "g.gag")
+    gg.save_gag(g, path)
+    assert not _differing_fields(gg.load_gag(path), g)
+    ref = load_graph("iupac20k")
+    gg.save_gag(ref, path)
+    assert not _differing_fields(gg.load_gag(path), ref)
