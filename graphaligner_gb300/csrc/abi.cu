@@ -85,29 +85,25 @@ struct ga_extender
     cudaStream_t copy[kCopyStreams] {};
     cudaEvent_t copyDone[kCopyStreams] {};
     int sms = 0;
-    ga_launch_shape shape {};             // how the longest-first order is cut into warp chunks
-    int block = 128;
-    gadev::Caps caps {};
-    uint8_t* workspace = nullptr;
+    ga_launch_shape shape {};             // warps per block, blocks per SM, first table layout, region size
+    uint8_t* workspace = nullptr;         // frontier tables of the global-memory layouts
     uint64_t workspaceBytes = 0;
     uint8_t* arena = nullptr;
     uint64_t arenaBytes = 0;
-    uint32_t* counters = nullptr;          // [0] fill work, [1] trace work, [2] status count
-    unsigned long long* arenaCursor = nullptr;
+    uint32_t* counters = nullptr;          // [0] work counter, [2] status count
+    unsigned long long* arenaCursor = nullptr;   // [0] overflow cursor, [1] bytes taken
     float lastFillMs = 0;
     float lastTraceMs = 0;
     float lastH2DMs = 0;                    // host-buffer copies of the last ga_extend_batch
     float lastD2HMs = 0;
     uint64_t lastArenaBytes = 0;
-    uint32_t lastDedicated = 0;             // single-lane chunks of the last batch
-    uint32_t lastChunks = 0;
     uint32_t lastLaunches = 0;
-    std::vector<uint32_t> chunkHost;
+    uint32_t lastRounds[3] {};              // extensions run in each layout by the last call
     std::vector<uint32_t> orderHost;      // processing order of the last host batch
     // host-batch staging
     DevBuf<uint8_t> seq;
     DevBuf<uint64_t> seqOff, traceOff, traceItems, cellSteps;
-    DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order, chunks;
+    DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order;
     DevBuf<int32_t> status, score, prevStatus;
 };
 
@@ -180,47 +176,38 @@ extern "C" int ga_graph_free(ga_graph_t g)
     return GA_OK;
 }
 
-// Default chunking of the longest-first order (chosen by timing launch shapes on the
-// 5 Mbp variation-graph batch; results do not depend on it): extensions of at least
-// twice the median length (and over 2 kbp) run one per warp, at most 12 per SM; the
-// rest run 16 per warp.
+// Default launch shape (results never depend on it): blocks of 4 warps, as many blocks per
+// SM as registers and shared memory allow, the frontier tables in shared memory first, and
+// a 128 KiB DP-table region per warp (the table of an extension of ~25 kbp at the band
+// sizes of variation graphs; longer ones continue in the shared overflow).
 static ga_launch_shape default_shape()
 {
     ga_launch_shape sh;
-    sh.single_factor = 2.0;
-    sh.single_min_bp = 2048;
-    sh.single_per_sm = 12;
-    sh.mid_factor = 1.0;
-    sh.mid_lanes = 16;
-    sh.bulk_lanes = 16;
+    sh.warps_per_block = 4;
+    sh.blocks_per_sm = 0;
+    sh.first_layout = 0;
+    sh.region_kib = 128;
     return sh;
 }
 
 static bool shape_ok(const ga_launch_shape& sh)
 {
-    return sh.single_factor > 0 && sh.mid_factor > 0 && sh.mid_lanes >= 1 && sh.mid_lanes <= 32 && sh.bulk_lanes >= 1 && sh.bulk_lanes <= 32;
+    return sh.warps_per_block >= 1 && sh.warps_per_block <= 4 && sh.first_layout <= 2 && sh.region_kib <= (1u << 20);
 }
 
-static gadev::Caps base_caps()
+// Frontier-table capacities of the three layouts: small tables in shared memory (a variation
+// graph's bands hold a handful of nodes), then larger ones in global memory for the
+// extensions that outgrew them (tangled de Bruijn graphs).
+static gadev::Caps layout_caps(int layout)
 {
     gadev::Caps c;
-    c.band = 64;
-    c.hash = 512;
-    c.heap = 128;
-    c.extras = 256;
+    if (layout == 0) { c.band = 32; c.hash = 64; c.heap = 32; c.extras = 64; }
+    else if (layout == 1) { c.band = 512; c.hash = 1024; c.heap = 512; c.extras = 1024; }
+    else { c.band = 16384; c.hash = 65536; c.heap = 16384; c.extras = 32768; }
     return c;
 }
 
-static gadev::Caps scaled_caps(int round)
-{
-    gadev::Caps c = base_caps();
-    uint32_t f = round == 0 ? 1 : (round == 1 ? 8 : 64);
-    c.band = std::min<uint32_t>(c.band * f, 16384);
-    c.hash = std::min<uint32_t>(c.hash * f, 65536);
-    c.heap = std::min<uint32_t>(c.heap * f, 16384);
-    c.extras = std::min<uint32_t>(c.extras * f, 32768);
-    return c;
-}
+static const char* kShapeError = "launch shape: warps_per_block within 1..4, first_layout within 0..2, region_kib at most 2^20";
 
 extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out)
 {
@@ -231,12 +218,9 @@ extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_ext
     cudaDeviceProp prop;
     GA_CUDA(cudaGetDeviceProperties(&prop, graph->device));
     x->sms = prop.multiProcessorCount;
-    x->caps = base_caps();
     x->shape = default_shape();
-    int occ = std::max(1, ga_extend_occupancy(x->block));
-    uint64_t slots = (uint64_t)x->sms * occ * x->block;
-    uint64_t stride = ga_workspace_bytes(x->caps);
-    x->workspaceBytes = slots * stride;
+    // the global-memory layouts' tables: room for a few thousand warps of the medium layout
+    x->workspaceBytes = 256ULL << 20;
     GA_CUDA(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking));
     for (int k = 0; k < ga_extender::kCopyStreams; k++)
     {
@@ -246,13 +230,12 @@ extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_ext
     for (auto& e : x->ev) GA_CUDA(cudaEventCreate(&e));
     cudaError_t e = cudaMalloc((void**)&x->workspace, x->workspaceBytes);
     if (e != cudaSuccess) { delete x; return cuda_fail(e, "workspace"); }
-    GA_CUDA(cudaMemset(x->workspace, 0, x->workspaceBytes));
     if (arena_bytes == 0) arena_bytes = 4ULL << 30;
     x->arenaBytes = arena_bytes;
     e = cudaMalloc((void**)&x->arena, x->arenaBytes);
     if (e != cudaSuccess) { cudaFree(x->workspace); delete x; return cuda_fail(e, "arena"); }
     GA_CUDA(cudaMalloc((void**)&x->counters, 16 * sizeof(uint32_t)));
-    GA_CUDA(cudaMalloc((void**)&x->arenaCursor, sizeof(unsigned long long)));
+    GA_CUDA(cudaMalloc((void**)&x->arenaCursor, 2 * sizeof(unsigned long long)));
     *out = x;
     return GA_OK;
 }
@@ -276,7 +259,7 @@ extern "C" int ga_extender_free(ga_extender_t x)
     cudaFree(x->arenaCursor);
     x->seq.release(); x->seqOff.release(); x->traceOff.release(); x->traceItems.release(); x->cellSteps.release();
     x->seqLen.release(); x->startNode.release(); x->startOffset.release(); x->traceCap.release(); x->traceLen.release();
-    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release(); x->chunks.release();
+    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
     for (int k = 0; k < ga_extender::kCopyStreams; k++)
@@ -289,9 +272,10 @@ extern "C" int ga_extender_free(ga_extender_t x)
 }
 
 // Runs one batch whose buffers are all on the device.  order: processing order
-// (longest first); lengths: host copy of the sequence lengths.
+// (longest first).  Extensions that outgrow a layout's tables (GA_CAPACITY) run again
+// in the next, larger layout; only those run.
 static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend_batch_desc* b, ga_extend_results* r,
-    const uint32_t* order, const std::vector<uint32_t>& sortedLen, int32_t* prevStatus, cudaStream_t stream)
+    const uint32_t* order, int32_t* prevStatus, cudaStream_t stream)
 {
     gadev::FillArgs fa {};
     fa.g = x->graph->d;
@@ -309,13 +293,10 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     fa.arena = x->arena;
     fa.arenaBytes = x->arenaBytes;
     fa.arenaCursor = x->arenaCursor;
-    fa.workspace = x->workspace;
 
     gadev::TraceArgs ta {};
     ta.g = x->graph->d;
     ta.cost = p->xscore_error_cost;
-    ta.num = b->num;
-    ta.order = order;
     ta.seq = b->seq;
     ta.seqOff = b->seq_offset;
     ta.seqLen = b->seq_len;
@@ -329,78 +310,61 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     ta.cellSteps = r->cell_steps;
 
     const uint32_t n = b->num;
-    if (n >= (1u << 26)) return fail(GA_ERR_ARGUMENT, "at most 2^26 - 1 extensions per batch");
     x->lastFillMs = 0;
     x->lastTraceMs = 0;
     x->lastLaunches = 0;
-    for (int round = 0; round < 3; round++)
+    for (int k = 0; k < 3; k++) x->lastRounds[k] = 0;
+    const ga_launch_shape& sh = x->shape;
+    const int wpb = (int)sh.warps_per_block;
+    uint32_t pending = n;                    // extensions the next round runs
+    for (int layout = (int)sh.first_layout; layout < 3; layout++)
     {
-        gadev::Caps caps = scaled_caps(round);
-        uint64_t stride = ga_workspace_bytes(caps);
-        uint64_t slots = x->workspaceBytes / stride;
-        if (round > 0)
+        const bool shared = layout == 0;
+        const gadev::Caps caps = layout_caps(layout);
+        const uint64_t stride = ga_warp_tables_bytes(caps);
+        int blocksPerSm = ga_extend_blocks_per_sm(wpb, caps, shared);
+        if (blocksPerSm <= 0) return fail(GA_ERR_CUDA, "the extension kernel does not fit an SM with this launch shape");
+        if (sh.blocks_per_sm > 0) blocksPerSm = std::min<int>(blocksPerSm, (int)sh.blocks_per_sm);
+        uint64_t warps = (uint64_t)x->sms * blocksPerSm * wpb;
+        if (!shared) warps = std::min<uint64_t>(warps, x->workspaceBytes / stride);
+        warps = std::min<uint64_t>(warps, ((uint64_t)pending + wpb - 1) / wpb * wpb);
+        warps = std::max<uint64_t>(warps / wpb, 1) * wpb;
+        const uint64_t blocks = warps / wpb;
+        // per-warp regions take at most half the arena; the rest is the shared overflow
+        uint64_t region = (uint64_t)sh.region_kib << 10;
+        region = std::min<uint64_t>(region, x->arenaBytes / 2 / warps) & ~15ULL;
+        if (layout > (int)sh.first_layout)
         {
             // only extensions that ran out of a capacity in the previous round run again
             GA_CUDA(cudaMemcpyAsync(prevStatus, r->status, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream));
-            // the workspace tables are laid out for other capacities: clear their stamps
-            GA_CUDA(cudaMemsetAsync(x->workspace, 0, x->workspaceBytes, stream));
         }
         fa.caps = caps;
+        fa.workspace = shared ? nullptr : x->workspace;
         fa.workspaceStride = stride;
-        fa.prevStatus = round > 0 ? prevStatus : nullptr;
-        ta.prevStatus = fa.prevStatus;
-        // chunk table over the longest-first order: (first position << 6) | (size - 1)
-        auto& ch = x->chunkHost;
-        ch.clear();
-        uint32_t pos = 0, singles = 0;
-        auto emit = [&](uint32_t size) { ch.push_back((pos << 6) | (size - 1)); pos += size; };
-        if (round == 0 && n > 0)
-        {
-            const ga_launch_shape& sh = x->shape;
-            const double median = sortedLen[n / 2];
-            const uint64_t maxSingles = (uint64_t)x->sms * sh.single_per_sm;
-            while (pos < n && singles < maxSingles && sortedLen[pos] >= sh.single_factor * median && sortedLen[pos] > sh.single_min_bp)
-            {
-                emit(1);
-                singles++;
-            }
-            while (pos < n && sortedLen[pos] >= sh.mid_factor * median) emit(std::min(sh.mid_lanes, n - pos));
-            while (pos < n) emit(std::min(sh.bulk_lanes, n - pos));
-        }
-        else
-        {
-            while (pos < n) emit(std::min(32u, n - pos));
-        }
-        const uint32_t numChunks = (uint32_t)ch.size();
-        GA_CUDA(x->chunks.reserve(std::max<uint32_t>(numChunks, 1)));
-        GA_CUDA(cudaMemcpyAsync(x->chunks.ptr, ch.data(), (size_t)numChunks * 4, cudaMemcpyHostToDevice, stream));
-        // every thread owns one workspace slot; a warp works one chunk at a time
-        if (slots < (uint64_t)x->block) return fail(GA_ERR_CUDA, "workspace too small for the batch's capacities");
-        const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(slots / x->block, ((uint64_t)numChunks * 32 + x->block - 1) / x->block));
+        fa.regionBytes = region;
+        fa.overflowBase = warps * region;
+        fa.prevStatus = layout > (int)sh.first_layout ? prevStatus : nullptr;
         GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), stream));
-        GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, sizeof(unsigned long long), stream));
+        GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, 2 * sizeof(unsigned long long), stream));
         GA_CUDA(cudaEventRecord(x->ev[0], stream));
-        ga_launch_extend(fa, ta, x->chunks.ptr, numChunks, x->counters, 0, (uint32_t)((uint64_t)grid * x->block), grid, x->block, stream);
-        GA_CUDA(cudaGetLastError());
+        if (ga_launch_extend(fa, ta, x->counters, (int)blocks, wpb, stream) != 0)
+            return fail(GA_ERR_CUDA, std::string("extension kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
         x->lastLaunches += 1;
+        x->lastRounds[layout] = pending;
         GA_CUDA(cudaEventRecord(x->ev[1], stream));
         count_status_kernel<<<64, 256, 0, stream>>>(r->status, n, GA_CAPACITY, x->counters + 2);
         GA_CUDA(cudaGetLastError());
         x->lastLaunches += 1;
         uint32_t capFails = 0;
-        unsigned long long arenaUsed = 0;
+        unsigned long long used[2] = {0, 0};
         GA_CUDA(cudaMemcpyAsync(&capFails, x->counters + 2, 4, cudaMemcpyDeviceToHost, stream));
-        GA_CUDA(cudaMemcpyAsync(&arenaUsed, x->arenaCursor, 8, cudaMemcpyDeviceToHost, stream));
+        GA_CUDA(cudaMemcpyAsync(used, x->arenaCursor, 16, cudaMemcpyDeviceToHost, stream));
         GA_CUDA(cudaStreamSynchronize(stream));
-        if (round == 0)
-        {
-            x->lastArenaBytes = std::min<uint64_t>(arenaUsed, x->arenaBytes);
-            x->lastDedicated = singles;
-            x->lastChunks = numChunks;
-        }
+        if (layout == (int)sh.first_layout) x->lastArenaBytes = used[1];
         float ms = 0;
         GA_CUDA(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
         x->lastFillMs += ms;
+        pending = capFails;
         if (capFails == 0) break;
     }
     return GA_OK;
@@ -426,9 +390,9 @@ static std::vector<uint32_t> longest_first(const uint32_t* len, uint32_t n)
 }
 
 // Copies a host batch into the extender's device buffers and points db/dr at them.
-// sortedLen: the lengths in processing order; items: trace items the batch spans.
+// items: trace items the batch spans.
 static int stage_host_batch(ga_extender* x, const ga_extend_batch_desc* b, ga_extend_batch_desc* db,
-    ga_extend_results* dr, std::vector<uint32_t>& sortedLen, uint64_t* itemsOut)
+    ga_extend_results* dr, uint64_t* itemsOut)
 {
     const uint32_t n = b->num;
     int rc = check_lengths(b->seq_len, n);
@@ -441,8 +405,6 @@ static int stage_host_batch(ga_extender* x, const ga_extend_batch_desc* b, ga_ex
     }
     std::vector<uint32_t>& order = x->orderHost;   // kept until the next batch: the copy below is asynchronous
     order = longest_first(b->seq_len, n);
-    sortedLen.resize(n);
-    for (uint32_t i = 0; i < n; i++) sortedLen[i] = b->seq_len[order[i]];
     GA_CUDA(x->seq.reserve(seqBytes));
     GA_CUDA(x->seqOff.reserve(n));
     GA_CUDA(x->seqLen.reserve(n));
@@ -494,12 +456,11 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
     if (n == 0) return GA_OK;
     ga_extend_batch_desc db;
     ga_extend_results dr;
-    std::vector<uint32_t> sortedLen;
     uint64_t items = 0;
-    int rc = stage_host_batch(x, b, &db, &dr, sortedLen, &items);
+    int rc = stage_host_batch(x, b, &db, &dr, &items);
     if (rc != GA_OK) return rc;
     cudaStream_t s = x->stream;
-    rc = run_device(x, p, &db, &dr, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
+    rc = run_device(x, p, &db, &dr, x->order.ptr, x->prevStatus.ptr, s);
     if (rc != GA_OK) return rc;
     GA_CUDA(cudaMemcpyAsync(r->status, dr.status, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->score, dr.score, n * 4ULL, cudaMemcpyDeviceToHost, s));
@@ -530,7 +491,7 @@ extern "C" int ga_extender_autotune(ga_extender_t x, const ga_extend_params* p, 
     if (!x || !p || !b || !shapes) return fail(GA_ERR_ARGUMENT, "null argument");
     if (count == 0) return fail(GA_ERR_ARGUMENT, "no launch shapes");
     for (uint32_t i = 0; i < count; i++)
-        if (!shape_ok(shapes[i])) return fail(GA_ERR_ARGUMENT, "launch shape: factors must be positive and lane counts within 1..32");
+        if (!shape_ok(shapes[i])) return fail(GA_ERR_ARGUMENT, kShapeError);
     GA_CUDA(cudaSetDevice(x->graph->device));
     x->lastH2DMs = x->lastD2HMs = 0;
     const uint32_t n = b->num;
@@ -538,9 +499,8 @@ extern "C" int ga_extender_autotune(ga_extender_t x, const ga_extend_params* p, 
     repeats = std::max<uint32_t>(repeats, 1);
     ga_extend_batch_desc db;
     ga_extend_results dr;
-    std::vector<uint32_t> sortedLen;
     uint64_t items = 0;
-    int rc = stage_host_batch(x, b, &db, &dr, sortedLen, &items);
+    int rc = stage_host_batch(x, b, &db, &dr, &items);
     if (rc != GA_OK) return rc;
     cudaStream_t s = x->stream;
     std::vector<int32_t> refStatus(n), refScore(n), status(n), score(n);
@@ -552,7 +512,7 @@ extern "C" int ga_extender_autotune(ga_extender_t x, const ga_extend_params* p, 
         std::vector<float> ms;
         for (uint32_t rep = 0; rep < repeats; rep++)
         {
-            rc = run_device(x, p, &db, &dr, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
+            rc = run_device(x, p, &db, &dr, x->order.ptr, x->prevStatus.ptr, s);
             if (rc != GA_OK) return rc;
             ms.push_back(x->lastFillMs);
         }
@@ -591,12 +551,10 @@ extern "C" int ga_extend_batch_device(ga_extender_t x, const ga_extend_params* p
     int rc = check_lengths(len.data(), n);
     if (rc != GA_OK) return rc;
     std::vector<uint32_t> order = longest_first(len.data(), n);
-    std::vector<uint32_t> sortedLen(n);
-    for (uint32_t i = 0; i < n; i++) sortedLen[i] = len[order[i]];
     GA_CUDA(x->order.reserve(n));
     GA_CUDA(x->prevStatus.reserve(n));
     GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
-    return run_device(x, p, b, r, x->order.ptr, sortedLen, x->prevStatus.ptr, s);
+    return run_device(x, p, b, r, x->order.ptr, x->prevStatus.ptr, s);
 }
 
 extern "C" int ga_extender_last_kernel_ms(ga_extender_t x, float* ms)
@@ -632,7 +590,7 @@ extern "C" int ga_extender_last_launches(ga_extender_t x, uint32_t* launches)
 extern "C" int ga_extender_set_launch_shape(ga_extender_t x, const ga_launch_shape* shape)
 {
     if (!x || !shape) return fail(GA_ERR_ARGUMENT, "null argument");
-    if (!shape_ok(*shape)) return fail(GA_ERR_ARGUMENT, "launch shape: factors must be positive and lane counts within 1..32");
+    if (!shape_ok(*shape)) return fail(GA_ERR_ARGUMENT, kShapeError);
     x->shape = *shape;
     return GA_OK;
 }
@@ -648,6 +606,13 @@ extern "C" int ga_extender_last_arena_bytes(ga_extender_t x, uint64_t* bytes)
 {
     if (!x || !bytes) return fail(GA_ERR_ARGUMENT, "null argument");
     *bytes = x->lastArenaBytes;
+    return GA_OK;
+}
+
+extern "C" int ga_extender_last_layout_counts(ga_extender_t x, uint32_t counts[3])
+{
+    if (!x || !counts) return fail(GA_ERR_ARGUMENT, "null argument");
+    for (int k = 0; k < 3; k++) counts[k] = x->lastRounds[k];
     return GA_OK;
 }
 

@@ -1,14 +1,32 @@
-// Batched seed extension on GB300: fill kernel (banded Myers DP over the graph
-// with the component-ordered frontier and X-drop) and traceback kernel.
+// Batched seed extension on GB300: one warp per extension.
 //
-// Work decomposition: one thread owns one extension at a time.  The DP of one
-// extension is a strictly sequential chain (each 64-row slice depends on the
-// previous one; inside a slice nodes are computed one at a time in frontier
-// order, and the admission test uses the running minimum), so the parallelism
-// is across extensions.  Both kernels are persistent: a thread takes the next
-// extension from a device work counter over a longest-first order, so short
-// extensions fill in behind long ones.  The fill streams every committed slice
-// into a batch arena in HBM; the traceback kernel walks it back.
+// A warp owns one extension at a time: the fill (banded Myers DP over the graph
+// with the component-ordered frontier and X-drop) and then the traceback.  The
+// DP of one extension is a sequential chain: each 64-row slice depends on the
+// whole band of the previous one, and inside a slice nodes are computed one at
+// a time in frontier order, the admission test using the running minimum.  So
+// the warp runs that control flow warp-uniformly (every lane holds the same
+// scalars, branches never diverge) and spreads over its lanes the work that is
+// parallel inside it:
+//   - the match masks of a slice (lane k reads rows k and k + 32; ballots),
+//   - the match mask of every column of a node, before its column loop,
+//   - per node: the X-score of every column (lane k scores columns k and k + 32),
+//     the minimum and its first column (reduce + ballot) and the bottom-row
+//     horizontal deltas (ballots), so the column loop itself only runs the
+//     Myers recurrence,
+//   - node-table lookups: 32 probes of the open-addressing table per step (ballot),
+//   - committing a slice to the DP table (coalesced copies),
+//   - the traceback's end-cell choice (slices and columns across lanes) and its
+//     band lookups (ballot over the slice's node ids),
+//   - trace output, staged in shared memory and written 32 items at a time.
+// The frontier tables (two bands, two node tables, the heap, the pending incoming
+// columns) and the node's recorded columns live in shared memory; an extension
+// that outgrows them is re-run with larger tables in global memory.  Each warp
+// writes its DP table into its own arena region, reused extension after
+// extension, so the table the traceback reads was written moments before and
+// stays in L2.
+//
+// Warps take extensions from a device counter over a longest-first order.
 //
 // Reference correspondence (GraphAligner src/):
 //   fill_extension   getReverseTraceFromSeed / getXdropSlices  (GraphAlignerBitvectorBanded.h:59-76, 580-725)
@@ -16,7 +34,7 @@
 //   node_calc<Fill>  calculateNodeInner                        (GraphAlignerBitvectorCommon.h:1113-1478)
 //   trace_extension  getReverseTraceFromTableExactEndPos / getReverseTraceFromTable
 //                                                              (GraphAlignerBitvectorCommon.h:496-758)
-//   bt_*             pickBacktraceInside/HorizontalCrossing/VerticalCrossing/Corner (:770-1054)
+//   bt_corner etc.   pickBacktraceInside/HorizontalCrossing/VerticalCrossing/Corner (:770-1054)
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "extend.cuh"
@@ -25,16 +43,9 @@
 namespace gadev
 {
 
-struct HSlot
-{
-    u32 node;
-    u32 gen;
-    int16_t band;       // index in the slice's band, -1 until the node is first popped
-    uint16_t active;    // node has a heap entry (ComponentPriorityQueue::active)
-    uint16_t head;      // pending incoming edges (ComponentPriorityQueue::extras), FIFO
-    uint16_t tail;
-};
+static constexpr unsigned kFull = 0xffffffffu;
 
+// a pending incoming column of a node (ComponentPriorityQueue::extras entry)
 struct Extra
 {
     u64 VP, VN;
@@ -45,73 +56,128 @@ struct Extra
 
 static constexpr uint16_t kNil = 0xffff;
 
+// node-table slot value: where the node sits in the slice's band and its queue state
+struct NodeVal
+{
+    int16_t band;       // index in the slice's band, -1 until the node is first popped
+    uint16_t active;    // node has a heap entry (ComponentPriorityQueue::active)
+    uint16_t head;      // pending incoming columns, FIFO
+    uint16_t tail;
+};
+
+// one recorded column of a node-slice: the fill's epilogue and the traceback read these
+struct __align__(16) Col
+{
+    u64 VP, VN;
+    u64 Mh;             // horizontal -1 deltas of the step (the X-score's candidate mask)
+    i32 end;
+    u32 phTop;          // horizontal +1 delta out of the last row
+};
+
 __device__ __forceinline__ u32 hash_node(u32 node)
 {
     u32 h = node * 0x9E3779B1u;
     return h ^ (h >> 15);
 }
 
-struct Workspace
+// One warp's tables.  A node-table key is (generation << 32) | node; a slot whose
+// generation is not the slice's is empty, so tables are never cleared between slices.
+struct WSpace
 {
     Item* band[2];
-    HSlot* hash[2];
+    u64* key[2];
+    NodeVal* val[2];
     HeapItem* heap;
     Extra* extras;
-    u32* header;
+    Col* cols;          // [64]
+    u64* eqcol;         // [64] match mask of each column of the current node
+    u64* ring;          // [64] trace items not yet written out
 };
 
 __host__ __device__ inline u64 align16(u64 x) { return (x + 15) & ~15ULL; }
 
-__device__ __forceinline__ Workspace workspace_at(uint8_t* base, const Caps& c)
+__host__ __device__ inline u64 wspace_bytes(const Caps& c)
 {
-    Workspace w;
-    u64 off = 16;
-    w.header = (u32*)base;
+    u64 b = 0;
+    b += 2 * align16((u64)c.band * sizeof(Item));
+    b += 2 * align16((u64)c.hash * 8);
+    b += 2 * align16((u64)c.hash * sizeof(NodeVal));
+    b += align16((u64)c.heap * sizeof(HeapItem));
+    b += align16((u64)c.extras * sizeof(Extra));
+    b += 64 * sizeof(Col) + 64 * 8 + 64 * 8;
+    return align16(b);
+}
+
+__device__ __forceinline__ WSpace wspace_at(uint8_t* base, const Caps& c)
+{
+    WSpace w;
+    u64 off = 0;
     w.band[0] = (Item*)(base + off); off += align16((u64)c.band * sizeof(Item));
     w.band[1] = (Item*)(base + off); off += align16((u64)c.band * sizeof(Item));
-    w.hash[0] = (HSlot*)(base + off); off += align16((u64)c.hash * sizeof(HSlot));
-    w.hash[1] = (HSlot*)(base + off); off += align16((u64)c.hash * sizeof(HSlot));
+    w.key[0] = (u64*)(base + off); off += align16((u64)c.hash * 8);
+    w.key[1] = (u64*)(base + off); off += align16((u64)c.hash * 8);
+    w.val[0] = (NodeVal*)(base + off); off += align16((u64)c.hash * sizeof(NodeVal));
+    w.val[1] = (NodeVal*)(base + off); off += align16((u64)c.hash * sizeof(NodeVal));
     w.heap = (HeapItem*)(base + off); off += align16((u64)c.heap * sizeof(HeapItem));
-    w.extras = (Extra*)(base + off);
+    w.extras = (Extra*)(base + off); off += align16((u64)c.extras * sizeof(Extra));
+    w.cols = (Col*)(base + off); off += 64 * sizeof(Col);
+    w.eqcol = (u64*)(base + off); off += 64 * 8;
+    w.ring = (u64*)(base + off);
     return w;
 }
 
-// returns the slot for node in a generation-stamped table, or nullptr
-__device__ __forceinline__ HSlot* hash_find(HSlot* t, u32 cap, u32 gen, u32 node)
+// Node-table lookup with 32 linear probes per step (lane k probes the k-th slot of the
+// step); the first slot in probe order that is the node's or empty ends the probe.
+// Returns the node's slot or -1.  Every lane gets the same answer.
+__device__ __forceinline__ int tbl_find(const u64* key, u32 cap, u32 gen, u32 node, u32 lane)
 {
-    u32 h = hash_node(node) & (cap - 1);
-    for (u32 probe = 0; probe < cap; probe++)
+    const u32 h = hash_node(node);
+    const u64 want = ((u64)gen << 32) | node;
+    for (u32 base = 0; base < cap; base += 32)
     {
-        HSlot* s = &t[h];
-        if (s->gen != gen) return nullptr;
-        if (s->node == node) return s;
-        h = (h + 1) & (cap - 1);
+        const u32 slot = (h + base + lane) & (cap - 1);
+        const u64 k = key[slot];
+        const u32 hit = __ballot_sync(kFull, k == want);
+        const u32 stop = hit | __ballot_sync(kFull, (u32)(k >> 32) != gen);
+        if (stop)
+        {
+            const u32 first = __ffs((int)stop) - 1;
+            return ((hit >> first) & 1) ? (int)((h + base + first) & (cap - 1)) : -1;
+        }
     }
-    return nullptr;
+    return -1;
 }
 
-__device__ __forceinline__ HSlot* hash_get_or_add(HSlot* t, u32 cap, u32 gen, u32 node, u32& used)
+// the node's slot, claimed (band -1, inactive, no pending columns) if it has none;
+// -1 when the table would pass half full
+__device__ __forceinline__ int tbl_get_or_add(u64* key, NodeVal* val, u32 cap, u32 gen, u32 node, u32& used, u32 lane)
 {
-    u32 h = hash_node(node) & (cap - 1);
-    for (u32 probe = 0; probe < cap; probe++)
+    const u32 h = hash_node(node);
+    const u64 want = ((u64)gen << 32) | node;
+    for (u32 base = 0; base < cap; base += 32)
     {
-        HSlot* s = &t[h];
-        if (s->gen != gen)
+        const u32 slot = (h + base + lane) & (cap - 1);
+        const u64 k = key[slot];
+        const u32 hit = __ballot_sync(kFull, k == want);
+        const u32 stop = hit | __ballot_sync(kFull, (u32)(k >> 32) != gen);
+        if (stop)
         {
-            if (2 * (used + 1) > cap) return nullptr;
+            const u32 first = __ffs((int)stop) - 1;
+            const u32 s = (h + base + first) & (cap - 1);
+            if ((hit >> first) & 1) return (int)s;
+            if (2 * (used + 1) > cap) return -1;
             used++;
-            s->gen = gen;
-            s->node = node;
-            s->band = -1;
-            s->active = 0;
-            s->head = kNil;
-            s->tail = kNil;
-            return s;
+            key[s] = want;
+            NodeVal v;
+            v.band = -1;
+            v.active = 0;
+            v.head = kNil;
+            v.tail = kNil;
+            val[s] = v;
+            return (int)s;
         }
-        if (s->node == node) return s;
-        h = (h + 1) & (cap - 1);
     }
-    return nullptr;
+    return -1;
 }
 
 // IUPAC membership of every byte value (bit0 A, bit1 C, bit2 G, bit3 T; 0 = '-',
@@ -128,46 +194,29 @@ __device__ __forceinline__ void load_iupac_table()
     __syncthreads();
 }
 
-__device__ __forceinline__ void eq_add(EqV4& eq, int m, u32 r, bool full, bool& ok)
+// Match masks of the 64 rows starting at read position j (getEqVector, Common.h:279-318):
+// lane k reads rows k and k + 32 and the masks come from ballots.  False when a row holds
+// a non-sequence byte, or a gap inside a full 64-row window (the reference asserts).
+__device__ __forceinline__ bool eq_vector(const uint8_t* seq, u32 len, int64_t j, EqV4& eq, u32 lane)
 {
-    // a non-sequence byte always fails; a gap fails only inside a full 64-row window
-    ok &= !(m < 0 || (m == 0 && full));
-    const u64 bit = 1ULL << r;
-    eq.a |= (m & 1) ? bit : 0;
-    eq.c |= (m & 2) ? bit : 0;
-    eq.g |= (m & 4) ? bit : 0;
-    eq.t |= (m & 8) ? bit : 0;
-}
-
-// match masks of the 64 rows starting at read position j (getEqVector, Common.h:279-318).
-// When the window and 3 bytes either side lie inside the read, it is read as aligned
-// 32-bit words (every word then lies inside the read); otherwise byte by byte.
-__device__ __forceinline__ bool eq_vector(const uint8_t* seq, u32 len, int64_t j, EqV4& eq)
-{
-    eq.a = eq.c = eq.g = eq.t = 0;
-    bool ok = true;
     const bool full = j + 64 <= (int64_t)len;
-    if (j >= 3 && j + 64 + 3 <= (int64_t)len)
+    int m0 = 0, m1 = 0;
+    bool bad = false;
+    if (j + lane < (int64_t)len)
     {
-        const uint8_t* p = seq + j;
-        const u32 shift = (u32)((uintptr_t)p & 3) * 8;
-        const u32* w = (const u32*)((uintptr_t)p & ~(uintptr_t)3);
-        u32 lo = w[0];
-#pragma unroll
-        for (u32 k = 0; k < 16; k++)
-        {
-            const u32 hi = w[k + 1];
-            const u32 word = __funnelshift_r(lo, hi, shift);
-            lo = hi;
-#pragma unroll
-            for (u32 b = 0; b < 4; b++) eq_add(eq, s_iupac[(word >> (8 * b)) & 0xff], k * 4 + b, full, ok);
-        }
-        return ok;
+        m0 = s_iupac[seq[j + lane]];
+        bad |= m0 < 0 || (m0 == 0 && full);
     }
-    const int64_t rem = (int64_t)len - j;
-    const u32 n = rem >= 64 ? 64u : (rem > 0 ? (u32)rem : 0u);
-    for (u32 r = 0; r < n; r++) eq_add(eq, s_iupac[seq[j + r]], r, full, ok);
-    return ok;
+    if (j + lane + 32 < (int64_t)len)
+    {
+        m1 = s_iupac[seq[j + lane + 32]];
+        bad |= m1 < 0 || (m1 == 0 && full);
+    }
+    eq.a = (u64)__ballot_sync(kFull, m0 & 1) | ((u64)__ballot_sync(kFull, m1 & 1) << 32);
+    eq.c = (u64)__ballot_sync(kFull, m0 & 2) | ((u64)__ballot_sync(kFull, m1 & 2) << 32);
+    eq.g = (u64)__ballot_sync(kFull, m0 & 4) | ((u64)__ballot_sync(kFull, m1 & 4) << 32);
+    eq.t = (u64)__ballot_sync(kFull, m0 & 8) | ((u64)__ballot_sync(kFull, m1 & 8) << 32);
+    return __ballot_sync(kFull, bad) == 0;
 }
 
 // graph character of node n at pos (AlignmentGraph::NodeSequences) as an IUPAC mask
@@ -209,9 +258,6 @@ struct PrevInfo
     u64 HP, HN;
 };
 
-// calculateNodeInner (Common.h:1113-1478) with the single-seed fake extra slice.
-// Fill = true: the slice fill (early leave allowed, calculateNodeClipPrecise).
-// Fill = false: recalcNodeWordslice (no early leave, every column written to cols).
 // An upper bound of ws_max_xscore(w, seqOffset, cost, 64, mask): every candidate row m scores
 // 100 (m + 1) - cost s(m) with s(m) >= -popc(VN), plus 100 seqOffset - cost before.
 __device__ __forceinline__ int64_t xscore_bound(const WS& w, i32 seqOffset, i32 cost)
@@ -225,14 +271,16 @@ __device__ __forceinline__ int64_t xscore_bound(const WS& w, i32 seqOffset, i32 
 // above also bounds the reference's (wrapping) arithmetic.
 static constexpr i32 kXBoundOffsetLimit = 10000000;
 
+// calculateNodeInner (Common.h:1113-1478) with the single-seed fake extra slice.
+// Fill = true: the slice fill (early leave allowed, calculateNodeClipPrecise).
+// Fill = false: recalcNodeWordslice (no early leave); columns 0..lastColumn land in cols.
+// The column loop runs the Myers recurrence warp-uniformly and records every column; the
+// per-column minimum, X-score and horizontal output bits are then taken across the lanes.
 template <bool Fill>
 __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const EqV4& eqv, const PrevInfo& prev,
-    const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, WS* cols, u64& steps, int& err,
-    i32 sliceMaxX = kIntMin, u32 lastColumn = 63)
+    const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, Col* cols, u64* eqcol,
+    u64& steps, int& err, u32 lane, i32 sliceMaxX = kIntMin, u32 lastColumn = 63)
 {
-    // The slice keeps the first node of strictly greatest X-score and the node keeps its
-    // greatest column, so a column whose bound is at most max(slice so far, node so far)
-    // changes neither: its exact X-score is skipped.
     const bool boundOk = seqOffset < kXBoundOffsetLimit;
     NodeCalc result;
     result.minScore = kIntMax;
@@ -254,9 +302,17 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
         const u64* a = g.seqAmb + (u64)(i - g.firstAmbiguous) * 4;
         a0 = a[0]; a1 = a[1]; a2 = a[2]; a3 = a[3];
     }
-    u64 eq0;
-    if (!amb) eq0 = eq_pick(eqv, (u32)(c0 & 3));
-    else eq0 = eq_amb(eqv, (u32)((a0 & 1) | ((a1 & 1) << 1) | ((a2 & 1) << 2) | ((a3 & 1) << 3)));
+    // the match mask of every column (lane k: columns k and k + 32)
+    __syncwarp();
+    for (u32 pos = lane; pos < nodeLength; pos += 32)
+    {
+        u64 e;
+        if (!amb) e = eq_pick(eqv, (u32)(((pos < 32 ? c0 : c1) >> ((pos & 31) * 2)) & 3));
+        else e = eq_amb(eqv, (u32)(((a0 >> pos) & 1) | (((a1 >> pos) & 1) << 1) | (((a2 >> pos) & 1) << 2) | (((a3 >> pos) & 1) << 3)));
+        eqcol[pos] = e;
+    }
+    __syncwarp();
+    const u64 eq0 = eqcol[0];
 
     WS ws = ws_make(0, 0, 0);
     bool hasWs = false;
@@ -397,48 +453,86 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
     slice.sVN = ws.VN;
     slice.sEnd = ws.end;
     slice.node = i | kExists;
-    if (!Fill) cols[0] = ws;
+    if (!Fill)
+    {
+        cols[0].VP = ws.VP;
+        cols[0].VN = ws.VN;
+        cols[0].end = ws.end;
+    }
     const u64 forceEq = prev.exists ? kAllOnes : (kAllOnes ^ 1);
-    u64 outHP = 0, outHN = 0;
-    u32 pos = 1;
     // the traceback's recomputation stops at the column it needs last
     const u32 columns = Fill ? nodeLength : (lastColumn + 1 < nodeLength ? lastColumn + 1 : nodeLength);
-    for (; pos < columns; pos++)
+    u64 hp = fixedHP >> 1, hn = fixedHN >> 1, fm = forceMask >> 1;   // bit 0: column 1
+    for (u32 pos = 1; pos < columns; pos++)
     {
-        u64 eq;
-        if (!amb)
-        {
-            u64 chunk = pos < 32 ? c0 : c1;
-            eq = eq_pick(eqv, (u32)((chunk >> ((pos & 31) * 2)) & 3));
-        }
-        else
-        {
-            eq = eq_amb(eqv, (u32)(((a0 >> pos) & 1) | (((a1 >> pos) & 1) << 1) | (((a2 >> pos) & 1) << 2) | (((a3 >> pos) & 1) << 3)));
-        }
-        eq &= forceEq;
+        const u64 eq = eqcol[pos] & forceEq;
         u64 Ph, Mh;
-        WS nw = myers_step(eq, ws, (fixedHP >> pos) & 1, (fixedHN >> pos) & 1, Ph, Mh);
-        steps++;
-        if ((forceMask >> pos) & 1)
+        WS nw = myers_step(eq, ws, hp & 1, hn & 1, Ph, Mh);
+        if (fm & 1)
         {
             nw.VP &= kAllOnes ^ 1;
             nw.VN |= 1;
         }
+        hp >>= 1;
+        hn >>= 1;
+        fm >>= 1;
         ws = nw;
-        if (ws.end < result.minScore)
-        {
-            result.minScore = ws.end;
-            result.minScoreOffset = pos;
-        }
-        if (Fill && (!boundOk || xscore_bound(ws, seqOffset, cost) > (int64_t)imax(sliceMaxX, result.maxX)))
-            result.maxX = imax(result.maxX, ws_max_xscore(ws, seqOffset, cost, 64, Mh));
-        if (!Fill) cols[pos] = ws;
-        outHP |= (Ph >> 63) << pos;
-        outHN |= (Mh >> 63) << pos;
+        Col c;
+        c.VP = ws.VP;
+        c.VN = ws.VN;
+        c.Mh = Mh;
+        c.end = ws.end;
+        c.phTop = (u32)(Ph >> 63);
+        cols[pos] = c;
     }
-    result.cells = pos;
-    slice.HP = outHP;
-    slice.HN = outHN;
+    steps += columns - 1;
+    result.cells = columns;
+    if (Fill)
+    {
+        // Across the lanes (lane k: columns k and k + 32; every lane wrote every column):
+        // the first column of least score, the greatest X-score and the bottom-row deltas.
+        // A column whose X-score bound is at most max(slice so far, column 0) cannot change
+        // the node's contribution to the slice (the slice keeps the first node of strictly
+        // greatest X-score), so its exact X-score is skipped.
+        const i32 thr = imax(sliceMaxX, result.maxX);
+        u32 loKey = 0xffffffffu, hiKey = 0xffffffffu;
+        i32 lmax = kIntMin;
+        u32 hpLo = 0, hpHi = 0, hnLo = 0, hnHi = 0;
+#pragma unroll
+        for (u32 h = 0; h < 2; h++)
+        {
+            const u32 pos = lane + 32 * h;
+            if (pos >= 1 && pos < columns)
+            {
+                const Col c = cols[pos];
+                const WS cw = ws_make(c.VP, c.VN, c.end);
+                const u32 key = (u32)c.end ^ 0x80000000u;   // signed order as unsigned
+                if (h == 0) loKey = key; else hiKey = key;
+                if (!boundOk || xscore_bound(cw, seqOffset, cost) > (int64_t)thr)
+                    lmax = imax(lmax, ws_max_xscore(cw, seqOffset, cost, 64, c.Mh));
+                if (h == 0) { hpLo = c.phTop; hnLo = (u32)(c.Mh >> 63); }
+                else { hpHi = c.phTop; hnHi = (u32)(c.Mh >> 63); }
+            }
+        }
+        const u32 gkey = __reduce_min_sync(kFull, loKey < hiKey ? loKey : hiKey);
+        const i32 gmax = __reduce_max_sync(kFull, lmax);
+        const u32 onLo = __ballot_sync(kFull, loKey == gkey);
+        const u32 onHi = __ballot_sync(kFull, hiKey == gkey);
+        const u64 outHP = (u64)__ballot_sync(kFull, hpLo) | ((u64)__ballot_sync(kFull, hpHi) << 32);
+        const u64 outHN = (u64)__ballot_sync(kFull, hnLo) | ((u64)__ballot_sync(kFull, hnHi) << 32);
+        if (gkey != 0xffffffffu)
+        {
+            const i32 gmin = (i32)(gkey ^ 0x80000000u);
+            if (gmin < result.minScore)
+            {
+                result.minScore = gmin;
+                result.minScoreOffset = onLo ? (u32)(__ffs((int)onLo) - 1) : (u32)(32 + __ffs((int)onHi) - 1);
+            }
+        }
+        result.maxX = imax(result.maxX, gmax);
+        slice.HP = outHP;
+        slice.HN = outHN;
+    }
     slice.eVP = ws.VP;
     slice.eVN = ws.VN;
     slice.eEnd = ws.end;
@@ -451,71 +545,59 @@ struct ArenaCursor
 {
     u64 pos;
     u64 end;
+    u64 used;           // bytes handed out to this warp since the launch began
 };
 
-__device__ __forceinline__ bool arena_alloc(const FillArgs& a, ArenaCursor& c, u64 bytes, u64& out)
+// bytes from the warp's region, else a chunk of the shared overflow (one atomic per chunk)
+__device__ __forceinline__ bool arena_alloc(const FillArgs& a, ArenaCursor& c, u64 bytes, u64& out, u32 lane)
 {
     bytes = align16(bytes);
     if (c.pos + bytes > c.end)
     {
-        const u64 chunk = 16 * 1024;
-        u64 grab = bytes > chunk ? bytes : chunk;
-        u64 p = atomicAdd(a.arenaCursor, (unsigned long long)grab);
+        const u64 chunk = 64 * 1024;
+        const u64 grab = bytes > chunk ? bytes : chunk;
+        unsigned long long p = 0;
+        if (lane == 0) p = a.overflowBase + atomicAdd(a.arenaCursor, (unsigned long long)grab);
+        p = __shfl_sync(kFull, p, 0);
         if (p + grab > a.arenaBytes) return false;
         c.pos = p;
         c.end = p + grab;
     }
     out = c.pos;
     c.pos += bytes;
+    c.used += bytes;
     return true;
 }
 
-__device__ __forceinline__ u32 rec_hash_cap(u32 count)
-{
-    if (count <= kInlineIds) return 0;
-    u32 cap = 4;
-    while (cap < 2 * count) cap <<= 1;
-    return cap;
-}
+__device__ __forceinline__ u64 rec_ids_bytes(u32 count) { return align16((u64)count * 4); }
 
-__device__ __forceinline__ u64 rec_bytes(u32 count, u32 cap)
-{
-    return sizeof(SliceRec) + (u64)count * sizeof(Item) + (u64)cap * sizeof(uint16_t);
-}
-
-// write one slice (record + band in first-pop order + node hash) into the arena
+// write one slice (record, node ids, band in first-pop order) into the arena, lanes copying
 __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 index, const Item* band, u32 count,
-    i32 minScore, i32 quit, i32 maxX, u32 maxXNode, bool notValid)
+    i32 minScore, i32 quit, i32 maxX, u32 maxXNode, bool notValid, u32 lane)
 {
-    u32 cap = rec_hash_cap(count);
+    const u64 idBytes = rec_ids_bytes(count);
     u64 off;
-    if (!arena_alloc(a, c, rec_bytes(count, cap), off)) return false;
+    if (!arena_alloc(a, c, sizeof(SliceRec) + idBytes + (u64)count * sizeof(Item), off, lane)) return false;
     uint8_t* base = a.arena + off;
-    SliceRec* r = (SliceRec*)base;
-    r->minScore = minScore;
-    r->quit = quit;
-    r->maxX = maxX;
-    r->maxXNode = maxXNode;
-    r->count = count;
-    r->hashCap = cap;
-    r->notValid = notValid ? 1u : 0u;
-    r->pad = 0;
-    for (u32 k = 0; k < kInlineIds; k++) r->ids[k] = k < count ? (band[k].node & kNodeMask) : 0xffffffffu;
-    Item* items = (Item*)(base + sizeof(SliceRec));
-    uint16_t* h = (uint16_t*)(base + sizeof(SliceRec) + (u64)count * sizeof(Item));
-    for (u32 k = 0; k < count; k++) items[k] = band[k];
-    if (cap > 0)
+    if (lane == 0)
     {
-        for (u32 k = 0; k < cap; k++) h[k] = 0;
-        for (u32 k = 0; k < count; k++)
-        {
-            u32 node = band[k].node & kNodeMask;
-            u32 p = hash_node(node) & (cap - 1);
-            while (h[p] != 0) p = (p + 1) & (cap - 1);
-            h[p] = (uint16_t)(k + 1);
-        }
+        SliceRec r;
+        r.minScore = minScore;
+        r.quit = quit;
+        r.maxX = maxX;
+        r.maxXNode = maxXNode;
+        r.count = count;
+        r.notValid = notValid ? 1u : 0u;
+        r.pad0 = 0;
+        r.pad1 = 0;
+        *(SliceRec*)base = r;
+        dir[index] = off;
     }
-    dir[index] = off;
+    u32* ids = (u32*)(base + sizeof(SliceRec));
+    for (u32 k = lane; k < count; k += 32) ids[k] = band[k].node & kNodeMask;
+    uint4* dst = (uint4*)(base + sizeof(SliceRec) + idBytes);
+    const uint4* src = (const uint4*)band;
+    for (u32 k = lane; k < count * 4; k += 32) dst[k] = src[k];
     return true;
 }
 
@@ -531,16 +613,18 @@ struct SliceResult
 };
 
 // calculateSlice (GraphAlignerBitvectorBanded.h:255-511), component-queue branch, no seed hits.
-__device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur, u32 curGen, u32 prevGen, u32& curCount, u32 prevCount,
-    const uint8_t* seq, u32 seqLen, int64_t j, i32 prevQuit, i32 prevMin, u64& steps, int& err)
+__device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u32 curGen, u32 prevGen, u32& curCount, u32 prevCount,
+    const uint8_t* seq, u32 seqLen, int64_t j, i32 prevQuit, i32 prevMin, u64& steps, int& err, u32 lane)
 {
     const DevGraph& g = a.g;
     const int bw = (int)a.bandwidth;
     const int prv = cur ^ 1;
     Item* curBand = w.band[cur];
     const Item* prevBand = w.band[prv];
-    HSlot* curHash = w.hash[cur];
-    HSlot* prevHash = w.hash[prv];
+    u64* curKey = w.key[cur];
+    NodeVal* curVal = w.val[cur];
+    const u64* prevKey = w.key[prv];
+    const NodeVal* prevVal = w.val[prv];
     const u32 hcap = a.caps.hash;
     SliceResult res;
     res.minScore = kIntMax - bw - 1;
@@ -549,32 +633,41 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
     res.maxXNode = 0;
     res.cells = 0;
     EqV4 eqv;
-    if (!eq_vector(seq, seqLen, j, eqv)) { err = GA_ASSERT; return res; }
+    if (!eq_vector(seq, seqLen, j, eqv, lane)) { err = GA_ASSERT; return res; }
     u32 heapN = 0;
     u32 poolN = 0;
-    u32 hashUsed = 0;
+    u32 used = 0;
     curCount = 0;
+
+    // band index of node in the previous slice, or -1
+    auto prevBandOf = [&](u32 node) -> int
+    {
+        const int s = tbl_find(prevKey, hcap, prevGen, node, lane);
+        return s < 0 ? -1 : (int)prevVal[s].band;
+    };
 
     auto insert = [&](u32 target, i32 score, u64 vp, u64 vn, i32 end, bool skip) -> bool
     {
-        HSlot* s = hash_get_or_add(curHash, hcap, curGen, target, hashUsed);
-        if (!s) return false;
-        if (!s->active)
+        const int slot = tbl_get_or_add(curKey, curVal, hcap, curGen, target, used, lane);
+        if (slot < 0) return false;
+        NodeVal& s = curVal[slot];
+        if (!s.active)
         {
             if (heapN >= a.caps.heap) return false;
             HeapItem hi; hi.component = g.comp[target]; hi.score = score; hi.node = target;
             heap_push(w.heap, heapN, hi);
-            s->active = 1;
-            s->head = kNil;
-            s->tail = kNil;
+            s.active = 1;
+            s.head = kNil;
+            s.tail = kNil;
         }
         if (poolN >= a.caps.extras) return false;
         uint16_t e = (uint16_t)poolN++;
-        Extra& x = w.extras[e];
+        Extra x;
         x.VP = vp; x.VN = vn; x.end = end; x.next = kNil; x.skip = skip ? 1 : 0;
-        if (s->head == kNil) s->head = e;
-        else w.extras[s->tail].next = e;
-        s->tail = e;
+        w.extras[e] = x;
+        if (s.head == kNil) s.head = e;
+        else w.extras[s.tail].next = e;
+        s.tail = e;
         return true;
     };
 
@@ -591,11 +684,10 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
             if (it.minScore > prevQuit) continue;
             if (g.lin[node])
             {
-                u32 nb = g.inNb[g.inOff[node]];
-                HSlot* ps = hash_find(prevHash, hcap, prevGen, nb);
-                if (ps && ps->band >= 0)
+                const int pb = prevBandOf(g.inNb[g.inOff[node]]);
+                if (pb >= 0)
                 {
-                    const Item& pn = prevBand[ps->band];
+                    const Item& pn = prevBand[pb];
                     if (pn.eEnd < prevQuit && pn.minScore < prevQuit) continue;
                 }
             }
@@ -609,26 +701,28 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
     while (heapN > 0)
     {
         u32 i = w.heap[0].node;
-        HSlot* s = hash_find(curHash, hcap, curGen, i);
-        if (!s) { err = GA_ASSERT; return res; }
-        if (s->band < 0)
+        const int slot = tbl_find(curKey, hcap, curGen, i, lane);
+        if (slot < 0) { err = GA_ASSERT; return res; }
+        NodeVal& s = curVal[slot];
+        if (s.band < 0)
         {
             if (curCount >= a.caps.band || curCount >= 32767) { err = GA_CAPACITY; return res; }
-            s->band = (int16_t)curCount;
-            Item& ni = curBand[curCount++];
+            s.band = (int16_t)curCount;
+            Item ni;
             ni.sVP = 0; ni.sVN = 0; ni.sEnd = kIntMax;
             ni.eVP = 0; ni.eVN = 0; ni.eEnd = kIntMax;
             ni.HP = 0; ni.HN = 0;
             ni.minScore = kIntMax;
             ni.node = i;
+            curBand[curCount++] = ni;
         }
-        Item& thisNode = curBand[s->band];
+        Item& thisNode = curBand[s.band];
         WS oldEnd = (thisNode.node & kExists) ? ws_make(thisNode.eVP, thisNode.eVN, thisNode.eEnd) : ws_make(0, 0, kIntMax);
         PrevInfo prev;
-        HSlot* ps = hash_find(prevHash, hcap, prevGen, i);
-        if (ps && ps->band >= 0)
+        const int pb = prevBandOf(i);
+        if (pb >= 0)
         {
-            const Item& pi = prevBand[ps->band];
+            const Item& pi = prevBand[pb];
             prev.exists = true;
             prev.sEnd = pi.sEnd;
             prev.HP = pi.HP;
@@ -642,17 +736,14 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
             prev.HN = 0;
         }
         bool singleInPrev = false;
-        if (g.inOff[i + 1] - g.inOff[i] == 1)
-        {
-            HSlot* q = hash_find(prevHash, hcap, prevGen, g.inNb[g.inOff[i]]);
-            singleInPrev = q && q->band >= 0;
-        }
-        NodeCalc nc = node_calc<true>(g, a.cost, i, thisNode, eqv, prev, w.extras, s->head, nullptr, singleInPrev, seqOffset, nullptr, steps, err, res.maxX);
+        if (g.inOff[i + 1] - g.inOff[i] == 1) singleInPrev = prevBandOf(g.inNb[g.inOff[i]]) >= 0;
+        NodeCalc nc = node_calc<true>(g, a.cost, i, thisNode, eqv, prev, w.extras, s.head, nullptr, singleInPrev, seqOffset,
+            w.cols, w.eqcol, steps, err, lane, res.maxX);
         if (err) return res;
         heap_pop(w.heap, heapN);
-        s->active = 0;
-        s->head = kNil;
-        s->tail = kNil;
+        s.active = 0;
+        s.head = kNil;
+        s.tail = kNil;
         if (nc.minScore > wadd(wadd(seqOffset, bw), 128)) { err = GA_ASSERT; return res; }
         curMin = imin(curMin, nc.minScore);
         if (nc.minScore < thisNode.minScore) thisNode.minScore = nc.minScore;
@@ -687,7 +778,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const Workspace& w, int cur
     return res;
 }
 
-__device__ ExtState fill_extension(const FillArgs& a, const Workspace& w, u32& gen, ArenaCursor& arena, u32 ext)
+__device__ ExtState fill_extension(const FillArgs& a, const WSpace& w, u32& gen, ArenaCursor& arena, u32 ext, u32 lane)
 {
     const DevGraph& g = a.g;
     ExtState st;
@@ -707,7 +798,7 @@ __device__ ExtState fill_extension(const FillArgs& a, const Workspace& w, u32& g
         return st;
     }
     u64 dirOff;
-    if (!arena_alloc(a, arena, (u64)(numSlices + 1) * 8, dirOff))
+    if (!arena_alloc(a, arena, (u64)(numSlices + 1) * 8, dirOff, lane))
     {
         st.status = GA_CAPACITY;
         return st;
@@ -719,7 +810,7 @@ __device__ ExtState fill_extension(const FillArgs& a, const Workspace& w, u32& g
     gen++;
     u32 prevGen = gen;
     {
-        Item& it = w.band[prv][0];
+        Item it;
         u32 L = g.len[startNode];
         it.sVP = 0; it.sVN = 0; it.sEnd = (i32)startOff;
         it.eVP = 0; it.eVN = 0; it.eEnd = (i32)L - 1 - (i32)startOff;
@@ -730,10 +821,11 @@ __device__ ExtState fill_extension(const FillArgs& a, const Workspace& w, u32& g
         for (u32 k = startOff + 1; k < L; k++) hp |= 1ULL << k;
         it.HP = hp;
         it.HN = hn;
+        w.band[prv][0] = it;
         u32 used = 0;
-        HSlot* s = hash_get_or_add(w.hash[prv], a.caps.hash, prevGen, startNode, used);
-        s->band = 0;
-        if (!commit_slice(a, arena, dir, 0, &it, 1, 0, 1, 0, startNode, false))
+        const int s = tbl_get_or_add(w.key[prv], w.val[prv], a.caps.hash, prevGen, startNode, used, lane);
+        w.val[prv][s].band = 0;
+        if (!commit_slice(a, arena, dir, 0, w.band[prv], 1, 0, 1, 0, startNode, false, lane))
         {
             st.status = GA_CAPACITY;
             return st;
@@ -751,14 +843,14 @@ __device__ ExtState fill_extension(const FillArgs& a, const Workspace& w, u32& g
         const u32 curGen = gen;
         u32 curCount = 0;
         const int64_t j = (int64_t)s * 64;
-        SliceResult r = fill_slice(a, w, cur, curGen, prevGen, curCount, prevCount, seq, seqLen, j, lastQuit, lastMin, st.steps, err);
+        SliceResult r = fill_slice(a, w, cur, curGen, prevGen, curCount, prevCount, seq, seqLen, j, lastQuit, lastMin, st.steps, err, lane);
         if (err) break;
         if (r.maxX > bestX) bestX = r.maxX;
         const bool notValid = r.cells >= a.maxCells;
         if ((int64_t)r.maxX < (int64_t)bestX - (int64_t)a.xdrop) break;
         if (r.minScore < lastMin) { err = GA_ASSERT; break; }
         const i32 quit = wadd(r.minScore, (i32)a.bandwidth);
-        if (!commit_slice(a, arena, dir, committed, w.band[cur], curCount, r.minScore, quit, r.maxX, r.maxXNode, notValid))
+        if (!commit_slice(a, arena, dir, committed, w.band[cur], curCount, r.minScore, quit, r.maxX, r.maxXNode, notValid, lane))
         {
             err = GA_CAPACITY;
             break;
@@ -783,6 +875,7 @@ struct Table
     const uint8_t* arena;
     const u64* dir;
     u32 count;
+    u32 lane;
     // the traceback works on one slice and the one before it: their records are remembered
     u32 cs[2];
     const SliceRec* cr[2];
@@ -796,28 +889,21 @@ struct Table
         cs[0] = s; cr[0] = r;
         return r;
     }
-    __device__ __forceinline__ const Item* items(u32 s) { return (const Item*)((const uint8_t*)rec(s) + sizeof(SliceRec)); }
+    // the band entry of node in slice s (a ballot over the slice's node ids), or nullptr
     __device__ __forceinline__ const Item* find(u32 s, u32 node)
     {
         const SliceRec* r = rec(s);
-        const Item* it = (const Item*)((const uint8_t*)r + sizeof(SliceRec));
-        const u32 count = r->count;
-        if (count <= kInlineIds)
+        const u32 n = r->count;
+        const u32* ids = (const u32*)((const uint8_t*)r + sizeof(SliceRec));
+        for (u32 base = 0; base < n; base += 32)
         {
-            // the record's own line holds the band's node ids
-            for (u32 k = 0; k < count; k++)
-                if (r->ids[k] == node) return &it[k];
-            return nullptr;
-        }
-        const uint16_t* h = (const uint16_t*)((const uint8_t*)it + (u64)count * sizeof(Item));
-        u32 cap = r->hashCap;
-        u32 p = hash_node(node) & (cap - 1);
-        for (u32 probe = 0; probe < cap; probe++)
-        {
-            uint16_t v = h[p];
-            if (v == 0) return nullptr;
-            if ((it[v - 1].node & kNodeMask) == node) return &it[v - 1];
-            p = (p + 1) & (cap - 1);
+            const u32 k = base + lane;
+            const u32 hit = __ballot_sync(kFull, k < n && ids[k] == node);
+            if (hit)
+            {
+                const Item* items = (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
+                return &items[base + __ffs((int)hit) - 1];
+            }
         }
         return nullptr;
     }
@@ -838,19 +924,42 @@ struct TStep
     bool sw;
 };
 
+// Trace items go to a 64-entry ring in shared memory (every lane writes every item) and
+// out to the caller's buffer 32 at a time, one item per lane.
 struct TraceOut
 {
     u64* items;
+    u64* ring;
     u32 cap;
     u32 n;
+    u32 lane;
     TPos back;
     bool overflow;
     __device__ __forceinline__ void push(const TPos& p, bool sw)
     {
         if (n >= cap) { overflow = true; return; }
         u64 sp1 = p.seq < 0 ? 0 : (u64)p.seq + 1;
-        items[n++] = (u64)p.node | ((u64)(p.off & 63) << 32) | ((u64)(sw ? 1 : 0) << 38) | (sp1 << 39);
+        ring[n & 63] = (u64)p.node | ((u64)(p.off & 63) << 32) | ((u64)(sw ? 1 : 0) << 38) | (sp1 << 39);
+        n++;
         back = p;
+        if ((n & 31) == 0)
+        {
+            const u32 k = n - 32 + lane;
+            items[k] = ring[k & 63];
+            __syncwarp();
+        }
+    }
+    // item k (k < n): from the ring while it holds it, else from the written output
+    __device__ __forceinline__ u64 get(u32 k) const
+    {
+        return k + 63 >= n ? ring[k & 63] : items[k];
+    }
+    // writes the items of the last, partial group of 32
+    __device__ __forceinline__ void finish()
+    {
+        const u32 k = (n & ~31u) + lane;
+        if (k < n) items[k] = ring[k & 63];
+        __syncwarp();
     }
 };
 
@@ -862,10 +971,10 @@ __device__ __forceinline__ bool trace_circular(const TraceOut& to)
 {
     if (to.n < 2) return false;
     const u64 keyMask = ~(1ULL << 38);
-    u64 last = to.items[to.n - 1];
+    u64 last = to.get(to.n - 1);
     for (int k = (int)to.n - 2; k >= 0; k--)
     {
-        u64 x = to.items[k];
+        u64 x = to.get((u32)k);
         if ((x & keyMask) == (last & keyMask)) return true;
         if ((x >> 39) != (last >> 39)) return false;
     }
@@ -880,9 +989,14 @@ struct TraceCtx
     Table t;
     i32 cost;
     int err;
+    Col* cols;
+    u64* eqcol;
+    u32 lane;
 };
 
 __device__ __forceinline__ i32 fake_value() { return kIntMax; }
+
+__device__ __forceinline__ i32 col_value(const Col& c, int row) { return ws_value(ws_make(c.VP, c.VN, c.end), row); }
 
 // pickBacktraceCorner (Common.h:936-1054)
 __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
@@ -995,7 +1109,7 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
 // (the traceback only moves left inside a node, so it never needs the columns after the
 // one it enters at).  When every column is recomputed the last one must equal the
 // stored end column, as the reference asserts.
-__device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, WS* cols, u32 lastColumn = 63)
+__device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, u32 lastColumn = 63)
 {
     const Item* it = c.t.find(s, node);
     if (!it) { c.err = GA_ASSERT; return false; }
@@ -1008,25 +1122,33 @@ __device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, WS* cols, 
     u64 steps = 0;
     int err = 0;
     int64_t j = ((int64_t)s - 1) * 64;
-    node_calc<false>(*c.g, c.cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, cols, steps, err, kIntMin, lastColumn);
+    node_calc<false>(*c.g, c.cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, c.cols, c.eqcol, steps, err,
+        c.lane, kIntMin, lastColumn);
     if (err) { c.err = err; return false; }
     u32 L = c.g->len[node];
-    if (!ws_eq(cols[0], start)) { c.err = GA_ASSERT; return false; }
-    if (lastColumn + 1 >= L && !ws_eq(cols[L - 1], ws_make(it->eVP, it->eVN, it->eEnd))) { c.err = GA_ASSERT; return false; }
+    if (!ws_eq(ws_make(c.cols[0].VP, c.cols[0].VN, c.cols[0].end), start)) { c.err = GA_ASSERT; return false; }
+    if (lastColumn + 1 >= L && !ws_eq(ws_make(c.cols[L - 1].VP, c.cols[L - 1].VN, c.cols[L - 1].end), ws_make(it->eVP, it->eVN, it->eEnd)))
+    {
+        c.err = GA_ASSERT;
+        return false;
+    }
     return true;
 }
 
-__device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st, WS* cols)
+__device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st, const WSpace& w, u32 lane)
 {
     const DevGraph& g = a.g;
     u64* out = a.traceItems + a.traceOffset[ext];
     const u32 cap = a.traceCap[ext];
-    if (a.cellSteps) a.cellSteps[ext] = st.steps;
+    if (lane == 0 && a.cellSteps) a.cellSteps[ext] = st.steps;
     if (st.status != GA_OK)
     {
-        a.status[ext] = st.status;
-        a.score[ext] = 0;
-        a.traceLen[ext] = 0;
+        if (lane == 0)
+        {
+            a.status[ext] = st.status;
+            a.score[ext] = 0;
+            a.traceLen[ext] = 0;
+        }
         return;
     }
     TraceCtx c;
@@ -1036,47 +1158,77 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
     c.t.arena = a.arena;
     c.t.dir = (const u64*)(a.arena + st.dir);
     c.t.count = st.committed;
+    c.t.lane = lane;
     c.t.init();
     c.cost = a.cost;
     c.err = 0;
+    c.cols = w.cols;
+    c.eqcol = w.eqcol;
+    c.lane = lane;
+    Col* cols = w.cols;
     TraceOut to;
     to.items = out;
+    to.ring = w.ring;
     to.cap = cap;
     to.n = 0;
+    to.lane = lane;
     to.overflow = false;
-    // choose the end cell (getReverseTraceFromTableExactEndPos, Common.h:496-562)
-    u32 best = 1;
-    for (u32 s = 1; s < st.committed; s++)
-        if (c.t.rec(s)->maxX > c.t.rec(best)->maxX) best = s;
+    // choose the end cell (getReverseTraceFromTableExactEndPos, Common.h:496-562): the first
+    // slice of greatest X-score (lanes stride over the slices) ...
+    i32 bx = kIntMin;
+    u32 bs = 0xffffffffu;
+    for (u32 s = 1 + lane; s < st.committed; s += 32)
+    {
+        const i32 mx = ((const SliceRec*)(a.arena + c.t.dir[s]))->maxX;
+        if (mx > bx) { bx = mx; bs = s; }
+    }
+    const i32 gbx = __reduce_max_sync(kFull, bx);
+    const u32 best = __reduce_min_sync(kFull, bx == gbx ? bs : 0xffffffffu);
     const SliceRec* br = c.t.rec(best);
     u32 node = br->maxXNode;
     i32 score = br->maxX;
     int64_t j = ((int64_t)best - 1) * 64;
     EqV4 eqv;
-    if (!eq_vector(c.seq, c.seqLen, j, eqv)) c.err = GA_ASSERT;
+    if (!eq_vector(c.seq, c.seqLen, j, eqv, lane)) c.err = GA_ASSERT;
     u32 nodeOffset = 0xffffffffu, bvOffset = 0xffffffffu;
-    if (!c.err && recalc(c, best, node, eqv, cols))
+    if (!c.err && recalc(c, best, node, eqv))
     {
-        int cells = (int)((int64_t)c.seqLen - j < 64 ? (int64_t)c.seqLen - j : 64);
-        u32 L = g.len[node];
-        for (u32 i = 0; i < L && !c.err; i++)
+        // ... then, across the lanes (lane k: columns k and k + 32), the cell of greatest row
+        // among those scoring the slice's X-score, the first column on ties
+        const int cells = (int)((int64_t)c.seqLen - j < 64 ? (int64_t)c.seqLen - j : 64);
+        const u32 L = g.len[node];
+        bool bad = false;
+        int candOff = -1;
+        u32 candCol = 0xffffffffu;
+        for (u32 h = 0; h < 2; h++)
         {
-            i32 mx = ws_max_xscore(cols[i], (i32)j, a.cost, cells, kAllOnes);
-            if (mx > score) { c.err = GA_ASSERT; break; }
+            const u32 i = lane + 32 * h;
+            if (i >= L || bad) continue;
+            const WS cw = ws_make(cols[i].VP, cols[i].VN, cols[i].end);
+            i32 mx = ws_max_xscore(cw, (i32)j, a.cost, cells, kAllOnes);
+            if (mx > score) { bad = true; continue; }
             if (mx == score)
             {
                 for (int off = 63; off >= 0; off--)
                 {
                     if (j + off >= (int64_t)c.seqLen) continue;
-                    i32 here = ws_xscore(cols[i], (i32)j, off, a.cost);
-                    if (here > score) { c.err = GA_ASSERT; break; }
-                    if (here == score && (nodeOffset == 0xffffffffu || (u32)off > bvOffset))
+                    i32 here = ws_xscore(cw, (i32)j, off, a.cost);
+                    if (here > score) { bad = true; break; }
+                    if (here == score && off > candOff)
                     {
-                        nodeOffset = i;
-                        bvOffset = (u32)off;
+                        candOff = off;
+                        candCol = i;
                     }
                 }
             }
+        }
+        if (__ballot_sync(kFull, bad)) c.err = GA_ASSERT;
+        const int gOff = __reduce_max_sync(kFull, candOff);
+        const u32 gCol = __reduce_min_sync(kFull, candOff == gOff ? candCol : 0xffffffffu);
+        if (gOff >= 0)
+        {
+            nodeOffset = gCol;
+            bvOffset = (u32)gOff;
         }
     }
     if (!c.err && (nodeOffset == 0xffffffffu || j + bvOffset >= (int64_t)c.seqLen)) c.err = GA_ASSERT;
@@ -1085,13 +1237,13 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
     {
         // getReverseTraceFromTable (Common.h:571-758)
         TPos start = TPos { node, nodeOffset, j + bvOffset };
-        i32 startScore = ws_value(cols[nodeOffset], (int)bvOffset);
+        i32 startScore = col_value(cols[nodeOffset], (int)bvOffset);
         resultScore = startScore;
         to.push(start, false);
         u32 curSlice = (u32)(start.seq / 64) + 1;
         u32 curNode = 0xffffffffu;
         u32 colsUpTo = 0;             // columns 0..colsUpTo of (curSlice, curNode) are in cols
-        if (!eq_vector(c.seq, c.seqLen, ((int64_t)curSlice - 1) * 64, eqv)) c.err = GA_ASSERT;
+        if (!eq_vector(c.seq, c.seqLen, ((int64_t)curSlice - 1) * 64, eqv, lane)) c.err = GA_ASSERT;
         i32 lastScore = kIntMax - 1;
         u64 guard = 0;
         const u64 guardMax = (u64)cap * 4 + 1024;
@@ -1104,22 +1256,22 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
             // a self-loop can re-enter the same node-slice further right than it was computed
             if (newSlice != curSlice || b.node != curNode || b.off > colsUpTo)
             {
-                if (newSlice != curSlice && !eq_vector(c.seq, c.seqLen, ((int64_t)newSlice - 1) * 64, eqv)) { c.err = GA_ASSERT; break; }
+                if (newSlice != curSlice && !eq_vector(c.seq, c.seqLen, ((int64_t)newSlice - 1) * 64, eqv, lane)) { c.err = GA_ASSERT; break; }
                 curSlice = newSlice;
                 curNode = b.node;
                 if (curSlice == 0) { c.err = GA_ASSERT; break; }
-                if (!recalc(c, curSlice, curNode, eqv, cols, b.off)) break;
+                if (!recalc(c, curSlice, curNode, eqv, b.off)) break;
                 colsUpTo = b.off;
             }
             const int64_t sj = ((int64_t)curSlice - 1) * 64;
             if (b.off >= g.len[curNode]) { c.err = GA_ASSERT; break; }
             const u32 row = mod64(b.seq);
-            lastScore = ws_value(cols[b.off], (int)row);
+            lastScore = col_value(cols[b.off], (int)row);
             if (row == 0 && b.off == 0)
             {
                 TStep bt = bt_corner(c, curSlice, curNode, sj);
                 if (c.err) break;
-                if (tpos_eq(bt.pos, b) && !bt.sw && ws_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == fake_value()) break;
+                if (tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == fake_value()) break;
                 to.push(bt.pos, bt.sw);
                 if (!to.overflow && trace_circular(to)) { c.err = GA_ASSERT; break; }
                 continue;
@@ -1135,7 +1287,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 }
                 // pickBacktraceVerticalCrossing (Common.h:886-934)
                 TPos p = b;
-                while (p.off > 0 && ws_value(cols[p.off - 1], 0) == ws_value(cols[p.off], 0) - 1) p.off--;
+                while (p.off > 0 && col_value(cols[p.off - 1], 0) == col_value(cols[p.off], 0) - 1) p.off--;
                 TStep second;
                 if (p.off == 0)
                 {
@@ -1149,7 +1301,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                     bool bad = false;
                     bool eq = char_match(g, c.seq[p.seq], p.node, p.off, bad);
                     if (bad) { c.err = GA_ASSERT; break; }
-                    i32 here = ws_value(cols[p.off], 0);
+                    i32 here = col_value(cols[p.off], 0);
                     i32 diag = pself->sEnd;
                     for (u32 k = 1; k + 1 <= p.off; k++)
                     {
@@ -1171,7 +1323,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                         else { c.err = GA_ASSERT; break; }
                     }
                 }
-                if (second.pos.seq == b.seq && ws_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
+                if (second.pos.seq == b.seq && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
                 if (p.off != b.off)
                 {
                     for (u32 k = b.off - 1; k != p.off; k--) to.push(TPos { p.node, k, p.seq }, false);
@@ -1255,7 +1407,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                         }
                     }
                 }
-                if (second.pos.node == b.node && !second.sw && ws_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
+                if (second.pos.node == b.node && !second.sw && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
                 if (p.seq != b.seq)
                 {
                     for (int64_t sp = b.seq - 1; sp != p.seq; sp--) to.push(TPos { p.node, p.off, sp }, false);
@@ -1285,8 +1437,8 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 };
                 if (hori > 0 && vert > 0)
                 {
-                    WS colH = cols[hori];
-                    WS colL = cols[hori - 1];
+                    WS colH = ws_make(cols[hori].VP, cols[hori].VN, cols[hori].end);
+                    WS colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
                     i32 here = ws_value(colH, (int)vert);
                     i32 left = ws_value(colL, (int)vert);
                     u64 eqH = colEq(hori);
@@ -1311,7 +1463,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                             colH = colL;
                             if (hori > 0)
                             {
-                                colL = cols[hori - 1];
+                                colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
                                 left = ws_value(colL, (int)vert);
                                 eqH = colEq(hori);
                             }
@@ -1324,7 +1476,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                             colH = colL;
                             if (hori > 0)
                             {
-                                colL = cols[hori - 1];
+                                colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
                                 left = ws_value(colL, (int)vert);
                                 eqH = colEq(hori);
                             }
@@ -1338,7 +1490,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                     }
                 }
                 if (c.err || to.overflow) break;
-                if (ws_value(cols[to.back.off], (int)mod64(to.back.seq)) == fake_value()) break;
+                if (col_value(cols[to.back.off], (int)mod64(to.back.seq)) == fake_value()) break;
             }
         }
         if (!c.err && !to.overflow)
@@ -1387,67 +1539,91 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
             }
         }
     }
+    to.finish();
     int status = c.err ? c.err : (to.overflow ? GA_CAPACITY : GA_OK);
-    a.status[ext] = status;
-    a.score[ext] = status == GA_OK ? resultScore : 0;
-    a.traceLen[ext] = status == GA_OK ? to.n : 0;
+    if (lane == 0)
+    {
+        a.status[ext] = status;
+        a.score[ext] = status == GA_OK ? resultScore : 0;
+        a.traceLen[ext] = status == GA_OK ? to.n : 0;
+    }
 }
 
-// One persistent kernel per batch: a thread fills the DP table of an extension
-// and walks it back right away.  Warps take chunks of the longest-first order from
-// a chunk table the host builds (ga_launch_shape): a chunk is up to 32 consecutive
-// extensions, one per lane, so the lanes of a warp hold extensions of similar
-// length.  The longest extensions come in chunks of one (lane 0 alone), which keeps
-// them free of divergence with other lanes; the chunk sizes trade divergence within
-// a warp against the number of extensions in flight.
-__global__ void __launch_bounds__(128) extend_kernel(FillArgs fa, TraceArgs ta, const u32* chunks, u32 numChunks,
-    u32* counter, u32 slotBase, u32 slotLimit)
+// One persistent launch per batch: a warp takes the next extension of the longest-first
+// order, fills its DP table into the warp's arena region and walks it back, then takes the
+// next.  The tables are in dynamic shared memory (fa.workspace == nullptr) or in the
+// global workspace, one stride per warp.
+__global__ void __launch_bounds__(128, 4) extend_kernel(FillArgs fa, TraceArgs ta, u32* counter)
 {
+    extern __shared__ __align__(16) uint8_t dsmem[];
     load_iupac_table();
-    const u32 slot = slotBase + blockIdx.x * blockDim.x + threadIdx.x;
-    // a warp whose slots are not all inside [slotBase, slotLimit) touches no workspace (warp-uniform)
-    if (slotBase + blockIdx.x * blockDim.x + (threadIdx.x & ~31u) + 32 > slotLimit) return;
-    Workspace w = workspace_at(fa.workspace + (u64)slot * fa.workspaceStride, fa.caps);
-    u32 gen = w.header[0];
-    ArenaCursor arena;
-    arena.pos = 0;
-    arena.end = 0;
-    WS cols[64];
     const u32 lane = threadIdx.x & 31;
+    const u32 warpInBlock = threadIdx.x >> 5;
+    const u64 gwarp = (u64)blockIdx.x * (blockDim.x >> 5) + warpInBlock;
+    uint8_t* base = fa.workspace ? fa.workspace + gwarp * fa.workspaceStride : dsmem + (u64)warpInBlock * fa.workspaceStride;
+    const WSpace w = wspace_at(base, fa.caps);
+    // generation 0 marks every node-table slot empty
+    for (u32 k = lane; k < fa.caps.hash; k += 32)
+    {
+        w.key[0][k] = 0;
+        w.key[1][k] = 0;
+    }
+    __syncwarp();
+    u32 gen = 0;
+    const u64 region = gwarp * fa.regionBytes;
+    ArenaCursor arena;
+    arena.used = 0;
     while (true)
     {
-        u32 ci = 0;
-        if (lane == 0) ci = atomicAdd(counter, 1u);
-        ci = __shfl_sync(0xffffffffu, ci, 0);
-        if (ci >= numChunks) break;
-        // chunk = first position in the order (high 26 bits) and size - 1 (low 6 bits)
-        const u32 chunk = chunks[ci];
-        if (lane <= (chunk & 63u))
+        u32 k = 0;
+        if (lane == 0) k = atomicAdd(counter, 1u);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= fa.num) break;
+        const u32 ext = fa.order ? fa.order[k] : k;
+        if (fa.prevStatus && fa.prevStatus[ext] != GA_CAPACITY) continue;
+        __syncwarp();
+        arena.pos = region;
+        arena.end = region + fa.regionBytes;
+        ExtState st = fill_extension(fa, w, gen, arena, ext, lane);
+        __syncwarp();
+        trace_extension(ta, ext, st, w, lane);
+        if (gen > 0xF0000000u)
         {
-            const u32 ext = fa.order[(chunk >> 6) + lane];
-            if (!fa.prevStatus || fa.prevStatus[ext] == GA_CAPACITY)
+            // generation stamps are about to wrap: clear this warp's tables
+            __syncwarp();
+            for (u32 k2 = lane; k2 < fa.caps.hash; k2 += 32)
             {
-                ExtState st = fill_extension(fa, w, gen, arena, ext);
-                trace_extension(ta, ext, st, cols);
-                if (gen > 0xF0000000u)
-                {
-                    // generation stamps are about to wrap: clear this thread's tables
-                    for (u32 t = 0; t < 2; t++)
-                        for (u32 k2 = 0; k2 < fa.caps.hash; k2++) w.hash[t][k2].gen = 0;
-                    gen = 0;
-                }
+                w.key[0][k2] = 0;
+                w.key[1][k2] = 0;
             }
+            __syncwarp();
+            gen = 0;
         }
     }
-    w.header[0] = gen;
+    if (lane == 0 && arena.used) atomicAdd(fa.arenaCursor + 1, (unsigned long long)arena.used);
 }
 
 }
 
-void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, const uint32_t* chunks, uint32_t numChunks,
-    uint32_t* counter, uint32_t slotBase, uint32_t slotLimit, int grid, int block, void* stream)
+uint64_t ga_warp_tables_bytes(const gadev::Caps& c) { return gadev::wspace_bytes(c); }
+
+int ga_extend_blocks_per_sm(int warpsPerBlock, const gadev::Caps& caps, bool shared)
 {
-    gadev::extend_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(fa, ta, chunks, numChunks, counter, slotBase, slotLimit);
+    const size_t smem = shared ? (size_t)gadev::wspace_bytes(caps) * warpsPerBlock : 0;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(gadev::extend_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::extend_kernel, warpsPerBlock * 32, smem) != cudaSuccess) return 0;
+    return n;
+}
+
+int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counter, int blocks, int warpsPerBlock, void* stream)
+{
+    const size_t smem = fa.workspace ? 0 : (size_t)fa.workspaceStride * warpsPerBlock;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(gadev::extend_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return -1;
+    gadev::extend_kernel<<<blocks, warpsPerBlock * 32, smem, (cudaStream_t)stream>>>(fa, ta, counter);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int ga_upload_tables()
@@ -1455,205 +1631,4 @@ int ga_upload_tables()
     int8_t t[256];
     for (int i = 0; i < 256; i++) t[i] = (int8_t)gadev::iupac_mask((unsigned char)i);
     return cudaMemcpyToSymbol(gadev::c_iupac, t, sizeof(t)) == cudaSuccess ? 0 : -1;
-}
-
-int ga_extend_occupancy(int block)
-{
-    int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::extend_kernel, block, 0);
-    return n;
-}
-
-uint64_t ga_workspace_bytes(const gadev::Caps& c)
-{
-    using namespace gadev;
-    u64 b = 16;
-    b += 2 * align16((u64)c.band * sizeof(Item));
-    b += 2 * align16((u64)c.hash * sizeof(HSlot));
-    b += align16((u64)c.heap * sizeof(HeapItem));
-    b += align16((u64)c.extras * sizeof(Extra));
-    return align16(b);
-}
-
-// ---------------------------------------------------------------- no-allocation entry point
-//
-// ga_extend_batch_noalloc serves callers that cannot call cudaMalloc when they
-// extend: processes whose device memory is handed out by another allocator
-// under a fixed budget (a framework's caching pool owns the GPU), and request
-// paths where the device-wide synchronisation of cudaMalloc/cudaFree is not
-// acceptable.  All of its scratch memory — the per-thread frontier tables and
-// the DP-table arena the fill writes and the traceback reads — lives in the
-// file-scope device array below, which every GPU that loads this library holds
-// until the process exits.  Inputs and outputs are the caller's device buffers.
-
-namespace gadev
-{
-static constexpr u64 kNoAllocScratchBytes = 128ULL << 20;       // 128 MiB per GPU
-static constexpr u32 kNoAllocThreads = 2048;                     // 16 blocks of 128
-static constexpr u32 kNoAllocMaxExtensions = 4096;               // per call
-static constexpr u64 kNoAllocMaxReadBp = 8000000;                // per call, summed over the batch
-static constexpr u64 kNoAllocHeaderBytes = 256;                  // work counter + arena cursor
-
-static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
-
-// The single-extension-per-thread fill + traceback of extend_kernel, with its
-// workspace and arena carved out of the scratch array and extensions taken in
-// index order (no length ordering, no second launch, no capacity retry: an
-// extension that outgrows the small tables reports GA_CAPACITY).
-__global__ void __launch_bounds__(128) extend_kernel_noalloc(FillArgs fa, TraceArgs ta, u32* counter)
-{
-    load_iupac_table();
-    const u32 slot = blockIdx.x * blockDim.x + threadIdx.x;
-    Workspace w = workspace_at(fa.workspace + (u64)slot * fa.workspaceStride, fa.caps);
-    u32 gen = w.header[0];
-    ArenaCursor arena;
-    arena.pos = 0;
-    arena.end = 0;
-    WS cols[64];
-    while (true)
-    {
-        const u32 ext = atomicAdd(counter, 1u);
-        if (ext >= fa.num) break;
-        ExtState st = fill_extension(fa, w, gen, arena, ext);
-        trace_extension(ta, ext, st, cols);
-    }
-    w.header[0] = gen;
-}
-}
-
-extern "C" int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const ga_extend_params* params,
-    const ga_extend_batch_desc* device_batch, ga_extend_results* device_results, void* stream)
-{
-    using namespace gadev;
-    if (!device_graph || !params || !device_batch || !device_results)
-    {
-        ga_set_last_error("ga_extend_batch_noalloc: null argument");
-        return GA_ERR_ARGUMENT;
-    }
-    const u32 n = device_batch->num;
-    if (n == 0) return GA_OK;
-    if (n > kNoAllocMaxExtensions)
-    {
-        ga_set_last_error("ga_extend_batch_noalloc: more than 4096 extensions in one call (the limit of its fixed scratch)");
-        return GA_ERR_ARGUMENT;
-    }
-    int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64)
-    {
-        ga_set_last_error("ga_extend_batch_noalloc: no current CUDA device (or ordinal above 63)");
-        return GA_ERR_CUDA;
-    }
-    // once per device, with that device current: the device address of the scratch
-    // array (its host-side name is not a device address) and the IUPAC table
-    static void* scratchAddress[64] = {};
-    if (!scratchAddress[device])
-    {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
-        {
-            ga_set_last_error("ga_extend_batch_noalloc: cudaGetSymbolAddress of the scratch array failed");
-            return GA_ERR_CUDA;
-        }
-        if (ga_upload_tables() != 0)
-        {
-            ga_set_last_error("ga_extend_batch_noalloc: loading the IUPAC table failed");
-            return GA_ERR_CUDA;
-        }
-        scratchAddress[device] = p;
-    }
-    uint8_t* scratch = (uint8_t*)scratchAddress[device];
-    cudaStream_t s = (cudaStream_t)stream;
-    // the batch must fit the arena: read the lengths back into a fixed host buffer
-    static thread_local uint32_t lengths[kNoAllocMaxExtensions];
-    if (cudaMemcpyAsync(lengths, device_batch->seq_len, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess
-        || cudaStreamSynchronize(s) != cudaSuccess)
-    {
-        ga_set_last_error("ga_extend_batch_noalloc: reading the sequence lengths back failed");
-        return GA_ERR_CUDA;
-    }
-    u64 totalBp = 0;
-    for (u32 i = 0; i < n; i++) totalBp += lengths[i];
-    if (totalBp > kNoAllocMaxReadBp)
-    {
-        ga_set_last_error("ga_extend_batch_noalloc: more than 8,000,000 read bp in one call (the limit of its fixed scratch)");
-        return GA_ERR_ARGUMENT;
-    }
-
-    Caps caps;
-    caps.band = 32;
-    caps.hash = 128;
-    caps.heap = 32;
-    caps.extras = 64;
-    const u64 stride = ga_workspace_bytes(caps);
-    const u64 workspaceBytes = stride * kNoAllocThreads;
-    uint8_t* workspace = scratch + kNoAllocHeaderBytes;
-    uint8_t* arena = workspace + workspaceBytes;
-    const u64 arenaBytes = kNoAllocScratchBytes - kNoAllocHeaderBytes - workspaceBytes;
-    // every call starts from zeroed counters and tables: the array keeps what the
-    // previous call left in it
-    if (cudaMemsetAsync(scratch, 0, kNoAllocHeaderBytes + workspaceBytes, s) != cudaSuccess)
-    {
-        ga_set_last_error("ga_extend_batch_noalloc: clearing the scratch tables failed");
-        return GA_ERR_CUDA;
-    }
-
-    DevGraph g;
-    g.N = device_graph->num_nodes;
-    g.firstAmbiguous = device_graph->first_ambiguous;
-    g.len = device_graph->node_length;
-    g.seq2 = device_graph->seq2bit;
-    g.seqAmb = device_graph->seq_ambiguous;
-    g.inOff = device_graph->in_offsets;
-    g.inNb = device_graph->in_neighbors;
-    g.outOff = device_graph->out_offsets;
-    g.outNb = device_graph->out_neighbors;
-    g.lin = device_graph->linearizable;
-    g.comp = device_graph->component;
-
-    FillArgs fa {};
-    fa.g = g;
-    fa.bandwidth = params->bandwidth;
-    fa.xdrop = params->xdrop;
-    fa.maxCells = params->max_cells_per_slice;
-    fa.cost = params->xscore_error_cost;
-    fa.num = n;
-    fa.order = nullptr;
-    fa.seq = device_batch->seq;
-    fa.seqOff = device_batch->seq_offset;
-    fa.seqLen = device_batch->seq_len;
-    fa.startNode = device_batch->start_node;
-    fa.startOffset = device_batch->start_offset;
-    fa.arena = arena;
-    fa.arenaBytes = arenaBytes;
-    fa.arenaCursor = (unsigned long long*)(scratch + 8);
-    fa.workspace = workspace;
-    fa.workspaceStride = stride;
-    fa.caps = caps;
-    fa.prevStatus = nullptr;
-
-    TraceArgs ta {};
-    ta.g = g;
-    ta.cost = params->xscore_error_cost;
-    ta.num = n;
-    ta.order = nullptr;
-    ta.seq = device_batch->seq;
-    ta.seqOff = device_batch->seq_offset;
-    ta.seqLen = device_batch->seq_len;
-    ta.arena = arena;
-    ta.traceOffset = device_batch->trace_offset;
-    ta.traceCap = device_batch->trace_capacity;
-    ta.status = device_results->status;
-    ta.score = device_results->score;
-    ta.traceLen = device_results->trace_len;
-    ta.traceItems = device_results->trace_items;
-    ta.cellSteps = device_results->cell_steps;
-    ta.prevStatus = nullptr;
-
-    extend_kernel_noalloc<<<kNoAllocThreads / 128, 128, 0, s>>>(fa, ta, (u32*)scratch);
-    if (cudaGetLastError() != cudaSuccess)
-    {
-        ga_set_last_error("ga_extend_batch_noalloc: kernel launch failed");
-        return GA_ERR_CUDA;
-    }
-    return GA_OK;
 }

@@ -1,4 +1,4 @@
-// Shared declarations of the batched seed-extension kernels (fill + traceback).
+// Shared declarations of the batched seed-extension kernel (fill + traceback, one warp per extension).
 #pragma once
 #include <stdint.h>
 #include "wordslice.cuh"
@@ -24,7 +24,7 @@ struct DevGraph
 
 // One band entry: the state of a <= 64 bp node for one 64-row slice
 // (NodeSliceMapItemStruct, NodeSlice.h:15-47).  64 bytes.
-struct Item
+struct __align__(16) Item
 {
     u64 sVP, sVN;          // first column
     u64 eVP, eVN;          // last column
@@ -36,25 +36,21 @@ struct Item
 static constexpr u32 kExists = 0x80000000u;
 static constexpr u32 kNodeMask = 0x7fffffffu;
 
-// A committed DP slice in the per-batch arena: SliceRec (one 64-byte line), then count
-// Items, then hashCap uint16 slots (band index + 1, 0 = empty) keyed by node when the
-// band is larger than kInlineIds nodes.
-static constexpr u32 kInlineIds = 8;
-
-struct SliceRec
+// A committed DP slice in the arena: this 32-byte record, then the band's node ids
+// (count u32, padded to 16 bytes), then count Items, all in first-pop order.  The
+// traceback finds a node's entry by a warp ballot over the ids.
+struct __align__(16) SliceRec
 {
     i32 minScore;
     i32 quit;              // minScore + bandwidth (the slice's band quit score)
     i32 maxX;              // maxExactEndposScore
     u32 maxXNode;          // maxExactEndposNode
     u32 count;
-    u32 hashCap;           // 0 when count <= kInlineIds (the ids below are the index)
     u32 notValid;          // scoresNotValid: the tangle-effort cap was hit
-    u32 pad;
-    u32 ids[kInlineIds];   // node of band entry k, for bands of up to kInlineIds nodes
+    u32 pad0, pad1;
 };
 
-// Per-extension state passed from the fill kernel to the traceback kernel.
+// Per-extension state passed from the fill to the traceback.
 struct ExtState
 {
     u64 dir;               // arena offset of the slice directory (u64 record offsets)
@@ -63,12 +59,13 @@ struct ExtState
     u64 steps;             // Myers column steps in the fill
 };
 
+// Capacities of one warp's frontier tables.
 struct Caps
 {
-    u32 band;              // BCAP: band entries per slice
-    u32 hash;              // HCAP: build-hash slots (power of two)
-    u32 heap;              // QCAP: heap entries
-    u32 extras;            // ECAP: pending incoming edges per slice
+    u32 band;              // band entries per slice
+    u32 hash;              // node-table slots per slice (power of two, >= 32)
+    u32 heap;              // heap entries
+    u32 extras;            // pending incoming columns per slice
 };
 
 struct FillArgs
@@ -79,17 +76,19 @@ struct FillArgs
     u64 maxCells;
     i32 cost;
     u32 num;
-    const u32* order;      // processing order (longest first)
+    const u32* order;      // processing order (longest first); nullptr = index order
     const uint8_t* seq;
     const u64* seqOff;
     const u32* seqLen;
     const u32* startNode;
     const u32* startOffset;
-    uint8_t* arena;
+    uint8_t* arena;        // per-warp regions [0, overflowBase), then the shared overflow
     u64 arenaBytes;
-    unsigned long long* arenaCursor;
-    uint8_t* workspace;
-    u64 workspaceStride;
+    unsigned long long* arenaCursor;   // [0] overflow bytes handed out, [1] bytes the warps took (both start at 0)
+    u64 regionBytes;       // DP-table region of each warp, reused extension after extension
+    u64 overflowBase;      // warps * regionBytes
+    uint8_t* workspace;    // nullptr: the frontier tables live in shared memory
+    u64 workspaceStride;   // bytes of one warp's tables
     Caps caps;
     const i32* prevStatus; // when non-null, only extensions whose previous status is GA_CAPACITY run
 };
@@ -98,8 +97,6 @@ struct TraceArgs
 {
     DevGraph g;
     i32 cost;
-    u32 num;
-    const u32* order;
     const uint8_t* seq;
     const u64* seqOff;
     const u32* seqLen;
@@ -111,14 +108,16 @@ struct TraceArgs
     u32* traceLen;
     u64* traceItems;
     u64* cellSteps;
-    const i32* prevStatus;
 };
 
 }
 
-void ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, const uint32_t* chunks, uint32_t numChunks,
-    uint32_t* counter, uint32_t slotBase, uint32_t slotLimit, int grid, int block, void* stream);
-int ga_extend_occupancy(int block);
+// bytes of one warp's frontier tables for these capacities
+uint64_t ga_warp_tables_bytes(const gadev::Caps& caps);
+// resident blocks of 32 * warpsPerBlock threads per SM; shared: tables in shared memory
+int ga_extend_blocks_per_sm(int warpsPerBlock, const gadev::Caps& caps, bool shared);
+// launches the extension kernel: `blocks` blocks of warpsPerBlock warps, one extension per warp at a time
+int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counter, int blocks, int warpsPerBlock,
+    void* stream);
 int ga_upload_tables();
 void ga_set_last_error(const char* message);
-uint64_t ga_workspace_bytes(const gadev::Caps& caps);

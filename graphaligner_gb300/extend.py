@@ -170,26 +170,28 @@ class DeviceGraph:
 
 
 class LaunchShape(ctypes.Structure):
-    """ga_launch_shape: how the longest-first order is cut into warp chunks (which extensions
-    share a warp; results never depend on it)."""
+    """ga_launch_shape: how the extension kernel is launched (one warp per extension; results
+    never depend on it): warps per block, resident blocks per SM (0 = as many as fit), the
+    first pass's frontier-table layout (0 shared memory, 1/2 global memory) and the per-warp
+    DP-table region in KiB."""
     _fields_ = [
-        ("single_factor", ctypes.c_double),
-        ("single_min_bp", ctypes.c_uint32),
-        ("single_per_sm", ctypes.c_uint32),
-        ("mid_factor", ctypes.c_double),
-        ("mid_lanes", ctypes.c_uint32),
-        ("bulk_lanes", ctypes.c_uint32),
+        ("warps_per_block", ctypes.c_uint32),
+        ("blocks_per_sm", ctypes.c_uint32),
+        ("first_layout", ctypes.c_uint32),
+        ("region_kib", ctypes.c_uint32),
     ]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
+    def as_tuple(self):
+        return tuple(getattr(self, n) for n, _ in self._fields_)
 
-# launch shapes the autotuner tries: (single_factor, single_per_sm, mid_factor, mid_lanes, bulk_lanes)
+
+# launch shapes the autotuner tries: (warps_per_block, blocks_per_sm, first_layout, region_kib)
 DEFAULT_CANDIDATES = [
-    (2.0, 12, 1.0, 16, 16), (3.0, 12, 1.0, 16, 16), (2.0, 12, 1.0, 8, 8), (2.0, 12, 1.3, 8, 16),
-    (2.0, 16, 1.3, 8, 32), (2.0, 12, 1.3, 4, 16), (2.0, 12, 1.5, 4, 8), (1.5, 16, 1.2, 8, 16),
-    (2.5, 12, 1.3, 8, 16), (2.0, 12, 1.0, 32, 32),
+    (4, 0, 0, 128), (2, 0, 0, 128), (1, 0, 0, 128), (4, 3, 0, 128), (4, 2, 0, 128),
+    (4, 0, 0, 32), (4, 0, 0, 512), (4, 0, 1, 128),
 ]
 
 
@@ -218,8 +220,8 @@ class Extender:
         check(lib().ga_extender_get_launch_shape(self.handle, ctypes.byref(sh)))
         return sh
 
-    def set_launch_shape(self, single_factor=2.0, single_per_sm=12, mid_factor=1.0, mid_lanes=16, bulk_lanes=16, single_min_bp=2048):
-        sh = LaunchShape(single_factor, single_min_bp, single_per_sm, mid_factor, mid_lanes, bulk_lanes)
+    def set_launch_shape(self, warps_per_block=4, blocks_per_sm=0, first_layout=0, region_kib=128):
+        sh = LaunchShape(warps_per_block, blocks_per_sm, first_layout, region_kib)
         check(lib().ga_extender_set_launch_shape(self.handle, ctypes.byref(sh)))
 
     def autotune(self, params: ExtendParams, batch: PackedBatch, candidates=None, sample_every: int = 4, repeats: int = 2) -> dict:
@@ -230,8 +232,8 @@ class Extender:
         sub = batch.subset(idx)
         cands = list(candidates or DEFAULT_CANDIDATES)
         shapes = (LaunchShape * len(cands))()
-        for i, (sf, sps, mf, ml, bl) in enumerate(cands):
-            shapes[i] = LaunchShape(sf, 2048, sps, mf, ml, bl)
+        for i, c in enumerate(cands):
+            shapes[i] = LaunchShape(*c)
         ms = (ctypes.c_float * len(cands))()
         p = params.c()
         d = sub.desc()
@@ -245,6 +247,12 @@ class Extender:
         t = ctypes.c_float()
         check(lib().ga_extender_last_times(self.handle, ctypes.byref(f), ctypes.byref(t)))
         return f.value, t.value
+
+    def last_layout_counts(self):
+        """Extensions run with each frontier-table layout (0, 1, 2) by the last call."""
+        c = (ctypes.c_uint32 * 3)()
+        check(lib().ga_extender_last_layout_counts(self.handle, c))
+        return [int(v) for v in c]
 
     def last_launches(self) -> int:
         n = ctypes.c_uint32()

@@ -118,7 +118,7 @@ int ga_graph_free(ga_graph_t graph);
 /* ---- batched extension ---- */
 typedef struct ga_extender* ga_extender_t;
 /* The device side of the per-thread AlignerGraphsizedState
- * (src/GraphAlignerCommon.h:52-81), for a whole batch: per-thread frontier tables and
+ * (src/GraphAlignerCommon.h:52-81), for a whole batch: per-warp frontier tables and
  * the DP-table arena.  arena_bytes: device bytes for per-extension DP tables; 0 = 4 GiB. */
 int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out);
 /* A second extender on the same device graph with the same arena size and launch shape
@@ -134,8 +134,8 @@ int ga_extend_batch(ga_extender_t ext, const ga_extend_params* params,
 /* Device-resident variant: every pointer in batch/results is a device pointer.
  * Work is enqueued on `stream` (a cudaStream_t; NULL = the extender's stream);
  * the call reads the lengths back once to order the work and waits for the
- * kernels, because extensions that outgrow the first pass's per-thread
- * capacities are re-run with larger capacities before it returns. */
+ * kernels, because extensions that outgrow the first pass's frontier tables
+ * are re-run with larger tables before it returns. */
 int ga_extend_batch_device(ga_extender_t ext, const ga_extend_params* params,
                            const ga_extend_batch_desc* batch, ga_extend_results* results,
                            void* stream);
@@ -143,17 +143,22 @@ int ga_extend_batch_device(ga_extender_t ext, const ga_extend_params* params,
  * device memory, for callers that cannot call cudaMalloc while they extend
  * (device memory owned by another allocator under a fixed budget, or request
  * paths that cannot afford cudaMalloc's device-wide synchronisation).
- * device_graph, device_batch and device_results hold device pointers.  The
- * scratch (frontier tables and DP-table arena) is a 128 MiB device array inside
- * this library, kept by every GPU that loads it until the process exits.
- * Limits per call: 4096 extensions and 8,000,000 read bp in total; larger
- * batches return GA_ERR_ARGUMENT.  Extensions that outgrow the fixed per-thread
- * tables report GA_CAPACITY (there is no retry).  The first call on a device
- * looks up the array's device address and loads a constant table; make that
- * first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU (other streams, other host threads) race.  The call
- * waits for the length read-back on `stream`, then enqueues the kernel there
- * and returns. */
+ * device_graph, device_batch and device_results hold device pointers; a NULL
+ * array in any of them is GA_ERR_ARGUMENT.  The frontier tables live in shared
+ * memory; the other scratch (counters and the DP-table arena) is a 128 MiB
+ * device array inside this library, kept by every GPU that loads it until the
+ * process exits.  Limits per call: 4096 extensions and 8,000,000 read bp in
+ * total; larger batches return GA_ERR_ARGUMENT.  Extensions whose band or
+ * frontier outgrows the shared-memory tables report GA_CAPACITY (there is no
+ * retry with larger tables); so do extensions that find the arena exhausted,
+ * which depends on what else the batch holds (on variation graphs the tables
+ * take about 5 bytes per read bp, far below the arena at the bp limit).  The
+ * first call on a device looks up the array's device address and loads a
+ * constant table (once per device, safe from several host threads).  Every
+ * call reads the lengths back and waits for `stream` before it enqueues the
+ * kernel there, so no call can be made inside a stream capture.  All calls
+ * share the array: calls that overlap on the GPU (other streams, other host
+ * threads) race. */
 int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const ga_extend_params* params,
                             const ga_extend_batch_desc* device_batch, ga_extend_results* device_results,
                             void* stream);
@@ -170,23 +175,27 @@ int ga_extender_last_copy_ms(ga_extender_t ext, float* h2d_ms, float* d2h_ms);
 /* Number of kernel launches made by the last ga_extend_batch* call. */
 int ga_extender_last_launches(ga_extender_t ext, uint32_t* launches);
 
-/* How a batch's longest-first order is cut into warp chunks (no reference
- * counterpart: it only decides which extensions share a warp, never a result).
- * The longest extensions -- at least single_factor x the median length and over
- * single_min_bp, at most single_per_sm per SM -- run one per warp; then those of at
- * least mid_factor x the median run mid_lanes per warp; the rest bulk_lanes per warp. */
+/* How the extension kernel is launched (no reference counterpart: it never changes a
+ * result).  One warp runs one extension at a time, taking the next of the batch's
+ * longest-first order.  warps_per_block (1..4) warps share a block; blocks_per_sm
+ * caps the resident blocks per SM (0 = as many as registers and shared memory allow).
+ * first_layout picks the frontier tables of the first pass: 0 = small tables in
+ * shared memory (variation graphs), 1 = medium tables in global memory, 2 = large
+ * tables in global memory (tangled de Bruijn graphs); extensions that outgrow them
+ * (GA_CAPACITY) run again with the next layout.  region_kib: each warp's DP-table
+ * region in the arena, reused extension after extension (longer tables continue in
+ * the arena's shared overflow). */
 typedef struct ga_launch_shape {
-    double   single_factor;
-    uint32_t single_min_bp;
-    uint32_t single_per_sm;
-    double   mid_factor;
-    uint32_t mid_lanes;               /* 1..32 */
-    uint32_t bulk_lanes;              /* 1..32 */
+    uint32_t warps_per_block;
+    uint32_t blocks_per_sm;
+    uint32_t first_layout;
+    uint32_t region_kib;
 } ga_launch_shape;
 int ga_extender_set_launch_shape(ga_extender_t ext, const ga_launch_shape* shape);
 int ga_extender_get_launch_shape(ga_extender_t ext, ga_launch_shape* shape);
 /* Times `count` launch shapes on a host batch and makes the fastest the extender's
- * shape (no reference counterpart).  The batch is copied to the device once; each
+ * shape (no reference counterpart; the autotuner over warps per block, resident
+ * blocks, first table layout and DP-table region).  The batch is copied to the device once; each
  * shape runs `repeats` times there (kernel time by CUDA events, the median kept) and
  * only statuses and scores come back: no trace is copied to the host.  Every shape
  * must reproduce the first one's statuses and scores, else GA_ERR_STATE and the first
@@ -194,8 +203,10 @@ int ga_extender_get_launch_shape(ga_extender_t ext, ga_launch_shape* shape);
 int ga_extender_autotune(ga_extender_t ext, const ga_extend_params* params,
                          const ga_extend_batch_desc* batch, const ga_launch_shape* shapes,
                          uint32_t count, uint32_t repeats, float* ms_out);
-/* DP-table bytes the first fill pass of the last call wrote to the arena. */
+/* DP-table bytes the first pass of the last call wrote to the arena. */
 int ga_extender_last_arena_bytes(ga_extender_t ext, uint64_t* bytes);
+/* Extensions run with each table layout (0, 1, 2) by the last call (0 = layout not run). */
+int ga_extender_last_layout_counts(ga_extender_t ext, uint32_t counts[3]);
 
 /* ---- utilities (no reference counterpart) ---- */
 /* Page-locked host memory for the host-buffer entry points. */

@@ -17,7 +17,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libga_oracle.so")
 SRC = os.path.join(HERE, "ga_oracle.cpp")
 REF_BIN = os.path.join(HERE, "_ref", "ga_ref")
-REFERENCE_SRC = "/root/reference/src"
+# the GraphAligner checkout whose src/ the Makefile compiles (GA_REFERENCE overrides the default)
+REFERENCE_ROOT = os.environ.get("GA_REFERENCE", "/root/reference")
+REFERENCE_SRC = os.path.join(REFERENCE_ROOT, "src")
 
 _lib = None
 
@@ -31,7 +33,7 @@ def build(reference: bool = True) -> str:
         subprocess.run(["g++", "-std=c++17", "-O3", "-shared", "-fPIC", "-o", tmp, SRC, "-lpthread"], check=True)
         os.replace(tmp, LIB)
     if reference and os.path.isdir(REFERENCE_SRC):
-        subprocess.run(["make", "-s", "-C", HERE, "-j8"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "-j8", f"GA_REFERENCE={REFERENCE_ROOT}"], check=True)
     return LIB
 
 

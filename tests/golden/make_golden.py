@@ -1,7 +1,8 @@
 """Regenerates the golden vectors in this directory from the REFERENCE itself.
 
 Runs oracle/_ref/ga_ref — GraphAligner's own hot-path source compiled by
-oracle/Makefile from /root/reference/src with dependency shims — on seeded
+oracle/Makefile from the reference checkout's src/ (GA_REFERENCE, default
+/root/reference) with dependency shims — on seeded
 synthetic inputs and stores what it produced:
 
   *_graph.gag.gz   the reference-built AlignmentGraph (GAG1 layout)
@@ -20,7 +21,7 @@ synthetic inputs and stores what it produced:
 The packed item layout is the one include/graphaligner_gb300.h documents, so
 the oracle restatement and the GPU kernels are compared byte for byte.
 
-Usage: python tests/golden/make_golden.py   (needs /root/reference; run in the build container)
+Usage: [GA_REFERENCE=<GraphAligner checkout>] python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -192,7 +193,7 @@ def main():
     g_iu, ext_iu = iupac_edge_set(5)
     make_set("iupac20k", g_iu, ext_iu, [10, 5])
     # the reference's quickstart
-    ref_test = "/root/reference/test"
+    ref_test = os.path.join(os.environ.get("GA_REFERENCE", "/root/reference"), "test")
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "aln.gaf")
         subprocess.run([REF, "align", os.path.join(ref_test, "graph.gfa"), os.path.join(ref_test, "read.fa"), out, "vg"], check=True)

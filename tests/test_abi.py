@@ -53,6 +53,7 @@ def test_null_arguments_are_rejected_before_any_device_call(cuda_lib):
         "ga_extender_get_launch_shape": (n, n),
         "ga_extender_autotune": (n, n, n, n, 0, 0, n),
         "ga_extender_last_arena_bytes": (n, n),
+        "ga_extender_last_layout_counts": (n, n),
         "ga_aligner_create": (n, n, n, n),
         "ga_align_reads": (n, 0, n, n, n, n),
         "ga_aligner_gaf": (n, n, n),
@@ -88,3 +89,20 @@ def test_host_graph_desc_points_at_every_node_name():
     g.names = ["a", "", "node 3"] + list(g.names[3:])
     d = HostGraphDesc.from_graph(g)
     assert [d.names[i].decode() for i in range(3)] == ["a", "", "node 3"]
+
+
+def test_noalloc_rejects_null_arrays_before_any_device_call(cuda_lib):
+    """ga_extend_batch_noalloc with descriptions whose arrays are NULL (num > 0) answers
+    GA_ERR_ARGUMENT with a message instead of handing NULL to the kernel."""
+    from graphaligner_gb300 import _abi
+    L = cuda_lib
+    L.ga_last_error.restype = ctypes.c_char_p
+    g = _abi.GraphDesc()
+    g.num_nodes = 4
+    b = _abi.BatchDesc()
+    b.num = 3
+    r = _abi.Results()
+    p = _abi.ExtendParams(10, 14705, 2**64 - 1, 294)
+    rc = L.ga_extend_batch_noalloc(ctypes.byref(g), ctypes.byref(p), ctypes.byref(b), ctypes.byref(r), None)
+    assert rc == GA_ERR_ARGUMENT
+    assert b"null array" in L.ga_last_error()

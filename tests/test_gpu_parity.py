@@ -95,31 +95,49 @@ def test_gpu_matches_oracle_generated(cuda_lib, oracle_lib):
 
 
 def test_launch_shapes_do_not_change_results(cuda_lib):
-    """Which extensions share a warp never changes a result: every chunking of the
-    longest-first order gives the reference's digests."""
+    """How the kernel is launched never changes a result: every launch shape (warps per block,
+    resident blocks, first table layout, DP-table region, including regions so small that every
+    table continues in the shared overflow) gives the reference's digests."""
     from graphaligner_gb300._lib import GAError
     g, batch = golden_case("vg50k")
     x = Extender(DeviceGraph(g))
     expected = load_digests("vg50k", 10)
-    for shape in [(2.0, 12, 1.0, 16, 16), (0.5, 64, 1.0, 1, 1), (1.0, 1, 0.5, 3, 32), (100.0, 1, 1.5, 32, 7)]:
+    for shape in [(4, 0, 0, 128), (1, 1, 0, 128), (2, 0, 1, 64), (3, 2, 2, 8), (4, 0, 0, 0)]:
         x.set_launch_shape(*shape)
         res = x.run(ExtendParams(bandwidth=10), batch)
         bad = compare(res, expected)
         assert not bad, f"shape {shape}: {len(bad)} extensions differ"
     with pytest.raises(GAError):
-        x.set_launch_shape(2.0, 12, 1.0, 0, 16)
+        x.set_launch_shape(0, 0, 0, 128)
     with pytest.raises(GAError):
-        x.set_launch_shape(2.0, 12, 1.0, 16, 33)
-    cands = [(2.0, 12, 1.0, 16, 16), (0.5, 64, 1.0, 1, 1), (100.0, 1, 1.5, 32, 7)]
+        x.set_launch_shape(5, 0, 0, 128)
+    with pytest.raises(GAError):
+        x.set_launch_shape(4, 0, 3, 128)
+    cands = [(4, 0, 0, 128), (1, 0, 0, 16), (2, 2, 1, 128)]
     tuned = x.autotune(ExtendParams(bandwidth=10), batch, candidates=cands, sample_every=2, repeats=1)
     assert len(tuned["candidates_ms"]) == len(cands) and all(ms > 0 for ms, _ in tuned["candidates_ms"])
     best_ms = min(ms for ms, _ in tuned["candidates_ms"])
-    ch = tuned["chosen"]
-    chosen = (ch["single_factor"], ch["single_per_sm"], ch["mid_factor"], ch["mid_lanes"], ch["bulk_lanes"])
+    chosen = tuple(tuned["chosen"].values())
     assert chosen in [tuple(c) for ms, c in tuned["candidates_ms"] if ms == best_ms]
     assert not compare(x.run(ExtendParams(bandwidth=10), batch), expected)
     with pytest.raises(GAError):
-        x.autotune(ExtendParams(bandwidth=10), batch, candidates=[(2.0, 12, 1.0, 16, 40)])
+        x.autotune(ExtendParams(bandwidth=10), batch, candidates=[(8, 0, 0, 128)])
+
+
+def test_table_layouts_agree_on_dbg(cuda_lib):
+    """The de Bruijn set outgrows the shared-memory tables: whichever layout a run starts with,
+    the extensions that overflow are re-run with larger tables and every digest is the reference's."""
+    g, batch = golden_case("dbg100k")
+    x = Extender(DeviceGraph(g))
+    expected = load_digests("dbg100k", 10)
+    p = ExtendParams(bandwidth=10, max_cells_per_slice=MAX_CELLS["dbg100k"])
+    for layout in (0, 1, 2):
+        x.set_launch_shape(4, 0, layout, 128)
+        res = x.run(p, batch)
+        bad = compare(res, expected)
+        assert not bad, f"first layout {layout}: {len(bad)} extensions differ"
+        counts = x.last_layout_counts()
+        assert counts[layout] == batch.num and all(c == 0 for c in counts[:layout])
 
 
 @pytest.mark.parametrize("bandwidth", [10, 5])
