@@ -197,7 +197,7 @@ __device__ __forceinline__ void load_iupac_table()
 // Match masks of the 64 rows starting at read position j (getEqVector, Common.h:279-318):
 // lane k reads rows k and k + 32 and the masks come from ballots.  False when a row holds
 // a non-sequence byte, or a gap inside a full 64-row window (the reference asserts).
-__device__ __forceinline__ bool eq_vector(const uint8_t* seq, u32 len, int64_t j, EqV4& eq, u32 lane)
+__device__ __noinline__ bool eq_vector(const uint8_t* seq, u32 len, int64_t j, EqV4& eq, u32 lane)
 {
     const bool full = j + 64 <= (int64_t)len;
     int m0 = 0, m1 = 0;
@@ -241,6 +241,80 @@ __device__ __forceinline__ bool char_match(const DevGraph& g, uint8_t c, u32 n, 
     return (a & b) != 0;
 }
 
+// ---------------------------------------------------------------- warp column algebra
+//
+// A column's scores at rows lane and lane + 32 are two prefix popcounts away from its
+// row-above score.  With them the cellwise operations take one shuffle, ballot or
+// reduction step instead of the bit walks of WordSlice::differenceMasksBitTwiddle
+// (WordSlice.h:566-664), whose trip counts depend on the data.  They return exactly what
+// ws_merge (mergeTwoSlices: the cellwise minimum) and ws_changed_min
+// (changedMinScoreLocalMinima: the least score among rows, and the row above, where the
+// column improved on the old one) return for valid columns.  Scores beyond +-2^29 take
+// the sequential forms, so no sum here can wrap.
+
+static constexpr i32 kWarpScoreLimit = 1 << 29;
+
+__device__ __forceinline__ bool score_ok(i32 v) { return v > -kWarpScoreLimit && v < kWarpScoreLimit; }
+
+// scores of rows lane and lane + 32 (WordSlice::getValue)
+__device__ __forceinline__ void ws_rows(const WS& w, i32 before, u32 lane, i32& v0, i32& v1)
+{
+    const u32 upto = (2u << lane) - 1u;
+    const u32 vpl = (u32)w.VP, vnl = (u32)w.VN;
+    const i32 low = popc32(vpl) - popc32(vnl);
+    v0 = before + popc32(vpl & upto) - popc32(vnl & upto);
+    v1 = before + low + popc32((u32)(w.VP >> 32) & upto) - popc32((u32)(w.VN >> 32) & upto);
+}
+
+// a column from its row-above score and its scores at rows lane and lane + 32
+__device__ __forceinline__ WS ws_from_rows(i32 before, i32 m0, i32 m1, u32 lane)
+{
+    i32 p0 = __shfl_up_sync(kFull, m0, 1);
+    i32 p1 = __shfl_up_sync(kFull, m1, 1);
+    const i32 m31 = __shfl_sync(kFull, m0, 31);
+    if (lane == 0)
+    {
+        p0 = before;
+        p1 = m31;
+    }
+    const i32 d0 = m0 - p0, d1 = m1 - p1;
+    WS r;
+    r.VP = (u64)__ballot_sync(kFull, d0 == 1) | ((u64)__ballot_sync(kFull, d1 == 1) << 32);
+    r.VN = (u64)__ballot_sync(kFull, d0 == -1) | ((u64)__ballot_sync(kFull, d1 == -1) << 32);
+    r.end = __shfl_sync(kFull, m1, 31);
+    return r;
+}
+
+__device__ __noinline__ WS merge_seq(WS a, WS b) { return ws_merge(a, b); }
+__device__ __noinline__ i32 changed_min_seq(WS w, WS old) { return ws_changed_min(w, old); }
+
+// mergeTwoSlices (WordSlice.h:502-541) across the lanes
+__device__ __forceinline__ WS merge_w(const WS& a, const WS& b, u32 lane)
+{
+    const i32 ba = ws_before(a), bb = ws_before(b);
+    if (!(score_ok(ba) && score_ok(bb) && score_ok(a.end) && score_ok(b.end))) return merge_seq(a, b);
+    i32 a0, a1, b0, b1;
+    ws_rows(a, ba, lane, a0, a1);
+    ws_rows(b, bb, lane, b0, b1);
+    return ws_from_rows(imin(ba, bb), imin(a0, b0), imin(a1, b1), lane);
+}
+
+// changedMinScoreLocalMinima (WordSlice.h:438-472) across the lanes; old may be the
+// never-computed column (0, 0, INT32_MAX), whose every score is INT32_MAX
+__device__ __forceinline__ i32 changed_min_w(const WS& w, const WS& old, u32 lane)
+{
+    const i32 bw = ws_before(w), bo = ws_before(old);
+    const bool oldUnset = old.VP == 0 && old.VN == 0 && old.end == kIntMax;
+    if (!(score_ok(bw) && score_ok(w.end) && (oldUnset || (score_ok(bo) && score_ok(old.end))))) return changed_min_seq(w, old);
+    i32 w0, w1, o0, o1;
+    ws_rows(w, bw, lane, w0, w1);
+    ws_rows(old, bo, lane, o0, o1);
+    i32 best = bw < bo ? bw : kIntMax;
+    if (w0 < o0) best = imin(best, w0);
+    if (w1 < o1) best = imin(best, w1);
+    return __reduce_min_sync(kFull, best);
+}
+
 struct NodeCalc
 {
     i32 minScore;
@@ -271,13 +345,70 @@ __device__ __forceinline__ int64_t xscore_bound(const WS& w, i32 seqOffset, i32 
 // above also bounds the reference's (wrapping) arithmetic.
 static constexpr i32 kXBoundOffsetLimit = 10000000;
 
+// The part of calculateNodeInner (Common.h:1209-1300) that runs when the node already
+// has a column in this slice: merge the new first column into it.  Returns true when the
+// reference leaves the node early (nothing changed).  Out of line: a node is computed
+// again within a slice only inside cyclic components.
+__device__ __noinline__ bool merge_existing(WS& ws, const Item& slice, bool hasSkipless, bool singleInEdge, u32 lane)
+{
+    WS s = ws_make(slice.sVP, slice.sVN, slice.sEnd);
+    if (hasSkipless && singleInEdge)
+    {
+        if (ws.end > s.end) return true;
+        if (ws.end < s.end) return false;
+        u64 newBigger = (ws.VP & ~s.VP) | (s.VN & ~ws.VN);
+        u64 oldBigger = (s.VP & ~ws.VP) | (ws.VN & ~s.VN);
+        if (newBigger > oldBigger) return false;
+        if (oldBigger > newBigger) return true;
+        if (newBigger == 0 && oldBigger == 0) return true;
+        WS t = merge_w(ws, s, lane);
+        if (ws_eq(t, s)) return true;
+        ws = t;
+        return false;
+    }
+    WS t = merge_w(ws, s, lane);
+    // the reference compares test.VP against the stored VN here (Common.h:1282)
+    if (t.end == s.end && t.VP == s.VP && t.VP == s.VN) return true;
+    ws = t;
+    return false;
+}
+
+// The horizontal input along the slice's first row when the column enters below the
+// previous slice's last row (Common.h:1310-1343): fixedHP/HN and the rows whose first
+// cell is forced.  False where the reference asserts.  Out of line: rarely taken.
+__device__ __noinline__ bool fix_horizontal(i32 scoreBefore, i32 scoreComparison, u64& fixedHP, u64& fixedHN, u64& forceMask)
+{
+    forceMask |= 1;
+    for (int off = 1; off < 64; off++)
+    {
+        i32 next = scoreComparison + (i32)((fixedHP >> off) & 1) - (i32)((fixedHN >> off) & 1);
+        u64 mask = 1ULL << off;
+        if (scoreBefore > next) return false;
+        if (scoreBefore < next)
+        {
+            fixedHP |= mask;
+            fixedHN &= ~mask;
+            forceMask |= mask;
+        }
+        else
+        {
+            fixedHP &= ~mask;
+            fixedHN &= ~mask;
+        }
+        scoreBefore++;
+        scoreComparison = next;
+        if (scoreBefore >= scoreComparison) break;
+    }
+    return true;
+}
+
 // calculateNodeInner (Common.h:1113-1478) with the single-seed fake extra slice.
 // Fill = true: the slice fill (early leave allowed, calculateNodeClipPrecise).
 // Fill = false: recalcNodeWordslice (no early leave); columns 0..lastColumn land in cols.
 // The column loop runs the Myers recurrence warp-uniformly and records every column; the
 // per-column minimum, X-score and horizontal output bits are then taken across the lanes.
 template <bool Fill>
-__device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const EqV4& eqv, const PrevInfo& prev,
+__device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const EqV4& eqv, const PrevInfo& prev,
     const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, Col* cols, u64* eqcol,
     u64& steps, int& err, u32 lane, i32 sliceMaxX = kIntMin, u32 lastColumn = 63)
 {
@@ -302,6 +433,7 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
         const u64* a = g.seqAmb + (u64)(i - g.firstAmbiguous) * 4;
         a0 = a[0]; a1 = a[1]; a2 = a[2]; a3 = a[3];
     }
+    const u32 inDeg = g.inOff[i + 1] - g.inOff[i];
     // the match mask of every column (lane k: columns k and k + 32)
     __syncwarp();
     for (u32 pos = lane; pos < nodeLength; pos += 32)
@@ -332,7 +464,7 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
             result.cells++;
             if (inc.skip)
             {
-                ws = hasWs ? ws_merge(ws, incWs) : incWs;
+                ws = hasWs ? merge_w(ws, incWs, lane) : incWs;
                 hasWs = true;
                 continue;
             }
@@ -350,68 +482,25 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
                 nw.VP &= kAllOnes ^ 1;
                 nw.VN |= 1;
             }
-            ws = hasWs ? ws_merge(ws, nw) : nw;
+            ws = hasWs ? merge_w(ws, nw, lane) : nw;
             hasWs = true;
         }
     }
     if (!hasWs) { err = GA_ASSERT; return result; }
+    // column 0 as the incoming columns make it: the node's first minimum candidate and,
+    // with every row a candidate, its first X-score
+    const WS ws0 = ws;
     result.minScore = ws.end;
     result.minScoreNode = i;
     result.minScoreOffset = 0;
-    if (Fill && (!boundOk || xscore_bound(ws, seqOffset, cost) > (int64_t)sliceMaxX))
-        result.maxX = ws_max_xscore(ws, seqOffset, cost, 64, kAllOnes);
     result.maxXNode = i;
-    const bool exists = (slice.node & kExists) != 0;
-    if (exists)
+    if ((slice.node & kExists) != 0 && merge_existing(ws, slice, hasSkipless, inDeg == 1 && singleInPrevBand, lane) && Fill)
     {
-        WS s = ws_make(slice.sVP, slice.sVN, slice.sEnd);
-        if (hasSkipless && g.inOff[i + 1] - g.inOff[i] == 1 && singleInPrevBand)
-        {
-            if (ws.end > s.end)
-            {
-                if (Fill) return result;
-            }
-            else if (ws.end < s.end)
-            {
-            }
-            else
-            {
-                u64 newBigger = (ws.VP & ~s.VP) | (s.VN & ~ws.VN);
-                u64 oldBigger = (s.VP & ~ws.VP) | (ws.VN & ~s.VN);
-                if (newBigger > oldBigger)
-                {
-                }
-                else if (oldBigger > newBigger)
-                {
-                    if (Fill) return result;
-                }
-                else if (newBigger == 0 && oldBigger == 0)
-                {
-                    if (Fill) return result;
-                }
-                else
-                {
-                    WS t = ws_merge(ws, s);
-                    if (ws_eq(t, s))
-                    {
-                        if (Fill) return result;
-                    }
-                    ws = t;
-                }
-            }
-        }
-        else
-        {
-            WS t = ws_merge(ws, s);
-            // the reference compares test.VP against the stored VN here (Common.h:1282)
-            if (t.end == s.end && t.VP == s.VP && t.VP == s.VN)
-            {
-                if (Fill) return result;
-            }
-            ws = t;
-        }
+        if (!boundOk || xscore_bound(ws0, seqOffset, cost) > (int64_t)sliceMaxX)
+            result.maxX = ws_max_xscore(ws0, seqOffset, cost, 64, kAllOnes);
+        return result;
     }
-    if (prev.exists && ws_before(ws) > prev.sEnd) ws = ws_merge(ws, ws_source(prev.sEnd));
+    if (prev.exists && ws_before(ws) > prev.sEnd) ws = merge_w(ws, ws_source(prev.sEnd), lane);
     u64 forceMask = 0;
     u64 fixedHP = prev.HP;
     u64 fixedHN = prev.HN;
@@ -420,29 +509,10 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
         i32 scoreBefore = ws_before(ws);
         i32 scoreComparison = prev.sEnd;
         if (scoreBefore > scoreComparison) { err = GA_ASSERT; return result; }
-        if (scoreBefore < scoreComparison)
+        if (scoreBefore < scoreComparison && !fix_horizontal(scoreBefore, scoreComparison, fixedHP, fixedHN, forceMask))
         {
-            forceMask |= 1;
-            for (int off = 1; off < 64; off++)
-            {
-                i32 next = scoreComparison + (i32)((fixedHP >> off) & 1) - (i32)((fixedHN >> off) & 1);
-                u64 mask = 1ULL << off;
-                if (scoreBefore > next) { err = GA_ASSERT; return result; }
-                if (scoreBefore < next)
-                {
-                    fixedHP |= mask;
-                    fixedHN &= ~mask;
-                    forceMask |= mask;
-                }
-                else
-                {
-                    fixedHP &= ~mask;
-                    fixedHN &= ~mask;
-                }
-                scoreBefore++;
-                scoreComparison = next;
-                if (scoreBefore >= scoreComparison) break;
-            }
+            err = GA_ASSERT;
+            return result;
         }
     }
     else
@@ -453,11 +523,16 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
     slice.sVN = ws.VN;
     slice.sEnd = ws.end;
     slice.node = i | kExists;
-    if (!Fill)
     {
-        cols[0].VP = ws.VP;
-        cols[0].VN = ws.VN;
-        cols[0].end = ws.end;
+        // Fill: column 0 as it enters the node, its X-score over every row; the traceback's
+        // recomputation: column 0 after the merges
+        Col c;
+        c.VP = Fill ? ws0.VP : ws.VP;
+        c.VN = Fill ? ws0.VN : ws.VN;
+        c.Mh = kAllOnes;
+        c.end = Fill ? ws0.end : ws.end;
+        c.phTop = 0;
+        cols[0] = c;
     }
     const u64 forceEq = prev.exists ? kAllOnes : (kAllOnes ^ 1);
     // the traceback's recomputation stops at the column it needs last
@@ -491,10 +566,9 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
     {
         // Across the lanes (lane k: columns k and k + 32; every lane wrote every column):
         // the first column of least score, the greatest X-score and the bottom-row deltas.
-        // A column whose X-score bound is at most max(slice so far, column 0) cannot change
-        // the node's contribution to the slice (the slice keeps the first node of strictly
-        // greatest X-score), so its exact X-score is skipped.
-        const i32 thr = imax(sliceMaxX, result.maxX);
+        // A column whose X-score bound is at most the slice's best so far cannot change the
+        // slice's choice (it keeps the first node of strictly greatest X-score), so its exact
+        // X-score is skipped; every column above that bound is scored exactly.
         u32 loKey = 0xffffffffu, hiKey = 0xffffffffu;
         i32 lmax = kIntMin;
         u32 hpLo = 0, hpHi = 0, hnLo = 0, hnHi = 0;
@@ -502,16 +576,19 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
         for (u32 h = 0; h < 2; h++)
         {
             const u32 pos = lane + 32 * h;
-            if (pos >= 1 && pos < columns)
+            if (pos < columns)
             {
                 const Col c = cols[pos];
                 const WS cw = ws_make(c.VP, c.VN, c.end);
                 const u32 key = (u32)c.end ^ 0x80000000u;   // signed order as unsigned
                 if (h == 0) loKey = key; else hiKey = key;
-                if (!boundOk || xscore_bound(cw, seqOffset, cost) > (int64_t)thr)
+                if (!boundOk || xscore_bound(cw, seqOffset, cost) > (int64_t)sliceMaxX)
                     lmax = imax(lmax, ws_max_xscore(cw, seqOffset, cost, 64, c.Mh));
-                if (h == 0) { hpLo = c.phTop; hnLo = (u32)(c.Mh >> 63); }
-                else { hpHi = c.phTop; hnHi = (u32)(c.Mh >> 63); }
+                if (pos >= 1)
+                {
+                    if (h == 0) { hpLo = c.phTop; hnLo = (u32)(c.Mh >> 63); }
+                    else { hpHi = c.phTop; hnHi = (u32)(c.Mh >> 63); }
+                }
             }
         }
         const u32 gkey = __reduce_min_sync(kFull, loKey < hiKey ? loKey : hiKey);
@@ -520,16 +597,10 @@ __device__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, c
         const u32 onHi = __ballot_sync(kFull, hiKey == gkey);
         const u64 outHP = (u64)__ballot_sync(kFull, hpLo) | ((u64)__ballot_sync(kFull, hpHi) << 32);
         const u64 outHN = (u64)__ballot_sync(kFull, hnLo) | ((u64)__ballot_sync(kFull, hnHi) << 32);
-        if (gkey != 0xffffffffu)
-        {
-            const i32 gmin = (i32)(gkey ^ 0x80000000u);
-            if (gmin < result.minScore)
-            {
-                result.minScore = gmin;
-                result.minScoreOffset = onLo ? (u32)(__ffs((int)onLo) - 1) : (u32)(32 + __ffs((int)onHi) - 1);
-            }
-        }
-        result.maxX = imax(result.maxX, gmax);
+        // column 0 always takes part, so the key is a real score
+        result.minScore = (i32)(gkey ^ 0x80000000u);
+        result.minScoreOffset = onLo ? (u32)(__ffs((int)onLo) - 1) : (u32)(32 + __ffs((int)onHi) - 1);
+        result.maxX = gmax;
         slice.HP = outHP;
         slice.HN = outHN;
     }
@@ -750,7 +821,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
         WS newEnd = ws_make(thisNode.eVP, thisNode.eVN, thisNode.eEnd);
         if (!ws_eq(newEnd, oldEnd))
         {
-            i32 newEndMin = ws_changed_min(newEnd, oldEnd);
+            i32 newEndMin = changed_min_w(newEnd, oldEnd, lane);
             if (newEndMin == kIntMax) { err = GA_ASSERT; return res; }
             if (newEndMin <= wadd(curMin, bw))
             {
@@ -981,34 +1052,21 @@ __device__ __forceinline__ bool trace_circular(const TraceOut& to)
     return false;
 }
 
-struct TraceCtx
-{
-    const DevGraph* g;
-    const uint8_t* seq;
-    u32 seqLen;
-    Table t;
-    i32 cost;
-    int err;
-    Col* cols;
-    u64* eqcol;
-    u32 lane;
-};
-
 __device__ __forceinline__ i32 fake_value() { return kIntMax; }
 
 __device__ __forceinline__ i32 col_value(const Col& c, int row) { return ws_value(ws_make(c.VP, c.VN, c.end), row); }
 
-// pickBacktraceCorner (Common.h:936-1054)
-__device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
+// pickBacktraceCorner (Common.h:936-1054).  Out of line, like the other crossing rules:
+// the walk inside a node-slice is the hot path.  t is a copy (its record cache is a hint).
+__device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, Table t, u32 cs, u32 node, int64_t j, int& err)
 {
-    const DevGraph& g = *c.g;
-    const SliceRec* cr = c.t.rec(cs);
-    const SliceRec* pr = c.t.rec(cs - 1);
-    const Item* self = c.t.find(cs, node);
+    const SliceRec* cr = t.rec(cs);
+    const SliceRec* pr = t.rec(cs - 1);
+    const Item* self = t.find(cs, node);
     TStep out; out.pos.node = 0; out.pos.off = 0; out.pos.seq = 0; out.sw = false;
-    if (!self) { c.err = GA_ASSERT; return out; }
+    if (!self) { err = GA_ASSERT; return out; }
     i32 scoreHere = ws_value(ws_make(self->sVP, self->sVN, self->sEnd), 0);
-    const Item* prevSelf = c.t.find(cs - 1, node);
+    const Item* prevSelf = t.find(cs - 1, node);
     if (cr->notValid || scoreHere > cr->quit)
     {
         if (scoreHere == fake_value()) { out.pos = TPos { node, 0, j }; return out; }
@@ -1024,14 +1082,14 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
         for (u32 e = g.inOff[node]; e < g.inOff[node + 1]; e++)
         {
             u32 nb = g.inNb[e];
-            const Item* pn = c.t.find(cs - 1, nb);
+            const Item* pn = t.find(cs - 1, nb);
             if (pn && pn->eEnd <= smallest)
             {
                 smallest = pn->eEnd;
                 sp = TPos { nb, g.len[nb] - 1, j - 1 };
                 change = true;
             }
-            const Item* cn = c.t.find(cs, nb);
+            const Item* cn = t.find(cs, nb);
             if (cn && nb != node)
             {
                 i32 v = ws_value(ws_make(cn->eVP, cn->eVN, cn->eEnd), 0);
@@ -1043,20 +1101,20 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
                 }
             }
         }
-        if (sp.node == 0xffffffffu) { c.err = GA_ASSERT; return out; }
+        if (sp.node == 0xffffffffu) { err = GA_ASSERT; return out; }
         out.pos = sp; out.sw = change;
         return out;
     }
     bool bad = false;
-    bool eq = char_match(g, c.seq[j], node, 0, bad);
-    if (bad) { c.err = GA_ASSERT; return out; }
+    bool eq = char_match(g, seq[j], node, 0, bad);
+    if (bad) { err = GA_ASSERT; return out; }
     TPos bestInvalid = TPos { 0xffffffffu, 0xffffffffu, -2 };
     i32 bestInvalidScore = scoreHere + 1;
     bool bestInvalidSw = false;
     if (prevSelf)
     {
         i32 ps = prevSelf->sEnd;
-        if (ps < scoreHere - 1) { c.err = GA_ASSERT; return out; }
+        if (ps < scoreHere - 1) { err = GA_ASSERT; return out; }
         if (ps == scoreHere - 1) { out.pos = TPos { node, 0, j - 1 }; return out; }
         if (pr->notValid || ps > pr->quit)
         {
@@ -1071,14 +1129,14 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
     for (u32 e = g.inOff[node]; e < g.inOff[node + 1]; e++)
     {
         u32 nb = g.inNb[e];
-        const Item* cn = c.t.find(cs, nb);
+        const Item* cn = t.find(cs, nb);
         if (cn)
         {
             i32 v = ws_value(ws_make(cn->eVP, cn->eVN, cn->eEnd), 0);
-            if (v < scoreHere - 1) { c.err = GA_ASSERT; return out; }
+            if (v < scoreHere - 1) { err = GA_ASSERT; return out; }
             if (v == scoreHere - 1) { out.pos = TPos { nb, g.len[nb] - 1, j }; out.sw = true; return out; }
         }
-        const Item* pn = c.t.find(cs - 1, nb);
+        const Item* pn = t.find(cs - 1, nb);
         if (pn)
         {
             i32 corner = pn->eEnd;
@@ -1093,7 +1151,7 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
             }
             else
             {
-                if (corner < scoreHere - (eq ? 0 : 1)) { c.err = GA_ASSERT; return out; }
+                if (corner < scoreHere - (eq ? 0 : 1)) { err = GA_ASSERT; return out; }
                 if (corner == scoreHere - (eq ? 0 : 1)) { out.pos = TPos { nb, g.len[nb] - 1, j - 1 }; out.sw = true; return out; }
             }
         }
@@ -1101,20 +1159,21 @@ __device__ TStep bt_corner(TraceCtx& c, u32 cs, u32 node, int64_t j)
     if (eq && scoreHere == fake_value()) { out.pos = TPos { node, 0, j }; return out; }
     if (scoreHere == fake_value()) { out.pos = TPos { node, 0, j }; return out; }
     if (bestInvalidScore < scoreHere + 1) { out.pos = bestInvalid; out.sw = bestInvalidSw; return out; }
-    c.err = GA_ASSERT;
+    err = GA_ASSERT;
     return out;
 }
 
 // recalcNodeWordslice (Common.h:1078-1102): the columns 0..lastColumn of one node-slice
-// (the traceback only moves left inside a node, so it never needs the columns after the
-// one it enters at).  When every column is recomputed the last one must equal the
-// stored end column, as the reference asserts.
-__device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, u32 lastColumn = 63)
+// into cols (the traceback only moves left inside a node, so it never needs the columns
+// after the one it enters at).  When every column is recomputed the last one must equal
+// the stored end column, as the reference asserts.  Returns 0 or the error status.
+__device__ __noinline__ int recalc(const DevGraph& g, i32 cost, Table t, u32 s, u32 node, const EqV4& eqv, Col* cols, u64* eqcol,
+    u32 lane, u32 lastColumn)
 {
-    const Item* it = c.t.find(s, node);
-    if (!it) { c.err = GA_ASSERT; return false; }
+    const Item* it = t.find(s, node);
+    if (!it) return GA_ASSERT;
     PrevInfo prev;
-    const Item* pi = c.t.find(s - 1, node);
+    const Item* pi = t.find(s - 1, node);
     if (pi) { prev.exists = true; prev.sEnd = pi->sEnd; prev.HP = pi->HP; prev.HN = pi->HN; }
     else { prev.exists = false; prev.sEnd = 0; prev.HP = kAllOnes; prev.HN = 0; }
     Item copy = *it;
@@ -1122,17 +1181,222 @@ __device__ bool recalc(TraceCtx& c, u32 s, u32 node, const EqV4& eqv, u32 lastCo
     u64 steps = 0;
     int err = 0;
     int64_t j = ((int64_t)s - 1) * 64;
-    node_calc<false>(*c.g, c.cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, c.cols, c.eqcol, steps, err,
-        c.lane, kIntMin, lastColumn);
-    if (err) { c.err = err; return false; }
-    u32 L = c.g->len[node];
-    if (!ws_eq(ws_make(c.cols[0].VP, c.cols[0].VN, c.cols[0].end), start)) { c.err = GA_ASSERT; return false; }
-    if (lastColumn + 1 >= L && !ws_eq(ws_make(c.cols[L - 1].VP, c.cols[L - 1].VN, c.cols[L - 1].end), ws_make(it->eVP, it->eVN, it->eEnd)))
+    node_calc<false>(g, cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, cols, eqcol, steps, err, lane, kIntMin, lastColumn);
+    if (err) return err;
+    u32 L = g.len[node];
+    if (!ws_eq(ws_make(cols[0].VP, cols[0].VN, cols[0].end), start)) return GA_ASSERT;
+    if (lastColumn + 1 >= L && !ws_eq(ws_make(cols[L - 1].VP, cols[L - 1].VN, cols[L - 1].end), ws_make(it->eVP, it->eVN, it->eEnd)))
+        return GA_ASSERT;
+    return 0;
+}
+
+// pickBacktraceVerticalCrossing (Common.h:886-934), the step out of (p.node, p.off > 0, row 0)
+// into the previous slice; pself is the node's entry there
+__device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* seq, Table t, u32 curSlice, const Item* pself, const Col* cols,
+    TPos p, int& err)
+{
+    TStep second;
+    second.pos = p;
+    second.sw = false;
+    const SliceRec* cr = t.rec(curSlice);
+    const SliceRec* pr = t.rec(curSlice - 1);
+    bool bad = false;
+    bool eq = char_match(g, seq[p.seq], p.node, p.off, bad);
+    if (bad) { err = GA_ASSERT; return second; }
+    i32 here = col_value(cols[p.off], 0);
+    i32 diag = pself->sEnd;
+    for (u32 k = 1; k + 1 <= p.off; k++)
     {
-        c.err = GA_ASSERT;
-        return false;
+        diag += (i32)((pself->HP >> k) & 1);
+        diag -= (i32)((pself->HN >> k) & 1);
     }
-    return true;
+    i32 up = diag + (i32)((pself->HP >> p.off) & 1) - (i32)((pself->HN >> p.off) & 1);
+    if (pr->notValid || cr->notValid || here > cr->quit || diag > pr->quit || up > pr->quit)
+    {
+        if (here == fake_value()) second = TStep { p, false };
+        else if (diag < up) second = TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
+        else second = TStep { TPos { p.node, p.off, p.seq - 1 }, false };
+        return second;
+    }
+    if (up < here - 1 || diag < here - (eq ? 0 : 1)) { err = GA_ASSERT; return second; }
+    if (up == here - 1) return TStep { TPos { p.node, p.off, p.seq - 1 }, false };
+    if (diag == here - (eq ? 0 : 1)) return TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
+    err = GA_ASSERT;
+    return second;
+}
+
+// pickBacktraceHorizontalCrossing (Common.h:817-884), the step out of (p.node, offset 0,
+// row off > 0) into an in-neighbour; self is the node's entry in the slice
+__device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* seq, Table t, u32 curSlice, u32 curNode, const Item* self,
+    TPos p, u32 off, int& err)
+{
+    TStep second;
+    second.pos = p;
+    second.sw = false;
+    const SliceRec* cr = t.rec(curSlice);
+    bool bad = false;
+    bool eq = char_match(g, seq[p.seq], p.node, p.off, bad);
+    if (bad) { err = GA_ASSERT; return second; }
+    WS sws = ws_make(self->sVP, self->sVN, self->sEnd);
+    i32 here = ws_value(sws, (int)off);
+    if (cr->notValid || here > cr->quit)
+    {
+        i32 smallest = ws_value(sws, (int)off - 1);
+        TPos sp = TPos { curNode, 0, p.seq - 1 };
+        bool change = false;
+        for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1]; e++)
+        {
+            u32 nb = g.inNb[e];
+            const Item* cn = t.find(curSlice, nb);
+            if (cn)
+            {
+                WS nws = ws_make(cn->eVP, cn->eVN, cn->eEnd);
+                if (ws_value(nws, (int)off - 1) <= smallest)
+                {
+                    smallest = ws_value(nws, (int)off - 1);
+                    sp = TPos { nb, g.len[nb] - 1, p.seq - 1 };
+                    change = true;
+                }
+                if (ws_value(nws, (int)off) < smallest && nb != curNode)
+                {
+                    smallest = ws_value(nws, (int)off);
+                    sp = TPos { nb, g.len[nb] - 1, p.seq };
+                    change = true;
+                }
+            }
+        }
+        if (tpos_eq(sp, p) && here != fake_value()) { err = GA_ASSERT; return second; }
+        return TStep { sp, change };
+    }
+    for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1]; e++)
+    {
+        u32 nb = g.inNb[e];
+        const Item* cn = t.find(curSlice, nb);
+        if (!cn) continue;
+        WS nws = ws_make(cn->eVP, cn->eVN, cn->eEnd);
+        i32 v0 = ws_value(nws, (int)off);
+        i32 v1 = ws_value(nws, (int)off - 1);
+        if (v0 < here - 1 || v1 < here - (eq ? 0 : 1)) { err = GA_ASSERT; return second; }
+        if (v0 == here - 1) return TStep { TPos { nb, g.len[nb] - 1, p.seq }, true };
+        if (v1 == here - (eq ? 0 : 1)) return TStep { TPos { nb, g.len[nb] - 1, p.seq - 1 }, true };
+    }
+    if (here != fake_value()) { err = GA_ASSERT; return second; }
+    return TStep { p, false };
+}
+
+struct EndCell
+{
+    u32 node;
+    u32 nodeOffset;
+    u32 bvOffset;
+    i32 score;
+    int64_t j;
+    int err;
+};
+
+// getReverseTraceFromTableExactEndPos (Common.h:496-562): the first slice of greatest
+// X-score (lanes stride over the slices), then across the lanes (lane k: columns k and
+// k + 32 of its best node) the cell of greatest row among those scoring the slice's
+// X-score, the first column on ties.  The node's columns are left in cols.
+__device__ __noinline__ EndCell end_cell(const DevGraph& g, i32 cost, const uint8_t* arena, Table t, u32 committed, const uint8_t* seq,
+    u32 seqLen, Col* cols, u64* eqcol, u32 lane)
+{
+    EndCell ec;
+    ec.err = 0;
+    ec.nodeOffset = 0xffffffffu;
+    ec.bvOffset = 0xffffffffu;
+    i32 bx = kIntMin;
+    u32 bs = 0xffffffffu;
+    for (u32 s = 1 + lane; s < committed; s += 32)
+    {
+        const i32 mx = ((const SliceRec*)(arena + t.dir[s]))->maxX;
+        if (mx > bx) { bx = mx; bs = s; }
+    }
+    const i32 gbx = __reduce_max_sync(kFull, bx);
+    const u32 best = __reduce_min_sync(kFull, bx == gbx ? bs : 0xffffffffu);
+    const SliceRec* br = t.rec(best);
+    ec.node = br->maxXNode;
+    ec.score = br->maxX;
+    ec.j = ((int64_t)best - 1) * 64;
+    const int64_t j = ec.j;
+    EqV4 eqv;
+    if (!eq_vector(seq, seqLen, j, eqv, lane)) { ec.err = GA_ASSERT; return ec; }
+    ec.err = recalc(g, cost, t, best, ec.node, eqv, cols, eqcol, lane, 63);
+    if (ec.err) return ec;
+    const int cells = (int)((int64_t)seqLen - j < 64 ? (int64_t)seqLen - j : 64);
+    const u32 L = g.len[ec.node];
+    bool bad = false;
+    int candOff = -1;
+    u32 candCol = 0xffffffffu;
+    for (u32 h = 0; h < 2; h++)
+    {
+        const u32 i = lane + 32 * h;
+        if (i >= L || bad) continue;
+        const WS cw = ws_make(cols[i].VP, cols[i].VN, cols[i].end);
+        i32 mx = ws_max_xscore(cw, (i32)j, cost, cells, kAllOnes);
+        if (mx > ec.score) { bad = true; continue; }
+        if (mx == ec.score)
+        {
+            for (int off = 63; off >= 0; off--)
+            {
+                if (j + off >= (int64_t)seqLen) continue;
+                i32 here = ws_xscore(cw, (i32)j, off, cost);
+                if (here > ec.score) { bad = true; break; }
+                if (here == ec.score && off > candOff)
+                {
+                    candOff = off;
+                    candCol = i;
+                }
+            }
+        }
+    }
+    if (__ballot_sync(kFull, bad)) { ec.err = GA_ASSERT; return ec; }
+    const int gOff = __reduce_max_sync(kFull, candOff);
+    const u32 gCol = __reduce_min_sync(kFull, candOff == gOff ? candCol : 0xffffffffu);
+    if (gOff < 0 || j + gOff >= (int64_t)seqLen) { ec.err = GA_ASSERT; return ec; }
+    ec.nodeOffset = gCol;
+    ec.bvOffset = (u32)gOff;
+    return ec;
+}
+
+// the start node's row above the read (Common.h:721-756): walks left along the start
+// slice while the score falls by one, then into an in-neighbour at offset 0
+__device__ __noinline__ int row_above(const DevGraph& g, Table t, TraceOut& to)
+{
+    if (to.back.seq != -1) return GA_ASSERT;
+    const Item* it = t.find(0, to.back.node);
+    if (!it) return GA_ASSERT;
+    const u32 L = g.len[to.back.node];
+    // before[k] = score of column k in the row above the read
+    auto before = [&](u32 k) -> i32
+    {
+        i32 v = it->sEnd;
+        for (u32 q = 1; q <= k; q++) v += (i32)((it->HP >> q) & 1) - (i32)((it->HN >> q) & 1);
+        return v;
+    };
+    if (before(L - 1) != it->eEnd) return GA_ASSERT;
+    while (!to.overflow)
+    {
+        TPos q = to.back;
+        i32 bq = before(q.off);
+        if (!(bq != 0 && q.off > 0 && before(q.off - 1) == bq - 1)) break;
+        to.push(TPos { q.node, q.off - 1, q.seq }, false);
+    }
+    TPos q = to.back;
+    if (!to.overflow && q.off == 0 && before(0) != 0)
+    {
+        for (u32 e = g.inOff[q.node]; e < g.inOff[q.node + 1]; e++)
+        {
+            u32 nb = g.inNb[e];
+            const Item* ni = t.find(0, nb);
+            if (ni && ws_before(ws_make(ni->eVP, ni->eVN, ni->eEnd)) == before(0) - 1)
+            {
+                to.push(TPos { nb, g.len[nb] - 1, q.seq }, true);
+                break;
+            }
+        }
+    }
+    return 0;
 }
 
 __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st, const WSpace& w, u32 lane)
@@ -1151,20 +1415,14 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
         }
         return;
     }
-    TraceCtx c;
-    c.g = &g;
-    c.seq = a.seq + a.seqOff[ext];
-    c.seqLen = a.seqLen[ext];
-    c.t.arena = a.arena;
-    c.t.dir = (const u64*)(a.arena + st.dir);
-    c.t.count = st.committed;
-    c.t.lane = lane;
-    c.t.init();
-    c.cost = a.cost;
-    c.err = 0;
-    c.cols = w.cols;
-    c.eqcol = w.eqcol;
-    c.lane = lane;
+    const uint8_t* seq = a.seq + a.seqOff[ext];
+    const u32 seqLen = a.seqLen[ext];
+    Table t;
+    t.arena = a.arena;
+    t.dir = (const u64*)(a.arena + st.dir);
+    t.count = st.committed;
+    t.lane = lane;
+    t.init();
     Col* cols = w.cols;
     TraceOut to;
     to.items = out;
@@ -1173,112 +1431,58 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
     to.n = 0;
     to.lane = lane;
     to.overflow = false;
-    // choose the end cell (getReverseTraceFromTableExactEndPos, Common.h:496-562): the first
-    // slice of greatest X-score (lanes stride over the slices) ...
-    i32 bx = kIntMin;
-    u32 bs = 0xffffffffu;
-    for (u32 s = 1 + lane; s < st.committed; s += 32)
-    {
-        const i32 mx = ((const SliceRec*)(a.arena + c.t.dir[s]))->maxX;
-        if (mx > bx) { bx = mx; bs = s; }
-    }
-    const i32 gbx = __reduce_max_sync(kFull, bx);
-    const u32 best = __reduce_min_sync(kFull, bx == gbx ? bs : 0xffffffffu);
-    const SliceRec* br = c.t.rec(best);
-    u32 node = br->maxXNode;
-    i32 score = br->maxX;
-    int64_t j = ((int64_t)best - 1) * 64;
-    EqV4 eqv;
-    if (!eq_vector(c.seq, c.seqLen, j, eqv, lane)) c.err = GA_ASSERT;
-    u32 nodeOffset = 0xffffffffu, bvOffset = 0xffffffffu;
-    if (!c.err && recalc(c, best, node, eqv))
-    {
-        // ... then, across the lanes (lane k: columns k and k + 32), the cell of greatest row
-        // among those scoring the slice's X-score, the first column on ties
-        const int cells = (int)((int64_t)c.seqLen - j < 64 ? (int64_t)c.seqLen - j : 64);
-        const u32 L = g.len[node];
-        bool bad = false;
-        int candOff = -1;
-        u32 candCol = 0xffffffffu;
-        for (u32 h = 0; h < 2; h++)
-        {
-            const u32 i = lane + 32 * h;
-            if (i >= L || bad) continue;
-            const WS cw = ws_make(cols[i].VP, cols[i].VN, cols[i].end);
-            i32 mx = ws_max_xscore(cw, (i32)j, a.cost, cells, kAllOnes);
-            if (mx > score) { bad = true; continue; }
-            if (mx == score)
-            {
-                for (int off = 63; off >= 0; off--)
-                {
-                    if (j + off >= (int64_t)c.seqLen) continue;
-                    i32 here = ws_xscore(cw, (i32)j, off, a.cost);
-                    if (here > score) { bad = true; break; }
-                    if (here == score && off > candOff)
-                    {
-                        candOff = off;
-                        candCol = i;
-                    }
-                }
-            }
-        }
-        if (__ballot_sync(kFull, bad)) c.err = GA_ASSERT;
-        const int gOff = __reduce_max_sync(kFull, candOff);
-        const u32 gCol = __reduce_min_sync(kFull, candOff == gOff ? candCol : 0xffffffffu);
-        if (gOff >= 0)
-        {
-            nodeOffset = gCol;
-            bvOffset = (u32)gOff;
-        }
-    }
-    if (!c.err && (nodeOffset == 0xffffffffu || j + bvOffset >= (int64_t)c.seqLen)) c.err = GA_ASSERT;
+    int err = 0;
     i32 resultScore = 0;
-    if (!c.err)
+    const EndCell ec = end_cell(g, a.cost, a.arena, t, st.committed, seq, seqLen, cols, w.eqcol, lane);
+    err = ec.err;
+    if (!err)
     {
         // getReverseTraceFromTable (Common.h:571-758)
-        TPos start = TPos { node, nodeOffset, j + bvOffset };
-        i32 startScore = col_value(cols[nodeOffset], (int)bvOffset);
+        TPos start = TPos { ec.node, ec.nodeOffset, ec.j + ec.bvOffset };
+        i32 startScore = col_value(cols[ec.nodeOffset], (int)ec.bvOffset);
         resultScore = startScore;
         to.push(start, false);
         u32 curSlice = (u32)(start.seq / 64) + 1;
         u32 curNode = 0xffffffffu;
         u32 colsUpTo = 0;             // columns 0..colsUpTo of (curSlice, curNode) are in cols
-        if (!eq_vector(c.seq, c.seqLen, ((int64_t)curSlice - 1) * 64, eqv, lane)) c.err = GA_ASSERT;
+        EqV4 eqv;
+        if (!eq_vector(seq, seqLen, ((int64_t)curSlice - 1) * 64, eqv, lane)) err = GA_ASSERT;
         i32 lastScore = kIntMax - 1;
         u64 guard = 0;
         const u64 guardMax = (u64)cap * 4 + 1024;
-        while (!c.err && !to.overflow && to.back.seq != -1)
+        while (!err && !to.overflow && to.back.seq != -1)
         {
-            if (++guard > guardMax) { c.err = GA_CAPACITY; break; }
+            if (++guard > guardMax) { err = GA_CAPACITY; break; }
             TPos b = to.back;
             u32 newSlice = (u32)(b.seq / 64) + 1;
-            if (newSlice >= st.committed) { c.err = GA_ASSERT; break; }
+            if (newSlice >= st.committed) { err = GA_ASSERT; break; }
             // a self-loop can re-enter the same node-slice further right than it was computed
             if (newSlice != curSlice || b.node != curNode || b.off > colsUpTo)
             {
-                if (newSlice != curSlice && !eq_vector(c.seq, c.seqLen, ((int64_t)newSlice - 1) * 64, eqv, lane)) { c.err = GA_ASSERT; break; }
+                if (newSlice != curSlice && !eq_vector(seq, seqLen, ((int64_t)newSlice - 1) * 64, eqv, lane)) { err = GA_ASSERT; break; }
                 curSlice = newSlice;
                 curNode = b.node;
-                if (curSlice == 0) { c.err = GA_ASSERT; break; }
-                if (!recalc(c, curSlice, curNode, eqv, b.off)) break;
+                if (curSlice == 0) { err = GA_ASSERT; break; }
+                err = recalc(g, a.cost, t, curSlice, curNode, eqv, cols, w.eqcol, lane, b.off);
+                if (err) break;
                 colsUpTo = b.off;
             }
             const int64_t sj = ((int64_t)curSlice - 1) * 64;
-            if (b.off >= g.len[curNode]) { c.err = GA_ASSERT; break; }
+            if (b.off >= g.len[curNode]) { err = GA_ASSERT; break; }
             const u32 row = mod64(b.seq);
             lastScore = col_value(cols[b.off], (int)row);
             if (row == 0 && b.off == 0)
             {
-                TStep bt = bt_corner(c, curSlice, curNode, sj);
-                if (c.err) break;
+                TStep bt = bt_corner(g, seq, t, curSlice, curNode, sj, err);
+                if (err) break;
                 if (tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == fake_value()) break;
                 to.push(bt.pos, bt.sw);
-                if (!to.overflow && trace_circular(to)) { c.err = GA_ASSERT; break; }
+                if (!to.overflow && trace_circular(to)) { err = GA_ASSERT; break; }
                 continue;
             }
             if (row == 0)
             {
-                const Item* pself = c.t.find(curSlice - 1, curNode);
+                const Item* pself = t.find(curSlice - 1, curNode);
                 if (!pself)
                 {
                     for (u32 k = b.off - 1; k > 0; k--) to.push(TPos { curNode, k, b.seq }, false);
@@ -1288,134 +1492,37 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 // pickBacktraceVerticalCrossing (Common.h:886-934)
                 TPos p = b;
                 while (p.off > 0 && col_value(cols[p.off - 1], 0) == col_value(cols[p.off], 0) - 1) p.off--;
-                TStep second;
-                if (p.off == 0)
-                {
-                    second = bt_corner(c, curSlice, curNode, sj);
-                    if (c.err) break;
-                }
-                else
-                {
-                    const SliceRec* cr = c.t.rec(curSlice);
-                    const SliceRec* pr = c.t.rec(curSlice - 1);
-                    bool bad = false;
-                    bool eq = char_match(g, c.seq[p.seq], p.node, p.off, bad);
-                    if (bad) { c.err = GA_ASSERT; break; }
-                    i32 here = col_value(cols[p.off], 0);
-                    i32 diag = pself->sEnd;
-                    for (u32 k = 1; k + 1 <= p.off; k++)
-                    {
-                        diag += (i32)((pself->HP >> k) & 1);
-                        diag -= (i32)((pself->HN >> k) & 1);
-                    }
-                    i32 up = diag + (i32)((pself->HP >> p.off) & 1) - (i32)((pself->HN >> p.off) & 1);
-                    if (pr->notValid || cr->notValid || here > cr->quit || diag > pr->quit || up > pr->quit)
-                    {
-                        if (here == fake_value()) second = TStep { p, false };
-                        else if (diag < up) second = TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
-                        else second = TStep { TPos { p.node, p.off, p.seq - 1 }, false };
-                    }
-                    else
-                    {
-                        if (up < here - 1 || diag < here - (eq ? 0 : 1)) { c.err = GA_ASSERT; break; }
-                        if (up == here - 1) second = TStep { TPos { p.node, p.off, p.seq - 1 }, false };
-                        else if (diag == here - (eq ? 0 : 1)) second = TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
-                        else { c.err = GA_ASSERT; break; }
-                    }
-                }
+                TStep second = p.off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : vertical_step(g, seq, t, curSlice, pself, cols, p, err);
+                if (err) break;
                 if (second.pos.seq == b.seq && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
                 if (p.off != b.off)
                 {
                     for (u32 k = b.off - 1; k != p.off; k--) to.push(TPos { p.node, k, p.seq }, false);
                 }
                 if (!tpos_eq(p, to.back)) to.push(p, false);
-                if (tpos_eq(second.pos, to.back)) { c.err = GA_ASSERT; break; }
+                if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
                 to.push(second.pos, second.sw);
                 continue;
             }
             if (b.off == 0)
             {
                 // pickBacktraceHorizontalCrossing (Common.h:817-884)
-                const Item* self = c.t.find(curSlice, curNode);
-                if (!self) { c.err = GA_ASSERT; break; }
+                const Item* self = t.find(curSlice, curNode);
+                if (!self) { err = GA_ASSERT; break; }
                 TPos p = b;
                 while (mod64(p.seq) != 0 && (self->sVP & (1ULL << mod64(p.seq)))) p.seq--;
                 const u32 off = mod64(p.seq);
-                TStep second;
-                if (off == 0)
-                {
-                    second = bt_corner(c, curSlice, curNode, sj);
-                    if (c.err) break;
-                }
-                else
-                {
-                    const SliceRec* cr = c.t.rec(curSlice);
-                    bool bad = false;
-                    bool eq = char_match(g, c.seq[p.seq], p.node, p.off, bad);
-                    if (bad) { c.err = GA_ASSERT; break; }
-                    WS sws = ws_make(self->sVP, self->sVN, self->sEnd);
-                    i32 here = ws_value(sws, (int)off);
-                    if (cr->notValid || here > cr->quit)
-                    {
-                        i32 smallest = ws_value(sws, (int)off - 1);
-                        TPos sp = TPos { curNode, 0, p.seq - 1 };
-                        bool change = false;
-                        for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1]; e++)
-                        {
-                            u32 nb = g.inNb[e];
-                            const Item* cn = c.t.find(curSlice, nb);
-                            if (cn)
-                            {
-                                WS nws = ws_make(cn->eVP, cn->eVN, cn->eEnd);
-                                if (ws_value(nws, (int)off - 1) <= smallest)
-                                {
-                                    smallest = ws_value(nws, (int)off - 1);
-                                    sp = TPos { nb, g.len[nb] - 1, p.seq - 1 };
-                                    change = true;
-                                }
-                                if (ws_value(nws, (int)off) < smallest && nb != curNode)
-                                {
-                                    smallest = ws_value(nws, (int)off);
-                                    sp = TPos { nb, g.len[nb] - 1, p.seq };
-                                    change = true;
-                                }
-                            }
-                        }
-                        if (tpos_eq(sp, p) && here != fake_value()) { c.err = GA_ASSERT; break; }
-                        second = TStep { sp, change };
-                    }
-                    else
-                    {
-                        bool found = false;
-                        for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1] && !found; e++)
-                        {
-                            u32 nb = g.inNb[e];
-                            const Item* cn = c.t.find(curSlice, nb);
-                            if (!cn) continue;
-                            WS nws = ws_make(cn->eVP, cn->eVN, cn->eEnd);
-                            i32 v0 = ws_value(nws, (int)off);
-                            i32 v1 = ws_value(nws, (int)off - 1);
-                            if (v0 < here - 1 || v1 < here - (eq ? 0 : 1)) { c.err = GA_ASSERT; break; }
-                            if (v0 == here - 1) { second = TStep { TPos { nb, g.len[nb] - 1, p.seq }, true }; found = true; }
-                            else if (v1 == here - (eq ? 0 : 1)) { second = TStep { TPos { nb, g.len[nb] - 1, p.seq - 1 }, true }; found = true; }
-                        }
-                        if (c.err) break;
-                        if (!found)
-                        {
-                            if (here != fake_value()) { c.err = GA_ASSERT; break; }
-                            second = TStep { p, false };
-                        }
-                    }
-                }
+                TStep second = off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : horizontal_step(g, seq, t, curSlice, curNode, self, p, off, err);
+                if (err) break;
                 if (second.pos.node == b.node && !second.sw && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
                 if (p.seq != b.seq)
                 {
                     for (int64_t sp = b.seq - 1; sp != p.seq; sp--) to.push(TPos { p.node, p.off, sp }, false);
                 }
                 if (!tpos_eq(p, to.back)) to.push(p, false);
-                if (tpos_eq(second.pos, to.back)) { c.err = GA_ASSERT; break; }
+                if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
                 to.push(second.pos, second.sw);
-                if (!to.overflow && trace_circular(to)) { c.err = GA_ASSERT; break; }
+                if (!to.overflow && trace_circular(to)) { err = GA_ASSERT; break; }
                 continue;
             }
             // pickBacktraceInside (Common.h:770-815).  The four neighbouring scores are
@@ -1483,64 +1590,25 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                         }
                         else
                         {
-                            if (here != fake_value()) c.err = GA_ASSERT;
+                            if (here != fake_value()) err = GA_ASSERT;
                             break;
                         }
                         if (to.overflow || hori == 0 || vert == 0) break;
                     }
                 }
-                if (c.err || to.overflow) break;
+                if (err || to.overflow) break;
                 if (col_value(cols[to.back.off], (int)mod64(to.back.seq)) == fake_value()) break;
             }
         }
-        if (!c.err && !to.overflow)
+        if (!err && !to.overflow)
         {
-            if (resultScore < lastScore) c.err = GA_ASSERT;
+            if (resultScore < lastScore) err = GA_ASSERT;
             resultScore -= lastScore;
         }
-        // the start node's row above the read (Common.h:721-756)
-        if (!c.err && !to.overflow)
-        {
-            if (to.back.seq != -1) c.err = GA_ASSERT;
-            const Item* it = c.err ? nullptr : c.t.find(0, to.back.node);
-            if (!c.err && !it) c.err = GA_ASSERT;
-            if (!c.err)
-            {
-                const u32 L = g.len[to.back.node];
-                // before[k] = score of column k in the row above the read
-                auto before = [&](u32 k) -> i32
-                {
-                    i32 v = it->sEnd;
-                    for (u32 q = 1; q <= k; q++) v += (i32)((it->HP >> q) & 1) - (i32)((it->HN >> q) & 1);
-                    return v;
-                };
-                if (before(L - 1) != it->eEnd) c.err = GA_ASSERT;
-                while (!c.err && !to.overflow)
-                {
-                    TPos q = to.back;
-                    i32 bq = before(q.off);
-                    if (!(bq != 0 && q.off > 0 && before(q.off - 1) == bq - 1)) break;
-                    to.push(TPos { q.node, q.off - 1, q.seq }, false);
-                }
-                TPos q = to.back;
-                if (!c.err && !to.overflow && q.off == 0 && before(0) != 0)
-                {
-                    for (u32 e = g.inOff[q.node]; e < g.inOff[q.node + 1]; e++)
-                    {
-                        u32 nb = g.inNb[e];
-                        const Item* ni = c.t.find(0, nb);
-                        if (ni && ws_before(ws_make(ni->eVP, ni->eVN, ni->eEnd)) == before(0) - 1)
-                        {
-                            to.push(TPos { nb, g.len[nb] - 1, q.seq }, true);
-                            break;
-                        }
-                    }
-                }
-            }
-        }
+        if (!err && !to.overflow) err = row_above(g, t, to);
     }
     to.finish();
-    int status = c.err ? c.err : (to.overflow ? GA_CAPACITY : GA_OK);
+    int status = err ? err : (to.overflow ? GA_CAPACITY : GA_OK);
     if (lane == 0)
     {
         a.status[ext] = status;
