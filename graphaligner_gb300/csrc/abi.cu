@@ -85,7 +85,7 @@ struct ga_extender
     cudaStream_t copy[kCopyStreams] {};
     cudaEvent_t copyDone[kCopyStreams] {};
     int sms = 0;
-    ga_launch_shape shape {};             // warps per block, blocks per SM, first table layout, region size
+    ga_launch_shape shape {};             // warps per block, blocks per SM, first table layout, arena chunk
     uint8_t* workspace = nullptr;         // frontier tables of the global-memory layouts
     uint64_t workspaceBytes = 0;
     uint8_t* arena = nullptr;
@@ -105,6 +105,7 @@ struct ga_extender
     DevBuf<uint64_t> seqOff, traceOff, traceItems, cellSteps;
     DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order;
     DevBuf<int32_t> status, score, prevStatus;
+    DevBuf<gadev::ExtState> states;        // where the fill left each extension's table
 };
 
 extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
@@ -178,21 +179,20 @@ extern "C" int ga_graph_free(ga_graph_t g)
 
 // Default launch shape (results never depend on it): blocks of 4 warps, as many blocks per
 // SM as registers and shared memory allow, the frontier tables in shared memory first, and
-// a 128 KiB DP-table region per warp (the table of an extension of ~25 kbp at the band
-// sizes of variation graphs; longer ones continue in the shared overflow).
+// 64 KiB arena chunks (the DP tables of a few extensions of a few kbp).
 static ga_launch_shape default_shape()
 {
     ga_launch_shape sh;
     sh.warps_per_block = 4;
     sh.blocks_per_sm = 0;
     sh.first_layout = 0;
-    sh.region_kib = 128;
+    sh.chunk_kib = 64;
     return sh;
 }
 
 static bool shape_ok(const ga_launch_shape& sh)
 {
-    return sh.warps_per_block >= 1 && sh.warps_per_block <= 4 && sh.first_layout <= 2 && sh.region_kib <= (1u << 20);
+    return sh.warps_per_block >= 1 && sh.warps_per_block <= 4 && sh.first_layout <= 2 && sh.chunk_kib >= 1 && sh.chunk_kib <= (1u << 20);
 }
 
 // Frontier-table capacities of the three layouts: small tables in shared memory (a variation
@@ -207,7 +207,7 @@ static gadev::Caps layout_caps(int layout)
     return c;
 }
 
-static const char* kShapeError = "launch shape: warps_per_block within 1..4, first_layout within 0..2, region_kib at most 2^20";
+static const char* kShapeError = "launch shape: warps_per_block within 1..4, first_layout within 0..2, chunk_kib within 1..2^20";
 
 extern "C" int ga_extender_create(ga_graph_t graph, uint64_t arena_bytes, ga_extender_t* out)
 {
@@ -259,7 +259,7 @@ extern "C" int ga_extender_free(ga_extender_t x)
     cudaFree(x->arenaCursor);
     x->seq.release(); x->seqOff.release(); x->traceOff.release(); x->traceItems.release(); x->cellSteps.release();
     x->seqLen.release(); x->startNode.release(); x->startOffset.release(); x->traceCap.release(); x->traceLen.release();
-    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release();
+    x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release(); x->states.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
     for (int k = 0; k < ga_extender::kCopyStreams; k++)
@@ -310,29 +310,36 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
     ta.cellSteps = r->cell_steps;
 
     const uint32_t n = b->num;
+    GA_CUDA(x->states.reserve(n));
+    fa.states = x->states.ptr;
+    ta.num = n;
+    ta.order = order;
+    ta.states = x->states.ptr;
     x->lastFillMs = 0;
     x->lastTraceMs = 0;
     x->lastLaunches = 0;
     for (int k = 0; k < 3; k++) x->lastRounds[k] = 0;
     const ga_launch_shape& sh = x->shape;
     const int wpb = (int)sh.warps_per_block;
+    fa.chunkBytes = (uint64_t)sh.chunk_kib << 10;
     uint32_t pending = n;                    // extensions the next round runs
     for (int layout = (int)sh.first_layout; layout < 3; layout++)
     {
         const bool shared = layout == 0;
         const gadev::Caps caps = layout_caps(layout);
         const uint64_t stride = ga_warp_tables_bytes(caps);
-        int blocksPerSm = ga_extend_blocks_per_sm(wpb, caps, shared);
-        if (blocksPerSm <= 0) return fail(GA_ERR_CUDA, "the extension kernel does not fit an SM with this launch shape");
-        if (sh.blocks_per_sm > 0) blocksPerSm = std::min<int>(blocksPerSm, (int)sh.blocks_per_sm);
-        uint64_t warps = (uint64_t)x->sms * blocksPerSm * wpb;
-        if (!shared) warps = std::min<uint64_t>(warps, x->workspaceBytes / stride);
-        warps = std::min<uint64_t>(warps, ((uint64_t)pending + wpb - 1) / wpb * wpb);
-        warps = std::max<uint64_t>(warps / wpb, 1) * wpb;
-        const uint64_t blocks = warps / wpb;
-        // per-warp regions take at most half the arena; the rest is the shared overflow
-        uint64_t region = (uint64_t)sh.region_kib << 10;
-        region = std::min<uint64_t>(region, x->arenaBytes / 2 / warps) & ~15ULL;
+        int fillPerSm = ga_fill_blocks_per_sm(wpb, caps, shared);
+        int tracePerSm = ga_trace_blocks_per_sm(wpb);
+        if (fillPerSm <= 0 || tracePerSm <= 0) return fail(GA_ERR_CUDA, "the extension kernels do not fit an SM with this launch shape");
+        if (sh.blocks_per_sm > 0)
+        {
+            fillPerSm = std::min<int>(fillPerSm, (int)sh.blocks_per_sm);
+            tracePerSm = std::min<int>(tracePerSm, (int)sh.blocks_per_sm);
+        }
+        const uint64_t pendingBlocks = std::max<uint64_t>(1, ((uint64_t)pending + wpb - 1) / wpb);
+        uint64_t fillBlocks = std::min<uint64_t>((uint64_t)x->sms * fillPerSm, pendingBlocks);
+        if (!shared) fillBlocks = std::max<uint64_t>(1, std::min<uint64_t>(fillBlocks, x->workspaceBytes / stride / wpb));
+        const uint64_t traceBlocks = std::min<uint64_t>((uint64_t)x->sms * tracePerSm, pendingBlocks);
         if (layout > (int)sh.first_layout)
         {
             // only extensions that ran out of a capacity in the previous round run again
@@ -341,15 +348,14 @@ static int run_device(ga_extender* x, const ga_extend_params* p, const ga_extend
         fa.caps = caps;
         fa.workspace = shared ? nullptr : x->workspace;
         fa.workspaceStride = stride;
-        fa.regionBytes = region;
-        fa.overflowBase = warps * region;
         fa.prevStatus = layout > (int)sh.first_layout ? prevStatus : nullptr;
+        ta.prevStatus = fa.prevStatus;
         GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), stream));
         GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, 2 * sizeof(unsigned long long), stream));
         GA_CUDA(cudaEventRecord(x->ev[0], stream));
-        if (ga_launch_extend(fa, ta, x->counters, (int)blocks, wpb, stream) != 0)
+        if (ga_launch_extend(fa, ta, x->counters, (int)fillBlocks, (int)traceBlocks, wpb, stream) != 0)
             return fail(GA_ERR_CUDA, std::string("extension kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
-        x->lastLaunches += 1;
+        x->lastLaunches += 2;
         x->lastRounds[layout] = pending;
         GA_CUDA(cudaEventRecord(x->ev[1], stream));
         count_status_kernel<<<64, 256, 0, stream>>>(r->status, n, GA_CAPACITY, x->counters + 2);

@@ -1,30 +1,34 @@
 // Batched seed extension on GB300: one warp per extension.
 //
-// A warp owns one extension at a time: the fill (banded Myers DP over the graph
-// with the component-ordered frontier and X-drop) and then the traceback.  The
-// DP of one extension is a sequential chain: each 64-row slice depends on the
-// whole band of the previous one, and inside a slice nodes are computed one at
-// a time in frontier order, the admission test using the running minimum.  So
-// the warp runs that control flow warp-uniformly (every lane holds the same
-// scalars, branches never diverge) and spreads over its lanes the work that is
-// parallel inside it:
+// Two persistent kernels run back to back.  In the fill kernel a warp owns one
+// extension at a time and runs the banded Myers DP over the graph with the
+// component-ordered frontier and X-drop, writing each committed slice into the
+// batch's DP-table arena; the traceback kernel then gives each warp one filled
+// extension to walk back.  The DP of one extension is a sequential chain: each
+// 64-row slice depends on the whole band of the previous one, and inside a slice
+// nodes are computed one at a time in frontier order, the admission test using the
+// running minimum.  So a warp runs that control flow warp-uniformly (every lane
+// holds the same scalars, branches never diverge) and spreads over its lanes the
+// work that is parallel inside it:
 //   - the match masks of a slice (lane k reads rows k and k + 32; ballots),
 //   - the match mask of every column of a node, before its column loop,
 //   - per node: the X-score of every column (lane k scores columns k and k + 32),
 //     the minimum and its first column (reduce + ballot) and the bottom-row
 //     horizontal deltas (ballots), so the column loop itself only runs the
 //     Myers recurrence,
+//   - cellwise merges of columns and the changed-minimum test (row scores by
+//     popcount, then a shuffle, ballots and a reduction),
 //   - node-table lookups: 32 probes of the open-addressing table per step (ballot),
 //   - committing a slice to the DP table (coalesced copies),
 //   - the traceback's end-cell choice (slices and columns across lanes) and its
 //     band lookups (ballot over the slice's node ids),
 //   - trace output, staged in shared memory and written 32 items at a time.
-// The frontier tables (two bands, two node tables, the heap, the pending incoming
-// columns) and the node's recorded columns live in shared memory; an extension
-// that outgrows them is re-run with larger tables in global memory.  Each warp
-// writes its DP table into its own arena region, reused extension after
-// extension, so the table the traceback reads was written moments before and
-// stays in L2.
+// The fill's frontier tables (two bands, two node tables, the heap, the pending
+// incoming columns) and a node's recorded columns live in shared memory; an
+// extension that outgrows them is re-run with larger tables in global memory.
+// Fill and traceback are separate kernels so that the warps of an SM share one
+// phase's code: fused, the two phases' code did not fit the instruction caches.
+// Cold paths (crossing rules, end-cell choice, sequential fallbacks) are out of line.
 //
 // Warps take extensions from a device counter over a longest-first order.
 //
@@ -133,6 +137,7 @@ __device__ __forceinline__ int tbl_find(const u64* key, u32 cap, u32 gen, u32 no
 {
     const u32 h = hash_node(node);
     const u64 want = ((u64)gen << 32) | node;
+    #pragma unroll 1
     for (u32 base = 0; base < cap; base += 32)
     {
         const u32 slot = (h + base + lane) & (cap - 1);
@@ -154,6 +159,7 @@ __device__ __forceinline__ int tbl_get_or_add(u64* key, NodeVal* val, u32 cap, u
 {
     const u32 h = hash_node(node);
     const u64 want = ((u64)gen << 32) | node;
+    #pragma unroll 1
     for (u32 base = 0; base < cap; base += 32)
     {
         const u32 slot = (h + base + lane) & (cap - 1);
@@ -379,6 +385,7 @@ __device__ __noinline__ bool merge_existing(WS& ws, const Item& slice, bool hasS
 __device__ __noinline__ bool fix_horizontal(i32 scoreBefore, i32 scoreComparison, u64& fixedHP, u64& fixedHN, u64& forceMask)
 {
     forceMask |= 1;
+    #pragma unroll 1
     for (int off = 1; off < 64; off++)
     {
         i32 next = scoreComparison + (i32)((fixedHP >> off) & 1) - (i32)((fixedHN >> off) & 1);
@@ -436,6 +443,7 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
     const u32 inDeg = g.inOff[i + 1] - g.inOff[i];
     // the match mask of every column (lane k: columns k and k + 32)
     __syncwarp();
+    #pragma unroll 1
     for (u32 pos = lane; pos < nodeLength; pos += 32)
     {
         u64 e;
@@ -457,6 +465,7 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
     }
     else
     {
+        #pragma unroll 1
         for (uint16_t e = head; e != kNil; e = pool[e].next)
         {
             const Extra& inc = pool[e];
@@ -538,6 +547,7 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
     // the traceback's recomputation stops at the column it needs last
     const u32 columns = Fill ? nodeLength : (lastColumn + 1 < nodeLength ? lastColumn + 1 : nodeLength);
     u64 hp = fixedHP >> 1, hn = fixedHN >> 1, fm = forceMask >> 1;   // bit 0: column 1
+    #pragma unroll 1
     for (u32 pos = 1; pos < columns; pos++)
     {
         const u64 eq = eqcol[pos] & forceEq;
@@ -619,16 +629,15 @@ struct ArenaCursor
     u64 used;           // bytes handed out to this warp since the launch began
 };
 
-// bytes from the warp's region, else a chunk of the shared overflow (one atomic per chunk)
+// bytes from the warp's current chunk, else a new chunk (one atomic per chunk)
 __device__ __forceinline__ bool arena_alloc(const FillArgs& a, ArenaCursor& c, u64 bytes, u64& out, u32 lane)
 {
     bytes = align16(bytes);
     if (c.pos + bytes > c.end)
     {
-        const u64 chunk = 64 * 1024;
-        const u64 grab = bytes > chunk ? bytes : chunk;
+        const u64 grab = bytes > a.chunkBytes ? bytes : a.chunkBytes;
         unsigned long long p = 0;
-        if (lane == 0) p = a.overflowBase + atomicAdd(a.arenaCursor, (unsigned long long)grab);
+        if (lane == 0) p = atomicAdd(a.arenaCursor, (unsigned long long)grab);
         p = __shfl_sync(kFull, p, 0);
         if (p + grab > a.arenaBytes) return false;
         c.pos = p;
@@ -665,9 +674,11 @@ __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 in
         dir[index] = off;
     }
     u32* ids = (u32*)(base + sizeof(SliceRec));
+    #pragma unroll 1
     for (u32 k = lane; k < count; k += 32) ids[k] = band[k].node & kNodeMask;
     uint4* dst = (uint4*)(base + sizeof(SliceRec) + idBytes);
     const uint4* src = (const uint4*)band;
+    #pragma unroll 1
     for (u32 k = lane; k < count * 4; k += 32) dst[k] = src[k];
     return true;
 }
@@ -742,6 +753,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
         return true;
     };
 
+    #pragma unroll 1
     for (u32 k = 0; k < prevCount; k++)
     {
         const Item& it = prevBand[k];
@@ -769,6 +781,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
     if (heapN == 0) { err = GA_ASSERT; return res; }
     i32 curMin = res.minScore;
     const i32 seqOffset = (i32)j;
+    #pragma unroll 1
     while (heapN > 0)
     {
         u32 i = w.heap[0].node;
@@ -825,6 +838,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
             if (newEndMin == kIntMax) { err = GA_ASSERT; return res; }
             if (newEndMin <= wadd(curMin, bw))
             {
+                #pragma unroll 1
                 for (u32 e = g.outOff[i]; e < g.outOff[i + 1]; e++)
                 {
                     if (!insert(g.outNb[e], newEndMin, newEnd.VP, newEnd.VN, newEnd.end, false)) { err = GA_CAPACITY; return res; }
@@ -888,7 +902,9 @@ __device__ ExtState fill_extension(const FillArgs& a, const WSpace& w, u32& gen,
         it.minScore = 0;
         it.node = startNode | kExists;
         u64 hn = 0, hp = 0;
+        #pragma unroll 1
         for (u32 k = 1; k <= startOff; k++) hn |= 1ULL << k;
+        #pragma unroll 1
         for (u32 k = startOff + 1; k < L; k++) hp |= 1ULL << k;
         it.HP = hp;
         it.HN = hn;
@@ -907,6 +923,7 @@ __device__ ExtState fill_extension(const FillArgs& a, const WSpace& w, u32& gen,
     i32 bestX = 0;
     i32 lastMin = 0;
     i32 lastQuit = 1;
+    #pragma unroll 1
     for (u32 s = 0; s < numSlices; s++)
     {
         const int cur = prv ^ 1;
@@ -966,6 +983,7 @@ struct Table
         const SliceRec* r = rec(s);
         const u32 n = r->count;
         const u32* ids = (const u32*)((const uint8_t*)r + sizeof(SliceRec));
+        #pragma unroll 1
         for (u32 base = 0; base < n; base += 32)
         {
             const u32 k = base + lane;
@@ -1043,6 +1061,7 @@ __device__ __forceinline__ bool trace_circular(const TraceOut& to)
     if (to.n < 2) return false;
     const u64 keyMask = ~(1ULL << 38);
     u64 last = to.get(to.n - 1);
+    #pragma unroll 1
     for (int k = (int)to.n - 2; k >= 0; k--)
     {
         u64 x = to.get((u32)k);
@@ -1079,6 +1098,7 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
             sp = TPos { node, 0, j - 1 };
             change = false;
         }
+        #pragma unroll 1
         for (u32 e = g.inOff[node]; e < g.inOff[node + 1]; e++)
         {
             u32 nb = g.inNb[e];
@@ -1126,6 +1146,7 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
             }
         }
     }
+    #pragma unroll 1
     for (u32 e = g.inOff[node]; e < g.inOff[node + 1]; e++)
     {
         u32 nb = g.inNb[e];
@@ -1205,6 +1226,7 @@ __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* se
     if (bad) { err = GA_ASSERT; return second; }
     i32 here = col_value(cols[p.off], 0);
     i32 diag = pself->sEnd;
+    #pragma unroll 1
     for (u32 k = 1; k + 1 <= p.off; k++)
     {
         diag += (i32)((pself->HP >> k) & 1);
@@ -1244,6 +1266,7 @@ __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* 
         i32 smallest = ws_value(sws, (int)off - 1);
         TPos sp = TPos { curNode, 0, p.seq - 1 };
         bool change = false;
+        #pragma unroll 1
         for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1]; e++)
         {
             u32 nb = g.inNb[e];
@@ -1268,6 +1291,7 @@ __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* 
         if (tpos_eq(sp, p) && here != fake_value()) { err = GA_ASSERT; return second; }
         return TStep { sp, change };
     }
+    #pragma unroll 1
     for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1]; e++)
     {
         u32 nb = g.inNb[e];
@@ -1307,6 +1331,7 @@ __device__ __noinline__ EndCell end_cell(const DevGraph& g, i32 cost, const uint
     ec.bvOffset = 0xffffffffu;
     i32 bx = kIntMin;
     u32 bs = 0xffffffffu;
+    #pragma unroll 1
     for (u32 s = 1 + lane; s < committed; s += 32)
     {
         const i32 mx = ((const SliceRec*)(arena + t.dir[s]))->maxX;
@@ -1328,6 +1353,7 @@ __device__ __noinline__ EndCell end_cell(const DevGraph& g, i32 cost, const uint
     bool bad = false;
     int candOff = -1;
     u32 candCol = 0xffffffffu;
+    #pragma unroll 1
     for (u32 h = 0; h < 2; h++)
     {
         const u32 i = lane + 32 * h;
@@ -1337,6 +1363,7 @@ __device__ __noinline__ EndCell end_cell(const DevGraph& g, i32 cost, const uint
         if (mx > ec.score) { bad = true; continue; }
         if (mx == ec.score)
         {
+            #pragma unroll 1
             for (int off = 63; off >= 0; off--)
             {
                 if (j + off >= (int64_t)seqLen) continue;
@@ -1371,10 +1398,12 @@ __device__ __noinline__ int row_above(const DevGraph& g, Table t, TraceOut& to)
     auto before = [&](u32 k) -> i32
     {
         i32 v = it->sEnd;
+        #pragma unroll 1
         for (u32 q = 1; q <= k; q++) v += (i32)((it->HP >> q) & 1) - (i32)((it->HN >> q) & 1);
         return v;
     };
     if (before(L - 1) != it->eEnd) return GA_ASSERT;
+    #pragma unroll 1
     while (!to.overflow)
     {
         TPos q = to.back;
@@ -1385,6 +1414,7 @@ __device__ __noinline__ int row_above(const DevGraph& g, Table t, TraceOut& to)
     TPos q = to.back;
     if (!to.overflow && q.off == 0 && before(0) != 0)
     {
+        #pragma unroll 1
         for (u32 e = g.inOff[q.node]; e < g.inOff[q.node + 1]; e++)
         {
             u32 nb = g.inNb[e];
@@ -1450,6 +1480,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
         i32 lastScore = kIntMax - 1;
         u64 guard = 0;
         const u64 guardMax = (u64)cap * 4 + 1024;
+        #pragma unroll 1
         while (!err && !to.overflow && to.back.seq != -1)
         {
             if (++guard > guardMax) { err = GA_CAPACITY; break; }
@@ -1485,18 +1516,21 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 const Item* pself = t.find(curSlice - 1, curNode);
                 if (!pself)
                 {
+                    #pragma unroll 1
                     for (u32 k = b.off - 1; k > 0; k--) to.push(TPos { curNode, k, b.seq }, false);
                     to.push(TPos { curNode, 0, b.seq }, false);
                     continue;
                 }
                 // pickBacktraceVerticalCrossing (Common.h:886-934)
                 TPos p = b;
+                #pragma unroll 1
                 while (p.off > 0 && col_value(cols[p.off - 1], 0) == col_value(cols[p.off], 0) - 1) p.off--;
                 TStep second = p.off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : vertical_step(g, seq, t, curSlice, pself, cols, p, err);
                 if (err) break;
                 if (second.pos.seq == b.seq && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
                 if (p.off != b.off)
                 {
+                    #pragma unroll 1
                     for (u32 k = b.off - 1; k != p.off; k--) to.push(TPos { p.node, k, p.seq }, false);
                 }
                 if (!tpos_eq(p, to.back)) to.push(p, false);
@@ -1510,6 +1544,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 const Item* self = t.find(curSlice, curNode);
                 if (!self) { err = GA_ASSERT; break; }
                 TPos p = b;
+                #pragma unroll 1
                 while (mod64(p.seq) != 0 && (self->sVP & (1ULL << mod64(p.seq)))) p.seq--;
                 const u32 off = mod64(p.seq);
                 TStep second = off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : horizontal_step(g, seq, t, curSlice, curNode, self, p, off, err);
@@ -1517,6 +1552,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 if (second.pos.node == b.node && !second.sw && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
                 if (p.seq != b.seq)
                 {
+                    #pragma unroll 1
                     for (int64_t sp = b.seq - 1; sp != p.seq; sp--) to.push(TPos { p.node, p.off, sp }, false);
                 }
                 if (!tpos_eq(p, to.back)) to.push(p, false);
@@ -1549,6 +1585,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                     i32 here = ws_value(colH, (int)vert);
                     i32 left = ws_value(colL, (int)vert);
                     u64 eqH = colEq(hori);
+                    #pragma unroll 1
                     while (true)
                     {
                         const i32 vs = here - (i32)((colH.VP >> vert) & 1) + (i32)((colH.VN >> vert) & 1);
@@ -1617,11 +1654,27 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
     }
 }
 
-// One persistent launch per batch: a warp takes the next extension of the longest-first
-// order, fills its DP table into the warp's arena region and walks it back, then takes the
-// next.  The tables are in dynamic shared memory (fa.workspace == nullptr) or in the
-// global workspace, one stride per warp.
-__global__ void __launch_bounds__(128, 4) extend_kernel(FillArgs fa, TraceArgs ta, u32* counter)
+// The next extension for this warp from the work counter, or false when none is left;
+// with a filter only extensions whose previous status is GA_CAPACITY are taken.
+__device__ __forceinline__ bool next_extension(u32* counter, u32 num, const u32* order, const i32* prevStatus, u32 lane, u32& ext)
+{
+#pragma unroll 1
+    while (true)
+    {
+        u32 k = 0;
+        if (lane == 0) k = atomicAdd(counter, 1u);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= num) return false;
+        ext = order ? order[k] : k;
+        if (!prevStatus || prevStatus[ext] == GA_CAPACITY) return true;
+    }
+}
+
+// The fill: a warp takes the next extension of the longest-first order, fills its DP table
+// into the arena and records where it is, then takes the next.  The frontier tables are in
+// dynamic shared memory (fa.workspace == nullptr) or in the global workspace, one stride
+// per warp.
+__global__ void __launch_bounds__(128, 4) fill_kernel(FillArgs fa, u32* counter)
 {
     extern __shared__ __align__(16) uint8_t dsmem[];
     load_iupac_table();
@@ -1631,6 +1684,7 @@ __global__ void __launch_bounds__(128, 4) extend_kernel(FillArgs fa, TraceArgs t
     uint8_t* base = fa.workspace ? fa.workspace + gwarp * fa.workspaceStride : dsmem + (u64)warpInBlock * fa.workspaceStride;
     const WSpace w = wspace_at(base, fa.caps);
     // generation 0 marks every node-table slot empty
+#pragma unroll 1
     for (u32 k = lane; k < fa.caps.hash; k += 32)
     {
         w.key[0][k] = 0;
@@ -1638,27 +1692,22 @@ __global__ void __launch_bounds__(128, 4) extend_kernel(FillArgs fa, TraceArgs t
     }
     __syncwarp();
     u32 gen = 0;
-    const u64 region = gwarp * fa.regionBytes;
     ArenaCursor arena;
+    arena.pos = 0;
+    arena.end = 0;
     arena.used = 0;
-    while (true)
+    u32 ext;
+#pragma unroll 1
+    while (next_extension(counter, fa.num, fa.order, fa.prevStatus, lane, ext))
     {
-        u32 k = 0;
-        if (lane == 0) k = atomicAdd(counter, 1u);
-        k = __shfl_sync(kFull, k, 0);
-        if (k >= fa.num) break;
-        const u32 ext = fa.order ? fa.order[k] : k;
-        if (fa.prevStatus && fa.prevStatus[ext] != GA_CAPACITY) continue;
         __syncwarp();
-        arena.pos = region;
-        arena.end = region + fa.regionBytes;
-        ExtState st = fill_extension(fa, w, gen, arena, ext, lane);
-        __syncwarp();
-        trace_extension(ta, ext, st, w, lane);
+        const ExtState st = fill_extension(fa, w, gen, arena, ext, lane);
+        if (lane == 0) fa.states[ext] = st;
         if (gen > 0xF0000000u)
         {
             // generation stamps are about to wrap: clear this warp's tables
             __syncwarp();
+#pragma unroll 1
             for (u32 k2 = lane; k2 < fa.caps.hash; k2 += 32)
             {
                 w.key[0][k2] = 0;
@@ -1671,26 +1720,65 @@ __global__ void __launch_bounds__(128, 4) extend_kernel(FillArgs fa, TraceArgs t
     if (lane == 0 && arena.used) atomicAdd(fa.arenaCursor + 1, (unsigned long long)arena.used);
 }
 
+static constexpr u32 kTraceSpaceBytes = 64 * sizeof(Col) + 64 * 8 + 64 * 8;
+
+// The traceback: a warp takes the next filled extension and walks its table back.  Its
+// shared memory holds the recomputed columns, the match masks and the trace staging.
+__global__ void __launch_bounds__(128, 6) trace_kernel(TraceArgs ta, u32* counter)
+{
+    extern __shared__ __align__(16) uint8_t dsmem[];
+    load_iupac_table();
+    const u32 lane = threadIdx.x & 31;
+    uint8_t* base = dsmem + (u64)(threadIdx.x >> 5) * kTraceSpaceBytes;
+    WSpace w {};
+    w.cols = (Col*)base;
+    w.eqcol = (u64*)(base + 64 * sizeof(Col));
+    w.ring = (u64*)(base + 64 * sizeof(Col) + 64 * 8);
+    u32 ext;
+#pragma unroll 1
+    while (next_extension(counter, ta.num, ta.order, ta.prevStatus, lane, ext))
+    {
+        __syncwarp();
+        trace_extension(ta, ext, ta.states[ext], w, lane);
+    }
+}
+
 }
 
 uint64_t ga_warp_tables_bytes(const gadev::Caps& c) { return gadev::wspace_bytes(c); }
 
-int ga_extend_blocks_per_sm(int warpsPerBlock, const gadev::Caps& caps, bool shared)
+static bool set_smem(const void* kernel, size_t smem)
+{
+    return smem <= 48 * 1024 || cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+}
+
+int ga_fill_blocks_per_sm(int warpsPerBlock, const gadev::Caps& caps, bool shared)
 {
     const size_t smem = shared ? (size_t)gadev::wspace_bytes(caps) * warpsPerBlock : 0;
-    if (smem > 48 * 1024 && cudaFuncSetAttribute(gadev::extend_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return 0;
+    if (!set_smem((const void*)gadev::fill_kernel, smem)) return 0;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::extend_kernel, warpsPerBlock * 32, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::fill_kernel, warpsPerBlock * 32, smem) != cudaSuccess) return 0;
     return n;
 }
 
-int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counter, int blocks, int warpsPerBlock, void* stream)
+int ga_trace_blocks_per_sm(int warpsPerBlock)
 {
-    const size_t smem = fa.workspace ? 0 : (size_t)fa.workspaceStride * warpsPerBlock;
-    if (smem > 48 * 1024 && cudaFuncSetAttribute(gadev::extend_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return -1;
-    gadev::extend_kernel<<<blocks, warpsPerBlock * 32, smem, (cudaStream_t)stream>>>(fa, ta, counter);
+    const size_t smem = (size_t)gadev::kTraceSpaceBytes * warpsPerBlock;
+    if (!set_smem((const void*)gadev::trace_kernel, smem)) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gadev::trace_kernel, warpsPerBlock * 32, smem) != cudaSuccess) return 0;
+    return n;
+}
+
+int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
+    int warpsPerBlock, void* stream)
+{
+    const size_t fillSmem = fa.workspace ? 0 : (size_t)fa.workspaceStride * warpsPerBlock;
+    const size_t traceSmem = (size_t)gadev::kTraceSpaceBytes * warpsPerBlock;
+    if (!set_smem((const void*)gadev::fill_kernel, fillSmem) || !set_smem((const void*)gadev::trace_kernel, traceSmem)) return -1;
+    gadev::fill_kernel<<<fillBlocks, warpsPerBlock * 32, fillSmem, (cudaStream_t)stream>>>(fa, counters);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    gadev::trace_kernel<<<traceBlocks, warpsPerBlock * 32, traceSmem, (cudaStream_t)stream>>>(ta, counters + 1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -1,4 +1,4 @@
-// Shared declarations of the batched seed-extension kernel (fill + traceback, one warp per extension).
+// Shared declarations of the batched seed-extension kernels (fill, then traceback; one warp per extension).
 #pragma once
 #include <stdint.h>
 #include "wordslice.cuh"
@@ -82,21 +82,25 @@ struct FillArgs
     const u32* seqLen;
     const u32* startNode;
     const u32* startOffset;
-    uint8_t* arena;        // per-warp regions [0, overflowBase), then the shared overflow
+    uint8_t* arena;        // DP tables of the batch, handed out in chunks
     u64 arenaBytes;
-    unsigned long long* arenaCursor;   // [0] overflow bytes handed out, [1] bytes the warps took (both start at 0)
-    u64 regionBytes;       // DP-table region of each warp, reused extension after extension
-    u64 overflowBase;      // warps * regionBytes
+    unsigned long long* arenaCursor;   // [0] bytes handed out in chunks, [1] bytes the tables took (both start at 0)
+    u64 chunkBytes;        // arena bytes a warp takes at once
     uint8_t* workspace;    // nullptr: the frontier tables live in shared memory
     u64 workspaceStride;   // bytes of one warp's tables
     Caps caps;
     const i32* prevStatus; // when non-null, only extensions whose previous status is GA_CAPACITY run
+    ExtState* states;      // [num] where each extension's table is, for the traceback
 };
 
 struct TraceArgs
 {
     DevGraph g;
     i32 cost;
+    u32 num;
+    const u32* order;      // the fill's processing order; nullptr = index order
+    const i32* prevStatus; // the fill's filter
+    const ExtState* states;
     const uint8_t* seq;
     const u64* seqOff;
     const u32* seqLen;
@@ -114,10 +118,13 @@ struct TraceArgs
 
 // bytes of one warp's frontier tables for these capacities
 uint64_t ga_warp_tables_bytes(const gadev::Caps& caps);
-// resident blocks of 32 * warpsPerBlock threads per SM; shared: tables in shared memory
-int ga_extend_blocks_per_sm(int warpsPerBlock, const gadev::Caps& caps, bool shared);
-// launches the extension kernel: `blocks` blocks of warpsPerBlock warps, one extension per warp at a time
-int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counter, int blocks, int warpsPerBlock,
-    void* stream);
+// resident blocks of 32 * warpsPerBlock threads per SM of the fill kernel (shared: tables in
+// shared memory) and of the traceback kernel
+int ga_fill_blocks_per_sm(int warpsPerBlock, const gadev::Caps& caps, bool shared);
+int ga_trace_blocks_per_sm(int warpsPerBlock);
+// launches the fill kernel and then the traceback kernel on `stream`, blocks of warpsPerBlock
+// warps, one extension per warp at a time; counters[0] and [1] must be zero
+int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
+    int warpsPerBlock, void* stream);
 int ga_upload_tables();
 void ga_set_last_error(const char* message);

@@ -3,11 +3,12 @@
 // It serves callers that cannot call cudaMalloc when they extend: processes whose
 // device memory is handed out by another allocator under a fixed budget (a
 // framework's caching pool owns the GPU), and request paths where the device-wide
-// synchronisation of cudaMalloc/cudaFree is not acceptable.  The extension kernel
-// keeps its frontier tables in shared memory; the only other scratch it needs -- a
-// work counter, the arena cursors and the DP-table arena the fill writes and the
-// traceback reads -- lives in the file-scope device array below, which every GPU
-// that loads this library holds until the process exits.  Inputs and outputs are
+// synchronisation of cudaMalloc/cudaFree is not acceptable.  The fill kernel keeps
+// its frontier tables in shared memory; the only other scratch the two kernels need --
+// work counters, the arena cursors, where each extension's DP table is, and the
+// DP-table arena the fill writes and the traceback reads -- lives in the file-scope
+// device array below, which every GPU that loads this library holds until the
+// process exits.  Inputs and outputs are
 // the caller's device buffers.
 #include <cuda_runtime.h>
 #include <mutex>
@@ -20,7 +21,8 @@ namespace
 using namespace gadev;
 
 constexpr u64 kScratchBytes = 128ULL << 20;       // 128 MiB per GPU
-constexpr u64 kHeaderBytes = 256;                 // work counter, status count, arena cursors
+constexpr u64 kHeaderBytes = 256;                 // work counters and arena cursors
+constexpr u64 kStatesBytes = 4096 * 32;           // where the fill left each extension's table
 constexpr u32 kWarpsPerBlock = 4;
 constexpr u32 kBlocks = 64;                       // 256 warps
 constexpr u32 kMaxExtensions = 4096;              // per call
@@ -131,8 +133,7 @@ extern "C" int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const 
     g.lin = gd.linearizable;
     g.comp = gd.component;
 
-    const u64 warps = (u64)kBlocks * kWarpsPerBlock;
-    const u64 arenaBytes = kScratchBytes - kHeaderBytes;
+    const u64 arenaBytes = kScratchBytes - kHeaderBytes - kStatesBytes;
     FillArgs fa {};
     fa.g = g;
     fa.bandwidth = params->bandwidth;
@@ -146,16 +147,15 @@ extern "C" int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const 
     fa.seqLen = bd.seq_len;
     fa.startNode = bd.start_node;
     fa.startOffset = bd.start_offset;
-    fa.arena = scratch + kHeaderBytes;
+    fa.arena = scratch + kHeaderBytes + kStatesBytes;
     fa.arenaBytes = arenaBytes;
     fa.arenaCursor = (unsigned long long*)(scratch + 16);
-    // half the arena is split into per-warp regions (256 KiB each), the rest is the overflow
-    fa.regionBytes = (arenaBytes / 2 / warps) & ~15ULL;
-    fa.overflowBase = warps * fa.regionBytes;
+    fa.chunkBytes = 16 * 1024;
     fa.workspace = nullptr;
     fa.caps = small_caps();
     fa.workspaceStride = ga_warp_tables_bytes(fa.caps);
     fa.prevStatus = nullptr;
+    fa.states = (ExtState*)(scratch + kHeaderBytes);
 
     TraceArgs ta {};
     ta.g = g;
@@ -163,7 +163,7 @@ extern "C" int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const 
     ta.seq = bd.seq;
     ta.seqOff = bd.seq_offset;
     ta.seqLen = bd.seq_len;
-    ta.arena = scratch + kHeaderBytes;
+    ta.arena = fa.arena;
     ta.traceOffset = bd.trace_offset;
     ta.traceCap = bd.trace_capacity;
     ta.status = rd.status;
@@ -171,8 +171,12 @@ extern "C" int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const 
     ta.traceLen = rd.trace_len;
     ta.traceItems = rd.trace_items;
     ta.cellSteps = rd.cell_steps;
+    ta.num = n;
+    ta.order = nullptr;
+    ta.prevStatus = nullptr;
+    ta.states = fa.states;
 
-    if (ga_launch_extend(fa, ta, (u32*)scratch, (int)kBlocks, (int)kWarpsPerBlock, s) != 0)
+    if (ga_launch_extend(fa, ta, (u32*)scratch, (int)kBlocks, (int)kBlocks, (int)kWarpsPerBlock, s) != 0)
     {
         ga_set_last_error("ga_extend_batch_noalloc: kernel launch failed");
         return GA_ERR_CUDA;

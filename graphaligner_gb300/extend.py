@@ -170,15 +170,15 @@ class DeviceGraph:
 
 
 class LaunchShape(ctypes.Structure):
-    """ga_launch_shape: how the extension kernel is launched (one warp per extension; results
+    """ga_launch_shape: how the extension kernels are launched (one warp per extension; results
     never depend on it): warps per block, resident blocks per SM (0 = as many as fit), the
-    first pass's frontier-table layout (0 shared memory, 1/2 global memory) and the per-warp
-    DP-table region in KiB."""
+    first pass's frontier-table layout (0 shared memory, 1/2 global memory) and the arena
+    chunk a warp takes at once, in KiB."""
     _fields_ = [
         ("warps_per_block", ctypes.c_uint32),
         ("blocks_per_sm", ctypes.c_uint32),
         ("first_layout", ctypes.c_uint32),
-        ("region_kib", ctypes.c_uint32),
+        ("chunk_kib", ctypes.c_uint32),
     ]
 
     def as_dict(self):
@@ -188,10 +188,10 @@ class LaunchShape(ctypes.Structure):
         return tuple(getattr(self, n) for n, _ in self._fields_)
 
 
-# launch shapes the autotuner tries: (warps_per_block, blocks_per_sm, first_layout, region_kib)
+# launch shapes the autotuner tries: (warps_per_block, blocks_per_sm, first_layout, chunk_kib)
 DEFAULT_CANDIDATES = [
-    (4, 0, 0, 128), (2, 0, 0, 128), (1, 0, 0, 128), (4, 3, 0, 128), (4, 2, 0, 128),
-    (4, 0, 0, 32), (4, 0, 0, 512), (4, 0, 1, 128),
+    (4, 0, 0, 64), (2, 0, 0, 64), (1, 0, 0, 64), (4, 3, 0, 64), (4, 2, 0, 64),
+    (4, 0, 0, 16), (4, 0, 0, 256), (4, 0, 1, 64),
 ]
 
 
@@ -220,8 +220,8 @@ class Extender:
         check(lib().ga_extender_get_launch_shape(self.handle, ctypes.byref(sh)))
         return sh
 
-    def set_launch_shape(self, warps_per_block=4, blocks_per_sm=0, first_layout=0, region_kib=128):
-        sh = LaunchShape(warps_per_block, blocks_per_sm, first_layout, region_kib)
+    def set_launch_shape(self, warps_per_block=4, blocks_per_sm=0, first_layout=0, chunk_kib=64):
+        sh = LaunchShape(warps_per_block, blocks_per_sm, first_layout, chunk_kib)
         check(lib().ga_extender_set_launch_shape(self.handle, ctypes.byref(sh)))
 
     def autotune(self, params: ExtendParams, batch: PackedBatch, candidates=None, sample_every: int = 4, repeats: int = 2) -> dict:

@@ -162,11 +162,11 @@ int ga_extend_batch_device(ga_extender_t ext, const ga_extend_params* params,
 int ga_extend_batch_noalloc(const ga_graph_desc* device_graph, const ga_extend_params* params,
                             const ga_extend_batch_desc* device_batch, ga_extend_results* device_results,
                             void* stream);
-/* Kernel time of the last ga_extend_batch* call in milliseconds (CUDA events on
- * the launching stream); valid after the stream has been synchronised. */
+/* Kernel time (fill and traceback) of the last ga_extend_batch* call in milliseconds
+ * (CUDA events on the launching stream); valid after the stream has been synchronised. */
 int ga_extender_last_kernel_ms(ga_extender_t ext, float* ms);
-/* The same as a pair: fill and traceback run fused in one kernel, so fill_ms is the
- * kernel time and trace_ms is 0. */
+/* The same as a pair: fill_ms is the time of the fill and traceback kernels together
+ * (they run back to back on one stream) and trace_ms is 0. */
 int ga_extender_last_times(ga_extender_t ext, float* fill_ms, float* trace_ms);
 /* Host-to-device and device-to-host copy times of the last ga_extend_batch call in
  * milliseconds (CUDA events; the trace items' copy spans the copy streams); 0 after
@@ -175,27 +175,27 @@ int ga_extender_last_copy_ms(ga_extender_t ext, float* h2d_ms, float* d2h_ms);
 /* Number of kernel launches made by the last ga_extend_batch* call. */
 int ga_extender_last_launches(ga_extender_t ext, uint32_t* launches);
 
-/* How the extension kernel is launched (no reference counterpart: it never changes a
- * result).  One warp runs one extension at a time, taking the next of the batch's
- * longest-first order.  warps_per_block (1..4) warps share a block; blocks_per_sm
- * caps the resident blocks per SM (0 = as many as registers and shared memory allow).
- * first_layout picks the frontier tables of the first pass: 0 = small tables in
- * shared memory (variation graphs), 1 = medium tables in global memory, 2 = large
- * tables in global memory (tangled de Bruijn graphs); extensions that outgrow them
- * (GA_CAPACITY) run again with the next layout.  region_kib: each warp's DP-table
- * region in the arena, reused extension after extension (longer tables continue in
- * the arena's shared overflow). */
+/* How the extension kernels are launched (no reference counterpart: it never changes a
+ * result).  A fill kernel and then a traceback kernel run one extension per warp,
+ * each warp taking the next of the batch's longest-first order.  warps_per_block
+ * (1..4) warps share a block; blocks_per_sm caps the resident blocks per SM (0 = as
+ * many as registers and shared memory allow).  first_layout picks the fill's frontier
+ * tables in the first pass: 0 = small tables in shared memory (variation graphs),
+ * 1 = medium tables in global memory, 2 = large tables in global memory (tangled de
+ * Bruijn graphs); extensions that outgrow them (GA_CAPACITY) run again with the next
+ * layout.  chunk_kib (1..2^20): the arena bytes a warp takes at once for the DP
+ * tables of the extensions it fills. */
 typedef struct ga_launch_shape {
     uint32_t warps_per_block;
     uint32_t blocks_per_sm;
     uint32_t first_layout;
-    uint32_t region_kib;
+    uint32_t chunk_kib;
 } ga_launch_shape;
 int ga_extender_set_launch_shape(ga_extender_t ext, const ga_launch_shape* shape);
 int ga_extender_get_launch_shape(ga_extender_t ext, ga_launch_shape* shape);
 /* Times `count` launch shapes on a host batch and makes the fastest the extender's
  * shape (no reference counterpart; the autotuner over warps per block, resident
- * blocks, first table layout and DP-table region).  The batch is copied to the device once; each
+ * blocks, first table layout and arena chunk).  The batch is copied to the device once; each
  * shape runs `repeats` times there (kernel time by CUDA events, the median kept) and
  * only statuses and scores come back: no trace is copied to the host.  Every shape
  * must reproduce the first one's statuses and scores, else GA_ERR_STATE and the first

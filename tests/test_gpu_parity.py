@@ -95,14 +95,14 @@ def test_gpu_matches_oracle_generated(cuda_lib, oracle_lib):
 
 
 def test_launch_shapes_do_not_change_results(cuda_lib):
-    """How the kernel is launched never changes a result: every launch shape (warps per block,
-    resident blocks, first table layout, DP-table region, including regions so small that every
-    table continues in the shared overflow) gives the reference's digests."""
+    """How the kernels are launched never changes a result: every launch shape (warps per block,
+    resident blocks, first table layout, arena chunk, including chunks smaller than one slice
+    record) gives the reference's digests."""
     from graphaligner_gb300._lib import GAError
     g, batch = golden_case("vg50k")
     x = Extender(DeviceGraph(g))
     expected = load_digests("vg50k", 10)
-    for shape in [(4, 0, 0, 128), (1, 1, 0, 128), (2, 0, 1, 64), (3, 2, 2, 8), (4, 0, 0, 0)]:
+    for shape in [(4, 0, 0, 64), (1, 1, 0, 128), (2, 0, 1, 64), (3, 2, 2, 8), (4, 0, 0, 1)]:
         x.set_launch_shape(*shape)
         res = x.run(ExtendParams(bandwidth=10), batch)
         bad = compare(res, expected)
@@ -113,7 +113,9 @@ def test_launch_shapes_do_not_change_results(cuda_lib):
         x.set_launch_shape(5, 0, 0, 128)
     with pytest.raises(GAError):
         x.set_launch_shape(4, 0, 3, 128)
-    cands = [(4, 0, 0, 128), (1, 0, 0, 16), (2, 2, 1, 128)]
+    with pytest.raises(GAError):
+        x.set_launch_shape(4, 0, 0, 0)
+    cands = [(4, 0, 0, 64), (1, 0, 0, 16), (2, 2, 1, 128)]
     tuned = x.autotune(ExtendParams(bandwidth=10), batch, candidates=cands, sample_every=2, repeats=1)
     assert len(tuned["candidates_ms"]) == len(cands) and all(ms > 0 for ms, _ in tuned["candidates_ms"])
     best_ms = min(ms for ms, _ in tuned["candidates_ms"])
@@ -132,7 +134,7 @@ def test_table_layouts_agree_on_dbg(cuda_lib):
     expected = load_digests("dbg100k", 10)
     p = ExtendParams(bandwidth=10, max_cells_per_slice=MAX_CELLS["dbg100k"])
     for layout in (0, 1, 2):
-        x.set_launch_shape(4, 0, layout, 128)
+        x.set_launch_shape(4, 0, layout, 64)
         res = x.run(p, batch)
         bad = compare(res, expected)
         assert not bad, f"first layout {layout}: {len(bad)} extensions differ"
