@@ -96,6 +96,7 @@ struct WSpace
     Col* cols;          // [64]
     u64* eqcol;         // [64] match mask of each column of the current node
     u64* ring;          // [64] trace items not yet written out
+    struct SliceSlot* slots;   // [2] the traceback's cached slices (odd and even)
 };
 
 __host__ __device__ inline u64 align16(u64 x) { return (x + 15) & ~15ULL; }
@@ -503,7 +504,8 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
     result.minScoreNode = i;
     result.minScoreOffset = 0;
     result.maxXNode = i;
-    if ((slice.node & kExists) != 0 && merge_existing(ws, slice, hasSkipless, inDeg == 1 && singleInPrevBand, lane) && Fill)
+    // (the recomputation starts from the stored first column, whose merge with itself changes nothing)
+    if (Fill && (slice.node & kExists) != 0 && merge_existing(ws, slice, hasSkipless, inDeg == 1 && singleInPrevBand, lane))
     {
         if (!boundOk || xscore_bound(ws0, seqOffset, cost) > (int64_t)sliceMaxX)
             result.maxX = ws_max_xscore(ws0, seqOffset, cost, 64, kAllOnes);
@@ -958,41 +960,77 @@ __device__ ExtState fill_extension(const FillArgs& a, const WSpace& w, u32& gen,
 
 // ---------------------------------------------------------------- traceback
 
+// A copy in shared memory of one committed slice whose band has at most kCachedBand nodes:
+// the traceback works on one slice and the one before it, so two slots (by the slice's
+// parity) hold both, and their band lookups are ballots over shared memory.
+static constexpr u32 kCachedBand = 16;
+
+struct __align__(16) SliceSlot
+{
+    SliceRec rec;
+    u32 slice;             // the cached slice, 0xffffffff = none
+    u32 pad[3];
+    u32 ids[kCachedBand];
+    Item items[kCachedBand];
+};
+
+// The record of slice s; a band of at most kCachedBand nodes is first copied into the
+// slot of the slice's parity (lanes copy 16 bytes each)
+__device__ __noinline__ const SliceRec* load_slice(const uint8_t* arena, const u64* dir, SliceSlot* slots, u32 s, u32 lane)
+{
+    const SliceRec* r = (const SliceRec*)(arena + dir[s]);
+    const u32 n = r->count;
+    if (n > kCachedBand) return r;
+    SliceSlot& sl = slots[s & 1];
+    __syncwarp();
+    const uint4* src = (const uint4*)r;
+    const u32* ids = (const u32*)((const uint8_t*)r + sizeof(SliceRec));
+    const uint4* items = (const uint4*)((const uint8_t*)ids + rec_ids_bytes(n));
+    if (lane < 2) ((uint4*)&sl.rec)[lane] = src[lane];
+    if (lane < n) sl.ids[lane] = ids[lane];
+#pragma unroll 1
+    for (u32 k = lane; k < n * 4; k += 32) ((uint4*)sl.items)[k] = items[k];
+    sl.slice = s;
+    __syncwarp();
+    return &sl.rec;
+}
+
 struct Table
 {
     const uint8_t* arena;
     const u64* dir;
     u32 count;
     u32 lane;
-    // the traceback works on one slice and the one before it: their records are remembered
-    u32 cs[2];
-    const SliceRec* cr[2];
-    __device__ __forceinline__ void init() { cs[0] = cs[1] = 0xffffffffu; cr[0] = cr[1] = nullptr; }
+    SliceSlot* slots;
+    __device__ __forceinline__ void init()
+    {
+        slots[0].slice = 0xffffffffu;
+        slots[1].slice = 0xffffffffu;
+        __syncwarp();
+    }
+    // the slice's record: its shared copy (made on first use when the band is small), else
+    // the arena's
     __device__ __forceinline__ const SliceRec* rec(u32 s)
     {
-        if (cs[0] == s) return cr[0];
-        if (cs[1] == s) return cr[1];
-        const SliceRec* r = (const SliceRec*)(arena + dir[s]);
-        cs[1] = cs[0]; cr[1] = cr[0];
-        cs[0] = s; cr[0] = r;
-        return r;
+        SliceSlot& sl = slots[s & 1];
+        if (sl.slice == s) return &sl.rec;
+        return load_slice(arena, dir, slots, s, lane);
     }
     // the band entry of node in slice s (a ballot over the slice's node ids), or nullptr
     __device__ __forceinline__ const Item* find(u32 s, u32 node)
     {
         const SliceRec* r = rec(s);
         const u32 n = r->count;
-        const u32* ids = (const u32*)((const uint8_t*)r + sizeof(SliceRec));
-        #pragma unroll 1
+        const SliceSlot& sl = slots[s & 1];
+        const bool cached = sl.slice == s;
+        const u32* ids = cached ? sl.ids : (const u32*)((const uint8_t*)r + sizeof(SliceRec));
+        const Item* items = cached ? sl.items : (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
+#pragma unroll 1
         for (u32 base = 0; base < n; base += 32)
         {
             const u32 k = base + lane;
             const u32 hit = __ballot_sync(kFull, k < n && ids[k] == node);
-            if (hit)
-            {
-                const Item* items = (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
-                return &items[base + __ffs((int)hit) - 1];
-            }
+            if (hit) return &items[base + __ffs((int)hit) - 1];
         }
         return nullptr;
     }
@@ -1013,6 +1051,14 @@ struct TStep
     bool sw;
 };
 
+// writes the 32 staged trace items that end at item n (lane k writes one)
+__device__ __noinline__ void flush32(u64* items, const u64* ring, u32 n, u32 lane)
+{
+    const u32 k = n - 32 + lane;
+    items[k] = ring[k & 63];
+    __syncwarp();
+}
+
 // Trace items go to a 64-entry ring in shared memory (every lane writes every item) and
 // out to the caller's buffer 32 at a time, one item per lane.
 struct TraceOut
@@ -1031,17 +1077,7 @@ struct TraceOut
         ring[n & 63] = (u64)p.node | ((u64)(p.off & 63) << 32) | ((u64)(sw ? 1 : 0) << 38) | (sp1 << 39);
         n++;
         back = p;
-        if ((n & 31) == 0)
-        {
-            const u32 k = n - 32 + lane;
-            items[k] = ring[k & 63];
-            __syncwarp();
-        }
-    }
-    // item k (k < n): from the ring while it holds it, else from the written output
-    __device__ __forceinline__ u64 get(u32 k) const
-    {
-        return k + 63 >= n ? ring[k & 63] : items[k];
+        if ((n & 31) == 0) flush32(items, ring, n, lane);
     }
     // writes the items of the last, partial group of 32
     __device__ __forceinline__ void finish()
@@ -1055,16 +1091,17 @@ struct TraceOut
 __device__ __forceinline__ u32 mod64(int64_t seq) { return (u32)((u64)seq & 63); }
 
 // checkBacktraceCircularity (Common.h:760-768): the newest item must not repeat an
-// earlier item of the same read position
-__device__ __forceinline__ bool trace_circular(const TraceOut& to)
+// earlier item of the same read position.  Items still in the ring are read there, older
+// ones from the written output.
+__device__ __noinline__ bool trace_circular(const u64* items, const u64* ring, u32 n)
 {
-    if (to.n < 2) return false;
+    if (n < 2) return false;
     const u64 keyMask = ~(1ULL << 38);
-    u64 last = to.get(to.n - 1);
-    #pragma unroll 1
-    for (int k = (int)to.n - 2; k >= 0; k--)
+    const u64 last = ring[(n - 1) & 63];
+#pragma unroll 1
+    for (int k = (int)n - 2; k >= 0; k--)
     {
-        u64 x = to.get((u32)k);
+        const u64 x = (u32)k + 63 >= n ? ring[k & 63] : items[k];
         if ((x & keyMask) == (last & keyMask)) return true;
         if ((x >> 39) != (last >> 39)) return false;
     }
@@ -1452,6 +1489,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
     t.dir = (const u64*)(a.arena + st.dir);
     t.count = st.committed;
     t.lane = lane;
+    t.slots = w.slots;
     t.init();
     Col* cols = w.cols;
     TraceOut to;
@@ -1508,7 +1546,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 if (err) break;
                 if (tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == fake_value()) break;
                 to.push(bt.pos, bt.sw);
-                if (!to.overflow && trace_circular(to)) { err = GA_ASSERT; break; }
+                if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
                 continue;
             }
             if (row == 0)
@@ -1558,7 +1596,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 if (!tpos_eq(p, to.back)) to.push(p, false);
                 if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
                 to.push(second.pos, second.sw);
-                if (!to.overflow && trace_circular(to)) { err = GA_ASSERT; break; }
+                if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
                 continue;
             }
             // pickBacktraceInside (Common.h:770-815).  The four neighbouring scores are
@@ -1720,7 +1758,7 @@ __global__ void __launch_bounds__(128, 4) fill_kernel(FillArgs fa, u32* counter)
     if (lane == 0 && arena.used) atomicAdd(fa.arenaCursor + 1, (unsigned long long)arena.used);
 }
 
-static constexpr u32 kTraceSpaceBytes = 64 * sizeof(Col) + 64 * 8 + 64 * 8;
+static constexpr u32 kTraceSpaceBytes = 64 * sizeof(Col) + 64 * 8 + 64 * 8 + 2 * sizeof(SliceSlot);
 
 // The traceback: a warp takes the next filled extension and walks its table back.  Its
 // shared memory holds the recomputed columns, the match masks and the trace staging.
@@ -1734,6 +1772,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(TraceArgs ta, u32* counte
     w.cols = (Col*)base;
     w.eqcol = (u64*)(base + 64 * sizeof(Col));
     w.ring = (u64*)(base + 64 * sizeof(Col) + 64 * 8);
+    w.slots = (SliceSlot*)(base + 64 * sizeof(Col) + 64 * 8 + 64 * 8);
     u32 ext;
 #pragma unroll 1
     while (next_extension(counter, ta.num, ta.order, ta.prevStatus, lane, ext))
