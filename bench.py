@@ -85,16 +85,62 @@ def dist_env():
     return rank, world, local
 
 
-def make_workload(n_reads: int, rank: int, truncate: int = 0):
+def make_workload(n_reads: int, rank: int, truncate: int = 0, native: bool = True):
+    """The batch's graph and extensions.  native=False builds the graph with the Python
+    restatement of the builder (tests/gfa_restatement.py, array for array the native
+    builder's graph), so that a process timing the CPU implementation never loads the
+    product's library."""
     from graphaligner_gb300 import datagen as dg
-    from graphaligner_gb300 import graph as gg
     from graphaligner_gb300.extend import pack_batch
     vg = dg.batch_vg(0)
-    g = gg.build_from_gfa(vg.to_gfa())
+    if native:
+        from graphaligner_gb300 import graph as gg
+        g = gg.build_from_gfa(vg.to_gfa())
+    else:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import gfa_restatement
+        g = gfa_restatement.build_from_gfa(vg.to_gfa())
     ext = dg.batch_extension_workload(n_reads, graph_seed=0, read_seed=1 + rank)
     seqs = [x[:truncate] for x in ext.seqs] if truncate else ext.seqs
     batch = pack_batch(g, seqs, ext.bignode, ext.offset)
     return g, batch
+
+
+def workload_config(g, batch, params, world: int) -> dict:
+    return {"workload": WORKLOAD, "extensions": int(batch.num), "read_bp": int(batch.seq_len.astype(np.int64).sum()),
+            "graph_nodes": int(g.num_nodes), "bandwidth": int(params.bandwidth), "xdrop": int(params.xdrop),
+            "l2": "inputs larger than L2 (sequences + DP-table arena written every step)",
+            "parallelism": f"replicas{world}"}
+
+
+def trace_checksums(res, idx) -> np.ndarray:
+    """Per extension at idx, a 64-bit checksum of its packed trace items (each item mixed with
+    its position, so reordered or shifted items change it); 0 for an empty trace."""
+    idx = np.asarray(idx, dtype=np.int64)
+    out = np.zeros(len(idx), dtype=np.uint64)
+    for a in range(0, len(idx), 4096):
+        sel = idx[a:a + 4096]
+        lens = res.trace_len[sel].astype(np.int64)
+        offs = res.trace_offset[sel].astype(np.int64)
+        total = int(lens.sum())
+        if total == 0:
+            continue
+        seg = np.cumsum(lens) - lens
+        within = np.arange(total, dtype=np.int64) - np.repeat(seg, lens)
+        items = res.trace_items[np.repeat(offs, lens) + within]
+        mixed = (items ^ (within.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15))) * np.uint64(0xBF58476D1CE4E5B9)
+        nz = lens > 0
+        part = np.zeros(len(sel), dtype=np.uint64)
+        part[nz] = np.add.reduceat(mixed, seg[nz])
+        out[a:a + 4096] = part
+    return out
+
+
+def result_key(res, idx) -> np.ndarray:
+    """(status, score, items, item checksum) per extension at idx: equal keys mean equal results."""
+    idx = np.asarray(idx, dtype=np.int64)
+    return np.stack([res.status[idx].astype(np.int64), res.score[idx].astype(np.int64),
+                     res.trace_len[idx].astype(np.int64), trace_checksums(res, idx).view(np.int64)])
 
 
 def aligned_bp(res) -> int:
@@ -178,12 +224,27 @@ def cpu_baseline(g, batch, params, sample_bp: float, threads: int):
             "sample": f"{len(idx)} of {batch.num} extensions (every {step}th, {int(lens[idx].sum())} read bp), oracle restatement in C++, {threads} threads, {dt:.1f} s"}, res, idx
 
 
+def repo_libraries_loaded() -> list:
+    """The shared libraries under this repository that this process has mapped (/proc/self/maps)."""
+    found = set()
+    try:
+        for line in open("/proc/self/maps"):
+            path = line.split()[-1] if len(line.split()) >= 6 else ""
+            if path.endswith(".so") and os.path.realpath(path).startswith(os.path.realpath(ROOT) + os.sep):
+                found.add(os.path.relpath(os.path.realpath(path), os.path.realpath(ROOT)))
+    except OSError:
+        pass
+    return sorted(found)
+
+
 def run_reference(args, rank, world):
-    """The reference arm: the CPU implementation of the path on this machine's host cores."""
+    """The reference arm: the CPU implementation of the path on this machine's host cores.  It
+    builds its graph with the Python restatement and times the oracle, so the product's
+    library is never loaded in this process."""
     if rank != 0:
         return
     from graphaligner_gb300.extend import ExtendParams
-    g, batch = make_workload(args.reads, 0)
+    g, batch = make_workload(args.reads, 0, args.truncate, native=False)
     params = ExtendParams(bandwidth=10)
     threads = os.cpu_count() or 1
     vals, secs = [], []
@@ -195,10 +256,11 @@ def run_reference(args, rank, world):
     v = statistics.median(vals)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": statistics.median(secs) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD},
+            "dtype": "u64", "data": "synthetic (seeded generator; graph, reads and seeds as the workload describes)",
+            "impl": "reference", "config": workload_config(g, batch, params, world),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "repo_libraries_loaded": repo_libraries_loaded(),
             "note": "the reference's own C++ source is not present where this runs; the oracle restatement (bit-exact with it on the golden vectors) is timed; a step is the bounded sample of the batch named in cpu_baseline.sample"}
     print(json.dumps(line), flush=True)
 
@@ -547,7 +609,8 @@ def main():
         check(L.ga_extender_last_copy_ms(ext.handle, ctypes.byref(h2d_ms), ctypes.byref(d2h_ms)))
         check(L.ga_extender_last_kernel_ms(ext.handle, ctypes.byref(k_ms)))
         e2e_parts.append((h2d_ms.value, k_ms.value, d2h_ms.value))
-    e2e_same = bool(np.array_equal(hr.status, res.status) and np.array_equal(hr.score, res.score))
+    # every extension's status, score and trace (checksum of its packed items) against the device run
+    e2e_same = bool(np.array_equal(result_key(hr, np.arange(n)), result_key(res, np.arange(n))))
     job_bp_e2e, e2e_s = combine_ranks(bp, statistics.median(e2e_times), world, dev)
     e2e_value = job_bp_e2e / e2e_s
 
@@ -572,8 +635,13 @@ def main():
             plain_ms += ms.value
         torch.cuda.synchronize()
         plain_wall = time.perf_counter() - t
-        st = d_status.cpu().numpy()
-        same = bool(np.array_equal(st[pidx], res.status[pidx]) and np.array_equal(d_score.cpu().numpy()[pidx], res.score[pidx]))
+        pres = alloc_results(batch)
+        pres.status[:] = d_status.cpu().numpy()
+        pres.score[:] = d_score.cpu().numpy()
+        pres.trace_len[:] = d_tlen.cpu().numpy().view(np.uint32)
+        pres.trace_items[:] = d_items.cpu().numpy().view(np.uint64)
+        same = bool(np.array_equal(result_key(pres, pidx), result_key(res, pidx)))
+        del pres
         first = res.trace_items[res.trace_offset[pidx].astype(np.int64)]
         pbp = int(np.where(res.status[pidx] == 0, (first >> np.uint64(39)).astype(np.int64), 0).sum())
         plain = {"value": pbp / plain_wall, "unit": UNIT, "kernel_only_value": pbp / (plain_ms / 1e3),
@@ -587,33 +655,34 @@ def main():
     cpu_agree = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, cpu_res, cpu_idx = cpu_baseline(g, batch, params, args.cpu_sample_bp, os.cpu_count() or 1)
-        cpu_agree = bool(np.array_equal(cpu_res.status, res.status[cpu_idx]) and np.array_equal(cpu_res.score, res.score[cpu_idx]))
+        cpu_agree = bool(np.array_equal(result_key(cpu_res, np.arange(len(cpu_idx))), result_key(res, cpu_idx)))
 
     # ---- roofline ----
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    fill_s = statistics.median(kernel_ms) / 1e3
-    # algorithmic bytes per launch: the reads, the committed DP slices (written by the fill,
-    # read by the traceback) and the trace items written
-    alg_bytes = int(batch.seq.nbytes + 2 * arena_bytes.value + int(res.trace_len.astype(np.int64).sum()) * 8)
-    achieved_gbs = alg_bytes / fill_s / 1e9
+    step_s = statistics.median(kernel_ms) / 1e3
+    # the bound: the Myers column steps of the fill at 40 INT32 ops each (20 u64 ops,
+    # GraphAlignerBitvectorCommon.h:242-262) against the INT32 issue rate measured on this GPU
     int_peak = ctypes.c_double()
     check(L.ga_measure_int32_peak(local, ctypes.byref(int_peak)))
-    alu_achieved = steps_total * INT32_OPS_PER_STEP / fill_s
+    alu_achieved = steps_total * INT32_OPS_PER_STEP / step_s
+    # beside it, HBM: algorithmic bytes per step are the reads, the DP tables (written by the fill,
+    # read by the traceback) and the trace items written; DRAM traffic per read bp comes from an
+    # ncu capture of both kernels on a smaller case of the same batch, scaled by read bp
+    read_bp_total = int(batch.seq_len.astype(np.int64).sum())
+    alg_bytes = int(batch.seq.nbytes + 2 * arena_bytes.value + int(res.trace_len.astype(np.int64).sum()) * 8)
+    achieved_gbs = alg_bytes / step_s / 1e9
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "extend_kernel_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "extension_kernels_traffic.json")
     if os.path.exists(tpath):
         t = json.load(open(tpath))
-        traffic = t.get("bytes_per_read_bp", 0) * int(batch.seq_len.astype(np.int64).sum())
+        traffic = t.get("bytes_per_read_bp", 0) * read_bp_total
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded generator; graph, reads and seeds as the workload describes)",
-        "config": {"workload": WORKLOAD, "extensions": n, "read_bp": int(batch.seq_len.astype(np.int64).sum()),
-                   "graph_nodes": g.num_nodes, "bandwidth": 10, "xdrop": params.xdrop,
-                   "l2": "inputs larger than L2 (sequences + DP-table arena written every step)",
-                   "parallelism": f"replicas{world}"},
+        "config": workload_config(g, batch, params, world),
         "gcups": gcups,
         "launch_shape": tuning,
         "gpu_launches": launches,
@@ -622,13 +691,14 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "seconds_per_step": statistics.median(e2e_times), "same_results": e2e_same,
                 "ms_h2d_kernel_d2h": [[round(v, 1) for v in part] for part in e2e_parts]},
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "traffic": traffic, "kernel": "extend_kernel (fill + traceback, fused)",
-                     "algorithmic_bytes": alg_bytes,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
-                     "note": "the fill is integer-ALU / dependency-latency bound, see alu"},
-        "alu": {"achieved": alu_achieved, "peak": int_peak.value, "unit": "int32 op/s", "frac": alu_achieved / int_peak.value,
-                "ops_per_column_step": INT32_OPS_PER_STEP, "peak_source": "ga_measure_int32_peak (xor+add chains, this GPU)"},
+        "roofline": {"bound": "int32", "achieved": alu_achieved / 1e12, "peak": int_peak.value / 1e12, "unit": "Tint32op/s",
+                     "frac": alu_achieved / int_peak.value, "traffic": traffic,
+                     "kernel": "fill_kernel + trace_kernel (one step: both launches)",
+                     "ops_per_column_step": INT32_OPS_PER_STEP, "column_steps": steps_total,
+                     "peak_source": "ga_measure_int32_peak (independent xor+add chains, this GPU)",
+                     "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                             "algorithmic_bytes": alg_bytes, "traffic_bytes": traffic,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}},
         "cpu_baseline": cpu, "cpu_sample_agrees": cpu_agree,
         "plain_per_extension": plain,
         "clocks": clocks.summary(),

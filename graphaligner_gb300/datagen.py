@@ -582,6 +582,12 @@ def small_dbg_genome(seed: int = 0) -> np.ndarray:
     return make_repeat_genome(100_000, 10, 2_000, 0.01, 0.03, 20, tandem_len=(200, 1000), seed=seed)
 
 
+def mid_dbg_genome(seed: int = 0) -> np.ndarray:
+    """1 Mbp genome, 20 copies of a 5 kbp repeat at 1-3 % divergence, 40 tandem arrays of period 2-50
+    (the de Bruijn stress genome's shape at a tenth of its size)."""
+    return make_repeat_genome(1_000_000, 20, 5_000, 0.01, 0.03, 40, seed=seed)
+
+
 def stress_dbg_genome(seed: int = 0) -> np.ndarray:
     """10 Mbp genome, 200 copies of a 5 kbp repeat at 1-3 % divergence, tandem repeats of period 2-50."""
     return make_repeat_genome(10_000_000, 200, 5_000, 0.01, 0.03, 400, seed=seed)

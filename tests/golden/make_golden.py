@@ -17,11 +17,19 @@ synthetic inputs and stores what it produced:
                    case, and edge requests (lengths 1-2, 63-65, 127-129; node first/last base)
   dbg100k_*        the same for a k=63 de Bruijn graph with repeats and tandem arrays
                    (cyclic components), extensions at tangle effort 10000, GAF at -x dbg
+  vg50k_px_*       on the vg50k graph, extensions of reads at 12-25 % error, every other one
+                   with a random block of 30-150 bp inside (low X-drop cutoffs stop there,
+                   the default one passes it), at bandwidths 10, 1, 3, 17 and 40 and at
+                   X-drop cutoffs 1500 and 3000 (bandwidth 10)
+  dbg1m_*          a k=63 de Bruijn graph of a 1 Mbp genome (20 copies of a 5 kbp repeat,
+                   40 tandem arrays): extensions of 20 kbp reads at 12 % error at tangle
+                   effort 10000 (bandwidths 5 and 10), and the GAF of 20 such reads at -x dbg
 
 The packed item layout is the one include/graphaligner_gb300.h documents, so
 the oracle restatement and the GPU kernels are compared byte for byte.
 
-Usage: [GA_REFERENCE=<GraphAligner checkout>] python tests/golden/make_golden.py
+Usage: [GA_REFERENCE=<GraphAligner checkout>] python tests/golden/make_golden.py [set ...]
+       (sets: base params dbg1m; default: all)
 """
 from __future__ import annotations
 
@@ -62,10 +70,10 @@ def digest_ref_output(path):
     return "\n".join(lines) + "\n"
 
 
-def run_ext(gfa, tsv, bandwidth, max_cells=UNLIMITED):
+def run_ext(gfa, tsv, bandwidth, max_cells=UNLIMITED, xdrop=XDROP):
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "out.txt")
-        subprocess.run([REF, "extend", gfa, tsv, out, str(bandwidth), str(XDROP), str(max_cells), "0.66"], check=True)
+        subprocess.run([REF, "extend", gfa, tsv, out, str(bandwidth), str(xdrop), str(max_cells), "0.66"], check=True)
         return digest_ref_output(out)
 
 
@@ -79,7 +87,9 @@ def gz_write(path, data: bytes):
         g.write(data)
 
 
-def make_set(name, graph, ext, bandwidths, max_cells=UNLIMITED, write_graph=True):
+def make_set(name, graph, ext, bandwidths, max_cells=UNLIMITED, write_graph=True, xdrops=(), write_requests=True):
+    """Digests of the reference's extensions of ext on graph: {name}_ext_b{bw}.digest per bandwidth
+    and {name}_ext_b{bw}_x{xdrop}.digest per (first bandwidth, X-drop cutoff) in xdrops."""
     with tempfile.TemporaryDirectory() as td:
         gfa = os.path.join(td, "g.gfa")
         open(gfa, "w").write(graph if isinstance(graph, str) else graph.to_gfa())
@@ -89,9 +99,12 @@ def make_set(name, graph, ext, bandwidths, max_cells=UNLIMITED, write_graph=True
             gz_write(os.path.join(HERE, f"{name}_graph.gag.gz"), open(gag, "rb").read())
         tsv = os.path.join(td, "ext.tsv")
         open(tsv, "w").write(ext.to_tsv())
-        gz_write(os.path.join(HERE, f"{name}_ext.tsv.gz"), ext.to_tsv().encode())
+        if write_requests:
+            gz_write(os.path.join(HERE, f"{name}_ext.tsv.gz"), ext.to_tsv().encode())
         for bw in bandwidths:
             open(os.path.join(HERE, f"{name}_ext_b{bw}.digest"), "w").write(run_ext(gfa, tsv, bw, max_cells))
+        for x in xdrops:
+            open(os.path.join(HERE, f"{name}_ext_b{bandwidths[0]}_x{x}.digest"), "w").write(run_ext(gfa, tsv, bandwidths[0], max_cells, x))
 
 
 def node_lengths(g):
@@ -147,13 +160,65 @@ def iupac_edge_set(seed: int = 5):
     return g, dg.ExtensionSet(seqs, np.array(nodes, dtype=np.int64), np.array(offs, dtype=np.int64))
 
 
+def vg50k_requests():
+    """The vg50k graph (50 kbp backbone, bubble every ~200 bp), its 200 reads (5-15 kbp at
+    10 % error) and the extension requests of the first 150."""
+    g = dg.small_vg(0)
+    reads = dg.small_vg_reads(g, 200, 1)
+    return g, reads, dg.seed_extensions(reads[:150], node_lengths(g), 15, 3, per_read=1)
+
+
+def params_sets():
+    """Extensions on the vg50k graph that the parameters change: reads at 12-25 % error, every
+    other one with a random block of 30-150 bp inserted at 20-60 % of its length (an X-drop
+    cutoff of 1500 or 3000 stops the extension there; the default one, 14705, passes the block
+    and its best end lies beyond it), at bandwidths 10, 1, 3, 17 and 40
+    (band admission, GraphAlignerBitvectorBanded.h:449-471) and at X-drop cutoffs 1500 and 3000
+    with bandwidth 10 (the X-drop stop, :651-669)."""
+    g, _, _ = vg50k_requests()
+    reads = dg.sample_reads(g, 80, 11, dg.uniform_length(2_000, 12_000), dg.uniform_error(0.12, 0.25))
+    ext = dg.seed_extensions(reads, node_lengths(g), 15, 12, per_read=2)
+    rng = np.random.default_rng(13)
+    seqs = list(ext.seqs)
+    for i in range(0, len(seqs), 2):
+        s = np.frombuffer(bytes(seqs[i]), dtype=np.uint8)
+        cut = int(len(s) * rng.uniform(0.2, 0.6))
+        block = dg._BASES[rng.integers(0, 4, int(rng.integers(30, 151)))]
+        seqs[i] = np.concatenate([s[:cut], block, s[cut:]]).tobytes()
+    make_set("vg50k_px", g, dg.ExtensionSet(seqs, ext.bignode, ext.offset), [10, 1, 3, 17, 40], write_graph=False,
+             xdrops=[1500, 3000])
+
+
+def dbg1m_sets():
+    """A k=63 de Bruijn graph of a 1 Mbp genome: extensions of 20 kbp reads at 12 % error at
+    tangle effort 10000 (bandwidths 5 and 10), and the GAF of 20 such reads at -x dbg."""
+    genome = dg.mid_dbg_genome(0)
+    d = dg.compact_dbg(genome, 63, with_positions=True)
+    ext_reads = dg.sample_genome_reads(genome, 60, 5, lambda rng: 20_000, lambda rng: 0.12, dbg=d)
+    make_set("dbg1m", d.gfa, dg.seed_extensions(ext_reads, d.node_len, 15, 4), [5, 10], max_cells=10000)
+    reads = dg.dbg_reads(genome, 20, 20_000, 0.12, 1)
+    with tempfile.TemporaryDirectory() as td:
+        gfa = os.path.join(td, "g.gfa")
+        open(gfa, "w").write(d.gfa)
+        fa = os.path.join(td, "reads.fa")
+        open(fa, "w").write(dg.write_fasta(reads))
+        gz_write(os.path.join(HERE, "dbg1m_reads.fa.gz"), dg.write_fasta(reads).encode())
+        out = os.path.join(td, "b5.gaf")
+        subprocess.run([REF, "align", gfa, fa, out, "dbg"], check=True)
+        gz_write(os.path.join(HERE, "dbg1m_b5.gaf.gz"), open(out, "rb").read())
+
+
 def main():
     if not os.path.exists(REF):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"], check=True)
-    # variation graph: 50 kbp backbone, bubble every ~200 bp; reads 5-15 kbp at 10% error
-    g = dg.small_vg(0)
-    reads = dg.small_vg_reads(g, 200, 1)
-    ext = dg.seed_extensions(reads[:150], node_lengths(g), 15, 3, per_read=1)
+    groups = sys.argv[1:] or ["base", "params", "dbg1m"]
+    if "params" in groups:
+        params_sets()
+    if "dbg1m" in groups:
+        dbg1m_sets()
+    if "base" not in groups:
+        return
+    g, reads, ext = vg50k_requests()
     make_set("vg50k", g, ext, [10, 5])
     # same graph, reads 0.5-20 kbp at 5-25% error
     reads2 = dg.sample_reads(g, 60, 7, dg.uniform_length(500, 20_000), dg.uniform_error(0.05, 0.25))

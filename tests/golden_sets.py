@@ -15,9 +15,11 @@ from graphaligner_gb300.extend import pack_batch
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-GRAPH_OF = {"vg50k_hi": "vg50k"}
+GRAPH_OF = {"vg50k_hi": "vg50k", "vg50k_px": "vg50k"}
 # tangle effort (maxCellsPerSlice) the extension digests were made with; unlimited otherwise
-MAX_CELLS = {"dbg100k": 10000}
+MAX_CELLS = {"dbg100k": 10000, "dbg1m": 10000}
+# X-drop cutoffs with digests of their own (at the set's first bandwidth); the default otherwise
+XDROPS = {"vg50k_px": (1500, 3000)}
 
 
 def load_graph(name: str):
@@ -38,9 +40,12 @@ def load_requests(name: str):
     return seqs, np.array(nodes), np.array(offs)
 
 
-def load_digests(name: str, bandwidth: int):
+def load_digests(name: str, bandwidth: int, xdrop: int | None = None):
+    """(status, score, items, sha1) per request of the set, from the reference at this
+    bandwidth and, when given, X-drop cutoff."""
     out = []
-    for line in open(os.path.join(GOLDEN, f"{name}_ext_b{bandwidth}.digest")):
+    suffix = f"_x{xdrop}" if xdrop is not None else ""
+    for line in open(os.path.join(GOLDEN, f"{name}_ext_b{bandwidth}{suffix}.digest")):
         s, sc, n, h = line.split()
         out.append((int(s), int(sc), int(n), h))
     return out

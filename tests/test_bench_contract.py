@@ -24,4 +24,7 @@ def test_reference_arm_prints_one_contract_line():
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
-    assert "workload" in d["config"]
+    assert "workload" in d["config"] and d["config"]["extensions"] > 0 and d["config"]["read_bp"] > 0
+    # the reference arm times the CPU implementation only: the product's library is never loaded
+    assert not any("libgraphaligner_gb300" in lib for lib in d["repo_libraries_loaded"]), d["repo_libraries_loaded"]
+    assert any("libga_oracle" in lib for lib in d["repo_libraries_loaded"])

@@ -52,6 +52,42 @@ def test_gpu_matches_reference_golden_dbg(cuda_lib, bandwidth):
     assert not bad, f"{len(bad)} extensions differ, first {bad[:5]}"
 
 
+@pytest.fixture(scope="module")
+def golden_px():
+    g, batch = golden_case("vg50k_px")
+    ext = Extender(DeviceGraph(g))
+    yield batch, ext
+    ext.close()
+
+
+@pytest.mark.parametrize("bandwidth,xdrop", [(10, None), (1, None), (3, None), (17, None), (40, None), (10, 1500), (10, 3000)])
+def test_gpu_matches_reference_golden_parameters(cuda_lib, golden_px, bandwidth, xdrop):
+    """Bandwidths 1-40 (band admission, GraphAlignerBitvectorBanded.h:449-471) and X-drop cutoffs
+    1500 and 3000 (the X-drop stop, :651-669) on extensions whose results they change: reads at
+    12-25 % error, half of them with a random block the low cutoffs stop at."""
+    batch, ext = golden_px
+    p = ExtendParams(bandwidth=bandwidth)
+    if xdrop is not None:
+        p.xdrop = xdrop
+    res = ext.run(p, batch)
+    bad = compare(res, load_digests("vg50k_px", bandwidth, xdrop))
+    assert not bad, f"{len(bad)} extensions differ from the reference, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("bandwidth", [5, 10])
+def test_gpu_matches_reference_golden_dbg1m(cuda_lib, bandwidth):
+    """The de Bruijn stress shape at 1 Mbp (20 copies of a 5 kbp repeat at 1-3 %, 40 tandem
+    arrays; k=63): extensions of 20 kbp reads at 12 % error at tangle effort 10000, against the
+    reference.  Extensions whose bands outgrow the shared-memory tables are re-run with larger
+    ones, so the digests also pin that path."""
+    g, batch = golden_case("dbg1m")
+    ext = Extender(DeviceGraph(g))
+    res = ext.run(ExtendParams(bandwidth=bandwidth, max_cells_per_slice=MAX_CELLS["dbg1m"]), batch)
+    bad = compare(res, load_digests("dbg1m", bandwidth))
+    assert not bad, f"{len(bad)} extensions differ, first {bad[:5]}"
+    print("layout counts", ext.last_layout_counts())
+
+
 def test_gpu_matches_oracle_dbg_generated(cuda_lib, oracle_lib):
     """A second de Bruijn graph built here (own numbering), GPU against the oracle on the same arrays,
     with tangle efforts that do and do not cut the band."""
@@ -62,8 +98,11 @@ def test_gpu_matches_oracle_dbg_generated(cuda_lib, oracle_lib):
     ext = dg.seed_extensions(reads, d.node_len, 15, 23, per_read=2)
     batch = pack_batch(g, ext.seqs, ext.bignode, ext.offset)
     x = Extender(DeviceGraph(g))
-    for bw, cells in ((5, 10000), (10, 10000), (5, 500)):
+    for bw, cells, xdrop in ((5, 10000, None), (10, 10000, None), (5, 500, None), (1, 10000, None), (3, 10000, None),
+                             (17, 10000, None), (40, 2000, None), (5, 10000, 1500), (5, 10000, 3000)):
         p = ExtendParams(bandwidth=bw, max_cells_per_slice=cells)
+        if xdrop is not None:
+            p.xdrop = xdrop
         gpu = x.run(p, batch)
         ref = oracle_lib.extend(g, p, batch, threads=8)
         _assert_same(gpu, ref, batch.num)
@@ -87,8 +126,13 @@ def test_gpu_matches_oracle_generated(cuda_lib, oracle_lib):
     batch = pack_batch(g, ext.seqs, ext.bignode, ext.offset)
     dgraph = DeviceGraph(g)
     x = Extender(dgraph)
-    for bw, cells in ((10, 2**64 - 1), (5, 2**64 - 1), (10, 300)):
+    unlimited = 2**64 - 1
+    for bw, cells, xdrop in ((10, unlimited, None), (5, unlimited, None), (10, 300, None), (1, unlimited, None),
+                             (3, unlimited, None), (17, unlimited, None), (40, unlimited, None), (10, unlimited, 1500),
+                             (10, unlimited, 3000)):
         p = ExtendParams(bandwidth=bw, max_cells_per_slice=cells)
+        if xdrop is not None:
+            p.xdrop = xdrop
         gpu = x.run(p, batch)
         ref = oracle_lib.extend(g, p, batch, threads=8)
         _assert_same(gpu, ref, batch.num)

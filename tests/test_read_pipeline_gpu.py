@@ -38,6 +38,19 @@ def test_gpu_gaf_matches_reference_dbg(cuda_lib):
     assert gaf == load_gaf("dbg100k", 5)
 
 
+def test_gpu_gaf_matches_reference_dbg1m(cuda_lib):
+    """-x dbg on the 1 Mbp de Bruijn stress graph (20 copies of a 5 kbp repeat, 40 tandem
+    arrays): 20 reads of 20 kbp at 12 % error, GAF bytes against the reference's."""
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    g = load_graph("dbg1m")
+    names, seqs = load_reads("dbg1m")
+    a = Aligner(Extender(DeviceGraph(g)), g, preset("dbg"))
+    gaf = a.align(names, seqs)
+    assert a.stats()["failed_reads"] == 0
+    assert gaf == load_gaf("dbg1m", 5)
+
+
 def test_gpu_quickstart(cuda_lib, tmp_path):
     from graphaligner_gb300 import graph as gg
     from graphaligner_gb300.align import Aligner, preset

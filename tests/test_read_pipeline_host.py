@@ -91,14 +91,15 @@ def test_reads_without_seeds(harness, oracle_lib, tmp_path):
     assert " failed 0 " in out.stderr
 
 
-def test_gaf_matches_reference_dbg(harness, oracle_lib, tmp_path):
-    """-x dbg on a k=63 de Bruijn graph with cyclic components."""
+@pytest.mark.parametrize("name", ["dbg100k", "dbg1m"])
+def test_gaf_matches_reference_dbg(harness, oracle_lib, tmp_path, name):
+    """-x dbg on k=63 de Bruijn graphs with cyclic components (100 kbp and 1 Mbp genomes)."""
     exe = harness[0]
     import gzip
     reads = os.path.join(tmp_path, "reads.fa")
-    open(reads, "wb").write(gzip.open(os.path.join(GOLDEN, "dbg100k_reads.fa.gz")).read())
-    out = subprocess.run([exe, graph_file("dbg100k", str(tmp_path)), reads, "gafdbg", "5"], check=True, capture_output=True, text=True).stdout
-    assert out == load_gaf("dbg100k", 5)
+    open(reads, "wb").write(gzip.open(os.path.join(GOLDEN, f"{name}_reads.fa.gz")).read())
+    out = subprocess.run([exe, graph_file(name, str(tmp_path)), reads, "gafdbg", "5"], check=True, capture_output=True, text=True).stdout
+    assert out == load_gaf(name, 5)
 
 
 def test_quickstart_gaf(harness, tmp_path):
