@@ -1262,13 +1262,9 @@ __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* se
     bool eq = char_match(g, seq[p.seq], p.node, p.off, bad);
     if (bad) { err = GA_ASSERT; return second; }
     i32 here = col_value(cols[p.off], 0);
-    i32 diag = pself->sEnd;
-    #pragma unroll 1
-    for (u32 k = 1; k + 1 <= p.off; k++)
-    {
-        diag += (i32)((pself->HP >> k) & 1);
-        diag -= (i32)((pself->HN >> k) & 1);
-    }
+    // the previous slice's last row at column p.off - 1: its first column plus the deltas of columns 1..p.off-1
+    const u64 upto = p.off >= 2 ? ((kAllOnes >> (64 - (p.off - 1))) << 1) : 0;
+    i32 diag = pself->sEnd + popc64(pself->HP & upto) - popc64(pself->HN & upto);
     i32 up = diag + (i32)((pself->HP >> p.off) & 1) - (i32)((pself->HN >> p.off) & 1);
     if (pr->notValid || cr->notValid || here > cr->quit || diag > pr->quit || up > pr->quit)
     {
@@ -1432,12 +1428,12 @@ __device__ __noinline__ int row_above(const DevGraph& g, Table t, TraceOut& to)
     if (!it) return GA_ASSERT;
     const u32 L = g.len[to.back.node];
     // before[k] = score of column k in the row above the read
+    const u64 hp = it->HP, hn = it->HN;
+    const i32 s0 = it->sEnd;
     auto before = [&](u32 k) -> i32
     {
-        i32 v = it->sEnd;
-        #pragma unroll 1
-        for (u32 q = 1; q <= k; q++) v += (i32)((it->HP >> q) & 1) - (i32)((it->HN >> q) & 1);
-        return v;
+        const u64 upto = k >= 1 ? ((kAllOnes >> (64 - k)) << 1) : 0;   // columns 1..k
+        return s0 + popc64(hp & upto) - popc64(hn & upto);
     };
     if (before(L - 1) != it->eEnd) return GA_ASSERT;
     #pragma unroll 1
@@ -1512,7 +1508,8 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
         to.push(start, false);
         u32 curSlice = (u32)(start.seq / 64) + 1;
         u32 curNode = 0xffffffffu;
-        u32 colsUpTo = 0;             // columns 0..colsUpTo of (curSlice, curNode) are in cols
+        u32 curLen = 0;
+        u32 colsUpTo = 0;             // columns 0..colsUpTo of (curSlice, curNode) are in cols, their match masks in eqcol
         EqV4 eqv;
         if (!eq_vector(seq, seqLen, ((int64_t)curSlice - 1) * 64, eqv, lane)) err = GA_ASSERT;
         i32 lastScore = kIntMax - 1;
@@ -1535,9 +1532,10 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 err = recalc(g, a.cost, t, curSlice, curNode, eqv, cols, w.eqcol, lane, b.off);
                 if (err) break;
                 colsUpTo = b.off;
+                curLen = g.len[curNode];
             }
             const int64_t sj = ((int64_t)curSlice - 1) * 64;
-            if (b.off >= g.len[curNode]) { err = GA_ASSERT; break; }
+            if (b.off >= curLen) { err = GA_ASSERT; break; }
             const u32 row = mod64(b.seq);
             lastScore = col_value(cols[b.off], (int)row);
             if (row == 0 && b.off == 0)
@@ -1608,21 +1606,15 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
             {
                 u32 hori = b.off;
                 u32 vert = row;
-                const bool amb = b.node >= g.firstAmbiguous;
-                const u64 nc0 = amb ? 0 : g.seq2[(u64)b.node * 2];
-                const u64 nc1 = amb ? 0 : g.seq2[(u64)b.node * 2 + 1];
-                auto colEq = [&](u32 h) -> u64
-                {
-                    if (!amb) return eq_pick(eqv, (u32)(((h < 32 ? nc0 : nc1) >> ((h & 31) * 2)) & 3));
-                    return eq_amb(eqv, (u32)node_char_mask(g, b.node, h));
-                };
+                // the recomputation left each column's match mask (the fill's Eq) in eqcol
+                const u64* eqcol = w.eqcol;
                 if (hori > 0 && vert > 0)
                 {
                     WS colH = ws_make(cols[hori].VP, cols[hori].VN, cols[hori].end);
                     WS colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
                     i32 here = ws_value(colH, (int)vert);
                     i32 left = ws_value(colL, (int)vert);
-                    u64 eqH = colEq(hori);
+                    u64 eqH = eqcol[hori];
                     #pragma unroll 1
                     while (true)
                     {
@@ -1647,7 +1639,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                             {
                                 colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
                                 left = ws_value(colL, (int)vert);
-                                eqH = colEq(hori);
+                                eqH = eqcol[hori];
                             }
                         }
                         else if (left == here - 1)
@@ -1660,7 +1652,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                             {
                                 colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
                                 left = ws_value(colL, (int)vert);
-                                eqH = colEq(hori);
+                                eqH = eqcol[hori];
                             }
                         }
                         else
