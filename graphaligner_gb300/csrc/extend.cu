@@ -1462,6 +1462,23 @@ __device__ __noinline__ int row_above(const DevGraph& g, Table t, TraceOut& to)
     return 0;
 }
 
+// The first column of the run of row-0 steps that ends at column off: the least c <= off with
+// score(c') = score(c' - 1) + 1 for every c < c' <= off (pickBacktraceVerticalCrossing's walk
+// along the slice's first row, Common.h:886-900).  Columns 0..off must be in cols.
+__device__ __forceinline__ u32 row0_run_start(const Col* cols, u32 off, u32 lane)
+{
+    const i32 v0 = col_value(cols[lane], 0);
+    const i32 v1 = col_value(cols[lane + 32], 0);
+    i32 p0 = __shfl_up_sync(kFull, v0, 1);
+    i32 p1 = __shfl_up_sync(kFull, v1, 1);
+    const i32 v31 = __shfl_sync(kFull, v0, 31);
+    if (lane == 0) p1 = v31;
+    // bit c: column c continues the run (column 0 never does)
+    const u64 cont = (u64)(__ballot_sync(kFull, lane > 0 && p0 == v0 - 1)) | ((u64)__ballot_sync(kFull, p1 == v1 - 1) << 32);
+    const u64 stops = ~cont & (off == 63 ? kAllOnes : ((2ULL << off) - 1));
+    return 63 - __clzll((long long)stops);
+}
+
 __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st, const WSpace& w, u32 lane)
 {
     const DevGraph& g = a.g;
@@ -1558,9 +1575,11 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                     continue;
                 }
                 // pickBacktraceVerticalCrossing (Common.h:886-934)
+                // step left along row 0 while the score falls by one per column: lane k tests
+                // columns k and k + 32 against their left neighbours, the run ends at the
+                // highest failing column at or below b.off (column 0 always ends it)
                 TPos p = b;
-                #pragma unroll 1
-                while (p.off > 0 && col_value(cols[p.off - 1], 0) == col_value(cols[p.off], 0) - 1) p.off--;
+                p.off = row0_run_start(cols, b.off, lane);
                 TStep second = p.off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : vertical_step(g, seq, t, curSlice, pself, cols, p, err);
                 if (err) break;
                 if (second.pos.seq == b.seq && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
@@ -1579,9 +1598,15 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
                 // pickBacktraceHorizontalCrossing (Common.h:817-884)
                 const Item* self = t.find(curSlice, curNode);
                 if (!self) { err = GA_ASSERT; break; }
+                // step up column 0 while its score falls by one per row (the start column's VP
+                // bits): the run ends at the highest row at or below this one whose bit is clear
+                // (row 0 always ends it)
                 TPos p = b;
-                #pragma unroll 1
-                while (mod64(p.seq) != 0 && (self->sVP & (1ULL << mod64(p.seq)))) p.seq--;
+                {
+                    const u32 r = mod64(b.seq);
+                    const u64 stops = (~self->sVP | 1ULL) & (r == 63 ? kAllOnes : ((2ULL << r) - 1));
+                    p.seq -= (int64_t)(r - (63 - __clzll((long long)stops)));
+                }
                 const u32 off = mod64(p.seq);
                 TStep second = off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : horizontal_step(g, seq, t, curSlice, curNode, self, p, off, err);
                 if (err) break;
