@@ -4,8 +4,14 @@
 //   pipeline <graph.gag> <reads.fa> seeds <k> <w> <density> <discard>
 //   pipeline <graph.gag> <reads.fa> table <k> <w> <discard>
 //   pipeline <graph.gag> <reads.fa> gaf <bandwidth> <maxcells|->
+//   pipeline <graph.gag> <reads.fa> gafreads|gafreadsdbg <bandwidth> <maxcells|-> <threads>
+//       the reference's worker shape (Aligner.cpp:777-785, runComponentMappings :390-606): each
+//       thread takes the next read and runs its seeding and whole seed loop alone, with the
+//       oracle's extensions on that thread; GAF in input order
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -155,6 +161,7 @@ struct Ctx
 {
     ga_graph_desc* d;
     ga_extend_params p;
+    int threads = 8;
 };
 
 static void oracleExtend(void* ctx, const std::vector<gahost::ExtensionRequest>& rq, std::vector<gahost::ExtensionResult>& rs)
@@ -178,7 +185,7 @@ static void oracleExtend(void* ctx, const std::vector<gahost::ExtensionRequest>&
     items.resize(ti + 1);
     ga_extend_batch_desc b { (uint32_t)n, blob.data(), off.data(), len.data(), node.data(), noff.data(), toff.data(), cap.data() };
     ga_extend_results r { status.data(), score.data(), tlen.data(), items.data(), steps.data() };
-    ora_extend_batch(c->d, &c->p, &b, &r, 8);
+    ora_extend_batch(c->d, &c->p, &b, &r, c->threads);
     for (size_t i = 0; i < n; i++)
     {
         rs[i].status = status[i];
@@ -272,7 +279,8 @@ int main(int argc, char** argv)
     // gaf (-x vg, AlignerMain.cpp:170-177), gafdbg (-x dbg, AlignerMain.cpp:160-168), gafmix
     // (-x vg with reads joining the seed-loop pool a few per round) or gaf2 (-x vg, reads in two
     // groups whose rounds alternate), with the given bandwidth
-    const bool dbg = mode == "gafdbg";
+    const bool perRead = mode == "gafreads" || mode == "gafreadsdbg";
+    const bool dbg = mode == "gafdbg" || mode == "gafreadsdbg";
     const bool mixed = mode == "gafmix";
     const bool twoLanes = mode == "gaf2";
     const size_t joinPerRound = 7;
@@ -280,6 +288,47 @@ int main(int argc, char** argv)
     uint64_t maxCells = (argc > 5 && std::string(argv[5]) != "-") ? std::stoull(argv[5]) : (dbg ? 10000 : UINT64_MAX);
     gahost::MinimizerIndex idx;
     gahost::buildMinimizerIndex(graph, dbg ? 19 : 15, dbg ? 30 : 20, 1.0 - (dbg ? 0.0002 : 0.001), idx);
+    if (perRead)
+    {
+        const size_t threads = argc > 6 ? std::stoul(argv[6]) : std::max(1u, std::thread::hardware_concurrency());
+        gahost::ReadAlignParams p;
+        if (dbg) p.seedExtendDensity = 0.002;
+        std::vector<gahost::ReadOutput> out(reads.size());
+        std::atomic<size_t> next(0);
+        std::atomic<uint64_t> bp(0), rounds(0), extensions(0), failed(0);
+        const auto t0 = std::chrono::steady_clock::now();
+        auto worker = [&]()
+        {
+            Ctx one { &hd.base, ga_extend_params { (uint32_t)bw, 14705, maxCells, 294 }, 1 };
+            std::vector<gahost::KmerMatch> km;
+            while (true)
+            {
+                const size_t i = next.fetch_add(1);
+                if (i >= reads.size()) break;
+                std::vector<gahost::ReadInput> in(1);
+                in[0].name = reads[i].first;
+                in[0].seq = reads[i].second;
+                kmerMatchesHost(idx, in[0].seq, km);
+                gahost::selectSeeds(graph, idx, in[0].seq, dbg ? 5 : 10, km, in[0].seeds);
+                std::vector<gahost::ReadOutput> o;
+                gahost::BatchStats st;
+                gahost::alignBatch(graph, p, in, oracleExtend, &one, o, st);
+                out[i] = std::move(o[0]);
+                bp += st.bpAligned;
+                rounds += st.rounds;
+                extensions += st.extensions;
+                failed += st.failedReads;
+            }
+        };
+        std::vector<std::thread> pool;
+        for (size_t t = 0; t < threads; t++) pool.emplace_back(worker);
+        for (auto& t : pool) t.join();
+        const double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        for (auto& o : out) std::cout << o.gaf;
+        std::cerr << "rounds " << rounds << " extensions " << extensions << " bp " << bp << " failed " << failed
+                  << " seconds " << seconds << " threads " << threads << std::endl;
+        return 0;
+    }
     const auto alignStart = std::chrono::steady_clock::now();
     std::vector<gahost::ReadInput> in(reads.size());
     std::vector<gahost::KmerMatch> km;
