@@ -69,11 +69,19 @@ class AlignParams(ctypes.Structure):
     ]
 
 
+class Seed(ctypes.Structure):
+    """ga_seed: one SeedHit of MinimizerSeeder::getSeeds."""
+    _fields_ = [("node_id", ctypes.c_int32), ("reverse", ctypes.c_uint32), ("node_offset", ctypes.c_uint64),
+                ("seq_pos", ctypes.c_uint64), ("match_len", ctypes.c_uint32), ("raw_seed_goodness", ctypes.c_uint32),
+                ("alignment_graph_node", ctypes.c_uint32), ("alignment_graph_offset", ctypes.c_uint32)]
+
+
 class AlignStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("reads", "reads_with_seeds", "reads_aligned", "failed_reads", "bp_aligned",
                                                 "rounds", "extensions", "cell_steps")] + \
                [(n, ctypes.c_double) for n in ("seed_ms", "extend_ms", "host_ms", "collect_ms", "staging_ms", "consume_ms", "finish_ms")] + \
-              [(n, ctypes.c_uint64) for n in ("speculative_used", "speculative_discarded")]
+              [(n, ctypes.c_uint64) for n in ("speculative_used", "speculative_discarded")] + \
+              [(n, ctypes.c_double) for n in ("seed_lookup_ms", "seed_select_ms")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -118,6 +126,26 @@ class Aligner:
         size = ctypes.c_uint64()
         check(lib().ga_aligner_gaf(self.handle, ctypes.byref(text), ctypes.byref(size)))
         return ctypes.string_at(text, size.value).decode()
+
+    def seeds(self, seqs) -> list:
+        """MinimizerSeeder::getSeeds per read (ga_aligner_get_seeds): a list of
+        (node_id, node_offset, seq_pos, match_len, reverse, alignment_graph_node,
+        alignment_graph_offset, raw_seed_goodness) tuples per read, in the reference's order."""
+        n = len(seqs)
+        lens = np.fromiter((len(s) for s in seqs), dtype=np.uint32, count=n)
+        offs = np.zeros(n, dtype=np.uint64)
+        if n > 1:
+            offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+        blob = np.frombuffer(b"".join(bytes(s) for s in seqs) or b"\0", dtype=np.uint8).copy()
+        sp = ctypes.POINTER(Seed)()
+        op = ctypes.POINTER(ctypes.c_uint64)()
+        check(lib().ga_aligner_get_seeds(self.handle, n, ptr(blob, ctypes.c_uint8), ptr(offs, ctypes.c_uint64),
+                                         ptr(lens, ctypes.c_uint32), ctypes.byref(sp), ctypes.byref(op)))
+        out = []
+        for i in range(n):
+            out.append([(h.node_id, h.node_offset, h.seq_pos, h.match_len, h.reverse, h.alignment_graph_node,
+                         h.alignment_graph_offset, h.raw_seed_goodness) for h in (sp[j] for j in range(op[i], op[i + 1]))])
+        return out
 
     def stats(self) -> dict:
         s = AlignStats()

@@ -100,6 +100,7 @@ gahost::ReadAlignParams ga_aligner_read_params(const ga_aligner* a)
 int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const uint8_t* seq, const uint64_t* seqOffset,
     const uint32_t* seqLen, std::vector<gahost::ReadInput>& reads)
 {
+    const auto t0 = std::chrono::steady_clock::now();
     reads.assign(n, gahost::ReadInput {});
     if (n == 0) return GA_OK;
     uint64_t seqBytes = 0, matchSlots = 0;
@@ -127,17 +128,24 @@ int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const u
     gadev::SeedTable table { a->slots, a->capacity, (uint32_t)std::min<uint64_t>(a->index.maxCount, 0xffffffffu) };
     ga_launch_seed_lookup(table, a->params.minimizer_length, a->params.minimizer_window, n, dSeq, dOff, dLen, dMatchOff, dMatch, dCount, a->stream);
     std::vector<uint32_t> counts(n);
-    // one slot per read base, of which only the first counts[i] of each read are read below:
-    // left uninitialised rather than zeroed (it is as large as 16 B per read base)
-    std::unique_ptr<gadev::SeedMatch[]> matches(new gadev::SeedMatch[std::max<uint64_t>(matchSlots, 1)]);
+    // one slot per read base, of which only the first counts[i] of each read are read below
+    // (pinned and reused: a pageable copy of 16 B per read base costs more than the lookups)
+    if (!a->hMatch.reserve(std::max<uint64_t>(matchSlots, 1)))
+    {
+        ga_set_last_error("seeding: pinned host buffer for the k-mer matches");
+        return GA_ERR_CUDA;
+    }
+    const gadev::SeedMatch* matches = a->hMatch.data();
     cudaMemcpyAsync(counts.data(), dCount, n * 4ULL, cudaMemcpyDeviceToHost, a->stream);
-    cudaMemcpyAsync(matches.get(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
+    cudaMemcpyAsync(a->hMatch.data(), dMatch, std::max<uint64_t>(matchSlots, 1) * sizeof(gadev::SeedMatch), cudaMemcpyDeviceToHost, a->stream);
     cudaError_t e = cudaStreamSynchronize(a->stream);
     if (e != cudaSuccess)
     {
         ga_set_last_error("seeding: seed lookup kernel failed");
         return GA_ERR_CUDA;
     }
+    a->stats.seed_lookup_ms = ms_since(t0);
+    const auto t1 = std::chrono::steady_clock::now();
     gahost::parallelFor(n, [&](size_t i)
     {
         reads[i].name = names[i] ? names[i] : "";
@@ -150,6 +158,7 @@ int ga_aligner_seed(ga_aligner* a, uint32_t n, const char* const* names, const u
         }
         gahost::selectSeeds(*a->graph, a->index, reads[i].seq, a->params.minimizer_density, km, reads[i].seeds);
     });
+    a->stats.seed_select_ms = ms_since(t1);
     return GA_OK;
 }
 
@@ -274,6 +283,40 @@ extern "C" int ga_aligner_gaf(ga_aligner_t a, const char** text, uint64_t* bytes
     if (!a || !text || !bytes) return GA_ERR_ARGUMENT;
     *text = a->gaf.c_str();
     *bytes = a->gaf.size();
+    return GA_OK;
+}
+
+extern "C" int ga_aligner_get_seeds(ga_aligner_t a, uint32_t n, const uint8_t* seq, const uint64_t* seqOffset,
+    const uint32_t* seqLen, const ga_seed** seeds, const uint64_t** seedOffsets)
+{
+    if (!a || !seeds || !seedOffsets || (n > 0 && (!seq || !seqOffset || !seqLen))) return GA_ERR_ARGUMENT;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        if (seqLen[i] > GA_MAX_SEQ_LEN)
+        {
+            ga_set_last_error(("ga_aligner_get_seeds: read " + std::to_string(i) + " is longer than GA_MAX_SEQ_LEN (33,554,431 bp)").c_str());
+            return GA_ERR_ARGUMENT;
+        }
+    }
+    cudaSetDevice(a->device);
+    std::vector<const char*> names(n, nullptr);
+    std::vector<gahost::ReadInput> reads;
+    int rc = ga_aligner_seed(a, n, names.data(), seq, seqOffset, seqLen, reads);
+    if (rc != GA_OK) return rc;
+    a->seedOffsets.assign(n + 1, 0);
+    for (uint32_t i = 0; i < n; i++) a->seedOffsets[i + 1] = a->seedOffsets[i] + reads[i].seeds.size();
+    a->seeds.resize(std::max<uint64_t>(a->seedOffsets[n], 1));
+    for (uint32_t i = 0; i < n; i++)
+    {
+        ga_seed* o = a->seeds.data() + a->seedOffsets[i];
+        for (const auto& h : reads[i].seeds)
+        {
+            *o++ = ga_seed { h.nodeID, h.reverse ? 1u : 0u, (uint64_t)h.nodeOffset, (uint64_t)h.seqPos, (uint32_t)h.matchLen,
+                (uint32_t)h.rawSeedGoodness, (uint32_t)h.alignmentGraphNodeId, (uint32_t)h.alignmentGraphNodeOffset };
+        }
+    }
+    *seeds = a->seeds.data();
+    *seedOffsets = a->seedOffsets.data();
     return GA_OK;
 }
 

@@ -93,9 +93,13 @@ struct ga_aligner
     DevGrow<uint64_t> dOff, dMatchOff;
     DevGrow<uint32_t> dLen, dCount;
     DevGrow<gadev::SeedMatch> dMatch;
+    Pinned<gadev::SeedMatch> hMatch;   // the matches copied back (one slot per read base)
+    std::vector<ga_seed> seeds;         // ga_aligner_get_seeds' output
+    std::vector<uint64_t> seedOffsets;
     ~ga_aligner()
     {
         dSeq.release(); dOff.release(); dMatchOff.release(); dLen.release(); dCount.release(); dMatch.release();
+        hMatch.release();
     }
 };
 

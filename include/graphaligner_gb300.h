@@ -272,6 +272,8 @@ typedef struct ga_align_stats {
     double   finish_ms;                /*           selection and GAF per read */
     uint64_t speculative_used;         /* extensions of later seeds sent ahead and then used ... */
     uint64_t speculative_discarded;    /* ... and sent ahead but not used (the loop went elsewhere) */
+    double   seed_lookup_ms;           /* of seed_ms: reads in, k-mer lookup kernel, matches back */
+    double   seed_select_ms;           /*             least-frequent selection per read (host) */
 } ga_align_stats;
 
 typedef struct ga_aligner* ga_aligner_t;
@@ -281,6 +283,23 @@ int ga_aligner_free(ga_aligner_t aligner);
 /* Aligns a batch of reads (host buffers); the GAF text stays with the aligner. */
 int ga_align_reads(ga_aligner_t aligner, uint32_t num_reads, const char* const* names, const uint8_t* seq,
                    const uint64_t* seq_offset, const uint32_t* seq_len);
+/* One seed of MinimizerSeeder::getSeeds (SeedHit, src/GraphAlignerWrapper.h:11-50). */
+typedef struct ga_seed {
+    int32_t  node_id;                 /* SeedHit::nodeID: the GFA node id */
+    uint32_t reverse;                 /* SeedHit::reverse */
+    uint64_t node_offset;             /* SeedHit::nodeOffset */
+    uint64_t seq_pos;                 /* SeedHit::seqPos */
+    uint32_t match_len;               /* SeedHit::matchLen (the minimizer length) */
+    uint32_t raw_seed_goodness;       /* SeedHit::rawSeedGoodness */
+    uint32_t alignment_graph_node;    /* SeedHit::alignmentGraphNodeId (split node index) */
+    uint32_t alignment_graph_offset;  /* SeedHit::alignmentGraphNodeOffset */
+} ga_seed;
+/* MinimizerSeeder::getSeeds(sequence, density) (src/MinimizerSeeder.cpp:521-543) for a batch of
+ * reads (host buffers): the k-mer lookups on the GPU, the least-frequent selection on the host.
+ * Read i's seeds, in the reference's order (before OrderSeeds), are seeds[seed_offsets[i] ..
+ * seed_offsets[i + 1]); both arrays stay valid until the next call on this aligner. */
+int ga_aligner_get_seeds(ga_aligner_t aligner, uint32_t num_reads, const uint8_t* seq, const uint64_t* seq_offset,
+                         const uint32_t* seq_len, const ga_seed** seeds, const uint64_t** seed_offsets);
 /* GAF lines of the last ga_align_reads call, reads in input order; valid until the next call. */
 int ga_aligner_gaf(ga_aligner_t aligner, const char** text, uint64_t* bytes);
 /* Per-read bp aligned of the last call. */

@@ -21,6 +21,10 @@ synthetic inputs and stores what it produced:
                    with a random block of 30-150 bp inside (low X-drop cutoffs stop there,
                    the default one passes it), at bandwidths 10, 1, 3, 17 and 40 and at
                    X-drop cutoffs 1500 and 3000 (bandwidth 10)
+  vg50k_seed_edges.fa.gz, vg50k_seed_edges_seeds.digest
+                   MinimizerSeeder::getSeeds + OrderSeeds (sha1 per output line) on reads
+                   with homopolymer runs longer than k, N runs, IUPAC codes, lower case and
+                   lengths below, at and just above k (-x vg minimizers)
   dbg1m_*          a k=63 de Bruijn graph of a 1 Mbp genome (20 copies of a 5 kbp repeat,
                    40 tandem arrays): extensions of 20 kbp reads at 12 % error at tangle
                    effort 10000 (bandwidths 5 and 10), and the GAF of 20 such reads at -x dbg
@@ -29,7 +33,7 @@ The packed item layout is the one include/graphaligner_gb300.h documents, so
 the oracle restatement and the GPU kernels are compared byte for byte.
 
 Usage: [GA_REFERENCE=<GraphAligner checkout>] python tests/golden/make_golden.py [set ...]
-       (sets: base params dbg1m; default: all)
+       (sets: base params dbg1m seeds; default: all)
 """
 from __future__ import annotations
 
@@ -189,6 +193,49 @@ def params_sets():
              xdrops=[1500, 3000])
 
 
+def seed_edge_reads(seed: int = 17):
+    """Reads on which iterateKmers' rules all fire: 30 vg50k reads (cut to 3 kbp) with
+    homopolymer runs of 16-80 bp (repeated k-mers: the window rule), N runs and single IUPAC
+    codes (restarts), lower-case stretches, plus reads of 1, 14, 15, 16 and 40 bp, an all-N
+    read and a 200 bp homopolymer."""
+    rng = np.random.default_rng(seed)
+    g = dg.small_vg(0)
+    base = dg.small_vg_reads(g, 30, seed)
+    out = []
+    for r in base:
+        b = np.frombuffer(r.seq[:3000], dtype=np.uint8).copy()
+        for _ in range(3):
+            pos = int(rng.integers(0, len(b) - 100))
+            run = int(rng.integers(16, 81))
+            b[pos:pos + run] = dg._BASES[rng.integers(0, 4)]
+        pos = int(rng.integers(0, len(b) - 20))
+        b[pos:pos + int(rng.integers(1, 12))] = ord("N")
+        iu = rng.random(len(b)) < 0.002
+        b[iu] = IUPAC[rng.integers(0, len(IUPAC), int(iu.sum()))]
+        pos = int(rng.integers(0, len(b) - 200))
+        seg = b[pos:pos + 200]
+        seg[seg < 97] += 32          # lower case (IUPAC and N too)
+        out.append(dg.Read(r.name + "_edges", b.tobytes(), r.bignode, r.bigoffset, r.exact))
+    for i, n in enumerate((1, 14, 15, 16, 40)):
+        out.append(dg.Read(f"short{i}", dg._BASES[rng.integers(0, 4, n)].tobytes(), 0, 0, False))
+    out.append(dg.Read("alln", b"N" * 300, 0, 0, False))
+    out.append(dg.Read("homopolymer", b"C" * 200, 0, 0, False))
+    return g, out
+
+
+def seed_sets():
+    g, reads = seed_edge_reads()
+    with tempfile.TemporaryDirectory() as td:
+        gfa = os.path.join(td, "g.gfa")
+        open(gfa, "w").write(g.to_gfa())
+        fa = os.path.join(td, "reads.fa")
+        open(fa, "w").write(dg.write_fasta(reads))
+        gz_write(os.path.join(HERE, "vg50k_seed_edges.fa.gz"), dg.write_fasta(reads).encode())
+        out = os.path.join(td, "seeds.txt")
+        subprocess.run([REF, "seeds", gfa, fa, out, "15", "20", "10", "0.001"], check=True)
+        open(os.path.join(HERE, "vg50k_seed_edges_seeds.digest"), "w").write(digest_lines(open(out).read()))
+
+
 def dbg1m_sets():
     """A k=63 de Bruijn graph of a 1 Mbp genome: extensions of 20 kbp reads at 12 % error at
     tangle effort 10000 (bandwidths 5 and 10), and the GAF of 20 such reads at -x dbg."""
@@ -211,7 +258,9 @@ def dbg1m_sets():
 def main():
     if not os.path.exists(REF):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"], check=True)
-    groups = sys.argv[1:] or ["base", "params", "dbg1m"]
+    groups = sys.argv[1:] or ["base", "params", "dbg1m", "seeds"]
+    if "seeds" in groups:
+        seed_sets()
     if "params" in groups:
         params_sets()
     if "dbg1m" in groups:

@@ -51,6 +51,30 @@ def test_gpu_gaf_matches_reference_dbg1m(cuda_lib):
     assert gaf == load_gaf("dbg1m", 5)
 
 
+def test_gpu_seeds_match_reference_on_edge_reads(cuda_lib):
+    """getSeeds through the k-mer lookup kernel (one warp per read) on reads with homopolymer
+    runs longer than k (iterateKmers' window rule for repeated k-mers), N runs and IUPAC codes
+    (restarts), lower case, and lengths below, at and just above k, plus the golden reads: every
+    read's seeds, in order, equal the reference's."""
+    import hashlib
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    g = load_graph("vg50k")
+    a = Aligner(Extender(DeviceGraph(g)), g, preset("vg"))
+    for fasta, digest in (("vg50k_seed_edges.fa.gz", "vg50k_seed_edges_seeds.digest"), ("vg50k_reads.fa.gz", "vg50k_seeds.digest")):
+        text = gzip.open(os.path.join(GOLDEN, fasta), "rt").read().split("\n")
+        names = [line[1:].split()[0] for line in text if line.startswith(">")]
+        seqs = [line.encode() for line in text if line and not line.startswith(">")]
+        lines = []
+        for name, seeds in zip(names, a.seeds(seqs)):
+            lines.append(f"R {name} {len(seeds)}" + "".join(f" {s[0]},{s[1]},{s[2]},{s[3]},{s[4]},{s[5]},{s[6]},{s[7]}" for s in seeds))
+        ref = open(os.path.join(GOLDEN, digest)).read().split()
+        # the reference's output: a maxCount line, then per read its getSeeds line and its OrderSeeds line
+        want = ref[1::2][:len(lines)]
+        got = [hashlib.sha1(line.encode()).hexdigest() for line in lines]
+        assert got == want, f"{fasta}: reads {[i for i, (x, y) in enumerate(zip(got, want)) if x != y][:5]} differ"
+
+
 def test_gpu_quickstart(cuda_lib, tmp_path):
     from graphaligner_gb300 import graph as gg
     from graphaligner_gb300.align import Aligner, preset

@@ -41,6 +41,19 @@ def test_seeds_match_reference(harness):
     assert mine == ref
 
 
+def test_seeds_match_reference_on_edge_reads(harness, tmp_path):
+    """getSeeds and OrderSeeds on reads with homopolymer runs longer than k (iterateKmers' window
+    rule for repeated k-mers), N runs and IUPAC codes (restarts), lower case, and lengths below,
+    at and just above k: every output line equals the reference's."""
+    import gzip
+    exe, gag, _, _ = harness
+    reads = os.path.join(tmp_path, "edges.fa")
+    open(reads, "wb").write(gzip.open(os.path.join(GOLDEN, "vg50k_seed_edges.fa.gz")).read())
+    out = subprocess.run([exe, gag, reads, "seeds", "15", "20", "10", "0.001"], check=True, capture_output=True, text=True).stdout
+    mine = [hashlib.sha1(line.encode()).hexdigest() for line in out.splitlines()]
+    assert mine == open(os.path.join(GOLDEN, "vg50k_seed_edges_seeds.digest")).read().split()
+
+
 @pytest.mark.parametrize("name,k,w,discard", [("vg50k", 15, 20, 0.001), ("dbg100k", 19, 30, 0.0002)])
 def test_seed_table_finds_every_key(harness, tmp_path, name, k, w, discard):
     """The k-mer table the lookup kernel probes, built on all cores: every k-mer of the index
