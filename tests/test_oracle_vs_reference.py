@@ -129,3 +129,11 @@ def test_read_level_matches_reference_on_generated_inputs(harness, oracle_lib, t
     expected = open(ref_gaf).read()
     assert expected.count("\n") >= len(reads) // 2
     assert mine == expected
+
+
+def test_integration_adapter_compiles_against_reference_headers():
+    """The reference-side binding INTEGRATION.md shows (oracle/integration_adapter.cpp, the body of
+    GraphAlignerBitvectorBanded::getReverseTraceFromSeed over ga_extend_batch) compiles against the
+    reference's own headers and include/graphaligner_gb300.h."""
+    import oracle
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "adapter", f"GA_REFERENCE={oracle.REFERENCE_ROOT}"], check=True)
