@@ -53,9 +53,10 @@ def parse():
     ap.add_argument("--workload", default="extend", choices=["extend", "reads-vg", "reads-dbg", "pipeline", "serve"],
                     help="extend: the batched-extension line; the others print read-level lines")
     ap.add_argument("--reads-n", type=int, default=0, help="reads of a read-level workload (0: its default)")
-    ap.add_argument("--rates", default="50,100,200,400", help="serve: Poisson arrival rates, reads/s")
+    ap.add_argument("--rates", default="10,20,40,60", help="serve: Poisson arrival rates, reads/s")
     ap.add_argument("--plain-reads", type=int, default=40, help="serve: reads timed one ga_align_reads call each")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serve: seconds of Poisson arrivals per rate")
+    ap.add_argument("--serve-min-reads", type=int, default=500, help="serve: reads per rate at least")
     ap.add_argument("--cpu-reads", type=int, default=40, help="read-level: reads of the CPU baseline sample")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="extend: keep the default launch shape")
     ap.add_argument("--truncate", type=int, default=0, help="extend: cut every extension to this many bases (small profiling cases)")
@@ -332,7 +333,9 @@ def run_reads(args):
             "read_bp": read_bp, "graph_nodes": g.num_nodes, "preset": preset_name},
             "workload_gen_s": gen_s, "graph_upload_and_index_s": index_s}
     if args.workload == "serve":
-        line.update(run_serving(args, aligner, names, seqs))
+        with ClockSampler(0) as clocks:
+            line.update(run_serving(args, aligner, names, seqs))
+        line["clocks"] = clocks.summary()
     else:
         # warm-up on a slice, then timed passes over all reads
         aligner.align(names[:64], seqs[:64])
@@ -413,7 +416,7 @@ def run_serving(args, aligner, names, seqs):
     pos = 0
     for rate in rates:
         # about --serve-seconds of arrivals per rate, reads taken in order from the workload
-        n = int(max(20, rate * args.serve_seconds))
+        n = int(max(args.serve_min_reads, rate * args.serve_seconds))
         idx = [(pos + k) % len(seqs) for k in range(n)]
         pos += n
         arrivals = np.cumsum(rng.exponential(1.0 / rate, len(idx)))
