@@ -87,6 +87,15 @@ class AlignStats(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class IndexInfo(ctypes.Structure):
+    """ga_index_info: sizes of the minimizer index built by ga_aligner_create."""
+    _fields_ = [(n, ctypes.c_uint64) for n in ("minimizer_length", "minimizer_window", "max_count", "num_keys", "num_positions",
+                                                "table_capacity")] + [("build_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 def preset(name: str = "vg", bandwidth: int | None = None, tangle_effort: int | None = None) -> AlignParams:
     """AlignerMain.cpp:119-231 for the two presets (X-drop from the 0.66 clipping cutoff)."""
     from .extend import default_xdrop, xscore_error_cost
@@ -146,6 +155,21 @@ class Aligner:
             out.append([(h.node_id, h.node_offset, h.seq_pos, h.match_len, h.reverse, h.alignment_graph_node,
                          h.alignment_graph_offset, h.raw_seed_goodness) for h in (sp[j] for j in range(op[i], op[i + 1]))])
         return out
+
+    def index(self, arrays: bool = False):
+        """The minimizer index built on the GPU (ga_aligner_index): its sizes and, with arrays,
+        the distinct k-mers, each k-mer's first occurrence and the occurrences
+        ((split node << 6) | offset, grouped by k-mer) as uint64 arrays."""
+        info = IndexInfo()
+        check(lib().ga_aligner_index(self.handle, ctypes.byref(info), None, None, None))
+        if not arrays:
+            return info.as_dict()
+        keys = np.zeros(max(1, info.num_keys), dtype=np.uint64)
+        start = np.zeros(info.num_keys + 1, dtype=np.uint64)
+        pos = np.zeros(max(1, info.num_positions), dtype=np.uint64)
+        check(lib().ga_aligner_index(self.handle, ctypes.byref(info), ptr(keys, ctypes.c_uint64), ptr(start, ctypes.c_uint64),
+                                     ptr(pos, ctypes.c_uint64)))
+        return info.as_dict(), keys[:info.num_keys], start, pos[:info.num_positions]
 
     def stats(self) -> dict:
         s = AlignStats()

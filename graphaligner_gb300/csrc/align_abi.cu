@@ -11,6 +11,7 @@
 #include "readalign.h"
 #include "seed_kernel.cuh"
 #include "extend.cuh"
+#include "index_build.h"
 #include "aligner.h"
 #include "../../include/graphaligner_gb300.h"
 
@@ -179,31 +180,47 @@ extern "C" int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* gr
     try
     {
         a->graph = new gahost::HostGraph(*graph);
-        gahost::buildMinimizerIndex(*a->graph, params->minimizer_length, params->minimizer_window, 1.0 - params->minimizer_discard_fraction, a->index);
     }
     catch (...)
     {
-        delete a->graph;
         delete a;
-        ga_set_last_error("ga_aligner_create: the graph or its minimizer index is inconsistent");
+        ga_set_last_error("ga_aligner_create: the graph is inconsistent");
         return GA_ERR_ARGUMENT;
     }
-    // open-addressing table of the distinct k-mers, built on all cores and uploaded once
-    const uint64_t capacity = gahost::seedTableCapacity(a->index);
-    std::unique_ptr<gadev::SeedSlot[]> slots(new gadev::SeedSlot[capacity]);
-    gahost::buildSeedTable(a->index, slots.get(), capacity);
-    if (cudaMalloc((void**)&a->slots, capacity * sizeof(gadev::SeedSlot)) != cudaSuccess
-        || cudaMemcpy(a->slots, slots.get(), capacity * sizeof(gadev::SeedSlot), cudaMemcpyHostToDevice) != cudaSuccess
-        || cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess)
+    // minimizer index and its open-addressing lookup table, built on the GPU; the table
+    // stays resident for the lookup kernel, the index's arrays come back for seed selection
+    const auto t0 = std::chrono::steady_clock::now();
+    std::string why;
+    uint64_t capacity = 0;
+    const int built = ga_build_index_gpu(*a->graph, params->minimizer_length, params->minimizer_window, 1.0 - params->minimizer_discard_fraction,
+        a->index, &a->slots, &capacity, why);
+    if (built != 0 || cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess)
     {
         if (a->slots) cudaFree(a->slots);
         delete a->graph;
         delete a;
-        ga_set_last_error("ga_aligner_create: uploading the seed table failed");
-        return GA_ERR_CUDA;
+        ga_set_last_error(("ga_aligner_create: " + (built != 0 ? why : std::string("stream creation failed"))).c_str());
+        return built == -1 ? GA_ERR_ARGUMENT : GA_ERR_CUDA;
     }
+    a->indexBuildMs = ms_since(t0);
     a->capacity = capacity;
     *out = a;
+    return GA_OK;
+}
+
+extern "C" int ga_aligner_index(ga_aligner_t a, ga_index_info* info, uint64_t* keys, uint64_t* start_pos, uint64_t* positions)
+{
+    if (!a || !info) return GA_ERR_ARGUMENT;
+    info->minimizer_length = a->index.k;
+    info->minimizer_window = a->index.w;
+    info->max_count = a->index.maxCount;
+    info->num_keys = a->index.keys.size();
+    info->num_positions = a->index.positions.size();
+    info->table_capacity = a->capacity;
+    info->build_ms = a->indexBuildMs;
+    if (keys && !a->index.keys.empty()) std::memcpy(keys, a->index.keys.data(), a->index.keys.size() * 8);
+    if (start_pos) std::memcpy(start_pos, a->index.startPos.data(), a->index.startPos.size() * 8);
+    if (positions && !a->index.positions.empty()) std::memcpy(positions, a->index.positions.data(), a->index.positions.size() * 8);
     return GA_OK;
 }
 

@@ -83,6 +83,7 @@ struct ga_aligner
     gahost::MinimizerIndex index;
     gadev::SeedSlot* slots = nullptr;
     uint64_t capacity = 0;
+    double indexBuildMs = 0;   // ga_aligner_create's index build on the GPU, copies included
     std::string gaf;
     std::vector<uint64_t> readBp;
     ga_align_stats stats {};

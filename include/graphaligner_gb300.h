@@ -277,8 +277,25 @@ typedef struct ga_align_stats {
 } ga_align_stats;
 
 typedef struct ga_aligner* ga_aligner_t;
-/* Builds the minimizer index of the graph on the host and uploads its lookup table. */
+/* Builds the minimizer index of the graph (MinimizerSeeder's constructor with one bucket,
+ * src/MinimizerSeeder.cpp:191-297) on the GPU and keeps its lookup table there.
+ * GA_ERR_ARGUMENT for minimizer parameters out of range (length 1..31, at most 64
+ * minimizer positions per window) or a graph whose split pieces do not tile their node. */
 int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* graph, const ga_align_params* params, ga_aligner_t* out);
+typedef struct ga_index_info {
+    uint64_t minimizer_length;
+    uint64_t minimizer_window;
+    uint64_t max_count;                /* MinimizerSeeder::maxCount: k-mers this frequent are not seeds */
+    uint64_t num_keys;                 /* distinct k-mers */
+    uint64_t num_positions;            /* minimizer occurrences in the graph */
+    uint64_t table_capacity;           /* slots of the lookup table on the device */
+    double   build_ms;                 /* the build in ga_aligner_create, copies included */
+} ga_index_info;
+/* The index built by ga_aligner_create: sizes in *info and, for each non-NULL array, the
+ * distinct k-mers in increasing order (num_keys), each k-mer's first occurrence
+ * (num_keys + 1, the last = num_positions) and the occurrences, (split node << 6) | offset
+ * grouped by k-mer (num_positions). */
+int ga_aligner_index(ga_aligner_t aligner, ga_index_info* info, uint64_t* keys, uint64_t* start_pos, uint64_t* positions);
 int ga_aligner_free(ga_aligner_t aligner);
 /* Aligns a batch of reads (host buffers); the GAF text stays with the aligner. */
 int ga_align_reads(ga_aligner_t aligner, uint32_t num_reads, const char* const* names, const uint8_t* seq,

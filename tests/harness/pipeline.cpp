@@ -3,6 +3,12 @@
 // formats oracle/_ref/ga_ref prints, so the two can be diffed.
 //   pipeline <graph.gag> <reads.fa> seeds <k> <w> <density> <discard>
 //   pipeline <graph.gag> <reads.fa> table <k> <w> <discard>
+//   pipeline <graph.gag> <reads.fa> indexdump <k> <w> <discard> <prefix>
+//       the host index build's arrays as raw u64 files <prefix>.keys/.start/.pos (none for
+//       "-"), with its sizes, a checksum per array and the build time on all cores
+//   pipeline <graph.gag> <reads.fa> walk <k> <w> <discard>
+//       the GPU build's per-node minimizer walk (index_walk.cuh) run on the host, grouped
+//       by k-mer, against the host index build
 //   pipeline <graph.gag> <reads.fa> gaf <bandwidth> <maxcells|->
 //   pipeline <graph.gag> <reads.fa> gafreads|gafreadsdbg <bandwidth> <maxcells|-> <threads>
 //       the reference's worker shape (Aligner.cpp:777-785, runComponentMappings :390-606): each
@@ -21,6 +27,7 @@
 #include <vector>
 #include "../../include/graphaligner_gb300.h"
 #include "../../graphaligner_gb300/csrc/readalign.h"
+#include "../../graphaligner_gb300/csrc/index_walk.cuh"
 
 extern "C" int ora_extend_batch(const ga_graph_desc*, const ga_extend_params*, const ga_extend_batch_desc*, ga_extend_results*, int);
 
@@ -251,6 +258,95 @@ int main(int argc, char** argv)
         }
         std::cout << "keys " << idx.keys.size() << " capacity " << capacity << " used " << used << " bad " << bad
                   << " absent_found " << absentFound << "\n";
+        return 0;
+    }
+    if (mode == "indexdump")
+    {
+        size_t k = std::stoul(argv[4]), w = std::stoul(argv[5]);
+        double discard = std::stod(argv[6]);
+        gahost::MinimizerIndex idx;
+        const auto t0 = std::chrono::steady_clock::now();
+        gahost::buildMinimizerIndex(graph, k, w, 1.0 - discard, idx);
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        const std::string prefix = argv[7];
+        auto dump = [&](const char* ext, const std::vector<uint64_t>& v)
+        {
+            if (prefix == "-") return;
+            std::ofstream f(prefix + ext, std::ios::binary);
+            f.write((const char*)v.data(), v.size() * 8);
+        };
+        dump(".keys", idx.keys);
+        dump(".start", idx.startPos);
+        dump(".pos", idx.positions);
+        // sum of v[i] * (2i + 1) mod 2^64 per array
+        auto sum = [](const std::vector<uint64_t>& v)
+        {
+            uint64_t h = 0;
+            for (size_t i = 0; i < v.size(); i++) h += v[i] * (2 * (uint64_t)i + 1);
+            return h;
+        };
+        std::cout << "maxCount " << idx.maxCount << " keys " << idx.keys.size() << " positions " << idx.positions.size() << " sumKeys "
+                  << sum(idx.keys) << " sumStart " << sum(idx.startPos) << " sumPos " << sum(idx.positions) << " ms " << (uint64_t)ms
+                  << " threads " << std::thread::hardware_concurrency() << "\n";
+        return 0;
+    }
+    if (mode == "walk")
+    {
+        size_t k = std::stoul(argv[4]), w = std::stoul(argv[5]);
+        double discard = std::stod(argv[6]);
+        gahost::MinimizerIndex idx;
+        gahost::buildMinimizerIndex(graph, k, w, 1.0 - discard, idx);
+        gadev::IndexGraph ig {};
+        ig.N = graph.N; ig.firstAmbiguous = graph.firstAmbiguous; ig.len = graph.len.data(); ig.seq2 = graph.seq2.data();
+        ig.seqAmb = graph.seqAmb.data(); ig.inOff = graph.inOff.data(); ig.inNb = graph.inNb.data(); ig.nodeIds = graph.nodeIds.data();
+        ig.nodeOffset = graph.nodeOffset.data(); ig.lookupOff = graph.lookupOff.data(); ig.lookupNodes = graph.lookupNodes.data();
+        ig.originalSize = graph.originalSize.data(); ig.numLookup = (uint32_t)graph.lookupIds.size();
+        // count pass, then write pass, in node order
+        std::vector<uint64_t> first(ig.numLookup + 1, 0);
+        bool bad = false;
+        for (uint32_t li = 0; li < ig.numLookup; li++) first[li + 1] = first[li] + gadev::node_minimizers(ig, li, k, w, nullptr, nullptr, bad);
+        std::vector<uint64_t> kmers(first.back()), pos(first.back());
+        for (uint32_t li = 0; li < ig.numLookup; li++)
+        {
+            const uint32_t n = gadev::node_minimizers(ig, li, k, w, kmers.data() + first[li], pos.data() + first[li], bad);
+            if (n != first[li + 1] - first[li]) bad = true;
+        }
+        // grouped by k-mer, insertion order reversed within a k-mer
+        std::vector<uint32_t> order(kmers.size());
+        for (size_t i = 0; i < order.size(); i++) order[i] = (uint32_t)i;
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return kmers[a] < kmers[b]; });
+        std::vector<uint64_t> keys, start, positions(order.size());
+        for (size_t i = 0; i < order.size(); i++)
+        {
+            if (i == 0 || kmers[order[i]] != kmers[order[i - 1]])
+            {
+                keys.push_back(kmers[order[i]]);
+                start.push_back(i);
+            }
+        }
+        start.push_back(order.size());
+        for (size_t r = 0; r + 1 < start.size(); r++)
+            for (size_t j = start[r]; j < start[r + 1]; j++) positions[start[r] + (start[r + 1] - 1 - j)] = pos[order[j]];
+        std::cout << "bad " << bad << " occurrences " << kmers.size() << " keys " << keys.size() << " equal "
+                  << (keys == idx.keys && start == idx.startPos && positions == idx.positions) << "\n";
+        if (getenv("WALK_DEBUG"))
+        {
+            std::cout << "host occurrences " << idx.positions.size() << " keys " << idx.keys.size() << "\n";
+            std::vector<std::pair<uint64_t, uint64_t>> a, b;
+            for (size_t i = 0; i < kmers.size(); i++) a.emplace_back(kmers[i], pos[i]);
+            for (size_t r = 0; r < idx.keys.size(); r++)
+                for (size_t j = idx.startPos[r]; j < idx.startPos[r + 1]; j++) b.emplace_back(idx.keys[r], idx.positions[j]);
+            std::sort(a.begin(), a.end());
+            std::sort(b.begin(), b.end());
+            std::vector<std::pair<uint64_t, uint64_t>> onlyA, onlyB;
+            std::set_difference(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(onlyA));
+            std::set_difference(b.begin(), b.end(), a.begin(), a.end(), std::back_inserter(onlyB));
+            for (auto& x : onlyA) std::cout << "walk only " << x.first << " node " << (x.second >> 6) << " off " << (x.second & 63) << " nodeOffset " << graph.nodeOffset[x.second >> 6] << " len " << graph.len[x.second >> 6] << "\n";
+            for (auto& x : onlyB) std::cout << "host only " << x.first << " node " << (x.second >> 6) << " off " << (x.second & 63) << "\n";
+            size_t shown = 0;
+            for (size_t i = 0; i < std::min(keys.size(), idx.keys.size()) && shown < 5; i++)
+                if (keys[i] != idx.keys[i]) { std::cout << "key " << i << " " << keys[i] << " " << idx.keys[i] << "\n"; shown++; }
+        }
         return 0;
     }
     if (mode == "seeds")

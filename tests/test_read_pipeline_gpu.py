@@ -7,7 +7,9 @@ import sys
 import pytest
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from golden_sets import GOLDEN, load_gaf, load_graph, load_reads  # noqa: E402
+from golden_sets import GOLDEN, graph_file, load_gaf, load_graph, load_reads  # noqa: E402
+from test_read_pipeline_host import INDEX_CASES, harness  # noqa: E402,F401  (the host read-level harness)
+import subprocess  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -73,6 +75,45 @@ def test_gpu_seeds_match_reference_on_edge_reads(cuda_lib):
         want = ref[1::2][:len(lines)]
         got = [hashlib.sha1(line.encode()).hexdigest() for line in lines]
         assert got == want, f"{fasta}: reads {[i for i, (x, y) in enumerate(zip(got, want)) if x != y][:5]} differ"
+
+
+@pytest.mark.parametrize("name,k,w,discard", INDEX_CASES)
+def test_gpu_index_matches_host_build(cuda_lib, harness, tmp_path, name, k, w, discard):  # noqa: F811
+    """The minimizer index built on the GPU (per-node minimizer walk, radix sort by k-mer,
+    reversed groups, maxCount, device lookup table) equals the host build array for array,
+    and every key of the table the lookup kernel probes is found: the seeds of the golden
+    reads through it equal the reference's on vg50k."""
+    import numpy as np
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    exe = harness[0]
+    gag = graph_file(name, str(tmp_path))
+    prefix = os.path.join(tmp_path, "host")
+    out = subprocess.run([exe, gag, harness[2], "indexdump", str(k), str(w), str(discard), prefix], check=True, capture_output=True,
+                         text=True).stdout.split()
+    f = dict(zip(out[0::2], (int(v) for v in out[1::2])))
+    g = load_graph(name)
+    p = preset("vg")
+    p.minimizer_length, p.minimizer_window, p.minimizer_discard_fraction = k, w, discard
+    a = Aligner(Extender(DeviceGraph(g)), g, p)
+    info, keys, start, pos = a.index(arrays=True)
+    assert info["max_count"] == f["maxCount"] and info["num_keys"] == f["keys"] and info["num_positions"] == f["positions"]
+    assert info["table_capacity"] >= 2 * info["num_keys"]
+    assert np.array_equal(keys, np.fromfile(prefix + ".keys", dtype=np.uint64))
+    assert np.array_equal(start, np.fromfile(prefix + ".start", dtype=np.uint64))
+    assert np.array_equal(pos, np.fromfile(prefix + ".pos", dtype=np.uint64))
+
+
+def test_gpu_index_rejects_out_of_range_windows(cuda_lib):
+    """Minimizer windows of more than 64 positions are refused with GA_ERR_ARGUMENT and a message."""
+    from graphaligner_gb300._lib import GAError
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    g = load_graph("vg50k")
+    p = preset("vg")
+    p.minimizer_length, p.minimizer_window = 15, 79
+    with pytest.raises(GAError, match="window"):
+        Aligner(Extender(DeviceGraph(g)), g, p)
 
 
 def test_gpu_quickstart(cuda_lib, tmp_path):

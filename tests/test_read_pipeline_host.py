@@ -23,7 +23,7 @@ SOURCES = [os.path.join(ROOT, "tests", "harness", "pipeline.cpp"),
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
     os.makedirs(BUILD, exist_ok=True)
-    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "seed_table.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
+    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "index_walk.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "seed_table.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
     if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < max(os.path.getmtime(d) for d in deps):
         subprocess.run(["g++", "-std=c++17", "-O2", "-o", HARNESS, *SOURCES, "-lpthread"], check=True)
     d = tmp_path_factory.mktemp("pipeline")
@@ -64,6 +64,24 @@ def test_seed_table_finds_every_key(harness, tmp_path, name, k, w, discard):
     f = dict(zip(out[0::2], (int(v) for v in out[1::2])))
     assert f["keys"] > 10000 and f["used"] == f["keys"] and f["capacity"] >= 2 * f["keys"]
     assert f["bad"] == 0 and f["absent_found"] == 0
+
+
+INDEX_CASES = [("vg50k", 15, 20, 0.001), ("dbg100k", 19, 30, 0.0002), ("iupac20k", 15, 20, 0.001), ("dbg1m", 19, 30, 0.0002),
+               ("vg50k", 11, 11, 0.001), ("vg50k", 5, 8, 0.001), ("vg50k", 31, 94, 0.01), ("iupac20k", 11, 40, 0.001)]
+
+
+@pytest.mark.parametrize("name,k,w,discard", INDEX_CASES)
+def test_index_walk_matches_host_build(harness, tmp_path, name, k, w, discard):
+    """The GPU index build's per-node minimizer walk (index_walk.cuh, compiled for the host),
+    its occurrences grouped by k-mer with insertion order reversed, gives the host build's
+    keys, start positions and positions: IUPAC pieces, nodes exactly one window long (the
+    initial window reads the end of the node), windows of 1 and of 64 minimizer positions,
+    k = 5 (groups of hundreds of occurrences)."""
+    exe, _, reads, _ = harness
+    out = subprocess.run([exe, graph_file(name, str(tmp_path)), reads, "walk", str(k), str(w), str(discard)],
+                         check=True, capture_output=True, text=True).stdout.split()
+    f = dict(zip(out[0::2], (int(v) for v in out[1::2])))
+    assert f["bad"] == 0 and f["occurrences"] > 1000 and f["equal"] == 1, f
 
 
 @pytest.mark.parametrize("bandwidth", [10, 5])
