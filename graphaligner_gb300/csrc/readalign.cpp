@@ -27,6 +27,7 @@
 #include <string>
 #include <tuple>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 #include "../../include/graphaligner_gb300.h"
 #include "readalign.h"
@@ -788,6 +789,345 @@ static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState
         o.bpAligned = 0;
         o.alignments = 0;
     }
+}
+
+// ------------------------------------------------------------------ multiseed DP
+
+void prepareMultiseeds(const HostGraph& g, const std::vector<SeedHit>& seeds, size_t seqLen, std::vector<uint32_t>& slices,
+    std::vector<uint32_t>& nodes)
+{
+    slices.clear();
+    nodes.clear();
+    std::vector<std::unordered_set<size_t>> actives((seqLen + 64 + 1) / 64);
+    for (const auto& seed : seeds)
+    {
+        const size_t sliceIndex = seed.seqPos / 64;
+        GAH_ASSERT(sliceIndex < actives.size());
+        size_t nodeId = seed.alignmentGraphNodeId;
+        if (nodeId == SIZE_MAX)
+        {
+            const int forwardNodeId = seed.reverse ? seed.nodeID * 2 + 1 : seed.nodeID * 2;
+            nodeId = g.unitigNode(forwardNodeId, seed.nodeOffset);
+        }
+        actives[sliceIndex].insert(nodeId);
+    }
+    for (size_t i = 0; i < actives.size(); i++)
+    {
+        for (size_t nodeId : actives[i])
+        {
+            slices.push_back((uint32_t)i);
+            nodes.push_back((uint32_t)nodeId);
+        }
+    }
+}
+
+void addMappingQualities(std::vector<AlignmentItem>& alignments)
+{
+    for (size_t i = 0; i < alignments.size(); i++)
+    {
+        double otherSum = 0;
+        for (size_t j = 0; j < alignments.size(); j++)
+        {
+            if (i == j) continue;
+            if (!alignmentIncompatible(alignments[i], alignments[j])) continue;
+            if (alignments[j].alignmentXScore >= alignments[i].alignmentXScore + 1)
+            {
+                otherSum += 10;
+                break;
+            }
+            otherSum += pow(10.0, alignments[j].alignmentXScore - alignments[i].alignmentXScore);
+            if (otherSum >= 10) break;
+        }
+        if (otherSum >= 10) alignments[i].mappingQuality = 0;
+        else if (otherSum <= 0.000001) alignments[i].mappingQuality = 60;
+        else
+        {
+            alignments[i].mappingQuality = -log(1.0 - 1.0 / (1.0 + otherSum)) * 10;
+            if (alignments[i].mappingQuality >= 60) alignments[i].mappingQuality = 60;
+        }
+    }
+}
+
+// int32 value of a size_t expression, as the reference's ScoreType assignments truncate it
+static inline int32_t score32(uint64_t x) { return (int32_t)(uint32_t)x; }
+
+// GraphAlignerBitvectorBanded::removeDuplicateTraces (GraphAlignerBitvectorBanded.h:144-169):
+// by X-score, best first (std::sort, as the reference), then a trace ending where an earlier
+// one ends is swapped out
+static void removeDuplicateTraces(std::vector<OnewayTrace>& traces, int32_t cost)
+{
+    if (traces.empty()) return;
+    std::sort(traces.begin(), traces.end(), [cost](const OnewayTrace& left, const OnewayTrace& right)
+    {
+        int32_t leftScore = score32((left.trace[0].seqPos - left.trace.back().seqPos + 1) * 100);
+        leftScore = score32((uint64_t)(uint32_t)leftScore - (uint64_t)(uint32_t)(left.score * cost));
+        int32_t rightScore = score32((right.trace[0].seqPos - right.trace.back().seqPos + 1) * 100);
+        rightScore = score32((uint64_t)(uint32_t)rightScore - (uint64_t)(uint32_t)(right.score * cost));
+        return leftScore > rightScore;
+    });
+    for (size_t i = traces.size() - 1; i > 0; i--)
+    {
+        for (size_t j = 0; j < i; j++)
+        {
+            const auto& a = traces[i].trace.back();
+            const auto& b = traces[j].trace.back();
+            if (a.node == b.node && a.nodeOffset == b.nodeOffset && a.seqPos == b.seqPos)
+            {
+                std::swap(traces[i], traces.back());
+                traces.pop_back();
+                break;
+            }
+        }
+    }
+}
+
+// GraphAligner::clipTraceStart (GraphAligner.h:702-738): the trace starts where its X-score
+// counted from the end is highest
+static void clipTraceStart(OnewayTrace& trace, int32_t cost)
+{
+    if (trace.trace.empty()) return;
+    int32_t maxX = INT32_MIN;
+    size_t maxXIndex = SIZE_MAX;
+    size_t score = 0;
+    size_t maxXScore = 0;
+    const size_t n = trace.trace.size();
+    for (size_t i = n - 1; i < n; i--)
+    {
+        const auto& t = trace.trace[i];
+        const bool posSwitch = (i == n - 1) || t.nodeSwitch || t.nodeOffset != trace.trace[i + 1].nodeOffset || t.node != trace.trace[i + 1].node;
+        if (i != n - 1 && trace.trace[i + 1].seqPos == t.seqPos) score += 1;
+        else if (i != n - 1 && !posSwitch) score += 1;
+        else if (!characterMatch(t.seqChar, t.graphChar)) score += 1;
+        const int32_t xHere = score32((trace.trace.back().seqPos - t.seqPos + 1) * 100 - score * (uint64_t)(int64_t)cost);
+        if (xHere > maxX)
+        {
+            maxX = xHere;
+            maxXIndex = i;
+            maxXScore = score;
+        }
+    }
+    GAH_ASSERT(maxXIndex < n);
+    if (maxXIndex > 0)
+    {
+        trace.score = (int32_t)maxXScore;
+        trace.trace.erase(trace.trace.begin(), trace.trace.begin() + maxXIndex);
+    }
+}
+
+// GraphAligner::mergeTraces (GraphAligner.h:316-345)
+static OnewayTrace mergeTraces(OnewayTrace&& bw, OnewayTrace&& fw)
+{
+    GAH_ASSERT(!fw.failed() || !bw.failed());
+    OnewayTrace merged;
+    if (!bw.failed())
+    {
+        GAH_ASSERT(!bw.trace.empty());
+        merged = std::move(bw);
+        if (!fw.failed())
+        {
+            GAH_ASSERT(!merged.trace.empty() && !fw.trace.empty());
+            const auto& a = merged.trace.back();
+            const auto& b = fw.trace[0];
+            GAH_ASSERT(a.node == b.node && a.nodeOffset == b.nodeOffset && a.seqPos == b.seqPos);
+            if (!characterMatch(b.seqChar, b.graphChar))
+            {
+                GAH_ASSERT(merged.score >= 1 && fw.score >= 1);
+                fw.score -= 1;
+            }
+            merged.trace.pop_back();
+            merged.trace.insert(merged.trace.end(), fw.trace.begin(), fw.trace.end());
+            merged.score += fw.score;
+        }
+    }
+    else if (!fw.failed())
+    {
+        merged = std::move(fw);
+    }
+    return merged;
+}
+
+void alignBatchMultiseed(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, MultiseedFn multiseed, void* msCtx,
+    ExtendFn extend, void* ctx, std::vector<ReadOutput>& out, BatchStats& stats)
+{
+    const size_t n = reads.size();
+    out.assign(n, ReadOutput {});
+    auto t0 = std::chrono::steady_clock::now();
+    struct MsRead
+    {
+        ReadState r;
+        std::vector<uint32_t> slices, nodes;
+        std::vector<OnewayTrace> forward;     // clipped, read order, bigraph positions
+        std::vector<int> backwardRequest;     // per forward trace: index in the backward batch, or -1
+    };
+    std::vector<MsRead> ms(n);
+    parallelFor(n, [&](size_t i)
+    {
+        MsRead& m = ms[i];
+        m.r.name = std::move(reads[i].name);
+        m.r.seq = std::move(reads[i].seq);
+        if (reads[i].seeds.empty())
+        {
+            out[i].noSeeds = true;
+            m.r.done = true;
+            return;
+        }
+        m.r.rev = reverseComplement(m.r.seq);
+        try
+        {
+            prepareMultiseeds(g, reads[i].seeds, m.r.seq.size(), m.slices, m.nodes);
+        }
+        catch (const ReadFailure&)
+        {
+            m.r.failed = true;
+        }
+    });
+    // the multiseed DP of every read with seeds
+    std::vector<MultiseedRequest> rq;
+    std::vector<size_t> rqRead;
+    for (size_t i = 0; i < n; i++)
+    {
+        if (ms[i].r.done || ms[i].r.failed) continue;
+        rq.push_back(MultiseedRequest { ms[i].r.seq.data(), (uint32_t)ms[i].r.seq.size(), ms[i].slices.data(), ms[i].nodes.data(), (uint32_t)ms[i].nodes.size() });
+        rqRead.push_back(i);
+    }
+    std::vector<MultiseedResult> rs(rq.size());
+    stats.collectMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (!rq.empty()) multiseed(msCtx, rq, rs);
+    stats.rounds += 1;
+    stats.extensions += rq.size();
+    t0 = std::chrono::steady_clock::now();
+    // duplicate removal, read order, clipping, and the backward extension of every trace
+    // that does not start at the read's first base
+    std::vector<std::vector<ExtensionRequest>> perRead(rq.size());
+    parallelFor(rq.size(), [&](size_t k)
+    {
+        MsRead& m = ms[rqRead[k]];
+        const MultiseedResult& res = rs[k];
+        if (res.status != GA_OK)
+        {
+            m.r.failed = true;
+            return;
+        }
+        try
+        {
+            std::vector<OnewayTrace> traces(res.traces.size());
+            for (size_t t = 0; t < res.traces.size(); t++)
+            {
+                ExtensionResult e;
+                e.status = GA_OK;
+                e.score = res.scores[t];
+                e.itemPtr = res.traces[t].data();
+                e.itemCount = res.traces[t].size();
+                traces[t] = decodeTrace(g, e, m.r.seq.data(), m.r.seq.size());
+                GAH_ASSERT(!traces[t].trace.empty());
+            }
+            removeDuplicateTraces(traces, p.xscoreErrorCost);
+            for (auto& t : traces) std::reverse(t.trace.begin(), t.trace.end());
+            for (auto& t : traces)
+            {
+                clipTraceStart(t, p.xscoreErrorCost);
+                fixForwardTraceSeqPos(g, t, 0, m.r.seq);
+                int request = -1;
+                if (t.trace[0].seqPos != 0)
+                {
+                    auto rp = g.reversePosition((int)t.trace[0].node, t.trace[0].nodeOffset);
+                    ExtensionRequest e;
+                    e.seq = m.r.rev.data() + m.r.rev.size() - t.trace[0].seqPos;
+                    e.len = (uint32_t)t.trace[0].seqPos;
+                    e.bignode = rp.first;
+                    e.offset = rp.second;
+                    const size_t node = g.unitigNode(e.bignode, e.offset);
+                    e.node = (uint32_t)node;
+                    e.nodeOffset = (uint32_t)(e.offset - g.nodeOffset[node]);
+                    request = (int)perRead[k].size();
+                    perRead[k].push_back(e);
+                }
+                m.backwardRequest.push_back(request);
+                m.forward.push_back(std::move(t));
+            }
+        }
+        catch (const ReadFailure&)
+        {
+            m.r.failed = true;
+            m.forward.clear();
+            m.backwardRequest.clear();
+            perRead[k].clear();
+        }
+    });
+    for (const auto& res : rs) stats.cellSteps += res.steps;
+    std::vector<ExtensionRequest> bq;
+    std::vector<size_t> firstRequest(rq.size());
+    for (size_t k = 0; k < rq.size(); k++)
+    {
+        firstRequest[k] = bq.size();
+        bq.insert(bq.end(), perRead[k].begin(), perRead[k].end());
+    }
+    std::vector<ExtensionResult> br(bq.size());
+    stats.consumeMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (!bq.empty()) extend(ctx, bq, br);
+    stats.rounds += 1;
+    stats.extensions += bq.size();
+    for (const auto& e : br) stats.cellSteps += e.steps;
+    t0 = std::chrono::steady_clock::now();
+    parallelFor(rq.size(), [&](size_t k)
+    {
+        MsRead& m = ms[rqRead[k]];
+        if (m.r.failed) return;
+        try
+        {
+            for (size_t t = 0; t < m.forward.size(); t++)
+            {
+                OnewayTrace fw = std::move(m.forward[t]);
+                OnewayTrace bw;
+                bw.score = INT32_MAX;
+                if (m.backwardRequest[t] >= 0)
+                {
+                    const size_t q = firstRequest[k] + (size_t)m.backwardRequest[t];
+                    if (br[q].status == GA_ASSERT) throw ReadFailure {};
+                    GAH_ASSERT(br[q].status == GA_OK || br[q].status == GA_TRACE_FAILED);
+                    bw = decodeTrace(g, br[q], bq[q].seq, bq[q].len);
+                    if (!bw.failed())
+                    {
+                        std::reverse(bw.trace.begin(), bw.trace.end());
+                        fixReverseTraceSeqPosAndOrder(g, bw, fw.trace[0].seqPos - 1, m.r.seq);
+                    }
+                }
+                OnewayTrace merged = mergeTraces(std::move(bw), std::move(fw));
+                if (merged.failed()) continue;
+                GAH_ASSERT(!merged.trace.empty());
+                const int32_t alignmentXScore = score32((merged.trace.back().seqPos - merged.trace[0].seqPos + 1) * 100)
+                    - p.xscoreErrorCost * merged.score;
+                if (alignmentXScore <= 0) continue;
+                AlignmentItem item;
+                item.trace = std::make_shared<OnewayTrace>(std::move(merged));
+                item.alignmentScore = item.trace->score;
+                item.alignmentStart = item.trace->trace[0].seqPos;
+                item.alignmentEnd = item.trace->trace.back().seqPos + 1;
+                GAH_ASSERT(item.alignmentEnd - 1 < m.r.seq.size());
+                item.alignmentXScore = (double)alignmentXScore / 100.0;
+                m.r.alignments.push_back(std::move(item));
+            }
+            addMappingQualities(m.r.alignments);
+        }
+        catch (const ReadFailure&)
+        {
+            m.r.failed = true;
+            m.r.alignments.clear();
+        }
+    });
+    stats.consumeMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    t0 = std::chrono::steady_clock::now();
+    parallelFor(n, [&](size_t i)
+    {
+        if (out[i].noSeeds) return;
+        finalizeRead(g, p, ms[i].r, out[i]);
+    });
+    for (size_t i = 0; i < n; i++)
+    {
+        stats.bpAligned += out[i].bpAligned;
+        stats.failedReads += out[i].failed ? 1 : 0;
+    }
+    stats.finishMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
 struct SeedLoopPool::Impl

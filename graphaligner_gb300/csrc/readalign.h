@@ -190,6 +190,44 @@ void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadIn
 void alignBatchTwoLanes(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend,
     void* ctxA, void* ctxB, std::vector<ReadOutput>& out, BatchStats& stats);
 
+// ---- multiseed DP (--multiseed-DP, Aligner.cpp:461-476) ----
+
+// GraphAligner::prepareSeedsForMultiseeding (GraphAligner.h:211-248): the distinct
+// alignment-graph nodes seeded in each 64-row slice of the read, slice by slice, in the
+// iteration order of the std::unordered_set the reference collects them in
+void prepareMultiseeds(const HostGraph& g, const std::vector<SeedHit>& seeds, size_t seqLen, std::vector<uint32_t>& slices,
+    std::vector<uint32_t>& nodes);
+
+// AlignmentSelection::AddMappingQualities (AlignmentSelection.cpp:97-135)
+void addMappingQualities(std::vector<AlignmentItem>& alignments);
+
+// One read's multiseed DP: its seeds (prepareMultiseeds) in, its traces out in the
+// reference's order, each in DP order (ga_multiseed_batch's contract).
+struct MultiseedRequest
+{
+    const char* seq;
+    uint32_t len;
+    const uint32_t* slices;
+    const uint32_t* nodes;
+    uint32_t numSeeds;
+};
+
+struct MultiseedResult
+{
+    int32_t status = 0;
+    uint64_t steps = 0;
+    std::vector<int32_t> scores;
+    std::vector<std::vector<uint64_t>> traces;   // packed items
+};
+
+typedef void (*MultiseedFn)(void* ctx, const std::vector<MultiseedRequest>& requests, std::vector<MultiseedResult>& results);
+
+// AlignMultiseed per read (GraphAligner.h:77-92, 603-629): the multiseed DP, duplicate
+// removal, clipping, a backward extension from each trace's start (clipAndAddBackwardTrace,
+// :347-373), mapping qualities, then selection and GAF as alignBatch.
+void alignBatchMultiseed(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, MultiseedFn multiseed, void* msCtx,
+    ExtendFn extend, void* ctx, std::vector<ReadOutput>& out, BatchStats& stats);
+
 // MinimizerSeeder with one bucket (MinimizerSeeder.h:14-47)
 struct MinimizerIndex
 {

@@ -131,6 +131,38 @@ int ga_extender_free(ga_extender_t ext);
  * GA_ASSERT a reference assert (ThreadReadAssertion). */
 int ga_extend_batch(ga_extender_t ext, const ga_extend_params* params,
                     const ga_extend_batch_desc* batch, ga_extend_results* results);
+/* ---- multiseed DP ----
+ * A batch of GraphAlignerBitvectorBanded::getMultiseedTraces calls (--multiseed-DP,
+ * src/GraphAlignerBitvectorBanded.h:45-57): per read, the DP over every slice of the
+ * read with its seeds started in their slices (getMultiseedSlices, :727-822), then a
+ * trace from each local maximum of the per-node exact-end-position X-scores
+ * (getLocalMaximaTracesFromTable, src/GraphAlignerBitvectorCommon.h:355-494).  The
+ * traces come in the reference's order, each in DP order (end first), before
+ * removeDuplicateTraces and the reversal, which stay with the caller. */
+typedef struct ga_multiseed_batch_desc {
+    uint32_t num;                     /* reads */
+    const uint8_t*  seq;
+    const uint64_t* seq_offset;
+    const uint32_t* seq_len;
+    const uint64_t* seed_offset;      /* [num + 1]: read i's seeds are [seed_offset[i], seed_offset[i+1]) */
+    const uint32_t* seed_slice;       /* seqPos / 64 of each seed, non-decreasing within a read */
+    const uint32_t* seed_node;        /* alignment-graph (split) node of each seed */
+    const uint64_t* trace_offset;     /* [num] where read i's trace items start in trace_items */
+    const uint64_t* trace_capacity;   /* [num] room for read i's items, all its traces together */
+    uint32_t max_traces;              /* room per read in the trace tables */
+    double   multimap_score_fraction; /* AlignerParams::multimapScoreFraction */
+} ga_multiseed_batch_desc;
+
+typedef struct ga_multiseed_results {
+    int32_t*  status;                 /* [num] GA_OK / GA_ASSERT / GA_CAPACITY / GA_BAD_REQUEST */
+    uint32_t* num_traces;             /* [num] */
+    int32_t*  trace_score;            /* [num * max_traces] OnewayTrace::score */
+    uint64_t* trace_start;            /* [num * max_traces] first item, counted from trace_offset[i] */
+    uint32_t* trace_len;              /* [num * max_traces] items */
+    uint64_t* trace_items;            /* packed items (GA_TRACE_* layout) */
+    uint64_t* cell_steps;             /* [num] or NULL */
+} ga_multiseed_results;
+
 /* Device-resident variant: every pointer in batch/results is a device pointer.
  * Work is enqueued on `stream` (a cudaStream_t; NULL = the extender's stream);
  * the call reads the lengths back once to order the work and waits for the

@@ -345,6 +345,10 @@ struct Item
 	u64 HP = 0;
 	u64 HN = 0;
 	i32 minScore = 0;
+	// multiseed DP only: DPSlice::seedstartNodes and DPSlice::nodeMaxExactEndposScore
+	// (Common.h:184-185) kept with the node's band entry
+	bool seedStart = false;
+	i32 nodeMax = 0;
 };
 
 // One band: node -> item in first-insertion order (see refshim/phmap.h)
@@ -389,6 +393,7 @@ struct Edge
 	uint32_t target;
 	WS incoming;
 	bool skipFirst;
+	bool force = false;     // EdgeWithPriority::forceCalculation (a seed start)
 };
 
 // ComponentPriorityQueue (ComponentPriorityQueue.h:8-156): a std::priority_queue
@@ -440,17 +445,24 @@ struct Params
 	i32 xdrop;
 	size_t maxCells;
 	i32 cost;
+	double multimapScoreFraction = 0.9;
 };
 
-// calculateNodeInner (GraphAlignerBitvectorCommon.h:1113-1478) with no extra (seed) slice:
-// the single-seed path passes the fake extraSlice (scoreEnd INT32_MAX) everywhere.
+static inline bool isFake(const WS& w) { return w.scoreEnd == INT32_MAX; }
+static const WS FakeSlice { 0, 0, INT32_MAX };
+
+// calculateNodeInner (GraphAlignerBitvectorCommon.h:1113-1478).  `extra` is the extraSlice:
+// the single-seed path passes the fake slice (scoreEnd INT32_MAX) everywhere; the multiseed
+// DP passes the seed-start slice (getSeedSlice) for a node that is a seed start in this slice.
 // AllowEarlyLeave = true is the fill (calculateNodeClipPrecise, :1104-1111);
 // false is recalcNodeWordslice (:1078-1102), which records every column.
 template <bool AllowEarlyLeave>
 static NodeCalc calcNode(const Graph& g, const Params& p, uint32_t i, Item& slice, const EqV& eqv, const Item& previousSlice,
 	const std::vector<Edge>& incoming, const std::vector<char>* previousBandHas, i32 seqOffset,
-	std::vector<WS>* columns, uint64_t& columnSteps)
+	std::vector<WS>* columns, uint64_t& columnSteps, const WS& extra)
 {
+	const bool hasExtra = !isFake(extra);
+	bool forceCalculation = false;
 	ORA_ASSERT(incoming.size() > 0);
 	WS ws;
 	bool hasWs = false;
@@ -467,6 +479,7 @@ static NodeCalc calcNode(const Graph& g, const Params& p, uint32_t i, Item& slic
 	for (const auto& inc : incoming)
 	{
 		result.cellsProcessed++;
+		if (inc.force) forceCalculation = true;
 		if (inc.skipFirst)
 		{
 			ws = hasWs ? merge(ws, inc.incoming) : inc.incoming;
@@ -477,6 +490,7 @@ static NodeCalc calcNode(const Graph& g, const Params& p, uint32_t i, Item& slic
 		u64 hinP, hinN;
 		i32 compareHin = INT32_MAX;
 		if (previousSlice.exists) compareHin = previousSlice.startSlice.scoreEnd;
+		if (hasExtra) compareHin = std::min(compareHin, scoreBeforeStart(extra));
 		i32 incBefore = scoreBeforeStart(inc.incoming);
 		if (compareHin < incBefore) { hinP = 0; hinN = 1; }
 		else if (compareHin > incBefore) { hinP = 1; hinN = 0; }
@@ -496,9 +510,10 @@ static NodeCalc calcNode(const Graph& g, const Params& p, uint32_t i, Item& slic
 	result.minScore = ws.scoreEnd;
 	result.minScoreNode = i;
 	result.minScoreNodeOffset = 0;
+	if (hasExtra) ws = merge(ws, extra);
 	result.maxExactEndposScore = maxXScore(ws, seqOffset, p.cost);
 	result.maxExactEndposNode = i;
-	if (slice.exists)
+	if (!forceCalculation && slice.exists)
 	{
 		uint32_t inCount = g.inCount(i);
 		bool singleInBand = false;
@@ -567,7 +582,42 @@ static NodeCalc calcNode(const Graph& g, const Params& p, uint32_t i, Item& slic
 		i32 scoreBefore = scoreBeforeStart(ws);
 		i32 scoreComparison = previousSlice.startSlice.scoreEnd;
 		ORA_ASSERT(scoreBefore <= scoreComparison);
-		if (scoreBefore < scoreComparison)
+		if (hasExtra)
+		{
+			// Common.h:1314-1362: the row above follows the lower of the previous slice's
+			// bottom row and the seed start's score before the slice
+			const i32 extraBefore = scoreBeforeStart(extra);
+			scoreBefore = std::min(scoreBefore, extraBefore);
+			if (scoreBefore < scoreComparison) forceMask |= 1;
+			i32 adjustScore = std::min(scoreBefore, scoreComparison);
+			for (uint32_t fixoffset = 1; fixoffset < 64 && fixoffset < nodeLength; fixoffset++)
+			{
+				i32 newScoreComparison = scoreComparison + (i32)((fixedHP >> fixoffset) & 1) - (i32)((fixedHN >> fixoffset) & 1);
+				if (scoreBefore < extraBefore) scoreBefore += 1;
+				u64 mask = 1ULL << fixoffset;
+				if (scoreBefore < newScoreComparison) forceMask |= mask;
+				i32 newAdjustScore = std::min(newScoreComparison, scoreBefore);
+				ORA_ASSERT(newAdjustScore >= adjustScore - 1 && newAdjustScore <= adjustScore + 1);
+				if (newAdjustScore == adjustScore - 1)
+				{
+					fixedHN |= mask;
+					fixedHP &= ~mask;
+				}
+				else if (newAdjustScore == adjustScore)
+				{
+					fixedHP &= ~mask;
+					fixedHN &= ~mask;
+				}
+				else
+				{
+					fixedHP |= mask;
+					fixedHN &= ~mask;
+				}
+				adjustScore = newAdjustScore;
+				scoreComparison = newScoreComparison;
+			}
+		}
+		else if (scoreBefore < scoreComparison)
 		{
 			forceMask |= 1;
 			for (int fixoffset = 1; fixoffset < 64; fixoffset++)
@@ -613,8 +663,19 @@ static NodeCalc calcNode(const Graph& g, const Params& p, uint32_t i, Item& slic
 			newWs.VP &= AllOnes ^ 1;
 			newWs.VN |= 1;
 		}
-		u64 hinP = newHP >> 63;
-		u64 hinN = newHN >> 63;
+		u64 hinP, hinN;
+		if (hasExtra)
+		{
+			newWs = merge(newWs, extra);
+			ORA_ASSERT(newWs.scoreEnd >= ws.scoreEnd - 1 && newWs.scoreEnd <= ws.scoreEnd + 1);
+			hinP = newWs.scoreEnd == ws.scoreEnd + 1 ? 1 : 0;
+			hinN = newWs.scoreEnd == ws.scoreEnd - 1 ? 1 : 0;
+		}
+		else
+		{
+			hinP = newHP >> 63;
+			hinN = newHN >> 63;
+		}
 		ws = newWs;
 		if (ws.scoreEnd < result.minScore)
 		{
@@ -636,16 +697,39 @@ struct State
 {
 	std::vector<char> previousBand;
 	std::vector<char> currentBand;
+	std::vector<char> hasSeedStart;
 	ComponentQueue queue;
-	explicit State(size_t n) : previousBand(n, 0), currentBand(n, 0) {}
+	explicit State(size_t n) : previousBand(n, 0), currentBand(n, 0), hasSeedStart(n, 0) {}
+};
+
+// The seeds one multiseed slice starts (seedHits[seedhitStart, seedhitEnd) of calculateSlice),
+// with the seed-start slice of that slice (getSeedSlice); none for the single-seed path.
+struct SliceSeeds
+{
+	const uint32_t* nodes = nullptr;
+	size_t count = 0;
+	WS slice { 0, 0, INT32_MAX };
+	bool store = false;     // storeNodeExactEndposScores
 };
 
 // GraphAlignerBitvectorBanded::calculateSlice (GraphAlignerBitvectorBanded.h:255-511),
-// component-queue branch without seed hits.
+// component-queue branch; seeds (multiseed DP) as addSeedHitToScoresAndQueue (:228-253).
 static NodeCalc calculateSlice(const Graph& g, const Params& p, const char* seq, size_t seqLen, size_t j,
 	Band& currentSlice, const Band& previousSlice, State& st, i32 previousQuitScore, int bandwidth, i32 previousMinScore,
-	uint64_t& columnSteps)
+	uint64_t& columnSteps, const SliceSeeds& seeds = SliceSeeds())
 {
+	const bool multiseed = !isFake(seeds.slice);
+	if (previousMinScore == INT32_MAX - bandwidth - 1)
+	{
+		ORA_ASSERT(multiseed);
+		previousMinScore = scoreBeforeStart(seeds.slice);
+		previousQuitScore = add(scoreBeforeStart(seeds.slice), bandwidth);
+	}
+	if (multiseed && previousMinScore > seeds.slice.scoreEnd)
+	{
+		previousMinScore = seeds.slice.scoreEnd;
+		previousQuitScore = add(seeds.slice.scoreEnd, bandwidth);
+	}
 	NodeCalc result;
 	result.minScore = INT32_MAX - bandwidth - 1;
 	result.minScoreNode = SIZE_MAX;
@@ -654,7 +738,7 @@ static NodeCalc calculateSlice(const Graph& g, const Params& p, const char* seq,
 	result.maxExactEndposScore = INT32_MIN;
 	result.cellsProcessed = 0;
 	EqV eqv = getEq(seq, seqLen, j);
-	ORA_ASSERT(previousSlice.size() > 0);
+	ORA_ASSERT(previousSlice.size() > 0 || multiseed);
 	for (size_t k = 0; k < previousSlice.size(); k++)
 	{
 		uint32_t node = previousSlice.nodes[k];
@@ -674,7 +758,28 @@ static NodeCalc calculateSlice(const Graph& g, const Params& p, const char* seq,
 		}
 		st.queue.insert(g.d->component[node], item.minScore, Edge { node, sourceSlice(item.startSlice.scoreEnd), true });
 	}
-	ORA_ASSERT(st.queue.size() > 0);
+	ORA_ASSERT(st.queue.size() > 0 || multiseed);
+	if (multiseed && scoreBeforeStart(seeds.slice) < add(previousQuitScore, 64))
+	{
+		for (size_t k = 0; k < seeds.count; k++)
+		{
+			const uint32_t node = seeds.nodes[k];
+			ORA_ASSERT(node < g.d->num_nodes);
+			st.currentBand[node] = 1;
+			Item& item = currentSlice.add(node);
+			if (seeds.store) item.nodeMax = 0;
+			item.minScore = seeds.slice.scoreEnd;
+			item.startSlice = seeds.slice;
+			item.endSlice = seeds.slice;
+			item.exists = true;
+			Edge e { node, seeds.slice, true };
+			e.force = true;
+			st.queue.insert(g.d->component[node], getValue(seeds.slice, 0), e);
+			ORA_ASSERT(!st.hasSeedStart[node]);
+			st.hasSeedStart[node] = 1;
+			item.seedStart = true;
+		}
+	}
 	i32 currentMinScoreAtEndRow = result.minScore;
 	while (st.queue.size() > 0)
 	{
@@ -691,6 +796,8 @@ static NodeCalc calculateSlice(const Graph& g, const Params& p, const char* seq,
 		Item& thisNode = currentSlice.at(i);
 		WS oldEnd = thisNode.endSlice;
 		if (!thisNode.exists) oldEnd = WS { 0, 0, INT32_MAX };
+		const WS extra = st.hasSeedStart[i] ? seeds.slice : FakeSlice;
+		if (!isFake(extra)) oldEnd = merge(oldEnd, extra);
 		Item previousThisNode;
 		if (st.previousBand[i])
 		{
@@ -703,9 +810,10 @@ static NodeCalc calculateSlice(const Graph& g, const Params& p, const char* seq,
 			previousThisNode.HN = 0;
 			previousThisNode.exists = false;
 		}
-		NodeCalc nodeCalc = calcNode<true>(g, p, i, thisNode, eqv, previousThisNode, extras, &st.previousBand, (i32)j, nullptr, columnSteps);
+		NodeCalc nodeCalc = calcNode<true>(g, p, i, thisNode, eqv, previousThisNode, extras, &st.previousBand, (i32)j, nullptr, columnSteps, extra);
 		ORA_ASSERT(nodeCalc.maxExactEndposScore != INT32_MIN);
 		st.queue.pop();
+		if (seeds.store) thisNode.nodeMax = std::max(nodeCalc.maxExactEndposScore, thisNode.nodeMax);
 		ORA_ASSERT(nodeCalc.minScore <= (i32)j + bandwidth + 64 + 64);
 		currentMinScoreAtEndRow = std::min(currentMinScoreAtEndRow, nodeCalc.minScore);
 		if (nodeCalc.minScore < thisNode.minScore) thisNode.minScore = nodeCalc.minScore;
@@ -738,7 +846,8 @@ static NodeCalc calculateSlice(const Graph& g, const Params& p, const char* seq,
 		ORA_ASSERT(nodeCalc.cellsProcessed > 0);
 		if (result.cellsProcessed > p.maxCells) break;
 	}
-	ORA_ASSERT(result.minScoreNode != SIZE_MAX);
+	for (size_t k = 0; k < seeds.count && multiseed; k++) st.hasSeedStart[seeds.nodes[k]] = 0;
+	ORA_ASSERT(result.minScoreNode != SIZE_MAX || (multiseed && seeds.count == 0));
 	st.queue.clear();
 	return result;
 }
@@ -757,9 +866,8 @@ struct Pos
 	bool operator!=(const Pos& o) const { return !(*this == o); }
 };
 
-static const WS FakeSlice { 0, 0, INT32_MAX };
-
-static std::vector<WS> recalc(const Graph& g, const Params& p, uint32_t node, const Item& slice, const EqV& eqv, const Item& previous, i32 seqOffset)
+static std::vector<WS> recalc(const Graph& g, const Params& p, uint32_t node, const Item& slice, const EqV& eqv, const Item& previous, i32 seqOffset,
+	const WS& extra = FakeSlice)
 {
 	std::vector<Edge> incoming;
 	incoming.push_back(Edge { node, slice.startSlice, true });
@@ -767,7 +875,7 @@ static std::vector<WS> recalc(const Graph& g, const Params& p, uint32_t node, co
 	result.reserve(64);
 	Item copy = slice;
 	uint64_t dummy = 0;
-	calcNode<false>(g, p, node, copy, eqv, previous, incoming, nullptr, seqOffset, &result, dummy);
+	calcNode<false>(g, p, node, copy, eqv, previous, incoming, nullptr, seqOffset, &result, dummy, extra);
 	ORA_ASSERT(result.size() == g.len(node));
 	ORA_ASSERT(result[0] == slice.startSlice);
 	ORA_ASSERT(result.back() == slice.endSlice);
@@ -784,7 +892,7 @@ static Item previousOrDefault(const Band& band, uint32_t node)
 }
 
 // pickBacktraceInside (Common.h:770-815)
-static std::vector<Pos> backtraceInside(const Graph& g, size_t verticalOffset, const std::vector<WS>& ns, Pos pos, const char* seq)
+static std::vector<Pos> backtraceInside(const Graph& g, size_t verticalOffset, const std::vector<WS>& ns, Pos pos, const char* seq, const WS& extra)
 {
 	size_t hori = pos.nodeOffset;
 	size_t vert = pos.seqPos - verticalOffset;
@@ -799,7 +907,7 @@ static std::vector<Pos> backtraceInside(const Graph& g, size_t verticalOffset, c
 		if (verticalScore == scoreHere - 1) { vert--; result.push_back(Pos { pos.node, hori, vert + verticalOffset }); continue; }
 		if (diagonalScore == scoreHere - (eq ? 0 : 1)) { hori--; vert--; result.push_back(Pos { pos.node, hori, vert + verticalOffset }); continue; }
 		if (horizontalScore == scoreHere - 1) { hori--; result.push_back(Pos { pos.node, hori, vert + verticalOffset }); continue; }
-		ORA_ASSERT(scoreHere == getValue(FakeSlice, (int)vert));
+		ORA_ASSERT(scoreHere == getValue(extra, (int)vert));
 		break;
 	}
 	return result;
@@ -809,12 +917,12 @@ struct Step { Pos pos; bool nodeSwitch; };
 
 // pickBacktraceCorner (Common.h:936-1054)
 static Step backtraceCorner(const Graph& g, const Band& current, const Band& previous, uint32_t node, size_t j, const char* seq,
-	i32 quitScore, bool scoresNotValid, i32 previousQuitScore, bool previousScoresNotValid)
+	i32 quitScore, bool scoresNotValid, i32 previousQuitScore, bool previousScoresNotValid, const WS& extra)
 {
 	i32 scoreHere = getValue(current.at(node).startSlice, 0);
 	if (scoresNotValid || scoreHere > quitScore)
 	{
-		if (scoreHere == getValue(FakeSlice, 0)) return Step { Pos { node, 0, j }, false };
+		if (scoreHere == getValue(extra, 0)) return Step { Pos { node, 0, j }, false };
 		i32 smallestFound = scoreHere + 1;
 		Pos smallestPos { SIZE_MAX, SIZE_MAX, SIZE_MAX };
 		bool nodeChange = false;
@@ -898,8 +1006,8 @@ static Step backtraceCorner(const Graph& g, const Band& current, const Band& pre
 			}
 		}
 	}
-	if (eq && scoreHere == scoreBeforeStart(FakeSlice)) return Step { Pos { node, 0, j }, false };
-	if (scoreHere == getValue(FakeSlice, 0)) return Step { Pos { node, 0, j }, false };
+	if (eq && scoreHere == scoreBeforeStart(extra)) return Step { Pos { node, 0, j }, false };
+	if (scoreHere == getValue(extra, 0)) return Step { Pos { node, 0, j }, false };
 	if (bestInvalidScore < scoreHere + 1) return Step { bestInvalid, bestInvalidSwitch };
 	ORA_ASSERT(false);
 	return Step { Pos { 0, 0, 0 }, false };
@@ -907,12 +1015,12 @@ static Step backtraceCorner(const Graph& g, const Band& current, const Band& pre
 
 // pickBacktraceHorizontalCrossing (Common.h:817-884): returns (walked-to position, next step)
 static std::pair<Step, Step> backtraceHorizontal(const Graph& g, const Band& current, const Band& previous, size_t j, uint32_t node, Pos pos,
-	const char* seq, i32 quitScore, bool scoresNotValid, i32 previousQuitScore, bool previousScoresNotValid)
+	const char* seq, i32 quitScore, bool scoresNotValid, i32 previousQuitScore, bool previousScoresNotValid, const WS& extra)
 {
 	WS startSlice = current.at(node).startSlice;
 	while (pos.seqPos % 64 != 0 && (startSlice.VP & (1ULL << (pos.seqPos % 64)))) pos.seqPos--;
 	size_t offset = pos.seqPos % 64;
-	if (offset == 0) return { Step { pos, false }, backtraceCorner(g, current, previous, node, j, seq, quitScore, scoresNotValid, previousQuitScore, previousScoresNotValid) };
+	if (offset == 0) return { Step { pos, false }, backtraceCorner(g, current, previous, node, j, seq, quitScore, scoresNotValid, previousQuitScore, previousScoresNotValid, extra) };
 	bool eq = characterMatch(seq[pos.seqPos], g.charAt((uint32_t)pos.node, (uint32_t)pos.nodeOffset));
 	i32 scoreHere = getValue(startSlice, (int)offset);
 	if (scoresNotValid || scoreHere > quitScore)
@@ -940,7 +1048,7 @@ static std::pair<Step, Step> backtraceHorizontal(const Graph& g, const Band& cur
 				}
 			}
 		}
-		if (smallestPos == pos) ORA_ASSERT(getValue(FakeSlice, (int)offset) == scoreHere);
+		if (smallestPos == pos) ORA_ASSERT(getValue(extra, (int)offset) == scoreHere);
 		return { Step { pos, false }, Step { smallestPos, nodeChange } };
 	}
 	for (const uint32_t* nbp = g.inBegin(node); nbp != g.inEnd(node); nbp++)
@@ -955,17 +1063,18 @@ static std::pair<Step, Step> backtraceHorizontal(const Graph& g, const Band& cur
 			if (getValue(ns, (int)offset - 1) == scoreHere - (eq ? 0 : 1)) return { Step { pos, false }, Step { Pos { nb, g.len(nb) - 1u, pos.seqPos - 1 }, true } };
 		}
 	}
-	ORA_ASSERT(scoreHere == getValue(FakeSlice, (int)offset));
+	ORA_ASSERT(scoreHere == getValue(extra, (int)offset));
 	return { Step { pos, false }, Step { pos, false } };
 }
 
 // pickBacktraceVerticalCrossing (Common.h:886-934)
 static std::pair<Step, Step> backtraceVertical(const Graph& g, const Band& current, const Band& previous, const std::vector<WS>& ns, size_t j,
-	uint32_t node, Pos pos, const char* seq, i32 quitScore, bool scoresNotValid, i32 previousQuitScore, bool previousScoresNotValid)
+	uint32_t node, Pos pos, const char* seq, i32 quitScore, bool scoresNotValid, i32 previousQuitScore, bool previousScoresNotValid,
+	const WS& extra)
 {
 	ORA_ASSERT(pos.nodeOffset > 0);
 	while (pos.nodeOffset > 0 && getValue(ns[pos.nodeOffset - 1], 0) == getValue(ns[pos.nodeOffset], 0) - 1) pos.nodeOffset--;
-	if (pos.nodeOffset == 0) return { Step { pos, false }, backtraceCorner(g, current, previous, node, j, seq, quitScore, scoresNotValid, previousQuitScore, previousScoresNotValid) };
+	if (pos.nodeOffset == 0) return { Step { pos, false }, backtraceCorner(g, current, previous, node, j, seq, quitScore, scoresNotValid, previousQuitScore, previousScoresNotValid, extra) };
 	ORA_ASSERT(previous.has(node));
 	bool eq = characterMatch(seq[pos.seqPos], g.charAt((uint32_t)pos.node, (uint32_t)pos.nodeOffset));
 	const Item& previousNode = previous.at(node);
@@ -981,7 +1090,7 @@ static std::pair<Step, Step> backtraceVertical(const Graph& g, const Band& curre
 	scoreUp -= (previousNode.HN >> pos.nodeOffset) & 1;
 	if (previousScoresNotValid || scoresNotValid || scoreHere > quitScore || scoreDiagonal > previousQuitScore || scoreUp > previousQuitScore)
 	{
-		if (scoreHere == getValue(FakeSlice, 0)) return { Step { pos, false }, Step { pos, false } };
+		if (scoreHere == getValue(extra, 0)) return { Step { pos, false }, Step { pos, false } };
 		if (scoreDiagonal < scoreUp) return { Step { pos, false }, Step { Pos { pos.node, pos.nodeOffset - 1, pos.seqPos - 1 }, false } };
 		return { Step { pos, false }, Step { Pos { pos.node, pos.nodeOffset, pos.seqPos - 1 }, false } };
 	}
@@ -989,7 +1098,7 @@ static std::pair<Step, Step> backtraceVertical(const Graph& g, const Band& curre
 	ORA_ASSERT(scoreDiagonal >= scoreHere - (eq ? 0 : 1));
 	if (scoreUp == scoreHere - 1) return { Step { pos, false }, Step { Pos { pos.node, pos.nodeOffset, pos.seqPos - 1 }, false } };
 	if (scoreDiagonal == scoreHere - (eq ? 0 : 1)) return { Step { pos, false }, Step { Pos { pos.node, pos.nodeOffset - 1, pos.seqPos - 1 }, false } };
-	ORA_ASSERT(scoreHere == getValue(FakeSlice, 0));
+	ORA_ASSERT(scoreHere == getValue(extra, 0));
 	return { Step { pos, false }, Step { pos, false } };
 }
 
@@ -1004,8 +1113,38 @@ static void checkCircularity(const Trace& t)   // checkBacktraceCircularity (Com
 	}
 }
 
-// getReverseTraceFromTable (Common.h:571-758), single-seed form (multiseed = false, no seed starts)
-static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, size_t seqLen, const std::vector<Slice>& table, Pos startPos, i32 startScore)
+// getSeedSlice (Common.h:320-353): the column of starting an alignment at each row of the
+// slice at j, scored as the X-score's error cost of the skipped read prefix
+static WS seedSlice(size_t j, size_t seqLen, i32 cost)
+{
+	ORA_ASSERT(j % 64 == 0);
+	WS r { 0, 0, 0 };
+	i32 oldSeedScore = 0;
+	if (j > 0) oldSeedScore = ((i32)(j - 1 + 1) * 100 + cost / 2) / cost;
+	for (size_t offset = 0; offset < 64; offset++)
+	{
+		if (j + offset >= seqLen)
+		{
+			r.VP |= 1ULL << offset;
+			oldSeedScore = oldSeedScore + 1;
+			continue;
+		}
+		i32 seedScore = ((i32)(j + offset + 1) * 100 + cost / 2) / cost;
+		ORA_ASSERT(seedScore == oldSeedScore || seedScore == oldSeedScore + 1);
+		if (seedScore == oldSeedScore + 1) r.VP |= 1ULL << offset;
+		oldSeedScore = seedScore;
+	}
+	r.scoreEnd = oldSeedScore;
+	r.VP &= ~1ULL;
+	r.VN |= 1;
+	return r;
+}
+
+// getReverseTraceFromTable (Common.h:571-758).  multiseed: a node that is a seed start in its
+// slice is recomputed and backtracked with the seed-start slice as extraSlice, and the walk
+// along the row above the read (:721-756) is skipped.
+static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, size_t seqLen, const std::vector<Slice>& table, Pos startPos, i32 startScore,
+	bool multiseed = false)
 {
 	ORA_ASSERT(table.size() > 0);
 	size_t currentSlice = startPos.seqPos / 64 + 1;
@@ -1017,6 +1156,7 @@ static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, si
 	std::vector<WS> nodeSlices;
 	EqV eqv = getEq(seq, seqLen, (size_t)table[currentSlice].j);
 	i32 lastScore = INT32_MAX - 1;
+	WS extra = FakeSlice;
 	auto back = [&]() -> Pos { const auto& b = result.items.back(); return Pos { b.node, b.nodeOffset, b.seqPos }; };
 	auto push = [&](Pos q, bool sw) { result.items.push_back({ q.node, q.nodeOffset, q.seqPos, sw }); };
 	while (result.items.back().seqPos != (size_t)-1)
@@ -1033,7 +1173,9 @@ static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, si
 			ORA_ASSERT(table[currentSlice].scores.has((uint32_t)currentNode));
 			ORA_ASSERT(currentSlice > 0);
 			Item previous = previousOrDefault(table[currentSlice - 1].scores, (uint32_t)currentNode);
-			nodeSlices = recalc(g, p, (uint32_t)currentNode, table[currentSlice].scores.at((uint32_t)currentNode), eqv, previous, (i32)table[currentSlice].j);
+			const Item& here = table[currentSlice].scores.at((uint32_t)currentNode);
+			extra = here.seedStart ? seedSlice((size_t)table[currentSlice].j, seqLen, p.cost) : FakeSlice;
+			nodeSlices = recalc(g, p, (uint32_t)currentNode, here, eqv, previous, (i32)table[currentSlice].j, extra);
 		}
 		const Slice& cs = table[currentSlice];
 		const Slice& ps = table[currentSlice - 1];
@@ -1043,9 +1185,9 @@ static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, si
 		lastScore = getValue(nodeSlices[b.nodeOffset], (int)(b.seqPos % 64));
 		if (b.seqPos % 64 == 0 && b.nodeOffset == 0)
 		{
-			Step bt = backtraceCorner(g, cs.scores, ps.scores, (uint32_t)currentNode, (size_t)cs.j, seq, quit, cs.scoresNotValid, pquit, ps.scoresNotValid);
-			if (bt.pos == b && !bt.nodeSwitch && getValue(nodeSlices[bt.pos.nodeOffset], (int)(bt.pos.seqPos % 64)) == getValue(FakeSlice, (int)(bt.pos.seqPos % 64))) break;
-			if (bt.pos == b && !bt.nodeSwitch && getValue(nodeSlices[bt.pos.nodeOffset], (int)(bt.pos.seqPos % 64)) == scoreBeforeStart(FakeSlice)) break;
+			Step bt = backtraceCorner(g, cs.scores, ps.scores, (uint32_t)currentNode, (size_t)cs.j, seq, quit, cs.scoresNotValid, pquit, ps.scoresNotValid, extra);
+			if (bt.pos == b && !bt.nodeSwitch && getValue(nodeSlices[bt.pos.nodeOffset], (int)(bt.pos.seqPos % 64)) == getValue(extra, (int)(bt.pos.seqPos % 64))) break;
+			if (bt.pos == b && !bt.nodeSwitch && getValue(nodeSlices[bt.pos.nodeOffset], (int)(bt.pos.seqPos % 64)) == scoreBeforeStart(extra)) break;
 			push(bt.pos, bt.nodeSwitch);
 			checkCircularity(result);
 			continue;
@@ -1059,8 +1201,8 @@ static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, si
 				push(Pos { currentNode, 0, b.seqPos }, false);
 				continue;
 			}
-			auto crossing = backtraceVertical(g, cs.scores, ps.scores, nodeSlices, (size_t)cs.j, (uint32_t)currentNode, b, seq, quit, cs.scoresNotValid, pquit, ps.scoresNotValid);
-			if (crossing.second.pos.seqPos == b.seqPos && getValue(nodeSlices[crossing.second.pos.nodeOffset], (int)(crossing.second.pos.seqPos % 64)) == getValue(FakeSlice, (int)(crossing.second.pos.seqPos % 64))) break;
+			auto crossing = backtraceVertical(g, cs.scores, ps.scores, nodeSlices, (size_t)cs.j, (uint32_t)currentNode, b, seq, quit, cs.scoresNotValid, pquit, ps.scoresNotValid, extra);
+			if (crossing.second.pos.seqPos == b.seqPos && getValue(nodeSlices[crossing.second.pos.nodeOffset], (int)(crossing.second.pos.seqPos % 64)) == getValue(extra, (int)(crossing.second.pos.seqPos % 64))) break;
 			ORA_ASSERT(crossing.first.pos.node == b.node);
 			ORA_ASSERT(crossing.first.pos.seqPos == b.seqPos);
 			ORA_ASSERT(crossing.first.pos.nodeOffset <= b.nodeOffset);
@@ -1075,8 +1217,8 @@ static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, si
 		}
 		if (b.nodeOffset == 0)
 		{
-			auto crossing = backtraceHorizontal(g, cs.scores, ps.scores, (size_t)cs.j, (uint32_t)currentNode, b, seq, quit, cs.scoresNotValid, pquit, ps.scoresNotValid);
-			if (crossing.second.pos.node == b.node && !crossing.second.nodeSwitch && getValue(nodeSlices[crossing.second.pos.nodeOffset], (int)(crossing.second.pos.seqPos % 64)) == getValue(FakeSlice, (int)(crossing.second.pos.seqPos % 64))) break;
+			auto crossing = backtraceHorizontal(g, cs.scores, ps.scores, (size_t)cs.j, (uint32_t)currentNode, b, seq, quit, cs.scoresNotValid, pquit, ps.scoresNotValid, extra);
+			if (crossing.second.pos.node == b.node && !crossing.second.nodeSwitch && getValue(nodeSlices[crossing.second.pos.nodeOffset], (int)(crossing.second.pos.seqPos % 64)) == getValue(extra, (int)(crossing.second.pos.seqPos % 64))) break;
 			ORA_ASSERT(crossing.first.pos.node == b.node);
 			ORA_ASSERT(crossing.first.pos.nodeOffset == b.nodeOffset);
 			ORA_ASSERT(crossing.first.pos.seqPos <= b.seqPos);
@@ -1090,14 +1232,15 @@ static Trace traceFromTable(const Graph& g, const Params& p, const char* seq, si
 			checkCircularity(result);
 			continue;
 		}
-		auto inner = backtraceInside(g, (size_t)cs.j, nodeSlices, b, seq);
+		auto inner = backtraceInside(g, (size_t)cs.j, nodeSlices, b, seq, extra);
 		for (const auto& q : inner) push(q, false);
 		Pos nb = back();
-		if (getValue(nodeSlices[nb.nodeOffset], (int)(nb.seqPos % 64)) == getValue(FakeSlice, (int)(nb.seqPos % 64))) break;
+		if (getValue(nodeSlices[nb.nodeOffset], (int)(nb.seqPos % 64)) == getValue(extra, (int)(nb.seqPos % 64))) break;
 	}
 	ORA_ASSERT(result.score >= lastScore);
 	result.score -= lastScore;
 	// walk along the start node's row above the read (Common.h:721-756)
+	if (!multiseed)
 	{
 		Pos b = back();
 		ORA_ASSERT(b.seqPos == (size_t)-1);
@@ -1250,6 +1393,154 @@ static int extendOne(const Graph& g, const Params& p, const char* seq, size_t se
 	return GA_OK;
 }
 
+// GraphAlignerBitvectorBanded::getMultiseedSlices (GraphAlignerBitvectorBanded.h:727-822): every
+// slice of the read from the empty initial slice, the seeds of each slice started in it.
+// seedSlices/seedNodes: the read's seeds in slice order (prepareSeedsForMultiseeding).
+static std::vector<Slice> multiseedFill(const Graph& g, const Params& p, const char* seq, size_t seqLen, const uint32_t* seedSlices,
+	const uint32_t* seedNodes, size_t numSeeds, State& st, uint64_t& columnSteps)
+{
+	const size_t numSlices = (seqLen + 63) / 64;
+	std::vector<Slice> table;
+	table.reserve(numSlices + 1);
+	Slice init;    // getInitialEmptySlice (Common.h:1541-1549)
+	init.j = -64;
+	init.bandwidth = 1;
+	init.minScore = 0;
+	table.push_back(init);
+	size_t lastSeedHit = 0;
+	try
+	{
+		for (size_t s = 0; s < numSlices; s++)
+		{
+			const Slice& lastSlice = table.back();
+			const size_t sliceIndex = (size_t)(lastSlice.j + 64) / 64;
+			size_t nextSeedHit = lastSeedHit;
+			ORA_ASSERT(nextSeedHit == numSeeds || seedSlices[nextSeedHit] >= sliceIndex);
+			while (nextSeedHit < numSeeds && seedSlices[nextSeedHit] == sliceIndex) nextSeedHit++;
+			Slice newSlice;
+			newSlice.j = lastSlice.j + 64;
+			SliceSeeds seeds;
+			seeds.nodes = seedNodes + lastSeedHit;
+			seeds.count = nextSeedHit - lastSeedHit;
+			seeds.slice = seedSlice((size_t)newSlice.j, seqLen, p.cost);
+			seeds.store = true;
+			NodeCalc r = calculateSlice(g, p, seq, seqLen, (size_t)newSlice.j, newSlice.scores, lastSlice.scores, st,
+				add(lastSlice.minScore, (i32)lastSlice.bandwidth), (int)p.bandwidth, lastSlice.minScore, columnSteps, seeds);
+			lastSeedHit = nextSeedHit;
+			newSlice.cellsProcessed = r.cellsProcessed;
+			newSlice.minScoreNode = r.minScoreNode;
+			newSlice.minScoreNodeOffset = r.minScoreNodeOffset;
+			newSlice.minScore = r.minScore;
+			newSlice.maxExactEndposScore = r.maxExactEndposScore;
+			newSlice.maxExactEndposNode = r.maxExactEndposNode;
+			newSlice.bandwidth = p.bandwidth;
+			if (newSlice.cellsProcessed >= p.maxCells) newSlice.scoresNotValid = true;
+			for (auto n : lastSlice.scores.nodes) st.previousBand[n] = 0;
+			table.push_back(std::move(newSlice));
+			if (s == numSlices - 1)
+			{
+				for (auto n : table.back().scores.nodes) st.currentBand[n] = 0;
+			}
+			else
+			{
+				std::swap(st.previousBand, st.currentBand);
+			}
+		}
+		ORA_ASSERT(lastSeedHit == numSeeds);
+	}
+	catch (...)
+	{
+		// leave the per-graph flags clear for the next read
+		for (const auto& sl : table)
+			for (auto n : sl.scores.nodes) st.previousBand[n] = st.currentBand[n] = st.hasSeedStart[n] = 0;
+		throw;
+	}
+	return table;
+}
+
+// GraphAlignerBitvectorCommon::getLocalMaximaTracesFromTable (Common.h:355-494) with
+// sliceConsistency and multiseed: a trace from every node whose best exact-end-position
+// X-score in a slice is a local maximum over the slices above and below and the node's
+// neighbours, in slice order from the last and band order within a slice.
+static std::vector<Trace> localMaximaTraces(const Graph& g, const Params& p, const char* seq, size_t seqLen, const std::vector<Slice>& table)
+{
+	std::vector<Trace> result;
+	ORA_ASSERT(table.size() > 1);
+	ORA_ASSERT(table[0].scores.size() == 0);
+	std::vector<i32> sliceMaxScores(table.size());
+	for (size_t i = 0; i < table.size(); i++) sliceMaxScores[i] = table[i].maxExactEndposScore;
+	auto maxOf = [&](size_t slice, uint32_t node, i32& out) -> bool
+	{
+		if (!table[slice].scores.has(node)) return false;
+		out = table[slice].scores.at(node).nodeMax;
+		return true;
+	};
+	for (size_t currentSlice = table.size() - 1; currentSlice > 0; currentSlice--)
+	{
+		const Slice& cs = table[currentSlice];
+		if (cs.maxExactEndposScore <= 0) continue;
+		for (size_t k = 0; k < cs.scores.size(); k++)
+		{
+			const uint32_t node = cs.scores.nodes[k];
+			const Item& item = cs.scores.items[k];
+			if (!item.exists) continue;
+			const i32 score = item.nodeMax;
+			if (score <= 0) continue;
+			if (score < sliceMaxScores[currentSlice] * p.multimapScoreFraction) continue;
+			i32 other;
+			if (maxOf(currentSlice - 1, node, other) && other > score) continue;
+			if (currentSlice < table.size() - 1 && maxOf(currentSlice + 1, node, other) && other >= score) continue;
+			bool notLocalMaximum = false;
+			for (const uint32_t* nb = g.inBegin(node); nb != g.inEnd(node) && !notLocalMaximum; nb++)
+			{
+				if (maxOf(currentSlice, *nb, other) && other > score) notLocalMaximum = true;
+				else if (maxOf(currentSlice - 1, *nb, other) && other > score) notLocalMaximum = true;
+			}
+			for (const uint32_t* nb = g.outBegin(node); nb != g.outEnd(node) && !notLocalMaximum; nb++)
+			{
+				if (maxOf(currentSlice, *nb, other) && other > score) notLocalMaximum = true;
+				else if (currentSlice < table.size() - 1 && maxOf(currentSlice + 1, *nb, other) && other > score) notLocalMaximum = true;
+			}
+			if (notLocalMaximum) continue;
+			Item previous = previousOrDefault(table[currentSlice - 1].scores, node);
+			const size_t j = (size_t)cs.j;
+			EqV eqv = getEq(seq, seqLen, j);
+			const WS extra = item.seedStart ? seedSlice(j, seqLen, p.cost) : FakeSlice;
+			std::vector<WS> ns = recalc(g, p, node, item, eqv, previous, (i32)j, extra);
+			size_t nodeOffset = SIZE_MAX;
+			size_t bvOffset = SIZE_MAX;
+			int cells = (int)std::min<size_t>(64, seqLen - j);
+			for (size_t i = 0; i < ns.size(); i++)
+			{
+				i32 maxScore = maxXScore(ns[i], (i32)j, p.cost, cells);
+				ORA_ASSERT(maxScore <= score);
+				if (maxScore != score) continue;
+				for (size_t off = 63; off < 64; off--)
+				{
+					if (j + off >= seqLen) continue;
+					i32 scoreHere = getXScore(ns[i], (i32)j, (int)off, p.cost);
+					ORA_ASSERT(scoreHere <= score);
+					if (scoreHere == score && (nodeOffset == SIZE_MAX || off > bvOffset))
+					{
+						nodeOffset = i;
+						bvOffset = off;
+					}
+				}
+			}
+			ORA_ASSERT(nodeOffset != SIZE_MAX && bvOffset != SIZE_MAX);
+			ORA_ASSERT(j + bvOffset < seqLen);
+			i32 startScore = getValue(ns[nodeOffset], (int)bvOffset);
+			result.push_back(traceFromTable(g, p, seq, seqLen, table, Pos { node, nodeOffset, j + bvOffset }, startScore, true));
+			const size_t traceEnd = result.back().items[0].seqPos;
+			const size_t traceStart = result.back().items.back().seqPos;
+			ORA_ASSERT(traceEnd >= traceStart);
+			const size_t startSlice = (size_t)(((double)(traceEnd - traceStart) * 0.05 + (double)traceStart + 64 - 1) / 64 + 1);
+			for (size_t i = startSlice; i < currentSlice; i++) sliceMaxScores[i] = std::max(sliceMaxScores[i], score);
+		}
+	}
+	return result;
+}
+
 }
 
 static inline uint64_t packItem(size_t node, size_t nodeOffset, size_t seqPos, bool sw)
@@ -1302,6 +1593,74 @@ extern "C" int ora_extend_batch(const ga_graph_desc* graph, const ga_extend_para
 				}
 			}
 			results->trace_len[i] = n;
+		}
+	};
+	std::vector<std::thread> pool;
+	for (int t = 1; t < threads; t++) pool.emplace_back(worker);
+	worker();
+	for (auto& t : pool) t.join();
+	return GA_OK;
+}
+
+// The multiseed DP of ga_multiseed_batch (include/graphaligner_gb300.h) on `threads` host threads:
+// multiseedFill + localMaximaTraces per read.
+extern "C" int ora_multiseed_batch(const ga_graph_desc* graph, const ga_extend_params* params, const ga_multiseed_batch_desc* batch,
+	ga_multiseed_results* results, int threads)
+{
+	if (!graph || !params || !batch || !results) return GA_ERR_ARGUMENT;
+	ora::Graph g { graph };
+	ora::Params p { params->bandwidth, params->xdrop, (size_t)params->max_cells_per_slice, params->xscore_error_cost, batch->multimap_score_fraction };
+	if (threads < 1) threads = 1;
+	std::atomic<uint32_t> next { 0 };
+	auto worker = [&]()
+	{
+		ora::State st { graph->num_nodes };
+		while (true)
+		{
+			uint32_t i = next.fetch_add(1);
+			if (i >= batch->num) break;
+			const uint64_t s0 = batch->seed_offset[i], s1 = batch->seed_offset[i + 1];
+			std::vector<ora::Trace> traces;
+			uint64_t steps = 0;
+			int status = GA_OK;
+			try
+			{
+				auto table = ora::multiseedFill(g, p, (const char*)batch->seq + batch->seq_offset[i], batch->seq_len[i], batch->seed_slice + s0,
+					batch->seed_node + s0, (size_t)(s1 - s0), st, steps);
+				traces = ora::localMaximaTraces(g, p, (const char*)batch->seq + batch->seq_offset[i], batch->seq_len[i], table);
+			}
+			catch (const ora::AssertFail&)
+			{
+				status = GA_ASSERT;
+				st = ora::State { graph->num_nodes };
+			}
+			if (results->cell_steps) results->cell_steps[i] = steps;
+			uint32_t nt = 0;
+			uint64_t used = 0;
+			if (status == GA_OK)
+			{
+				uint64_t total = 0;
+				for (const auto& t : traces) total += t.items.size();
+				if (traces.size() > batch->max_traces || total > batch->trace_capacity[i])
+				{
+					status = GA_CAPACITY;
+				}
+				else
+				{
+					uint64_t* dst = results->trace_items + batch->trace_offset[i];
+					for (const auto& t : traces)
+					{
+						const size_t k = (size_t)i * batch->max_traces + nt;
+						results->trace_score[k] = t.score;
+						results->trace_start[k] = used;
+						results->trace_len[k] = (uint32_t)t.items.size();
+						for (const auto& it : t.items) dst[used++] = packItem(it.node, it.nodeOffset, it.seqPos, it.nodeSwitch);
+						nt++;
+					}
+				}
+			}
+			results->status[i] = status;
+			results->num_traces[i] = nt;
 		}
 	};
 	std::vector<std::thread> pool;

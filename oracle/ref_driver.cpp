@@ -13,9 +13,11 @@
 //       request line "bigraphNodeId offset sequence"
 //       (GraphAlignerBitvectorBanded.h:59).  Writes status, score and every
 //       trace item; with "slices" also dumps each DP slice's band.
-//   align <graph.gfa> <reads.fa> <out.gaf> <preset vg|dbg> [bandwidth] [tangle]
+//   align <graph.gfa> <reads.fa> <out.gaf> <preset vg|dbg> [bandwidth] [tangle] [multiseed]
 //       One worker, in-order output: the GAF path of runComponentMappings
-//       (Aligner.cpp:440-592) restated line by line with the reference calls.
+//       (Aligner.cpp:440-592) restated line by line with the reference calls;
+//       "multiseed" takes the --multiseed-DP branch (PrepareMultiseeds,
+//       AlignMultiseed, AddMappingQualities; Aligner.cpp:461-476).
 //   seeds <graph.gfa> <reads.fa> <out.txt> <k> <w> <density> <discardFraction>
 //       MinimizerSeeder::getSeeds + OrderSeeds per read.
 #include <algorithm>
@@ -288,9 +290,10 @@ static Preset makePreset(const std::string& name, int argc, char** argv, int fir
 
 static int runAlign(int argc, char** argv)
 {
-	if (argc < 6) { std::cerr << "align <gfa> <reads.fa> <out.gaf> <preset> [bw] [tangle]" << std::endl; return 1; }
+	if (argc < 6) { std::cerr << "align <gfa> <reads.fa> <out.gaf> <preset> [bw] [tangle] [multiseed]" << std::endl; return 1; }
 	AlignmentGraph graph = loadGraph(argv[2]);
 	Preset p = makePreset(argv[5], argc, argv, 6);
+	const bool multiseed = argc > 8 && std::string(argv[8]) == "multiseed";
 	MinimizerSeeder seeder { graph, p.minimizerLength, p.minimizerWindowSize, 1, 1.0 - p.discard };
 	auto reads = readFasta(argv[3]);
 	std::ofstream out { argv[4] };
@@ -311,8 +314,17 @@ static int runAlign(int argc, char** argv)
 		{
 			std::vector<SeedHit> seeds = seeder.getSeeds(read.second, p.minimizerSeedDensity);
 			if (seeds.size() == 0) continue;
-			OrderSeeds(graph, seeds);
-			alignments = AlignOneWay(graph, read.first, read.second, p.alignmentBandwidth, p.maxCellsPerSlice, true, true, seeds, reusableState, p.clusterMin, p.seedExtendDensity, p.precise, p.Xdrop);
+			if (multiseed)
+			{
+				PrepareMultiseeds(graph, seeds, read.second.size());
+				alignments = AlignMultiseed(graph, read.first, read.second, p.alignmentBandwidth, p.maxCellsPerSlice, true, true, seeds, reusableState, p.clusterMin, p.seedExtendDensity, p.precise, p.Xdrop, p.multimapScoreFraction);
+				AlignmentSelection::AddMappingQualities(alignments.alignments);
+			}
+			else
+			{
+				OrderSeeds(graph, seeds);
+				alignments = AlignOneWay(graph, read.first, read.second, p.alignmentBandwidth, p.maxCellsPerSlice, true, true, seeds, reusableState, p.clusterMin, p.seedExtendDensity, p.precise, p.Xdrop);
+			}
 		}
 		catch (const ThreadReadAssertion::AssertionFailure&)
 		{

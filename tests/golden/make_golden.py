@@ -28,12 +28,16 @@ synthetic inputs and stores what it produced:
   dbg1m_*          a k=63 de Bruijn graph of a 1 Mbp genome (20 copies of a 5 kbp repeat,
                    40 tandem arrays): extensions of 20 kbp reads at 12 % error at tangle
                    effort 10000 (bandwidths 5 and 10), and the GAF of 20 such reads at -x dbg
+  *_ms_b*.gaf.gz   GAF of the --multiseed-DP branch (PrepareMultiseeds, AlignMultiseed,
+                   AddMappingQualities): vg50k reads at bandwidths 10 and 5, dbg100k reads at
+                   -x dbg, and vg50k_chimera_reads.fa.gz (two or three pieces of reads from
+                   different places, some reverse-complemented, joined by random blocks)
 
 The packed item layout is the one include/graphaligner_gb300.h documents, so
 the oracle restatement and the GPU kernels are compared byte for byte.
 
 Usage: [GA_REFERENCE=<GraphAligner checkout>] python tests/golden/make_golden.py [set ...]
-       (sets: base params dbg1m seeds; default: all)
+       (sets: base params dbg1m seeds multiseed; default: all)
 """
 from __future__ import annotations
 
@@ -43,6 +47,7 @@ import os
 import subprocess
 import sys
 import tempfile
+import types
 
 import numpy as np
 
@@ -255,10 +260,64 @@ def dbg1m_sets():
         gz_write(os.path.join(HERE, "dbg1m_b5.gaf.gz"), open(out, "rb").read())
 
 
+def chimeric_reads(g, n: int = 60, seed: int = 21):
+    """Reads made of two or three pieces of vg50k reads (2-8 kbp at 5-20 % error), the later
+    pieces from elsewhere in the graph and every other one reverse-complemented, with a random
+    block of 0-400 bp between pieces: the multiseed DP finds a local maximum per piece."""
+    parts = dg.sample_reads(g, 3 * n, seed, dg.uniform_length(2_000, 8_000), dg.uniform_error(0.05, 0.20))
+    rng = np.random.default_rng(seed + 1)
+    reads = []
+    for i in range(n):
+        pieces = [np.frombuffer(bytes(parts[3 * i].seq), dtype=np.uint8)]
+        for k in range(1, 2 + int(rng.integers(0, 2))):
+            block = dg._BASES[rng.integers(0, 4, int(rng.integers(0, 401)))]
+            piece = np.frombuffer(bytes(parts[3 * i + k].seq), dtype=np.uint8)
+            if k % 2 == 1:
+                piece = dg.revcomp(piece)
+            pieces += [block, piece]
+        reads.append(types.SimpleNamespace(name=f"chimera{i}", seq=np.concatenate(pieces).tobytes()))
+    return reads
+
+
+def multiseed_sets():
+    """GAF of the reference's --multiseed-DP branch (ga_ref align ... multiseed): the vg50k reads
+    at bandwidths 10 and 5, chimeric vg50k reads at bandwidth 10, and the dbg100k reads at -x dbg."""
+    g, reads, _ = vg50k_requests()
+    chim = chimeric_reads(g)
+    with tempfile.TemporaryDirectory() as td:
+        gfa = os.path.join(td, "g.gfa")
+        open(gfa, "w").write(g.to_gfa())
+        fa = os.path.join(td, "reads.fa")
+        open(fa, "w").write(dg.write_fasta(reads))
+        for bw in (10, 5):
+            out = os.path.join(td, f"ms{bw}.gaf")
+            subprocess.run([REF, "align", gfa, fa, out, "vg", str(bw), "-", "multiseed"], check=True)
+            gz_write(os.path.join(HERE, f"vg50k_ms_b{bw}.gaf.gz"), open(out, "rb").read())
+        fa = os.path.join(td, "chim.fa")
+        open(fa, "w").write(dg.write_fasta(chim))
+        gz_write(os.path.join(HERE, "vg50k_chimera_reads.fa.gz"), dg.write_fasta(chim).encode())
+        out = os.path.join(td, "chim.gaf")
+        subprocess.run([REF, "align", gfa, fa, out, "vg", "10", "-", "multiseed"], check=True)
+        gz_write(os.path.join(HERE, "vg50k_chimera_ms_b10.gaf.gz"), open(out, "rb").read())
+    genome = dg.small_dbg_genome(0)
+    d = dg.compact_dbg(genome, 63, with_positions=True)
+    reads = dg.dbg_reads(genome, 30, 20_000, 0.12, 1)
+    with tempfile.TemporaryDirectory() as td:
+        gfa = os.path.join(td, "g.gfa")
+        open(gfa, "w").write(d.gfa)
+        fa = os.path.join(td, "reads.fa")
+        open(fa, "w").write(dg.write_fasta(reads))
+        out = os.path.join(td, "ms.gaf")
+        subprocess.run([REF, "align", gfa, fa, out, "dbg", "-", "-", "multiseed"], check=True)
+        gz_write(os.path.join(HERE, "dbg100k_ms_b5.gaf.gz"), open(out, "rb").read())
+
+
 def main():
     if not os.path.exists(REF):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"], check=True)
-    groups = sys.argv[1:] or ["base", "params", "dbg1m", "seeds"]
+    groups = sys.argv[1:] or ["base", "params", "dbg1m", "seeds", "multiseed"]
+    if "multiseed" in groups:
+        multiseed_sets()
     if "seeds" in groups:
         seed_sets()
     if "params" in groups:

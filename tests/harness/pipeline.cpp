@@ -9,7 +9,7 @@
 //   pipeline <graph.gag> <reads.fa> walk <k> <w> <discard>
 //       the GPU build's per-node minimizer walk (index_walk.cuh) run on the host, grouped
 //       by k-mer, against the host index build
-//   pipeline <graph.gag> <reads.fa> gaf <bandwidth> <maxcells|->
+//   pipeline <graph.gag> <reads.fa> gaf|gafdbg|gafms|gafmsdbg <bandwidth> <maxcells|->
 //   pipeline <graph.gag> <reads.fa> gafreads|gafreadsdbg <bandwidth> <maxcells|-> <threads>
 //       the reference's worker shape (Aligner.cpp:777-785, runComponentMappings :390-606): each
 //       thread takes the next read and runs its seeding and whole seed loop alone, with the
@@ -202,6 +202,54 @@ static void oracleExtend(void* ctx, const std::vector<gahost::ExtensionRequest>&
     }
 }
 
+extern "C" int ora_multiseed_batch(const ga_graph_desc*, const ga_extend_params*, const ga_multiseed_batch_desc*, ga_multiseed_results*, int);
+
+static void oracleMultiseed(void* ctx, const std::vector<gahost::MultiseedRequest>& rq, std::vector<gahost::MultiseedResult>& rs)
+{
+    Ctx* c = (Ctx*)ctx;
+    const size_t n = rq.size();
+    const uint32_t maxTraces = 4096;
+    std::vector<uint8_t> blob;
+    std::vector<uint64_t> off(n), soff(n + 1, 0), toff(n), cap(n), steps(n);
+    std::vector<uint32_t> len(n), sslice, snode, ntr(n);
+    std::vector<int32_t> status(n);
+    uint64_t ti = 0;
+    for (size_t i = 0; i < n; i++)
+    {
+        off[i] = blob.size();
+        blob.insert(blob.end(), rq[i].seq, rq[i].seq + rq[i].len);
+        len[i] = rq[i].len;
+        sslice.insert(sslice.end(), rq[i].slices, rq[i].slices + rq[i].numSeeds);
+        snode.insert(snode.end(), rq[i].nodes, rq[i].nodes + rq[i].numSeeds);
+        soff[i + 1] = sslice.size();
+        cap[i] = (uint64_t)rq[i].len * 64 + 4096;
+        toff[i] = ti;
+        ti += cap[i];
+    }
+    if (blob.empty()) blob.push_back(0);
+    if (sslice.empty()) { sslice.push_back(0); snode.push_back(0); }
+    std::vector<uint64_t> items(ti + 1), tstart(n * maxTraces);
+    std::vector<int32_t> tscore(n * maxTraces);
+    std::vector<uint32_t> tlen(n * maxTraces);
+    ga_multiseed_batch_desc b { (uint32_t)n, blob.data(), off.data(), len.data(), soff.data(), sslice.data(), snode.data(), toff.data(), cap.data(),
+        maxTraces, 0.9 };
+    ga_multiseed_results r { status.data(), ntr.data(), tscore.data(), tstart.data(), tlen.data(), items.data(), steps.data() };
+    ora_multiseed_batch(c->d, &c->p, &b, &r, c->threads);
+    for (size_t i = 0; i < n; i++)
+    {
+        rs[i].status = status[i];
+        rs[i].steps = steps[i];
+        rs[i].scores.clear();
+        rs[i].traces.clear();
+        for (uint32_t t = 0; t < ntr[i]; t++)
+        {
+            const size_t k = i * maxTraces + t;
+            rs[i].scores.push_back(tscore[k]);
+            rs[i].traces.emplace_back(items.begin() + toff[i] + tstart[k], items.begin() + toff[i] + tstart[k] + tlen[k]);
+        }
+    }
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 4) return 1;
@@ -373,10 +421,11 @@ int main(int argc, char** argv)
         return 0;
     }
     // gaf (-x vg, AlignerMain.cpp:170-177), gafdbg (-x dbg, AlignerMain.cpp:160-168), gafmix
-    // (-x vg with reads joining the seed-loop pool a few per round) or gaf2 (-x vg, reads in two
-    // groups whose rounds alternate), with the given bandwidth
+    // (-x vg with reads joining the seed-loop pool a few per round), gaf2 (-x vg, reads in two
+    // groups whose rounds alternate) or gafms / gafmsdbg (--multiseed-DP 1), with the given bandwidth
     const bool perRead = mode == "gafreads" || mode == "gafreadsdbg";
-    const bool dbg = mode == "gafdbg" || mode == "gafreadsdbg";
+    const bool dbg = mode == "gafdbg" || mode == "gafreadsdbg" || mode == "gafmsdbg";
+    const bool multiseed = mode == "gafms" || mode == "gafmsdbg";
     const bool mixed = mode == "gafmix";
     const bool twoLanes = mode == "gaf2";
     const size_t joinPerRound = 7;
@@ -471,6 +520,7 @@ int main(int argc, char** argv)
         Ctx ctx2 = ctx;
         gahost::alignBatchTwoLanes(graph, p, in, oracleExtend, &ctx, &ctx2, out, st);
     }
+    else if (multiseed) gahost::alignBatchMultiseed(graph, p, in, oracleMultiseed, &ctx, oracleExtend, &ctx, out, st);
     else gahost::alignBatch(graph, p, in, oracleExtend, &ctx, out, st);
     for (auto& o : out) std::cout << o.gaf;
     const double alignSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - alignStart).count();

@@ -133,6 +133,26 @@ def test_gaf_matches_reference_dbg(harness, oracle_lib, tmp_path, name):
     assert out == load_gaf(name, 5)
 
 
+MULTISEED_CASES = [("vg50k", "vg50k_reads", "gafms", 10, "vg50k_ms_b10"), ("vg50k", "vg50k_reads", "gafms", 5, "vg50k_ms_b5"),
+                   ("vg50k", "vg50k_chimera_reads", "gafms", 10, "vg50k_chimera_ms_b10"),
+                   ("dbg100k", "dbg100k_reads", "gafmsdbg", 5, "dbg100k_ms_b5")]
+
+
+@pytest.mark.parametrize("graph,reads,mode,bandwidth,gaf", MULTISEED_CASES)
+def test_multiseed_gaf_matches_reference(harness, oracle_lib, tmp_path, graph, reads, mode, bandwidth, gaf):
+    """--multiseed-DP 1: prepareSeedsForMultiseeding, the oracle's multiseed DP (seeds started
+    in their slices, local-maximum traces), duplicate removal, clipping, backward extensions,
+    mapping qualities, selection and GAF, byte for byte against the reference's GAF; the
+    chimeric reads give two or three alignments each."""
+    import gzip
+    exe = harness[0]
+    fa = os.path.join(tmp_path, "reads.fa")
+    open(fa, "wb").write(gzip.open(os.path.join(GOLDEN, f"{reads}.fa.gz")).read())
+    out = subprocess.run([exe, graph_file(graph, str(tmp_path)), fa, mode, str(bandwidth)], check=True, capture_output=True, text=True)
+    assert out.stdout == gzip.open(os.path.join(GOLDEN, f"{gaf}.gaf.gz"), "rt").read()
+    assert " failed 0 " in out.stderr
+
+
 def test_quickstart_gaf(harness, tmp_path):
     exe, _, _, _ = harness
     import gzip
