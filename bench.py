@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serve: seconds of Poisson arrivals per rate")
     ap.add_argument("--serve-min-reads", type=int, default=500, help="serve: reads per rate at least")
     ap.add_argument("--cpu-reads", type=int, default=40, help="read-level: reads of the CPU baseline sample")
+    ap.add_argument("--multiseed", action="store_true", help="read-level: --multiseed-DP 1 (one multiseed DP per read)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="extend: keep the default launch shape")
     ap.add_argument("--truncate", type=int, default=0, help="extend: cut every extension to this many bases (small profiling cases)")
     ap.add_argument("--arena-gb", type=float, default=0, help="extend: DP-table arena size (default: from the batch)")
@@ -326,11 +327,11 @@ def run_reads(args):
     t0 = time.perf_counter()
     dgraph = DeviceGraph(g)
     ext = Extender(dgraph, arena_bytes=arena)
-    aligner = Aligner(ext, g, preset(preset_name))
+    aligner = Aligner(ext, g, preset(preset_name, multiseed=args.multiseed))
     index_s = time.perf_counter() - t0
     line = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "u64",
             "data": "synthetic (seeded generator)", "config": {"workload": READ_WORKLOADS[args.workload], "reads": len(seqs),
-            "read_bp": read_bp, "graph_nodes": g.num_nodes, "preset": preset_name},
+            "read_bp": read_bp, "graph_nodes": g.num_nodes, "preset": preset_name, "multiseed_dp": bool(args.multiseed)},
             "workload_gen_s": gen_s, "graph_upload_and_index_s": index_s}
     if args.workload == "serve":
         with ClockSampler(0) as clocks:
@@ -359,7 +360,7 @@ def run_reads(args):
         line["index"] = {k: v for k, v in aligner.index().items()}
         if not args.no_cpu_baseline:
             line["cpu_baseline"], line["cpu_sample_gaf_identical"], host_index = read_cpu_baseline(g, names, seqs, preset_name, gaf,
-                                                                                                  args.cpu_reads)
+                                                                                                  args.cpu_reads, args.multiseed)
             line["index"]["identical_to_host_build"] = index_checksums(aligner) == host_index.pop("checksums")
             line["index"].update(host_index)
     print(json.dumps(line), flush=True)
@@ -375,7 +376,7 @@ def index_checksums(aligner):
     return [info["max_count"], info["num_keys"], info["num_positions"], s(keys), s(start), s(pos)]
 
 
-def read_cpu_baseline(g, names, seqs, preset_name, gaf, n_sample):
+def read_cpu_baseline(g, names, seqs, preset_name, gaf, n_sample, multiseed=False):
     """The same read-level flow on the host cores in the reference's worker shape
     (Aligner.cpp:777-785): one read per thread, each through its seeding and whole seed loop,
     every core busy (tests/harness/pipeline.cpp, the package's host code with the oracle's
@@ -393,6 +394,9 @@ def read_cpu_baseline(g, names, seqs, preset_name, gaf, n_sample):
     subprocess.run(["g++", "-std=c++17", "-O2", "-o", exe, *srcs, "-lpthread"], check=True)
     cores = os.cpu_count() or 1
     mode = "gafreadsdbg" if preset_name == "dbg" else "gafreads"
+    if multiseed:
+        # the multiseed DPs and backward extensions of the sample on every core
+        mode = "gafmsdbg" if preset_name == "dbg" else "gafms"
     bw = "5" if preset_name == "dbg" else "10"
     n_sample = min(len(seqs), max(n_sample, 4 * cores))
     with tempfile.TemporaryDirectory() as td:
@@ -426,7 +430,11 @@ def read_cpu_baseline(g, names, seqs, preset_name, gaf, n_sample):
     gpu_lines = [ln for ln in gaf.splitlines(keepends=True) if ln.split("\t", 1)[0] in want]
     cpu_lines = out.stdout.splitlines(keepends=True)
     return ({"value": bp / dt, "unit": UNIT, "cores": cores, "kind": "port",
-             "sample": f"{len(idx)} of {len(seqs)} reads (evenly spaced), one read per thread through its whole seed loop on {cores} threads (the reference's worker shape); the package's host read-level code with the oracle restatement's extensions, {dt:.1f} s after the index build"},
+             "sample": f"{len(idx)} of {len(seqs)} reads (evenly spaced), " + (
+                 f"the multiseed DPs and then the backward extensions, reads across {cores} threads; the package's host read-level code with the oracle restatement's multiseed DP and extensions"
+                 if multiseed else
+                 f"one read per thread through its whole seed loop on {cores} threads (the reference's worker shape); the package's host read-level code with the oracle restatement's extensions")
+             + f", {dt:.1f} s after the index build"},
             sorted(gpu_lines) == sorted(cpu_lines), host_index)
 
 

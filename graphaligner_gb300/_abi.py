@@ -79,3 +79,31 @@ class Results(ctypes.Structure):
 
 
 GA_OK, GA_TRACE_FAILED, GA_ASSERT, GA_CAPACITY, GA_BAD_REQUEST = 0, 1, 2, 3, 4
+
+
+class MultiseedBatchDesc(ctypes.Structure):
+    _fields_ = [
+        ("num", ctypes.c_uint32),
+        ("seq", _u8p),
+        ("seq_offset", _u64p),
+        ("seq_len", _u32p),
+        ("seed_offset", _u64p),
+        ("seed_slice", _u32p),
+        ("seed_node", _u32p),
+        ("trace_offset", _u64p),
+        ("trace_capacity", _u64p),
+        ("max_traces", ctypes.c_uint32),
+        ("multimap_score_fraction", ctypes.c_double),
+    ]
+
+
+class MultiseedResults(ctypes.Structure):
+    _fields_ = [
+        ("status", _i32p),
+        ("num_traces", _u32p),
+        ("trace_score", _i32p),
+        ("trace_start", _u64p),
+        ("trace_len", _u32p),
+        ("trace_items", _u64p),
+        ("cell_steps", _u64p),
+    ]

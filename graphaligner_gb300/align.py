@@ -66,6 +66,7 @@ class AlignParams(ctypes.Structure):
         ("cigar_match_mismatch", ctypes.c_uint8),
         ("min_alignment_score", ctypes.c_int32),
         ("multimap_score_fraction", ctypes.c_double),
+        ("multiseed_dp", ctypes.c_uint8),
     ]
 
 
@@ -96,7 +97,7 @@ class IndexInfo(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
-def preset(name: str = "vg", bandwidth: int | None = None, tangle_effort: int | None = None) -> AlignParams:
+def preset(name: str = "vg", bandwidth: int | None = None, tangle_effort: int | None = None, multiseed: bool = False) -> AlignParams:
     """AlignerMain.cpp:119-231 for the two presets (X-drop from the 0.66 clipping cutoff)."""
     from .extend import default_xdrop, xscore_error_cost
     if name == "vg":
@@ -110,7 +111,7 @@ def preset(name: str = "vg", bandwidth: int | None = None, tangle_effort: int | 
     if tangle_effort is not None:
         cells = tangle_effort
     return AlignParams(_abi.ExtendParams(bw, default_xdrop(), cells, xscore_error_cost()), k, w, dens, discard,
-                       ext_dens, 1, 1, 0, 0, 0.9)
+                       ext_dens, 1, 1, 0, 0, 0.9, 1 if multiseed else 0)
 
 
 class Aligner:

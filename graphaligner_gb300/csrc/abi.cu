@@ -106,6 +106,10 @@ struct ga_extender
     DevBuf<uint32_t> seqLen, startNode, startOffset, traceCap, traceLen, order;
     DevBuf<int32_t> status, score, prevStatus;
     DevBuf<gadev::ExtState> states;        // where the fill left each extension's table
+    // multiseed DP staging
+    DevBuf<uint64_t> msSeedOff, msTraceCap, msTraceStart;
+    DevBuf<uint32_t> msSeedSlice, msSeedNode, msNumTraces, msTraceLen;
+    DevBuf<int32_t> msTraceScore;
 };
 
 extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
@@ -117,6 +121,8 @@ extern "C" int ga_graph_upload(const ga_graph_desc* desc, int device, ga_graph_t
 {
     if (!desc || !out) return fail(GA_ERR_ARGUMENT, "null argument");
     if (desc->num_nodes == 0 || desc->first_ambiguous > desc->num_nodes) return fail(GA_ERR_ARGUMENT, "bad node counts");
+    // a band entry keeps two flags above the node index
+    if (desc->num_nodes > gadev::kNodeMask) return fail(GA_ERR_ARGUMENT, "more than 2^30 - 1 split nodes");
     const uint32_t N = desc->num_nodes;
     for (uint32_t i = 0; i < N; i++)
         if (desc->node_length[i] == 0 || desc->node_length[i] > 64) return fail(GA_ERR_ARGUMENT, "node length outside 1..64");
@@ -488,6 +494,170 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
     GA_CUDA(cudaStreamSynchronize(s));
     GA_CUDA(cudaEventElapsedTime(&x->lastH2DMs, x->ev[3], x->ev[4]));
     GA_CUDA(cudaEventElapsedTime(&x->lastD2HMs, x->ev[2], x->ev[5]));
+    return GA_OK;
+}
+
+// ---- multiseed DP ----
+
+extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, const ga_multiseed_batch_desc* b, ga_multiseed_results* r)
+{
+    if (!x || !p || !b || !r) return fail(GA_ERR_ARGUMENT, "null argument");
+    const uint32_t n = b->num;
+    if (n == 0) return GA_OK;
+    if (!b->seq || !b->seq_offset || !b->seq_len || !b->seed_offset || !b->trace_offset || !b->trace_capacity || !r->status || !r->num_traces
+        || !r->trace_score || !r->trace_start || !r->trace_len || !r->trace_items)
+        return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: a required array is NULL");
+    if (b->max_traces == 0) return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: max_traces must be at least 1");
+    int rc = check_lengths(b->seq_len, n);
+    if (rc != GA_OK) return rc;
+    // seeds: in the graph, within their read, in slice order
+    const uint64_t seedBase = b->seed_offset[0];
+    const uint64_t seedEnd = b->seed_offset[n];
+    if (seedEnd > seedBase && (!b->seed_slice || !b->seed_node)) return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: seeds without seed arrays");
+    for (uint32_t i = 0; i < n; i++)
+    {
+        if (b->seed_offset[i + 1] < b->seed_offset[i]) return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: seed_offset decreases at read " + std::to_string(i));
+        const uint32_t slices = (b->seq_len[i] + 63) / 64;
+        for (uint64_t k = b->seed_offset[i]; k < b->seed_offset[i + 1]; k++)
+        {
+            if (b->seed_node[k] >= x->graph->N || b->seed_slice[k] >= slices || (k > b->seed_offset[i] && b->seed_slice[k] < b->seed_slice[k - 1]))
+                return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: read " + std::to_string(i) + " seed " + std::to_string(k - b->seed_offset[i])
+                    + " is outside the graph or the read, or out of slice order");
+        }
+    }
+    GA_CUDA(cudaSetDevice(x->graph->device));
+    uint64_t seqBytes = 0, items = 0;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        seqBytes = std::max<uint64_t>(seqBytes, b->seq_offset[i] + b->seq_len[i]);
+        items = std::max<uint64_t>(items, b->trace_offset[i] + b->trace_capacity[i]);
+    }
+    const uint64_t seeds = seedEnd;     // seed arrays are indexed from 0 as given
+    const uint64_t tables = (uint64_t)n * b->max_traces;
+    std::vector<uint32_t>& order = x->orderHost;
+    order = longest_first(b->seq_len, n);
+    GA_CUDA(x->seq.reserve(std::max<uint64_t>(seqBytes, 1)));
+    GA_CUDA(x->seqOff.reserve(n));
+    GA_CUDA(x->seqLen.reserve(n));
+    GA_CUDA(x->msSeedOff.reserve(n + 1));
+    GA_CUDA(x->msSeedSlice.reserve(std::max<uint64_t>(seeds, 1)));
+    GA_CUDA(x->msSeedNode.reserve(std::max<uint64_t>(seeds, 1)));
+    GA_CUDA(x->traceOff.reserve(n));
+    GA_CUDA(x->msTraceCap.reserve(n));
+    GA_CUDA(x->order.reserve(n));
+    GA_CUDA(x->status.reserve(n));
+    GA_CUDA(x->prevStatus.reserve(n));
+    GA_CUDA(x->msNumTraces.reserve(n));
+    GA_CUDA(x->cellSteps.reserve(n));
+    GA_CUDA(x->msTraceScore.reserve(tables));
+    GA_CUDA(x->msTraceStart.reserve(tables));
+    GA_CUDA(x->msTraceLen.reserve(tables));
+    GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(items, 1)));
+    GA_CUDA(x->states.reserve(n));
+    cudaStream_t s = x->stream;
+    GA_CUDA(cudaMemcpyAsync(x->seq.ptr, b->seq, seqBytes, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->seqOff.ptr, b->seq_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->seqLen.ptr, b->seq_len, n * 4ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->msSeedOff.ptr, b->seed_offset, (n + 1) * 8ULL, cudaMemcpyHostToDevice, s));
+    if (seeds)
+    {
+        GA_CUDA(cudaMemcpyAsync(x->msSeedSlice.ptr, b->seed_slice, seeds * 4, cudaMemcpyHostToDevice, s));
+        GA_CUDA(cudaMemcpyAsync(x->msSeedNode.ptr, b->seed_node, seeds * 4, cudaMemcpyHostToDevice, s));
+    }
+    GA_CUDA(cudaMemcpyAsync(x->traceOff.ptr, b->trace_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->msTraceCap.ptr, b->trace_capacity, n * 8ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
+
+    gadev::FillArgs fa {};
+    fa.g = x->graph->d;
+    fa.bandwidth = p->bandwidth;
+    fa.xdrop = p->xdrop;
+    fa.maxCells = p->max_cells_per_slice;
+    fa.cost = p->xscore_error_cost;
+    fa.num = n;
+    fa.order = x->order.ptr;
+    fa.seq = x->seq.ptr;
+    fa.seqOff = x->seqOff.ptr;
+    fa.seqLen = x->seqLen.ptr;
+    fa.arena = x->arena;
+    fa.arenaBytes = x->arenaBytes;
+    fa.arenaCursor = x->arenaCursor;
+    fa.states = x->states.ptr;
+    fa.seedOff = x->msSeedOff.ptr;
+    fa.seedSlice = x->msSeedSlice.ptr;
+    fa.seedNode = x->msSeedNode.ptr;
+    fa.chunkBytes = (uint64_t)x->shape.chunk_kib << 10;
+    gadev::MultiTraceArgs ta {};
+    ta.g = x->graph->d;
+    ta.cost = p->xscore_error_cost;
+    ta.num = n;
+    ta.order = x->order.ptr;
+    ta.states = x->states.ptr;
+    ta.seq = x->seq.ptr;
+    ta.seqOff = x->seqOff.ptr;
+    ta.seqLen = x->seqLen.ptr;
+    ta.arena = x->arena;
+    ta.traceOffset = x->traceOff.ptr;
+    ta.traceCap = x->msTraceCap.ptr;
+    ta.maxTraces = b->max_traces;
+    ta.multimapScoreFraction = b->multimap_score_fraction;
+    ta.status = x->status.ptr;
+    ta.numTraces = x->msNumTraces.ptr;
+    ta.traceScore = x->msTraceScore.ptr;
+    ta.traceStart = x->msTraceStart.ptr;
+    ta.traceLen = x->msTraceLen.ptr;
+    ta.traceItems = x->traceItems.ptr;
+    ta.cellSteps = x->cellSteps.ptr;
+
+    x->lastFillMs = 0;
+    x->lastLaunches = 0;
+    for (int k = 0; k < 3; k++) x->lastRounds[k] = 0;
+    const int wpb = 4;
+    uint32_t pending = n;
+    // the frontier tables are in the global workspace: the multiseed band holds every seed
+    // start of a slice besides the alignments' own nodes
+    for (int layout = 1; layout < 3; layout++)
+    {
+        const gadev::Caps caps = layout_caps(layout);
+        const uint64_t stride = ga_multiseed_tables_bytes(caps);
+        const uint64_t pendingBlocks = std::max<uint64_t>(1, ((uint64_t)pending + wpb - 1) / wpb);
+        uint64_t fillBlocks = std::min<uint64_t>((uint64_t)x->sms * 4, pendingBlocks);
+        fillBlocks = std::max<uint64_t>(1, std::min<uint64_t>(fillBlocks, x->workspaceBytes / stride / wpb));
+        const uint64_t traceBlocks = std::min<uint64_t>((uint64_t)x->sms * 6, pendingBlocks);
+        if (layout > 1) GA_CUDA(cudaMemcpyAsync(x->prevStatus.ptr, x->status.ptr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        fa.caps = caps;
+        fa.workspace = x->workspace;
+        fa.workspaceStride = stride;
+        fa.prevStatus = layout > 1 ? x->prevStatus.ptr : nullptr;
+        ta.prevStatus = fa.prevStatus;
+        GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), s));
+        GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, 2 * sizeof(unsigned long long), s));
+        GA_CUDA(cudaEventRecord(x->ev[0], s));
+        if (ga_launch_multiseed(fa, ta, x->counters, (int)fillBlocks, (int)traceBlocks, wpb, s) != 0)
+            return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+        x->lastLaunches += 2;
+        x->lastRounds[layout] = pending;
+        GA_CUDA(cudaEventRecord(x->ev[1], s));
+        count_status_kernel<<<64, 256, 0, s>>>(x->status.ptr, n, GA_CAPACITY, x->counters + 2);
+        GA_CUDA(cudaGetLastError());
+        x->lastLaunches += 1;
+        uint32_t capFails = 0;
+        GA_CUDA(cudaMemcpyAsync(&capFails, x->counters + 2, 4, cudaMemcpyDeviceToHost, s));
+        GA_CUDA(cudaStreamSynchronize(s));
+        float ms = 0;
+        GA_CUDA(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
+        x->lastFillMs += ms;
+        pending = capFails;
+        if (capFails == 0) break;
+    }
+    GA_CUDA(cudaMemcpyAsync(r->status, x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaMemcpyAsync(r->num_traces, x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaMemcpyAsync(r->trace_score, x->msTraceScore.ptr, tables * 4, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaMemcpyAsync(r->trace_start, x->msTraceStart.ptr, tables * 8, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaMemcpyAsync(r->trace_len, x->msTraceLen.ptr, tables * 4, cudaMemcpyDeviceToHost, s));
+    if (items) GA_CUDA(cudaMemcpyAsync(r->trace_items, x->traceItems.ptr, items * 8, cudaMemcpyDeviceToHost, s));
+    if (r->cell_steps) GA_CUDA(cudaMemcpyAsync(r->cell_steps, x->cellSteps.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaStreamSynchronize(s));
     return GA_OK;
 }
 

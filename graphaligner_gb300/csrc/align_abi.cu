@@ -74,6 +74,71 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
     }
 }
 
+// The multiseed DP of a group of reads through ga_multiseed_batch; reads whose traces
+// outgrow their room run again with eight times as much, once.
+void ga_aligner_multiseed(void* ctx, const std::vector<gahost::MultiseedRequest>& rq, std::vector<gahost::MultiseedResult>& rs)
+{
+    MultiseedLane* m = (MultiseedLane*)ctx;
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<size_t> todo(rq.size());
+    for (size_t i = 0; i < rq.size(); i++) todo[i] = i;
+    uint64_t perBp = 16;
+    uint32_t maxTraces = 64;
+    for (int attempt = 0; attempt < 2 && !todo.empty(); attempt++, perBp *= 8, maxTraces *= 8)
+    {
+        const size_t n = todo.size();
+        m->off.assign(n, 0); m->len.assign(n, 0); m->seedOff.assign(n + 1, 0); m->toff.assign(n, 0); m->cap.assign(n, 0);
+        m->slices.clear(); m->nodes.clear(); m->blob.clear();
+        uint64_t items = 0;
+        for (size_t k = 0; k < n; k++)
+        {
+            const auto& q = rq[todo[k]];
+            m->off[k] = m->blob.size();
+            m->blob.insert(m->blob.end(), q.seq, q.seq + q.len);
+            m->len[k] = q.len;
+            m->slices.insert(m->slices.end(), q.slices, q.slices + q.numSeeds);
+            m->nodes.insert(m->nodes.end(), q.nodes, q.nodes + q.numSeeds);
+            m->seedOff[k + 1] = m->slices.size();
+            m->cap[k] = (uint64_t)q.len * perBp + 4096;
+            m->toff[k] = items;
+            items += m->cap[k];
+        }
+        if (m->blob.empty()) m->blob.push_back(0);
+        m->status.assign(n, 0); m->ntr.assign(n, 0); m->steps.assign(n, 0);
+        m->tscore.assign(n * maxTraces, 0); m->tstart.assign(n * maxTraces, 0); m->tlen.assign(n * maxTraces, 0);
+        m->items.resize(std::max<uint64_t>(items, 1));
+        ga_multiseed_batch_desc b { (uint32_t)n, m->blob.data(), m->off.data(), m->len.data(), m->seedOff.data(),
+            m->slices.empty() ? nullptr : m->slices.data(), m->nodes.empty() ? nullptr : m->nodes.data(), m->toff.data(), m->cap.data(),
+            maxTraces, m->multimapScoreFraction };
+        ga_multiseed_results r { m->status.data(), m->ntr.data(), m->tscore.data(), m->tstart.data(), m->tlen.data(), m->items.data(), m->steps.data() };
+        const int rc = ga_multiseed_batch(m->ext, m->params, &b, &r);
+        std::vector<size_t> again;
+        for (size_t k = 0; k < n; k++)
+        {
+            gahost::MultiseedResult& out = rs[todo[k]];
+            out.status = rc == GA_OK ? m->status[k] : GA_CAPACITY;
+            out.steps = m->steps[k];
+            out.scores.clear();
+            out.traces.clear();
+            if (out.status == GA_CAPACITY && attempt == 0 && rc == GA_OK)
+            {
+                again.push_back(todo[k]);
+                continue;
+            }
+            if (out.status != GA_OK) continue;
+            for (uint32_t t = 0; t < m->ntr[k]; t++)
+            {
+                const size_t slot = k * maxTraces + t;
+                const uint64_t* first = m->items.data() + m->toff[k] + m->tstart[slot];
+                out.scores.push_back(m->tscore[slot]);
+                out.traces.emplace_back(first, first + m->tlen[slot]);
+            }
+        }
+        todo.swap(again);
+    }
+    m->ms += ms_since(t0);
+}
+
 int ga_aligner_second_lane(ga_aligner* a)
 {
     ExtendLane& l = a->lanes[1];
@@ -265,11 +330,19 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     for (auto& l : a->lanes) { l.extendMs = 0; l.stagingMs = 0; }
     // two groups of reads on two extenders, the host finishing one group's round while
     // the other's runs on the GPU; small batches use one
-    if (n >= kTwoLaneMinReads && ga_aligner_second_lane(a) == GA_OK)
+    a->multiseed.ms = 0;
+    if (a->params.multiseed_dp)
+    {
+        a->multiseed.ext = a->ext;
+        a->multiseed.params = &a->params.extend;
+        a->multiseed.multimapScoreFraction = a->params.multimap_score_fraction;
+        gahost::alignBatchMultiseed(*a->graph, rp, reads, ga_aligner_multiseed, &a->multiseed, ga_aligner_extend, &a->lanes[0], outs, bs);
+    }
+    else if (n >= kTwoLaneMinReads && ga_aligner_second_lane(a) == GA_OK)
         gahost::alignBatchTwoLanes(*a->graph, rp, reads, ga_aligner_extend, &a->lanes[0], &a->lanes[1], outs, bs);
     else
         gahost::alignBatch(*a->graph, rp, reads, ga_aligner_extend, &a->lanes[0], outs, bs);
-    a->stats.extend_ms = a->lanes[0].extendMs + a->lanes[1].extendMs;
+    a->stats.extend_ms = a->lanes[0].extendMs + a->lanes[1].extendMs + a->multiseed.ms;
     size_t gafBytes = 0;
     for (uint32_t i = 0; i < n; i++) gafBytes += outs[i].gaf.size();
     a->gaf.reserve(gafBytes);

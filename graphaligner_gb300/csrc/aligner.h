@@ -74,6 +74,19 @@ struct ExtendLane
     }
 };
 
+// host staging of ga_multiseed_batch calls
+struct MultiseedLane
+{
+    ga_extender_t ext = nullptr;
+    const ga_extend_params* params = nullptr;
+    double multimapScoreFraction = 0.9;
+    std::vector<uint8_t> blob;
+    std::vector<uint64_t> off, seedOff, toff, cap, tstart, items, steps;
+    std::vector<uint32_t> len, slices, nodes, ntr, tlen;
+    std::vector<int32_t> status, tscore;
+    double ms = 0;
+};
+
 struct ga_aligner
 {
     ga_extender_t ext = nullptr;
@@ -89,6 +102,7 @@ struct ga_aligner
     ga_align_stats stats {};
     cudaStream_t stream = nullptr;
     ExtendLane lanes[2];       // lanes[0] uses ext; lanes[1] an extender made like it on first use
+    MultiseedLane multiseed;   // the multiseed DP's calls (on ext)
     // k-mer lookup buffers
     DevGrow<uint8_t> dSeq;
     DevGrow<uint64_t> dOff, dMatchOff;

@@ -97,13 +97,14 @@ struct WSpace
     u64* eqcol;         // [64] match mask of each column of the current node
     u64* ring;          // [64] trace items not yet written out
     struct SliceSlot* slots;   // [2] the traceback's cached slices (odd and even)
+    i32* nodeMax;       // multiseed DP: [band] each band node's best exact-end-position X-score
 };
 
 __host__ __device__ inline u64 align16(u64 x) { return (x + 15) & ~15ULL; }
 
-__host__ __device__ inline u64 wspace_bytes(const Caps& c)
+__host__ __device__ inline u64 wspace_bytes(const Caps& c, bool multi = false)
 {
-    u64 b = 0;
+    u64 b = multi ? align16((u64)c.band * 4) : 0;
     b += 2 * align16((u64)c.band * sizeof(Item));
     b += 2 * align16((u64)c.hash * 8);
     b += 2 * align16((u64)c.hash * sizeof(NodeVal));
@@ -127,7 +128,9 @@ __device__ __forceinline__ WSpace wspace_at(uint8_t* base, const Caps& c)
     w.extras = (Extra*)(base + off); off += align16((u64)c.extras * sizeof(Extra));
     w.cols = (Col*)(base + off); off += 64 * sizeof(Col);
     w.eqcol = (u64*)(base + off); off += 64 * 8;
-    w.ring = (u64*)(base + off);
+    w.ring = (u64*)(base + off); off += 64 * 8;
+    w.nodeMax = (i32*)(base + off);    // inside the stride only when it was sized for the multiseed DP
+    w.slots = nullptr;
     return w;
 }
 
@@ -410,16 +413,60 @@ __device__ __noinline__ bool fix_horizontal(i32 scoreBefore, i32 scoreComparison
     return true;
 }
 
-// calculateNodeInner (Common.h:1113-1478) with the single-seed fake extra slice.
+// The same when the node is a seed start of the multiseed DP (Common.h:1314-1362): the row
+// above follows the lower of the previous slice's last row and the seed start's score
+// before the slice, and every column of the first row takes its delta from that.
+__device__ __noinline__ bool fix_horizontal_extra(i32 scoreBefore, i32 scoreComparison, i32 extraBefore, u32 nodeLength, u64& fixedHP,
+    u64& fixedHN, u64& forceMask)
+{
+    scoreBefore = imin(scoreBefore, extraBefore);
+    if (scoreBefore < scoreComparison) forceMask |= 1;
+    i32 adjust = imin(scoreBefore, scoreComparison);
+    #pragma unroll 1
+    for (u32 off = 1; off < 64 && off < nodeLength; off++)
+    {
+        const i32 next = scoreComparison + (i32)((fixedHP >> off) & 1) - (i32)((fixedHN >> off) & 1);
+        if (scoreBefore < extraBefore) scoreBefore += 1;
+        const u64 mask = 1ULL << off;
+        if (scoreBefore < next) forceMask |= mask;
+        const i32 na = imin(next, scoreBefore);
+        if (na < adjust - 1 || na > adjust + 1) return false;
+        if (na == adjust - 1)
+        {
+            fixedHN |= mask;
+            fixedHP &= ~mask;
+        }
+        else if (na == adjust)
+        {
+            fixedHP &= ~mask;
+            fixedHN &= ~mask;
+        }
+        else
+        {
+            fixedHP |= mask;
+            fixedHN &= ~mask;
+        }
+        adjust = na;
+        scoreComparison = next;
+    }
+    return true;
+}
+
+// calculateNodeInner (Common.h:1113-1478).  Multi = false: the single-seed path, whose extra
+// slice is always the fake one.  Multi = true: the multiseed DP, where `extra` (non-null for
+// a node that is a seed start in this slice) is merged into every column and an incoming
+// column that starts a seed forces the computation (EdgeWithPriority::forceCalculation).
 // Fill = true: the slice fill (early leave allowed, calculateNodeClipPrecise).
 // Fill = false: recalcNodeWordslice (no early leave); columns 0..lastColumn land in cols.
 // The column loop runs the Myers recurrence warp-uniformly and records every column; the
 // per-column minimum, X-score and horizontal output bits are then taken across the lanes.
-template <bool Fill>
+template <bool Fill, bool Multi = false>
 __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i, Item& slice, const EqV4& eqv, const PrevInfo& prev,
     const Extra* pool, uint16_t head, const WS* singleIncoming, bool singleInPrevBand, i32 seqOffset, Col* cols, u64* eqcol,
-    u64& steps, int& err, u32 lane, i32 sliceMaxX = kIntMin, u32 lastColumn = 63)
+    u64& steps, int& err, u32 lane, i32 sliceMaxX = kIntMin, u32 lastColumn = 63, const WS* extra = nullptr)
 {
+    const bool hasExtra = Multi && extra != nullptr;
+    bool forceCalculation = false;
     const bool boundOk = seqOffset < kXBoundOffsetLimit;
     NodeCalc result;
     result.minScore = kIntMax;
@@ -472,7 +519,8 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
             const Extra& inc = pool[e];
             WS incWs = ws_make(inc.VP, inc.VN, inc.end);
             result.cells++;
-            if (inc.skip)
+            if (Multi && (inc.skip & 2)) forceCalculation = true;
+            if (inc.skip & 1)
             {
                 ws = hasWs ? merge_w(ws, incWs, lane) : incWs;
                 hasWs = true;
@@ -480,6 +528,7 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
             }
             hasSkipless = true;
             i32 compareHin = prev.exists ? prev.sEnd : kIntMax;
+            if (hasExtra) compareHin = imin(compareHin, ws_before(*extra));
             i32 incBefore = ws_before(incWs);
             u64 hinP = 0, hinN = 0;
             if (compareHin < incBefore) hinN = 1;
@@ -504,11 +553,14 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
     result.minScoreNode = i;
     result.minScoreOffset = 0;
     result.maxXNode = i;
+    // the seed start's column joins after the first minimum and before the first X-score
+    if (hasExtra) ws = merge_w(ws, *extra, lane);
+    const WS wsX = ws;
     // (the recomputation starts from the stored first column, whose merge with itself changes nothing)
-    if (Fill && (slice.node & kExists) != 0 && merge_existing(ws, slice, hasSkipless, inDeg == 1 && singleInPrevBand, lane))
+    if (Fill && !forceCalculation && (slice.node & kExists) != 0 && merge_existing(ws, slice, hasSkipless, inDeg == 1 && singleInPrevBand, lane))
     {
-        if (!boundOk || xscore_bound(ws0, seqOffset, cost) > (int64_t)sliceMaxX)
-            result.maxX = ws_max_xscore(ws0, seqOffset, cost, 64, kAllOnes);
+        if (!boundOk || xscore_bound(wsX, seqOffset, cost) > (int64_t)sliceMaxX)
+            result.maxX = ws_max_xscore(wsX, seqOffset, cost, 64, kAllOnes);
         return result;
     }
     if (prev.exists && ws_before(ws) > prev.sEnd) ws = merge_w(ws, ws_source(prev.sEnd), lane);
@@ -520,7 +572,15 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
         i32 scoreBefore = ws_before(ws);
         i32 scoreComparison = prev.sEnd;
         if (scoreBefore > scoreComparison) { err = GA_ASSERT; return result; }
-        if (scoreBefore < scoreComparison && !fix_horizontal(scoreBefore, scoreComparison, fixedHP, fixedHN, forceMask))
+        if (hasExtra)
+        {
+            if (!fix_horizontal_extra(scoreBefore, scoreComparison, ws_before(*extra), nodeLength, fixedHP, fixedHN, forceMask))
+            {
+                err = GA_ASSERT;
+                return result;
+            }
+        }
+        else if (scoreBefore < scoreComparison && !fix_horizontal(scoreBefore, scoreComparison, fixedHP, fixedHN, forceMask))
         {
             err = GA_ASSERT;
             return result;
@@ -533,7 +593,7 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
     slice.sVP = ws.VP;
     slice.sVN = ws.VN;
     slice.sEnd = ws.end;
-    slice.node = i | kExists;
+    slice.node = i | kExists | (slice.node & kSeedStart);
     {
         // Fill: column 0 as it enters the node, its X-score over every row; the traceback's
         // recomputation: column 0 after the merges
@@ -563,13 +623,26 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
         hp >>= 1;
         hn >>= 1;
         fm >>= 1;
+        // the multiseed DP keeps both bottom-row deltas in phTop (bit 0 +1, bit 1 -1): with a
+        // seed start they come from the merged column's last-row score
+        u32 top = (u32)(Ph >> 63);
+        if (Multi)
+        {
+            if (hasExtra)
+            {
+                const WS m = merge_w(nw, *extra, lane);
+                top = (m.end == ws.end + 1 ? 1u : 0u) | (m.end == ws.end - 1 ? 2u : 0u);
+                nw = m;
+            }
+            else top |= (u32)(Mh >> 63) << 1;
+        }
         ws = nw;
         Col c;
         c.VP = ws.VP;
         c.VN = ws.VN;
         c.Mh = Mh;
         c.end = ws.end;
-        c.phTop = (u32)(Ph >> 63);
+        c.phTop = top;
         cols[pos] = c;
     }
     steps += columns - 1;
@@ -591,15 +664,18 @@ __device__ __forceinline__ NodeCalc node_calc(const DevGraph& g, i32 cost, u32 i
             if (pos < columns)
             {
                 const Col c = cols[pos];
-                const WS cw = ws_make(c.VP, c.VN, c.end);
+                // column 0's X-score is taken after the seed start's column joins it
+                const WS cw = (Multi && pos == 0) ? wsX : ws_make(c.VP, c.VN, c.end);
                 const u32 key = (u32)c.end ^ 0x80000000u;   // signed order as unsigned
                 if (h == 0) loKey = key; else hiKey = key;
                 if (!boundOk || xscore_bound(cw, seqOffset, cost) > (int64_t)sliceMaxX)
                     lmax = imax(lmax, ws_max_xscore(cw, seqOffset, cost, 64, c.Mh));
                 if (pos >= 1)
                 {
-                    if (h == 0) { hpLo = c.phTop; hnLo = (u32)(c.Mh >> 63); }
-                    else { hpHi = c.phTop; hnHi = (u32)(c.Mh >> 63); }
+                    const u32 tp = Multi ? (c.phTop & 1) : c.phTop;
+                    const u32 tn = Multi ? ((c.phTop >> 1) & 1) : (u32)(c.Mh >> 63);
+                    if (h == 0) { hpLo = tp; hnLo = tn; }
+                    else { hpHi = tp; hnHi = tn; }
                 }
             }
         }
@@ -653,13 +729,15 @@ __device__ __forceinline__ bool arena_alloc(const FillArgs& a, ArenaCursor& c, u
 
 __device__ __forceinline__ u64 rec_ids_bytes(u32 count) { return align16((u64)count * 4); }
 
-// write one slice (record, node ids, band in first-pop order) into the arena, lanes copying
+// write one slice (record, node ids, band in first-pop order and, for the multiseed DP, each
+// node's best X-score) into the arena, lanes copying
 __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 index, const Item* band, u32 count,
-    i32 minScore, i32 quit, i32 maxX, u32 maxXNode, bool notValid, u32 lane)
+    i32 minScore, i32 quit, i32 maxX, u32 maxXNode, bool notValid, u32 lane, const i32* nodeMax = nullptr)
 {
     const u64 idBytes = rec_ids_bytes(count);
     u64 off;
-    if (!arena_alloc(a, c, sizeof(SliceRec) + idBytes + (u64)count * sizeof(Item), off, lane)) return false;
+    const u64 maxBytes = nodeMax ? rec_ids_bytes(count) : 0;
+    if (!arena_alloc(a, c, sizeof(SliceRec) + idBytes + (u64)count * sizeof(Item) + maxBytes, off, lane)) return false;
     uint8_t* base = a.arena + off;
     if (lane == 0)
     {
@@ -682,7 +760,19 @@ __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 in
     const uint4* src = (const uint4*)band;
     #pragma unroll 1
     for (u32 k = lane; k < count * 4; k += 32) dst[k] = src[k];
+    if (nodeMax)
+    {
+        i32* m = (i32*)(base + sizeof(SliceRec) + idBytes + (u64)count * sizeof(Item));
+        #pragma unroll 1
+        for (u32 k = lane; k < count; k += 32) m[k] = nodeMax[k];
+    }
     return true;
+}
+
+// the multiseed DP's per-node best X-scores of a committed slice
+__device__ __forceinline__ const i32* rec_node_max(const SliceRec* r)
+{
+    return (const i32*)((const uint8_t*)r + sizeof(SliceRec) + rec_ids_bytes(r->count) + (u64)r->count * sizeof(Item));
 }
 
 // ---------------------------------------------------------------- fill
@@ -696,10 +786,57 @@ struct SliceResult
     u64 cells;
 };
 
-// calculateSlice (GraphAlignerBitvectorBanded.h:255-511), component-queue branch, no seed hits.
-__device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u32 curGen, u32 prevGen, u32& curCount, u32 prevCount,
-    const uint8_t* seq, u32 seqLen, int64_t j, i32 prevQuit, i32 prevMin, u64& steps, int& err, u32 lane)
+// getSeedSlice (Common.h:320-353): the column of starting an alignment at each row of the slice
+// at j, each row scored as the X-score's error cost of the read before it (rows past the read's
+// end one more each)
+__device__ __noinline__ WS seed_ws(int64_t j, u32 seqLen, i32 cost)
 {
+    u64 vp = 0;
+    i32 old = j > 0 ? (i32)((j * 100 + cost / 2) / cost) : 0;
+    #pragma unroll 1
+    for (u32 off = 0; off < 64; off++)
+    {
+        if (j + off >= (int64_t)seqLen)
+        {
+            vp |= 1ULL << off;
+            old += 1;
+            continue;
+        }
+        const i32 score = (i32)(((j + off + 1) * 100 + cost / 2) / cost);
+        if (score == old + 1) vp |= 1ULL << off;
+        old = score;
+    }
+    return ws_make(vp & ~1ULL, 1, old);
+}
+
+// The seeds the multiseed DP starts in one slice, with the slice's seed-start column.
+struct SliceSeeds
+{
+    const u32* nodes;
+    u32 count;
+    WS ws;
+};
+
+// calculateSlice (GraphAlignerBitvectorBanded.h:255-511), component-queue branch.  Multi:
+// the multiseed DP's slice, whose seeds enter the band first (addSeedHitToScoresAndQueue,
+// :228-253) and whose nodes keep their best exact-end-position X-score in w.nodeMax.
+template <bool Multi = false>
+__device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u32 curGen, u32 prevGen, u32& curCount, u32 prevCount,
+    const uint8_t* seq, u32 seqLen, int64_t j, i32 prevQuit, i32 prevMin, u64& steps, int& err, u32 lane, const SliceSeeds* seeds = nullptr)
+{
+    if (Multi)
+    {
+        if (prevMin == kIntMax - (i32)a.bandwidth - 1)
+        {
+            prevMin = ws_before(seeds->ws);
+            prevQuit = wadd(prevMin, (i32)a.bandwidth);
+        }
+        if (prevMin > seeds->ws.end)
+        {
+            prevMin = seeds->ws.end;
+            prevQuit = wadd(seeds->ws.end, (i32)a.bandwidth);
+        }
+    }
     const DevGraph& g = a.g;
     const int bw = (int)a.bandwidth;
     const int prv = cur ^ 1;
@@ -730,7 +867,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
         return s < 0 ? -1 : (int)prevVal[s].band;
     };
 
-    auto insert = [&](u32 target, i32 score, u64 vp, u64 vn, i32 end, bool skip) -> bool
+    auto insert = [&](u32 target, i32 score, u64 vp, u64 vn, i32 end, bool skip, bool force) -> bool
     {
         const int slot = tbl_get_or_add(curKey, curVal, hcap, curGen, target, used, lane);
         if (slot < 0) return false;
@@ -747,7 +884,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
         if (poolN >= a.caps.extras) return false;
         uint16_t e = (uint16_t)poolN++;
         Extra x;
-        x.VP = vp; x.VN = vn; x.end = end; x.next = kNil; x.skip = skip ? 1 : 0;
+        x.VP = vp; x.VN = vn; x.end = end; x.next = kNil; x.skip = (skip ? 1 : 0) | (force ? 2 : 0);
         w.extras[e] = x;
         if (s.head == kNil) s.head = e;
         else w.extras[s.tail].next = e;
@@ -778,9 +915,34 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
             }
         }
         WS src = ws_source(it.sEnd);
-        if (!insert(node, it.minScore, src.VP, src.VN, src.end, true)) { err = GA_CAPACITY; return res; }
+        if (!insert(node, it.minScore, src.VP, src.VN, src.end, true, false)) { err = GA_CAPACITY; return res; }
     }
-    if (heapN == 0) { err = GA_ASSERT; return res; }
+    if (!Multi && heapN == 0) { err = GA_ASSERT; return res; }
+    if (Multi && ws_before(seeds->ws) < wadd(prevQuit, 64))
+    {
+        // the seed starts: in the band before any node of the queue, computed first among equals
+        #pragma unroll 1
+        for (u32 k = 0; k < seeds->count; k++)
+        {
+            const u32 node = seeds->nodes[k];
+            const int slot = tbl_get_or_add(curKey, curVal, hcap, curGen, node, used, lane);
+            if (slot < 0) { err = GA_CAPACITY; return res; }
+            NodeVal& sv = curVal[slot];
+            if (sv.band >= 0) { err = GA_ASSERT; return res; }
+            if (curCount >= a.caps.band || curCount >= 32767) { err = GA_CAPACITY; return res; }
+            sv.band = (int16_t)curCount;
+            Item ni;
+            ni.sVP = seeds->ws.VP; ni.sVN = seeds->ws.VN; ni.sEnd = seeds->ws.end;
+            ni.eVP = seeds->ws.VP; ni.eVN = seeds->ws.VN; ni.eEnd = seeds->ws.end;
+            ni.HP = 0; ni.HN = 0;
+            ni.minScore = seeds->ws.end;
+            ni.node = node | kExists | kSeedStart;
+            curBand[curCount] = ni;
+            w.nodeMax[curCount] = 0;
+            curCount++;
+            if (!insert(node, ws_value(seeds->ws, 0), seeds->ws.VP, seeds->ws.VN, seeds->ws.end, true, true)) { err = GA_CAPACITY; return res; }
+        }
+    }
     i32 curMin = res.minScore;
     const i32 seqOffset = (i32)j;
     #pragma unroll 1
@@ -800,10 +962,13 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
             ni.HP = 0; ni.HN = 0;
             ni.minScore = kIntMax;
             ni.node = i;
+            if (Multi) w.nodeMax[curCount] = 0;
             curBand[curCount++] = ni;
         }
         Item& thisNode = curBand[s.band];
         WS oldEnd = (thisNode.node & kExists) ? ws_make(thisNode.eVP, thisNode.eVN, thisNode.eEnd) : ws_make(0, 0, kIntMax);
+        const WS* extra = (Multi && (thisNode.node & kSeedStart)) ? &seeds->ws : nullptr;
+        if (Multi && extra) oldEnd = merge_w(oldEnd, *extra, lane);
         PrevInfo prev;
         const int pb = prevBandOf(i);
         if (pb >= 0)
@@ -823,9 +988,13 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
         }
         bool singleInPrev = false;
         if (g.inOff[i + 1] - g.inOff[i] == 1) singleInPrev = prevBandOf(g.inNb[g.inOff[i]]) >= 0;
-        NodeCalc nc = node_calc<true>(g, a.cost, i, thisNode, eqv, prev, w.extras, s.head, nullptr, singleInPrev, seqOffset,
-            w.cols, w.eqcol, steps, err, lane, res.maxX);
+        // a column whose X-score bound is at most both the slice's and the node's best so far
+        // changes neither, so the node computation may skip its exact X-score
+        const i32 skipBelow = Multi ? imin(res.maxX, w.nodeMax[s.band]) : res.maxX;
+        NodeCalc nc = node_calc<true, Multi>(g, a.cost, i, thisNode, eqv, prev, w.extras, s.head, nullptr, singleInPrev, seqOffset,
+            w.cols, w.eqcol, steps, err, lane, skipBelow, 63, extra);
         if (err) return res;
+        if (Multi) w.nodeMax[s.band] = imax(nc.maxX, w.nodeMax[s.band]);
         heap_pop(w.heap, heapN);
         s.active = 0;
         s.head = kNil;
@@ -843,7 +1012,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
                 #pragma unroll 1
                 for (u32 e = g.outOff[i]; e < g.outOff[i + 1]; e++)
                 {
-                    if (!insert(g.outNb[e], newEndMin, newEnd.VP, newEnd.VN, newEnd.end, false)) { err = GA_CAPACITY; return res; }
+                    if (!insert(g.outNb[e], newEndMin, newEnd.VP, newEnd.VN, newEnd.end, false, false)) { err = GA_CAPACITY; return res; }
                 }
             }
         }
@@ -861,7 +1030,7 @@ __device__ SliceResult fill_slice(const FillArgs& a, const WSpace& w, int cur, u
         res.cells += nc.cells;
         if (res.cells > a.maxCells) break;
     }
-    if (res.minScoreNode == 0xffffffffu) err = GA_ASSERT;
+    if (res.minScoreNode == 0xffffffffu && !(Multi && seeds->count == 0)) err = GA_ASSERT;
     return res;
 }
 
@@ -955,6 +1124,95 @@ __device__ ExtState fill_extension(const FillArgs& a, const WSpace& w, u32& gen,
     st.committed = committed;
     if (err) st.status = err;
     else if (committed <= 1) st.status = GA_TRACE_FAILED;
+    return st;
+}
+
+// GraphAlignerBitvectorBanded::getMultiseedSlices (GraphAlignerBitvectorBanded.h:727-822): every
+// slice of read r from the empty initial slice, each slice's seeds started in it.  Each slice's
+// best X-score also goes to a per-read array (st.aux) that the traceback lowers as it finds
+// traces.
+__device__ ExtState fill_multiseed(const FillArgs& a, const WSpace& w, u32& gen, ArenaCursor& arena, u32 r, u32 lane)
+{
+    ExtState st;
+    st.dir = 0;
+    st.committed = 0;
+    st.status = GA_OK;
+    st.steps = 0;
+    st.aux = 0;
+    const uint8_t* seq = a.seq + a.seqOff[r];
+    const u32 seqLen = a.seqLen[r];
+    const u32 numSlices = (seqLen + 63) / 64;
+    const i32 bw = (i32)a.bandwidth;
+    u64 dirOff, auxOff;
+    if (!arena_alloc(a, arena, (u64)(numSlices + 1) * 8, dirOff, lane) || !arena_alloc(a, arena, (u64)(numSlices + 1) * 4, auxOff, lane))
+    {
+        st.status = GA_CAPACITY;
+        return st;
+    }
+    u64* dir = (u64*)(a.arena + dirOff);
+    i32* sliceMax = (i32*)(a.arena + auxOff);
+    st.dir = dirOff;
+    st.aux = auxOff;
+    // getInitialEmptySlice (Common.h:1541-1549): no nodes, minimum 0, bandwidth 1
+    if (!commit_slice(a, arena, dir, 0, w.band[0], 0, 0, 1, kIntMin, 0xffffffffu, false, lane, w.nodeMax))
+    {
+        st.status = GA_CAPACITY;
+        return st;
+    }
+    if (lane == 0) sliceMax[0] = kIntMin;
+    int prv = 0;
+    gen++;
+    u32 prevGen = gen;
+    u32 prevCount = 0;
+    u32 committed = 1;
+    i32 lastMin = 0;
+    i32 lastQuit = 1;
+    u64 k = a.seedOff[r];
+    const u64 kEnd = a.seedOff[r + 1];
+    int err = 0;
+    #pragma unroll 1
+    for (u32 s = 0; s < numSlices; s++)
+    {
+        const int cur = prv ^ 1;
+        gen++;
+        const u32 curGen = gen;
+        u32 curCount = 0;
+        const int64_t j = (int64_t)s * 64;
+        u64 next = k;
+        while (next < kEnd && a.seedSlice[next] == s) next++;
+        SliceSeeds seeds;
+        seeds.nodes = a.seedNode + k;
+        seeds.count = (u32)(next - k);
+        seeds.ws = seed_ws(j, seqLen, a.cost);
+        k = next;
+        SliceResult res = fill_slice<true>(a, w, cur, curGen, prevGen, curCount, prevCount, seq, seqLen, j, lastQuit, lastMin, st.steps, err, lane, &seeds);
+        if (err) break;
+        // fillDPSlice's checks of a slice that started seeds (GraphAlignerBitvectorBanded.h:543-549)
+        if (seeds.count > 0)
+        {
+            const double lim = ((double)j + 64) * (double)a.cost;
+            if (res.minScore > (i32)j + 64 || res.maxX == kIntMin || (double)res.maxX < -lim || (double)res.maxX > lim) { err = GA_ASSERT; break; }
+        }
+        if (!(res.minScore >= lastMin || res.minScore >= ws_value(seeds.ws, 0) || lastMin == kIntMax - bw - 1)) { err = GA_ASSERT; break; }
+        const bool notValid = res.cells >= a.maxCells;
+        const i32 quit = wadd(res.minScore, bw);
+        if (!commit_slice(a, arena, dir, committed, w.band[cur], curCount, res.minScore, quit, res.maxX, res.maxXNode, notValid, lane, w.nodeMax))
+        {
+            err = GA_CAPACITY;
+            break;
+        }
+        if (lane == 0) sliceMax[committed] = res.maxX;
+        committed++;
+        prv = cur;
+        prevGen = curGen;
+        prevCount = curCount;
+        lastMin = res.minScore;
+        lastQuit = quit;
+    }
+    if (!err && k != kEnd) err = GA_ASSERT;
+    st.committed = committed;
+    if (err) st.status = err;
+    __syncwarp();
     return st;
 }
 
@@ -1108,13 +1366,16 @@ __device__ __noinline__ bool trace_circular(const u64* items, const u64* ring, u
     return false;
 }
 
-__device__ __forceinline__ i32 fake_value() { return kIntMax; }
+// The extraSlice of a node-slice: the multiseed DP's seed-start column (getSeedSlice) where the
+// node is a seed start, else the fake column (0, 0, INT32_MAX), all of whose scores are INT32_MAX.
+__device__ __forceinline__ WS fake_ws() { return ws_make(0, 0, kIntMax); }
+
 
 __device__ __forceinline__ i32 col_value(const Col& c, int row) { return ws_value(ws_make(c.VP, c.VN, c.end), row); }
 
 // pickBacktraceCorner (Common.h:936-1054).  Out of line, like the other crossing rules:
 // the walk inside a node-slice is the hot path.  t is a copy (its record cache is a hint).
-__device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, Table t, u32 cs, u32 node, int64_t j, int& err)
+__device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, Table t, u32 cs, u32 node, int64_t j, int& err, WS extra)
 {
     const SliceRec* cr = t.rec(cs);
     const SliceRec* pr = t.rec(cs - 1);
@@ -1125,7 +1386,7 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
     const Item* prevSelf = t.find(cs - 1, node);
     if (cr->notValid || scoreHere > cr->quit)
     {
-        if (scoreHere == fake_value()) { out.pos = TPos { node, 0, j }; return out; }
+        if (scoreHere == ws_value(extra, 0)) { out.pos = TPos { node, 0, j }; return out; }
         i32 smallest = scoreHere + 1;
         TPos sp = TPos { 0xffffffffu, 0xffffffffu, -2 };
         bool change = false;
@@ -1214,8 +1475,8 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
             }
         }
     }
-    if (eq && scoreHere == fake_value()) { out.pos = TPos { node, 0, j }; return out; }
-    if (scoreHere == fake_value()) { out.pos = TPos { node, 0, j }; return out; }
+    if (eq && scoreHere == ws_before(extra)) { out.pos = TPos { node, 0, j }; return out; }
+    if (scoreHere == ws_value(extra, 0)) { out.pos = TPos { node, 0, j }; return out; }
     if (bestInvalidScore < scoreHere + 1) { out.pos = bestInvalid; out.sw = bestInvalidSw; return out; }
     err = GA_ASSERT;
     return out;
@@ -1225,8 +1486,9 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
 // into cols (the traceback only moves left inside a node, so it never needs the columns
 // after the one it enters at).  When every column is recomputed the last one must equal
 // the stored end column, as the reference asserts.  Returns 0 or the error status.
+template <bool Multi = false>
 __device__ __noinline__ int recalc(const DevGraph& g, i32 cost, Table t, u32 s, u32 node, const EqV4& eqv, Col* cols, u64* eqcol,
-    u32 lane, u32 lastColumn)
+    u32 lane, u32 lastColumn, WS extra = fake_ws())
 {
     const Item* it = t.find(s, node);
     if (!it) return GA_ASSERT;
@@ -1239,7 +1501,8 @@ __device__ __noinline__ int recalc(const DevGraph& g, i32 cost, Table t, u32 s, 
     u64 steps = 0;
     int err = 0;
     int64_t j = ((int64_t)s - 1) * 64;
-    node_calc<false>(g, cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, cols, eqcol, steps, err, lane, kIntMin, lastColumn);
+    node_calc<false, Multi>(g, cost, node, copy, eqv, prev, nullptr, kNil, &start, false, (i32)j, cols, eqcol, steps, err, lane, kIntMin, lastColumn,
+        (Multi && extra.end != kIntMax) ? &extra : nullptr);
     if (err) return err;
     u32 L = g.len[node];
     if (!ws_eq(ws_make(cols[0].VP, cols[0].VN, cols[0].end), start)) return GA_ASSERT;
@@ -1251,7 +1514,7 @@ __device__ __noinline__ int recalc(const DevGraph& g, i32 cost, Table t, u32 s, 
 // pickBacktraceVerticalCrossing (Common.h:886-934), the step out of (p.node, p.off > 0, row 0)
 // into the previous slice; pself is the node's entry there
 __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* seq, Table t, u32 curSlice, const Item* pself, const Col* cols,
-    TPos p, int& err)
+    TPos p, int& err, WS extra)
 {
     TStep second;
     second.pos = p;
@@ -1268,7 +1531,7 @@ __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* se
     i32 up = diag + (i32)((pself->HP >> p.off) & 1) - (i32)((pself->HN >> p.off) & 1);
     if (pr->notValid || cr->notValid || here > cr->quit || diag > pr->quit || up > pr->quit)
     {
-        if (here == fake_value()) second = TStep { p, false };
+        if (here == ws_value(extra, 0)) second = TStep { p, false };
         else if (diag < up) second = TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
         else second = TStep { TPos { p.node, p.off, p.seq - 1 }, false };
         return second;
@@ -1276,14 +1539,14 @@ __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* se
     if (up < here - 1 || diag < here - (eq ? 0 : 1)) { err = GA_ASSERT; return second; }
     if (up == here - 1) return TStep { TPos { p.node, p.off, p.seq - 1 }, false };
     if (diag == here - (eq ? 0 : 1)) return TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
-    err = GA_ASSERT;
+    if (here != ws_value(extra, 0)) err = GA_ASSERT;
     return second;
 }
 
 // pickBacktraceHorizontalCrossing (Common.h:817-884), the step out of (p.node, offset 0,
 // row off > 0) into an in-neighbour; self is the node's entry in the slice
 __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* seq, Table t, u32 curSlice, u32 curNode, const Item* self,
-    TPos p, u32 off, int& err)
+    TPos p, u32 off, int& err, WS extra)
 {
     TStep second;
     second.pos = p;
@@ -1321,7 +1584,7 @@ __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* 
                 }
             }
         }
-        if (tpos_eq(sp, p) && here != fake_value()) { err = GA_ASSERT; return second; }
+        if (tpos_eq(sp, p) && here != ws_value(extra, (int)off)) { err = GA_ASSERT; return second; }
         return TStep { sp, change };
     }
     #pragma unroll 1
@@ -1337,7 +1600,7 @@ __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* 
         if (v0 == here - 1) return TStep { TPos { nb, g.len[nb] - 1, p.seq }, true };
         if (v1 == here - (eq ? 0 : 1)) return TStep { TPos { nb, g.len[nb] - 1, p.seq - 1 }, true };
     }
-    if (here != fake_value()) { err = GA_ASSERT; return second; }
+    if (here != ws_value(extra, (int)off)) { err = GA_ASSERT; return second; }
     return TStep { p, false };
 }
 
@@ -1479,6 +1742,204 @@ __device__ __forceinline__ u32 row0_run_start(const Col* cols, u32 off, u32 lane
     return 63 - __clzll((long long)stops);
 }
 
+// getReverseTraceFromTable's walk (Common.h:571-720) from `start`, whose score is startScore,
+// up to the row above the read or, in the multiseed DP (Multi), to a seed start.  resultScore:
+// the trace's OnewayTrace::score.  Returns 0 or the error status.
+template <bool Multi>
+__device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 seqLen, u32 committed, Table& t, TraceOut& to, const WSpace& w,
+    TPos start, i32 startScore, i32& resultScore, u32 lane)
+{
+    int err = 0;
+    Col* cols = w.cols;
+    const u64 guardMax = (u64)to.cap * 4 + 1024;
+    resultScore = startScore;
+    to.push(start, false);
+    // the extraSlice of the current node-slice and its score at a row
+    WS extra = fake_ws();
+    auto xv = [&](u32 row) -> i32 { return Multi ? ws_value(extra, (int)row) : kIntMax; };
+    u32 curSlice = (u32)(start.seq / 64) + 1;
+    u32 curNode = 0xffffffffu;
+    u32 curLen = 0;
+    u32 colsUpTo = 0;             // columns 0..colsUpTo of (curSlice, curNode) are in cols, their match masks in eqcol
+    EqV4 eqv;
+    if (!eq_vector(seq, seqLen, ((int64_t)curSlice - 1) * 64, eqv, lane)) err = GA_ASSERT;
+    i32 lastScore = kIntMax - 1;
+    u64 guard = 0;
+    #pragma unroll 1
+    while (!err && !to.overflow && to.back.seq != -1)
+    {
+        if (++guard > guardMax) { err = GA_CAPACITY; break; }
+        TPos b = to.back;
+        u32 newSlice = (u32)(b.seq / 64) + 1;
+        if (newSlice >= committed) { err = GA_ASSERT; break; }
+        // a self-loop can re-enter the same node-slice further right than it was computed
+        if (newSlice != curSlice || b.node != curNode || b.off > colsUpTo)
+        {
+            if (newSlice != curSlice && !eq_vector(seq, seqLen, ((int64_t)newSlice - 1) * 64, eqv, lane)) { err = GA_ASSERT; break; }
+            curSlice = newSlice;
+            curNode = b.node;
+            if (curSlice == 0) { err = GA_ASSERT; break; }
+            if (Multi)
+            {
+                const Item* here = t.find(curSlice, curNode);
+                if (!here) { err = GA_ASSERT; break; }
+                extra = (here->node & kSeedStart) ? seed_ws(((int64_t)curSlice - 1) * 64, seqLen, cost) : fake_ws();
+            }
+            err = recalc<Multi>(g, cost, t, curSlice, curNode, eqv, cols, w.eqcol, lane, b.off, extra);
+            if (err) break;
+            colsUpTo = b.off;
+            curLen = g.len[curNode];
+        }
+        const int64_t sj = ((int64_t)curSlice - 1) * 64;
+        if (b.off >= curLen) { err = GA_ASSERT; break; }
+        const u32 row = mod64(b.seq);
+        lastScore = col_value(cols[b.off], (int)row);
+        if (row == 0 && b.off == 0)
+        {
+            TStep bt = bt_corner(g, seq, t, curSlice, curNode, sj, err, extra);
+            if (err) break;
+            if (tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == xv(mod64(bt.pos.seq))) break;
+            if (Multi && tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == ws_before(extra)) break;
+            to.push(bt.pos, bt.sw);
+            if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
+            continue;
+        }
+        if (row == 0)
+        {
+            const Item* pself = t.find(curSlice - 1, curNode);
+            if (!pself)
+            {
+                #pragma unroll 1
+                for (u32 k = b.off - 1; k > 0; k--) to.push(TPos { curNode, k, b.seq }, false);
+                to.push(TPos { curNode, 0, b.seq }, false);
+                continue;
+            }
+            // pickBacktraceVerticalCrossing (Common.h:886-934)
+            // step left along row 0 while the score falls by one per column: lane k tests
+            // columns k and k + 32 against their left neighbours, the run ends at the
+            // highest failing column at or below b.off (column 0 always ends it)
+            TPos p = b;
+            p.off = row0_run_start(cols, b.off, lane);
+            TStep second = p.off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err, extra) : vertical_step(g, seq, t, curSlice, pself, cols, p, err, extra);
+            if (err) break;
+            if (second.pos.seq == b.seq && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == xv(mod64(second.pos.seq))) break;
+            if (p.off != b.off)
+            {
+                #pragma unroll 1
+                for (u32 k = b.off - 1; k != p.off; k--) to.push(TPos { p.node, k, p.seq }, false);
+            }
+            if (!tpos_eq(p, to.back)) to.push(p, false);
+            if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
+            to.push(second.pos, second.sw);
+            continue;
+        }
+        if (b.off == 0)
+        {
+            // pickBacktraceHorizontalCrossing (Common.h:817-884)
+            const Item* self = t.find(curSlice, curNode);
+            if (!self) { err = GA_ASSERT; break; }
+            // step up column 0 while its score falls by one per row (the start column's VP
+            // bits): the run ends at the highest row at or below this one whose bit is clear
+            // (row 0 always ends it)
+            TPos p = b;
+            {
+                const u32 r = mod64(b.seq);
+                const u64 stops = (~self->sVP | 1ULL) & (r == 63 ? kAllOnes : ((2ULL << r) - 1));
+                p.seq -= (int64_t)(r - (63 - __clzll((long long)stops)));
+            }
+            const u32 off = mod64(p.seq);
+            TStep second = off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err, extra) : horizontal_step(g, seq, t, curSlice, curNode, self, p, off, err, extra);
+            if (err) break;
+            if (second.pos.node == b.node && !second.sw && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == xv(mod64(second.pos.seq))) break;
+            if (p.seq != b.seq)
+            {
+                #pragma unroll 1
+                for (int64_t sp = b.seq - 1; sp != p.seq; sp--) to.push(TPos { p.node, p.off, sp }, false);
+            }
+            if (!tpos_eq(p, to.back)) to.push(p, false);
+            if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
+            to.push(second.pos, second.sw);
+            if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
+            continue;
+        }
+        // pickBacktraceInside (Common.h:770-815).  The four neighbouring scores are
+        // carried incrementally: a vertical step moves up one row in both columns
+        // (score(r-1) = score(r) - VP_r + VN_r); a diagonal or horizontal step makes
+        // the left column current and loads the next one.  The read/graph match of
+        // a cell is bit `row` of the column's match mask (the fill's Eq), which is
+        // GraphAlignerCommon::characterMatch for every read and graph character.
+        {
+            u32 hori = b.off;
+            u32 vert = row;
+            // the recomputation left each column's match mask (the fill's Eq) in eqcol
+            const u64* eqcol = w.eqcol;
+            if (hori > 0 && vert > 0)
+            {
+                WS colH = ws_make(cols[hori].VP, cols[hori].VN, cols[hori].end);
+                WS colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
+                i32 here = ws_value(colH, (int)vert);
+                i32 left = ws_value(colL, (int)vert);
+                u64 eqH = eqcol[hori];
+                #pragma unroll 1
+                while (true)
+                {
+                    const i32 vs = here - (i32)((colH.VP >> vert) & 1) + (i32)((colH.VN >> vert) & 1);
+                    const i32 ds = left - (i32)((colL.VP >> vert) & 1) + (i32)((colL.VN >> vert) & 1);
+                    const bool eq = (eqH >> vert) & 1;
+                    if (vs == here - 1)
+                    {
+                        vert--;
+                        to.push(TPos { b.node, hori, sj + vert }, false);
+                        here = vs;
+                        left = ds;
+                    }
+                    else if (ds == here - (eq ? 0 : 1))
+                    {
+                        hori--;
+                        vert--;
+                        to.push(TPos { b.node, hori, sj + vert }, false);
+                        here = ds;
+                        colH = colL;
+                        if (hori > 0)
+                        {
+                            colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
+                            left = ws_value(colL, (int)vert);
+                            eqH = eqcol[hori];
+                        }
+                    }
+                    else if (left == here - 1)
+                    {
+                        hori--;
+                        to.push(TPos { b.node, hori, sj + vert }, false);
+                        here = left;
+                        colH = colL;
+                        if (hori > 0)
+                        {
+                            colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
+                            left = ws_value(colL, (int)vert);
+                            eqH = eqcol[hori];
+                        }
+                    }
+                    else
+                    {
+                        if (here != xv(vert)) err = GA_ASSERT;
+                        break;
+                    }
+                    if (to.overflow || hori == 0 || vert == 0) break;
+                }
+            }
+            if (err || to.overflow) break;
+            if (col_value(cols[to.back.off], (int)mod64(to.back.seq)) == xv(mod64(to.back.seq))) break;
+        }
+    }
+    if (!err && !to.overflow)
+    {
+        if (resultScore < lastScore) err = GA_ASSERT;
+        resultScore -= lastScore;
+    }
+    return err;
+}
+
 __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st, const WSpace& w, u32 lane)
 {
     const DevGraph& g = a.g;
@@ -1521,182 +1982,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
         // getReverseTraceFromTable (Common.h:571-758)
         TPos start = TPos { ec.node, ec.nodeOffset, ec.j + ec.bvOffset };
         i32 startScore = col_value(cols[ec.nodeOffset], (int)ec.bvOffset);
-        resultScore = startScore;
-        to.push(start, false);
-        u32 curSlice = (u32)(start.seq / 64) + 1;
-        u32 curNode = 0xffffffffu;
-        u32 curLen = 0;
-        u32 colsUpTo = 0;             // columns 0..colsUpTo of (curSlice, curNode) are in cols, their match masks in eqcol
-        EqV4 eqv;
-        if (!eq_vector(seq, seqLen, ((int64_t)curSlice - 1) * 64, eqv, lane)) err = GA_ASSERT;
-        i32 lastScore = kIntMax - 1;
-        u64 guard = 0;
-        const u64 guardMax = (u64)cap * 4 + 1024;
-        #pragma unroll 1
-        while (!err && !to.overflow && to.back.seq != -1)
-        {
-            if (++guard > guardMax) { err = GA_CAPACITY; break; }
-            TPos b = to.back;
-            u32 newSlice = (u32)(b.seq / 64) + 1;
-            if (newSlice >= st.committed) { err = GA_ASSERT; break; }
-            // a self-loop can re-enter the same node-slice further right than it was computed
-            if (newSlice != curSlice || b.node != curNode || b.off > colsUpTo)
-            {
-                if (newSlice != curSlice && !eq_vector(seq, seqLen, ((int64_t)newSlice - 1) * 64, eqv, lane)) { err = GA_ASSERT; break; }
-                curSlice = newSlice;
-                curNode = b.node;
-                if (curSlice == 0) { err = GA_ASSERT; break; }
-                err = recalc(g, a.cost, t, curSlice, curNode, eqv, cols, w.eqcol, lane, b.off);
-                if (err) break;
-                colsUpTo = b.off;
-                curLen = g.len[curNode];
-            }
-            const int64_t sj = ((int64_t)curSlice - 1) * 64;
-            if (b.off >= curLen) { err = GA_ASSERT; break; }
-            const u32 row = mod64(b.seq);
-            lastScore = col_value(cols[b.off], (int)row);
-            if (row == 0 && b.off == 0)
-            {
-                TStep bt = bt_corner(g, seq, t, curSlice, curNode, sj, err);
-                if (err) break;
-                if (tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == fake_value()) break;
-                to.push(bt.pos, bt.sw);
-                if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
-                continue;
-            }
-            if (row == 0)
-            {
-                const Item* pself = t.find(curSlice - 1, curNode);
-                if (!pself)
-                {
-                    #pragma unroll 1
-                    for (u32 k = b.off - 1; k > 0; k--) to.push(TPos { curNode, k, b.seq }, false);
-                    to.push(TPos { curNode, 0, b.seq }, false);
-                    continue;
-                }
-                // pickBacktraceVerticalCrossing (Common.h:886-934)
-                // step left along row 0 while the score falls by one per column: lane k tests
-                // columns k and k + 32 against their left neighbours, the run ends at the
-                // highest failing column at or below b.off (column 0 always ends it)
-                TPos p = b;
-                p.off = row0_run_start(cols, b.off, lane);
-                TStep second = p.off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : vertical_step(g, seq, t, curSlice, pself, cols, p, err);
-                if (err) break;
-                if (second.pos.seq == b.seq && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
-                if (p.off != b.off)
-                {
-                    #pragma unroll 1
-                    for (u32 k = b.off - 1; k != p.off; k--) to.push(TPos { p.node, k, p.seq }, false);
-                }
-                if (!tpos_eq(p, to.back)) to.push(p, false);
-                if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
-                to.push(second.pos, second.sw);
-                continue;
-            }
-            if (b.off == 0)
-            {
-                // pickBacktraceHorizontalCrossing (Common.h:817-884)
-                const Item* self = t.find(curSlice, curNode);
-                if (!self) { err = GA_ASSERT; break; }
-                // step up column 0 while its score falls by one per row (the start column's VP
-                // bits): the run ends at the highest row at or below this one whose bit is clear
-                // (row 0 always ends it)
-                TPos p = b;
-                {
-                    const u32 r = mod64(b.seq);
-                    const u64 stops = (~self->sVP | 1ULL) & (r == 63 ? kAllOnes : ((2ULL << r) - 1));
-                    p.seq -= (int64_t)(r - (63 - __clzll((long long)stops)));
-                }
-                const u32 off = mod64(p.seq);
-                TStep second = off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err) : horizontal_step(g, seq, t, curSlice, curNode, self, p, off, err);
-                if (err) break;
-                if (second.pos.node == b.node && !second.sw && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == fake_value()) break;
-                if (p.seq != b.seq)
-                {
-                    #pragma unroll 1
-                    for (int64_t sp = b.seq - 1; sp != p.seq; sp--) to.push(TPos { p.node, p.off, sp }, false);
-                }
-                if (!tpos_eq(p, to.back)) to.push(p, false);
-                if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
-                to.push(second.pos, second.sw);
-                if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
-                continue;
-            }
-            // pickBacktraceInside (Common.h:770-815).  The four neighbouring scores are
-            // carried incrementally: a vertical step moves up one row in both columns
-            // (score(r-1) = score(r) - VP_r + VN_r); a diagonal or horizontal step makes
-            // the left column current and loads the next one.  The read/graph match of
-            // a cell is bit `row` of the column's match mask (the fill's Eq), which is
-            // GraphAlignerCommon::characterMatch for every read and graph character.
-            {
-                u32 hori = b.off;
-                u32 vert = row;
-                // the recomputation left each column's match mask (the fill's Eq) in eqcol
-                const u64* eqcol = w.eqcol;
-                if (hori > 0 && vert > 0)
-                {
-                    WS colH = ws_make(cols[hori].VP, cols[hori].VN, cols[hori].end);
-                    WS colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
-                    i32 here = ws_value(colH, (int)vert);
-                    i32 left = ws_value(colL, (int)vert);
-                    u64 eqH = eqcol[hori];
-                    #pragma unroll 1
-                    while (true)
-                    {
-                        const i32 vs = here - (i32)((colH.VP >> vert) & 1) + (i32)((colH.VN >> vert) & 1);
-                        const i32 ds = left - (i32)((colL.VP >> vert) & 1) + (i32)((colL.VN >> vert) & 1);
-                        const bool eq = (eqH >> vert) & 1;
-                        if (vs == here - 1)
-                        {
-                            vert--;
-                            to.push(TPos { b.node, hori, sj + vert }, false);
-                            here = vs;
-                            left = ds;
-                        }
-                        else if (ds == here - (eq ? 0 : 1))
-                        {
-                            hori--;
-                            vert--;
-                            to.push(TPos { b.node, hori, sj + vert }, false);
-                            here = ds;
-                            colH = colL;
-                            if (hori > 0)
-                            {
-                                colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
-                                left = ws_value(colL, (int)vert);
-                                eqH = eqcol[hori];
-                            }
-                        }
-                        else if (left == here - 1)
-                        {
-                            hori--;
-                            to.push(TPos { b.node, hori, sj + vert }, false);
-                            here = left;
-                            colH = colL;
-                            if (hori > 0)
-                            {
-                                colL = ws_make(cols[hori - 1].VP, cols[hori - 1].VN, cols[hori - 1].end);
-                                left = ws_value(colL, (int)vert);
-                                eqH = eqcol[hori];
-                            }
-                        }
-                        else
-                        {
-                            if (here != fake_value()) err = GA_ASSERT;
-                            break;
-                        }
-                        if (to.overflow || hori == 0 || vert == 0) break;
-                    }
-                }
-                if (err || to.overflow) break;
-                if (col_value(cols[to.back.off], (int)mod64(to.back.seq)) == fake_value()) break;
-            }
-        }
-        if (!err && !to.overflow)
-        {
-            if (resultScore < lastScore) err = GA_ASSERT;
-            resultScore -= lastScore;
-        }
+        err = trace_walk<false>(g, a.cost, seq, seqLen, st.committed, t, to, w, start, startScore, resultScore, lane);
         if (!err && !to.overflow) err = row_above(g, t, to);
     }
     to.finish();
@@ -1706,6 +1992,175 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
         a.status[ext] = status;
         a.score[ext] = status == GA_OK ? resultScore : 0;
         a.traceLen[ext] = status == GA_OK ? to.n : 0;
+    }
+}
+
+// The multiseed DP's best X-score of node in committed slice s (a ballot over the slice's
+// node ids, read from the arena); false when the node is not in the slice's band
+__device__ __forceinline__ bool slice_node_max(const uint8_t* arena, const u64* dir, u32 s, u32 node, u32 lane, i32& out)
+{
+    const SliceRec* r = (const SliceRec*)(arena + dir[s]);
+    const u32 n = r->count;
+    const u32* ids = (const u32*)((const uint8_t*)r + sizeof(SliceRec));
+#pragma unroll 1
+    for (u32 base = 0; base < n; base += 32)
+    {
+        const u32 k = base + lane;
+        const u32 hit = __ballot_sync(kFull, k < n && ids[k] == node);
+        if (hit)
+        {
+            out = rec_node_max(r)[base + __ffs((int)hit) - 1];
+            return true;
+        }
+    }
+    return false;
+}
+
+// getLocalMaximaTracesFromTable (Common.h:355-494) for read r: slices from the last, band
+// nodes in order; a node whose best exact-end-position X-score in a slice is positive, at
+// least the multimap fraction of the slice's (lowered) best and not below any of its own in
+// the slices above and below or its neighbours' starts a trace at its best cell.  Each trace
+// raises the best of the slices it spans beyond its first 5 %.
+__device__ void trace_multiseed(const MultiTraceArgs& a, u32 r, const ExtState& st, const WSpace& w, u32 lane)
+{
+    const DevGraph& g = a.g;
+    if (lane == 0 && a.cellSteps) a.cellSteps[r] = st.steps;
+    if (st.status != GA_OK)
+    {
+        if (lane == 0)
+        {
+            a.status[r] = st.status;
+            a.numTraces[r] = 0;
+        }
+        return;
+    }
+    const uint8_t* seq = a.seq + a.seqOff[r];
+    const u32 seqLen = a.seqLen[r];
+    Table t;
+    t.arena = a.arena;
+    t.dir = (const u64*)(a.arena + st.dir);
+    t.count = st.committed;
+    t.lane = lane;
+    t.slots = w.slots;
+    t.init();
+    i32* sliceMax = (i32*)(a.arena + st.aux);
+    u64* out = a.traceItems + a.traceOffset[r];
+    const u64 cap = a.traceCap[r];
+    u64 used = 0;
+    u32 nt = 0;
+    int err = 0;
+    Col* cols = w.cols;
+    const u32 last = st.committed - 1;
+#pragma unroll 1
+    for (u32 cs = last; cs >= 1 && !err; cs--)
+    {
+        const SliceRec* cr = (const SliceRec*)(a.arena + t.dir[cs]);
+        if (cr->maxX <= 0) continue;
+        const u32 n = cr->count;
+        const u32* ids = (const u32*)((const uint8_t*)cr + sizeof(SliceRec));
+        const Item* items = (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
+        const i32* nodeMax = rec_node_max(cr);
+        const double threshold = (double)sliceMax[cs] * a.multimapScoreFraction;
+        const int64_t j = ((int64_t)cs - 1) * 64;
+#pragma unroll 1
+        for (u32 k = 0; k < n && !err; k++)
+        {
+            const u32 node = ids[k];
+            const i32 score = nodeMax[k];
+            if (!(items[k].node & kExists) || score <= 0 || (double)score < threshold) continue;
+            i32 other;
+            if (slice_node_max(a.arena, t.dir, cs - 1, node, lane, other) && other > score) continue;
+            if (cs < last && slice_node_max(a.arena, t.dir, cs + 1, node, lane, other) && other >= score) continue;
+            bool notLocal = false;
+#pragma unroll 1
+            for (u32 e = g.inOff[node]; e < g.inOff[node + 1] && !notLocal; e++)
+            {
+                const u32 nb = g.inNb[e];
+                if (slice_node_max(a.arena, t.dir, cs, nb, lane, other) && other > score) notLocal = true;
+                else if (slice_node_max(a.arena, t.dir, cs - 1, nb, lane, other) && other > score) notLocal = true;
+            }
+#pragma unroll 1
+            for (u32 e = g.outOff[node]; e < g.outOff[node + 1] && !notLocal; e++)
+            {
+                const u32 nb = g.outNb[e];
+                if (slice_node_max(a.arena, t.dir, cs, nb, lane, other) && other > score) notLocal = true;
+                else if (cs < last && slice_node_max(a.arena, t.dir, cs + 1, nb, lane, other) && other > score) notLocal = true;
+            }
+            if (notLocal) continue;
+            // the node's columns with its seed start, and among them the cell of greatest row that
+            // scores the node's best X-score (the first column on ties), across the lanes
+            EqV4 eqv;
+            if (!eq_vector(seq, seqLen, j, eqv, lane)) { err = GA_ASSERT; break; }
+            const WS extra = (items[k].node & kSeedStart) ? seed_ws(j, seqLen, a.cost) : fake_ws();
+            err = recalc<true>(g, a.cost, t, cs, node, eqv, cols, w.eqcol, lane, 63, extra);
+            if (err) break;
+            const int cells = (int)((int64_t)seqLen - j < 64 ? (int64_t)seqLen - j : 64);
+            const u32 L = g.len[node];
+            bool bad = false;
+            int candOff = -1;
+            u32 candCol = 0xffffffffu;
+#pragma unroll 1
+            for (u32 h = 0; h < 2; h++)
+            {
+                const u32 i = lane + 32 * h;
+                if (i >= L || bad) continue;
+                const WS cw = ws_make(cols[i].VP, cols[i].VN, cols[i].end);
+                const i32 mx = ws_max_xscore(cw, (i32)j, a.cost, cells, kAllOnes);
+                if (mx > score) { bad = true; continue; }
+                if (mx != score) continue;
+#pragma unroll 1
+                for (int off = 63; off >= 0; off--)
+                {
+                    if (j + off >= (int64_t)seqLen) continue;
+                    const i32 here = ws_xscore(cw, (i32)j, off, a.cost);
+                    if (here > score) { bad = true; break; }
+                    if (here == score && off > candOff)
+                    {
+                        candOff = off;
+                        candCol = i;
+                    }
+                }
+            }
+            if (__ballot_sync(kFull, bad)) { err = GA_ASSERT; break; }
+            const int gOff = __reduce_max_sync(kFull, candOff);
+            const u32 gCol = __reduce_min_sync(kFull, candOff == gOff ? candCol : 0xffffffffu);
+            if (gOff < 0 || j + gOff >= (int64_t)seqLen) { err = GA_ASSERT; break; }
+            if (nt >= a.maxTraces) { err = GA_CAPACITY; break; }
+            const TPos start = TPos { node, gCol, j + gOff };
+            const i32 startScore = col_value(cols[gCol], gOff);
+            TraceOut to;
+            to.items = out + used;
+            to.ring = w.ring;
+            to.cap = (u32)(cap - used < 0xffffffffULL ? cap - used : 0xffffffffULL);
+            to.n = 0;
+            to.lane = lane;
+            to.overflow = false;
+            i32 traceScore = 0;
+            err = trace_walk<true>(g, a.cost, seq, seqLen, st.committed, t, to, w, start, startScore, traceScore, lane);
+            to.finish();
+            if (!err && to.overflow) err = GA_CAPACITY;
+            if (err) break;
+            const int64_t traceEnd = start.seq, traceStart = to.back.seq;
+            if (traceStart < 0 || traceEnd < traceStart) { err = GA_ASSERT; break; }
+            if (lane == 0)
+            {
+                const u64 slot = (u64)r * a.maxTraces + nt;
+                a.traceScore[slot] = traceScore;
+                a.traceStart[slot] = used;
+                a.traceLen[slot] = to.n;
+            }
+            const u32 startSlice = (u32)(((double)(traceEnd - traceStart) * 0.05 + (double)traceStart + 64 - 1) / 64 + 1);
+#pragma unroll 1
+            for (u32 i = startSlice + lane; i < cs; i += 32) sliceMax[i] = imax(sliceMax[i], score);
+            __syncwarp();
+            used += to.n;
+            nt++;
+        }
+    }
+    if (lane == 0)
+    {
+        a.status[r] = err ? err : GA_OK;
+        a.numTraces[r] = err ? 0 : nt;
     }
 }
 
@@ -1799,9 +2254,75 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(TraceArgs ta, u32* counte
     }
 }
 
+
+// The multiseed DP's fill: a warp takes the next read and fills its whole DP table; its
+// frontier tables and per-node X-scores live in the global workspace.
+__global__ void __launch_bounds__(128, 4) fill_multiseed_kernel(FillArgs fa, u32* counter)
+{
+    load_iupac_table();
+    const u32 lane = threadIdx.x & 31;
+    const u64 gwarp = (u64)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const WSpace w = wspace_at(fa.workspace + gwarp * fa.workspaceStride, fa.caps);
+#pragma unroll 1
+    for (u32 k = lane; k < fa.caps.hash; k += 32)
+    {
+        w.key[0][k] = 0;
+        w.key[1][k] = 0;
+    }
+    __syncwarp();
+    u32 gen = 0;
+    ArenaCursor arena;
+    arena.pos = 0;
+    arena.end = 0;
+    arena.used = 0;
+    u32 r;
+#pragma unroll 1
+    while (next_extension(counter, fa.num, fa.order, fa.prevStatus, lane, r))
+    {
+        __syncwarp();
+        const ExtState st = fill_multiseed(fa, w, gen, arena, r, lane);
+        if (lane == 0) fa.states[r] = st;
+        if (gen > 0xF0000000u)
+        {
+            __syncwarp();
+#pragma unroll 1
+            for (u32 k2 = lane; k2 < fa.caps.hash; k2 += 32)
+            {
+                w.key[0][k2] = 0;
+                w.key[1][k2] = 0;
+            }
+            __syncwarp();
+            gen = 0;
+        }
+    }
+    if (lane == 0 && arena.used) atomicAdd(fa.arenaCursor + 1, (unsigned long long)arena.used);
+}
+
+// The multiseed DP's traceback: a warp takes the next filled read and traces from every
+// local maximum of its table.
+__global__ void __launch_bounds__(128, 6) trace_multiseed_kernel(MultiTraceArgs ta, u32* counter)
+{
+    extern __shared__ __align__(16) uint8_t dsmem[];
+    load_iupac_table();
+    const u32 lane = threadIdx.x & 31;
+    uint8_t* base = dsmem + (u64)(threadIdx.x >> 5) * kTraceSpaceBytes;
+    WSpace w {};
+    w.cols = (Col*)base;
+    w.eqcol = (u64*)(base + 64 * sizeof(Col));
+    w.ring = (u64*)(base + 64 * sizeof(Col) + 64 * 8);
+    w.slots = (SliceSlot*)(base + 64 * sizeof(Col) + 64 * 8 + 64 * 8);
+    u32 r;
+#pragma unroll 1
+    while (next_extension(counter, ta.num, ta.order, ta.prevStatus, lane, r))
+    {
+        __syncwarp();
+        trace_multiseed(ta, r, ta.states[r], w, lane);
+    }
+}
 }
 
 uint64_t ga_warp_tables_bytes(const gadev::Caps& c) { return gadev::wspace_bytes(c); }
+uint64_t ga_multiseed_tables_bytes(const gadev::Caps& c) { return gadev::wspace_bytes(c, true); }
 
 static bool set_smem(const void* kernel, size_t smem)
 {
@@ -1835,6 +2356,17 @@ int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint
     gadev::fill_kernel<<<fillBlocks, warpsPerBlock * 32, fillSmem, (cudaStream_t)stream>>>(fa, counters);
     if (cudaGetLastError() != cudaSuccess) return -1;
     gadev::trace_kernel<<<traceBlocks, warpsPerBlock * 32, traceSmem, (cudaStream_t)stream>>>(ta, counters + 1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int ga_launch_multiseed(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
+    int warpsPerBlock, void* stream)
+{
+    const size_t traceSmem = (size_t)gadev::kTraceSpaceBytes * warpsPerBlock;
+    if (!fa.workspace || !set_smem((const void*)gadev::trace_multiseed_kernel, traceSmem)) return -1;
+    gadev::fill_multiseed_kernel<<<fillBlocks, warpsPerBlock * 32, 0, (cudaStream_t)stream>>>(fa, counters);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    gadev::trace_multiseed_kernel<<<traceBlocks, warpsPerBlock * 32, traceSmem, (cudaStream_t)stream>>>(ta, counters + 1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -31,14 +31,18 @@ struct __align__(16) Item
     u64 HP, HN;            // horizontal deltas along the slice's last row
     i32 sEnd, eEnd;
     i32 minScore;
-    u32 node;              // bit 31: the node has been computed ("exists")
+    u32 node;              // bit 31: the node has been computed ("exists"); bit 30: it is a
+                           // seed start in this slice (multiseed DP, DPSlice::seedstartNodes)
 };
 static constexpr u32 kExists = 0x80000000u;
-static constexpr u32 kNodeMask = 0x7fffffffu;
+static constexpr u32 kSeedStart = 0x40000000u;
+static constexpr u32 kNodeMask = 0x3fffffffu;
 
 // A committed DP slice in the arena: this 32-byte record, then the band's node ids
-// (count u32, padded to 16 bytes), then count Items, all in first-pop order.  The
-// traceback finds a node's entry by a warp ballot over the ids.
+// (count u32, padded to 16 bytes), then count Items, all in first-pop order (the multiseed
+// DP's seed starts first), then for the multiseed DP each node's best exact-end-position
+// X-score (count i32, DPSlice::nodeMaxExactEndposScore).  The traceback finds a node's
+// entry by a warp ballot over the ids.
 struct __align__(16) SliceRec
 {
     i32 minScore;
@@ -57,6 +61,7 @@ struct ExtState
     u32 committed;         // slices in the table, including the start slice
     i32 status;
     u64 steps;             // Myers column steps in the fill
+    u64 aux;               // multiseed DP: arena offset of the per-slice best X-scores (i32 [committed])
 };
 
 // Capacities of one warp's frontier tables.
@@ -91,6 +96,11 @@ struct FillArgs
     Caps caps;
     const i32* prevStatus; // when non-null, only extensions whose previous status is GA_CAPACITY run
     ExtState* states;      // [num] where each extension's table is, for the traceback
+    // multiseed DP (nullptr otherwise): read i's seeds are [seedOff[i], seedOff[i+1]),
+    // slice index and split node each, in slice order
+    const u64* seedOff;
+    const u32* seedSlice;
+    const u32* seedNode;
 };
 
 struct TraceArgs
@@ -114,10 +124,38 @@ struct TraceArgs
     u64* cellSteps;
 };
 
+// The multiseed DP's traceback outputs (ga_multiseed_results).
+struct MultiTraceArgs
+{
+    DevGraph g;
+    i32 cost;
+    u32 num;
+    const u32* order;
+    const i32* prevStatus;
+    const ExtState* states;
+    const uint8_t* seq;
+    const u64* seqOff;
+    const u32* seqLen;
+    const uint8_t* arena;
+    const u64* traceOffset;
+    const u64* traceCap;
+    u32 maxTraces;
+    double multimapScoreFraction;
+    i32* status;
+    u32* numTraces;
+    i32* traceScore;
+    u64* traceStart;
+    u32* traceLen;
+    u64* traceItems;
+    u64* cellSteps;
+};
+
 }
 
-// bytes of one warp's frontier tables for these capacities
+// bytes of one warp's frontier tables for these capacities (the multiseed DP's add each band
+// node's best X-score)
 uint64_t ga_warp_tables_bytes(const gadev::Caps& caps);
+uint64_t ga_multiseed_tables_bytes(const gadev::Caps& caps);
 // resident blocks of 32 * warpsPerBlock threads per SM of the fill kernel (shared: tables in
 // shared memory) and of the traceback kernel
 int ga_fill_blocks_per_sm(int warpsPerBlock, const gadev::Caps& caps, bool shared);
@@ -125,6 +163,9 @@ int ga_trace_blocks_per_sm(int warpsPerBlock);
 // launches the fill kernel and then the traceback kernel on `stream`, blocks of warpsPerBlock
 // warps, one extension per warp at a time; counters[0] and [1] must be zero
 int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
+    int warpsPerBlock, void* stream);
+// the multiseed DP's fill and traceback kernels (the frontier tables always in the global workspace)
+int ga_launch_multiseed(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
     int warpsPerBlock, void* stream);
 int ga_upload_tables();
 void ga_set_last_error(const char* message);

@@ -296,6 +296,11 @@ static void serve_loop(ga_server* s)
 extern "C" int ga_server_create(ga_aligner_t aligner, const ga_server_params* params, ga_server_t* out)
 {
     if (!aligner || !out) return GA_ERR_ARGUMENT;
+    if (aligner->params.multiseed_dp)
+    {
+        ga_set_last_error("ga_server_create: the serving loop runs the seed loop; the multiseed DP is ga_align_reads only");
+        return GA_ERR_ARGUMENT;
+    }
     ga_server* s = new ga_server();
     s->a = aligner;
     if (params)

@@ -147,6 +147,88 @@ def results_desc(r: BatchResult):
                         ptr(r.trace_items, ctypes.c_uint64), ptr(r.cell_steps, ctypes.c_uint64))
 
 
+@dataclasses.dataclass
+class MultiseedBatch:
+    """Reads and their multiseed DP seeds (prepareSeedsForMultiseeding: per read, (slice, split
+    node) pairs in slice order), laid out for ga_multiseed_batch."""
+    seq: np.ndarray
+    seq_offset: np.ndarray
+    seq_len: np.ndarray
+    seed_offset: np.ndarray
+    seed_slice: np.ndarray
+    seed_node: np.ndarray
+    trace_offset: np.ndarray
+    trace_capacity: np.ndarray
+    max_traces: int
+    multimap_score_fraction: float = 0.9
+
+    @property
+    def num(self) -> int:
+        return len(self.seq_len)
+
+    @classmethod
+    def pack(cls, seqs, seeds, max_traces: int = 64, items_per_bp: int = 4, multimap_score_fraction: float = 0.9):
+        """seqs: read sequences; seeds: per read a list of (slice, split node)."""
+        n = len(seqs)
+        lens = np.fromiter((len(x) for x in seqs), dtype=np.uint32, count=n)
+        offs = np.zeros(n, dtype=np.uint64)
+        if n > 1:
+            offs[1:] = np.cumsum(lens[:-1], dtype=np.uint64)
+        blob = np.frombuffer(b"".join(bytes(x) for x in seqs) or b"\0", dtype=np.uint8).copy()
+        soff = np.zeros(n + 1, dtype=np.uint64)
+        soff[1:] = np.cumsum([len(x) for x in seeds], dtype=np.uint64)
+        flat = [p for x in seeds for p in x] or [(0, 0)]
+        sslice = np.array([p[0] for p in flat], dtype=np.uint32)
+        snode = np.array([p[1] for p in flat], dtype=np.uint32)
+        cap = lens.astype(np.uint64) * items_per_bp + 4096
+        toff = np.zeros(n, dtype=np.uint64)
+        if n > 1:
+            toff[1:] = np.cumsum(cap[:-1])
+        return cls(blob, offs, lens, soff, sslice, snode, toff, cap, max_traces, multimap_score_fraction)
+
+    def desc(self):
+        return _abi.MultiseedBatchDesc(self.num, ptr(self.seq, ctypes.c_uint8), ptr(self.seq_offset, ctypes.c_uint64),
+                                       ptr(self.seq_len, ctypes.c_uint32), ptr(self.seed_offset, ctypes.c_uint64),
+                                       ptr(self.seed_slice, ctypes.c_uint32), ptr(self.seed_node, ctypes.c_uint32),
+                                       ptr(self.trace_offset, ctypes.c_uint64), ptr(self.trace_capacity, ctypes.c_uint64),
+                                       self.max_traces, self.multimap_score_fraction)
+
+
+@dataclasses.dataclass
+class MultiseedResult:
+    status: np.ndarray
+    num_traces: np.ndarray
+    trace_score: np.ndarray
+    trace_start: np.ndarray
+    trace_len: np.ndarray
+    trace_items: np.ndarray
+    cell_steps: np.ndarray
+    trace_offset: np.ndarray
+    max_traces: int
+
+    @classmethod
+    def alloc(cls, b: MultiseedBatch):
+        n, m = b.num, b.max_traces
+        items = int(b.trace_offset[-1] + b.trace_capacity[-1]) if n else 1
+        return cls(np.zeros(n, np.int32), np.zeros(n, np.uint32), np.zeros(n * m, np.int32), np.zeros(n * m, np.uint64),
+                   np.zeros(n * m, np.uint32), np.zeros(max(items, 1), np.uint64), np.zeros(n, np.uint64), b.trace_offset, m)
+
+    def desc(self):
+        return _abi.MultiseedResults(ptr(self.status, ctypes.c_int32), ptr(self.num_traces, ctypes.c_uint32),
+                                     ptr(self.trace_score, ctypes.c_int32), ptr(self.trace_start, ctypes.c_uint64),
+                                     ptr(self.trace_len, ctypes.c_uint32), ptr(self.trace_items, ctypes.c_uint64),
+                                     ptr(self.cell_steps, ctypes.c_uint64))
+
+    def traces(self, i: int):
+        """Read i's traces as (score, packed items), in the DP's order."""
+        out = []
+        for t in range(int(self.num_traces[i])):
+            k = i * self.max_traces + t
+            o = int(self.trace_offset[i] + self.trace_start[k])
+            out.append((int(self.trace_score[k]), self.trace_items[o:o + int(self.trace_len[k])]))
+        return out
+
+
 class DeviceGraph:
     """AlignmentGraph arrays resident in HBM (ga_graph_upload)."""
 
@@ -214,6 +296,15 @@ class Extender:
 
     def extend(self, params: ExtendParams, seqs, bignodes, offsets) -> BatchResult:
         return self.run(params, pack_batch(self.dgraph.graph, seqs, bignodes, offsets))
+
+    def multiseed(self, params: ExtendParams, batch: MultiseedBatch) -> MultiseedResult:
+        """ga_multiseed_batch: the multiseed DP of every read of the batch."""
+        r = MultiseedResult.alloc(batch)
+        p = params.c()
+        d = batch.desc()
+        rd = r.desc()
+        check(lib().ga_multiseed_batch(self.handle, ctypes.byref(p), ctypes.byref(d), ctypes.byref(rd)))
+        return r
 
     def launch_shape(self) -> LaunchShape:
         sh = LaunchShape()

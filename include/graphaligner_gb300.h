@@ -163,6 +163,12 @@ typedef struct ga_multiseed_results {
     uint64_t* cell_steps;             /* [num] or NULL */
 } ga_multiseed_results;
 
+/* Host buffers in and out, like ga_extend_batch.  Seeds outside the graph or their read, or
+ * out of slice order, are GA_ERR_ARGUMENT.  A read whose traces outgrow trace_capacity or
+ * max_traces reports GA_CAPACITY; the caller may run it again with more room. */
+int ga_multiseed_batch(ga_extender_t ext, const ga_extend_params* params,
+                       const ga_multiseed_batch_desc* batch, ga_multiseed_results* results);
+
 /* Device-resident variant: every pointer in batch/results is a device pointer.
  * Work is enqueued on `stream` (a cudaStream_t; NULL = the extender's stream);
  * the call reads the lengths back once to order the work and waits for the
@@ -284,6 +290,7 @@ typedef struct ga_align_params {
     uint8_t  cigar_match_mismatch;
     int32_t  min_alignment_score;
     double   multimap_score_fraction;
+    uint8_t  multiseed_dp;             /* --multiseed-DP 1: one multiseed DP per read instead of the seed loop */
 } ga_align_params;
 
 typedef struct ga_align_stats {
@@ -398,6 +405,7 @@ typedef struct ga_server_stats {
 typedef struct ga_server* ga_server_t;
 /* Starts the worker thread.  The aligner must outlive the server and must not be
  * used by other calls meanwhile. */
+/* GA_ERR_ARGUMENT for an aligner made with multiseed_dp: the loop runs the seed loop. */
 int ga_server_create(ga_aligner_t aligner, const ga_server_params* params, ga_server_t* out);
 /* Copies the read and queues it; returns at once with a ticket (from 1 up). */
 int ga_server_submit(ga_server_t server, const char* name, const uint8_t* seq, uint32_t len, uint64_t* ticket);

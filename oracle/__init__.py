@@ -58,3 +58,17 @@ def extend(graph, params, batch, threads: int = 1):
     if rc != 0:
         raise RuntimeError(f"ora_extend_batch failed: {rc}")
     return r
+
+
+def multiseed(graph, params, batch, threads: int = 1):
+    """Runs ora_multiseed_batch on a graphaligner_gb300.extend.MultiseedBatch; returns a MultiseedResult."""
+    from graphaligner_gb300.extend import MultiseedResult
+    r = MultiseedResult.alloc(batch)
+    d = graph.desc()
+    p = params.c()
+    b = batch.desc()
+    rd = r.desc()
+    rc = lib().ora_multiseed_batch(ctypes.byref(d), ctypes.byref(p), ctypes.byref(b), ctypes.byref(rd), int(threads))
+    if rc != 0:
+        raise RuntimeError(f"ora_multiseed_batch failed: {rc}")
+    return r

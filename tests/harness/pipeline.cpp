@@ -6,10 +6,12 @@
 //   pipeline <graph.gag> <reads.fa> indexdump <k> <w> <discard> <prefix>
 //       the host index build's arrays as raw u64 files <prefix>.keys/.start/.pos (none for
 //       "-"), with its sizes, a checksum per array and the build time on all cores
+//   pipeline <graph.gag> <reads.fa> msseeds|msseedsdbg
+//       per read: name, then the (slice, split node) seeds of prepareSeedsForMultiseeding
 //   pipeline <graph.gag> <reads.fa> walk <k> <w> <discard>
 //       the GPU build's per-node minimizer walk (index_walk.cuh) run on the host, grouped
 //       by k-mer, against the host index build
-//   pipeline <graph.gag> <reads.fa> gaf|gafdbg|gafms|gafmsdbg <bandwidth> <maxcells|->
+//   pipeline <graph.gag> <reads.fa> gaf|gafdbg|gafms|gafmsdbg <bandwidth> <maxcells|-> [threads (gafms*)]
 //   pipeline <graph.gag> <reads.fa> gafreads|gafreadsdbg <bandwidth> <maxcells|-> <threads>
 //       the reference's worker shape (Aligner.cpp:777-785, runComponentMappings :390-606): each
 //       thread takes the next read and runs its seeding and whole seed loop alone, with the
@@ -308,6 +310,26 @@ int main(int argc, char** argv)
                   << " absent_found " << absentFound << "\n";
         return 0;
     }
+    if (mode == "msseeds" || mode == "msseedsdbg")
+    {
+        // per read: getSeeds, then prepareSeedsForMultiseeding's (slice, split node) pairs
+        const bool dbgPreset = mode == "msseedsdbg";
+        gahost::MinimizerIndex idx;
+        gahost::buildMinimizerIndex(graph, dbgPreset ? 19 : 15, dbgPreset ? 30 : 20, 1.0 - (dbgPreset ? 0.0002 : 0.001), idx);
+        std::vector<gahost::KmerMatch> km;
+        std::vector<gahost::SeedHit> seeds;
+        std::vector<uint32_t> slices, nodes;
+        for (const auto& r : reads)
+        {
+            kmerMatchesHost(idx, r.second, km);
+            gahost::selectSeeds(graph, idx, r.second, dbgPreset ? 5 : 10, km, seeds);
+            gahost::prepareMultiseeds(graph, seeds, r.second.size(), slices, nodes);
+            std::cout << r.first << " " << slices.size();
+            for (size_t k = 0; k < slices.size(); k++) std::cout << " " << slices[k] << " " << nodes[k];
+            std::cout << "\n";
+        }
+        return 0;
+    }
     if (mode == "indexdump")
     {
         size_t k = std::stoul(argv[4]), w = std::stoul(argv[5]);
@@ -485,6 +507,8 @@ int main(int argc, char** argv)
         gahost::selectSeeds(graph, idx, in[i].seq, dbg ? 5 : 10, km, in[i].seeds);
     }
     Ctx ctx { &hd.base, ga_extend_params { (uint32_t)bw, 14705, maxCells, 294 } };
+    // gafms / gafmsdbg: the oracle's multiseed DPs and backward extensions on this many threads
+    if (multiseed && argc > 6) ctx.threads = (int)std::stoul(argv[6]);
     gahost::ReadAlignParams p;
     if (dbg) p.seedExtendDensity = 0.002;
     std::vector<gahost::ReadOutput> out;

@@ -61,6 +61,7 @@ def test_null_arguments_are_rejected_before_any_device_call(cuda_lib):
         "ga_aligner_read_bp": (n, n),
         "ga_aligner_stats": (n, n),
         "ga_aligner_index": (n, n, n, n, n),
+        "ga_multiseed_batch": (n, n, n, n),
         "ga_server_create": (n, n, n),
         "ga_server_submit": (n, n, n, 0, n),
         "ga_server_poll": (n, n, 0, n, 0),

@@ -1,0 +1,111 @@
+"""The multiseed DP (--multiseed-DP 1) on the GPU: ga_multiseed_batch against the oracle's
+multiseed DP trace for trace, and ga_align_reads with multiseed_dp against the reference's
+GAF byte for byte."""
+import gzip
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from golden_sets import GOLDEN, graph_file, load_graph  # noqa: E402
+from test_read_pipeline_host import MULTISEED_CASES, harness  # noqa: E402,F401  (the host read-level harness)
+
+pytestmark = pytest.mark.gpu
+
+
+def read_fasta(name):
+    text = gzip.open(os.path.join(GOLDEN, f"{name}.fa.gz"), "rt").read().split("\n")
+    names = [line[1:].split()[0] for line in text if line.startswith(">")]
+    seqs = [line.encode() for line in text if line and not line.startswith(">")]
+    return names, seqs
+
+
+def multiseed_seeds(exe, graph, reads, dbg, tmp_path):
+    """prepareSeedsForMultiseeding's (slice, split node) pairs per read, from the harness."""
+    fa = os.path.join(tmp_path, "reads.fa")
+    open(fa, "wb").write(gzip.open(os.path.join(GOLDEN, f"{reads}.fa.gz")).read())
+    out = subprocess.run([exe, graph_file(graph, str(tmp_path)), fa, "msseedsdbg" if dbg else "msseeds"], check=True,
+                         capture_output=True, text=True).stdout.splitlines()
+    seeds = []
+    for line in out:
+        f = line.split()
+        v = list(map(int, f[2:]))
+        seeds.append([(v[2 * k], v[2 * k + 1]) for k in range(int(f[1]))])
+    return seeds
+
+
+TRACE_CASES = [("vg50k", "vg50k_chimera_reads", False, 10), ("vg50k", "vg50k_reads", False, 5), ("dbg100k", "dbg100k_reads", True, 5)]
+
+
+@pytest.mark.parametrize("graph,reads,dbg,bandwidth", TRACE_CASES)
+def test_gpu_multiseed_traces_match_oracle(cuda_lib, oracle_lib, harness, tmp_path, graph, reads, dbg, bandwidth):  # noqa: F811
+    """Every read's status, number of traces, and each trace's score and packed items (in the
+    reference's order) equal the oracle's multiseed DP: seeds started in their slices, seed-start
+    columns merged into the node columns, local maxima over slices and neighbours, traces that
+    end at a seed start."""
+    from graphaligner_gb300.extend import DeviceGraph, Extender, ExtendParams, MultiseedBatch
+    g = load_graph(graph)
+    _, seqs = read_fasta(reads)
+    seeds = multiseed_seeds(harness[0], graph, reads, dbg, tmp_path)
+    assert len(seeds) == len(seqs)
+    batch = MultiseedBatch.pack(seqs, seeds, max_traces=256, items_per_bp=64)
+    p = ExtendParams(bandwidth=bandwidth, max_cells_per_slice=10000 if dbg else 2**64 - 1)
+    gpu = Extender(DeviceGraph(g)).multiseed(p, batch)
+    cpu = oracle_lib.multiseed(g, p, batch, threads=8)
+    assert (cpu.status == 0).all()
+    assert np.array_equal(gpu.status, cpu.status), np.nonzero(gpu.status != cpu.status)[0][:10]
+    assert np.array_equal(gpu.num_traces, cpu.num_traces)
+    bad = []
+    for i in range(batch.num):
+        for (gs, gi), (cs, ci) in zip(gpu.traces(i), cpu.traces(i)):
+            if gs != cs or not np.array_equal(gi, ci):
+                bad.append(i)
+                break
+    assert not bad, f"reads {bad[:10]} differ"
+    assert int(cpu.num_traces.sum()) > batch.num
+
+
+def test_gpu_multiseed_reports_capacity(cuda_lib, oracle_lib, harness, tmp_path):  # noqa: F811
+    """With room for eight traces per read, the chimeric reads that have more report GA_CAPACITY,
+    as the oracle does, and the others keep their traces."""
+    from graphaligner_gb300.extend import DeviceGraph, Extender, ExtendParams, MultiseedBatch
+    g = load_graph("vg50k")
+    _, seqs = read_fasta("vg50k_chimera_reads")
+    seeds = multiseed_seeds(harness[0], "vg50k", "vg50k_chimera_reads", False, tmp_path)
+    batch = MultiseedBatch.pack(seqs, seeds, max_traces=8, items_per_bp=64)
+    p = ExtendParams(bandwidth=10)
+    gpu = Extender(DeviceGraph(g)).multiseed(p, batch)
+    cpu = oracle_lib.multiseed(g, p, batch, threads=8)
+    assert np.array_equal(gpu.status, cpu.status)
+    assert 0 < int((cpu.status == 3).sum()) < batch.num
+    for i in np.nonzero(cpu.status == 0)[0]:
+        assert [(s, list(t)) for s, t in gpu.traces(int(i))] == [(s, list(t)) for s, t in cpu.traces(int(i))]
+
+
+def test_gpu_multiseed_rejects_bad_seeds(cuda_lib):
+    """Seeds outside the graph, beyond their read or out of slice order are GA_ERR_ARGUMENT."""
+    from graphaligner_gb300._lib import GAError
+    from graphaligner_gb300.extend import DeviceGraph, Extender, ExtendParams, MultiseedBatch
+    g = load_graph("vg50k")
+    x = Extender(DeviceGraph(g))
+    seq = [b"ACGT" * 100]
+    for seeds in ([(0, g.num_nodes)], [(7, 0)], [(2, 0), (1, 0)]):
+        with pytest.raises(GAError, match="seed"):
+            x.multiseed(ExtendParams(bandwidth=10), MultiseedBatch.pack(seq, [seeds]))
+
+
+@pytest.mark.parametrize("graph,reads,mode,bandwidth,gaf", MULTISEED_CASES)
+def test_gpu_multiseed_gaf_matches_reference(cuda_lib, graph, reads, mode, bandwidth, gaf):
+    """ga_align_reads with multiseed_dp: GAF bytes equal to the reference's --multiseed-DP 1."""
+    from graphaligner_gb300.align import Aligner, preset
+    from graphaligner_gb300.extend import DeviceGraph, Extender
+    g = load_graph(graph)
+    names, seqs = read_fasta(reads)
+    dbg = mode.endswith("dbg")
+    a = Aligner(Extender(DeviceGraph(g)), g, preset("dbg" if dbg else "vg", bandwidth=bandwidth, multiseed=True))
+    out = a.align(names, seqs)
+    assert a.stats()["failed_reads"] == 0
+    assert out == gzip.open(os.path.join(GOLDEN, f"{gaf}.gaf.gz"), "rt").read()
