@@ -106,4 +106,6 @@ class MultiseedResults(ctypes.Structure):
         ("trace_len", _u32p),
         ("trace_items", _u64p),
         ("cell_steps", _u64p),
+        ("items_needed", _u64p),
+        ("traces_needed", _u32p),
     ]

@@ -172,6 +172,21 @@ class Aligner:
                                      ptr(pos, ctypes.c_uint64)))
         return info.as_dict(), keys[:info.num_keys], start, pos[:info.num_positions]
 
+    def select_alignments(self, spans, min_alignment_score: int = 0, multimap_score_fraction: float = 0.9):
+        """SelectAlignments on the device (ga_aligner_select_alignments): spans is, per read, a
+        list of (alignmentStart, alignmentEnd, alignmentXScore); returns per read the kept flags."""
+        first = np.zeros(len(spans) + 1, dtype=np.uint64)
+        first[1:] = np.cumsum([len(x) for x in spans], dtype=np.uint64)
+        flat = [a for x in spans for a in x] or [(0, 0, 0.0)]
+        starts = np.array([a[0] for a in flat], dtype=np.uint64)
+        ends = np.array([a[1] for a in flat], dtype=np.uint64)
+        xs = np.array([a[2] for a in flat], dtype=np.float64)
+        keep = np.zeros(len(flat), dtype=np.uint8)
+        check(lib().ga_aligner_select_alignments(self.handle, len(spans), ptr(first, ctypes.c_uint64), ptr(starts, ctypes.c_uint64),
+                                                 ptr(ends, ctypes.c_uint64), ptr(xs, ctypes.c_double), ctypes.c_int32(min_alignment_score),
+                                                 ctypes.c_double(multimap_score_fraction), ptr(keep, ctypes.c_uint8)))
+        return [list(keep[int(first[i]):int(first[i + 1])].astype(bool)) for i in range(len(spans))]
+
     def stats(self) -> dict:
         s = AlignStats()
         check(lib().ga_aligner_stats(self.handle, ctypes.byref(s)))

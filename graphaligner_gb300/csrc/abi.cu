@@ -107,8 +107,8 @@ struct ga_extender
     DevBuf<int32_t> status, score, prevStatus;
     DevBuf<gadev::ExtState> states;        // where the fill left each extension's table
     // multiseed DP staging
-    DevBuf<uint64_t> msSeedOff, msTraceCap, msTraceStart;
-    DevBuf<uint32_t> msSeedSlice, msSeedNode, msNumTraces, msTraceLen;
+    DevBuf<uint64_t> msSeedOff, msTraceCap, msTraceStart, msItemsNeeded;
+    DevBuf<uint32_t> msSeedSlice, msSeedNode, msNumTraces, msTraceLen, msTracesNeeded;
     DevBuf<int32_t> msTraceScore;
 };
 
@@ -548,6 +548,8 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     GA_CUDA(x->status.reserve(n));
     GA_CUDA(x->prevStatus.reserve(n));
     GA_CUDA(x->msNumTraces.reserve(n));
+    GA_CUDA(x->msItemsNeeded.reserve(n));
+    GA_CUDA(x->msTracesNeeded.reserve(n));
     GA_CUDA(x->cellSteps.reserve(n));
     GA_CUDA(x->msTraceScore.reserve(tables));
     GA_CUDA(x->msTraceStart.reserve(tables));
@@ -567,6 +569,8 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     GA_CUDA(cudaMemcpyAsync(x->traceOff.ptr, b->trace_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->msTraceCap.ptr, b->trace_capacity, n * 8ULL, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
+    GA_CUDA(cudaMemsetAsync(x->msItemsNeeded.ptr, 0, n * 8ULL, s));
+    GA_CUDA(cudaMemsetAsync(x->msTracesNeeded.ptr, 0, n * 4ULL, s));
 
     gadev::FillArgs fa {};
     fa.g = x->graph->d;
@@ -608,15 +612,20 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     ta.traceLen = x->msTraceLen.ptr;
     ta.traceItems = x->traceItems.ptr;
     ta.cellSteps = x->cellSteps.ptr;
+    ta.itemsNeeded = x->msItemsNeeded.ptr;
+    ta.tracesNeeded = x->msTracesNeeded.ptr;
 
     x->lastFillMs = 0;
     x->lastLaunches = 0;
     for (int k = 0; k < 3; k++) x->lastRounds[k] = 0;
     const int wpb = 4;
     uint32_t pending = n;
-    // the frontier tables are in the global workspace: the multiseed band holds every seed
-    // start of a slice besides the alignments' own nodes
-    for (int layout = 1; layout < 3; layout++)
+    // The frontier tables are in the global workspace: the multiseed band holds every seed
+    // start of a slice besides the alignments' own nodes.  A read that runs out of room (its
+    // tables, or the arena the batch shares) runs again in the next pass, which starts a fresh
+    // arena; passes go on while they finish reads, then once more with the large tables.
+    int layout = 1;
+    for (int pass = 0; pass < 32; pass++)
     {
         const gadev::Caps caps = layout_caps(layout);
         const uint64_t stride = ga_multiseed_tables_bytes(caps);
@@ -624,11 +633,11 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
         uint64_t fillBlocks = std::min<uint64_t>((uint64_t)x->sms * 4, pendingBlocks);
         fillBlocks = std::max<uint64_t>(1, std::min<uint64_t>(fillBlocks, x->workspaceBytes / stride / wpb));
         const uint64_t traceBlocks = std::min<uint64_t>((uint64_t)x->sms * 6, pendingBlocks);
-        if (layout > 1) GA_CUDA(cudaMemcpyAsync(x->prevStatus.ptr, x->status.ptr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        if (pass > 0) GA_CUDA(cudaMemcpyAsync(x->prevStatus.ptr, x->status.ptr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
         fa.caps = caps;
         fa.workspace = x->workspace;
         fa.workspaceStride = stride;
-        fa.prevStatus = layout > 1 ? x->prevStatus.ptr : nullptr;
+        fa.prevStatus = pass > 0 ? x->prevStatus.ptr : nullptr;
         ta.prevStatus = fa.prevStatus;
         GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), s));
         GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, 2 * sizeof(unsigned long long), s));
@@ -636,7 +645,7 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
         if (ga_launch_multiseed(fa, ta, x->counters, (int)fillBlocks, (int)traceBlocks, wpb, s) != 0)
             return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
         x->lastLaunches += 2;
-        x->lastRounds[layout] = pending;
+        x->lastRounds[layout] += pending;
         GA_CUDA(cudaEventRecord(x->ev[1], s));
         count_status_kernel<<<64, 256, 0, s>>>(x->status.ptr, n, GA_CAPACITY, x->counters + 2);
         GA_CUDA(cudaGetLastError());
@@ -647,8 +656,14 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
         float ms = 0;
         GA_CUDA(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
         x->lastFillMs += ms;
+        const bool progress = capFails < pending;
         pending = capFails;
         if (capFails == 0) break;
+        if (!progress)
+        {
+            if (layout == 2) break;
+            layout = 2;
+        }
     }
     GA_CUDA(cudaMemcpyAsync(r->status, x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->num_traces, x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
@@ -657,6 +672,8 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     GA_CUDA(cudaMemcpyAsync(r->trace_len, x->msTraceLen.ptr, tables * 4, cudaMemcpyDeviceToHost, s));
     if (items) GA_CUDA(cudaMemcpyAsync(r->trace_items, x->traceItems.ptr, items * 8, cudaMemcpyDeviceToHost, s));
     if (r->cell_steps) GA_CUDA(cudaMemcpyAsync(r->cell_steps, x->cellSteps.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
+    if (r->items_needed) GA_CUDA(cudaMemcpyAsync(r->items_needed, x->msItemsNeeded.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
+    if (r->traces_needed) GA_CUDA(cudaMemcpyAsync(r->traces_needed, x->msTracesNeeded.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaStreamSynchronize(s));
     return GA_OK;
 }

@@ -74,19 +74,25 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
     }
 }
 
-// The multiseed DP of a group of reads through ga_multiseed_batch; reads whose traces
-// outgrow their room run again with eight times as much, once.
+// The multiseed DP of a group of reads through ga_multiseed_batch; reads whose traces outgrow
+// their room run again with the room the first run measured for them.
 void ga_aligner_multiseed(void* ctx, const std::vector<gahost::MultiseedRequest>& rq, std::vector<gahost::MultiseedResult>& rs)
 {
     MultiseedLane* m = (MultiseedLane*)ctx;
     const auto t0 = std::chrono::steady_clock::now();
     std::vector<size_t> todo(rq.size());
     for (size_t i = 0; i < rq.size(); i++) todo[i] = i;
-    uint64_t perBp = 16;
-    uint32_t maxTraces = 64;
-    for (int attempt = 0; attempt < 2 && !todo.empty(); attempt++, perBp *= 8, maxTraces *= 8)
+    std::vector<uint64_t> wantItems(rq.size(), 0);
+    std::vector<uint32_t> wantTraces(rq.size(), 0);
+    for (int attempt = 0; attempt < 2 && !todo.empty(); attempt++)
     {
         const size_t n = todo.size();
+        uint32_t maxTraces = 64;
+        if (attempt > 0)
+        {
+            maxTraces = 1;
+            for (size_t k = 0; k < n; k++) maxTraces = std::max(maxTraces, wantTraces[todo[k]]);
+        }
         m->off.assign(n, 0); m->len.assign(n, 0); m->seedOff.assign(n + 1, 0); m->toff.assign(n, 0); m->cap.assign(n, 0);
         m->slices.clear(); m->nodes.clear(); m->blob.clear();
         uint64_t items = 0;
@@ -99,18 +105,19 @@ void ga_aligner_multiseed(void* ctx, const std::vector<gahost::MultiseedRequest>
             m->slices.insert(m->slices.end(), q.slices, q.slices + q.numSeeds);
             m->nodes.insert(m->nodes.end(), q.nodes, q.nodes + q.numSeeds);
             m->seedOff[k + 1] = m->slices.size();
-            m->cap[k] = (uint64_t)q.len * perBp + 4096;
+            m->cap[k] = attempt == 0 ? (uint64_t)q.len * 16 + 4096 : wantItems[todo[k]] + 64;
             m->toff[k] = items;
             items += m->cap[k];
         }
         if (m->blob.empty()) m->blob.push_back(0);
-        m->status.assign(n, 0); m->ntr.assign(n, 0); m->steps.assign(n, 0);
-        m->tscore.assign(n * maxTraces, 0); m->tstart.assign(n * maxTraces, 0); m->tlen.assign(n * maxTraces, 0);
+        m->status.assign(n, 0); m->ntr.assign(n, 0); m->steps.assign(n, 0); m->needItems.assign(n, 0); m->needTraces.assign(n, 0);
+        m->tscore.assign((size_t)n * maxTraces, 0); m->tstart.assign((size_t)n * maxTraces, 0); m->tlen.assign((size_t)n * maxTraces, 0);
         m->items.resize(std::max<uint64_t>(items, 1));
         ga_multiseed_batch_desc b { (uint32_t)n, m->blob.data(), m->off.data(), m->len.data(), m->seedOff.data(),
             m->slices.empty() ? nullptr : m->slices.data(), m->nodes.empty() ? nullptr : m->nodes.data(), m->toff.data(), m->cap.data(),
             maxTraces, m->multimapScoreFraction };
-        ga_multiseed_results r { m->status.data(), m->ntr.data(), m->tscore.data(), m->tstart.data(), m->tlen.data(), m->items.data(), m->steps.data() };
+        ga_multiseed_results r { m->status.data(), m->ntr.data(), m->tscore.data(), m->tstart.data(), m->tlen.data(), m->items.data(), m->steps.data(),
+            m->needItems.data(), m->needTraces.data() };
         const int rc = ga_multiseed_batch(m->ext, m->params, &b, &r);
         std::vector<size_t> again;
         for (size_t k = 0; k < n; k++)
@@ -120,8 +127,10 @@ void ga_aligner_multiseed(void* ctx, const std::vector<gahost::MultiseedRequest>
             out.steps = m->steps[k];
             out.scores.clear();
             out.traces.clear();
-            if (out.status == GA_CAPACITY && attempt == 0 && rc == GA_OK)
+            if (out.status == GA_CAPACITY && attempt == 0 && rc == GA_OK && (m->needItems[k] > 0 || m->needTraces[k] > 0))
             {
+                wantItems[todo[k]] = m->needItems[k];
+                wantTraces[todo[k]] = m->needTraces[k];
                 again.push_back(todo[k]);
                 continue;
             }
@@ -160,6 +169,11 @@ gahost::ReadAlignParams ga_aligner_read_params(const ga_aligner* a)
     rp.minAlignmentScore = a->params.min_alignment_score;
     rp.multimapScoreFraction = a->params.multimap_score_fraction;
     rp.cigarMatchMismatchMerge = a->params.cigar_match_mismatch != 0;
+    // selection and GAF lines on the device
+    rp.gafWrite = ga_gaf_device_write;
+    rp.gafCtx = const_cast<GafDevice*>(&a->gafDev);
+    rp.select = ga_gaf_device_select;
+    rp.selectCtx = const_cast<GafDevice*>(&a->gafDev);
     return rp;
 }
 
@@ -268,6 +282,14 @@ extern "C" int ga_aligner_create(ga_extender_t ext, const ga_host_graph_desc* gr
         return built == -1 ? GA_ERR_ARGUMENT : GA_ERR_CUDA;
     }
     a->indexBuildMs = ms_since(t0);
+    if (ga_gaf_device_init(a->gafDev, *a->graph) != GA_OK)
+    {
+        cudaFree(a->slots);
+        delete a->graph;
+        delete a;
+        ga_set_last_error("ga_aligner_create: uploading the node names failed");
+        return GA_ERR_CUDA;
+    }
     a->capacity = capacity;
     *out = a;
     return GA_OK;

@@ -6,6 +6,7 @@
 #include <vector>
 #include "readalign.h"
 #include "seed_kernel.cuh"
+#include "gaf_format.cuh"
 #include "../../include/graphaligner_gb300.h"
 
 // pinned host staging, grown as needed, never cleared
@@ -81,11 +82,69 @@ struct MultiseedLane
     const ga_extend_params* params = nullptr;
     double multimapScoreFraction = 0.9;
     std::vector<uint8_t> blob;
-    std::vector<uint64_t> off, seedOff, toff, cap, tstart, items, steps;
-    std::vector<uint32_t> len, slices, nodes, ntr, tlen;
+    std::vector<uint64_t> off, seedOff, toff, cap, tstart, items, steps, needItems;
+    std::vector<uint32_t> len, slices, nodes, ntr, tlen, needTraces;
     std::vector<int32_t> status, tscore;
     double ms = 0;
 };
+
+// The device GAF formatter and alignment selection (gaf_device.cu): the graph's node names
+// resident, the staging of one group of lines.
+struct GafDevice
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // node names by nodeLookup index, the bigraph-id lookup, node sizes
+    DevGrow<uint8_t> nodeNames;
+    DevGrow<uint64_t> nodeNameOff;
+    DevGrow<uint32_t> originalSize, idVal;
+    DevGrow<int32_t> idKey;
+    uint64_t idCap = 0;
+    gaf::NamesHost host;                  // the same tables on the host (node sizes for the classification)
+    // one chunk of lines
+    Pinned<uint8_t> hOps, hNames;
+    Pinned<gaf::LineMeta> hMeta;
+    Pinned<int32_t> hEntries;
+    Pinned<uint64_t> hNameOff, hStart;
+    Pinned<uint32_t> hLen32;
+    Pinned<int64_t> hLen;
+    DevGrow<uint8_t> ops, names;
+    DevGrow<gaf::LineMeta> meta;
+    DevGrow<int32_t> entries;
+    DevGrow<uint64_t> nameOff, start;
+    DevGrow<uint32_t> readLen;
+    DevGrow<int64_t> len;
+    DevGrow<char> text;
+    // selection
+    Pinned<uint64_t> hSel;
+    Pinned<double> hScore;
+    Pinned<char> hKeep;
+    DevGrow<uint64_t> sel;
+    DevGrow<double> score;
+    DevGrow<char> keep;
+    std::string lastText;                  // ga_aligner_format_gaf's output
+    std::vector<uint64_t> lastEnds;
+    std::vector<uint8_t> lastFailed;
+    double ms = 0;
+    void release()
+    {
+        nodeNames.release(); nodeNameOff.release(); originalSize.release(); idVal.release(); idKey.release();
+        hOps.release(); hNames.release(); hMeta.release(); hEntries.release(); hNameOff.release(); hStart.release(); hLen32.release(); hLen.release();
+        ops.release(); names.release(); meta.release(); entries.release(); nameOff.release(); start.release(); readLen.release(); len.release();
+        text.release();
+        hSel.release(); hScore.release(); hKeep.release(); sel.release(); score.release(); keep.release();
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+// uploads the graph's names (at aligner creation); GA_OK or an error code
+int ga_gaf_device_init(GafDevice& d, const gahost::HostGraph& g);
+// gahost::GafWriteFn and gahost::SelectFn on the device (ctx = GafDevice*)
+bool ga_gaf_device_write(void* ctx, const std::vector<const std::string*>& names, const std::vector<const gahost::ClassifiedLines*>& reads,
+    std::string& text, std::vector<uint64_t>& readEnd);
+bool ga_gaf_device_select(void* ctx, const std::vector<uint64_t>& first, const std::vector<uint64_t>& start, const std::vector<uint64_t>& end,
+    const std::vector<double>& xscore, int minAlignmentScore, double fractionCutoff, std::vector<char>& keep);
 
 struct ga_aligner
 {
@@ -103,6 +162,7 @@ struct ga_aligner
     cudaStream_t stream = nullptr;
     ExtendLane lanes[2];       // lanes[0] uses ext; lanes[1] an extender made like it on first use
     MultiseedLane multiseed;   // the multiseed DP's calls (on ext)
+    GafDevice gafDev;          // GAF lines and alignment selection on the device
     // k-mer lookup buffers
     DevGrow<uint8_t> dSeq;
     DevGrow<uint64_t> dOff, dMatchOff;
@@ -115,6 +175,7 @@ struct ga_aligner
     {
         dSeq.release(); dOff.release(); dMatchOff.release(); dLen.release(); dCount.release(); dMatch.release();
         hMatch.release();
+        gafDev.release();
     }
 };
 

@@ -1319,6 +1319,8 @@ __device__ __noinline__ void flush32(u64* items, const u64* ring, u32 n, u32 lan
 
 // Trace items go to a 64-entry ring in shared memory (every lane writes every item) and
 // out to the caller's buffer 32 at a time, one item per lane.
+// counting: nothing goes out, the items are only counted (the multiseed traceback measures
+// the room a read needs once its own has run out).
 struct TraceOut
 {
     u64* items;
@@ -1328,6 +1330,7 @@ struct TraceOut
     u32 lane;
     TPos back;
     bool overflow;
+    bool counting = false;
     __device__ __forceinline__ void push(const TPos& p, bool sw)
     {
         if (n >= cap) { overflow = true; return; }
@@ -1335,11 +1338,12 @@ struct TraceOut
         ring[n & 63] = (u64)p.node | ((u64)(p.off & 63) << 32) | ((u64)(sw ? 1 : 0) << 38) | (sp1 << 39);
         n++;
         back = p;
-        if ((n & 31) == 0) flush32(items, ring, n, lane);
+        if (!counting && (n & 31) == 0) flush32(items, ring, n, lane);
     }
     // writes the items of the last, partial group of 32
     __device__ __forceinline__ void finish()
     {
+        if (counting) return;
         const u32 k = (n & ~31u) + lane;
         if (k < n) items[k] = ring[k & 63];
         __syncwarp();
@@ -1350,8 +1354,8 @@ __device__ __forceinline__ u32 mod64(int64_t seq) { return (u32)((u64)seq & 63);
 
 // checkBacktraceCircularity (Common.h:760-768): the newest item must not repeat an
 // earlier item of the same read position.  Items still in the ring are read there, older
-// ones from the written output.
-__device__ __noinline__ bool trace_circular(const u64* items, const u64* ring, u32 n)
+// ones from the written output (a counting walk checks the ring only).
+__device__ __noinline__ bool trace_circular(const u64* items, const u64* ring, u32 n, bool ringOnly = false)
 {
     if (n < 2) return false;
     const u64 keyMask = ~(1ULL << 38);
@@ -1359,6 +1363,7 @@ __device__ __noinline__ bool trace_circular(const u64* items, const u64* ring, u
 #pragma unroll 1
     for (int k = (int)n - 2; k >= 0; k--)
     {
+        if (ringOnly && (u32)k + 63 < n) return false;
         const u64 x = (u32)k + 63 >= n ? ring[k & 63] : items[k];
         if ((x & keyMask) == (last & keyMask)) return true;
         if ((x >> 39) != (last >> 39)) return false;
@@ -1751,7 +1756,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
 {
     int err = 0;
     Col* cols = w.cols;
-    const u64 guardMax = (u64)to.cap * 4 + 1024;
+    const u64 guardMax = (u64)(to.counting ? (1u << 26) : to.cap) * 4 + 1024;
     resultScore = startScore;
     to.push(start, false);
     // the extraSlice of the current node-slice and its score at a row
@@ -1801,7 +1806,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
             if (tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == xv(mod64(bt.pos.seq))) break;
             if (Multi && tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == ws_before(extra)) break;
             to.push(bt.pos, bt.sw);
-            if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
+            if (!to.overflow && trace_circular(to.items, to.ring, to.n, to.counting)) { err = GA_ASSERT; break; }
             continue;
         }
         if (row == 0)
@@ -1859,7 +1864,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
             if (!tpos_eq(p, to.back)) to.push(p, false);
             if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
             to.push(second.pos, second.sw);
-            if (!to.overflow && trace_circular(to.items, to.ring, to.n)) { err = GA_ASSERT; break; }
+            if (!to.overflow && trace_circular(to.items, to.ring, to.n, to.counting)) { err = GA_ASSERT; break; }
             continue;
         }
         // pickBacktraceInside (Common.h:770-815).  The four neighbouring scores are
@@ -2049,6 +2054,9 @@ __device__ void trace_multiseed(const MultiTraceArgs& a, u32 r, const ExtState& 
     u64 used = 0;
     u32 nt = 0;
     int err = 0;
+    bool counting = false;
+    u64 neededItems = 0;
+    u32 neededTraces = 0;
     Col* cols = w.cols;
     const u32 last = st.committed - 1;
 #pragma unroll 1
@@ -2125,24 +2133,37 @@ __device__ void trace_multiseed(const MultiTraceArgs& a, u32 r, const ExtState& 
             const int gOff = __reduce_max_sync(kFull, candOff);
             const u32 gCol = __reduce_min_sync(kFull, candOff == gOff ? candCol : 0xffffffffu);
             if (gOff < 0 || j + gOff >= (int64_t)seqLen) { err = GA_ASSERT; break; }
-            if (nt >= a.maxTraces) { err = GA_CAPACITY; break; }
             const TPos start = TPos { node, gCol, j + gOff };
             const i32 startScore = col_value(cols[gCol], gOff);
+            // once the read's room for traces or items has run out, the rest are only counted
+            if (!counting && nt >= a.maxTraces) counting = true;
             TraceOut to;
             to.items = out + used;
             to.ring = w.ring;
-            to.cap = (u32)(cap - used < 0xffffffffULL ? cap - used : 0xffffffffULL);
-            to.n = 0;
             to.lane = lane;
-            to.overflow = false;
             i32 traceScore = 0;
-            err = trace_walk<true>(g, a.cost, seq, seqLen, st.committed, t, to, w, start, startScore, traceScore, lane);
-            to.finish();
+#pragma unroll 1
+            for (int attempt = 0; attempt < 2; attempt++)
+            {
+                to.counting = counting;
+                to.cap = counting ? 0xffffffffu : (u32)(cap - used < 0xffffffffULL ? cap - used : 0xffffffffULL);
+                to.n = 0;
+                to.overflow = false;
+                err = trace_walk<true>(g, a.cost, seq, seqLen, st.committed, t, to, w, start, startScore, traceScore, lane);
+                to.finish();
+                if (err || !to.overflow || counting) break;
+                counting = true;   // the trace did not fit: count it again from its start
+            }
             if (!err && to.overflow) err = GA_CAPACITY;
             if (err) break;
             const int64_t traceEnd = start.seq, traceStart = to.back.seq;
             if (traceStart < 0 || traceEnd < traceStart) { err = GA_ASSERT; break; }
-            if (lane == 0)
+            if (counting)
+            {
+                neededItems += to.n;
+                neededTraces++;
+            }
+            else if (lane == 0)
             {
                 const u64 slot = (u64)r * a.maxTraces + nt;
                 a.traceScore[slot] = traceScore;
@@ -2153,14 +2174,21 @@ __device__ void trace_multiseed(const MultiTraceArgs& a, u32 r, const ExtState& 
 #pragma unroll 1
             for (u32 i = startSlice + lane; i < cs; i += 32) sliceMax[i] = imax(sliceMax[i], score);
             __syncwarp();
-            used += to.n;
-            nt++;
+            if (!counting)
+            {
+                used += to.n;
+                nt++;
+            }
         }
     }
+    if (!err && counting) err = GA_CAPACITY;
     if (lane == 0)
     {
         a.status[r] = err ? err : GA_OK;
         a.numTraces[r] = err ? 0 : nt;
+        // the room the read needs, when only the room ran out
+        if (a.itemsNeeded) a.itemsNeeded[r] = counting ? used + neededItems : 0;
+        if (a.tracesNeeded) a.tracesNeeded[r] = counting ? nt + neededTraces : 0;
     }
 }
 

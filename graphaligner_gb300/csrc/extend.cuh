@@ -148,6 +148,8 @@ struct MultiTraceArgs
     u32* traceLen;
     u64* traceItems;
     u64* cellSteps;
+    u64* itemsNeeded;      // [num] or null: when the traces outgrow the read's room, the room they need
+    u32* tracesNeeded;
 };
 
 }

@@ -747,9 +747,11 @@ static void finishSeed(const HostGraph& g, const ReadAlignParams& p, ReadState& 
     }
 }
 
-// Aligner.cpp:505-566: selection, bp aligned, order by X-score, GAF
-static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState& r, ReadOutput& o)
+// Aligner.cpp:505-548: selection (the kept ones of keep, when given), bp aligned, order by
+// X-score; the lines to write in `lines`
+static void finalizeSelect(const ReadAlignParams& p, ReadState& r, ReadOutput& o, std::vector<AlignmentItem>& lines, const char* keep = nullptr)
 {
+    lines.clear();
     if (r.failed)
     {
         o.failed = true;
@@ -758,7 +760,13 @@ static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState
     if (r.alignments.empty()) return;
     try
     {
-        std::vector<AlignmentItem> alns = selectAlignments(r.alignments, p.minAlignmentScore, p.multimapScoreFraction);
+        std::vector<AlignmentItem> alns;
+        if (keep)
+        {
+            for (size_t k = 0; k < r.alignments.size(); k++)
+                if (keep[k]) alns.push_back(r.alignments[k]);
+        }
+        else alns = selectAlignments(r.alignments, p.minAlignmentScore, p.multimapScoreFraction);
         if (alns.empty()) return;
         std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentStart < b.alignmentStart; });
         size_t bpAligned = 0, lastEnd = 0;
@@ -772,23 +780,202 @@ static void finalizeRead(const HostGraph& g, const ReadAlignParams& p, ReadState
             }
         }
         std::sort(alns.begin(), alns.end(), [](const AlignmentItem& a, const AlignmentItem& b) { return a.alignmentXScore > b.alignmentXScore; });
-        std::string text;
-        for (auto& a : alns)
-        {
-            text += gafLine(g, r.name, r.seq, *a.trace, a.alignmentXScore, a.mappingQuality, p.cigarMatchMismatchMerge);
-            text += '\n';
-        }
-        o.gaf = std::move(text);
         o.bpAligned = bpAligned;
         o.alignments = alns.size();
+        lines = std::move(alns);
     }
     catch (const ReadFailure&)
     {
         o.failed = true;
-        o.gaf.clear();
         o.bpAligned = 0;
         o.alignments = 0;
+        lines.clear();
     }
+}
+
+static void failOutput(ReadOutput& o);
+
+// finalizeSelect for a group of finished reads, the selection by the hook when one is set
+static void finalizeGroup(const ReadAlignParams& p, const std::vector<ReadState*>& rs, const std::vector<ReadOutput*>& os,
+    std::vector<std::vector<AlignmentItem>>& lines, bool hostSelect = false)
+{
+    const size_t n = rs.size();
+    lines.assign(n, {});
+    if (!p.select || hostSelect)
+    {
+        parallelFor(n, [&](size_t i) { finalizeSelect(p, *rs[i], *os[i], lines[i]); });
+        return;
+    }
+    std::vector<uint64_t> first(n + 1, 0), start, end;
+    std::vector<double> xscore;
+    for (size_t i = 0; i < n; i++)
+    {
+        if (!rs[i]->failed)
+            for (const auto& a : rs[i]->alignments)
+            {
+                start.push_back(a.alignmentStart);
+                end.push_back(a.alignmentEnd);
+                xscore.push_back(a.alignmentXScore);
+            }
+        first[i + 1] = start.size();
+    }
+    std::vector<char> keep(start.size(), 0);
+    if (!start.empty() && !p.select(p.selectCtx, first, start, end, xscore, p.minAlignmentScore, p.multimapScoreFraction, keep))
+    {
+        for (size_t i = 0; i < n; i++)
+        {
+            rs[i]->failed = true;
+            failOutput(*os[i]);
+        }
+        return;
+    }
+    parallelFor(n, [&](size_t i) { finalizeSelect(p, *rs[i], *os[i], lines[i], keep.data() + first[i]); });
+}
+
+static void failOutput(ReadOutput& o)
+{
+    o.failed = true;
+    o.gaf.clear();
+    o.bpAligned = 0;
+    o.alignments = 0;
+}
+
+// Aligner.cpp:549-566: the GAF lines of finished reads.  Without a writer hook, gafLine on the
+// host's cores; with one, each line's trace is walked on the host's cores (gaf::classify_line)
+// into the read's pending lines, and the hook writes the text (at once, or later through
+// writeFinished when `write` is false).
+static void formatFinished(const HostGraph& g, const ReadAlignParams& p, const std::vector<ReadState*>& rs, const std::vector<ReadOutput*>& os,
+    const std::vector<std::vector<AlignmentItem>>& lines, bool write = true)
+{
+    const size_t n = rs.size();
+    if (!p.gafWrite)
+    {
+        parallelFor(n, [&](size_t i)
+        {
+            if (lines[i].empty()) return;
+            try
+            {
+                std::string text;
+                for (const auto& a : lines[i])
+                {
+                    text += gafLine(g, rs[i]->name, rs[i]->seq, *a.trace, a.alignmentXScore, a.mappingQuality, p.cigarMatchMismatchMerge);
+                    text += '\n';
+                }
+                os[i]->gaf = std::move(text);
+            }
+            catch (const ReadFailure&)
+            {
+                failOutput(*os[i]);
+            }
+        });
+        return;
+    }
+    auto sizeOf = [&g](int32_t bignode) -> uint64_t
+    {
+        auto f = g.lookupIndex.find(bignode);
+        return f == g.lookupIndex.end() ? 0 : g.originalSize[f->second];
+    };
+    parallelFor(n, [&](size_t i)
+    {
+        if (lines[i].empty()) return;
+        ClassifiedLines& c = os[i]->pending;
+        size_t items = 0;
+        for (const auto& a : lines[i]) items += a.trace->trace.size();
+        c.lines.resize(lines[i].size());
+        c.ops.resize(items);
+        c.entries.clear();
+        std::vector<int32_t> entries;
+        uint64_t op = 0;
+        for (size_t k = 0; k < lines[i].size(); k++)
+        {
+            const AlignmentItem& a = lines[i][k];
+            const auto& t = a.trace->trace;
+            auto item = [&t](uint32_t q) -> gaf::Item
+            {
+                const TraceItem& x = t[q];
+                return gaf::Item { (int32_t)x.node, (uint32_t)x.nodeOffset, (uint32_t)x.seqPos, (uint8_t)(x.nodeSwitch ? 1 : 0),
+                    (uint8_t)x.seqChar, (uint8_t)x.graphChar, 0 };
+            };
+            entries.resize(std::max<size_t>(t.size(), 1));
+            gaf::LineMeta& m = c.lines[k];
+            if (!gaf::classify_line(item, (uint32_t)t.size(), (uint32_t)rs[i]->seq.size(), p.cigarMatchMismatchMerge, sizeOf, m, c.ops.data() + op,
+                    entries.data()))
+            {
+                c = ClassifiedLines {};
+                failOutput(*os[i]);
+                return;
+            }
+            m.op = op;
+            m.entry = c.entries.size();
+            m.read = 0;
+            m.xscore100 = (int32_t)std::llround(a.alignmentXScore * 100);
+            m.mapq = a.mappingQuality;
+            c.entries.insert(c.entries.end(), entries.begin(), entries.begin() + m.entries);
+            op += t.size();
+        }
+    });
+    if (!write) return;
+    std::vector<const std::string*> names;
+    std::vector<const ClassifiedLines*> reads;
+    std::vector<size_t> which;
+    for (size_t i = 0; i < n; i++)
+    {
+        if (os[i]->pending.lines.empty()) continue;
+        names.push_back(&rs[i]->name);
+        reads.push_back(&os[i]->pending);
+        which.push_back(i);
+    }
+    if (reads.empty()) return;
+    std::string text;
+    std::vector<uint64_t> readEnd;
+    const bool ok = p.gafWrite(p.gafCtx, names, reads, text, readEnd);
+    parallelFor(which.size(), [&](size_t k)
+    {
+        ReadOutput& o = *os[which[k]];
+        if (!ok)
+        {
+            failOutput(o);
+        }
+        else
+        {
+            const uint64_t from = k == 0 ? 0 : readEnd[k - 1];
+            o.gaf.assign(text.data() + from, readEnd[k] - from);
+        }
+        o.pending = ClassifiedLines {};
+    });
+}
+
+void writeFinished(const ReadAlignParams& p, std::vector<std::pair<uint64_t, ReadOutput>>& outs, const std::vector<const std::string*>& names)
+{
+    if (!p.gafWrite) return;
+    std::vector<const std::string*> nm;
+    std::vector<const ClassifiedLines*> reads;
+    std::vector<size_t> which;
+    for (size_t i = 0; i < outs.size(); i++)
+    {
+        if (outs[i].second.pending.lines.empty()) continue;
+        nm.push_back(names[i]);
+        reads.push_back(&outs[i].second.pending);
+        which.push_back(i);
+    }
+    if (reads.empty()) return;
+    std::string text;
+    std::vector<uint64_t> readEnd;
+    const bool ok = p.gafWrite(p.gafCtx, nm, reads, text, readEnd);
+    parallelFor(which.size(), [&](size_t k)
+    {
+        ReadOutput& o = outs[which[k]].second;
+        if (!ok)
+        {
+            failOutput(o);
+        }
+        else
+        {
+            const uint64_t from = k == 0 ? 0 : readEnd[k - 1];
+            o.gaf.assign(text.data() + from, readEnd[k] - from);
+        }
+        o.pending = ClassifiedLines {};
+    });
 }
 
 // ------------------------------------------------------------------ multiseed DP
@@ -1117,11 +1304,19 @@ void alignBatchMultiseed(const HostGraph& g, const ReadAlignParams& p, std::vect
     });
     stats.consumeMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     t0 = std::chrono::steady_clock::now();
-    parallelFor(n, [&](size_t i)
     {
-        if (out[i].noSeeds) return;
-        finalizeRead(g, p, ms[i].r, out[i]);
-    });
+        // reads without seeds have no alignments and stay as they are
+        std::vector<ReadState*> rsp(n);
+        std::vector<ReadOutput*> osp(n);
+        for (size_t i = 0; i < n; i++)
+        {
+            rsp[i] = &ms[i].r;
+            osp[i] = &out[i];
+        }
+        std::vector<std::vector<AlignmentItem>> lines;
+        finalizeGroup(p, rsp, osp, lines);
+        formatFinished(g, p, rsp, osp, lines);
+    }
     for (size_t i = 0; i < n; i++)
     {
         stats.bpAligned += out[i].bpAligned;
@@ -1525,19 +1720,26 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
     stats.consumeMs += msSince(t0);
 }
 
-void SeedLoopPool::takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats)
+void SeedLoopPool::takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats, bool overlapped)
 {
     const auto t0 = std::chrono::steady_clock::now();
     auto& fin = impl->finished;
     const size_t base = out.size();
     out.resize(base + fin.size());
-    parallelFor(fin.size(), [&](size_t i)
     {
-        ReadOutput o;
-        o.noSeeds = fin[i].noSeeds;
-        finalizeRead(impl->g, impl->p, *fin[i].r, o);
-        out[base + i] = std::make_pair(fin[i].tag, std::move(o));
-    });
+        std::vector<ReadState*> rsp(fin.size());
+        std::vector<ReadOutput*> osp(fin.size());
+        for (size_t i = 0; i < fin.size(); i++)
+        {
+            out[base + i].first = fin[i].tag;
+            out[base + i].second.noSeeds = fin[i].noSeeds;
+            rsp[i] = fin[i].r.get();
+            osp[i] = &out[base + i].second;
+        }
+        std::vector<std::vector<AlignmentItem>> lines;
+        finalizeGroup(impl->p, rsp, osp, lines, overlapped);
+        formatFinished(impl->g, impl->p, rsp, osp, lines, !overlapped);
+    }
     for (size_t i = base; i < out.size(); i++)
     {
         if (out[i].second.failed) stats.failedReads++;
@@ -1578,6 +1780,8 @@ void alignBatchTwoLanes(const HostGraph& g, const ReadAlignParams& p, std::vecto
     std::stable_sort(byLen.begin(), byLen.end(), [&](size_t a, size_t b) { return reads[a].seq.size() > reads[b].seq.size(); });
     std::vector<ReadInput> part[2];
     std::vector<uint64_t> tags[2];
+    std::vector<std::string> nameOf(reads.size());     // the reads are moved into the pools
+    for (size_t i = 0; i < reads.size(); i++) nameOf[i] = reads[i].name;
     for (size_t k = 0; k < byLen.size(); k++)
     {
         part[k & 1].push_back(std::move(reads[byLen[k]]));
@@ -1598,19 +1802,22 @@ void alignBatchTwoLanes(const HostGraph& g, const ReadAlignParams& p, std::vecto
         rs[k].assign(rq[k].size(), ExtensionResult {});
         if (!rq[k].empty()) worker[k] = std::thread([&, k]() { extend(ctx[k], rq[k], rs[k]); });
     };
+    // finished reads are selected and their GAF lines walked between rounds on the host's
+    // cores, while the other group's extensions hold the GPU; a GAF writer hook writes all the
+    // text at the end
     auto finish = [&](int k)
     {
         if (worker[k].joinable()) worker[k].join();
         pool[k]->consume(rs[k], stats);
-        pool[k]->takeFinished(done, stats);
+        pool[k]->takeFinished(done, stats, true);
         active[k] = pool[k]->collect(rq[k]);
-        pool[k]->takeFinished(done, stats);
+        pool[k]->takeFinished(done, stats, true);
     };
     active[0] = pool0.collect(rq[0]);
-    pool0.takeFinished(done, stats);
+    pool0.takeFinished(done, stats, true);
     if (active[0]) launch(0);
     active[1] = pool1.collect(rq[1]);
-    pool1.takeFinished(done, stats);
+    pool1.takeFinished(done, stats, true);
     while (active[0] || active[1])
     {
         // group 1 goes to the GPU while the host finishes group 0, and the other way round
@@ -1623,6 +1830,15 @@ void alignBatchTwoLanes(const HostGraph& g, const ReadAlignParams& p, std::vecto
         if (active[1]) finish(1);
     }
     for (auto& t : worker) if (t.joinable()) t.join();
+    pool0.takeFinished(done, stats, true);
+    pool1.takeFinished(done, stats, true);
+    {
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<const std::string*> names(done.size());
+        for (size_t i = 0; i < done.size(); i++) names[i] = &nameOf[done[i].first];
+        writeFinished(p, done, names);
+        stats.finishMs += msSince(t0);
+    }
     for (auto& d : done) out[d.first] = std::move(d.second);
 }
 

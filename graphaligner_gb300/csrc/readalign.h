@@ -1,5 +1,6 @@
 // Host-side types of the read-level layer (readalign.cpp, seeding.cpp).
 #pragma once
+#include "gaf_format.cuh"
 #include <cstdint>
 #include <functional>
 #include <memory>
@@ -80,6 +81,29 @@ struct AlignmentItem
     int mappingQuality = 255;
 };
 
+// A finished read's GAF lines walked on the host (gaf::classify_line), their text not yet
+// written: one record per line, one edit-op byte per trace item, the node-path entries (the
+// records' op and entry offsets count from this read's arrays).
+struct ClassifiedLines
+{
+    std::vector<gaf::LineMeta> lines;
+    std::vector<uint8_t> ops;
+    std::vector<int32_t> entries;
+};
+
+// Writes the classified GAF lines of a group of reads (the text half of traceToAlignment,
+// GraphAlignerGAFAlignment.h:37-200): read i's lines, each with its newline, back to back into
+// text; readEnd[i] = where read i's text ends.  False when it could not run (every read of the
+// group then fails).
+typedef bool (*GafWriteFn)(void* ctx, const std::vector<const std::string*>& names, const std::vector<const ClassifiedLines*>& reads,
+    std::string& text, std::vector<uint64_t>& readEnd);
+
+// AlignmentSelection::SelectAlignments (AlignmentSelection.cpp:31-95) over the alignments of
+// a group of reads: read i's are [first[i], first[i+1]) of start/end/xscore, keep[k] = kept.
+// False when it could not run (every read of the group then fails).
+typedef bool (*SelectFn)(void* ctx, const std::vector<uint64_t>& first, const std::vector<uint64_t>& start, const std::vector<uint64_t>& end,
+    const std::vector<double>& xscore, int minAlignmentScore, double fractionCutoff, std::vector<char>& keep);
+
 struct ReadAlignParams
 {
     bool sloppy = true;
@@ -96,6 +120,13 @@ struct ReadAlignParams
     // in order on the read's true state, extends exactly that seed next
     double speculationSteps = 6e7;
     size_t maxSpeculation = 8;
+    // GAF lines of finished reads: the host's gafLine when null; else the lines are walked on
+    // the host (gaf::classify_line) and this hook writes their text (the product's device writer)
+    GafWriteFn gafWrite = nullptr;
+    void* gafCtx = nullptr;
+    // the selection of finished reads' alignments: selectAlignments on the host when null
+    SelectFn select = nullptr;
+    void* selectCtx = nullptr;
 };
 
 struct ReadInput
@@ -112,6 +143,7 @@ struct ReadOutput
     size_t alignments = 0;
     bool failed = false;     // an assert would have dropped the read
     bool noSeeds = false;
+    ClassifiedLines pending; // with a GAF writer: lines waiting for writeFinished
 };
 
 struct BatchStats
@@ -175,12 +207,17 @@ public:
     bool collect(std::vector<ExtensionRequest>& requests);
     // results of the requests of the last collect, in the same order
     void consume(const std::vector<ExtensionResult>& results, BatchStats& stats);
-    // selection, aligned bp and GAF of the finished reads (Aligner.cpp:505-566), with their tags
-    void takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats);
+    // selection, aligned bp and GAF of the finished reads (Aligner.cpp:505-566), with their tags.
+    // overlapped: the call runs while another group's extensions hold the GPU, so the
+    // selection runs on the host and the GAF text is left for writeFinished.
+    void takeFinished(std::vector<std::pair<uint64_t, ReadOutput>>& out, BatchStats& stats, bool overlapped = false);
 private:
     struct Impl;
     std::unique_ptr<Impl> impl;
 };
+
+// Writes the GAF text of outputs whose lines wait (ReadOutput::pending), in one call of the writer.
+void writeFinished(const ReadAlignParams& p, std::vector<std::pair<uint64_t, ReadOutput>>& outs, const std::vector<const std::string*>& names);
 
 void alignBatch(const HostGraph& g, const ReadAlignParams& p, std::vector<ReadInput>& reads, ExtendFn extend, void* ctx,
     std::vector<ReadOutput>& out, BatchStats& stats);

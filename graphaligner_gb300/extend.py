@@ -205,19 +205,23 @@ class MultiseedResult:
     cell_steps: np.ndarray
     trace_offset: np.ndarray
     max_traces: int
+    items_needed: np.ndarray
+    traces_needed: np.ndarray
 
     @classmethod
     def alloc(cls, b: MultiseedBatch):
         n, m = b.num, b.max_traces
         items = int(b.trace_offset[-1] + b.trace_capacity[-1]) if n else 1
         return cls(np.zeros(n, np.int32), np.zeros(n, np.uint32), np.zeros(n * m, np.int32), np.zeros(n * m, np.uint64),
-                   np.zeros(n * m, np.uint32), np.zeros(max(items, 1), np.uint64), np.zeros(n, np.uint64), b.trace_offset, m)
+                   np.zeros(n * m, np.uint32), np.zeros(max(items, 1), np.uint64), np.zeros(n, np.uint64), b.trace_offset, m,
+                   np.zeros(n, np.uint64), np.zeros(n, np.uint32))
 
     def desc(self):
         return _abi.MultiseedResults(ptr(self.status, ctypes.c_int32), ptr(self.num_traces, ctypes.c_uint32),
                                      ptr(self.trace_score, ctypes.c_int32), ptr(self.trace_start, ctypes.c_uint64),
                                      ptr(self.trace_len, ctypes.c_uint32), ptr(self.trace_items, ctypes.c_uint64),
-                                     ptr(self.cell_steps, ctypes.c_uint64))
+                                     ptr(self.cell_steps, ctypes.c_uint64), ptr(self.items_needed, ctypes.c_uint64),
+                                     ptr(self.traces_needed, ctypes.c_uint32))
 
     def traces(self, i: int):
         """Read i's traces as (score, packed items), in the DP's order."""

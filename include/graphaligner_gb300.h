@@ -161,11 +161,14 @@ typedef struct ga_multiseed_results {
     uint32_t* trace_len;              /* [num * max_traces] items */
     uint64_t* trace_items;            /* packed items (GA_TRACE_* layout) */
     uint64_t* cell_steps;             /* [num] or NULL */
+    uint64_t* items_needed;           /* [num] or NULL: for a read whose traces outgrew its room (GA_CAPACITY), */
+    uint32_t* traces_needed;          /* [num] or NULL: the items and traces it needs; 0 for other statuses */
 } ga_multiseed_results;
 
 /* Host buffers in and out, like ga_extend_batch.  Seeds outside the graph or their read, or
  * out of slice order, are GA_ERR_ARGUMENT.  A read whose traces outgrow trace_capacity or
- * max_traces reports GA_CAPACITY; the caller may run it again with more room. */
+ * max_traces reports GA_CAPACITY with the room it needs in items_needed / traces_needed; run
+ * it again with that room. */
 int ga_multiseed_batch(ga_extender_t ext, const ga_extend_params* params,
                        const ga_multiseed_batch_desc* batch, ga_multiseed_results* results);
 
@@ -356,6 +359,41 @@ typedef struct ga_seed {
  * seed_offsets[i + 1]); both arrays stay valid until the next call on this aligner. */
 int ga_aligner_get_seeds(ga_aligner_t aligner, uint32_t num_reads, const uint8_t* seq, const uint64_t* seq_offset,
                          const uint32_t* seq_len, const ga_seed** seeds, const uint64_t** seed_offsets);
+/* ---- GAF lines and alignment selection on the device ----
+ * What ga_align_reads does after the seed loop, for callers that keep their own: the
+ * selection of one read's alignments (AlignmentSelection::SelectAlignments,
+ * src/AlignmentSelection.cpp:31-95, without the E-value filter) and the GAF line of an
+ * alignment (GraphAlignerGAFAlignment::traceToAlignment, src/GraphAlignerGAFAlignment.h:37-200).
+ * One trace item after the fix-ups (fixForwardTraceSeqPos / fixReverseTraceSeqPosAndOrder):
+ * bigraph node id, offset in it, read position, nodeSwitch and the two characters. */
+typedef struct ga_gaf_item {
+    int32_t  node;
+    uint32_t node_offset;
+    uint32_t seq_pos;
+    uint8_t  node_switch;
+    uint8_t  seq_char;
+    uint8_t  graph_char;
+    uint8_t  pad;
+} ga_gaf_item;
+typedef struct ga_gaf_line {
+    uint64_t first_item;               /* the trace is items[first_item .. +item_count) */
+    uint32_t item_count;
+    uint32_t read;                     /* index into read_names / read_lens */
+    int32_t  xscore100;                /* alignmentXScore * 100; -100 leaves AS:f out, as the reference does for -1 */
+    int32_t  mapq;                     /* mappingQuality */
+} ga_gaf_line;
+/* The lines, each with its newline, into one text kept by the aligner until the next call;
+ * line_ends[k] = where line k's newline ends; failed[k] = 1 where the reference would have
+ * asserted (the line is then a lone newline). */
+int ga_aligner_format_gaf(ga_aligner_t aligner, uint32_t num_lines, const ga_gaf_line* lines, uint64_t num_items,
+                          const ga_gaf_item* items, uint32_t num_reads, const char* const* read_names, const uint32_t* read_lens,
+                          uint8_t cigar_match_mismatch, const char** text, uint64_t* bytes, const uint64_t** line_ends,
+                          const uint8_t** failed);
+/* Read r's alignments are [first[r], first[r+1]) of starts, ends (alignmentStart / End),
+ * xscores (alignmentXScore) and keep; keep[k] = 1 for the alignments SelectAlignments keeps. */
+int ga_aligner_select_alignments(ga_aligner_t aligner, uint32_t num_reads, const uint64_t* first, const uint64_t* starts,
+                                 const uint64_t* ends, const double* xscores, int32_t min_alignment_score,
+                                 double multimap_score_fraction, uint8_t* keep);
 /* GAF lines of the last ga_align_reads call, reads in input order; valid until the next call. */
 int ga_aligner_gaf(ga_aligner_t aligner, const char** text, uint64_t* bytes);
 /* Per-read bp aligned of the last call. */

@@ -1635,6 +1635,8 @@ extern "C" int ora_multiseed_batch(const ga_graph_desc* graph, const ga_extend_p
 				st = ora::State { graph->num_nodes };
 			}
 			if (results->cell_steps) results->cell_steps[i] = steps;
+			if (results->items_needed) results->items_needed[i] = 0;
+			if (results->traces_needed) results->traces_needed[i] = 0;
 			uint32_t nt = 0;
 			uint64_t used = 0;
 			if (status == GA_OK)
@@ -1644,6 +1646,8 @@ extern "C" int ora_multiseed_batch(const ga_graph_desc* graph, const ga_extend_p
 				if (traces.size() > batch->max_traces || total > batch->trace_capacity[i])
 				{
 					status = GA_CAPACITY;
+					if (results->items_needed) results->items_needed[i] = total;
+					if (results->traces_needed) results->traces_needed[i] = (uint32_t)traces.size();
 				}
 				else
 				{

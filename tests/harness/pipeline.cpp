@@ -30,6 +30,8 @@
 #include "../../include/graphaligner_gb300.h"
 #include "../../graphaligner_gb300/csrc/readalign.h"
 #include "../../graphaligner_gb300/csrc/index_walk.cuh"
+#include "../../graphaligner_gb300/csrc/gaf_format.cuh"
+#include <cmath>
 
 extern "C" int ora_extend_batch(const ga_graph_desc*, const ga_extend_params*, const ga_extend_batch_desc*, ga_extend_results*, int);
 
@@ -204,51 +206,112 @@ static void oracleExtend(void* ctx, const std::vector<gahost::ExtensionRequest>&
     }
 }
 
+// GAF lines through the read flow's writer hook with gaf_format.cuh's line writer on the host
+// (the read flow classifies the lines with gaf_format.cuh either way): the code the product
+// runs, the writer on the device, checked here against the reference's GAF
+static gaf::NamesHost g_gafNames;
+
+static bool hostWriter(void*, const std::vector<const std::string*>& names, const std::vector<const gahost::ClassifiedLines*>& reads,
+    std::string& text, std::vector<uint64_t>& readEnd)
+{
+    gaf::Names nm = gaf::names_view(g_gafNames);
+    text.clear();
+    readEnd.assign(reads.size(), 0);
+    for (size_t i = 0; i < reads.size(); i++)
+    {
+        const uint64_t nameOff[2] = { 0, names[i]->size() };
+        nm.readNames = (const uint8_t*)names[i]->data();
+        nm.readNameOff = nameOff;
+        for (const auto& m : reads[i]->lines)
+        {
+            const int64_t len = gaf::write_line(nm, m, reads[i]->ops.data(), reads[i]->entries.data(), nullptr);
+            const size_t at = text.size();
+            text.resize(at + (size_t)len);
+            gaf::write_line(nm, m, reads[i]->ops.data(), reads[i]->entries.data(), &text[at]);
+            text += '\n';
+        }
+        readEnd[i] = text.size();
+    }
+    return true;
+}
+
+static bool hostSelect(void*, const std::vector<uint64_t>& first, const std::vector<uint64_t>& start, const std::vector<uint64_t>& end,
+    const std::vector<double>& xscore, int minAlignmentScore, double fractionCutoff, std::vector<char>& keep)
+{
+    for (size_t i = 0; i + 1 < first.size(); i++)
+        gaf::select_read((uint32_t)(first[i + 1] - first[i]), start.data() + first[i], end.data() + first[i], xscore.data() + first[i],
+            minAlignmentScore, fractionCutoff, keep.data() + first[i]);
+    return true;
+}
+
 extern "C" int ora_multiseed_batch(const ga_graph_desc*, const ga_extend_params*, const ga_multiseed_batch_desc*, ga_multiseed_results*, int);
 
 static void oracleMultiseed(void* ctx, const std::vector<gahost::MultiseedRequest>& rq, std::vector<gahost::MultiseedResult>& rs)
 {
     Ctx* c = (Ctx*)ctx;
-    const size_t n = rq.size();
-    const uint32_t maxTraces = 4096;
-    std::vector<uint8_t> blob;
-    std::vector<uint64_t> off(n), soff(n + 1, 0), toff(n), cap(n), steps(n);
-    std::vector<uint32_t> len(n), sslice, snode, ntr(n);
-    std::vector<int32_t> status(n);
-    uint64_t ti = 0;
-    for (size_t i = 0; i < n; i++)
+    std::vector<size_t> todo(rq.size());
+    for (size_t i = 0; i < rq.size(); i++) todo[i] = i;
+    std::vector<uint64_t> wantItems(rq.size(), 0);
+    std::vector<uint32_t> wantTraces(rq.size(), 0);
+    for (int attempt = 0; attempt < 2 && !todo.empty(); attempt++)
     {
-        off[i] = blob.size();
-        blob.insert(blob.end(), rq[i].seq, rq[i].seq + rq[i].len);
-        len[i] = rq[i].len;
-        sslice.insert(sslice.end(), rq[i].slices, rq[i].slices + rq[i].numSeeds);
-        snode.insert(snode.end(), rq[i].nodes, rq[i].nodes + rq[i].numSeeds);
-        soff[i + 1] = sslice.size();
-        cap[i] = (uint64_t)rq[i].len * 64 + 4096;
-        toff[i] = ti;
-        ti += cap[i];
-    }
-    if (blob.empty()) blob.push_back(0);
-    if (sslice.empty()) { sslice.push_back(0); snode.push_back(0); }
-    std::vector<uint64_t> items(ti + 1), tstart(n * maxTraces);
-    std::vector<int32_t> tscore(n * maxTraces);
-    std::vector<uint32_t> tlen(n * maxTraces);
-    ga_multiseed_batch_desc b { (uint32_t)n, blob.data(), off.data(), len.data(), soff.data(), sslice.data(), snode.data(), toff.data(), cap.data(),
-        maxTraces, 0.9 };
-    ga_multiseed_results r { status.data(), ntr.data(), tscore.data(), tstart.data(), tlen.data(), items.data(), steps.data() };
-    ora_multiseed_batch(c->d, &c->p, &b, &r, c->threads);
-    for (size_t i = 0; i < n; i++)
-    {
-        rs[i].status = status[i];
-        rs[i].steps = steps[i];
-        rs[i].scores.clear();
-        rs[i].traces.clear();
-        for (uint32_t t = 0; t < ntr[i]; t++)
+        const size_t n = todo.size();
+        uint32_t maxTraces = 4096;
+        if (attempt > 0)
         {
-            const size_t k = i * maxTraces + t;
-            rs[i].scores.push_back(tscore[k]);
-            rs[i].traces.emplace_back(items.begin() + toff[i] + tstart[k], items.begin() + toff[i] + tstart[k] + tlen[k]);
+            maxTraces = 1;
+            for (size_t k = 0; k < n; k++) maxTraces = std::max(maxTraces, wantTraces[todo[k]]);
         }
+        std::vector<uint8_t> blob;
+        std::vector<uint64_t> off(n), soff(n + 1, 0), toff(n), cap(n), steps(n), needI(n);
+        std::vector<uint32_t> len(n), sslice, snode, ntr(n), needT(n);
+        std::vector<int32_t> status(n);
+        uint64_t ti = 0;
+        for (size_t k = 0; k < n; k++)
+        {
+            const auto& q = rq[todo[k]];
+            off[k] = blob.size();
+            blob.insert(blob.end(), q.seq, q.seq + q.len);
+            len[k] = q.len;
+            sslice.insert(sslice.end(), q.slices, q.slices + q.numSeeds);
+            snode.insert(snode.end(), q.nodes, q.nodes + q.numSeeds);
+            soff[k + 1] = sslice.size();
+            cap[k] = attempt == 0 ? (uint64_t)q.len * 64 + 4096 : wantItems[todo[k]] + 64;
+            toff[k] = ti;
+            ti += cap[k];
+        }
+        if (blob.empty()) blob.push_back(0);
+        if (sslice.empty()) { sslice.push_back(0); snode.push_back(0); }
+        std::vector<uint64_t> items(ti + 1), tstart(n * maxTraces);
+        std::vector<int32_t> tscore(n * maxTraces);
+        std::vector<uint32_t> tlen(n * maxTraces);
+        ga_multiseed_batch_desc b { (uint32_t)n, blob.data(), off.data(), len.data(), soff.data(), sslice.data(), snode.data(), toff.data(), cap.data(),
+            maxTraces, 0.9 };
+        ga_multiseed_results r { status.data(), ntr.data(), tscore.data(), tstart.data(), tlen.data(), items.data(), steps.data(), needI.data(), needT.data() };
+        ora_multiseed_batch(c->d, &c->p, &b, &r, c->threads);
+        std::vector<size_t> again;
+        for (size_t k = 0; k < n; k++)
+        {
+            gahost::MultiseedResult& out = rs[todo[k]];
+            out.status = status[k];
+            out.steps = steps[k];
+            out.scores.clear();
+            out.traces.clear();
+            if (status[k] == GA_CAPACITY && attempt == 0 && (needI[k] > 0 || needT[k] > 0))
+            {
+                wantItems[todo[k]] = needI[k];
+                wantTraces[todo[k]] = needT[k];
+                again.push_back(todo[k]);
+                continue;
+            }
+            for (uint32_t t = 0; t < ntr[k]; t++)
+            {
+                const size_t slot = k * maxTraces + t;
+                out.scores.push_back(tscore[slot]);
+                out.traces.emplace_back(items.begin() + toff[k] + tstart[slot], items.begin() + toff[k] + tstart[slot] + tlen[slot]);
+            }
+        }
+        todo.swap(again);
     }
 }
 
@@ -506,11 +569,18 @@ int main(int argc, char** argv)
         kmerMatchesHost(idx, in[i].seq, km);
         gahost::selectSeeds(graph, idx, in[i].seq, dbg ? 5 : 10, km, in[i].seeds);
     }
+    if (getenv("GAF_LINE_FORMATTER")) gaf::build_names(graph.lookupIds, graph.names, graph.originalSize, g_gafNames);
     Ctx ctx { &hd.base, ga_extend_params { (uint32_t)bw, 14705, maxCells, 294 } };
     // gafms / gafmsdbg: the oracle's multiseed DPs and backward extensions on this many threads
     if (multiseed && argc > 6) ctx.threads = (int)std::stoul(argv[6]);
     gahost::ReadAlignParams p;
     if (dbg) p.seedExtendDensity = 0.002;
+    // GAF_LINE_FORMATTER set: the GAF lines come from gaf_format.cuh through the formatter hook
+    if (getenv("GAF_LINE_FORMATTER"))
+    {
+        p.gafWrite = hostWriter;
+        p.select = hostSelect;
+    }
     std::vector<gahost::ReadOutput> out;
     gahost::BatchStats st;
     if (mixed)

@@ -81,6 +81,8 @@ def test_gpu_multiseed_reports_capacity(cuda_lib, oracle_lib, harness, tmp_path)
     cpu = oracle_lib.multiseed(g, p, batch, threads=8)
     assert np.array_equal(gpu.status, cpu.status)
     assert 0 < int((cpu.status == 3).sum()) < batch.num
+    # the room the overflowing reads need, counted on the device as the oracle counts it
+    assert np.array_equal(gpu.items_needed, cpu.items_needed) and np.array_equal(gpu.traces_needed, cpu.traces_needed)
     for i in np.nonzero(cpu.status == 0)[0]:
         assert [(s, list(t)) for s, t in gpu.traces(int(i))] == [(s, list(t)) for s, t in cpu.traces(int(i))]
 

@@ -23,7 +23,7 @@ SOURCES = [os.path.join(ROOT, "tests", "harness", "pipeline.cpp"),
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
     os.makedirs(BUILD, exist_ok=True)
-    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "index_walk.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "seed_table.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
+    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "index_walk.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "gaf_format.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "seed_table.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
     if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < max(os.path.getmtime(d) for d in deps):
         subprocess.run(["g++", "-std=c++17", "-O2", "-o", HARNESS, *SOURCES, "-lpthread"], check=True)
     d = tmp_path_factory.mktemp("pipeline")
@@ -151,6 +151,70 @@ def test_multiseed_gaf_matches_reference(harness, oracle_lib, tmp_path, graph, r
     out = subprocess.run([exe, graph_file(graph, str(tmp_path)), fa, mode, str(bandwidth)], check=True, capture_output=True, text=True)
     assert out.stdout == gzip.open(os.path.join(GOLDEN, f"{gaf}.gaf.gz"), "rt").read()
     assert " failed 0 " in out.stderr
+
+
+GAF_HOOK_CASES = [("vg50k", "vg50k_reads", "gaf", 10, "vg50k_b10"), ("vg50k", "vg50k_reads", "gaf2", 5, "vg50k_b5"),
+                  ("dbg100k", "dbg100k_reads", "gafdbg", 5, "dbg100k_b5"), ("vg50k", "vg50k_chimera_reads", "gafms", 10, "vg50k_chimera_ms_b10"),
+                  ("dbg100k", "dbg100k_reads", "gafmsdbg", 5, "dbg100k_ms_b5")]
+
+
+@pytest.mark.parametrize("graph,reads,mode,bandwidth,gaf", GAF_HOOK_CASES)
+def test_gaf_formatter_hook_matches_reference(harness, oracle_lib, tmp_path, graph, reads, mode, bandwidth, gaf):
+    """The selection and GAF line code the device runs (gaf_format.cuh: select_read, gaf_line),
+    compiled for the host and plugged into the read flow's formatter hooks: GAF bytes equal to
+    the reference's."""
+    import gzip
+    exe = harness[0]
+    fa = os.path.join(tmp_path, "reads.fa")
+    open(fa, "wb").write(gzip.open(os.path.join(GOLDEN, f"{reads}.fa.gz")).read())
+    env = dict(os.environ, GAF_LINE_FORMATTER="1")
+    out = subprocess.run([exe, graph_file(graph, str(tmp_path)), fa, mode, str(bandwidth)], check=True, capture_output=True, text=True, env=env)
+    assert out.stdout == gzip.open(os.path.join(GOLDEN, f"{gaf}.gaf.gz"), "rt").read()
+
+
+def test_multiseed_reports_room_needed(harness, oracle_lib, tmp_path):
+    """A read whose multiseed traces outgrow max_traces reports GA_CAPACITY with the items and
+    traces it needs, which equal what a run with room enough returns."""
+    import gzip
+    import numpy as np
+    from graphaligner_gb300.extend import ExtendParams, MultiseedBatch
+    from golden_sets import load_graph
+    exe = harness[0]
+    fa = os.path.join(tmp_path, "reads.fa")
+    open(fa, "wb").write(gzip.open(os.path.join(GOLDEN, "vg50k_chimera_reads.fa.gz")).read())
+    out = subprocess.run([exe, graph_file("vg50k", str(tmp_path)), fa, "msseeds"], check=True, capture_output=True, text=True).stdout.splitlines()
+    seeds = []
+    for line in out[:20]:
+        f = line.split()
+        v = list(map(int, f[2:]))
+        seeds.append([(v[2 * k], v[2 * k + 1]) for k in range(int(f[1]))])
+    seqs = [line.encode() for line in open(fa).read().split("\n") if line and not line.startswith(">")][:20]
+    g = load_graph("vg50k")
+    p = ExtendParams(bandwidth=10)
+    tight = oracle_lib.multiseed(g, p, MultiseedBatch.pack(seqs, seeds, max_traces=2, items_per_bp=64), threads=4)
+    roomy = oracle_lib.multiseed(g, p, MultiseedBatch.pack(seqs, seeds, max_traces=4096, items_per_bp=64), threads=4)
+    assert (roomy.status == 0).all() and (tight.status == 3).any()
+    for i in range(len(seqs)):
+        if tight.status[i] == 3:
+            assert tight.traces_needed[i] == roomy.num_traces[i]
+            assert tight.items_needed[i] == sum(len(t) for _, t in roomy.traces(i))
+        else:
+            assert tight.items_needed[i] == 0 and tight.traces_needed[i] == 0
+
+
+def test_gaf_number_formatting_matches_ostream():
+    """gaf_format.cuh's double formatting (six significant digits from the exact binary value,
+    ties to even, fixed or scientific as %g) and integer formatting equal std::ostream's on X-scores,
+    identity ratios and doubles over the whole exponent range."""
+    exe = os.path.join(BUILD, "gaf_fmt")
+    src = os.path.join(ROOT, "tests", "harness", "gaf_fmt.cpp")
+    hdr = os.path.join(ROOT, "graphaligner_gb300", "csrc", "gaf_format.cuh")
+    os.makedirs(BUILD, exist_ok=True)
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        subprocess.run(["g++", "-std=c++17", "-O2", "-o", exe, src], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout[-2000:]
+    assert "mismatches 0" in out.stdout
 
 
 def test_quickstart_gaf(harness, tmp_path):
