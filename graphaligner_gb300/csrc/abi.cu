@@ -90,7 +90,7 @@ struct ga_extender
     uint64_t workspaceBytes = 0;
     uint8_t* arena = nullptr;
     uint64_t arenaBytes = 0;
-    uint32_t* counters = nullptr;          // [0] work counter, [2] status count
+    uint32_t* counters = nullptr;          // [0] work counter, [2] status count; the multiseed DP: work counters [1], [3]-[6], candidate total (u64) [8]-[9]
     unsigned long long* arenaCursor = nullptr;   // [0] overflow cursor, [1] bytes taken
     float lastFillMs = 0;
     float lastTraceMs = 0;
@@ -110,6 +110,9 @@ struct ga_extender
     DevBuf<uint64_t> msSeedOff, msTraceCap, msTraceStart, msItemsNeeded;
     DevBuf<uint32_t> msSeedSlice, msSeedNode, msNumTraces, msTraceLen, msTracesNeeded;
     DevBuf<int32_t> msTraceScore;
+    DevBuf<uint64_t> msCandBegin;
+    DevBuf<uint32_t> msCandCount;
+    DevBuf<gadev::MsCand> msCands;
 };
 
 extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
@@ -556,6 +559,8 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     GA_CUDA(x->msTraceLen.reserve(tables));
     GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(items, 1)));
     GA_CUDA(x->states.reserve(n));
+    GA_CUDA(x->msCandBegin.reserve(n));
+    GA_CUDA(x->msCandCount.reserve(n));
     cudaStream_t s = x->stream;
     GA_CUDA(cudaMemcpyAsync(x->seq.ptr, b->seq, seqBytes, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->seqOff.ptr, b->seq_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
@@ -614,6 +619,9 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     ta.cellSteps = x->cellSteps.ptr;
     ta.itemsNeeded = x->msItemsNeeded.ptr;
     ta.tracesNeeded = x->msTracesNeeded.ptr;
+    ta.candBegin = x->msCandBegin.ptr;
+    ta.candCount = x->msCandCount.ptr;
+    ta.candTotal = (unsigned long long*)(x->counters + 8);
 
     x->lastFillMs = 0;
     x->lastLaunches = 0;
@@ -623,7 +631,9 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     // The frontier tables are in the global workspace: the multiseed band holds every seed
     // start of a slice besides the alignments' own nodes.  A read that runs out of room (its
     // tables, or the arena the batch shares) runs again in the next pass, which starts a fresh
-    // arena; passes go on while they finish reads, then once more with the large tables.
+    // arena; passes go on while they finish reads, then once more with the large tables.  A
+    // read whose traces outgrow its output room (kMsRoom) is not run again: it reports the
+    // room it needs.  Between the fill and the traceback the host sizes the candidate list.
     int layout = 1;
     for (int pass = 0; pass < 32; pass++)
     {
@@ -632,7 +642,7 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
         const uint64_t pendingBlocks = std::max<uint64_t>(1, ((uint64_t)pending + wpb - 1) / wpb);
         uint64_t fillBlocks = std::min<uint64_t>((uint64_t)x->sms * 4, pendingBlocks);
         fillBlocks = std::max<uint64_t>(1, std::min<uint64_t>(fillBlocks, x->workspaceBytes / stride / wpb));
-        const uint64_t traceBlocks = std::min<uint64_t>((uint64_t)x->sms * 6, pendingBlocks);
+        const uint64_t readBlocks = std::min<uint64_t>((uint64_t)x->sms * 6, pendingBlocks);
         if (pass > 0) GA_CUDA(cudaMemcpyAsync(x->prevStatus.ptr, x->status.ptr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
         fa.caps = caps;
         fa.workspace = x->workspace;
@@ -642,9 +652,18 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
         GA_CUDA(cudaMemsetAsync(x->counters, 0, 16 * sizeof(uint32_t), s));
         GA_CUDA(cudaMemsetAsync(x->arenaCursor, 0, 2 * sizeof(unsigned long long), s));
         GA_CUDA(cudaEventRecord(x->ev[0], s));
-        if (ga_launch_multiseed(fa, ta, x->counters, (int)fillBlocks, (int)traceBlocks, wpb, s) != 0)
+        if (ga_launch_multiseed_fill(fa, ta, x->counters, (int)fillBlocks, (int)readBlocks, wpb, s) != 0)
             return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
-        x->lastLaunches += 2;
+        unsigned long long candTotal = 0;
+        GA_CUDA(cudaMemcpyAsync(&candTotal, ta.candTotal, 8, cudaMemcpyDeviceToHost, s));
+        GA_CUDA(cudaStreamSynchronize(s));
+        GA_CUDA(x->msCands.reserve(std::max<uint64_t>(candTotal, 1)));
+        ta.cands = x->msCands.ptr;
+        ta.candCap = x->msCands.count;
+        const uint64_t candBlocks = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)x->sms * 6, (candTotal + wpb - 1) / wpb));
+        if (ga_launch_multiseed_trace(ta, x->counters, (int)readBlocks, (int)candBlocks, wpb, s) != 0)
+            return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+        x->lastLaunches += 6;
         x->lastRounds[layout] += pending;
         GA_CUDA(cudaEventRecord(x->ev[1], s));
         count_status_kernel<<<64, 256, 0, s>>>(x->status.ptr, n, GA_CAPACITY, x->counters + 2);
@@ -667,6 +686,9 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     }
     GA_CUDA(cudaMemcpyAsync(r->status, x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->num_traces, x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < n; i++)
+        if (r->status[i] == gadev::kMsRoom) r->status[i] = GA_CAPACITY;
     GA_CUDA(cudaMemcpyAsync(r->trace_score, x->msTraceScore.ptr, tables * 4, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->trace_start, x->msTraceStart.ptr, tables * 8, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->trace_len, x->msTraceLen.ptr, tables * 4, cudaMemcpyDeviceToHost, s));

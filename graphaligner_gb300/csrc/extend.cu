@@ -729,15 +729,27 @@ __device__ __forceinline__ bool arena_alloc(const FillArgs& a, ArenaCursor& c, u
 
 __device__ __forceinline__ u64 rec_ids_bytes(u32 count) { return align16((u64)count * 4); }
 
-// write one slice (record, node ids, band in first-pop order and, for the multiseed DP, each
-// node's best X-score) into the arena, lanes copying
+// slots of a committed band's index: none up to kHashedBand nodes, else the power of two at
+// least twice the band (the index is at most half full)
+__device__ __forceinline__ u32 band_hash_size(u32 count)
+{
+    if (count <= kHashedBand) return 0;
+    u32 h = 256;
+    while (h < 2 * count) h <<= 1;
+    return h;
+}
+
+// write one slice (record, node ids, band in first-pop order, for the multiseed DP each node's
+// best X-score and, for a large band, its index) into the arena, lanes copying
 __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 index, const Item* band, u32 count,
     i32 minScore, i32 quit, i32 maxX, u32 maxXNode, bool notValid, u32 lane, const i32* nodeMax = nullptr)
 {
     const u64 idBytes = rec_ids_bytes(count);
     u64 off;
     const u64 maxBytes = nodeMax ? rec_ids_bytes(count) : 0;
-    if (!arena_alloc(a, c, sizeof(SliceRec) + idBytes + (u64)count * sizeof(Item) + maxBytes, off, lane)) return false;
+    const u32 hashSize = band_hash_size(count);
+    const u64 hashOff = sizeof(SliceRec) + idBytes + (u64)count * sizeof(Item) + maxBytes;
+    if (!arena_alloc(a, c, hashOff + (u64)hashSize * 4, off, lane)) return false;
     uint8_t* base = a.arena + off;
     if (lane == 0)
     {
@@ -748,8 +760,8 @@ __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 in
         r.maxXNode = maxXNode;
         r.count = count;
         r.notValid = notValid ? 1u : 0u;
-        r.pad0 = 0;
-        r.pad1 = 0;
+        r.hashSize = hashSize;
+        r.hashOff = hashSize ? (u32)hashOff : 0;
         *(SliceRec*)base = r;
         dir[index] = off;
     }
@@ -766,7 +778,55 @@ __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 in
         #pragma unroll 1
         for (u32 k = lane; k < count; k += 32) m[k] = nodeMax[k];
     }
+    if (hashSize)
+    {
+        // every slot empty, then each entry claims the first empty slot from its node's hash
+        u32* slots = (u32*)(base + hashOff);
+        #pragma unroll 1
+        for (u32 k = lane; k < hashSize; k += 32) slots[k] = kEmptySlot;
+        __syncwarp();
+        #pragma unroll 1
+        for (u32 k = lane; k < count; k += 32)
+        {
+            u32 h = hash_node(band[k].node & kNodeMask) & (hashSize - 1);
+            #pragma unroll 1
+            while (atomicCAS(&slots[h], kEmptySlot, k) != kEmptySlot) h = (h + 1) & (hashSize - 1);
+        }
+        __syncwarp();
+    }
     return true;
+}
+
+// position of node's entry in committed slice r (whose node ids are `ids`), or -1; every lane
+// gets the answer.  Through the band index where the slice has one (32 slots per probe step,
+// the first slot in probe order that is empty or the node's ends it), else a ballot over the ids.
+__device__ __forceinline__ int rec_index(const SliceRec* r, const u32* ids, u32 node, u32 lane)
+{
+    const u32 hashSize = r->hashSize;
+    if (hashSize)
+    {
+        const u32* slots = (const u32*)((const uint8_t*)r + r->hashOff);
+        const u32 h = hash_node(node);
+#pragma unroll 1
+        for (u32 step = 0; step < hashSize; step += 32)
+        {
+            const u32 e = __ldcg(&slots[(h + step + lane) & (hashSize - 1)]);
+            const bool empty = e == kEmptySlot;
+            const bool hit = !empty && ids[e] == node;
+            const u32 stop = __ballot_sync(kFull, empty || hit);
+            if (stop) return __shfl_sync(kFull, hit ? (int)e : -1, __ffs((int)stop) - 1);
+        }
+        return -1;
+    }
+    const u32 n = r->count;
+#pragma unroll 1
+    for (u32 base = 0; base < n; base += 32)
+    {
+        const u32 k = base + lane;
+        const u32 hit = __ballot_sync(kFull, k < n && ids[k] == node);
+        if (hit) return (int)(base + __ffs((int)hit) - 1);
+    }
+    return -1;
 }
 
 // the multiseed DP's per-node best X-scores of a committed slice
@@ -1283,14 +1343,8 @@ struct Table
         const bool cached = sl.slice == s;
         const u32* ids = cached ? sl.ids : (const u32*)((const uint8_t*)r + sizeof(SliceRec));
         const Item* items = cached ? sl.items : (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
-#pragma unroll 1
-        for (u32 base = 0; base < n; base += 32)
-        {
-            const u32 k = base + lane;
-            const u32 hit = __ballot_sync(kFull, k < n && ids[k] == node);
-            if (hit) return &items[base + __ffs((int)hit) - 1];
-        }
-        return nullptr;
+        const int k = rec_index(r, ids, node, lane);
+        return k < 0 ? nullptr : &items[k];
     }
 };
 
@@ -2000,35 +2054,257 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
     }
 }
 
-// The multiseed DP's best X-score of node in committed slice s (a ballot over the slice's
-// node ids, read from the arena); false when the node is not in the slice's band
+// The multiseed DP's best X-score of node in committed slice s (read from the arena); false
+// when the node is not in the slice's band
 __device__ __forceinline__ bool slice_node_max(const uint8_t* arena, const u64* dir, u32 s, u32 node, u32 lane, i32& out)
 {
     const SliceRec* r = (const SliceRec*)(arena + dir[s]);
-    const u32 n = r->count;
-    const u32* ids = (const u32*)((const uint8_t*)r + sizeof(SliceRec));
-#pragma unroll 1
-    for (u32 base = 0; base < n; base += 32)
-    {
-        const u32 k = base + lane;
-        const u32 hit = __ballot_sync(kFull, k < n && ids[k] == node);
-        if (hit)
-        {
-            out = rec_node_max(r)[base + __ffs((int)hit) - 1];
-            return true;
-        }
-    }
-    return false;
+    const int k = rec_index(r, (const u32*)((const uint8_t*)r + sizeof(SliceRec)), node, lane);
+    if (k < 0) return false;
+    out = rec_node_max(r)[k];
+    return true;
 }
 
-// getLocalMaximaTracesFromTable (Common.h:355-494) for read r: slices from the last, band
-// nodes in order; a node whose best exact-end-position X-score in a slice is positive, at
-// least the multimap fraction of the slice's (lowered) best and not below any of its own in
-// the slices above and below or its neighbours' starts a trace at its best cell.  Each trace
-// raises the best of the slices it spans beyond its first 5 %.
-__device__ void trace_multiseed(const MultiTraceArgs& a, u32 r, const ExtState& st, const WSpace& w, u32 lane)
+// getLocalMaximaTracesFromTable's (Common.h:355-494) local-maximum test of `node` in committed
+// slice cs, whose best X-score there is `score`: not below its own in the slices above and
+// below, nor below its in-neighbours' in this slice and the one above or its out-neighbours'
+// in this slice and the one below.
+__device__ bool ms_local_max(const DevGraph& g, const uint8_t* arena, const u64* dir, u32 cs, u32 last, u32 node, i32 score, u32 lane)
+{
+    i32 other;
+    if (slice_node_max(arena, dir, cs - 1, node, lane, other) && other > score) return false;
+    if (cs < last && slice_node_max(arena, dir, cs + 1, node, lane, other) && other >= score) return false;
+#pragma unroll 1
+    for (u32 e = g.inOff[node]; e < g.inOff[node + 1]; e++)
+    {
+        const u32 nb = g.inNb[e];
+        if (slice_node_max(arena, dir, cs, nb, lane, other) && other > score) return false;
+        if (slice_node_max(arena, dir, cs - 1, nb, lane, other) && other > score) return false;
+    }
+#pragma unroll 1
+    for (u32 e = g.outOff[node]; e < g.outOff[node + 1]; e++)
+    {
+        const u32 nb = g.outNb[e];
+        if (slice_node_max(arena, dir, cs, nb, lane, other) && other > score) return false;
+        if (cs < last && slice_node_max(arena, dir, cs + 1, nb, lane, other) && other > score) return false;
+    }
+    return true;
+}
+
+// The candidates of read r in getLocalMaximaTracesFromTable's order (slices from the last,
+// band order within a slice): band nodes whose best X-score is positive, reaches the
+// multimap fraction of the slice's best as the fill left it and is a local maximum.  The
+// slice bests only rise as traces are taken, so the traces the read keeps are among these.
+// write = false counts them and reserves the read's run of the list; write = true fills it.
+__device__ void ms_candidates(const MultiTraceArgs& a, u32 r, const ExtState& st, bool write, u32 lane)
+{
+    u32 c = 0;
+    const u64 base = write ? a.candBegin[r] : 0;
+    if (st.status == GA_OK)
+    {
+        const u64* dir = (const u64*)(a.arena + st.dir);
+        const i32* sliceMax = (const i32*)(a.arena + st.aux);
+        const u32 last = st.committed - 1;
+#pragma unroll 1
+        for (u32 cs = last; cs >= 1; cs--)
+        {
+            const SliceRec* cr = (const SliceRec*)(a.arena + dir[cs]);
+            if (cr->maxX <= 0) continue;
+            const u32 n = cr->count;
+            const u32* ids = (const u32*)((const uint8_t*)cr + sizeof(SliceRec));
+            const Item* items = (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
+            const i32* nodeMax = rec_node_max(cr);
+            const double threshold = (double)sliceMax[cs] * a.multimapScoreFraction;
+#pragma unroll 1
+            for (u32 b = 0; b < n; b += 32)
+            {
+                const u32 k = b + lane;
+                bool pass = false;
+                if (k < n)
+                {
+                    const i32 score = nodeMax[k];
+                    pass = (items[k].node & kExists) && score > 0 && !((double)score < threshold);
+                }
+                u32 m = __ballot_sync(kFull, pass);
+#pragma unroll 1
+                while (m)
+                {
+                    const u32 kk = b + __ffs((int)m) - 1;
+                    m &= m - 1;
+                    const u32 node = ids[kk];
+                    const i32 score = nodeMax[kk];
+                    if (!ms_local_max(a.g, a.arena, dir, cs, last, node, score, lane)) continue;
+                    if (write && lane == 0 && base + c < a.candCap)
+                    {
+                        MsCand x {};
+                        x.read = r;
+                        x.slice = cs;
+                        x.index = kk;
+                        x.score = score;
+                        x.slot = kNoSlot;
+                        a.cands[base + c] = x;
+                    }
+                    c++;
+                }
+            }
+        }
+    }
+    if (!write && lane == 0)
+    {
+        a.candCount[r] = c;
+        a.candBegin[r] = c ? atomicAdd(a.candTotal, (unsigned long long)c) : 0;
+    }
+    __syncwarp();
+}
+
+// The first cell of a candidate's trace (getLocalMaximaTracesFromTable): among the node's
+// columns, recomputed with its seed start, the cell of greatest row that scores the node's
+// best X-score (the first column on ties); a cell above it is GA_ASSERT.
+__device__ int ms_start_cell(const MultiTraceArgs& a, Table& t, const WSpace& w, const uint8_t* seq, u32 seqLen, const MsCand& c,
+    TPos& start, i32& startScore, u32 lane)
 {
     const DevGraph& g = a.g;
+    const SliceRec* cr = (const SliceRec*)(a.arena + t.dir[c.slice]);
+    const Item* items = (const Item*)((const uint8_t*)cr + sizeof(SliceRec) + rec_ids_bytes(cr->count));
+    const u32 node = items[c.index].node & kNodeMask;
+    const int64_t j = ((int64_t)c.slice - 1) * 64;
+    EqV4 eqv;
+    if (!eq_vector(seq, seqLen, j, eqv, lane)) return GA_ASSERT;
+    const WS extra = (items[c.index].node & kSeedStart) ? seed_ws(j, seqLen, a.cost) : fake_ws();
+    int err = recalc<true>(g, a.cost, t, c.slice, node, eqv, w.cols, w.eqcol, lane, 63, extra);
+    if (err) return err;
+    const Col* cols = w.cols;
+    const i32 score = c.score;
+    const int cells = (int)((int64_t)seqLen - j < 64 ? (int64_t)seqLen - j : 64);
+    const u32 L = g.len[node];
+    bool bad = false;
+    int candOff = -1;
+    u32 candCol = 0xffffffffu;
+#pragma unroll 1
+    for (u32 h = 0; h < 2; h++)
+    {
+        const u32 i = lane + 32 * h;
+        if (i >= L || bad) continue;
+        const WS cw = ws_make(cols[i].VP, cols[i].VN, cols[i].end);
+        const i32 mx = ws_max_xscore(cw, (i32)j, a.cost, cells, kAllOnes);
+        if (mx > score) { bad = true; continue; }
+        if (mx != score) continue;
+#pragma unroll 1
+        for (int off = 63; off >= 0; off--)
+        {
+            if (j + off >= (int64_t)seqLen) continue;
+            const i32 here = ws_xscore(cw, (i32)j, off, a.cost);
+            if (here > score) { bad = true; break; }
+            if (here == score && off > candOff)
+            {
+                candOff = off;
+                candCol = i;
+            }
+        }
+    }
+    if (__ballot_sync(kFull, bad)) return GA_ASSERT;
+    const int gOff = __reduce_max_sync(kFull, candOff);
+    const u32 gCol = __reduce_min_sync(kFull, candOff == gOff ? candCol : 0xffffffffu);
+    if (gOff < 0 || j + gOff >= (int64_t)seqLen) return GA_ASSERT;
+    start = TPos { node, gCol, j + gOff };
+    startScore = col_value(cols[gCol], gOff);
+    return 0;
+}
+
+// One candidate's trace (getReverseTraceFromTable to a seed start).  write = false: finds the
+// first cell and walks the trace only counting its items, recording its length, score and
+// read span.  write = true (a kept trace of a read whose traces all fit): walks it again
+// into the read's output at the place the read's pass gave it.
+__device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace& w, bool write, u32 lane)
+{
+    const MsCand c = *cp;
+    const u32 r = c.read;
+    if (write)
+    {
+        // the read's status can change under other warps (a kept trace of it that failed)
+        int readStatus = 0;
+        if (lane == 0) readStatus = a.status[r];
+        readStatus = __shfl_sync(kFull, readStatus, 0);
+        if (c.slot == kNoSlot || readStatus != GA_OK) return;
+    }
+    const ExtState st = a.states[r];
+    const uint8_t* seq = a.seq + a.seqOff[r];
+    const u32 seqLen = a.seqLen[r];
+    Table t;
+    t.arena = a.arena;
+    t.dir = (const u64*)(a.arena + st.dir);
+    t.count = st.committed;
+    t.lane = lane;
+    t.slots = w.slots;
+    t.init();
+    TPos start;
+    i32 startScore = 0;
+    int err = 0;
+    if (write)
+    {
+        start = TPos { c.startNode, c.startOff, c.startSeq };
+        startScore = c.startScore;
+    }
+    else
+    {
+        err = ms_start_cell(a, t, w, seq, seqLen, c, start, startScore, lane);
+    }
+    TraceOut to;
+    to.items = write ? a.traceItems + a.traceOffset[r] + c.outOff : nullptr;
+    to.ring = w.ring;
+    to.lane = lane;
+    to.counting = !write;
+    to.cap = write ? c.len : 0xffffffffu;
+    to.n = 0;
+    to.overflow = false;
+    to.back = start;
+    i32 traceScore = 0;
+    if (!err)
+    {
+        err = trace_walk<true>(a.g, a.cost, seq, seqLen, st.committed, t, to, w, start, startScore, traceScore, lane);
+        to.finish();
+        // a walk past its step guard or its counted length is broken, not short of room
+        if (err == GA_CAPACITY || (!err && to.overflow)) err = GA_ASSERT;
+        if (!err && (to.back.seq < 0 || start.seq < to.back.seq)) err = GA_ASSERT;
+    }
+    if (lane == 0)
+    {
+        if (!write)
+        {
+            cp->startNode = start.node;
+            cp->startOff = start.off;
+            cp->startSeq = start.seq;
+            cp->startScore = startScore;
+            cp->err = err;
+            cp->traceScore = traceScore;
+            cp->len = err ? 0 : to.n;
+            cp->traceStart = to.back.seq;
+        }
+        else if (err || to.n != c.len || traceScore != c.traceScore)
+        {
+            // the walk differs from its count only where the written trace's full circularity
+            // check (the counting walk checks the ring) stops it
+            a.status[r] = err ? err : GA_ASSERT;
+            a.numTraces[r] = 0;
+        }
+        else
+        {
+            const u64 slot = (u64)r * a.maxTraces + c.slot;
+            a.traceScore[slot] = traceScore;
+            a.traceStart[slot] = c.outOff;
+            a.traceLen[slot] = to.n;
+        }
+    }
+    __syncwarp();
+}
+
+// getLocalMaximaTracesFromTable's selection for read r over its counted candidates, in order:
+// a candidate reaching the multimap fraction of its slice's best (as raised so far) is kept,
+// and raises the best of the slices its trace spans beyond its first 5 %.  Kept traces get
+// their place in the read's output while they fit its room (max_traces, trace_capacity);
+// past that they are only counted, and the read reports the room it needs.
+__device__ void ms_select(const MultiTraceArgs& a, u32 r, const ExtState& st, u32 lane)
+{
     if (lane == 0 && a.cellSteps) a.cellSteps[r] = st.steps;
     if (st.status != GA_OK)
     {
@@ -2039,158 +2315,57 @@ __device__ void trace_multiseed(const MultiTraceArgs& a, u32 r, const ExtState& 
         }
         return;
     }
-    const uint8_t* seq = a.seq + a.seqOff[r];
-    const u32 seqLen = a.seqLen[r];
-    Table t;
-    t.arena = a.arena;
-    t.dir = (const u64*)(a.arena + st.dir);
-    t.count = st.committed;
-    t.lane = lane;
-    t.slots = w.slots;
-    t.init();
     i32* sliceMax = (i32*)(a.arena + st.aux);
-    u64* out = a.traceItems + a.traceOffset[r];
     const u64 cap = a.traceCap[r];
-    u64 used = 0;
-    u32 nt = 0;
+    const u64 begin = a.candBegin[r];
+    const u32 count = a.candCount[r];
+    u64 used = 0, items = 0;
+    u32 nt = 0, traces = 0;
+    bool room = true;
     int err = 0;
-    bool counting = false;
-    u64 neededItems = 0;
-    u32 neededTraces = 0;
-    Col* cols = w.cols;
-    const u32 last = st.committed - 1;
 #pragma unroll 1
-    for (u32 cs = last; cs >= 1 && !err; cs--)
+    for (u32 i = 0; i < count; i++)
     {
-        const SliceRec* cr = (const SliceRec*)(a.arena + t.dir[cs]);
-        if (cr->maxX <= 0) continue;
-        const u32 n = cr->count;
-        const u32* ids = (const u32*)((const uint8_t*)cr + sizeof(SliceRec));
-        const Item* items = (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
-        const i32* nodeMax = rec_node_max(cr);
-        const double threshold = (double)sliceMax[cs] * a.multimapScoreFraction;
-        const int64_t j = ((int64_t)cs - 1) * 64;
-#pragma unroll 1
-        for (u32 k = 0; k < n && !err; k++)
+        MsCand* cp = a.cands + begin + i;
+        const u32 cs = cp->slice;
+        const i32 score = cp->score;
+        if ((double)score < (double)sliceMax[cs] * a.multimapScoreFraction) continue;
+        if (cp->err)
         {
-            const u32 node = ids[k];
-            const i32 score = nodeMax[k];
-            if (!(items[k].node & kExists) || score <= 0 || (double)score < threshold) continue;
-            i32 other;
-            if (slice_node_max(a.arena, t.dir, cs - 1, node, lane, other) && other > score) continue;
-            if (cs < last && slice_node_max(a.arena, t.dir, cs + 1, node, lane, other) && other >= score) continue;
-            bool notLocal = false;
-#pragma unroll 1
-            for (u32 e = g.inOff[node]; e < g.inOff[node + 1] && !notLocal; e++)
-            {
-                const u32 nb = g.inNb[e];
-                if (slice_node_max(a.arena, t.dir, cs, nb, lane, other) && other > score) notLocal = true;
-                else if (slice_node_max(a.arena, t.dir, cs - 1, nb, lane, other) && other > score) notLocal = true;
-            }
-#pragma unroll 1
-            for (u32 e = g.outOff[node]; e < g.outOff[node + 1] && !notLocal; e++)
-            {
-                const u32 nb = g.outNb[e];
-                if (slice_node_max(a.arena, t.dir, cs, nb, lane, other) && other > score) notLocal = true;
-                else if (cs < last && slice_node_max(a.arena, t.dir, cs + 1, nb, lane, other) && other > score) notLocal = true;
-            }
-            if (notLocal) continue;
-            // the node's columns with its seed start, and among them the cell of greatest row that
-            // scores the node's best X-score (the first column on ties), across the lanes
-            EqV4 eqv;
-            if (!eq_vector(seq, seqLen, j, eqv, lane)) { err = GA_ASSERT; break; }
-            const WS extra = (items[k].node & kSeedStart) ? seed_ws(j, seqLen, a.cost) : fake_ws();
-            err = recalc<true>(g, a.cost, t, cs, node, eqv, cols, w.eqcol, lane, 63, extra);
-            if (err) break;
-            const int cells = (int)((int64_t)seqLen - j < 64 ? (int64_t)seqLen - j : 64);
-            const u32 L = g.len[node];
-            bool bad = false;
-            int candOff = -1;
-            u32 candCol = 0xffffffffu;
-#pragma unroll 1
-            for (u32 h = 0; h < 2; h++)
-            {
-                const u32 i = lane + 32 * h;
-                if (i >= L || bad) continue;
-                const WS cw = ws_make(cols[i].VP, cols[i].VN, cols[i].end);
-                const i32 mx = ws_max_xscore(cw, (i32)j, a.cost, cells, kAllOnes);
-                if (mx > score) { bad = true; continue; }
-                if (mx != score) continue;
-#pragma unroll 1
-                for (int off = 63; off >= 0; off--)
-                {
-                    if (j + off >= (int64_t)seqLen) continue;
-                    const i32 here = ws_xscore(cw, (i32)j, off, a.cost);
-                    if (here > score) { bad = true; break; }
-                    if (here == score && off > candOff)
-                    {
-                        candOff = off;
-                        candCol = i;
-                    }
-                }
-            }
-            if (__ballot_sync(kFull, bad)) { err = GA_ASSERT; break; }
-            const int gOff = __reduce_max_sync(kFull, candOff);
-            const u32 gCol = __reduce_min_sync(kFull, candOff == gOff ? candCol : 0xffffffffu);
-            if (gOff < 0 || j + gOff >= (int64_t)seqLen) { err = GA_ASSERT; break; }
-            const TPos start = TPos { node, gCol, j + gOff };
-            const i32 startScore = col_value(cols[gCol], gOff);
-            // once the read's room for traces or items has run out, the rest are only counted
-            if (!counting && nt >= a.maxTraces) counting = true;
-            TraceOut to;
-            to.items = out + used;
-            to.ring = w.ring;
-            to.lane = lane;
-            i32 traceScore = 0;
-#pragma unroll 1
-            for (int attempt = 0; attempt < 2; attempt++)
-            {
-                to.counting = counting;
-                to.cap = counting ? 0xffffffffu : (u32)(cap - used < 0xffffffffULL ? cap - used : 0xffffffffULL);
-                to.n = 0;
-                to.overflow = false;
-                err = trace_walk<true>(g, a.cost, seq, seqLen, st.committed, t, to, w, start, startScore, traceScore, lane);
-                to.finish();
-                if (err || !to.overflow || counting) break;
-                counting = true;   // the trace did not fit: count it again from its start
-            }
-            if (!err && to.overflow) err = GA_CAPACITY;
-            if (err) break;
-            const int64_t traceEnd = start.seq, traceStart = to.back.seq;
-            if (traceStart < 0 || traceEnd < traceStart) { err = GA_ASSERT; break; }
-            if (counting)
-            {
-                neededItems += to.n;
-                neededTraces++;
-            }
-            else if (lane == 0)
-            {
-                const u64 slot = (u64)r * a.maxTraces + nt;
-                a.traceScore[slot] = traceScore;
-                a.traceStart[slot] = used;
-                a.traceLen[slot] = to.n;
-            }
-            const u32 startSlice = (u32)(((double)(traceEnd - traceStart) * 0.05 + (double)traceStart + 64 - 1) / 64 + 1);
-#pragma unroll 1
-            for (u32 i = startSlice + lane; i < cs; i += 32) sliceMax[i] = imax(sliceMax[i], score);
-            __syncwarp();
-            if (!counting)
-            {
-                used += to.n;
-                nt++;
-            }
+            err = cp->err;
+            break;
         }
+        const u32 len = cp->len;
+        if (room && (nt >= a.maxTraces || len > cap - used)) room = false;
+        if (room)
+        {
+            if (lane == 0)
+            {
+                cp->slot = nt;
+                cp->outOff = used;
+            }
+            used += len;
+            nt++;
+        }
+        items += len;
+        traces++;
+        const int64_t traceEnd = cp->startSeq, traceStart = cp->traceStart;
+        const u32 startSlice = (u32)(((double)(traceEnd - traceStart) * 0.05 + (double)traceStart + 64 - 1) / 64 + 1);
+        __syncwarp();
+#pragma unroll 1
+        for (u32 s = startSlice + lane; s < cs; s += 32) sliceMax[s] = imax(sliceMax[s], score);
+        __syncwarp();
     }
-    if (!err && counting) err = GA_CAPACITY;
     if (lane == 0)
     {
-        a.status[r] = err ? err : GA_OK;
-        a.numTraces[r] = err ? 0 : nt;
-        // the room the read needs, when only the room ran out
-        if (a.itemsNeeded) a.itemsNeeded[r] = counting ? used + neededItems : 0;
-        if (a.tracesNeeded) a.tracesNeeded[r] = counting ? nt + neededTraces : 0;
+        a.status[r] = err ? err : (room ? GA_OK : kMsRoom);
+        a.numTraces[r] = (err || !room) ? 0 : nt;
+        if (a.itemsNeeded) a.itemsNeeded[r] = (!err && !room) ? items : 0;
+        if (a.tracesNeeded) a.tracesNeeded[r] = (!err && !room) ? traces : 0;
     }
+    __syncwarp();
 }
+
 
 // The next extension for this warp from the work counter, or false when none is left;
 // with a filter only extensions whose previous status is GA_CAPACITY are taken.
@@ -2326,9 +2501,35 @@ __global__ void __launch_bounds__(128, 4) fill_multiseed_kernel(FillArgs fa, u32
     if (lane == 0 && arena.used) atomicAdd(fa.arenaCursor + 1, (unsigned long long)arena.used);
 }
 
-// The multiseed DP's traceback: a warp takes the next filled read and traces from every
-// local maximum of its table.
-__global__ void __launch_bounds__(128, 6) trace_multiseed_kernel(MultiTraceArgs ta, u32* counter)
+// The per-read passes of the multiseed traceback (write = false: count the candidates and
+// reserve their run; write = true: list them), a warp per read.
+__global__ void __launch_bounds__(128, 6) ms_candidates_kernel(MultiTraceArgs ta, u32* counter, int write)
+{
+    const u32 lane = threadIdx.x & 31;
+    u32 r;
+#pragma unroll 1
+    while (next_extension(counter, ta.num, ta.order, ta.prevStatus, lane, r))
+    {
+        __syncwarp();
+        ms_candidates(ta, r, ta.states[r], write != 0, lane);
+    }
+}
+
+__global__ void __launch_bounds__(128, 6) ms_select_kernel(MultiTraceArgs ta, u32* counter)
+{
+    const u32 lane = threadIdx.x & 31;
+    u32 r;
+#pragma unroll 1
+    while (next_extension(counter, ta.num, ta.order, ta.prevStatus, lane, r))
+    {
+        __syncwarp();
+        ms_select(ta, r, ta.states[r], lane);
+    }
+}
+
+// The candidates' traces, a warp per candidate (write = false: counted; write = true: the kept
+// ones written).  A read's traces spread over as many warps as it has candidates.
+__global__ void __launch_bounds__(128, 6) ms_trace_kernel(MultiTraceArgs ta, u32* counter, int write)
 {
     extern __shared__ __align__(16) uint8_t dsmem[];
     load_iupac_table();
@@ -2339,12 +2540,16 @@ __global__ void __launch_bounds__(128, 6) trace_multiseed_kernel(MultiTraceArgs 
     w.eqcol = (u64*)(base + 64 * sizeof(Col));
     w.ring = (u64*)(base + 64 * sizeof(Col) + 64 * 8);
     w.slots = (SliceSlot*)(base + 64 * sizeof(Col) + 64 * 8 + 64 * 8);
-    u32 r;
+    const u64 total = *ta.candTotal < ta.candCap ? *ta.candTotal : ta.candCap;
 #pragma unroll 1
-    while (next_extension(counter, ta.num, ta.order, ta.prevStatus, lane, r))
+    while (true)
     {
+        u32 i = 0;
+        if (lane == 0) i = atomicAdd(counter, 1u);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= total) break;
         __syncwarp();
-        trace_multiseed(ta, r, ta.states[r], w, lane);
+        ms_trace_cand(ta, ta.cands + i, w, write != 0, lane);
     }
 }
 }
@@ -2387,14 +2592,28 @@ int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int ga_launch_multiseed(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
+int ga_launch_multiseed_fill(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int readBlocks,
     int warpsPerBlock, void* stream)
 {
-    const size_t traceSmem = (size_t)gadev::kTraceSpaceBytes * warpsPerBlock;
-    if (!fa.workspace || !set_smem((const void*)gadev::trace_multiseed_kernel, traceSmem)) return -1;
+    if (!fa.workspace) return -1;
     gadev::fill_multiseed_kernel<<<fillBlocks, warpsPerBlock * 32, 0, (cudaStream_t)stream>>>(fa, counters);
     if (cudaGetLastError() != cudaSuccess) return -1;
-    gadev::trace_multiseed_kernel<<<traceBlocks, warpsPerBlock * 32, traceSmem, (cudaStream_t)stream>>>(ta, counters + 1);
+    gadev::ms_candidates_kernel<<<readBlocks, warpsPerBlock * 32, 0, (cudaStream_t)stream>>>(ta, counters + 1, 0);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int ga_launch_multiseed_trace(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int candBlocks, int warpsPerBlock, void* stream)
+{
+    const size_t traceSmem = (size_t)gadev::kTraceSpaceBytes * warpsPerBlock;
+    if (!set_smem((const void*)gadev::ms_trace_kernel, traceSmem)) return -1;
+    cudaStream_t s = (cudaStream_t)stream;
+    gadev::ms_candidates_kernel<<<readBlocks, warpsPerBlock * 32, 0, s>>>(ta, counters + 3, 1);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    gadev::ms_trace_kernel<<<candBlocks, warpsPerBlock * 32, traceSmem, s>>>(ta, counters + 4, 0);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    gadev::ms_select_kernel<<<readBlocks, warpsPerBlock * 32, 0, s>>>(ta, counters + 5);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    gadev::ms_trace_kernel<<<candBlocks, warpsPerBlock * 32, traceSmem, s>>>(ta, counters + 6, 1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -41,8 +41,12 @@ static constexpr u32 kNodeMask = 0x3fffffffu;
 // A committed DP slice in the arena: this 32-byte record, then the band's node ids
 // (count u32, padded to 16 bytes), then count Items, all in first-pop order (the multiseed
 // DP's seed starts first), then for the multiseed DP each node's best exact-end-position
-// X-score (count i32, DPSlice::nodeMaxExactEndposScore).  The traceback finds a node's
-// entry by a warp ballot over the ids.
+// X-score (count i32, DPSlice::nodeMaxExactEndposScore), then, for a band of more than
+// kHashedBand nodes, an open-addressing index of the band (hashSize u32 slots, each an
+// entry's position or kEmptySlot, linear probing from the node's hash).  The traceback finds
+// a node's entry through the index, else by a warp ballot over the ids.
+static constexpr u32 kHashedBand = 64;
+static constexpr u32 kEmptySlot = 0xffffffffu;
 struct __align__(16) SliceRec
 {
     i32 minScore;
@@ -51,7 +55,8 @@ struct __align__(16) SliceRec
     u32 maxXNode;          // maxExactEndposNode
     u32 count;
     u32 notValid;          // scoresNotValid: the tangle-effort cap was hit
-    u32 pad0, pad1;
+    u32 hashSize;          // slots of the band index (a power of two), 0 = none
+    u32 hashOff;           // byte offset of the band index from the record
 };
 
 // Per-extension state passed from the fill to the traceback.
@@ -124,6 +129,34 @@ struct TraceArgs
     u64* cellSteps;
 };
 
+// One local maximum of a multiseed read's table that may start a trace: a node whose best
+// X-score in a slice beats its neighbours' and reaches the multimap fraction of the slice's
+// best before any trace raised it.  The traces from the candidates are independent, so one
+// warp traces each; the read's own pass then keeps them in getLocalMaximaTracesFromTable's
+// order against the raised slice bests.
+struct MsCand
+{
+    u32 read;
+    u32 slice;
+    u32 index;             // the node's position in the slice's band
+    i32 score;             // its best X-score in the slice
+    u32 startNode;         // the trace's first cell
+    u32 startOff;
+    int64_t startSeq;
+    i32 startScore;
+    i32 err;               // 0 or the status the trace failed with
+    i32 traceScore;
+    u32 len;               // trace items
+    int64_t traceStart;    // read position of the trace's last item
+    u64 outOff;            // kept traces: items from the read's trace_offset
+    u32 slot;              // kept traces: the trace's index in the read, else kNoSlot
+    u32 pad;
+};
+static constexpr u32 kNoSlot = 0xffffffffu;
+// the status of a multiseed read whose traces outgrew its room (reported as GA_CAPACITY with
+// the room it needs; the batch does not run it again as it does a read whose tables ran out)
+static constexpr i32 kMsRoom = 100;
+
 // The multiseed DP's traceback outputs (ga_multiseed_results).
 struct MultiTraceArgs
 {
@@ -150,6 +183,11 @@ struct MultiTraceArgs
     u64* cellSteps;
     u64* itemsNeeded;      // [num] or null: when the traces outgrow the read's room, the room they need
     u32* tracesNeeded;
+    MsCand* cands;         // [candCap] the batch's candidates, each read's together and in order
+    u64 candCap;
+    u64* candBegin;        // [num] read i's candidates are [candBegin[i], candBegin[i] + candCount[i])
+    u32* candCount;
+    unsigned long long* candTotal;   // candidates of the batch
 };
 
 }
@@ -167,7 +205,12 @@ int ga_trace_blocks_per_sm(int warpsPerBlock);
 int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
     int warpsPerBlock, void* stream);
 // the multiseed DP's fill and traceback kernels (the frontier tables always in the global workspace)
-int ga_launch_multiseed(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
+// the multiseed DP in two steps, blocks of warpsPerBlock warps: the fill and the count of each
+// read's trace candidates (counters[0], [1] zero; ta.candTotal zero), then, once ta.cands has
+// room for *ta.candTotal, the candidates listed, traced, selected and the kept ones written
+// (counters[3] to [6] zero); counters[2] is left to the caller
+int ga_launch_multiseed_fill(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int readBlocks,
     int warpsPerBlock, void* stream);
+int ga_launch_multiseed_trace(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int candBlocks, int warpsPerBlock, void* stream);
 int ga_upload_tables();
 void ga_set_last_error(const char* message);
