@@ -109,3 +109,18 @@ class MultiseedResults(ctypes.Structure):
         ("items_needed", _u64p),
         ("traces_needed", _u32p),
     ]
+
+
+class MultiseedOutput(ctypes.Structure):
+    _fields_ = [
+        ("status", _i32p),
+        ("num_traces", _u32p),
+        ("trace_first", _u64p),
+        ("trace_score", _i32p),
+        ("trace_start", _u64p),
+        ("trace_len", _u32p),
+        ("trace_items", _u64p),
+        ("cell_steps", _u64p),
+        ("total_traces", ctypes.c_uint64),
+        ("total_items", ctypes.c_uint64),
+    ]

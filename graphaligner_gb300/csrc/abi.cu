@@ -57,6 +57,66 @@ struct DevBuf
     }
 };
 
+// pinned host memory that grows keeping its first `keep` elements
+template <typename T>
+struct HostPinned
+{
+    T* ptr = nullptr;
+    size_t count = 0;
+    bool reserve(size_t n, size_t keep)
+    {
+        if (n <= count) return true;
+        const size_t grow = std::max(n, count * 3 / 2);
+        T* q = nullptr;
+        if (cudaHostAlloc((void**)&q, grow * sizeof(T), cudaHostAllocDefault) != cudaSuccess) return false;
+        if (keep) memcpy(q, ptr, keep * sizeof(T));
+        if (ptr) cudaFreeHost(ptr);
+        ptr = q;
+        count = grow;
+        return true;
+    }
+    void release()
+    {
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+};
+
+// ga_multiseed_batch_exact's results, kept until the extender's next call
+struct MsExactOut
+{
+    std::vector<int32_t> status;
+    std::vector<uint32_t> numTraces;
+    std::vector<uint64_t> traceFirst, cellSteps;
+    HostPinned<int32_t> score;
+    HostPinned<uint64_t> start, item;
+    HostPinned<uint32_t> len;
+    uint64_t traces = 0, items = 0;
+    bool grow(uint64_t t, uint64_t i)
+    {
+        return score.reserve(std::max<uint64_t>(t, 1), traces) && start.reserve(std::max<uint64_t>(t, 1), traces)
+            && len.reserve(std::max<uint64_t>(t, 1), traces) && item.reserve(std::max<uint64_t>(i, 1), items);
+    }
+    void publish(ga_multiseed_output* o) const
+    {
+        o->status = status.data();
+        o->num_traces = numTraces.data();
+        o->trace_first = traceFirst.data();
+        o->trace_score = score.ptr;
+        o->trace_start = start.ptr;
+        o->trace_len = len.ptr;
+        o->trace_items = item.ptr;
+        o->cell_steps = cellSteps.data();
+        o->total_traces = traces;
+        o->total_items = items;
+    }
+    ~MsExactOut()
+    {
+        score.release(); start.release(); item.release(); len.release();
+    }
+};
+
 __global__ void count_status_kernel(const int32_t* status, uint32_t n, int32_t value, uint32_t* out)
 {
     uint32_t local = 0;
@@ -110,9 +170,11 @@ struct ga_extender
     DevBuf<uint64_t> msSeedOff, msTraceCap, msTraceStart, msItemsNeeded;
     DevBuf<uint32_t> msSeedSlice, msSeedNode, msNumTraces, msTraceLen, msTracesNeeded;
     DevBuf<int32_t> msTraceScore;
-    DevBuf<uint64_t> msCandBegin;
+    DevBuf<uint64_t> msCandBegin, msTraceBase, msItemBase;
     DevBuf<uint32_t> msCandCount;
     DevBuf<gadev::MsCand> msCands;
+    MsExactOut msOut;                      // ga_multiseed_batch_exact's results
+    uint64_t lastCandidates = 0, lastKept = 0;
 };
 
 extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
@@ -269,6 +331,10 @@ extern "C" int ga_extender_free(ga_extender_t x)
     x->seq.release(); x->seqOff.release(); x->traceOff.release(); x->traceItems.release(); x->cellSteps.release();
     x->seqLen.release(); x->startNode.release(); x->startOffset.release(); x->traceCap.release(); x->traceLen.release();
     x->order.release(); x->status.release(); x->score.release(); x->prevStatus.release(); x->states.release();
+    x->msSeedOff.release(); x->msTraceCap.release(); x->msTraceStart.release(); x->msItemsNeeded.release();
+    x->msSeedSlice.release(); x->msSeedNode.release(); x->msNumTraces.release(); x->msTraceLen.release(); x->msTracesNeeded.release();
+    x->msTraceScore.release(); x->msCandBegin.release(); x->msCandCount.release(); x->msCands.release();
+    x->msTraceBase.release(); x->msItemBase.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
     for (int k = 0; k < ga_extender::kCopyStreams; k++)
@@ -502,15 +568,32 @@ extern "C" int ga_extend_batch(ga_extender_t x, const ga_extend_params* p, const
 
 // ---- multiseed DP ----
 
-extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, const ga_multiseed_batch_desc* b, ga_multiseed_results* r)
+// The multiseed batch with the caller's room (r) or, with ex, exact room in the extender's
+// own buffers: each pass's finished reads get their room once their traces are counted.
+static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_multiseed_batch_desc* b, ga_multiseed_results* r,
+    ga_multiseed_output* ex)
 {
-    if (!x || !p || !b || !r) return fail(GA_ERR_ARGUMENT, "null argument");
+    if (!x || !p || !b || (!r && !ex)) return fail(GA_ERR_ARGUMENT, "null argument");
+    const bool exact = ex != nullptr;
     const uint32_t n = b->num;
+    if (exact)
+    {
+        MsExactOut& o = x->msOut;
+        o.status.assign(n, 0);
+        o.numTraces.assign(n, 0);
+        o.traceFirst.assign(n, 0);
+        o.cellSteps.assign(n, 0);
+        o.traces = 0;
+        o.items = 0;
+        o.publish(ex);
+    }
     if (n == 0) return GA_OK;
-    if (!b->seq || !b->seq_offset || !b->seq_len || !b->seed_offset || !b->trace_offset || !b->trace_capacity || !r->status || !r->num_traces
-        || !r->trace_score || !r->trace_start || !r->trace_len || !r->trace_items)
+    if (!b->seq || !b->seq_offset || !b->seq_len || !b->seed_offset)
         return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: a required array is NULL");
-    if (b->max_traces == 0) return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: max_traces must be at least 1");
+    if (!exact && (!b->trace_offset || !b->trace_capacity || !r->status || !r->num_traces || !r->trace_score || !r->trace_start || !r->trace_len
+        || !r->trace_items))
+        return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: a required array is NULL");
+    if (!exact && b->max_traces == 0) return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: max_traces must be at least 1");
     int rc = check_lengths(b->seq_len, n);
     if (rc != GA_OK) return rc;
     // seeds: in the graph, within their read, in slice order
@@ -533,10 +616,10 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     for (uint32_t i = 0; i < n; i++)
     {
         seqBytes = std::max<uint64_t>(seqBytes, b->seq_offset[i] + b->seq_len[i]);
-        items = std::max<uint64_t>(items, b->trace_offset[i] + b->trace_capacity[i]);
+        if (!exact) items = std::max<uint64_t>(items, b->trace_offset[i] + b->trace_capacity[i]);
     }
     const uint64_t seeds = seedEnd;     // seed arrays are indexed from 0 as given
-    const uint64_t tables = (uint64_t)n * b->max_traces;
+    const uint64_t tables = exact ? 0 : (uint64_t)n * b->max_traces;
     std::vector<uint32_t>& order = x->orderHost;
     order = longest_first(b->seq_len, n);
     GA_CUDA(x->seq.reserve(std::max<uint64_t>(seqBytes, 1)));
@@ -554,10 +637,15 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     GA_CUDA(x->msItemsNeeded.reserve(n));
     GA_CUDA(x->msTracesNeeded.reserve(n));
     GA_CUDA(x->cellSteps.reserve(n));
-    GA_CUDA(x->msTraceScore.reserve(tables));
-    GA_CUDA(x->msTraceStart.reserve(tables));
-    GA_CUDA(x->msTraceLen.reserve(tables));
+    GA_CUDA(x->msTraceScore.reserve(std::max<uint64_t>(tables, 1)));
+    GA_CUDA(x->msTraceStart.reserve(std::max<uint64_t>(tables, 1)));
+    GA_CUDA(x->msTraceLen.reserve(std::max<uint64_t>(tables, 1)));
     GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(items, 1)));
+    if (exact)
+    {
+        GA_CUDA(x->msTraceBase.reserve(n));
+        GA_CUDA(x->msItemBase.reserve(n));
+    }
     GA_CUDA(x->states.reserve(n));
     GA_CUDA(x->msCandBegin.reserve(n));
     GA_CUDA(x->msCandCount.reserve(n));
@@ -571,8 +659,11 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
         GA_CUDA(cudaMemcpyAsync(x->msSeedSlice.ptr, b->seed_slice, seeds * 4, cudaMemcpyHostToDevice, s));
         GA_CUDA(cudaMemcpyAsync(x->msSeedNode.ptr, b->seed_node, seeds * 4, cudaMemcpyHostToDevice, s));
     }
-    GA_CUDA(cudaMemcpyAsync(x->traceOff.ptr, b->trace_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
-    GA_CUDA(cudaMemcpyAsync(x->msTraceCap.ptr, b->trace_capacity, n * 8ULL, cudaMemcpyHostToDevice, s));
+    if (!exact)
+    {
+        GA_CUDA(cudaMemcpyAsync(x->traceOff.ptr, b->trace_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
+        GA_CUDA(cudaMemcpyAsync(x->msTraceCap.ptr, b->trace_capacity, n * 8ULL, cudaMemcpyHostToDevice, s));
+    }
     GA_CUDA(cudaMemcpyAsync(x->order.ptr, order.data(), n * 4ULL, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemsetAsync(x->msItemsNeeded.ptr, 0, n * 8ULL, s));
     GA_CUDA(cudaMemsetAsync(x->msTracesNeeded.ptr, 0, n * 4ULL, s));
@@ -606,9 +697,12 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     ta.seqOff = x->seqOff.ptr;
     ta.seqLen = x->seqLen.ptr;
     ta.arena = x->arena;
-    ta.traceOffset = x->traceOff.ptr;
-    ta.traceCap = x->msTraceCap.ptr;
-    ta.maxTraces = b->max_traces;
+    ta.traceOffset = exact ? nullptr : x->traceOff.ptr;
+    ta.traceCap = exact ? nullptr : x->msTraceCap.ptr;
+    ta.maxTraces = exact ? 0 : b->max_traces;
+    ta.traceBase = exact ? x->msTraceBase.ptr : nullptr;
+    ta.itemBase = exact ? x->msItemBase.ptr : nullptr;
+    ta.itemBias = 0;
     ta.multimapScoreFraction = b->multimap_score_fraction;
     ta.status = x->status.ptr;
     ta.numTraces = x->msNumTraces.ptr;
@@ -625,6 +719,8 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
 
     x->lastFillMs = 0;
     x->lastLaunches = 0;
+    x->lastCandidates = 0;
+    x->lastKept = 0;
     for (int k = 0; k < 3; k++) x->lastRounds[k] = 0;
     const int wpb = 4;
     uint32_t pending = n;
@@ -635,6 +731,14 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
     // read whose traces outgrow its output room (kMsRoom) is not run again: it reports the
     // room it needs.  Between the fill and the traceback the host sizes the candidate list.
     int layout = 1;
+    std::vector<uint8_t> finished(exact ? n : 0, 0);
+    std::vector<uint64_t> passUsed, traceBase, itemBase;
+    if (exact)
+    {
+        passUsed.resize(n);
+        traceBase.assign(n, 0);
+        itemBase.assign(n, 0);
+    }
     for (int pass = 0; pass < 32; pass++)
     {
         const gadev::Caps caps = layout_caps(layout);
@@ -660,9 +764,61 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
         GA_CUDA(x->msCands.reserve(std::max<uint64_t>(candTotal, 1)));
         ta.cands = x->msCands.ptr;
         ta.candCap = x->msCands.count;
+        x->lastCandidates += candTotal;
         const uint64_t candBlocks = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)x->sms * 6, (candTotal + wpb - 1) / wpb));
         if (ga_launch_multiseed_trace(ta, x->counters, (int)readBlocks, (int)candBlocks, wpb, s) != 0)
             return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+        if (exact)
+        {
+            // the reads this pass finished take their room: trace and item runs after the earlier
+            // passes' (the tables of this pass are gone once the next one starts)
+            MsExactOut& o = x->msOut;
+            GA_CUDA(cudaMemcpyAsync(o.status.data(), x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+            GA_CUDA(cudaMemcpyAsync(o.numTraces.data(), x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+            GA_CUDA(cudaMemcpyAsync(passUsed.data(), x->msItemsNeeded.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
+            GA_CUDA(cudaStreamSynchronize(s));
+            uint64_t passTraces = 0, passItems = 0;
+            for (uint32_t i = 0; i < n; i++)
+            {
+                if (finished[i] || o.status[i] == GA_CAPACITY) continue;
+                finished[i] = 1;
+                if (o.status[i] != GA_OK) continue;
+                traceBase[i] = passTraces;
+                itemBase[i] = passItems;
+                o.traceFirst[i] = o.traces + passTraces;
+                passTraces += o.numTraces[i];
+                passItems += passUsed[i];
+            }
+            GA_CUDA(x->msTraceScore.reserve(std::max<uint64_t>(passTraces, 1)));
+            GA_CUDA(x->msTraceStart.reserve(std::max<uint64_t>(passTraces, 1)));
+            GA_CUDA(x->msTraceLen.reserve(std::max<uint64_t>(passTraces, 1)));
+            GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(passItems, 1)));
+            GA_CUDA(cudaMemcpyAsync(x->msTraceBase.ptr, traceBase.data(), n * 8ULL, cudaMemcpyHostToDevice, s));
+            GA_CUDA(cudaMemcpyAsync(x->msItemBase.ptr, itemBase.data(), n * 8ULL, cudaMemcpyHostToDevice, s));
+            ta.traceScore = x->msTraceScore.ptr;
+            ta.traceStart = x->msTraceStart.ptr;
+            ta.traceLen = x->msTraceLen.ptr;
+            ta.traceItems = x->traceItems.ptr;
+            ta.itemBias = o.items;
+            if (ga_launch_multiseed_write(ta, x->counters, (int)candBlocks, wpb, s) != 0)
+                return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+            if (!o.grow(o.traces + passTraces, o.items + passItems))
+                return fail(GA_ERR_CUDA, "ga_multiseed_batch_exact: pinned host memory for the traces");
+            if (passTraces)
+            {
+                GA_CUDA(cudaMemcpyAsync(o.score.ptr + o.traces, x->msTraceScore.ptr, passTraces * 4, cudaMemcpyDeviceToHost, s));
+                GA_CUDA(cudaMemcpyAsync(o.start.ptr + o.traces, x->msTraceStart.ptr, passTraces * 8, cudaMemcpyDeviceToHost, s));
+                GA_CUDA(cudaMemcpyAsync(o.len.ptr + o.traces, x->msTraceLen.ptr, passTraces * 4, cudaMemcpyDeviceToHost, s));
+            }
+            if (passItems) GA_CUDA(cudaMemcpyAsync(o.item.ptr + o.items, x->traceItems.ptr, passItems * 8, cudaMemcpyDeviceToHost, s));
+            o.traces += passTraces;
+            o.items += passItems;
+        }
+        else
+        {
+            if (ga_launch_multiseed_write(ta, x->counters, (int)candBlocks, wpb, s) != 0)
+                return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+        }
         x->lastLaunches += 6;
         x->lastRounds[layout] += pending;
         GA_CUDA(cudaEventRecord(x->ev[1], s));
@@ -684,20 +840,72 @@ extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, co
             layout = 2;
         }
     }
+    if (exact)
+    {
+        // a kept trace whose written walk failed fails its read after the counts were taken
+        MsExactOut& o = x->msOut;
+        GA_CUDA(cudaMemcpyAsync(o.status.data(), x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+        GA_CUDA(cudaMemcpyAsync(o.cellSteps.data(), x->cellSteps.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
+        GA_CUDA(cudaStreamSynchronize(s));
+        for (uint32_t i = 0; i < n; i++)
+        {
+            if (o.status[i] != GA_OK) o.numTraces[i] = 0;
+            x->lastKept += o.numTraces[i];
+        }
+        o.publish(ex);
+        return GA_OK;
+    }
     GA_CUDA(cudaMemcpyAsync(r->status, x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->num_traces, x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
-    GA_CUDA(cudaStreamSynchronize(s));
-    for (uint32_t i = 0; i < n; i++)
-        if (r->status[i] == gadev::kMsRoom) r->status[i] = GA_CAPACITY;
     GA_CUDA(cudaMemcpyAsync(r->trace_score, x->msTraceScore.ptr, tables * 4, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->trace_start, x->msTraceStart.ptr, tables * 8, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaMemcpyAsync(r->trace_len, x->msTraceLen.ptr, tables * 4, cudaMemcpyDeviceToHost, s));
-    if (items) GA_CUDA(cudaMemcpyAsync(r->trace_items, x->traceItems.ptr, items * 8, cudaMemcpyDeviceToHost, s));
     if (r->cell_steps) GA_CUDA(cudaMemcpyAsync(r->cell_steps, x->cellSteps.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
     if (r->items_needed) GA_CUDA(cudaMemcpyAsync(r->items_needed, x->msItemsNeeded.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
     if (r->traces_needed) GA_CUDA(cudaMemcpyAsync(r->traces_needed, x->msTracesNeeded.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
     GA_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < n; i++)
+    {
+        if (r->status[i] == gadev::kMsRoom) r->status[i] = GA_CAPACITY;
+        if (r->status[i] == GA_OK) x->lastKept += r->num_traces[i];
+    }
+    // Trace items: a read's traces lie back to back from its trace_offset, and only those come
+    // back (the room is usually far larger), in runs that take in gaps of up to 256 KiB.
+    const uint64_t kGap = 32768;
+    uint64_t runFrom = 0, runTo = 0;
+    bool open = false;
+    for (uint32_t i = 0; i < n; i++)
+    {
+        if (r->status[i] != GA_OK) continue;
+        uint64_t used = 0;
+        for (uint32_t t = 0; t < r->num_traces[i]; t++) used += r->trace_len[(uint64_t)i * b->max_traces + t];
+        if (used == 0) continue;
+        const uint64_t from = b->trace_offset[i], to = from + used;
+        if (open && from >= runTo && from - runTo <= kGap)
+        {
+            runTo = to;
+            continue;
+        }
+        if (open) GA_CUDA(cudaMemcpyAsync(r->trace_items + runFrom, x->traceItems.ptr + runFrom, (runTo - runFrom) * 8, cudaMemcpyDeviceToHost, s));
+        runFrom = from;
+        runTo = to;
+        open = true;
+    }
+    if (open) GA_CUDA(cudaMemcpyAsync(r->trace_items + runFrom, x->traceItems.ptr + runFrom, (runTo - runFrom) * 8, cudaMemcpyDeviceToHost, s));
+    GA_CUDA(cudaStreamSynchronize(s));
     return GA_OK;
+}
+
+extern "C" int ga_multiseed_batch(ga_extender_t x, const ga_extend_params* p, const ga_multiseed_batch_desc* b, ga_multiseed_results* r)
+{
+    if (!r) return fail(GA_ERR_ARGUMENT, "null argument");
+    return multiseed_run(x, p, b, r, nullptr);
+}
+
+extern "C" int ga_multiseed_batch_exact(ga_extender_t x, const ga_extend_params* p, const ga_multiseed_batch_desc* b, ga_multiseed_output* out)
+{
+    if (!out) return fail(GA_ERR_ARGUMENT, "null argument");
+    return multiseed_run(x, p, b, nullptr, out);
 }
 
 extern "C" int ga_extender_autotune(ga_extender_t x, const ga_extend_params* p, const ga_extend_batch_desc* b,
@@ -828,6 +1036,14 @@ extern "C" int ga_extender_last_layout_counts(ga_extender_t x, uint32_t counts[3
 {
     if (!x || !counts) return fail(GA_ERR_ARGUMENT, "null argument");
     for (int k = 0; k < 3; k++) counts[k] = x->lastRounds[k];
+    return GA_OK;
+}
+
+extern "C" int ga_extender_last_multiseed_counts(ga_extender_t x, uint64_t* candidates, uint64_t* traces)
+{
+    if (!x || !candidates || !traces) return fail(GA_ERR_ARGUMENT, "null argument");
+    *candidates = x->lastCandidates;
+    *traces = x->lastKept;
     return GA_OK;
 }
 

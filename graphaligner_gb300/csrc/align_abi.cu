@@ -74,76 +74,56 @@ void ga_aligner_extend(void* ctx, const std::vector<gahost::ExtensionRequest>& r
     }
 }
 
-// The multiseed DP of a group of reads through ga_multiseed_batch; reads whose traces outgrow
-// their room run again with the room the first run measured for them.
+// The multiseed DP of a group of reads through ga_multiseed_batch_exact: every read's traces
+// in the extender's buffers, which the results point into until the next call.
 void ga_aligner_multiseed(void* ctx, const std::vector<gahost::MultiseedRequest>& rq, std::vector<gahost::MultiseedResult>& rs)
 {
     MultiseedLane* m = (MultiseedLane*)ctx;
     const auto t0 = std::chrono::steady_clock::now();
-    std::vector<size_t> todo(rq.size());
-    for (size_t i = 0; i < rq.size(); i++) todo[i] = i;
-    std::vector<uint64_t> wantItems(rq.size(), 0);
-    std::vector<uint32_t> wantTraces(rq.size(), 0);
-    for (int attempt = 0; attempt < 2 && !todo.empty(); attempt++)
+    const size_t n = rq.size();
+    m->off.assign(n, 0); m->len.assign(n, 0); m->seedOff.assign(n + 1, 0);
+    m->slices.clear(); m->nodes.clear(); m->blob.clear();
+    for (size_t k = 0; k < n; k++)
     {
-        const size_t n = todo.size();
-        uint32_t maxTraces = 64;
-        if (attempt > 0)
+        const auto& q = rq[k];
+        m->off[k] = m->blob.size();
+        m->blob.insert(m->blob.end(), q.seq, q.seq + q.len);
+        m->len[k] = q.len;
+        m->slices.insert(m->slices.end(), q.slices, q.slices + q.numSeeds);
+        m->nodes.insert(m->nodes.end(), q.nodes, q.nodes + q.numSeeds);
+        m->seedOff[k + 1] = m->slices.size();
+    }
+    if (m->blob.empty()) m->blob.push_back(0);
+    ga_multiseed_batch_desc b { (uint32_t)n, m->blob.data(), m->off.data(), m->len.data(), m->seedOff.data(),
+        m->slices.empty() ? nullptr : m->slices.data(), m->nodes.empty() ? nullptr : m->nodes.data(), nullptr, nullptr, 0,
+        m->multimapScoreFraction };
+    ga_multiseed_output o {};
+    const int rc = ga_multiseed_batch_exact(m->ext, m->params, &b, &o);
+    float kernelMs = 0;
+    if (rc == GA_OK && ga_extender_last_kernel_ms(m->ext, &kernelMs) == GA_OK) m->kernelMs += kernelMs;
+    uint64_t candidates = 0, traces = 0;
+    if (rc == GA_OK && ga_extender_last_multiseed_counts(m->ext, &candidates, &traces) == GA_OK)
+    {
+        m->candidates += candidates;
+        m->traces += traces;
+    }
+    for (size_t k = 0; k < n; k++)
+    {
+        gahost::MultiseedResult& out = rs[k];
+        out.status = rc == GA_OK ? o.status[k] : GA_CAPACITY;
+        out.steps = rc == GA_OK ? o.cell_steps[k] : 0;
+        out.scores.clear();
+        out.items.clear();
+        out.lengths.clear();
+        out.own.clear();
+        if (out.status != GA_OK) continue;
+        for (uint32_t t = 0; t < o.num_traces[k]; t++)
         {
-            maxTraces = 1;
-            for (size_t k = 0; k < n; k++) maxTraces = std::max(maxTraces, wantTraces[todo[k]]);
+            const uint64_t i = o.trace_first[k] + t;
+            out.scores.push_back(o.trace_score[i]);
+            out.items.push_back(o.trace_items + o.trace_start[i]);
+            out.lengths.push_back(o.trace_len[i]);
         }
-        m->off.assign(n, 0); m->len.assign(n, 0); m->seedOff.assign(n + 1, 0); m->toff.assign(n, 0); m->cap.assign(n, 0);
-        m->slices.clear(); m->nodes.clear(); m->blob.clear();
-        uint64_t items = 0;
-        for (size_t k = 0; k < n; k++)
-        {
-            const auto& q = rq[todo[k]];
-            m->off[k] = m->blob.size();
-            m->blob.insert(m->blob.end(), q.seq, q.seq + q.len);
-            m->len[k] = q.len;
-            m->slices.insert(m->slices.end(), q.slices, q.slices + q.numSeeds);
-            m->nodes.insert(m->nodes.end(), q.nodes, q.nodes + q.numSeeds);
-            m->seedOff[k + 1] = m->slices.size();
-            m->cap[k] = attempt == 0 ? (uint64_t)q.len * 16 + 4096 : wantItems[todo[k]] + 64;
-            m->toff[k] = items;
-            items += m->cap[k];
-        }
-        if (m->blob.empty()) m->blob.push_back(0);
-        m->status.assign(n, 0); m->ntr.assign(n, 0); m->steps.assign(n, 0); m->needItems.assign(n, 0); m->needTraces.assign(n, 0);
-        m->tscore.assign((size_t)n * maxTraces, 0); m->tstart.assign((size_t)n * maxTraces, 0); m->tlen.assign((size_t)n * maxTraces, 0);
-        m->items.resize(std::max<uint64_t>(items, 1));
-        ga_multiseed_batch_desc b { (uint32_t)n, m->blob.data(), m->off.data(), m->len.data(), m->seedOff.data(),
-            m->slices.empty() ? nullptr : m->slices.data(), m->nodes.empty() ? nullptr : m->nodes.data(), m->toff.data(), m->cap.data(),
-            maxTraces, m->multimapScoreFraction };
-        ga_multiseed_results r { m->status.data(), m->ntr.data(), m->tscore.data(), m->tstart.data(), m->tlen.data(), m->items.data(), m->steps.data(),
-            m->needItems.data(), m->needTraces.data() };
-        const int rc = ga_multiseed_batch(m->ext, m->params, &b, &r);
-        std::vector<size_t> again;
-        for (size_t k = 0; k < n; k++)
-        {
-            gahost::MultiseedResult& out = rs[todo[k]];
-            out.status = rc == GA_OK ? m->status[k] : GA_CAPACITY;
-            out.steps = m->steps[k];
-            out.scores.clear();
-            out.traces.clear();
-            if (out.status == GA_CAPACITY && attempt == 0 && rc == GA_OK && (m->needItems[k] > 0 || m->needTraces[k] > 0))
-            {
-                wantItems[todo[k]] = m->needItems[k];
-                wantTraces[todo[k]] = m->needTraces[k];
-                again.push_back(todo[k]);
-                continue;
-            }
-            if (out.status != GA_OK) continue;
-            for (uint32_t t = 0; t < m->ntr[k]; t++)
-            {
-                const size_t slot = k * maxTraces + t;
-                const uint64_t* first = m->items.data() + m->toff[k] + m->tstart[slot];
-                out.scores.push_back(m->tscore[slot]);
-                out.traces.emplace_back(first, first + m->tlen[slot]);
-            }
-        }
-        todo.swap(again);
     }
     m->ms += ms_since(t0);
 }
@@ -353,6 +333,9 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     // two groups of reads on two extenders, the host finishing one group's round while
     // the other's runs on the GPU; small batches use one
     a->multiseed.ms = 0;
+    a->multiseed.kernelMs = 0;
+    a->multiseed.candidates = 0;
+    a->multiseed.traces = 0;
     if (a->params.multiseed_dp)
     {
         a->multiseed.ext = a->ext;
@@ -385,6 +368,9 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     a->stats.rounds = bs.rounds;
     a->stats.extensions = bs.extensions;
     a->stats.cell_steps = bs.cellSteps;
+    a->stats.multiseed_kernel_ms = a->multiseed.kernelMs;
+    a->stats.multiseed_candidates = a->multiseed.candidates;
+    a->stats.multiseed_traces = a->multiseed.traces;
     // with two lanes the GPU calls overlap host work: host_ms is what they do not cover
     a->stats.host_ms = std::max(0.0, ms_since(start) - a->stats.extend_ms);
     return GA_OK;

@@ -82,10 +82,11 @@ struct MultiseedLane
     const ga_extend_params* params = nullptr;
     double multimapScoreFraction = 0.9;
     std::vector<uint8_t> blob;
-    std::vector<uint64_t> off, seedOff, toff, cap, tstart, items, steps, needItems;
-    std::vector<uint32_t> len, slices, nodes, ntr, tlen, needTraces;
-    std::vector<int32_t> status, tscore;
+    std::vector<uint64_t> off, seedOff;
+    std::vector<uint32_t> len, slices, nodes;
     double ms = 0;
+    double kernelMs = 0;                   // of ms: the batch's kernels and trace copies
+    uint64_t candidates = 0, traces = 0;   // local maxima counted, traces kept
 };
 
 // The device GAF formatter and alignment selection (gaf_device.cu): the graph's node names

@@ -2249,8 +2249,9 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
     {
         err = ms_start_cell(a, t, w, seq, seqLen, c, start, startScore, lane);
     }
+    const bool exact = a.traceBase != nullptr;
     TraceOut to;
-    to.items = write ? a.traceItems + a.traceOffset[r] + c.outOff : nullptr;
+    to.items = write ? a.traceItems + (exact ? a.itemBase[r] : a.traceOffset[r]) + c.outOff : nullptr;
     to.ring = w.ring;
     to.lane = lane;
     to.counting = !write;
@@ -2289,9 +2290,9 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
         }
         else
         {
-            const u64 slot = (u64)r * a.maxTraces + c.slot;
+            const u64 slot = exact ? a.traceBase[r] + c.slot : (u64)r * a.maxTraces + c.slot;
             a.traceScore[slot] = traceScore;
-            a.traceStart[slot] = c.outOff;
+            a.traceStart[slot] = exact ? a.itemBias + a.itemBase[r] + c.outOff : c.outOff;
             a.traceLen[slot] = to.n;
         }
     }
@@ -2302,7 +2303,8 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
 // a candidate reaching the multimap fraction of its slice's best (as raised so far) is kept,
 // and raises the best of the slices its trace spans beyond its first 5 %.  Kept traces get
 // their place in the read's output while they fit its room (max_traces, trace_capacity);
-// past that they are only counted, and the read reports the room it needs.
+// past that they are only counted, and the read reports the room it needs.  With exact room
+// (a.traceBase) every kept trace gets its place, and the read reports the items they take.
 __device__ void ms_select(const MultiTraceArgs& a, u32 r, const ExtState& st, u32 lane)
 {
     if (lane == 0 && a.cellSteps) a.cellSteps[r] = st.steps;
@@ -2316,7 +2318,9 @@ __device__ void ms_select(const MultiTraceArgs& a, u32 r, const ExtState& st, u3
         return;
     }
     i32* sliceMax = (i32*)(a.arena + st.aux);
-    const u64 cap = a.traceCap[r];
+    const bool exact = a.traceBase != nullptr;
+    const u64 cap = exact ? ~0ULL : a.traceCap[r];
+    const u32 maxTraces = exact ? 0xffffffffu : a.maxTraces;
     const u64 begin = a.candBegin[r];
     const u32 count = a.candCount[r];
     u64 used = 0, items = 0;
@@ -2336,7 +2340,7 @@ __device__ void ms_select(const MultiTraceArgs& a, u32 r, const ExtState& st, u3
             break;
         }
         const u32 len = cp->len;
-        if (room && (nt >= a.maxTraces || len > cap - used)) room = false;
+        if (room && (nt >= maxTraces || len > cap - used)) room = false;
         if (room)
         {
             if (lane == 0)
@@ -2360,7 +2364,8 @@ __device__ void ms_select(const MultiTraceArgs& a, u32 r, const ExtState& st, u3
     {
         a.status[r] = err ? err : (room ? GA_OK : kMsRoom);
         a.numTraces[r] = (err || !room) ? 0 : nt;
-        if (a.itemsNeeded) a.itemsNeeded[r] = (!err && !room) ? items : 0;
+        // with exact room: the items the read's traces take
+        if (a.itemsNeeded) a.itemsNeeded[r] = err ? 0 : (exact ? used : (!room ? items : 0));
         if (a.tracesNeeded) a.tracesNeeded[r] = (!err && !room) ? traces : 0;
     }
     __syncwarp();
@@ -2612,8 +2617,14 @@ int ga_launch_multiseed_trace(const gadev::MultiTraceArgs& ta, uint32_t* counter
     gadev::ms_trace_kernel<<<candBlocks, warpsPerBlock * 32, traceSmem, s>>>(ta, counters + 4, 0);
     if (cudaGetLastError() != cudaSuccess) return -1;
     gadev::ms_select_kernel<<<readBlocks, warpsPerBlock * 32, 0, s>>>(ta, counters + 5);
-    if (cudaGetLastError() != cudaSuccess) return -1;
-    gadev::ms_trace_kernel<<<candBlocks, warpsPerBlock * 32, traceSmem, s>>>(ta, counters + 6, 1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int ga_launch_multiseed_write(const gadev::MultiTraceArgs& ta, uint32_t* counters, int candBlocks, int warpsPerBlock, void* stream)
+{
+    const size_t traceSmem = (size_t)gadev::kTraceSpaceBytes * warpsPerBlock;
+    if (!set_smem((const void*)gadev::ms_trace_kernel, traceSmem)) return -1;
+    gadev::ms_trace_kernel<<<candBlocks, warpsPerBlock * 32, traceSmem, (cudaStream_t)stream>>>(ta, counters + 6, 1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

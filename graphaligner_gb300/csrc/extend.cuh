@@ -183,6 +183,12 @@ struct MultiTraceArgs
     u64* cellSteps;
     u64* itemsNeeded;      // [num] or null: when the traces outgrow the read's room, the room they need
     u32* tracesNeeded;
+    // exact room (traceBase non-null): read i's kept traces go to the trace tables from
+    // traceBase[i] and their items from itemBase[i], and a trace's start is counted from
+    // itemBias; traceOffset, traceCap and maxTraces are not used
+    const u64* traceBase;
+    const u64* itemBase;
+    u64 itemBias;
     MsCand* cands;         // [candCap] the batch's candidates, each read's together and in order
     u64 candCap;
     u64* candBegin;        // [num] read i's candidates are [candBegin[i], candBegin[i] + candCount[i])
@@ -205,12 +211,13 @@ int ga_trace_blocks_per_sm(int warpsPerBlock);
 int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
     int warpsPerBlock, void* stream);
 // the multiseed DP's fill and traceback kernels (the frontier tables always in the global workspace)
-// the multiseed DP in two steps, blocks of warpsPerBlock warps: the fill and the count of each
-// read's trace candidates (counters[0], [1] zero; ta.candTotal zero), then, once ta.cands has
-// room for *ta.candTotal, the candidates listed, traced, selected and the kept ones written
-// (counters[3] to [6] zero); counters[2] is left to the caller
+// the multiseed DP in steps, blocks of warpsPerBlock warps: the fill and the count of each
+// read's trace candidates (counters[0], [1] zero; ta.candTotal zero); then, once ta.cands has
+// room for *ta.candTotal, the candidates listed, traced and selected (counters[3] to [5]
+// zero); then the kept traces written (counters[6] zero).  counters[2] is left to the caller.
 int ga_launch_multiseed_fill(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int readBlocks,
     int warpsPerBlock, void* stream);
 int ga_launch_multiseed_trace(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int candBlocks, int warpsPerBlock, void* stream);
+int ga_launch_multiseed_write(const gadev::MultiTraceArgs& ta, uint32_t* counters, int candBlocks, int warpsPerBlock, void* stream);
 int ga_upload_tables();
 void ga_set_last_error(const char* message);

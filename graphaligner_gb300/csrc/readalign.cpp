@@ -1197,14 +1197,14 @@ void alignBatchMultiseed(const HostGraph& g, const ReadAlignParams& p, std::vect
         }
         try
         {
-            std::vector<OnewayTrace> traces(res.traces.size());
-            for (size_t t = 0; t < res.traces.size(); t++)
+            std::vector<OnewayTrace> traces(res.items.size());
+            for (size_t t = 0; t < res.items.size(); t++)
             {
                 ExtensionResult e;
                 e.status = GA_OK;
                 e.score = res.scores[t];
-                e.itemPtr = res.traces[t].data();
-                e.itemCount = res.traces[t].size();
+                e.itemPtr = res.items[t];
+                e.itemCount = res.lengths[t];
                 traces[t] = decodeTrace(g, e, m.r.seq.data(), m.r.seq.size());
                 GAH_ASSERT(!traces[t].trace.empty());
             }

@@ -254,7 +254,10 @@ struct MultiseedResult
     int32_t status = 0;
     uint64_t steps = 0;
     std::vector<int32_t> scores;
-    std::vector<std::vector<uint64_t>> traces;   // packed items
+    // each trace's packed items: in `own`, or in the callback's buffers until its next call
+    std::vector<const uint64_t*> items;
+    std::vector<uint32_t> lengths;
+    std::vector<uint64_t> own;
 };
 
 typedef void (*MultiseedFn)(void* ctx, const std::vector<MultiseedRequest>& requests, std::vector<MultiseedResult>& results);

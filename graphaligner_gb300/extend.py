@@ -233,6 +233,39 @@ class MultiseedResult:
         return out
 
 
+@dataclasses.dataclass
+class MultiseedExactResult:
+    """ga_multiseed_batch_exact's output, copied out of the extender's buffers."""
+    status: np.ndarray
+    num_traces: np.ndarray
+    trace_first: np.ndarray
+    trace_score: np.ndarray
+    trace_start: np.ndarray
+    trace_len: np.ndarray
+    trace_items: np.ndarray
+    cell_steps: np.ndarray
+
+    @classmethod
+    def copy_of(cls, o, n: int):
+        def arr(p, count, dtype):
+            if count == 0 or not p:
+                return np.zeros(0, dtype)
+            return np.ctypeslib.as_array(p, shape=(count,)).astype(dtype, copy=True)
+        t, i = int(o.total_traces), int(o.total_items)
+        return cls(arr(o.status, n, np.int32), arr(o.num_traces, n, np.uint32), arr(o.trace_first, n, np.uint64),
+                   arr(o.trace_score, t, np.int32), arr(o.trace_start, t, np.uint64), arr(o.trace_len, t, np.uint32),
+                   arr(o.trace_items, i, np.uint64), arr(o.cell_steps, n, np.uint64))
+
+    def traces(self, i: int):
+        """Read i's traces as (score, packed items), in the DP's order."""
+        out = []
+        for t in range(int(self.num_traces[i])):
+            k = int(self.trace_first[i]) + t
+            o = int(self.trace_start[k])
+            out.append((int(self.trace_score[k]), self.trace_items[o:o + int(self.trace_len[k])]))
+        return out
+
+
 class DeviceGraph:
     """AlignmentGraph arrays resident in HBM (ga_graph_upload)."""
 
@@ -309,6 +342,14 @@ class Extender:
         rd = r.desc()
         check(lib().ga_multiseed_batch(self.handle, ctypes.byref(p), ctypes.byref(d), ctypes.byref(rd)))
         return r
+
+    def multiseed_exact(self, params: ExtendParams, batch: MultiseedBatch) -> MultiseedExactResult:
+        """ga_multiseed_batch_exact: the same DP with every read's traces in room sized to them."""
+        o = _abi.MultiseedOutput()
+        p = params.c()
+        d = batch.desc()
+        check(lib().ga_multiseed_batch_exact(self.handle, ctypes.byref(p), ctypes.byref(d), ctypes.byref(o)))
+        return MultiseedExactResult.copy_of(o, batch.num)
 
     def launch_shape(self) -> LaunchShape:
         sh = LaunchShape()

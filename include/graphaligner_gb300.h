@@ -168,9 +168,33 @@ typedef struct ga_multiseed_results {
 /* Host buffers in and out, like ga_extend_batch.  Seeds outside the graph or their read, or
  * out of slice order, are GA_ERR_ARGUMENT.  A read whose traces outgrow trace_capacity or
  * max_traces reports GA_CAPACITY with the room it needs in items_needed / traces_needed; run
- * it again with that room. */
+ * it again with that room.  Of trace_items only the GA_OK reads' traces are defined after the
+ * call; the rest of the span the batch's rooms cover may be overwritten. */
 int ga_multiseed_batch(ga_extender_t ext, const ga_extend_params* params,
                        const ga_multiseed_batch_desc* batch, ga_multiseed_results* results);
+
+/* The same DP with no room limit, closer to the reference's getMultiseedTraces (which returns
+ * every trace): each read's traces land in buffers the extender owns, sized once they are
+ * counted, so no read has to run twice.  Read i's traces are trace_first[i] ..
+ * trace_first[i] + num_traces[i] - 1 of the trace arrays; trace_start indexes trace_items.
+ * batch->trace_offset, trace_capacity and max_traces are not used (may be NULL / 0).  The
+ * arrays stay valid until the extender's next call or ga_extender_free.  GA_CAPACITY now
+ * means only that the read's frontier tables outgrew the largest layout. */
+typedef struct ga_multiseed_output {
+    const int32_t*  status;           /* [num] */
+    const uint32_t* num_traces;       /* [num] */
+    const uint64_t* trace_first;      /* [num] */
+    const int32_t*  trace_score;      /* [total_traces] OnewayTrace::score */
+    const uint64_t* trace_start;      /* [total_traces] */
+    const uint32_t* trace_len;        /* [total_traces] */
+    const uint64_t* trace_items;      /* [total_items] packed items (GA_TRACE_* layout) */
+    const uint64_t* cell_steps;       /* [num] */
+    uint64_t total_traces;
+    uint64_t total_items;
+} ga_multiseed_output;
+
+int ga_multiseed_batch_exact(ga_extender_t ext, const ga_extend_params* params,
+                             const ga_multiseed_batch_desc* batch, ga_multiseed_output* out);
 
 /* Device-resident variant: every pointer in batch/results is a device pointer.
  * Work is enqueued on `stream` (a cudaStream_t; NULL = the extender's stream);
@@ -248,6 +272,9 @@ int ga_extender_autotune(ga_extender_t ext, const ga_extend_params* params,
 int ga_extender_last_arena_bytes(ga_extender_t ext, uint64_t* bytes);
 /* Extensions run with each table layout (0, 1, 2) by the last call (0 = layout not run). */
 int ga_extender_last_layout_counts(ga_extender_t ext, uint32_t counts[3]);
+/* The last multiseed call's local-maximum candidates (each walked once to count its trace)
+ * and the traces it kept, summed over its passes. */
+int ga_extender_last_multiseed_counts(ga_extender_t ext, uint64_t* candidates, uint64_t* traces);
 
 /* ---- utilities (no reference counterpart) ---- */
 /* Page-locked host memory for the host-buffer entry points. */
@@ -316,6 +343,9 @@ typedef struct ga_align_stats {
     uint64_t speculative_discarded;    /* ... and sent ahead but not used (the loop went elsewhere) */
     double   seed_lookup_ms;           /* of seed_ms: reads in, k-mer lookup kernel, matches back */
     double   seed_select_ms;           /*             least-frequent selection per read (host) */
+    double   multiseed_kernel_ms;      /* of extend_ms with multiseed_dp: the multiseed DP's kernels and trace copies */
+    uint64_t multiseed_candidates;     /* local maxima whose traces were counted */
+    uint64_t multiseed_traces;         /* traces the multiseed DPs kept */
 } ga_align_stats;
 
 typedef struct ga_aligner* ga_aligner_t;

@@ -296,7 +296,9 @@ static void oracleMultiseed(void* ctx, const std::vector<gahost::MultiseedReques
             out.status = status[k];
             out.steps = steps[k];
             out.scores.clear();
-            out.traces.clear();
+            out.items.clear();
+            out.lengths.clear();
+            out.own.clear();
             if (status[k] == GA_CAPACITY && attempt == 0 && (needI[k] > 0 || needT[k] > 0))
             {
                 wantItems[todo[k]] = needI[k];
@@ -308,7 +310,14 @@ static void oracleMultiseed(void* ctx, const std::vector<gahost::MultiseedReques
             {
                 const size_t slot = k * maxTraces + t;
                 out.scores.push_back(tscore[slot]);
-                out.traces.emplace_back(items.begin() + toff[k] + tstart[slot], items.begin() + toff[k] + tstart[slot] + tlen[slot]);
+                out.lengths.push_back(tlen[slot]);
+                out.own.insert(out.own.end(), items.begin() + toff[k] + tstart[slot], items.begin() + toff[k] + tstart[slot] + tlen[slot]);
+            }
+            uint64_t at = 0;
+            for (uint32_t t = 0; t < ntr[k]; t++)
+            {
+                out.items.push_back(out.own.data() + at);
+                at += tlen[k * maxTraces + t];
             }
         }
         todo.swap(again);

@@ -66,6 +66,14 @@ def test_gpu_multiseed_traces_match_oracle(cuda_lib, oracle_lib, harness, tmp_pa
                 break
     assert not bad, f"reads {bad[:10]} differ"
     assert int(cpu.num_traces.sum()) > batch.num
+    # with exact room: the same traces, in room sized to them
+    ex = Extender(DeviceGraph(g)).multiseed_exact(p, batch)
+    assert np.array_equal(ex.status, cpu.status)
+    assert np.array_equal(ex.num_traces, cpu.num_traces)
+    assert int(ex.trace_len.sum()) == len(ex.trace_items)
+    bad = [i for i in range(batch.num)
+           if any(gs != cs or not np.array_equal(gi, ci) for (gs, gi), (cs, ci) in zip(ex.traces(i), cpu.traces(i)))]
+    assert not bad, f"reads {bad[:10]} differ with exact room"
 
 
 def test_gpu_multiseed_reports_capacity(cuda_lib, oracle_lib, harness, tmp_path):  # noqa: F811
