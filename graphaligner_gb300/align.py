@@ -83,7 +83,7 @@ class AlignStats(ctypes.Structure):
                [(n, ctypes.c_double) for n in ("seed_ms", "extend_ms", "host_ms", "collect_ms", "staging_ms", "consume_ms", "finish_ms")] + \
               [(n, ctypes.c_uint64) for n in ("speculative_used", "speculative_discarded")] + \
               [(n, ctypes.c_double) for n in ("seed_lookup_ms", "seed_select_ms", "multiseed_kernel_ms")] + \
-              [(n, ctypes.c_uint64) for n in ("multiseed_candidates", "multiseed_traces")]
+              [(n, ctypes.c_uint64) for n in ("multiseed_candidates", "multiseed_walks", "multiseed_traces", "multiseed_rounds")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -171,10 +171,12 @@ struct ga_extender
     DevBuf<uint32_t> msSeedSlice, msSeedNode, msNumTraces, msTraceLen, msTracesNeeded;
     DevBuf<int32_t> msTraceScore;
     DevBuf<uint64_t> msCandBegin, msTraceBase, msItemBase;
-    DevBuf<uint32_t> msCandCount;
+    DevBuf<uint32_t> msCandCount, msWork;
     DevBuf<gadev::MsCand> msCands;
+    DevBuf<gadev::MsSel> msSel;
     MsExactOut msOut;                      // ga_multiseed_batch_exact's results
-    uint64_t lastCandidates = 0, lastKept = 0;
+    uint64_t lastCandidates = 0, lastKept = 0, lastWalks = 0;
+    uint32_t lastResolveRounds = 0;
 };
 
 extern "C" const char* ga_last_error(void) { return g_lastError.c_str(); }
@@ -334,7 +336,7 @@ extern "C" int ga_extender_free(ga_extender_t x)
     x->msSeedOff.release(); x->msTraceCap.release(); x->msTraceStart.release(); x->msItemsNeeded.release();
     x->msSeedSlice.release(); x->msSeedNode.release(); x->msNumTraces.release(); x->msTraceLen.release(); x->msTracesNeeded.release();
     x->msTraceScore.release(); x->msCandBegin.release(); x->msCandCount.release(); x->msCands.release();
-    x->msTraceBase.release(); x->msItemBase.release();
+    x->msTraceBase.release(); x->msItemBase.release(); x->msWork.release(); x->msSel.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
     for (int k = 0; k < ga_extender::kCopyStreams; k++)
@@ -649,6 +651,7 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
     GA_CUDA(x->states.reserve(n));
     GA_CUDA(x->msCandBegin.reserve(n));
     GA_CUDA(x->msCandCount.reserve(n));
+    GA_CUDA(x->msSel.reserve(n));
     cudaStream_t s = x->stream;
     GA_CUDA(cudaMemcpyAsync(x->seq.ptr, b->seq, seqBytes, cudaMemcpyHostToDevice, s));
     GA_CUDA(cudaMemcpyAsync(x->seqOff.ptr, b->seq_offset, n * 8ULL, cudaMemcpyHostToDevice, s));
@@ -721,6 +724,8 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
     x->lastLaunches = 0;
     x->lastCandidates = 0;
     x->lastKept = 0;
+    x->lastWalks = 0;
+    x->lastResolveRounds = 0;
     for (int k = 0; k < 3; k++) x->lastRounds[k] = 0;
     const int wpb = 4;
     uint32_t pending = n;
@@ -765,9 +770,36 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
         ta.cands = x->msCands.ptr;
         ta.candCap = x->msCands.count;
         x->lastCandidates += candTotal;
+        if (candTotal > 0xffffffffULL) return fail(GA_ERR_ARGUMENT, "ga_multiseed_batch: more than 2^32 - 1 trace candidates in one batch");
+        GA_CUDA(x->msWork.reserve(std::max<uint64_t>(candTotal, 1)));
+        ta.work = x->msWork.ptr;
+        ta.workCount = x->counters + 7;
+        ta.sel = x->msSel.ptr;
         const uint64_t candBlocks = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)x->sms * 6, (candTotal + wpb - 1) / wpb));
-        if (ga_launch_multiseed_trace(ta, x->counters, (int)readBlocks, (int)candBlocks, wpb, s) != 0)
+        GA_CUDA(cudaMemsetAsync(x->msSel.ptr, 0, n * sizeof(gadev::MsSel), s));
+        if (ga_launch_multiseed_list(ta, x->counters, (int)readBlocks, wpb, s) != 0)
             return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+        x->lastLaunches += 3;
+        // rounds: each read decides its candidates as far as their walks are known and queues
+        // the next walks, twice as many each round, up to 1024
+        for (uint32_t round = 0;; round++)
+        {
+            GA_CUDA(cudaMemsetAsync(x->counters + 4, 0, 4 * sizeof(uint32_t), s));
+            ta.window = round < 10 ? 1u << round : 1024u;
+            if (ga_launch_multiseed_resolve(ta, x->counters, (int)readBlocks, wpb, s) != 0)
+                return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+            uint32_t walks = 0;
+            GA_CUDA(cudaMemcpyAsync(&walks, ta.workCount, 4, cudaMemcpyDeviceToHost, s));
+            GA_CUDA(cudaStreamSynchronize(s));
+            x->lastLaunches += 1;
+            if (walks == 0) break;
+            x->lastWalks += walks;
+            x->lastResolveRounds++;
+            const uint64_t walkBlocks = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)x->sms * 6, ((uint64_t)walks + wpb - 1) / wpb));
+            if (ga_launch_multiseed_walk(ta, x->counters, (int)walkBlocks, wpb, s) != 0)
+                return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+            x->lastLaunches += 1;
+        }
         if (exact)
         {
             // the reads this pass finished take their room: trace and item runs after the earlier
@@ -819,7 +851,7 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
             if (ga_launch_multiseed_write(ta, x->counters, (int)candBlocks, wpb, s) != 0)
                 return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
         }
-        x->lastLaunches += 6;
+        x->lastLaunches += 1;
         x->lastRounds[layout] += pending;
         GA_CUDA(cudaEventRecord(x->ev[1], s));
         count_status_kernel<<<64, 256, 0, s>>>(x->status.ptr, n, GA_CAPACITY, x->counters + 2);
@@ -1039,11 +1071,13 @@ extern "C" int ga_extender_last_layout_counts(ga_extender_t x, uint32_t counts[3
     return GA_OK;
 }
 
-extern "C" int ga_extender_last_multiseed_counts(ga_extender_t x, uint64_t* candidates, uint64_t* traces)
+extern "C" int ga_extender_last_multiseed_counts(ga_extender_t x, uint64_t* candidates, uint64_t* walks, uint64_t* traces, uint32_t* rounds)
 {
-    if (!x || !candidates || !traces) return fail(GA_ERR_ARGUMENT, "null argument");
+    if (!x || !candidates || !walks || !traces || !rounds) return fail(GA_ERR_ARGUMENT, "null argument");
     *candidates = x->lastCandidates;
+    *walks = x->lastWalks;
     *traces = x->lastKept;
+    *rounds = x->lastResolveRounds;
     return GA_OK;
 }
 

@@ -101,11 +101,14 @@ void ga_aligner_multiseed(void* ctx, const std::vector<gahost::MultiseedRequest>
     const int rc = ga_multiseed_batch_exact(m->ext, m->params, &b, &o);
     float kernelMs = 0;
     if (rc == GA_OK && ga_extender_last_kernel_ms(m->ext, &kernelMs) == GA_OK) m->kernelMs += kernelMs;
-    uint64_t candidates = 0, traces = 0;
-    if (rc == GA_OK && ga_extender_last_multiseed_counts(m->ext, &candidates, &traces) == GA_OK)
+    uint64_t candidates = 0, walks = 0, traces = 0;
+    uint32_t rounds = 0;
+    if (rc == GA_OK && ga_extender_last_multiseed_counts(m->ext, &candidates, &walks, &traces, &rounds) == GA_OK)
     {
         m->candidates += candidates;
+        m->walks += walks;
         m->traces += traces;
+        m->rounds += rounds;
     }
     for (size_t k = 0; k < n; k++)
     {
@@ -335,7 +338,9 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     a->multiseed.ms = 0;
     a->multiseed.kernelMs = 0;
     a->multiseed.candidates = 0;
+    a->multiseed.walks = 0;
     a->multiseed.traces = 0;
+    a->multiseed.rounds = 0;
     if (a->params.multiseed_dp)
     {
         a->multiseed.ext = a->ext;
@@ -370,7 +375,9 @@ extern "C" int ga_align_reads(ga_aligner_t a, uint32_t n, const char* const* nam
     a->stats.cell_steps = bs.cellSteps;
     a->stats.multiseed_kernel_ms = a->multiseed.kernelMs;
     a->stats.multiseed_candidates = a->multiseed.candidates;
+    a->stats.multiseed_walks = a->multiseed.walks;
     a->stats.multiseed_traces = a->multiseed.traces;
+    a->stats.multiseed_rounds = a->multiseed.rounds;
     // with two lanes the GPU calls overlap host work: host_ms is what they do not cover
     a->stats.host_ms = std::max(0.0, ms_since(start) - a->stats.extend_ms);
     return GA_OK;

@@ -86,7 +86,7 @@ struct MultiseedLane
     std::vector<uint32_t> len, slices, nodes;
     double ms = 0;
     double kernelMs = 0;                   // of ms: the batch's kernels and trace copies
-    uint64_t candidates = 0, traces = 0;   // local maxima counted, traces kept
+    uint64_t candidates = 0, walks = 0, traces = 0, rounds = 0;   // local maxima, walks, kept traces, rounds
 };
 
 // The device GAF formatter and alignment selection (gaf_device.cu): the graph's node names

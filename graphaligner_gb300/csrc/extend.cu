@@ -739,15 +739,15 @@ __device__ __forceinline__ u32 band_hash_size(u32 count)
     return h;
 }
 
-// write one slice (record, node ids, band in first-pop order, for the multiseed DP each node's
-// best X-score and, for a large band, its index) into the arena, lanes copying
+// write one slice (record, node ids, band in first-pop order and, for the multiseed DP, each
+// node's best X-score and a large band's index) into the arena, lanes copying
 __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 index, const Item* band, u32 count,
     i32 minScore, i32 quit, i32 maxX, u32 maxXNode, bool notValid, u32 lane, const i32* nodeMax = nullptr)
 {
     const u64 idBytes = rec_ids_bytes(count);
     u64 off;
     const u64 maxBytes = nodeMax ? rec_ids_bytes(count) : 0;
-    const u32 hashSize = band_hash_size(count);
+    const u32 hashSize = nodeMax ? band_hash_size(count) : 0;
     const u64 hashOff = sizeof(SliceRec) + idBytes + (u64)count * sizeof(Item) + maxBytes;
     if (!arena_alloc(a, c, hashOff + (u64)hashSize * 4, off, lane)) return false;
     uint8_t* base = a.arena + off;
@@ -797,27 +797,34 @@ __device__ bool commit_slice(const FillArgs& a, ArenaCursor& c, u64* dir, u32 in
     return true;
 }
 
-// position of node's entry in committed slice r (whose node ids are `ids`), or -1; every lane
-// gets the answer.  Through the band index where the slice has one (32 slots per probe step,
-// the first slot in probe order that is empty or the node's ends it), else a ballot over the ids.
-__device__ __forceinline__ int rec_index(const SliceRec* r, const u32* ids, u32 node, u32 lane)
+// position of node's entry in committed slice r (whose node ids are `ids`) through its band
+// index: 32 slots per probe step, the first slot in probe order that is empty or the node's
+// ends it.  Out of line: most bands are small, and the lookups are inlined in many places.
+__device__ __noinline__ int rec_index_hashed(const SliceRec* r, const u32* ids, u32 node, u32 lane)
 {
     const u32 hashSize = r->hashSize;
-    if (hashSize)
-    {
-        const u32* slots = (const u32*)((const uint8_t*)r + r->hashOff);
-        const u32 h = hash_node(node);
+    const u32* slots = (const u32*)((const uint8_t*)r + r->hashOff);
+    const u32 h = hash_node(node);
 #pragma unroll 1
-        for (u32 step = 0; step < hashSize; step += 32)
-        {
-            const u32 e = __ldcg(&slots[(h + step + lane) & (hashSize - 1)]);
-            const bool empty = e == kEmptySlot;
-            const bool hit = !empty && ids[e] == node;
-            const u32 stop = __ballot_sync(kFull, empty || hit);
-            if (stop) return __shfl_sync(kFull, hit ? (int)e : -1, __ffs((int)stop) - 1);
-        }
-        return -1;
+    for (u32 step = 0; step < hashSize; step += 32)
+    {
+        const u32 e = __ldcg(&slots[(h + step + lane) & (hashSize - 1)]);
+        const bool empty = e == kEmptySlot;
+        const bool hit = !empty && ids[e] == node;
+        const u32 stop = __ballot_sync(kFull, empty || hit);
+        if (stop) return __shfl_sync(kFull, hit ? (int)e : -1, __ffs((int)stop) - 1);
     }
+    return -1;
+}
+
+// position of node's entry in committed slice r (whose node ids are `ids`), or -1; every lane
+// gets the answer.  Hashed (the multiseed DP's tables): through the band index where the slice
+// has one.  Else a ballot over the ids: the extension's tables have no index, and their lookups
+// keep the short form.
+template <bool Hashed>
+__device__ __forceinline__ int rec_index(const SliceRec* r, const u32* ids, u32 node, u32 lane)
+{
+    if (Hashed && r->hashSize) return rec_index_hashed(r, ids, node, lane);
     const u32 n = r->count;
 #pragma unroll 1
     for (u32 base = 0; base < n; base += 32)
@@ -1334,7 +1341,8 @@ struct Table
         if (sl.slice == s) return &sl.rec;
         return load_slice(arena, dir, slots, s, lane);
     }
-    // the band entry of node in slice s (a ballot over the slice's node ids), or nullptr
+    // the band entry of node in slice s, or nullptr (Hashed: the multiseed DP's tables)
+    template <bool Hashed = false>
     __device__ __forceinline__ const Item* find(u32 s, u32 node)
     {
         const SliceRec* r = rec(s);
@@ -1343,7 +1351,7 @@ struct Table
         const bool cached = sl.slice == s;
         const u32* ids = cached ? sl.ids : (const u32*)((const uint8_t*)r + sizeof(SliceRec));
         const Item* items = cached ? sl.items : (const Item*)((const uint8_t*)ids + rec_ids_bytes(n));
-        const int k = rec_index(r, ids, node, lane);
+        const int k = rec_index<Hashed>(r, ids, node, lane);
         return k < 0 ? nullptr : &items[k];
     }
 };
@@ -1373,9 +1381,10 @@ __device__ __noinline__ void flush32(u64* items, const u64* ring, u32 n, u32 lan
 
 // Trace items go to a 64-entry ring in shared memory (every lane writes every item) and
 // out to the caller's buffer 32 at a time, one item per lane.
-// counting: nothing goes out, the items are only counted (the multiseed traceback measures
-// the room a read needs once its own has run out).
-struct TraceOut
+// counting (MayCount only, the multiseed traceback): nothing goes out, the items are only
+// counted.
+template <bool MayCount>
+struct TraceOutT
 {
     u64* items;
     u64* ring;
@@ -1392,17 +1401,18 @@ struct TraceOut
         ring[n & 63] = (u64)p.node | ((u64)(p.off & 63) << 32) | ((u64)(sw ? 1 : 0) << 38) | (sp1 << 39);
         n++;
         back = p;
-        if (!counting && (n & 31) == 0) flush32(items, ring, n, lane);
+        if (!(MayCount && counting) && (n & 31) == 0) flush32(items, ring, n, lane);
     }
     // writes the items of the last, partial group of 32
     __device__ __forceinline__ void finish()
     {
-        if (counting) return;
+        if (MayCount && counting) return;
         const u32 k = (n & ~31u) + lane;
         if (k < n) items[k] = ring[k & 63];
         __syncwarp();
     }
 };
+using TraceOut = TraceOutT<false>;
 
 __device__ __forceinline__ u32 mod64(int64_t seq) { return (u32)((u64)seq & 63); }
 
@@ -1428,24 +1438,29 @@ __device__ __noinline__ bool trace_circular(const u64* items, const u64* ring, u
 // The extraSlice of a node-slice: the multiseed DP's seed-start column (getSeedSlice) where the
 // node is a seed start, else the fake column (0, 0, INT32_MAX), all of whose scores are INT32_MAX.
 __device__ __forceinline__ WS fake_ws() { return ws_make(0, 0, kIntMax); }
+// the extraSlice's score at a row and before the slice: the seed-start column's (Multi) or
+// the fake column's, INT32_MAX, which no cell reaches
+template <bool Multi> __device__ __forceinline__ i32 xval(const WS& e, int row) { return Multi ? ws_value(e, row) : kIntMax; }
+template <bool Multi> __device__ __forceinline__ i32 xbefore(const WS& e) { return Multi ? ws_before(e) : kIntMax; }
 
 
 __device__ __forceinline__ i32 col_value(const Col& c, int row) { return ws_value(ws_make(c.VP, c.VN, c.end), row); }
 
 // pickBacktraceCorner (Common.h:936-1054).  Out of line, like the other crossing rules:
 // the walk inside a node-slice is the hot path.  t is a copy (its record cache is a hint).
+template <bool Multi>
 __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, Table t, u32 cs, u32 node, int64_t j, int& err, WS extra)
 {
     const SliceRec* cr = t.rec(cs);
     const SliceRec* pr = t.rec(cs - 1);
-    const Item* self = t.find(cs, node);
+    const Item* self = t.template find<Multi>(cs, node);
     TStep out; out.pos.node = 0; out.pos.off = 0; out.pos.seq = 0; out.sw = false;
     if (!self) { err = GA_ASSERT; return out; }
     i32 scoreHere = ws_value(ws_make(self->sVP, self->sVN, self->sEnd), 0);
-    const Item* prevSelf = t.find(cs - 1, node);
+    const Item* prevSelf = t.template find<Multi>(cs - 1, node);
     if (cr->notValid || scoreHere > cr->quit)
     {
-        if (scoreHere == ws_value(extra, 0)) { out.pos = TPos { node, 0, j }; return out; }
+        if (scoreHere == xval<Multi>(extra, 0)) { out.pos = TPos { node, 0, j }; return out; }
         i32 smallest = scoreHere + 1;
         TPos sp = TPos { 0xffffffffu, 0xffffffffu, -2 };
         bool change = false;
@@ -1459,14 +1474,14 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
         for (u32 e = g.inOff[node]; e < g.inOff[node + 1]; e++)
         {
             u32 nb = g.inNb[e];
-            const Item* pn = t.find(cs - 1, nb);
+            const Item* pn = t.template find<Multi>(cs - 1, nb);
             if (pn && pn->eEnd <= smallest)
             {
                 smallest = pn->eEnd;
                 sp = TPos { nb, g.len[nb] - 1, j - 1 };
                 change = true;
             }
-            const Item* cn = t.find(cs, nb);
+            const Item* cn = t.template find<Multi>(cs, nb);
             if (cn && nb != node)
             {
                 i32 v = ws_value(ws_make(cn->eVP, cn->eVN, cn->eEnd), 0);
@@ -1507,14 +1522,14 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
     for (u32 e = g.inOff[node]; e < g.inOff[node + 1]; e++)
     {
         u32 nb = g.inNb[e];
-        const Item* cn = t.find(cs, nb);
+        const Item* cn = t.template find<Multi>(cs, nb);
         if (cn)
         {
             i32 v = ws_value(ws_make(cn->eVP, cn->eVN, cn->eEnd), 0);
             if (v < scoreHere - 1) { err = GA_ASSERT; return out; }
             if (v == scoreHere - 1) { out.pos = TPos { nb, g.len[nb] - 1, j }; out.sw = true; return out; }
         }
-        const Item* pn = t.find(cs - 1, nb);
+        const Item* pn = t.template find<Multi>(cs - 1, nb);
         if (pn)
         {
             i32 corner = pn->eEnd;
@@ -1534,8 +1549,8 @@ __device__ __noinline__ TStep bt_corner(const DevGraph& g, const uint8_t* seq, T
             }
         }
     }
-    if (eq && scoreHere == ws_before(extra)) { out.pos = TPos { node, 0, j }; return out; }
-    if (scoreHere == ws_value(extra, 0)) { out.pos = TPos { node, 0, j }; return out; }
+    if (eq && scoreHere == xbefore<Multi>(extra)) { out.pos = TPos { node, 0, j }; return out; }
+    if (scoreHere == xval<Multi>(extra, 0)) { out.pos = TPos { node, 0, j }; return out; }
     if (bestInvalidScore < scoreHere + 1) { out.pos = bestInvalid; out.sw = bestInvalidSw; return out; }
     err = GA_ASSERT;
     return out;
@@ -1549,10 +1564,10 @@ template <bool Multi = false>
 __device__ __noinline__ int recalc(const DevGraph& g, i32 cost, Table t, u32 s, u32 node, const EqV4& eqv, Col* cols, u64* eqcol,
     u32 lane, u32 lastColumn, WS extra = fake_ws())
 {
-    const Item* it = t.find(s, node);
+    const Item* it = t.template find<Multi>(s, node);
     if (!it) return GA_ASSERT;
     PrevInfo prev;
-    const Item* pi = t.find(s - 1, node);
+    const Item* pi = t.template find<Multi>(s - 1, node);
     if (pi) { prev.exists = true; prev.sEnd = pi->sEnd; prev.HP = pi->HP; prev.HN = pi->HN; }
     else { prev.exists = false; prev.sEnd = 0; prev.HP = kAllOnes; prev.HN = 0; }
     Item copy = *it;
@@ -1572,6 +1587,7 @@ __device__ __noinline__ int recalc(const DevGraph& g, i32 cost, Table t, u32 s, 
 
 // pickBacktraceVerticalCrossing (Common.h:886-934), the step out of (p.node, p.off > 0, row 0)
 // into the previous slice; pself is the node's entry there
+template <bool Multi>
 __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* seq, Table t, u32 curSlice, const Item* pself, const Col* cols,
     TPos p, int& err, WS extra)
 {
@@ -1590,7 +1606,7 @@ __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* se
     i32 up = diag + (i32)((pself->HP >> p.off) & 1) - (i32)((pself->HN >> p.off) & 1);
     if (pr->notValid || cr->notValid || here > cr->quit || diag > pr->quit || up > pr->quit)
     {
-        if (here == ws_value(extra, 0)) second = TStep { p, false };
+        if (here == xval<Multi>(extra, 0)) second = TStep { p, false };
         else if (diag < up) second = TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
         else second = TStep { TPos { p.node, p.off, p.seq - 1 }, false };
         return second;
@@ -1598,12 +1614,13 @@ __device__ __noinline__ TStep vertical_step(const DevGraph& g, const uint8_t* se
     if (up < here - 1 || diag < here - (eq ? 0 : 1)) { err = GA_ASSERT; return second; }
     if (up == here - 1) return TStep { TPos { p.node, p.off, p.seq - 1 }, false };
     if (diag == here - (eq ? 0 : 1)) return TStep { TPos { p.node, p.off - 1, p.seq - 1 }, false };
-    if (here != ws_value(extra, 0)) err = GA_ASSERT;
+    if (here != xval<Multi>(extra, 0)) err = GA_ASSERT;
     return second;
 }
 
 // pickBacktraceHorizontalCrossing (Common.h:817-884), the step out of (p.node, offset 0,
 // row off > 0) into an in-neighbour; self is the node's entry in the slice
+template <bool Multi>
 __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* seq, Table t, u32 curSlice, u32 curNode, const Item* self,
     TPos p, u32 off, int& err, WS extra)
 {
@@ -1625,7 +1642,7 @@ __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* 
         for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1]; e++)
         {
             u32 nb = g.inNb[e];
-            const Item* cn = t.find(curSlice, nb);
+            const Item* cn = t.template find<Multi>(curSlice, nb);
             if (cn)
             {
                 WS nws = ws_make(cn->eVP, cn->eVN, cn->eEnd);
@@ -1643,14 +1660,14 @@ __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* 
                 }
             }
         }
-        if (tpos_eq(sp, p) && here != ws_value(extra, (int)off)) { err = GA_ASSERT; return second; }
+        if (tpos_eq(sp, p) && here != xval<Multi>(extra, (int)off)) { err = GA_ASSERT; return second; }
         return TStep { sp, change };
     }
     #pragma unroll 1
     for (u32 e = g.inOff[curNode]; e < g.inOff[curNode + 1]; e++)
     {
         u32 nb = g.inNb[e];
-        const Item* cn = t.find(curSlice, nb);
+        const Item* cn = t.template find<Multi>(curSlice, nb);
         if (!cn) continue;
         WS nws = ws_make(cn->eVP, cn->eVN, cn->eEnd);
         i32 v0 = ws_value(nws, (int)off);
@@ -1659,7 +1676,7 @@ __device__ __noinline__ TStep horizontal_step(const DevGraph& g, const uint8_t* 
         if (v0 == here - 1) return TStep { TPos { nb, g.len[nb] - 1, p.seq }, true };
         if (v1 == here - (eq ? 0 : 1)) return TStep { TPos { nb, g.len[nb] - 1, p.seq - 1 }, true };
     }
-    if (here != ws_value(extra, (int)off)) { err = GA_ASSERT; return second; }
+    if (here != xval<Multi>(extra, (int)off)) { err = GA_ASSERT; return second; }
     return TStep { p, false };
 }
 
@@ -1805,12 +1822,12 @@ __device__ __forceinline__ u32 row0_run_start(const Col* cols, u32 off, u32 lane
 // up to the row above the read or, in the multiseed DP (Multi), to a seed start.  resultScore:
 // the trace's OnewayTrace::score.  Returns 0 or the error status.
 template <bool Multi>
-__device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 seqLen, u32 committed, Table& t, TraceOut& to, const WSpace& w,
+__device__ __forceinline__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 seqLen, u32 committed, Table& t, TraceOutT<Multi>& to, const WSpace& w,
     TPos start, i32 startScore, i32& resultScore, u32 lane)
 {
     int err = 0;
     Col* cols = w.cols;
-    const u64 guardMax = (u64)(to.counting ? (1u << 26) : to.cap) * 4 + 1024;
+    const u64 guardMax = (u64)((Multi && to.counting) ? (1u << 26) : to.cap) * 4 + 1024;
     resultScore = startScore;
     to.push(start, false);
     // the extraSlice of the current node-slice and its score at a row
@@ -1840,7 +1857,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
             if (curSlice == 0) { err = GA_ASSERT; break; }
             if (Multi)
             {
-                const Item* here = t.find(curSlice, curNode);
+                const Item* here = t.template find<Multi>(curSlice, curNode);
                 if (!here) { err = GA_ASSERT; break; }
                 extra = (here->node & kSeedStart) ? seed_ws(((int64_t)curSlice - 1) * 64, seqLen, cost) : fake_ws();
             }
@@ -1855,17 +1872,17 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
         lastScore = col_value(cols[b.off], (int)row);
         if (row == 0 && b.off == 0)
         {
-            TStep bt = bt_corner(g, seq, t, curSlice, curNode, sj, err, extra);
+            TStep bt = bt_corner<Multi>(g, seq, t, curSlice, curNode, sj, err, extra);
             if (err) break;
             if (tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == xv(mod64(bt.pos.seq))) break;
             if (Multi && tpos_eq(bt.pos, b) && !bt.sw && col_value(cols[bt.pos.off], (int)mod64(bt.pos.seq)) == ws_before(extra)) break;
             to.push(bt.pos, bt.sw);
-            if (!to.overflow && trace_circular(to.items, to.ring, to.n, to.counting)) { err = GA_ASSERT; break; }
+            if (!to.overflow && trace_circular(to.items, to.ring, to.n, Multi && to.counting)) { err = GA_ASSERT; break; }
             continue;
         }
         if (row == 0)
         {
-            const Item* pself = t.find(curSlice - 1, curNode);
+            const Item* pself = t.template find<Multi>(curSlice - 1, curNode);
             if (!pself)
             {
                 #pragma unroll 1
@@ -1879,7 +1896,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
             // highest failing column at or below b.off (column 0 always ends it)
             TPos p = b;
             p.off = row0_run_start(cols, b.off, lane);
-            TStep second = p.off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err, extra) : vertical_step(g, seq, t, curSlice, pself, cols, p, err, extra);
+            TStep second = p.off == 0 ? bt_corner<Multi>(g, seq, t, curSlice, curNode, sj, err, extra) : vertical_step<Multi>(g, seq, t, curSlice, pself, cols, p, err, extra);
             if (err) break;
             if (second.pos.seq == b.seq && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == xv(mod64(second.pos.seq))) break;
             if (p.off != b.off)
@@ -1895,7 +1912,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
         if (b.off == 0)
         {
             // pickBacktraceHorizontalCrossing (Common.h:817-884)
-            const Item* self = t.find(curSlice, curNode);
+            const Item* self = t.template find<Multi>(curSlice, curNode);
             if (!self) { err = GA_ASSERT; break; }
             // step up column 0 while its score falls by one per row (the start column's VP
             // bits): the run ends at the highest row at or below this one whose bit is clear
@@ -1907,7 +1924,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
                 p.seq -= (int64_t)(r - (63 - __clzll((long long)stops)));
             }
             const u32 off = mod64(p.seq);
-            TStep second = off == 0 ? bt_corner(g, seq, t, curSlice, curNode, sj, err, extra) : horizontal_step(g, seq, t, curSlice, curNode, self, p, off, err, extra);
+            TStep second = off == 0 ? bt_corner<Multi>(g, seq, t, curSlice, curNode, sj, err, extra) : horizontal_step<Multi>(g, seq, t, curSlice, curNode, self, p, off, err, extra);
             if (err) break;
             if (second.pos.node == b.node && !second.sw && col_value(cols[second.pos.off], (int)mod64(second.pos.seq)) == xv(mod64(second.pos.seq))) break;
             if (p.seq != b.seq)
@@ -1918,7 +1935,7 @@ __device__ int trace_walk(const DevGraph& g, i32 cost, const uint8_t* seq, u32 s
             if (!tpos_eq(p, to.back)) to.push(p, false);
             if (tpos_eq(second.pos, to.back)) { err = GA_ASSERT; break; }
             to.push(second.pos, second.sw);
-            if (!to.overflow && trace_circular(to.items, to.ring, to.n, to.counting)) { err = GA_ASSERT; break; }
+            if (!to.overflow && trace_circular(to.items, to.ring, to.n, Multi && to.counting)) { err = GA_ASSERT; break; }
             continue;
         }
         // pickBacktraceInside (Common.h:770-815).  The four neighbouring scores are
@@ -2059,7 +2076,7 @@ __device__ void trace_extension(const TraceArgs& a, u32 ext, const ExtState& st,
 __device__ __forceinline__ bool slice_node_max(const uint8_t* arena, const u64* dir, u32 s, u32 node, u32 lane, i32& out)
 {
     const SliceRec* r = (const SliceRec*)(arena + dir[s]);
-    const int k = rec_index(r, (const u32*)((const uint8_t*)r + sizeof(SliceRec)), node, lane);
+    const int k = rec_index<true>(r, (const u32*)((const uint8_t*)r + sizeof(SliceRec)), node, lane);
     if (k < 0) return false;
     out = rec_node_max(r)[k];
     return true;
@@ -2250,7 +2267,7 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
         err = ms_start_cell(a, t, w, seq, seqLen, c, start, startScore, lane);
     }
     const bool exact = a.traceBase != nullptr;
-    TraceOut to;
+    TraceOutT<true> to;
     to.items = write ? a.traceItems + (exact ? a.itemBase[r] : a.traceOffset[r]) + c.outOff : nullptr;
     to.ring = w.ring;
     to.lane = lane;
@@ -2280,6 +2297,7 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
             cp->traceScore = traceScore;
             cp->len = err ? 0 : to.n;
             cp->traceStart = to.back.seq;
+            cp->state = kTraced;
         }
         else if (err || to.n != c.len || traceScore != c.traceScore)
         {
@@ -2299,78 +2317,111 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
     __syncwarp();
 }
 
-// getLocalMaximaTracesFromTable's selection for read r over its counted candidates, in order:
-// a candidate reaching the multimap fraction of its slice's best (as raised so far) is kept,
-// and raises the best of the slices its trace spans beyond its first 5 %.  Kept traces get
-// their place in the read's output while they fit its room (max_traces, trace_capacity);
-// past that they are only counted, and the read reports the room it needs.  With exact room
-// (a.traceBase) every kept trace gets its place, and the read reports the items they take.
-__device__ void ms_select(const MultiTraceArgs& a, u32 r, const ExtState& st, u32 lane)
+// getLocalMaximaTracesFromTable's selection for read r, one round: its candidates in order
+// from the cursor.  A candidate below the multimap fraction of its slice's best (as raised so
+// far) is passed over for good, the slice bests only rise.  One that reaches it is kept once
+// its trace has been walked, and raises the best of the slices its trace spans beyond its
+// first 5 %; the first one whose walk is still to come stops the round.  Then the read queues
+// that walk and up to window - 1 more of the candidates after it that the slice bests do not
+// yet rule out.  Kept traces get their place in the read's output while they fit its room
+// (max_traces, trace_capacity); past that they are only counted, and the read reports the
+// room it needs.  With exact room (a.traceBase) every kept trace gets its place, and the read
+// reports the items they take.  A kept trace that failed fails the read.
+__device__ void ms_resolve(const MultiTraceArgs& a, u32 r, const ExtState& st, u32 lane)
 {
-    if (lane == 0 && a.cellSteps) a.cellSteps[r] = st.steps;
+    MsSel* sp = a.sel + r;
+    if (sp->done) return;
     if (st.status != GA_OK)
     {
         if (lane == 0)
         {
+            if (a.cellSteps) a.cellSteps[r] = st.steps;
             a.status[r] = st.status;
             a.numTraces[r] = 0;
+            sp->done = 1;
         }
+        __syncwarp();
         return;
     }
+    MsSel sel = *sp;
     i32* sliceMax = (i32*)(a.arena + st.aux);
     const bool exact = a.traceBase != nullptr;
     const u64 cap = exact ? ~0ULL : a.traceCap[r];
     const u32 maxTraces = exact ? 0xffffffffu : a.maxTraces;
     const u64 begin = a.candBegin[r];
     const u32 count = a.candCount[r];
-    u64 used = 0, items = 0;
-    u32 nt = 0, traces = 0;
-    bool room = true;
     int err = 0;
+    u32 i = sel.cursor;
 #pragma unroll 1
-    for (u32 i = 0; i < count; i++)
+    for (; i < count; i++)
     {
         MsCand* cp = a.cands + begin + i;
         const u32 cs = cp->slice;
         const i32 score = cp->score;
         if ((double)score < (double)sliceMax[cs] * a.multimapScoreFraction) continue;
+        if (cp->state != kTraced) break;
         if (cp->err)
         {
             err = cp->err;
             break;
         }
         const u32 len = cp->len;
-        if (room && (nt >= maxTraces || len > cap - used)) room = false;
-        if (room)
+        if (!sel.full && (sel.nt >= maxTraces || len > cap - sel.used)) sel.full = 1;
+        if (!sel.full)
         {
             if (lane == 0)
             {
-                cp->slot = nt;
-                cp->outOff = used;
+                cp->slot = sel.nt;
+                cp->outOff = sel.used;
             }
-            used += len;
-            nt++;
+            sel.used += len;
+            sel.nt++;
         }
-        items += len;
-        traces++;
+        sel.items += len;
+        sel.traces++;
         const int64_t traceEnd = cp->startSeq, traceStart = cp->traceStart;
         const u32 startSlice = (u32)(((double)(traceEnd - traceStart) * 0.05 + (double)traceStart + 64 - 1) / 64 + 1);
         __syncwarp();
 #pragma unroll 1
-        for (u32 s = startSlice + lane; s < cs; s += 32) sliceMax[s] = imax(sliceMax[s], score);
+        for (u32 k = startSlice + lane; k < cs; k += 32) sliceMax[k] = imax(sliceMax[k], score);
         __syncwarp();
     }
-    if (lane == 0)
+    sel.cursor = i;
+    if (err || i == count)
     {
-        a.status[r] = err ? err : (room ? GA_OK : kMsRoom);
-        a.numTraces[r] = (err || !room) ? 0 : nt;
-        // with exact room: the items the read's traces take
-        if (a.itemsNeeded) a.itemsNeeded[r] = err ? 0 : (exact ? used : (!room ? items : 0));
-        if (a.tracesNeeded) a.tracesNeeded[r] = (!err && !room) ? traces : 0;
+        if (lane == 0)
+        {
+            const bool room = !sel.full;
+            if (a.cellSteps) a.cellSteps[r] = st.steps;
+            a.status[r] = err ? err : (room ? GA_OK : kMsRoom);
+            a.numTraces[r] = (err || !room) ? 0 : sel.nt;
+            // with exact room: the items the read's traces take
+            if (a.itemsNeeded) a.itemsNeeded[r] = err ? 0 : (exact ? sel.used : (!room ? sel.items : 0));
+            if (a.tracesNeeded) a.tracesNeeded[r] = (!err && !room) ? sel.traces : 0;
+            sel.done = 1;
+            *sp = sel;
+        }
+        __syncwarp();
+        return;
     }
+    // the walk the read waits for, and a few after it that may be kept too
+    u32 queued = 0;
+#pragma unroll 1
+    for (u32 j = i; j < count && queued < a.window; j++)
+    {
+        MsCand* cp = a.cands + begin + j;
+        if (cp->state != kUntraced) continue;
+        if ((double)cp->score < (double)sliceMax[cp->slice] * a.multimapScoreFraction) continue;
+        if (lane == 0)
+        {
+            cp->state = kQueued;
+            a.work[atomicAdd(a.workCount, 1u)] = (u32)(begin + j);
+        }
+        queued++;
+    }
+    if (lane == 0) *sp = sel;
     __syncwarp();
 }
-
 
 // The next extension for this warp from the work counter, or false when none is left;
 // with a filter only extensions whose previous status is GA_CAPACITY are taken.
@@ -2520,7 +2571,7 @@ __global__ void __launch_bounds__(128, 6) ms_candidates_kernel(MultiTraceArgs ta
     }
 }
 
-__global__ void __launch_bounds__(128, 6) ms_select_kernel(MultiTraceArgs ta, u32* counter)
+__global__ void __launch_bounds__(128, 6) ms_resolve_kernel(MultiTraceArgs ta, u32* counter)
 {
     const u32 lane = threadIdx.x & 31;
     u32 r;
@@ -2528,12 +2579,13 @@ __global__ void __launch_bounds__(128, 6) ms_select_kernel(MultiTraceArgs ta, u3
     while (next_extension(counter, ta.num, ta.order, ta.prevStatus, lane, r))
     {
         __syncwarp();
-        ms_select(ta, r, ta.states[r], lane);
+        ms_resolve(ta, r, ta.states[r], lane);
     }
 }
 
-// The candidates' traces, a warp per candidate (write = false: counted; write = true: the kept
-// ones written).  A read's traces spread over as many warps as it has candidates.
+// The candidates' traces, a warp per candidate (write = false: the round's queued walks,
+// counted; write = true: the kept ones written).  A read's traces spread over as many warps
+// as it has walks in the round.
 __global__ void __launch_bounds__(128, 6) ms_trace_kernel(MultiTraceArgs ta, u32* counter, int write)
 {
     extern __shared__ __align__(16) uint8_t dsmem[];
@@ -2545,7 +2597,7 @@ __global__ void __launch_bounds__(128, 6) ms_trace_kernel(MultiTraceArgs ta, u32
     w.eqcol = (u64*)(base + 64 * sizeof(Col));
     w.ring = (u64*)(base + 64 * sizeof(Col) + 64 * 8);
     w.slots = (SliceSlot*)(base + 64 * sizeof(Col) + 64 * 8 + 64 * 8);
-    const u64 total = *ta.candTotal < ta.candCap ? *ta.candTotal : ta.candCap;
+    const u64 total = write ? (*ta.candTotal < ta.candCap ? *ta.candTotal : ta.candCap) : *ta.workCount;
 #pragma unroll 1
     while (true)
     {
@@ -2554,7 +2606,7 @@ __global__ void __launch_bounds__(128, 6) ms_trace_kernel(MultiTraceArgs ta, u32
         i = __shfl_sync(kFull, i, 0);
         if (i >= total) break;
         __syncwarp();
-        ms_trace_cand(ta, ta.cands + i, w, write != 0, lane);
+        ms_trace_cand(ta, ta.cands + (write ? i : ta.work[i]), w, write != 0, lane);
     }
 }
 }
@@ -2607,16 +2659,23 @@ int ga_launch_multiseed_fill(const gadev::FillArgs& fa, const gadev::MultiTraceA
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int ga_launch_multiseed_trace(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int candBlocks, int warpsPerBlock, void* stream)
+int ga_launch_multiseed_list(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int warpsPerBlock, void* stream)
+{
+    gadev::ms_candidates_kernel<<<readBlocks, warpsPerBlock * 32, 0, (cudaStream_t)stream>>>(ta, counters + 3, 1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int ga_launch_multiseed_resolve(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int warpsPerBlock, void* stream)
+{
+    gadev::ms_resolve_kernel<<<readBlocks, warpsPerBlock * 32, 0, (cudaStream_t)stream>>>(ta, counters + 4);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int ga_launch_multiseed_walk(const gadev::MultiTraceArgs& ta, uint32_t* counters, int candBlocks, int warpsPerBlock, void* stream)
 {
     const size_t traceSmem = (size_t)gadev::kTraceSpaceBytes * warpsPerBlock;
     if (!set_smem((const void*)gadev::ms_trace_kernel, traceSmem)) return -1;
-    cudaStream_t s = (cudaStream_t)stream;
-    gadev::ms_candidates_kernel<<<readBlocks, warpsPerBlock * 32, 0, s>>>(ta, counters + 3, 1);
-    if (cudaGetLastError() != cudaSuccess) return -1;
-    gadev::ms_trace_kernel<<<candBlocks, warpsPerBlock * 32, traceSmem, s>>>(ta, counters + 4, 0);
-    if (cudaGetLastError() != cudaSuccess) return -1;
-    gadev::ms_select_kernel<<<readBlocks, warpsPerBlock * 32, 0, s>>>(ta, counters + 5);
+    gadev::ms_trace_kernel<<<candBlocks, warpsPerBlock * 32, traceSmem, (cudaStream_t)stream>>>(ta, counters + 5, 0);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -41,10 +41,10 @@ static constexpr u32 kNodeMask = 0x3fffffffu;
 // A committed DP slice in the arena: this 32-byte record, then the band's node ids
 // (count u32, padded to 16 bytes), then count Items, all in first-pop order (the multiseed
 // DP's seed starts first), then for the multiseed DP each node's best exact-end-position
-// X-score (count i32, DPSlice::nodeMaxExactEndposScore), then, for a band of more than
+// X-score (count i32, DPSlice::nodeMaxExactEndposScore) and, for a band of more than
 // kHashedBand nodes, an open-addressing index of the band (hashSize u32 slots, each an
 // entry's position or kEmptySlot, linear probing from the node's hash).  The traceback finds
-// a node's entry through the index, else by a warp ballot over the ids.
+// a node's entry through the index where there is one, else by a warp ballot over the ids.
 static constexpr u32 kHashedBand = 64;
 static constexpr u32 kEmptySlot = 0xffffffffu;
 struct __align__(16) SliceRec
@@ -132,8 +132,9 @@ struct TraceArgs
 // One local maximum of a multiseed read's table that may start a trace: a node whose best
 // X-score in a slice beats its neighbours' and reaches the multimap fraction of the slice's
 // best before any trace raised it.  The traces from the candidates are independent, so one
-// warp traces each; the read's own pass then keeps them in getLocalMaximaTracesFromTable's
-// order against the raised slice bests.
+// warp traces each; the read's own pass keeps them in getLocalMaximaTracesFromTable's order
+// against the raised slice bests, in rounds: a candidate is traced only once the traces kept
+// before it have not ruled it out (or as one of a few traced ahead of the read's next one).
 struct MsCand
 {
     u32 read;
@@ -150,9 +151,23 @@ struct MsCand
     int64_t traceStart;    // read position of the trace's last item
     u64 outOff;            // kept traces: items from the read's trace_offset
     u32 slot;              // kept traces: the trace's index in the read, else kNoSlot
-    u32 pad;
+    u32 state;             // kUntraced, kQueued (for this round's walks) or kTraced
 };
 static constexpr u32 kNoSlot = 0xffffffffu;
+static constexpr u32 kUntraced = 0, kQueued = 1, kTraced = 2;
+
+// A multiseed read's selection so far: its candidates before `cursor` are decided.
+struct MsSel
+{
+    u64 used;              // items of the kept traces that have their place
+    u64 items;             // items of all kept traces
+    u32 nt;                // kept traces that have their place
+    u32 traces;            // kept traces
+    u32 cursor;
+    u32 full;              // the kept traces have outgrown the read's room
+    u32 done;
+    u32 pad;
+};
 // the status of a multiseed read whose traces outgrew its room (reported as GA_CAPACITY with
 // the room it needs; the batch does not run it again as it does a read whose tables ran out)
 static constexpr i32 kMsRoom = 100;
@@ -189,6 +204,10 @@ struct MultiTraceArgs
     const u64* traceBase;
     const u64* itemBase;
     u64 itemBias;
+    MsSel* sel;            // [num] each read's selection
+    u32* work;             // this round's candidates to walk (indices into cands)
+    u32* workCount;
+    u32 window;            // candidates a read may have walked in this round
     MsCand* cands;         // [candCap] the batch's candidates, each read's together and in order
     u64 candCap;
     u64* candBegin;        // [num] read i's candidates are [candBegin[i], candBegin[i] + candCount[i])
@@ -211,13 +230,21 @@ int ga_trace_blocks_per_sm(int warpsPerBlock);
 int ga_launch_extend(const gadev::FillArgs& fa, const gadev::TraceArgs& ta, uint32_t* counters, int fillBlocks, int traceBlocks,
     int warpsPerBlock, void* stream);
 // the multiseed DP's fill and traceback kernels (the frontier tables always in the global workspace)
-// the multiseed DP in steps, blocks of warpsPerBlock warps: the fill and the count of each
-// read's trace candidates (counters[0], [1] zero; ta.candTotal zero); then, once ta.cands has
-// room for *ta.candTotal, the candidates listed, traced and selected (counters[3] to [5]
-// zero); then the kept traces written (counters[6] zero).  counters[2] is left to the caller.
+// the multiseed DP in steps, blocks of warpsPerBlock warps, each on `stream`:
+// - fill: the fill and the count of each read's trace candidates (counters[0], [1] and
+//   ta.candTotal zero);
+// - list: once ta.cands has room for *ta.candTotal, the candidates listed (counters[3] zero,
+//   ta.sel zeroed);
+// - rounds, until a resolve queues nothing: resolve (each read decides its candidates in
+//   order as far as their walks are known, then queues the next ta.window walks; counters[4]
+//   and *ta.workCount zero) and walk (the queued candidates' traces counted; counters[5] zero);
+// - write: the kept traces written (counters[6] zero).
+// counters[2] is left to the caller.
 int ga_launch_multiseed_fill(const gadev::FillArgs& fa, const gadev::MultiTraceArgs& ta, uint32_t* counters, int fillBlocks, int readBlocks,
     int warpsPerBlock, void* stream);
-int ga_launch_multiseed_trace(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int candBlocks, int warpsPerBlock, void* stream);
+int ga_launch_multiseed_list(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int warpsPerBlock, void* stream);
+int ga_launch_multiseed_resolve(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int warpsPerBlock, void* stream);
+int ga_launch_multiseed_walk(const gadev::MultiTraceArgs& ta, uint32_t* counters, int candBlocks, int warpsPerBlock, void* stream);
 int ga_launch_multiseed_write(const gadev::MultiTraceArgs& ta, uint32_t* counters, int candBlocks, int warpsPerBlock, void* stream);
 int ga_upload_tables();
 void ga_set_last_error(const char* message);

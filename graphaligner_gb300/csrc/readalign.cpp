@@ -1038,34 +1038,50 @@ void addMappingQualities(std::vector<AlignmentItem>& alignments)
 // int32 value of a size_t expression, as the reference's ScoreType assignments truncate it
 static inline int32_t score32(uint64_t x) { return (int32_t)(uint32_t)x; }
 
-// GraphAlignerBitvectorBanded::removeDuplicateTraces (GraphAlignerBitvectorBanded.h:144-169):
-// by X-score, best first (std::sort, as the reference), then a trace ending where an earlier
-// one ends is swapped out
-static void removeDuplicateTraces(std::vector<OnewayTrace>& traces, int32_t cost)
+// GraphAlignerBitvectorBanded::removeDuplicateTraces (GraphAlignerBitvectorBanded.h:144-169)
+// on the packed traces of one multiseed DP, before any is decoded: sorted by the X-score of
+// their span (the first item is the trace's end in DP order, the last its start), then of
+// two that start at the same cell (node, offset and read position; the switch flag is not
+// compared) the later one goes, swapped with the last and popped as the reference does.
+// Sorting handles instead of the traces makes the same comparisons and moves, so the order
+// is the reference's.  Returns the surviving traces' indices in their final order.
+static std::vector<uint32_t> dedupeMultiseedTraces(const MultiseedResult& res, int32_t cost)
 {
-    if (traces.empty()) return;
-    std::sort(traces.begin(), traces.end(), [cost](const OnewayTrace& left, const OnewayTrace& right)
+    struct Key
     {
-        int32_t leftScore = score32((left.trace[0].seqPos - left.trace.back().seqPos + 1) * 100);
-        leftScore = score32((uint64_t)(uint32_t)leftScore - (uint64_t)(uint32_t)(left.score * cost));
-        int32_t rightScore = score32((right.trace[0].seqPos - right.trace.back().seqPos + 1) * 100);
-        rightScore = score32((uint64_t)(uint32_t)rightScore - (uint64_t)(uint32_t)(right.score * cost));
-        return leftScore > rightScore;
-    });
-    for (size_t i = traces.size() - 1; i > 0; i--)
+        int32_t sortScore;
+        uint32_t index;
+        uint64_t start;    // the last item without its switch flag
+    };
+    const uint64_t kSwitch = 1ULL << 38;
+    std::vector<Key> keys(res.items.size());
+    for (size_t t = 0; t < keys.size(); t++)
+    {
+        const uint64_t* it = res.items[t];
+        const uint64_t n = res.lengths[t];
+        GAH_ASSERT(n > 0);
+        auto seqPos = [](uint64_t x) -> size_t { const uint64_t sp1 = GA_TRACE_SEQPOS1(x); return sp1 == 0 ? (size_t)-1 : (size_t)(sp1 - 1); };
+        int32_t score = score32((seqPos(it[0]) - seqPos(it[n - 1]) + 1) * 100);
+        score = score32((uint64_t)(uint32_t)score - (uint64_t)(uint32_t)(res.scores[t] * cost));
+        keys[t] = Key { score, (uint32_t)t, it[n - 1] & ~kSwitch };
+    }
+    if (keys.empty()) return {};
+    std::sort(keys.begin(), keys.end(), [](const Key& left, const Key& right) { return left.sortScore > right.sortScore; });
+    for (size_t i = keys.size() - 1; i > 0; i--)
     {
         for (size_t j = 0; j < i; j++)
         {
-            const auto& a = traces[i].trace.back();
-            const auto& b = traces[j].trace.back();
-            if (a.node == b.node && a.nodeOffset == b.nodeOffset && a.seqPos == b.seqPos)
+            if (keys[i].start == keys[j].start)
             {
-                std::swap(traces[i], traces.back());
-                traces.pop_back();
+                std::swap(keys[i], keys.back());
+                keys.pop_back();
                 break;
             }
         }
     }
+    std::vector<uint32_t> order(keys.size());
+    for (size_t k = 0; k < keys.size(); k++) order[k] = keys[k].index;
+    return order;
 }
 
 // GraphAligner::clipTraceStart (GraphAligner.h:702-738): the trace starts where its X-score
@@ -1184,61 +1200,88 @@ void alignBatchMultiseed(const HostGraph& g, const ReadAlignParams& p, std::vect
     stats.extensions += rq.size();
     t0 = std::chrono::steady_clock::now();
     // duplicate removal, read order, clipping, and the backward extension of every trace
-    // that does not start at the read's first base
+    // that does not start at the read's first base.  Duplicates go before any trace is
+    // decoded; the survivors are decoded, reversed and clipped one trace per job (a read can
+    // have thousands), then each read lists its backward extensions in trace order.
     std::vector<std::vector<ExtensionRequest>> perRead(rq.size());
+    std::vector<std::vector<uint32_t>> keep(rq.size());
     parallelFor(rq.size(), [&](size_t k)
     {
         MsRead& m = ms[rqRead[k]];
-        const MultiseedResult& res = rs[k];
-        if (res.status != GA_OK)
+        if (rs[k].status != GA_OK)
         {
             m.r.failed = true;
             return;
         }
         try
         {
-            std::vector<OnewayTrace> traces(res.items.size());
-            for (size_t t = 0; t < res.items.size(); t++)
-            {
-                ExtensionResult e;
-                e.status = GA_OK;
-                e.score = res.scores[t];
-                e.itemPtr = res.items[t];
-                e.itemCount = res.lengths[t];
-                traces[t] = decodeTrace(g, e, m.r.seq.data(), m.r.seq.size());
-                GAH_ASSERT(!traces[t].trace.empty());
-            }
-            removeDuplicateTraces(traces, p.xscoreErrorCost);
-            for (auto& t : traces) std::reverse(t.trace.begin(), t.trace.end());
-            for (auto& t : traces)
-            {
-                clipTraceStart(t, p.xscoreErrorCost);
-                fixForwardTraceSeqPos(g, t, 0, m.r.seq);
-                int request = -1;
-                if (t.trace[0].seqPos != 0)
-                {
-                    auto rp = g.reversePosition((int)t.trace[0].node, t.trace[0].nodeOffset);
-                    ExtensionRequest e;
-                    e.seq = m.r.rev.data() + m.r.rev.size() - t.trace[0].seqPos;
-                    e.len = (uint32_t)t.trace[0].seqPos;
-                    e.bignode = rp.first;
-                    e.offset = rp.second;
-                    const size_t node = g.unitigNode(e.bignode, e.offset);
-                    e.node = (uint32_t)node;
-                    e.nodeOffset = (uint32_t)(e.offset - g.nodeOffset[node]);
-                    request = (int)perRead[k].size();
-                    perRead[k].push_back(e);
-                }
-                m.backwardRequest.push_back(request);
-                m.forward.push_back(std::move(t));
-            }
+            keep[k] = dedupeMultiseedTraces(rs[k], p.xscoreErrorCost);
+            m.forward.resize(keep[k].size());
         }
         catch (const ReadFailure&)
         {
             m.r.failed = true;
+            keep[k].clear();
+        }
+    });
+    std::vector<std::pair<uint32_t, uint32_t>> jobs;     // (read, trace in its final order)
+    for (size_t k = 0; k < rq.size(); k++)
+        for (uint32_t q = 0; q < keep[k].size(); q++) jobs.emplace_back((uint32_t)k, q);
+    std::unique_ptr<std::atomic<uint8_t>[]> broken(new std::atomic<uint8_t>[rq.size()]);
+    for (size_t k = 0; k < rq.size(); k++) broken[k].store(0);
+    parallelFor(jobs.size(), [&](size_t job)
+    {
+        const uint32_t k = jobs[job].first, q = jobs[job].second;
+        if (broken[k].load(std::memory_order_relaxed)) return;
+        MsRead& m = ms[rqRead[k]];
+        const MultiseedResult& res = rs[k];
+        const uint32_t t = keep[k][q];
+        try
+        {
+            ExtensionResult e;
+            e.status = GA_OK;
+            e.score = res.scores[t];
+            e.itemPtr = res.items[t];
+            e.itemCount = res.lengths[t];
+            OnewayTrace tr = decodeTrace(g, e, m.r.seq.data(), m.r.seq.size());
+            std::reverse(tr.trace.begin(), tr.trace.end());
+            clipTraceStart(tr, p.xscoreErrorCost);
+            fixForwardTraceSeqPos(g, tr, 0, m.r.seq);
+            m.forward[q] = std::move(tr);
+        }
+        catch (const ReadFailure&)
+        {
+            broken[k].store(1);
+        }
+    });
+    parallelFor(rq.size(), [&](size_t k)
+    {
+        MsRead& m = ms[rqRead[k]];
+        if (m.r.failed) return;
+        if (broken[k].load())
+        {
+            m.r.failed = true;
             m.forward.clear();
-            m.backwardRequest.clear();
-            perRead[k].clear();
+            return;
+        }
+        for (const OnewayTrace& t : m.forward)
+        {
+            int request = -1;
+            if (t.trace[0].seqPos != 0)
+            {
+                auto rp = g.reversePosition((int)t.trace[0].node, t.trace[0].nodeOffset);
+                ExtensionRequest e;
+                e.seq = m.r.rev.data() + m.r.rev.size() - t.trace[0].seqPos;
+                e.len = (uint32_t)t.trace[0].seqPos;
+                e.bignode = rp.first;
+                e.offset = rp.second;
+                const size_t node = g.unitigNode(e.bignode, e.offset);
+                e.node = (uint32_t)node;
+                e.nodeOffset = (uint32_t)(e.offset - g.nodeOffset[node]);
+                request = (int)perRead[k].size();
+                perRead[k].push_back(e);
+            }
+            m.backwardRequest.push_back(request);
         }
     });
     for (const auto& res : rs) stats.cellSteps += res.steps;

@@ -272,9 +272,10 @@ int ga_extender_autotune(ga_extender_t ext, const ga_extend_params* params,
 int ga_extender_last_arena_bytes(ga_extender_t ext, uint64_t* bytes);
 /* Extensions run with each table layout (0, 1, 2) by the last call (0 = layout not run). */
 int ga_extender_last_layout_counts(ga_extender_t ext, uint32_t counts[3]);
-/* The last multiseed call's local-maximum candidates (each walked once to count its trace)
- * and the traces it kept, summed over its passes. */
-int ga_extender_last_multiseed_counts(ga_extender_t ext, uint64_t* candidates, uint64_t* traces);
+/* The last multiseed call's local-maximum candidates, the walks that counted their traces
+ * (candidates the traces kept before them ruled out are not walked), the traces it kept and
+ * the rounds of walks, summed over its passes. */
+int ga_extender_last_multiseed_counts(ga_extender_t ext, uint64_t* candidates, uint64_t* walks, uint64_t* traces, uint32_t* rounds);
 
 /* ---- utilities (no reference counterpart) ---- */
 /* Page-locked host memory for the host-buffer entry points. */
@@ -344,8 +345,10 @@ typedef struct ga_align_stats {
     double   seed_lookup_ms;           /* of seed_ms: reads in, k-mer lookup kernel, matches back */
     double   seed_select_ms;           /*             least-frequent selection per read (host) */
     double   multiseed_kernel_ms;      /* of extend_ms with multiseed_dp: the multiseed DP's kernels and trace copies */
-    uint64_t multiseed_candidates;     /* local maxima whose traces were counted */
+    uint64_t multiseed_candidates;     /* local maxima that could start a trace */
+    uint64_t multiseed_walks;          /* of them: walked to count their traces */
     uint64_t multiseed_traces;         /* traces the multiseed DPs kept */
+    uint64_t multiseed_rounds;         /* rounds of walks */
 } ga_align_stats;
 
 typedef struct ga_aligner* ga_aligner_t;

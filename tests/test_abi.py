@@ -54,7 +54,7 @@ def test_null_arguments_are_rejected_before_any_device_call(cuda_lib):
         "ga_extender_autotune": (n, n, n, n, 0, 0, n),
         "ga_extender_last_arena_bytes": (n, n),
         "ga_extender_last_layout_counts": (n, n),
-        "ga_extender_last_multiseed_counts": (n, n, n),
+        "ga_extender_last_multiseed_counts": (n, n, n, n, n),
         "ga_aligner_create": (n, n, n, n),
         "ga_align_reads": (n, 0, n, n, n, n),
         "ga_aligner_gaf": (n, n, n),
