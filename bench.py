@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--multiseed", action="store_true", help="read-level: --multiseed-DP 1 (one multiseed DP per read)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="extend: keep the default launch shape")
     ap.add_argument("--truncate", type=int, default=0, help="extend: cut every extension to this many bases (small profiling cases)")
-    ap.add_argument("--arena-gb", type=float, default=0, help="extend: DP-table arena size (default: from the batch)")
+    ap.add_argument("--arena-gb", type=float, default=0, help="DP-table arena size (default: from the batch or the reads)")
     return ap.parse_args()
 
 
@@ -323,7 +323,7 @@ def run_reads(args):
     names = [r.name for r in reads]
     seqs = [r.seq for r in reads]
     read_bp = int(sum(len(s) for s in seqs))
-    arena = int(min(96 << 30, max(4 << 30, read_bp * 24)))
+    arena = int(args.arena_gb * (1 << 30)) if args.arena_gb else int(min(96 << 30, max(4 << 30, read_bp * 24)))
     t0 = time.perf_counter()
     dgraph = DeviceGraph(g)
     ext = Extender(dgraph, arena_bytes=arena)
@@ -354,7 +354,7 @@ def run_reads(args):
                      "e2e": {"value": st["bp_aligned"] / wall, "unit": UNIT, "h2d_bytes_per_step": read_bp, "d2h_bytes_per_step": len(gaf)}})
         if args.workload == "reads-vg":
             import gzip
-            golden = os.path.join(ROOT, "tests", "golden", "vg50k_b10.gaf.gz")
+            golden = os.path.join(ROOT, "tests", "golden", "vg50k_ms_b10.gaf.gz" if args.multiseed else "vg50k_b10.gaf.gz")
             if os.path.exists(golden):
                 line["gaf_identical_to_reference"] = gzip.open(golden, "rt").read() == gaf
         line["index"] = {k: v for k, v in aligner.index().items()}

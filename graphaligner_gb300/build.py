@@ -11,7 +11,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgraphaligner_gb300.so")
 SOURCES = ["extend.cu", "noalloc.cu", "abi.cu", "seed_kernel.cu", "index_build.cu", "gaf_device.cu", "align_abi.cu", "readalign.cpp", "seeding.cpp", "serve.cpp", "gfa_build.cpp"]
-HEADERS = ["extend.cuh", "wordslice.cuh", "seed_kernel.cuh", "seed_table.h", "index_build.h", "index_walk.cuh", "gaf_format.cuh", "readalign.h", "aligner.h", "gfa_build.h"]
+HEADERS = ["extend.cuh", "wordslice.cuh", "seed_kernel.cuh", "seed_table.h", "index_build.h", "index_walk.cuh", "gaf_format.cuh", "readalign.h", "aligner.h", "gfa_build.h", "trace_dedupe.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 #include "extend.cuh"
+#include "trace_dedupe.h"
 #include "../../include/graphaligner_gb300.h"
 
 namespace
@@ -170,8 +171,9 @@ struct ga_extender
     DevBuf<uint64_t> msSeedOff, msTraceCap, msTraceStart, msItemsNeeded;
     DevBuf<uint32_t> msSeedSlice, msSeedNode, msNumTraces, msTraceLen, msTracesNeeded;
     DevBuf<int32_t> msTraceScore;
-    DevBuf<uint64_t> msCandBegin, msTraceBase, msItemBase;
-    DevBuf<uint32_t> msCandCount, msWork;
+    DevBuf<uint64_t> msCandBegin, msTraceBase, msKeptItem;
+    DevBuf<uint32_t> msCandCount, msWork, msKeptSlot;
+    DevBuf<gadev::MsKey> msKeys;
     DevBuf<gadev::MsCand> msCands;
     DevBuf<gadev::MsSel> msSel;
     MsExactOut msOut;                      // ga_multiseed_batch_exact's results
@@ -336,7 +338,8 @@ extern "C" int ga_extender_free(ga_extender_t x)
     x->msSeedOff.release(); x->msTraceCap.release(); x->msTraceStart.release(); x->msItemsNeeded.release();
     x->msSeedSlice.release(); x->msSeedNode.release(); x->msNumTraces.release(); x->msTraceLen.release(); x->msTracesNeeded.release();
     x->msTraceScore.release(); x->msCandBegin.release(); x->msCandCount.release(); x->msCands.release();
-    x->msTraceBase.release(); x->msItemBase.release(); x->msWork.release(); x->msSel.release();
+    x->msTraceBase.release(); x->msKeptItem.release(); x->msWork.release(); x->msSel.release();
+    x->msKeptSlot.release(); x->msKeys.release();
     for (auto& e : x->ev) cudaEventDestroy(e);
     cudaStreamDestroy(x->stream);
     for (int k = 0; k < ga_extender::kCopyStreams; k++)
@@ -646,7 +649,6 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
     if (exact)
     {
         GA_CUDA(x->msTraceBase.reserve(n));
-        GA_CUDA(x->msItemBase.reserve(n));
     }
     GA_CUDA(x->states.reserve(n));
     GA_CUDA(x->msCandBegin.reserve(n));
@@ -704,7 +706,6 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
     ta.traceCap = exact ? nullptr : x->msTraceCap.ptr;
     ta.maxTraces = exact ? 0 : b->max_traces;
     ta.traceBase = exact ? x->msTraceBase.ptr : nullptr;
-    ta.itemBase = exact ? x->msItemBase.ptr : nullptr;
     ta.itemBias = 0;
     ta.multimapScoreFraction = b->multimap_score_fraction;
     ta.status = x->status.ptr;
@@ -737,13 +738,7 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
     // room it needs.  Between the fill and the traceback the host sizes the candidate list.
     int layout = 1;
     std::vector<uint8_t> finished(exact ? n : 0, 0);
-    std::vector<uint64_t> passUsed, traceBase, itemBase;
-    if (exact)
-    {
-        passUsed.resize(n);
-        traceBase.assign(n, 0);
-        itemBase.assign(n, 0);
-    }
+    std::vector<uint64_t> traceBase(exact ? n : 0, 0);
     for (int pass = 0; pass < 32; pass++)
     {
         const gadev::Caps caps = layout_caps(layout);
@@ -802,31 +797,75 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
         }
         if (exact)
         {
-            // the reads this pass finished take their room: trace and item runs after the earlier
-            // passes' (the tables of this pass are gone once the next one starts)
+            // The reads this pass finished list their kept traces; the host removes the
+            // duplicates (removeDuplicateTraces, as getMultiseedTraces does), and the survivors
+            // get trace and item runs after the earlier passes' (this pass's tables are gone
+            // once the next one starts).  Only the survivors are written and copied back.
             MsExactOut& o = x->msOut;
             GA_CUDA(cudaMemcpyAsync(o.status.data(), x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
             GA_CUDA(cudaMemcpyAsync(o.numTraces.data(), x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
-            GA_CUDA(cudaMemcpyAsync(passUsed.data(), x->msItemsNeeded.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
             GA_CUDA(cudaStreamSynchronize(s));
-            uint64_t passTraces = 0, passItems = 0;
+            std::vector<uint32_t> passReads;
+            uint64_t passKept = 0;
             for (uint32_t i = 0; i < n; i++)
             {
                 if (finished[i] || o.status[i] == GA_CAPACITY) continue;
                 finished[i] = 1;
                 if (o.status[i] != GA_OK) continue;
-                traceBase[i] = passTraces;
-                itemBase[i] = passItems;
+                traceBase[i] = passKept;
+                passKept += o.numTraces[i];
+                passReads.push_back(i);
+            }
+            x->lastKept += passKept;
+            GA_CUDA(x->msKeys.reserve(std::max<uint64_t>(passKept, 1)));
+            GA_CUDA(x->msKeptSlot.reserve(std::max<uint64_t>(passKept, 1)));
+            GA_CUDA(x->msKeptItem.reserve(std::max<uint64_t>(passKept, 1)));
+            GA_CUDA(cudaMemcpyAsync(x->msTraceBase.ptr, traceBase.data(), n * 8ULL, cudaMemcpyHostToDevice, s));
+            ta.keys = x->msKeys.ptr;
+            ta.keptSlot = x->msKeptSlot.ptr;
+            ta.keptItem = x->msKeptItem.ptr;
+            std::vector<gadev::MsKey> keys(passKept);
+            if (passKept)
+            {
+                if (ga_launch_multiseed_keys(ta, s) != 0)
+                    return fail(GA_ERR_CUDA, std::string("multiseed kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
+                x->lastLaunches += 1;
+                GA_CUDA(cudaMemcpyAsync(keys.data(), x->msKeys.ptr, passKept * sizeof(gadev::MsKey), cudaMemcpyDeviceToHost, s));
+                GA_CUDA(cudaStreamSynchronize(s));
+            }
+            std::vector<uint32_t> keptSlot(passKept, gadev::kNoSlot);
+            std::vector<uint64_t> keptItem(passKept, 0);
+            uint64_t passTraces = 0, passItems = 0;
+            std::vector<gahost::DedupeKey> dk;
+            for (uint32_t i : passReads)
+            {
+                const uint64_t base = traceBase[i];
+                dk.resize(o.numTraces[i]);
+                for (uint32_t t = 0; t < o.numTraces[i]; t++)
+                {
+                    const gadev::MsKey& k = keys[base + t];
+                    const uint64_t start = (uint64_t)k.lastNode | ((uint64_t)(k.lastOff & 63) << 32) | ((uint64_t)(k.last + 1) << 39);
+                    dk[t] = gahost::DedupeKey { gahost::dedupeScore((size_t)k.first, (size_t)k.last, k.score, p->xscore_error_cost), t, start };
+                }
+                const std::vector<uint32_t> order = gahost::dedupeOrder(dk);
                 o.traceFirst[i] = o.traces + passTraces;
-                passTraces += o.numTraces[i];
-                passItems += passUsed[i];
+                o.numTraces[i] = (uint32_t)order.size();
+                for (uint32_t t : order)
+                {
+                    keptSlot[base + t] = (uint32_t)passTraces++;
+                    keptItem[base + t] = passItems;
+                    passItems += keys[base + t].len;
+                }
+            }
+            if (passKept)
+            {
+                GA_CUDA(cudaMemcpyAsync(x->msKeptSlot.ptr, keptSlot.data(), passKept * 4, cudaMemcpyHostToDevice, s));
+                GA_CUDA(cudaMemcpyAsync(x->msKeptItem.ptr, keptItem.data(), passKept * 8, cudaMemcpyHostToDevice, s));
             }
             GA_CUDA(x->msTraceScore.reserve(std::max<uint64_t>(passTraces, 1)));
             GA_CUDA(x->msTraceStart.reserve(std::max<uint64_t>(passTraces, 1)));
             GA_CUDA(x->msTraceLen.reserve(std::max<uint64_t>(passTraces, 1)));
             GA_CUDA(x->traceItems.reserve(std::max<uint64_t>(passItems, 1)));
-            GA_CUDA(cudaMemcpyAsync(x->msTraceBase.ptr, traceBase.data(), n * 8ULL, cudaMemcpyHostToDevice, s));
-            GA_CUDA(cudaMemcpyAsync(x->msItemBase.ptr, itemBase.data(), n * 8ULL, cudaMemcpyHostToDevice, s));
             ta.traceScore = x->msTraceScore.ptr;
             ta.traceStart = x->msTraceStart.ptr;
             ta.traceLen = x->msTraceLen.ptr;
@@ -880,10 +919,7 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
         GA_CUDA(cudaMemcpyAsync(o.cellSteps.data(), x->cellSteps.ptr, n * 8ULL, cudaMemcpyDeviceToHost, s));
         GA_CUDA(cudaStreamSynchronize(s));
         for (uint32_t i = 0; i < n; i++)
-        {
             if (o.status[i] != GA_OK) o.numTraces[i] = 0;
-            x->lastKept += o.numTraces[i];
-        }
         o.publish(ex);
         return GA_OK;
     }

@@ -119,6 +119,7 @@ void ga_aligner_multiseed(void* ctx, const std::vector<gahost::MultiseedRequest>
         out.items.clear();
         out.lengths.clear();
         out.own.clear();
+        out.deduplicated = true;
         if (out.status != GA_OK) continue;
         for (uint32_t t = 0; t < o.num_traces[k]; t++)
         {

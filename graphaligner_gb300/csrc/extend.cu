@@ -2267,8 +2267,12 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
         err = ms_start_cell(a, t, w, seq, seqLen, c, start, startScore, lane);
     }
     const bool exact = a.traceBase != nullptr;
+    // exact room: the kept trace's place after the duplicates went, or none
+    const u64 kept = exact && write ? a.traceBase[r] + c.slot : 0;
+    const u32 outSlot = exact && write ? a.keptSlot[kept] : 0;
+    if (exact && write && outSlot == kNoSlot) return;
     TraceOutT<true> to;
-    to.items = write ? a.traceItems + (exact ? a.itemBase[r] : a.traceOffset[r]) + c.outOff : nullptr;
+    to.items = write ? a.traceItems + (exact ? a.keptItem[kept] : a.traceOffset[r] + c.outOff) : nullptr;
     to.ring = w.ring;
     to.lane = lane;
     to.counting = !write;
@@ -2297,6 +2301,8 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
             cp->traceScore = traceScore;
             cp->len = err ? 0 : to.n;
             cp->traceStart = to.back.seq;
+            cp->lastNode = to.back.node;
+            cp->lastOff = to.back.off;
             cp->state = kTraced;
         }
         else if (err || to.n != c.len || traceScore != c.traceScore)
@@ -2308,9 +2314,9 @@ __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace&
         }
         else
         {
-            const u64 slot = exact ? a.traceBase[r] + c.slot : (u64)r * a.maxTraces + c.slot;
+            const u64 slot = exact ? outSlot : (u64)r * a.maxTraces + c.slot;
             a.traceScore[slot] = traceScore;
-            a.traceStart[slot] = exact ? a.itemBias + a.itemBase[r] + c.outOff : c.outOff;
+            a.traceStart[slot] = exact ? a.itemBias + a.keptItem[kept] : c.outOff;
             a.traceLen[slot] = to.n;
         }
     }
@@ -2571,6 +2577,26 @@ __global__ void __launch_bounds__(128, 6) ms_candidates_kernel(MultiTraceArgs ta
     }
 }
 
+// Exact room: each kept trace of a read that finished GA_OK, summarised for the host's
+// removeDuplicateTraces, a thread per candidate.
+__global__ void ms_keys_kernel(MultiTraceArgs ta)
+{
+    const u64 total = *ta.candTotal < ta.candCap ? *ta.candTotal : ta.candCap;
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x)
+    {
+        const MsCand& c = ta.cands[i];
+        if (c.slot == kNoSlot || ta.status[c.read] != GA_OK) continue;
+        MsKey k;
+        k.first = c.startSeq;
+        k.last = c.traceStart;
+        k.lastNode = c.lastNode;
+        k.lastOff = c.lastOff;
+        k.score = c.traceScore;
+        k.len = c.len;
+        ta.keys[ta.traceBase[c.read] + c.slot] = k;
+    }
+}
+
 __global__ void __launch_bounds__(128, 6) ms_resolve_kernel(MultiTraceArgs ta, u32* counter)
 {
     const u32 lane = threadIdx.x & 31;
@@ -2662,6 +2688,12 @@ int ga_launch_multiseed_fill(const gadev::FillArgs& fa, const gadev::MultiTraceA
 int ga_launch_multiseed_list(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int warpsPerBlock, void* stream)
 {
     gadev::ms_candidates_kernel<<<readBlocks, warpsPerBlock * 32, 0, (cudaStream_t)stream>>>(ta, counters + 3, 1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int ga_launch_multiseed_keys(const gadev::MultiTraceArgs& ta, void* stream)
+{
+    gadev::ms_keys_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(ta);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

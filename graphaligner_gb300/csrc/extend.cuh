@@ -152,6 +152,20 @@ struct MsCand
     u64 outOff;            // kept traces: items from the read's trace_offset
     u32 slot;              // kept traces: the trace's index in the read, else kNoSlot
     u32 state;             // kUntraced, kQueued (for this round's walks) or kTraced
+    u32 lastNode;          // the trace's last item (its start in the read)
+    u32 lastOff;
+};
+
+// What removeDuplicateTraces looks at in a kept trace: the read positions of its first and
+// last items, its last item's cell, its score (and its length, for the room it takes).
+struct MsKey
+{
+    int64_t first;
+    int64_t last;
+    u32 lastNode;
+    u32 lastOff;
+    i32 score;
+    u32 len;
 };
 static constexpr u32 kNoSlot = 0xffffffffu;
 static constexpr u32 kUntraced = 0, kQueued = 1, kTraced = 2;
@@ -198,11 +212,14 @@ struct MultiTraceArgs
     u64* cellSteps;
     u64* itemsNeeded;      // [num] or null: when the traces outgrow the read's room, the room they need
     u32* tracesNeeded;
-    // exact room (traceBase non-null): read i's kept traces go to the trace tables from
-    // traceBase[i] and their items from itemBase[i], and a trace's start is counted from
-    // itemBias; traceOffset, traceCap and maxTraces are not used
+    // exact room (traceBase non-null): read i's kept traces are traceBase[i] + slot in the
+    // kept list, whose summaries go to keys; after removeDuplicateTraces kept trace k is
+    // written as trace keptSlot[k] (kNoSlot: a duplicate) with its items from keptItem[k], its
+    // start counted from itemBias; traceOffset, traceCap and maxTraces are not used
     const u64* traceBase;
-    const u64* itemBase;
+    MsKey* keys;
+    const u32* keptSlot;
+    const u64* keptItem;
     u64 itemBias;
     MsSel* sel;            // [num] each read's selection
     u32* work;             // this round's candidates to walk (indices into cands)
@@ -246,5 +263,7 @@ int ga_launch_multiseed_list(const gadev::MultiTraceArgs& ta, uint32_t* counters
 int ga_launch_multiseed_resolve(const gadev::MultiTraceArgs& ta, uint32_t* counters, int readBlocks, int warpsPerBlock, void* stream);
 int ga_launch_multiseed_walk(const gadev::MultiTraceArgs& ta, uint32_t* counters, int candBlocks, int warpsPerBlock, void* stream);
 int ga_launch_multiseed_write(const gadev::MultiTraceArgs& ta, uint32_t* counters, int candBlocks, int warpsPerBlock, void* stream);
+// exact room: each kept trace's summary into ta.keys
+int ga_launch_multiseed_keys(const gadev::MultiTraceArgs& ta, void* stream);
 int ga_upload_tables();
 void ga_set_last_error(const char* message);

@@ -31,6 +31,7 @@
 #include <vector>
 #include "../../include/graphaligner_gb300.h"
 #include "readalign.h"
+#include "trace_dedupe.h"
 
 namespace gahost
 {
@@ -1038,50 +1039,23 @@ void addMappingQualities(std::vector<AlignmentItem>& alignments)
 // int32 value of a size_t expression, as the reference's ScoreType assignments truncate it
 static inline int32_t score32(uint64_t x) { return (int32_t)(uint32_t)x; }
 
-// GraphAlignerBitvectorBanded::removeDuplicateTraces (GraphAlignerBitvectorBanded.h:144-169)
-// on the packed traces of one multiseed DP, before any is decoded: sorted by the X-score of
-// their span (the first item is the trace's end in DP order, the last its start), then of
-// two that start at the same cell (node, offset and read position; the switch flag is not
-// compared) the later one goes, swapped with the last and popped as the reference does.
-// Sorting handles instead of the traces makes the same comparisons and moves, so the order
-// is the reference's.  Returns the surviving traces' indices in their final order.
+// removeDuplicateTraces on the packed traces of one multiseed DP, before any is decoded
+// (trace_dedupe.h); the first item is the trace's end in DP order, the last its start, whose
+// cell and read position without the switch flag identify it.  Returns the surviving
+// traces' indices in their final order.
 static std::vector<uint32_t> dedupeMultiseedTraces(const MultiseedResult& res, int32_t cost)
 {
-    struct Key
-    {
-        int32_t sortScore;
-        uint32_t index;
-        uint64_t start;    // the last item without its switch flag
-    };
     const uint64_t kSwitch = 1ULL << 38;
-    std::vector<Key> keys(res.items.size());
+    std::vector<DedupeKey> keys(res.items.size());
     for (size_t t = 0; t < keys.size(); t++)
     {
         const uint64_t* it = res.items[t];
         const uint64_t n = res.lengths[t];
         GAH_ASSERT(n > 0);
         auto seqPos = [](uint64_t x) -> size_t { const uint64_t sp1 = GA_TRACE_SEQPOS1(x); return sp1 == 0 ? (size_t)-1 : (size_t)(sp1 - 1); };
-        int32_t score = score32((seqPos(it[0]) - seqPos(it[n - 1]) + 1) * 100);
-        score = score32((uint64_t)(uint32_t)score - (uint64_t)(uint32_t)(res.scores[t] * cost));
-        keys[t] = Key { score, (uint32_t)t, it[n - 1] & ~kSwitch };
+        keys[t] = DedupeKey { dedupeScore(seqPos(it[0]), seqPos(it[n - 1]), res.scores[t], cost), (uint32_t)t, it[n - 1] & ~kSwitch };
     }
-    if (keys.empty()) return {};
-    std::sort(keys.begin(), keys.end(), [](const Key& left, const Key& right) { return left.sortScore > right.sortScore; });
-    for (size_t i = keys.size() - 1; i > 0; i--)
-    {
-        for (size_t j = 0; j < i; j++)
-        {
-            if (keys[i].start == keys[j].start)
-            {
-                std::swap(keys[i], keys.back());
-                keys.pop_back();
-                break;
-            }
-        }
-    }
-    std::vector<uint32_t> order(keys.size());
-    for (size_t k = 0; k < keys.size(); k++) order[k] = keys[k].index;
-    return order;
+    return dedupeOrder(keys);
 }
 
 // GraphAligner::clipTraceStart (GraphAligner.h:702-738): the trace starts where its X-score
@@ -1215,7 +1189,12 @@ void alignBatchMultiseed(const HostGraph& g, const ReadAlignParams& p, std::vect
         }
         try
         {
-            keep[k] = dedupeMultiseedTraces(rs[k], p.xscoreErrorCost);
+            if (rs[k].deduplicated)
+            {
+                keep[k].resize(rs[k].items.size());
+                for (uint32_t t = 0; t < keep[k].size(); t++) keep[k][t] = t;
+            }
+            else keep[k] = dedupeMultiseedTraces(rs[k], p.xscoreErrorCost);
             m.forward.resize(keep[k].size());
         }
         catch (const ReadFailure&)

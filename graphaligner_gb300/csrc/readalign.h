@@ -258,6 +258,7 @@ struct MultiseedResult
     std::vector<const uint64_t*> items;
     std::vector<uint32_t> lengths;
     std::vector<uint64_t> own;
+    bool deduplicated = false;   // removeDuplicateTraces already ran (its order)
 };
 
 typedef void (*MultiseedFn)(void* ctx, const std::vector<MultiseedRequest>& requests, std::vector<MultiseedResult>& results);

@@ -173,10 +173,12 @@ typedef struct ga_multiseed_results {
 int ga_multiseed_batch(ga_extender_t ext, const ga_extend_params* params,
                        const ga_multiseed_batch_desc* batch, ga_multiseed_results* results);
 
-/* The same DP with no room limit, closer to the reference's getMultiseedTraces (which returns
- * every trace): each read's traces land in buffers the extender owns, sized once they are
- * counted, so no read has to run twice.  Read i's traces are trace_first[i] ..
- * trace_first[i] + num_traces[i] - 1 of the trace arrays; trace_start indexes trace_items.
+/* The whole of GraphAlignerBitvectorBanded::getMultiseedTraces but the final reversal, with
+ * no room limit: each read's traces after removeDuplicateTraces (:144-169, in its order),
+ * each in DP order, land in buffers the extender owns, sized once they are counted, so no
+ * read has to run twice and duplicates are neither written nor copied.  Read i's traces are
+ * trace_first[i] .. trace_first[i] + num_traces[i] - 1 of the trace arrays; trace_start
+ * indexes trace_items.
  * batch->trace_offset, trace_capacity and max_traces are not used (may be NULL / 0).  The
  * arrays stay valid until the extender's next call or ga_extender_free.  GA_CAPACITY now
  * means only that the read's frontier tables outgrew the largest layout. */

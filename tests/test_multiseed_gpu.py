@@ -66,14 +66,42 @@ def test_gpu_multiseed_traces_match_oracle(cuda_lib, oracle_lib, harness, tmp_pa
                 break
     assert not bad, f"reads {bad[:10]} differ"
     assert int(cpu.num_traces.sum()) > batch.num
-    # with exact room: the same traces, in room sized to them
+    # with exact room: removeDuplicateTraces' survivors of the same traces, in room sized to them
     ex = Extender(DeviceGraph(g)).multiseed_exact(p, batch)
     assert np.array_equal(ex.status, cpu.status)
-    assert np.array_equal(ex.num_traces, cpu.num_traces)
     assert int(ex.trace_len.sum()) == len(ex.trace_items)
-    bad = [i for i in range(batch.num)
-           if any(gs != cs or not np.array_equal(gi, ci) for (gs, gi), (cs, ci) in zip(ex.traces(i), cpu.traces(i)))]
-    assert not bad, f"reads {bad[:10]} differ with exact room"
+    for i in range(batch.num):
+        assert_deduplicated(ex.traces(i), cpu.traces(i), p.xscore_error_cost)
+    assert int(ex.num_traces.sum()) <= int(cpu.num_traces.sum())
+
+
+def _start_cell(items):
+    return int(items[-1]) & ~(1 << 38)
+
+
+def _sort_score(score, items, cost):
+    first, last = (int(items[0]) >> 39) - 1, (int(items[-1]) >> 39) - 1
+    return ((first - last + 1) * 100 - score * cost + 2**31) % 2**32 - 2**31
+
+
+def assert_deduplicated(got, traces, cost):
+    """got is removeDuplicateTraces applied to traces: one trace per start cell, each one of the
+    given traces, and where a start cell's traces differ in their sort key the survivor has the
+    greatest (ties go by std::sort's arrangement, which the GAF goldens pin)."""
+    cells = {}
+    for score, items in traces:
+        cells.setdefault(_start_cell(items), []).append((_sort_score(score, items, cost), score, items))
+    seen = set()
+    for score, items in got:
+        cell = _start_cell(items)
+        assert cell not in seen
+        seen.add(cell)
+        group = cells[cell]
+        assert any(score == s and np.array_equal(items, it) for _, s, it in group)
+        best = max(k for k, _, _ in group)
+        if sum(1 for k, _, _ in group if k == best) == 1:
+            assert _sort_score(score, items, cost) == best
+    assert seen == set(cells)
 
 
 def test_gpu_multiseed_reports_capacity(cuda_lib, oracle_lib, harness, tmp_path):  # noqa: F811
