@@ -801,16 +801,22 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
             // duplicates (removeDuplicateTraces, as getMultiseedTraces does), and the survivors
             // get trace and item runs after the earlier passes' (this pass's tables are gone
             // once the next one starts).  Only the survivors are written and copied back.
+            // (only the reads this pass finished take their status and kept count from the
+            // device: the others keep what their own pass gave them)
             MsExactOut& o = x->msOut;
-            GA_CUDA(cudaMemcpyAsync(o.status.data(), x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
-            GA_CUDA(cudaMemcpyAsync(o.numTraces.data(), x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+            std::vector<int32_t> passStatus(n);
+            std::vector<uint32_t> passKeptCount(n);
+            GA_CUDA(cudaMemcpyAsync(passStatus.data(), x->status.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
+            GA_CUDA(cudaMemcpyAsync(passKeptCount.data(), x->msNumTraces.ptr, n * 4ULL, cudaMemcpyDeviceToHost, s));
             GA_CUDA(cudaStreamSynchronize(s));
             std::vector<uint32_t> passReads;
             uint64_t passKept = 0;
             for (uint32_t i = 0; i < n; i++)
             {
-                if (finished[i] || o.status[i] == GA_CAPACITY) continue;
+                if (finished[i] || passStatus[i] == GA_CAPACITY) continue;
                 finished[i] = 1;
+                o.status[i] = passStatus[i];
+                o.numTraces[i] = passKeptCount[i];
                 if (o.status[i] != GA_OK) continue;
                 traceBase[i] = passKept;
                 passKept += o.numTraces[i];
@@ -897,8 +903,11 @@ static int multiseed_run(ga_extender_t x, const ga_extend_params* p, const ga_mu
         GA_CUDA(cudaGetLastError());
         x->lastLaunches += 1;
         uint32_t capFails = 0;
+        unsigned long long used[2] = {0, 0};
         GA_CUDA(cudaMemcpyAsync(&capFails, x->counters + 2, 4, cudaMemcpyDeviceToHost, s));
+        GA_CUDA(cudaMemcpyAsync(used, x->arenaCursor, 16, cudaMemcpyDeviceToHost, s));
         GA_CUDA(cudaStreamSynchronize(s));
+        if (pass == 0) x->lastArenaBytes = used[1];
         float ms = 0;
         GA_CUDA(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
         x->lastFillMs += ms;

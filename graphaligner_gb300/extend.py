@@ -384,6 +384,12 @@ class Extender:
         check(lib().ga_extender_last_times(self.handle, ctypes.byref(f), ctypes.byref(t)))
         return f.value, t.value
 
+    def last_arena_bytes(self) -> int:
+        """DP-table bytes the first pass of the last call wrote to the arena."""
+        b = ctypes.c_uint64()
+        check(lib().ga_extender_last_arena_bytes(self.handle, ctypes.byref(b)))
+        return int(b.value)
+
     def last_layout_counts(self):
         """Extensions run with each frontier-table layout (0, 1, 2) by the last call."""
         c = (ctypes.c_uint32 * 3)()

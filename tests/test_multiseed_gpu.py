@@ -123,6 +123,38 @@ def test_gpu_multiseed_reports_capacity(cuda_lib, oracle_lib, harness, tmp_path)
         assert [(s, list(t)) for s, t in gpu.traces(int(i))] == [(s, list(t)) for s, t in cpu.traces(int(i))]
 
 
+def test_gpu_multiseed_exact_room_over_several_passes(cuda_lib, harness, tmp_path):  # noqa: F811
+    """With a DP-table arena far too small for the batch, reads that find it exhausted run
+    again in later passes, each pass giving its finished reads their room after the earlier
+    passes' traces; statuses, trace counts and every trace equal a run with room to spare, in
+    both the exact-room and the caller's-room forms."""
+    from graphaligner_gb300.extend import DeviceGraph, Extender, ExtendParams, MultiseedBatch
+    g = load_graph("vg50k")
+    _, seqs = read_fasta("vg50k_chimera_reads")
+    seeds = multiseed_seeds(harness[0], "vg50k", "vg50k_chimera_reads", False, tmp_path)
+    batch = MultiseedBatch.pack(seqs, seeds, max_traces=256, items_per_bp=64)
+    p = ExtendParams(bandwidth=10)
+    dg = DeviceGraph(g)
+    roomy = Extender(dg)
+    want = roomy.multiseed_exact(p, batch)
+    need = roomy.last_arena_bytes()
+    want_cap = roomy.multiseed(p, batch)
+    # two thirds of what the batch takes: the reads that are short of it when it runs out go
+    # again with a fresh arena
+    tight = Extender(dg, arena_bytes=max(need * 2 // 3, 1 << 20))
+    got = tight.multiseed_exact(p, batch)
+    passes = sum(tight.last_layout_counts())
+    got_cap = tight.multiseed(p, batch)
+    assert passes > batch.num, "the small arena should have sent reads to a second pass"
+    assert (want.status == 0).all()
+    assert np.array_equal(got.status, want.status) and np.array_equal(got.num_traces, want.num_traces)
+    for i in range(batch.num):
+        assert [(s, list(t)) for s, t in got.traces(i)] == [(s, list(t)) for s, t in want.traces(i)]
+    assert np.array_equal(got_cap.status, want_cap.status) and np.array_equal(got_cap.num_traces, want_cap.num_traces)
+    for i in range(batch.num):
+        assert [(s, list(t)) for s, t in got_cap.traces(i)] == [(s, list(t)) for s, t in want_cap.traces(i)]
+
+
 def test_gpu_multiseed_rejects_bad_seeds(cuda_lib):
     """Seeds outside the graph, beyond their read or out of slice order are GA_ERR_ARGUMENT."""
     from graphaligner_gb300._lib import GAError
