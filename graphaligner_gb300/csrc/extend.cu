@@ -2229,9 +2229,10 @@ __device__ int ms_start_cell(const MultiTraceArgs& a, Table& t, const WSpace& w,
 }
 
 // One candidate's trace (getReverseTraceFromTable to a seed start).  write = false: finds the
-// first cell and walks the trace only counting its items, recording its length, score and
-// read span.  write = true (a kept trace of a read whose traces all fit): walks it again
-// into the read's output at the place the read's pass gave it.
+// first cell and walks the trace only counting its items, recording its length, score, read
+// span and last cell.  write = true (a kept trace of a read whose traces all fit and, with
+// exact room, that removeDuplicateTraces kept): walks it again into the read's output at
+// the place the read's selection (or the host, with exact room) gave it.
 __device__ void ms_trace_cand(const MultiTraceArgs& a, MsCand* cp, const WSpace& w, bool write, u32 lane)
 {
     const MsCand c = *cp;

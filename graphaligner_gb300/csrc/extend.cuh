@@ -211,6 +211,7 @@ struct MultiTraceArgs
     u64* traceItems;
     u64* cellSteps;
     u64* itemsNeeded;      // [num] or null: when the traces outgrow the read's room, the room they need
+                           // (with exact room: the items of the kept traces)
     u32* tracesNeeded;
     // exact room (traceBase non-null): read i's kept traces are traceBase[i] + slot in the
     // kept list, whose summaries go to keys; after removeDuplicateTraces kept trace k is
