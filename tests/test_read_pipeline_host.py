@@ -23,7 +23,7 @@ SOURCES = [os.path.join(ROOT, "tests", "harness", "pipeline.cpp"),
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
     os.makedirs(BUILD, exist_ok=True)
-    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "index_walk.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "gaf_format.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "seed_table.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
+    deps = SOURCES + [os.path.join(ROOT, "graphaligner_gb300", "csrc", "readalign.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "index_walk.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "gaf_format.cuh"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "seed_table.h"), os.path.join(ROOT, "graphaligner_gb300", "csrc", "trace_dedupe.h"), os.path.join(ROOT, "include", "graphaligner_gb300.h")]
     if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < max(os.path.getmtime(d) for d in deps):
         subprocess.run(["g++", "-std=c++17", "-O2", "-o", HARNESS, *SOURCES, "-lpthread"], check=True)
     d = tmp_path_factory.mktemp("pipeline")

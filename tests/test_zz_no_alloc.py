@@ -108,3 +108,28 @@ def test_noalloc_rejects_oversized_batch(cuda_lib):
     assert rc != 0
     assert b"4096" in lib().ga_last_error()
     del null
+
+
+def test_noalloc_rejects_more_than_its_read_bp(cuda_lib):
+    """A batch within the extension count but over the 8,000,000 read bp the fixed scratch
+    holds is GA_ERR_ARGUMENT with the limit in the message, before any kernel runs (the
+    lengths are read back first; the other arrays are never touched)."""
+    torch = pytest.importorskip("torch")
+    from graphaligner_gb300 import _abi
+    from graphaligner_gb300._lib import lib
+    n = 2000
+    lens = torch.full((n,), 4001, dtype=torch.int32, device="cuda")     # 8,002,000 bp
+    dummy = torch.zeros(64, dtype=torch.int64, device="cuda")
+
+    def p(ctype, t=dummy):
+        return ctypes.cast(ctypes.c_void_p(t.data_ptr()), ctypes.POINTER(ctype))
+
+    u8, u32, u64, i32 = ctypes.c_uint8, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
+    gdesc = _abi.GraphDesc(4, 4, p(u32), p(u64), p(u64), p(u32), p(u32), p(u32), p(u32), p(u8), p(u32))
+    bdesc = _abi.BatchDesc(n, p(u8), p(u64), p(u32, lens), p(u32), p(u32), p(u64), p(u32))
+    rdesc = _abi.Results(p(i32), p(i32), p(u32), p(u64), p(u64))
+    params = _abi.ExtendParams(10, 14705, 2**64 - 1, 294)
+    rc = lib().ga_extend_batch_noalloc(ctypes.byref(gdesc), ctypes.byref(params), ctypes.byref(bdesc), ctypes.byref(rdesc), None)
+    torch.cuda.synchronize()
+    assert rc == -1
+    assert b"8,000,000" in lib().ga_last_error()
