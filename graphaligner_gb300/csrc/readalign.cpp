@@ -135,6 +135,13 @@ HostGraph::HostGraph(const ga_host_graph_desc& d) :
     }
     bpSize = 0;
     for (uint32_t i = 0; i < N; i++) bpSize += len[i];
+    // each split node's bigraph node size, so reversing a trace item needs no hash lookup
+    bigSize.resize(N);
+    for (uint32_t i = 0; i < N; i++)
+    {
+        auto f = lookupIndex.find(nodeIds[i]);
+        bigSize[i] = f == lookupIndex.end() ? 0 : originalSize[f->second];
+    }
 }
 
 size_t HostGraph::lookup(int bignode) const
@@ -284,10 +291,11 @@ void fixForwardTraceSeqPos(const HostGraph& g, OnewayTrace& trace, size_t start,
 }
 
 // GraphAligner::fixReverseTraceSeqPosAndOrder (GraphAligner.h:562-601)
-void fixReverseTraceSeqPosAndOrder(const HostGraph& g, OnewayTrace& trace, size_t end, const std::string& sequence)
+// inReadOrder: the caller already put the trace in the order this function's reversal gives
+void fixReverseTraceSeqPosAndOrder(const HostGraph& g, OnewayTrace& trace, size_t end, const std::string& sequence, bool inReadOrder)
 {
     if (trace.trace.size() == 0) return;
-    std::reverse(trace.trace.begin(), trace.trace.end());
+    if (!inReadOrder) std::reverse(trace.trace.begin(), trace.trace.end());
     trace.score = 0;
     for (size_t i = 0; i + 1 < trace.trace.size(); i++) trace.trace[i].nodeSwitch = trace.trace[i + 1].nodeSwitch;
     trace.trace.back().nodeSwitch = false;
@@ -296,10 +304,13 @@ void fixReverseTraceSeqPosAndOrder(const HostGraph& g, OnewayTrace& trace, size_
         auto& t = trace.trace[i];
         GAH_ASSERT(t.seqPos <= end || t.seqPos == (size_t)-1);
         t.seqPos = end - t.seqPos;
-        size_t offset = g.nodeOffset[t.node] + t.nodeOffset;
-        auto rp = g.reversePosition(g.nodeIds[t.node], offset);
-        t.node = rp.first;
-        t.nodeOffset = rp.second;
+        // reversePosition of the item's bigraph node and offset, its size from the split node
+        const size_t offset = g.nodeOffset[t.node] + t.nodeOffset;
+        const int bignode = g.nodeIds[t.node];
+        const size_t size = g.bigSize[t.node];
+        GAH_ASSERT(offset < size);
+        t.node = (bignode % 2 == 0) ? (bignode / 2) * 2 + 1 : (bignode / 2) * 2;
+        t.nodeOffset = size - offset - 1;
         GAH_ASSERT(t.seqPos < sequence.size());
         t.seqChar = sequence[t.seqPos];
         t.graphChar = complement(t.graphChar);
@@ -626,7 +637,10 @@ static bool nextSeed(const ReadAlignParams& p, ReadState& r, size_t& seedIndex)
     return more;
 }
 
-static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, const char* seq, size_t seqLen)
+// The packed items of an extension as trace items, in DP order or (reversed) read order;
+// `extra` more items of room are kept for a trace that will be appended.
+static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, const char* seq, size_t seqLen, bool reversed = false,
+    size_t extra = 0)
 {
     OnewayTrace t;
     if (e.status == GA_TRACE_FAILED)
@@ -638,11 +652,12 @@ static OnewayTrace decodeTrace(const HostGraph& g, const ExtensionResult& e, con
     t.score = e.score;
     const uint64_t* items = e.begin();
     const uint64_t n = e.size();
+    t.trace.reserve(n + extra);
     t.trace.resize(n);
     for (uint64_t i = 0; i < n; i++)
     {
         const uint64_t x = items[i];
-        TraceItem& it = t.trace[i];
+        TraceItem& it = t.trace[reversed ? n - 1 - i : i];
         it.node = GA_TRACE_NODE(x);
         it.nodeOffset = GA_TRACE_OFFSET(x);
         uint64_t sp1 = GA_TRACE_SEQPOS1(x);
@@ -679,25 +694,26 @@ void parallelFor(size_t n, const std::function<void(size_t)>& fn)
     for (auto& t : pool) t.join();
 }
 
-// GraphAligner::getAlignmentFromSeed (GraphAligner.h:631-692) after the two extensions ran
+// GraphAligner::getAlignmentFromSeed (GraphAligner.h:631-692) after the two extensions ran.
+// The backward trace comes in DP order and the forward one already reversed (decodeTrace),
+// so neither is reversed here: getTwoDirectionalTrace (GraphAligner.h:508-518) reverses the
+// backward trace and fixReverseTraceSeqPosAndOrder reverses it back, and the forward trace
+// is reversed once.
 static void finishSeed(const HostGraph& g, const ReadAlignParams& p, ReadState& r, const SeedHit& seedHit,
     OnewayTrace backward, OnewayTrace forward, int backwardNodeId, int forwardNodeId)
 {
-    // getTwoDirectionalTrace (GraphAligner.h:508-518): both traces to read order
     if (!backward.failed())
     {
         auto rp = g.reversePosition(forwardNodeId, seedHit.nodeOffset);
         const auto& b = backward.trace.back();
         GAH_ASSERT(b.seqPos == (size_t)-1 && g.nodeIds[b.node] == backwardNodeId && g.nodeOffset[b.node] + b.nodeOffset == rp.second);
-        std::reverse(backward.trace.begin(), backward.trace.end());
     }
     if (!forward.failed())
     {
-        const auto& b = forward.trace.back();
+        const auto& b = forward.trace.front();
         GAH_ASSERT(b.seqPos == (size_t)-1 && g.nodeIds[b.node] == forwardNodeId && g.nodeOffset[b.node] + b.nodeOffset == seedHit.nodeOffset);
-        std::reverse(forward.trace.begin(), forward.trace.end());
     }
-    fixReverseTraceSeqPosAndOrder(g, backward, seedHit.seqPos - 1, r.seq);
+    fixReverseTraceSeqPosAndOrder(g, backward, seedHit.seqPos - 1, r.seq, true);
     fixForwardTraceSeqPos(g, forward, seedHit.seqPos + 1, r.seq);
     if (forward.failed() && backward.failed()) return;
     GAH_ASSERT(backward.trace.size() > 0 || backward.failed());
@@ -1298,7 +1314,7 @@ void alignBatchMultiseed(const HostGraph& g, const ReadAlignParams& p, std::vect
                     if (!bw.failed())
                     {
                         std::reverse(bw.trace.begin(), bw.trace.end());
-                        fixReverseTraceSeqPosAndOrder(g, bw, fw.trace[0].seqPos - 1, m.r.seq);
+                        fixReverseTraceSeqPosAndOrder(g, bw, fw.trace[0].seqPos - 1, m.r.seq, false);
                     }
                 }
                 OnewayTrace merged = mergeTraces(std::move(bw), std::move(fw));
@@ -1667,8 +1683,10 @@ void SeedLoopPool::consume(const std::vector<ExtensionResult>& results, BatchSta
             OnewayTrace bw, fw;
             bw.score = INT32_MAX;
             fw.score = INT32_MAX;
-            if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], requests[pe.backward].seq, requests[pe.backward].len);
-            if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], requests[pe.forward].seq, requests[pe.forward].len);
+            // the backward trace keeps room for the forward one, which finishSeed appends
+            const size_t forwardItems = pe.forward >= 0 ? results[pe.forward].size() : 0;
+            if (pe.backward >= 0) bw = decodeTrace(g, results[pe.backward], requests[pe.backward].seq, requests[pe.backward].len, false, forwardItems);
+            if (pe.forward >= 0) fw = decodeTrace(g, results[pe.forward], requests[pe.forward].seq, requests[pe.forward].len, true);
             finishSeed(g, p, r, s, std::move(bw), std::move(fw), backwardNodeId, forwardNodeId);
             return true;
         }

@@ -27,6 +27,7 @@ struct HostGraph
     std::vector<uint32_t> originalSize, lookupOff, lookupNodes;
     std::vector<std::string> names;
     std::unordered_map<int, size_t> lookupIndex;
+    std::vector<uint32_t> bigSize;      // per split node: originalSize of its bigraph node
     size_t bpSize;
     size_t lookup(int bignode) const;
     char charAt(size_t node, size_t pos) const;
